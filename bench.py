@@ -1,0 +1,355 @@
+"""Benchmark: element residual+Jacobian assembly throughput on GB300.
+
+One step = one full residual + Jacobian assembly (Problem::get_jacobian) of
+the workload: dof -> nodal-value scatter, the fused element kernel
+(geometry + weak form + element matrices), and the deterministic scatter
+into the CSR values and the residual.  Inputs are resident in HBM
+(``value``); ``e2e`` repeats the step through the public API with the dof
+vector copied in from pinned host memory and R + CSR values copied back.
+
+Default workload: 2D steady incompressible Navier-Stokes, Taylor-Hood P2/P1
+on a 256x256 split structured mesh (131,072 triangles), Re = 100, lid
+u_x = 16x^2(1-x)^2, dofs perturbed by N(0, 1e-3); FP64 residual with FP64
+Jacobian (headline) and FP32 Jacobian (variant).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload ns|poisson|hex] [--size S]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (description, default size)
+    "ns": ("navier_stokes_th_p2p1_split_left_Re100", 256),
+    "poisson": ("poisson_q2_quad_8gaussians", 64),
+    "hex": ("nonlinear_diffusion_q2_hex_16gaussians", 48),
+}
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_problem(workload: str, size: int, precision: str):
+    from pyoomph_gb300 import workloads as W
+    if workload == "ns":
+        P = W.navier_stokes_problem(N=size, jacobian_precision=precision)
+        P.initialise()
+        W.perturb_dofs(P, seed=0, sigma=1e-3)
+    elif workload == "poisson":
+        P = W.poisson_problem(N=size, seed=0, jacobian_precision=precision)
+        P.initialise()
+    else:
+        P = W.nonlinear_diffusion_problem(N=size, seed=0, jacobian_precision=precision)
+        P.initialise()
+        x = np.random.default_rng(0).normal(0.0, 0.1, P.n_dof)
+        P.set_dofs(x)
+    return P
+
+
+def element_algorithmic_bytes(P) -> int:
+    """Compulsory HBM bytes of one element-kernel launch: connectivity,
+    nodal positions and values read once, element residuals and matrices
+    written once (tables are negligible)."""
+    m = P.mesh
+    nl = P.kernel.layout.n
+    jb = 8 if P._prec == "f64" else 4
+    return int(m.n_elem * m.etype.nnode * 4 + m.n_nodes * m.dim * 8 + m.n_nodes * len(P.fields) * 8
+               + m.n_elem * nl * 8 + m.n_elem * nl * nl * jb)
+
+
+def time_steps(torch, fn, steps: int, warmup: int):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(steps):
+        fn()
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def run_gb300(args):
+    import torch
+    from pyoomph_gb300 import problem as _p  # noqa: F401
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    hbm_peak, peak_kind = _peaks()
+    results = {}
+    for prec in ("fp64", "fp32"):
+        P = make_problem(args.workload, args.size, prec)
+        P.check()
+        asm = lambda: P.assemble_device(with_jacobian=True)
+        # device-resident throughput
+        for _ in range(args.warmup):
+            asm()
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        with ClockSampler(local) as cs:
+            ms = time_steps(torch, asm, args.steps, 0)
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        P.check()
+        # stage breakdown (element kernel = dominant kernel)
+        P.set_stage_timing(True)
+        for _ in range(max(3, min(args.steps, 10))):
+            asm()
+        stage_ms, calls = P.stage_times()
+        P.set_stage_timing(False)
+        stage_ms = stage_ms / max(calls, 1)
+        # end to end through the public API with host buffers
+        xh = torch.from_numpy(P.get_dofs()).pin_memory()
+        Rh = torch.empty(P.n_dof, dtype=torch.float64).pin_memory()
+        Jh = torch.empty(P.nnz, dtype=P.J_dev.dtype).pin_memory()
+
+        def e2e():
+            P.x_dev.copy_(xh, non_blocking=True)
+            P.assemble_device(with_jacobian=True)
+            Rh.copy_(P.R_dev[:P.n_dof], non_blocking=True)
+            Jh.copy_(P.J_dev[:P.nnz], non_blocking=True)
+
+        ms_e2e = time_steps(torch, e2e, max(3, args.steps), args.warmup)
+        torch.cuda.synchronize()
+        results[prec] = dict(P=P, ms=ms, stage_ms=stage_ms, ms_e2e=ms_e2e, clocks=cs.summary(),
+                             h2d=int(P.n_dof * 8), d2h=int(P.n_dof * 8 + P.nnz * P.J_dev.element_size()))
+    main = results["fp64"]
+    P = main["P"]
+    n_elem = P.mesh.n_elem
+    value = n_elem * world / (main["ms"] / 1e3)
+    elem_ms = float(main["stage_ms"][1])
+    abytes = element_algorithmic_bytes(P)
+    achieved = abytes / (elem_ms / 1e3) / 1e9
+    launches = P.launch_count(True)
+    line = {
+        "metric": "element residual+Jacobian assemblies/s (full CSR assembly)",
+        "value": value,
+        "unit": "elements/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": main["ms"],
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload][0], "mesh_side": args.size, "n_elem": n_elem,
+                   "n_dof": P.n_dof, "nnz": P.nnz, "jacobian": "fp64", "residual": "fp64",
+                   "l2": "working set per step > L2 (element matrices + CSR + contribution lists)",
+                   "parallelism": "replicas" if world > 1 else "single-gpu"},
+        "assemblies_per_s": 1e3 / main["ms"],
+        "stage_ms": {"dof_scatter": float(main["stage_ms"][0]), "element_kernel": elem_ms,
+                     "residual_gather": float(main["stage_ms"][2]), "jacobian_gather": float(main["stage_ms"][3])},
+        "roofline": {"bound": "hbm", "kernel": P.kernel.name, "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": abytes, "traffic": None},
+        "e2e": {"value": n_elem * world / (main["ms_e2e"] / 1e3), "unit": "elements/s",
+                "h2d_bytes_per_step": main["h2d"], "d2h_bytes_per_step": main["d2h"],
+                "ms_per_step": main["ms_e2e"]},
+        "gpu_launches": launches * args.steps,
+        "clocks": main["clocks"],
+    }
+    r32 = results["fp32"]
+    line["fp32_jacobian"] = {"value": n_elem * world / (r32["ms"] / 1e3), "unit": "elements/s",
+                             "ms_per_step": r32["ms"], "element_kernel_ms": float(r32["stage_ms"][1]),
+                             "e2e": {"value": n_elem * world / (r32["ms_e2e"] / 1e3),
+                                     "h2d_bytes_per_step": r32["h2d"], "d2h_bytes_per_step": r32["d2h"]}}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args, threads=1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def _oracle_problem(workload: str, side: int):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from pyoomph_gb300.workloads import draw_gaussians
+    if workload == "ns":
+        m = O.mesh(O.P2_TRI, side, side)
+        OP = O.navier_stokes_problem(m, rho=1.0, mu=0.01)
+        OP.set_dofs(OP.dofs() + np.random.default_rng(0).normal(0.0, 1e-3, OP.n_dof))
+    elif workload == "poisson":
+        OP = O.poisson_problem(O.mesh(O.Q2_QUAD, side, side), draw_gaussians(0, 8, 2))
+    else:
+        OP = O.poisson_problem(O.mesh(O.Q2_HEX, side, side, side), draw_gaussians(0, 16, 3),
+                               eq=O.EQ_NONLINEAR_DIFFUSION)
+    return OP
+
+
+def _sample_side(workload: str, size: int) -> int:
+    # bounded CPU sample: about 10^4 elements per assembly
+    return {"ns": min(size, 64), "poisson": min(size, 64), "hex": min(size, 12)}[workload]
+
+
+def _cpu_worker(args_tuple):
+    workload, side, seconds = args_tuple
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    OP = _oracle_problem(workload, side)
+    n_elem = OP.mesh.conn.shape[0]
+    O.assemble(OP, True, 0.0)  # warm-up
+    t0 = time.perf_counter()
+    done = 0
+    while True:
+        O.assemble(OP, True, 0.0)
+        done += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    return n_elem * done, time.perf_counter() - t0, done
+
+
+def cpu_baseline(args, threads: int = 1, seconds: float = 10.0):
+    """The oracle's restated reference assembly (vectors-of-pairs, restated
+    element code) timed on the host cores on a bounded sample."""
+    side = _sample_side(args.workload, args.size)
+    if threads == 1:
+        elems, dt, n = _cpu_worker((args.workload, side, seconds))
+        value = elems / dt
+    else:
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(threads) as pool:
+            res = pool.map(_cpu_worker, [(args.workload, side, seconds)] * threads)
+        value = sum(r[0] / r[1] for r in res)
+        n = sum(r[2] for r in res)
+    return {"value": value, "unit": "elements/s", "cores": threads, "kind": "port",
+            "sample": f"{WORKLOADS[args.workload][0]} side {side}, {n} full assemblies in ~{seconds:.0f}s "
+                      f"per core (oracle/fe_oracle.c, vectors-of-pairs)"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    seconds = max(2.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
+    vals = []
+    cb = None
+    for _ in range(args.warmup):
+        cpu_baseline(args, threads=threads, seconds=seconds / 4)
+    for _ in range(args.steps):
+        cb = cpu_baseline(args, threads=threads, seconds=seconds)
+        vals.append(cb["value"])
+    value = float(np.median(vals))
+    cb["value"] = value
+    line = {"impl": "reference", "metric": "element residual+Jacobian assemblies/s (full CSR assembly)",
+            "value": value, "unit": "elements/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOADS[args.workload][0], "mesh_side": args.size, "jacobian": "fp64",
+                       "residual": "fp64"},
+            "cpu_baseline": cb, "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="ns", choices=list(WORKLOADS))
+    ap.add_argument("--size", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.size is None:
+        args.size = WORKLOADS[args.workload][1]
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,184 @@
+/*
+ * fe_gb300.h -- C-ABI of the GB300 finite-element assembly engine
+ * (libfe_gb300.so).  Plain pointers and sizes; no C++ or torch types.
+ *
+ * It replaces, for the residual/Jacobian hot path of pyoomph:
+ *   - the element function table a JIT element library fills
+ *     (JIT_ELEMENT_init / JITFuncSpec_Table_FiniteElement_t,
+ *     src/jitbridge.h:329-499) and the per-element call
+ *     ResidualAndJacobian[i](eleminfo, shapeinfo, R, J, M, flag)
+ *     (src/jitbridge.h:285, called from src/elements.cpp:5104-5113):
+ *     fe_code_compile + fe_problem_create take the generated element code
+ *     and run it for every element of a domain in one launch;
+ *   - the shape buffer callback fill_shape_buffer_for_point
+ *     (src/elements.cpp:60, :3593-4270): computed on the device inside the
+ *     element kernel from reference tables staged in shared memory;
+ *   - the global assembly Problem::get_jacobian / get_residuals with the
+ *     vectors-of-pairs sparse assembler (oomph problem.cc:3810-3930,
+ *     4038-4165, 5332-5666) and pyoomph's Problem::get_jacobian /
+ *     get_residuals (src/problem.cpp:902-965): fe_assemble;
+ *   - the residual max-norm of the Newton loop (DoubleVector::max,
+ *     double_vector.cc:611-629): fe_residual_max.
+ *
+ * Every function returns FE_OK (0) or an FE_ERR_* code; fe_last_error()
+ * gives the message of the last failure on the calling thread.  No
+ * exception crosses the boundary.  A problem handle is not thread-safe;
+ * distinct handles may be used from distinct threads.
+ */
+#ifndef FE_GB300_H
+#define FE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  FE_OK = 0,
+  FE_ERR_ARG = 1,     /* invalid argument */
+  FE_ERR_CUDA = 2,    /* CUDA runtime/driver failure */
+  FE_ERR_COMPILE = 3, /* nvrtc failed to compile element code */
+  FE_ERR_NOMEM = 4,   /* device or host allocation refused */
+  FE_ERR_STATE = 5,   /* call out of order */
+  FE_ERR_DEVICE = 6,  /* a kernel reported an error in its status word */
+  FE_ERR_NOGPU = 7    /* no usable CUDA device */
+};
+
+/* flags of fe_assemble */
+enum {
+  FE_ASSEMBLE_RESIDUAL = 1, /* fill R (Problem::get_residuals) */
+  FE_ASSEMBLE_JACOBIAN = 2, /* fill the CSR values of J (Problem::get_jacobian) */
+  FE_ASSEMBLE_VALUES_FROM_DOFS = 4 /* first scatter the dof vector into the nodal values */
+};
+
+/* Jacobian value precision */
+enum { FE_JAC_F64 = 0, FE_JAC_F32 = 1 };
+
+typedef struct fe_code fe_code_t;       /* compiled element code (one domain) */
+typedef struct fe_problem fe_problem_t; /* resident mesh + CSR + buffers */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *fe_last_error(void);
+
+/* Library version string. */
+const char *fe_version(void);
+
+/* Device 0 properties; FE_ERR_NOGPU without a device. */
+int fe_device_info(int *sm_count, int *cc_major, int *cc_minor, size_t *free_bytes,
+                   size_t *total_bytes);
+
+/*
+ * Compile generated element code for sm_103a with nvrtc and load it.
+ * Replaces CCompiler::compile + dlopen/dlsym("JIT_ELEMENT_init")
+ * (pyoomph/generic/ccompiler.py:207-242, src/ccompiler.cpp:191-213).
+ *   source       CUDA C source of one domain (from the code generator)
+ *   kernel_name  extern "C" __global__ entry in that source
+ *   include_dir  directory holding fe_device.cuh
+ *   cache_dir    directory for cubin caching by source hash (may be NULL)
+ *   log/log_cap  compiler log on failure (may be NULL)
+ */
+int fe_code_compile(const char *source, const char *kernel_name, const char *include_dir,
+                    const char *cache_dir, fe_code_t **out, char *log, size_t log_cap);
+void fe_code_destroy(fe_code_t *code);
+
+/* Compile only (nvrtc -> cubin into cache_dir); needs no GPU.  cubin_bytes
+ * receives the image size.  fe_code_compile reuses the cached image. */
+int fe_code_build(const char *source, const char *kernel_name, const char *include_dir,
+                  const char *cache_dir, size_t *cubin_bytes, char *log, size_t log_cap);
+
+/* One domain: one element type, one compiled code. */
+typedef struct fe_domain_desc {
+  fe_code_t *code;
+  int nnode_el;             /* nodes per element */
+  int nlocal;               /* local values per element, node-major */
+  int64_t n_elem;
+  const int32_t *conn;      /* host [n_elem * nnode_el], global node numbers */
+  const int32_t *local_node;/* host [nlocal]: element node slot of local value k */
+  const int32_t *local_val; /* host [nlocal]: nodal value index of local value k */
+  const double *tables;     /* host reference tables (layout fixed by the code) */
+  int64_t n_tables;
+  int elems_per_block;      /* launch shape chosen by the code generator / tuner */
+  int threads_per_block;
+  int smem_bytes;           /* dynamic shared memory per block */
+} fe_domain_desc_t;
+
+typedef struct fe_problem_desc {
+  int dim;                  /* nodal dimension */
+  int64_t n_nodes;
+  int nval;                 /* values per node (max) */
+  const double *x;          /* host [n_nodes * dim] nodal positions */
+  const int32_t *eqn;       /* host [n_nodes * nval] equation numbers, -1 pinned/absent */
+  int64_t n_dof;
+  int n_domains;
+  const fe_domain_desc_t *domains;
+  int n_params;
+  const double *params;     /* global parameters read by the element code */
+  int jac_precision;        /* FE_JAC_F64 or FE_JAC_F32 */
+} fe_problem_desc_t;
+
+/*
+ * Upload the mesh, build the CSR pattern of the global Jacobian in the
+ * reference's order (rows = equations; columns of a row in order of first
+ * insertion over (element, local i, local j), every structural coupling
+ * kept) and the per-slot contribution lists of the deterministic scatter.
+ */
+int fe_problem_create(const fe_problem_desc_t *desc, fe_problem_t **out);
+void fe_problem_destroy(fe_problem_t *p);
+
+int fe_problem_sizes(const fe_problem_t *p, int64_t *n_dof, int64_t *nnz);
+/* Host copies of the CSR pattern. */
+int fe_problem_pattern(const fe_problem_t *p, int32_t *rowptr, int32_t *colidx);
+/* Device pointers of the resident CSR pattern. */
+int fe_problem_pattern_device(const fe_problem_t *p, const int32_t **rowptr,
+                              const int32_t **colidx);
+
+/* Set all nodal values (incl. pinned boundary values) from a host array. */
+int fe_problem_set_values(fe_problem_t *p, const double *values_host);
+/* Read the nodal values back to the host. */
+int fe_problem_get_values(const fe_problem_t *p, double *values_host);
+/* Update the global parameters (host array, n_params values). */
+int fe_problem_set_params(fe_problem_t *p, const double *params_host);
+
+/*
+ * Assemble on the device.  dofs, R, J_vals are DEVICE pointers (R: n_dof
+ * doubles; J_vals: nnz doubles or floats per jac_precision).  With
+ * FE_ASSEMBLE_VALUES_FROM_DOFS the dof vector is first scattered into the
+ * nodal values.  stream is a cudaStream_t (NULL = legacy default stream).
+ * Asynchronous: errors reported by kernels surface at the next
+ * fe_problem_check or synchronising call.
+ */
+int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags,
+                void *stream);
+
+/* The same with HOST buffers: copies in, assembles, copies out, synchronises. */
+int fe_assemble_host(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags);
+
+/* max |R| over n entries of a device vector, NaN -> +inf; result to host. */
+int fe_residual_max(fe_problem_t *p, const double *R, int64_t n, double *out, void *stream);
+
+/* x[i] -= dx[i] for device vectors (the Newton update). */
+int fe_dof_update(fe_problem_t *p, double *x, const double *dx, int64_t n, void *stream);
+
+/* Synchronise the problem's work and report any kernel status error. */
+int fe_problem_check(fe_problem_t *p);
+
+/*
+ * Stage tracing.  With timing enabled, fe_assemble records CUDA events on
+ * its stream around its four stages; fe_problem_stage_times synchronises,
+ * returns the summed milliseconds per stage since the last query
+ * (ms[0] dof scatter, ms[1] element kernels, ms[2] residual gather,
+ * ms[3] Jacobian gather) and the number of calls, and resets the sums.
+ * The counterpart of oomph's Jacobian_setup_time (linear_solver.cc:884-894).
+ */
+int fe_problem_set_timing(fe_problem_t *p, int enable);
+int fe_problem_stage_times(fe_problem_t *p, double *ms, int64_t *calls);
+
+/* Number of element and scatter kernels one fe_assemble launches. */
+int fe_problem_launch_count(const fe_problem_t *p, int flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

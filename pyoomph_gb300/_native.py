@@ -1,0 +1,159 @@
+"""ctypes binding of libfe_gb300.so (the C-ABI in include/fe_gb300.h).
+
+The library is built in-tree by ``pyoomph_gb300.build``.  There is no
+fallback: if the library is missing or a call fails, an exception says so.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+FE_OK, FE_ERR_ARG, FE_ERR_CUDA, FE_ERR_COMPILE, FE_ERR_NOMEM, FE_ERR_STATE, FE_ERR_DEVICE, FE_ERR_NOGPU = range(8)
+FE_ASSEMBLE_RESIDUAL, FE_ASSEMBLE_JACOBIAN, FE_ASSEMBLE_VALUES_FROM_DOFS = 1, 2, 4
+FE_JAC_F64, FE_JAC_F32 = 0, 1
+
+INCLUDE_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc")
+CACHE_DIR = os.environ.get("PYOOMPH_GB300_CACHE",
+                           os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "_build",
+                                        "jit_cache"))
+
+# every symbol include/fe_gb300.h declares
+EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "fe_code_destroy", "fe_code_build",
+           "fe_problem_create", "fe_problem_destroy", "fe_problem_sizes", "fe_problem_pattern",
+           "fe_problem_pattern_device", "fe_problem_set_values", "fe_problem_get_values",
+           "fe_problem_set_params", "fe_assemble", "fe_assemble_host", "fe_residual_max", "fe_dof_update",
+           "fe_problem_check", "fe_problem_launch_count", "fe_problem_set_timing", "fe_problem_stage_times"]
+
+
+class FeError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[fe_gb300 error {code}] {msg}")
+        self.code = code
+
+
+class DomainDesc(ctypes.Structure):
+    _fields_ = [
+        ("code", ctypes.c_void_p),
+        ("nnode_el", ctypes.c_int),
+        ("nlocal", ctypes.c_int),
+        ("n_elem", ctypes.c_int64),
+        ("conn", ctypes.c_void_p),
+        ("local_node", ctypes.c_void_p),
+        ("local_val", ctypes.c_void_p),
+        ("tables", ctypes.c_void_p),
+        ("n_tables", ctypes.c_int64),
+        ("elems_per_block", ctypes.c_int),
+        ("threads_per_block", ctypes.c_int),
+        ("smem_bytes", ctypes.c_int),
+    ]
+
+
+class ProblemDesc(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int),
+        ("n_nodes", ctypes.c_int64),
+        ("nval", ctypes.c_int),
+        ("x", ctypes.c_void_p),
+        ("eqn", ctypes.c_void_p),
+        ("n_dof", ctypes.c_int64),
+        ("n_domains", ctypes.c_int),
+        ("domains", ctypes.POINTER(DomainDesc)),
+        ("n_params", ctypes.c_int),
+        ("params", ctypes.c_void_p),
+        ("jac_precision", ctypes.c_int),
+    ]
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed) the native library."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(_build.LIB):
+            if not build_if_missing:
+                raise FeError(FE_ERR_STATE, f"native library missing: {_build.LIB}")
+            _build.build()
+        L = ctypes.CDLL(_build.LIB)
+        vp, i64, c_int, sz = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_size_t
+        L.fe_last_error.restype = ctypes.c_char_p
+        L.fe_version.restype = ctypes.c_char_p
+        L.fe_device_info.argtypes = [vp] * 5
+        L.fe_code_compile.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, vp,
+                                      ctypes.c_char_p, sz]
+        L.fe_code_build.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, vp,
+                                    ctypes.c_char_p, sz]
+        L.fe_code_destroy.argtypes = [vp]
+        L.fe_code_destroy.restype = None
+        L.fe_problem_create.argtypes = [ctypes.POINTER(ProblemDesc), vp]
+        L.fe_problem_destroy.argtypes = [vp]
+        L.fe_problem_destroy.restype = None
+        L.fe_problem_sizes.argtypes = [vp, vp, vp]
+        L.fe_problem_pattern.argtypes = [vp, vp, vp]
+        L.fe_problem_pattern_device.argtypes = [vp, vp, vp]
+        L.fe_problem_set_values.argtypes = [vp, vp]
+        L.fe_problem_get_values.argtypes = [vp, vp]
+        L.fe_problem_set_params.argtypes = [vp, vp]
+        L.fe_assemble.argtypes = [vp, vp, vp, vp, c_int, vp]
+        L.fe_assemble_host.argtypes = [vp, vp, vp, vp, c_int]
+        L.fe_residual_max.argtypes = [vp, vp, i64, vp, vp]
+        L.fe_dof_update.argtypes = [vp, vp, vp, i64, vp]
+        L.fe_problem_check.argtypes = [vp]
+        L.fe_problem_launch_count.argtypes = [vp, c_int]
+        L.fe_problem_set_timing.argtypes = [vp, c_int]
+        L.fe_problem_stage_times.argtypes = [vp, vp, vp]
+        _lib = L
+        return L
+
+
+def check(rc: int) -> None:
+    if rc != FE_OK:
+        raise FeError(rc, load().fe_last_error().decode(errors="replace"))
+
+
+def code_build(source: str, name: str, cache_dir: str = CACHE_DIR) -> int:
+    """nvrtc-compile only (no GPU needed); returns the cubin size."""
+    L = load()
+    os.makedirs(cache_dir, exist_ok=True)
+    n = ctypes.c_size_t()
+    log = ctypes.create_string_buffer(1 << 16)
+    rc = L.fe_code_build(source.encode(), name.encode(), INCLUDE_DIR.encode(), cache_dir.encode(),
+                         ctypes.byref(n), log, len(log))
+    if rc:
+        raise FeError(rc, L.fe_last_error().decode(errors="replace") + "\n" + log.value.decode(errors="replace"))
+    return n.value
+
+
+class Code:
+    """A compiled, loaded element kernel (owns the CUmodule)."""
+
+    def __init__(self, source: str, name: str, cache_dir: str = CACHE_DIR):
+        L = load()
+        os.makedirs(cache_dir, exist_ok=True)
+        h = ctypes.c_void_p()
+        log = ctypes.create_string_buffer(1 << 16)
+        rc = L.fe_code_compile(source.encode(), name.encode(), INCLUDE_DIR.encode(), cache_dir.encode(),
+                               ctypes.byref(h), log, len(log))
+        if rc:
+            raise FeError(rc, L.fe_last_error().decode(errors="replace") + "\n" + log.value.decode(errors="replace"))
+        self.handle = h
+        self.name = name
+
+    def __del__(self):
+        try:
+            if self.handle:
+                load().fe_code_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass

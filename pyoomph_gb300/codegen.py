@@ -1,0 +1,424 @@
+"""CUDA code generator: lowers a weak form to a fused element kernel.
+
+The reference's ``FiniteElementCode::write_code`` (``src/codegen.cpp:4684``,
+``write_generic_RJM`` :3912-4110) emits, per domain, a C function that loops
+over integration points, asks the host for the shape buffer
+(``fill_shape_buffer_for_point``), interpolates the fields, and adds
+``R[l_test] += ...`` and ``J[l_test][l_shape] += ...``.
+
+Here the same weak form is split into
+
+* a *pointwise* function of the field values and gradients at one
+  integration point that returns the test-component coefficients ``r`` and
+  their derivatives ``D = dr/d(field components)`` (sympy differentiates and
+  eliminates common subexpressions, the job GiNaC does in the reference),
+* a fixed kernel skeleton that stages reference tables and nodal data in
+  shared memory, computes the metric-tensor geometry of
+  ``fill_shape_info_at_s`` (``elements.cpp:3593-3990``) per (element,
+  integration point) thread, and contracts ``J_e = sum_q B^T D B`` per
+  (element, row) thread.
+
+The residual is accumulated in FP64 with the coefficients pulled back to
+reference coordinates (``rhat_b = w sum_i g^{bi} r_i``), so it never needs
+per-element physical shape gradients; the Jacobian uses physical gradients
+and ``D`` in FP64 or FP32 (``jac_precision``).
+"""
+from __future__ import annotations
+
+import hashlib
+from dataclasses import dataclass, field
+from typing import Dict, List, Tuple
+
+import numpy as np
+import sympy as sp
+from sympy.printing.c import C99CodePrinter
+
+from . import expressions as E
+from .spaces import ElementType, Layout, make_layout
+
+
+class _Printer(C99CodePrinter):
+    """C printer: small integer powers as products, exp/sqrt as libm calls."""
+
+    def __init__(self, names: Dict[sp.Symbol, str]):
+        super().__init__()
+        self._names = names
+
+    def _print_Symbol(self, s):
+        if s in self._names:
+            return self._names[s]
+        return super()._print_Symbol(s)
+
+    def _print_Pow(self, e):
+        b, x = e.args
+        if x.is_Integer:
+            n = int(x)
+            if n == 2:
+                bs = self._print(b)
+                return f"(({bs})*({bs}))"
+            if n == -1:
+                return f"(1.0/({self._print(b)}))"
+            if n == -2:
+                bs = self._print(b)
+                return f"(1.0/(({bs})*({bs})))"
+            if 2 < n <= 4:
+                bs = self._print(b)
+                return "(" + "*".join([f"({bs})"] * n) + ")"
+        if x == sp.Rational(1, 2):
+            return f"sqrt({self._print(b)})"
+        return f"pow({self._print(b)}, {self._print(x)})"
+
+    def _print_Rational(self, e):
+        return f"({float(e.p)!r}/{float(e.q)!r})"
+
+    def _print_Float(self, e):
+        return repr(float(e))
+
+    def _print_Integer(self, e):
+        return f"{float(int(e))!r}"
+
+    def _print_Pi(self, e):
+        return "3.141592653589793"
+
+
+@dataclass
+class Pointwise:
+    """Result of differentiating a weak form at one integration point."""
+    fields: List[Tuple[str, str]]          # (name, space) in nodal value order
+    dim: int
+    params: List[str]                      # parameter names in array order
+    r_exprs: List[sp.Expr]                 # [NTC]
+    d_entries: List[Tuple[int, int, sp.Expr]]  # (tc, ic, expr), nonzero only
+    uses_x: bool
+
+    @property
+    def ntc(self) -> int:
+        return len(self.fields) * (1 + self.dim)
+
+
+def differentiate(fields: List[Tuple[str, str]], dim: int, integrand: sp.Expr,
+                  params: List[str]) -> Pointwise:
+    """r_tc = d(integrand)/d(test component tc); D[tc, ic] = d r_tc / d(field
+    component ic).  Components per field: value, d/dx_0 .. d/dx_{dim-1}."""
+    integrand = sp.expand(integrand) if integrand.has(sp.Symbol) else integrand
+    tsyms, usyms = [], []
+    for name, _ in fields:
+        E.REG.field(name)
+        tsyms += [E.REG.test[name]] + list(E.REG.test_grad[name][:dim])
+        usyms += [E.REG.value[name]] + list(E.REG.grad[name][:dim])
+    r_exprs = []
+    for t in tsyms:
+        r = sp.diff(integrand, t)
+        if any(r.has(tt) for tt in tsyms):
+            raise ValueError("residual is not linear in the test functions")
+        r_exprs.append(sp.simplify(r) if r.count_ops() < 40 else r)
+    d_entries = []
+    for tc, r in enumerate(r_exprs):
+        for ic, u in enumerate(usyms):
+            d = sp.diff(r, u)
+            if d != 0:
+                d_entries.append((tc, ic, d))
+    uses_x = any(any(e.has(x) for x in E.X) for e in r_exprs)
+    return Pointwise(fields, dim, params, r_exprs, d_entries, uses_x)
+
+
+def _symbol_names(pw: Pointwise) -> Dict[sp.Symbol, str]:
+    names = {}
+    nc = 1 + pw.dim
+    for f, (name, _) in enumerate(pw.fields):
+        names[E.REG.value[name]] = f"U[{f * nc}]"
+        for i in range(pw.dim):
+            names[E.REG.grad[name][i]] = f"U[{f * nc + 1 + i}]"
+    for i in range(3):
+        names[E.X[i]] = f"Xq[{i}]"
+    for k, p in enumerate(pw.params):
+        names[E.parameter(p)] = f"P[{k}]"
+    return names
+
+
+def pointwise_source(pw: Pointwise) -> str:
+    """The generated device function fe_pointwise(U, Xq, P, r, D, flag)."""
+    names = _symbol_names(pw)
+    pr = _Printer(names)
+    lines = ["__device__ __forceinline__ void fe_pointwise(const double* __restrict__ U, "
+             "const double* __restrict__ Xq, const double* __restrict__ P, double* __restrict__ r, "
+             "double* __restrict__ D, int flag) {"]
+    exprs = list(pw.r_exprs)
+    n_r = len(exprs)
+    exprs += [d for (_, _, d) in pw.d_entries]
+    repl, reduced = sp.cse(exprs, symbols=sp.numbered_symbols("t_"), optimizations="basic")
+    for s, e in repl:
+        names[s] = s.name
+    for s, e in repl:
+        lines.append(f"  const double {s.name} = {pr.doprint(e)};")
+    for k in range(n_r):
+        lines.append(f"  r[{k}] = {pr.doprint(reduced[k])};")
+    if pw.d_entries:
+        lines.append("  if (flag) {")
+        for k in range(len(pw.d_entries)):
+            lines.append(f"    D[{k}] = {pr.doprint(reduced[n_r + k])};")
+        lines.append("  }")
+    lines.append("}")
+    return "\n".join(lines)
+
+
+@dataclass
+class KernelSpec:
+    name: str
+    source: str
+    et: ElementType
+    layout: Layout
+    pointwise: Pointwise
+    epb: int
+    threads: int
+    smem_bytes: int
+    jac_precision: str
+    tables: np.ndarray = field(repr=False, default=None)
+
+    @property
+    def key(self) -> str:
+        return hashlib.sha1(self.source.encode()).hexdigest()[:16]
+
+
+def _launch_shape(et: ElementType, nloc: int, per_elem_bytes: int, table_bytes: int,
+                  smem_cap: int = 200 * 1024) -> Tuple[int, int]:
+    """Elements per block and threads: keep both thread phases (element x
+    integration point, element x row) busy in whole warps, within the
+    shared-memory budget."""
+    best = None
+    for epb in range(1, 65):
+        smem = table_bytes + epb * per_elem_bytes
+        if smem > smem_cap:
+            break
+        work = max(epb * et.nq, epb * nloc)
+        threads = ((work + 31) // 32) * 32
+        if threads > 1024:
+            break
+        # prefer whole-warp phases and larger blocks
+        waste = (threads - epb * et.nq) / threads + (threads - epb * nloc) / threads
+        score = (-waste, epb)
+        if best is None or score > best[0]:
+            best = (score, epb, threads)
+    if best is None:
+        raise ValueError("element does not fit in shared memory")
+    return best[1], best[2]
+
+
+def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
+                    name: str = None, epb: int = None) -> KernelSpec:
+    dim, nn, nn1, nq = et.dim, et.nnode, et.nnode_c1, et.nq
+    fields = pw.fields
+    nf = len(fields)
+    nc = 1 + dim
+    ntc = nf * nc
+    spaces = [sp_ for _, sp_ in fields]
+    layout = make_layout(et, spaces)
+    nloc = layout.n
+    nval = nf
+    has_c1 = any(s == "C1" for s in spaces)
+    ndnz = max(1, len(pw.d_entries))
+    jreal = "double" if jac_precision == "f64" else "float"
+    jbytes = 8 if jac_precision == "f64" else 4
+    table_doubles = nq + nq * nn + nq * nn * dim + nq * nn1 + nq * nn1 * dim
+    table_bytes = table_doubles * 8
+    per_elem = (nn * dim + nn * nval + nq * ntc) * 8 + (nq * ndnz + nq * nn * dim + (nq * nn1 * dim if has_c1 else 0)) * jbytes
+    if epb is None:
+        epb, threads = _launch_shape(et, nloc, per_elem, table_bytes)
+    else:
+        threads = ((max(epb * nq, epb * nloc) + 31) // 32) * 32
+    smem = table_bytes + epb * per_elem
+    smem = (smem + 15) // 16 * 16
+    if name is None:
+        h = hashlib.sha1((et.name + jac_precision + str(pw.r_exprs) + str(pw.d_entries)).encode()).hexdigest()[:10]
+        name = f"fe_elem_{et.name.lower()}_{jac_precision}_{h}"
+
+    # trial components that carry any D entry, per field
+    used_ic = sorted({ic for (_, ic, _) in pw.d_entries})
+    src = []
+    w = src.append
+    w("// generated element kernel -- do not edit")
+    w('#include "fe_device.cuh"')
+    w(f"#define FE_DIM {dim}\n#define FE_NN {nn}\n#define FE_NN1 {nn1}\n#define FE_NQ {nq}")
+    w(f"#define FE_NVAL {nval}\n#define FE_NLOC {nloc}\n#define FE_EPB {epb}\n#define FE_NT {threads}")
+    w(f"#define FE_NF {nf}\n#define FE_NTC {ntc}\n#define FE_NDNZ {ndnz}")
+    w(f"typedef {jreal} jreal;")
+    w(f"__constant__ int c_loc_field[FE_NLOC] = {{{', '.join(map(str, layout.field))}}};")
+    w(f"__constant__ int c_loc_sub[FE_NLOC] = {{{', '.join(map(str, layout.sub))}}};")
+    w(f"__constant__ int c_fspace1[FE_NF] = {{{', '.join('1' if s == 'C1' else '0' for s in spaces)}}};")
+    w(f"__constant__ int c_c1idx[FE_NN1] = {{{', '.join(map(str, et.c1_index))}}};")
+    w(pointwise_source(pw))
+    w(f'extern "C" __global__ void __launch_bounds__(FE_NT) {name}(const FeElemArgs a) {{')
+    w("  extern __shared__ __align__(16) unsigned char fe_smem[];")
+    w("  double* sW = reinterpret_cast<double*>(fe_smem);")
+    w("  double* sPsi2 = sW + FE_NQ;")
+    w("  double* sDps2 = sPsi2 + FE_NQ * FE_NN;")
+    w("  double* sPsi1 = sDps2 + FE_NQ * FE_NN * FE_DIM;")
+    w("  double* sDps1 = sPsi1 + FE_NQ * FE_NN1;")
+    w("  double* sX = sDps1 + FE_NQ * FE_NN1 * FE_DIM;")
+    w("  double* sU = sX + FE_EPB * FE_NN * FE_DIM;")
+    w("  double* sRh = sU + FE_EPB * FE_NN * FE_NVAL;")
+    w("  jreal* sD = reinterpret_cast<jreal*>(sRh + FE_EPB * FE_NQ * FE_NTC);")
+    w("  jreal* sDx2 = sD + FE_EPB * FE_NQ * FE_NDNZ;")
+    w("  jreal* sDx1 = sDx2 + FE_EPB * FE_NQ * FE_NN * FE_DIM;")
+    w("  (void)sDx1;")
+    w("  const long long e0 = (long long)blockIdx.x * FE_EPB;")
+    w("  const long long rem = a.n_elem - e0;")
+    w("  const int nel = rem < FE_EPB ? (int)rem : FE_EPB;")
+    w("  const int flag = a.flag;")
+    w(f"  for (int k = threadIdx.x; k < {table_doubles}; k += FE_NT) sW[k] = a.tables[k];")
+    w("  for (int k = threadIdx.x; k < nel * FE_NN; k += FE_NT) {")
+    w("    const int el = k / FE_NN, l = k - el * FE_NN;")
+    w("    const int node = a.conn[(e0 + el) * FE_NN + l];")
+    w("    #pragma unroll")
+    w("    for (int d = 0; d < FE_DIM; ++d) sX[k * FE_DIM + d] = a.x[(long long)node * FE_DIM + d];")
+    w("    #pragma unroll")
+    w("    for (int v = 0; v < FE_NVAL; ++v) sU[k * FE_NVAL + v] = a.values[(long long)node * a.nval + v];")
+    w("  }")
+    w("  __syncthreads();")
+    # ---------------- phase A ----------------
+    w("  for (int p = threadIdx.x; p < nel * FE_NQ; p += FE_NT) {")
+    w("    const int el = p / FE_NQ, q = p - el * FE_NQ;")
+    w("    const double* X = sX + el * FE_NN * FE_DIM;")
+    w("    const double* dps = sDps2 + q * FE_NN * FE_DIM;")
+    w("    double g[FE_DIM][FE_DIM]; double J;")
+    w("    fe_metric_geometry<FE_DIM, FE_NN>(X, dps, g, J);")
+    w("    if (!(J > 0.0)) atomicExch(a.status, 1);")
+    w("    const double wq = sW[q] * J;")
+    w("    double Xq[3] = {0.0, 0.0, 0.0};")
+    if pw.uses_x:
+        w("    #pragma unroll")
+        w("    for (int l = 0; l < FE_NN; ++l) {")
+        w("      const double ps = sPsi2[q * FE_NN + l];")
+        w("      #pragma unroll")
+        w("      for (int i = 0; i < FE_DIM; ++i) Xq[i] += X[l * FE_DIM + i] * ps;")
+        w("    }")
+    w("    double U[FE_NTC];")
+    for f, (fname, fsp) in enumerate(fields):
+        base = f * nc
+        if fsp == "C2":
+            w(f"    {{ double v = 0.0, gs[FE_DIM] = {{{', '.join(['0.0'] * dim)}}};")
+            w("      #pragma unroll")
+            w("      for (int l = 0; l < FE_NN; ++l) {")
+            w(f"        const double u = sU[(el * FE_NN + l) * FE_NVAL + {f}];")
+            w("        v += u * sPsi2[q * FE_NN + l];")
+            w("        #pragma unroll")
+            w("        for (int b = 0; b < FE_DIM; ++b) gs[b] += u * dps[l * FE_DIM + b];")
+            w("      }")
+        else:
+            w(f"    {{ double v = 0.0, gs[FE_DIM] = {{{', '.join(['0.0'] * dim)}}};")
+            w("      #pragma unroll")
+            w("      for (int l = 0; l < FE_NN1; ++l) {")
+            w(f"        const double u = sU[(el * FE_NN + c_c1idx[l]) * FE_NVAL + {f}];")
+            w("        v += u * sPsi1[q * FE_NN1 + l];")
+            w("        #pragma unroll")
+            w("        for (int b = 0; b < FE_DIM; ++b) gs[b] += u * sDps1[(q * FE_NN1 + l) * FE_DIM + b];")
+            w("      }")
+        w(f"      U[{base}] = v;")
+        w("      #pragma unroll")
+        w(f"      for (int i = 0; i < FE_DIM; ++i) {{ double s = 0.0;")
+        w("        #pragma unroll")
+        w(f"        for (int b = 0; b < FE_DIM; ++b) s += g[b][i] * gs[b];")
+        w(f"        U[{base} + 1 + i] = s; }}")
+        w("    }")
+    w("    double r[FE_NTC]; double D[FE_NDNZ];")
+    w("    fe_pointwise(U, Xq, a.params, r, D, flag);")
+    w("    double* rh = sRh + (el * FE_NQ + q) * FE_NTC;")
+    w("    #pragma unroll")
+    w("    for (int f = 0; f < FE_NF; ++f) {")
+    w("      rh[f * (1 + FE_DIM)] = wq * r[f * (1 + FE_DIM)];")
+    w("      #pragma unroll")
+    w("      for (int b = 0; b < FE_DIM; ++b) { double s = 0.0;")
+    w("        #pragma unroll")
+    w("        for (int i = 0; i < FE_DIM; ++i) s += g[b][i] * r[f * (1 + FE_DIM) + 1 + i];")
+    w("        rh[f * (1 + FE_DIM) + 1 + b] = wq * s; }")
+    w("    }")
+    w("    if (flag) {")
+    w("      jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZ;")
+    w("      #pragma unroll")
+    w("      for (int k = 0; k < FE_NDNZ; ++k) Dq[k] = (jreal)(wq * D[k]);")
+    w("      fe_phys_grad<FE_DIM, FE_NN, jreal>(g, dps, sDx2 + (el * FE_NQ + q) * FE_NN * FE_DIM);")
+    if has_c1:
+        w("      fe_phys_grad<FE_DIM, FE_NN1, jreal>(g, sDps1 + q * FE_NN1 * FE_DIM, sDx1 + (el * FE_NQ + q) * FE_NN1 * FE_DIM);")
+    w("    }")
+    w("  }")
+    w("  __syncthreads();")
+    # ---------------- phase B ----------------
+    w("  for (int p = threadIdx.x; p < nel * FE_NLOC; p += FE_NT) {")
+    w("    const int el = p / FE_NLOC, i = p - el * FE_NLOC;")
+    w("    const int tf = c_loc_field[i], lt = c_loc_sub[i];")
+    w("    const int t1 = c_fspace1[tf];")
+    w("    const int tnn = t1 ? FE_NN1 : FE_NN;")
+    w("    const double* tpsi = t1 ? sPsi1 : sPsi2;")
+    w("    const double* tdps = t1 ? sDps1 : sDps2;")
+    w("    double Racc = 0.0;")
+    w("    jreal Jr[FE_NLOC];")
+    w("    #pragma unroll")
+    w("    for (int k = 0; k < FE_NLOC; ++k) Jr[k] = (jreal)0;")
+    w("    for (int q = 0; q < FE_NQ; ++q) {")
+    w("      const double* rh = sRh + (el * FE_NQ + q) * FE_NTC + tf * (1 + FE_DIM);")
+    w("      const double pv = tpsi[q * tnn + lt];")
+    w("      double racc = rh[0] * pv;")
+    w("      #pragma unroll")
+    w("      for (int b = 0; b < FE_DIM; ++b) racc += rh[1 + b] * tdps[(q * tnn + lt) * FE_DIM + b];")
+    w("      Racc += racc;")
+    w("      if (flag) {")
+    w("        const jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZ;")
+    w("        const jreal* tdx = t1 ? (sDx1 + ((el * FE_NQ + q) * FE_NN1 + lt) * FE_DIM)")
+    w("                             : (sDx2 + ((el * FE_NQ + q) * FE_NN + lt) * FE_DIM);")
+    w("        const jreal phi0 = (jreal)pv;")
+    for d in range(dim):
+        w(f"        const jreal phi{d + 1} = tdx[{d}];")
+    # a_ic accumulators
+    for ic in used_ic:
+        w(f"        jreal a{ic} = (jreal)0;")
+    for k, (tc, ic, _) in enumerate(pw.d_entries):
+        tfield, tcomp = divmod(tc, nc)
+        w(f"        a{ic} += (tf == {tfield}) ? phi{tcomp} * Dq[{k}] : (jreal)0;")
+    # j loop per trial field
+    for f, (fname, fsp) in enumerate(fields):
+        comps = [ic for ic in used_ic if ic // nc == f]
+        if not comps:
+            continue
+        if fsp == "C2":
+            w("        {")
+            w("          const double* psi = sPsi2 + q * FE_NN;")
+            w("          const jreal* dx = sDx2 + (el * FE_NQ + q) * FE_NN * FE_DIM;")
+            for ls in range(nn):
+                terms = []
+                for ic in comps:
+                    c = ic % nc
+                    if c == 0:
+                        terms.append(f"a{ic} * (jreal)psi[{ls}]")
+                    else:
+                        terms.append(f"a{ic} * dx[{ls * dim + c - 1}]")
+                w(f"          Jr[{layout.loc_of[f][ls]}] += {' + '.join(terms)};")
+            w("        }")
+        else:
+            w("        {")
+            w("          const double* psi = sPsi1 + q * FE_NN1;")
+            w("          const jreal* dx = sDx1 + (el * FE_NQ + q) * FE_NN1 * FE_DIM;")
+            for ls in range(nn1):
+                terms = []
+                for ic in comps:
+                    c = ic % nc
+                    if c == 0:
+                        terms.append(f"a{ic} * (jreal)psi[{ls}]")
+                    else:
+                        terms.append(f"a{ic} * dx[{ls * dim + c - 1}]")
+                w(f"          Jr[{layout.loc_of[f][ls]}] += {' + '.join(terms)};")
+            w("        }")
+    w("      }")
+    w("    }")
+    w("    const long long row = (e0 + el) * FE_NLOC + i;")
+    w("    a.rbuf[row] = Racc;")
+    w("    if (flag) {")
+    w("      jreal* jb = reinterpret_cast<jreal*>(a.jbuf) + row * FE_NLOC;")
+    w("      #pragma unroll")
+    w("      for (int k = 0; k < FE_NLOC; ++k) jb[k] = Jr[k];")
+    w("    }")
+    w("  }")
+    w("}")
+    source = "\n".join(src) + "\n"
+    return KernelSpec(name=name, source=source, et=et, layout=layout, pointwise=pw, epb=epb,
+                      threads=threads, smem_bytes=smem, jac_precision=jac_precision,
+                      tables=et.packed_tables())

@@ -1,0 +1,22 @@
+// fe_abi.h -- argument block shared by the runtime (fe_gb300.cu) and the
+// generated element kernels (compiled by nvrtc, which include fe_device.cuh).
+// Plain types only: the same bytes are built on the host and read on the
+// device through the kernel-parameter buffer.
+#ifndef FE_ABI_H
+#define FE_ABI_H
+
+struct FeElemArgs {
+  const double *x;      // [n_nodes * dim] nodal positions
+  const int *conn;      // [n_elem * nnode] global node numbers
+  const double *values; // [n_nodes * nval] nodal values
+  const double *params; // global parameters
+  const double *tables; // reference shape/quadrature tables of the element type
+  double *rbuf;         // [n_elem * nlocal] element residuals
+  void *jbuf;           // [n_elem * nlocal * nlocal] element Jacobians (f64 or f32)
+  long long n_elem;
+  int nval;
+  int flag;             // 0: residual only, 1: residual and Jacobian
+  int *status;          // device status word (0 = ok)
+};
+
+#endif

@@ -1,0 +1,103 @@
+// fe_device.cuh -- device helpers included by the generated element kernels
+// (compiled at run time by nvrtc for sm_103a; no standard headers).
+#ifndef FE_DEVICE_CUH
+#define FE_DEVICE_CUH
+
+#include "fe_abi.h"
+
+// Geometry at one integration point through the metric tensor, the route of
+// BulkElementBase::fill_shape_info_at_s (src/elements.cpp:3593-3990):
+//   t[a][i]  = sum_l x_l,i dpsi_l/ds_a         (tangent vectors)
+//   a_ab     = t_a . t_b,  aup = a^{-1}
+//   g[b][i]  = sum_a aup(a,b) t[a][i]          ([g^{ab} g_a]_i)
+//   J        = sqrt(det a_ab)
+// so that d/dx_i = sum_b g[b][i] d/ds_b and the weight is W * J.
+template <int DIM, int NN>
+__device__ __forceinline__ void fe_metric_geometry(const double *__restrict__ X,
+                                                   const double *__restrict__ dps,
+                                                   double (&g)[DIM][DIM], double &J) {
+  double t[DIM][DIM];
+#pragma unroll
+  for (int a = 0; a < DIM; ++a)
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) t[a][i] = 0.0;
+#pragma unroll
+  for (int l = 0; l < NN; ++l)
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      const double xl = X[l * DIM + i];
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) t[a][i] += xl * dps[l * DIM + a];
+    }
+  double am[DIM][DIM];
+#pragma unroll
+  for (int al = 0; al < DIM; ++al)
+#pragma unroll
+    for (int be = 0; be < DIM; ++be) {
+      double s = 0.0;
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) s += t[al][i] * t[be][i];
+      am[al][be] = s;
+    }
+  double aup[DIM][DIM];
+  double det;
+  if constexpr (DIM == 1) {
+    det = am[0][0];
+    aup[0][0] = 1.0 / det;
+  } else if constexpr (DIM == 2) {
+    det = am[0][0] * am[1][1] - am[0][1] * am[1][0];
+    aup[0][0] = am[1][1] / det;
+    aup[0][1] = -am[0][1] / det;
+    aup[1][0] = -am[1][0] / det;
+    aup[1][1] = am[0][0] / det;
+  } else {
+    det = am[0][0] * am[1][1] * am[2][2] + am[0][1] * am[1][2] * am[2][0] + am[0][2] * am[1][0] * am[2][1] -
+          am[0][0] * am[1][2] * am[2][1] - am[0][1] * am[1][0] * am[2][2] - am[0][2] * am[1][1] * am[2][0];
+    aup[0][0] = (am[1][1] * am[2][2] - am[1][2] * am[2][1]) / det;
+    aup[0][1] = -(am[0][1] * am[2][2] - am[0][2] * am[2][1]) / det;
+    aup[0][2] = (am[0][1] * am[1][2] - am[0][2] * am[1][1]) / det;
+    aup[1][0] = -(am[1][0] * am[2][2] - am[1][2] * am[2][0]) / det;
+    aup[1][1] = (am[0][0] * am[2][2] - am[0][2] * am[2][0]) / det;
+    aup[1][2] = -(am[0][0] * am[1][2] - am[0][2] * am[1][0]) / det;
+    aup[2][0] = (am[1][0] * am[2][1] - am[1][1] * am[2][0]) / det;
+    aup[2][1] = -(am[0][0] * am[2][1] - am[0][1] * am[2][0]) / det;
+    aup[2][2] = (am[0][0] * am[1][1] - am[0][1] * am[1][0]) / det;
+  }
+#pragma unroll
+  for (int b = 0; b < DIM; ++b)
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      double s = 0.0;
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) s += aup[a][b] * t[a][i];
+      g[b][i] = s;
+    }
+  J = sqrt(det);
+}
+
+// Physical shape gradients dx[l][i] = sum_b g[b][i] dps[l][b] (dx_shape_*
+// of the shape buffer), written in the Jacobian's precision T.
+template <int DIM, int NN, typename T>
+__device__ __forceinline__ void fe_phys_grad(const double (&g)[DIM][DIM], const double *__restrict__ dps,
+                                             T *__restrict__ out) {
+  T gl[DIM][DIM];
+#pragma unroll
+  for (int b = 0; b < DIM; ++b)
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) gl[b][i] = (T)g[b][i];
+#pragma unroll
+  for (int l = 0; l < NN; ++l) {
+    T d[DIM];
+#pragma unroll
+    for (int b = 0; b < DIM; ++b) d[b] = (T)dps[l * DIM + b];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      T s = (T)0;
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) s += gl[b][i] * d[b];
+      out[l * DIM + i] = s;
+    }
+  }
+}
+
+#endif

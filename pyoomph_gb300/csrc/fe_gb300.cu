@@ -1,0 +1,814 @@
+// fe_gb300.cu -- runtime of the GB300 finite-element assembly engine.
+//
+// Implements the C-ABI of include/fe_gb300.h:
+//   * element code JIT (nvrtc -> cubin for sm_103a -> cudaLibraryLoadData),
+//     the device counterpart of pyoomph's C compiler + dlopen path
+//     (pyoomph/generic/ccompiler.py:207-242, src/ccompiler.cpp:191-213);
+//   * the resident problem: nodal positions/values, connectivity and
+//     equation numbers in HBM;
+//   * the CSR pattern of oomph's vectors-of-pairs assembler
+//     (problem.cc:5332-5666): rows in equation order, columns in order of
+//     first insertion over (element, local i, local j), built once per mesh;
+//   * the deterministic scatter: every CSR slot (and every residual entry)
+//     owns the list of element contributions that reach it, in element
+//     order, so a slot is summed by one thread in exactly the order the
+//     reference accumulates it (problem.cc:5500-5560) -- no atomics;
+//   * Newton helpers: dof -> nodal value scatter, residual max-norm with
+//     NaN -> inf (double_vector.cc:611-629), x -= dx.
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/fe_gb300.h"
+#include "fe_abi.h"
+
+#define FE_VERSION "fe_gb300 0.1.0 (sm_103a)"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                      \
+  do {                                                                                      \
+    cudaError_t _e = (expr);                                                                \
+    if (_e != cudaSuccess)                                                                  \
+      return fail(_e == cudaErrorMemoryAllocation ? FE_ERR_NOMEM : FE_ERR_CUDA, "%s: %s (%s:%d)", \
+                  #expr, cudaGetErrorString(_e), __FILE__, __LINE__);                       \
+  } while (0)
+
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  int alloc(size_t n) {
+    if (p) {
+      cudaFree(p);
+      p = nullptr;
+    }
+    bytes = n;
+    if (n == 0) return FE_OK;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return fail(FE_ERR_NOMEM, "cudaMalloc(%zu) failed: %s", n, cudaGetErrorString(e));
+    }
+    return FE_OK;
+  }
+  int upload(const void *h, size_t n) {
+    int rc = alloc(n);
+    if (rc) return rc;
+    if (n) CUDA_TRY(cudaMemcpy(p, h, n, cudaMemcpyHostToDevice));
+    return FE_OK;
+  }
+  template <class T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+// ---------------------------------------------------------------------------
+// kernels of the runtime (element kernels come from nvrtc)
+// ---------------------------------------------------------------------------
+
+// dofs -> nodal values (the Data values a Newton update writes)
+__global__ void k_scatter_dofs(const double *__restrict__ dofs, const int *__restrict__ eqn,
+                               double *__restrict__ values, long long n) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x) {
+    int e = eqn[k];
+    if (e >= 0) values[k] = dofs[e];
+  }
+}
+
+// CSR slot s = sum of its element contributions in element order
+template <typename T>
+__global__ void k_gather_slots(const long long *__restrict__ cptr, const unsigned *__restrict__ cidx,
+                               const T *__restrict__ jbuf, T *__restrict__ vals, long long nnz) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nnz;
+       s += (long long)gridDim.x * blockDim.x) {
+    const long long b = cptr[s], e = cptr[s + 1];
+    T acc = jbuf[cidx[b]];
+    for (long long k = b + 1; k < e; k++) acc += jbuf[cidx[k]];
+    vals[s] = acc;
+  }
+}
+
+// residual entry r = sum of its element contributions in element order
+__global__ void k_gather_rows(const long long *__restrict__ rptr, const unsigned *__restrict__ ridx,
+                              const double *__restrict__ rbuf, double *__restrict__ R, long long n) {
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;
+       r += (long long)gridDim.x * blockDim.x) {
+    const long long b = rptr[r], e = rptr[r + 1];
+    double acc = 0.0;
+    for (long long k = b; k < e; k++) acc += rbuf[ridx[k]];
+    R[r] = acc;
+  }
+}
+
+// max |R| with NaN -> inf; one block per chunk, then a single finishing block
+__device__ __forceinline__ double absnan(double v) { return (v != v) ? __longlong_as_double(0x7ff0000000000000LL) : fabs(v); }
+
+__global__ void k_absmax_partial(const double *__restrict__ R, long long n, double *__restrict__ part) {
+  __shared__ double sm[32];
+  double m = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    m = fmax(m, absnan(R[i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) part[blockIdx.x] = m;
+  }
+}
+
+__global__ void k_dof_update(double *__restrict__ x, const double *__restrict__ dx, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] -= dx[i];
+}
+
+int grid_for(long long n, int threads, int sms) {
+  long long g = (n + threads - 1) / threads;
+  long long cap = (long long)sms * 16;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+// ---------------------------------------------------------------------------
+// JIT
+// ---------------------------------------------------------------------------
+uint64_t fnv1a(const std::string &s) {
+  uint64_t h = 1469598103934665603ULL;
+  for (unsigned char c : s) {
+    h ^= c;
+    h *= 1099511628211ULL;
+  }
+  return h;
+}
+
+bool read_file(const std::string &path, std::string &out) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) return false;
+  std::ostringstream ss;
+  ss << f.rdbuf();
+  out = ss.str();
+  return true;
+}
+
+int ensure_context() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return fail(FE_ERR_NOGPU, "no CUDA device: %s", cudaGetErrorString(e));
+  CUDA_TRY(cudaFree(0)); // creates / binds the primary context
+  return FE_OK;
+}
+
+int sm_count_cached() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (!sms) sms = 1;
+  }
+  return sms;
+}
+
+} // namespace
+
+// A loaded element kernel.  The runtime's library-management API
+// (cudaLibraryLoadData / cudaLibraryGetKernel) is used instead of the driver
+// API so that the library links only against cudart and nvrtc.
+struct fe_code {
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t func = nullptr;
+  std::string name;
+  ~fe_code() {
+    if (lib) cudaLibraryUnload(lib);
+  }
+};
+
+struct Domain {
+  fe_code_t *code = nullptr;
+  int nnode = 0, nlocal = 0;
+  long long n_elem = 0;
+  int epb = 1, threads = 128, smem = 0;
+  DevBuf conn, tables, rbuf, jbuf;
+  long long jbase = 0; // flat offset of this domain's entries in the global contribution space
+  long long rbase = 0;
+  std::vector<int32_t> local_node, local_val;
+};
+
+struct fe_problem {
+  int dim = 0, nval = 0, jac_prec = FE_JAC_F64;
+  long long n_nodes = 0, n_dof = 0, nnz = 0;
+  int n_params = 0;
+  std::vector<Domain> domains;
+  DevBuf x, values, eqn, params, status;
+  DevBuf rowptr, colidx, cptr, cidx, rptr, ridx;
+  DevBuf partial;
+  // the domain buffers are one allocation per kind, addressed by offsets:
+  DevBuf jbuf_all, rbuf_all;
+  std::vector<int32_t> h_rowptr, h_colidx;
+  // stage timing (tracing): events recorded around the stages of fe_assemble
+  bool timing = false;
+  std::vector<std::vector<cudaEvent_t>> pending; // per call: 5 events
+  double stage_ms[4] = {0, 0, 0, 0};
+  long long stage_calls = 0;
+  ~fe_problem() {
+    for (auto &v : pending)
+      for (auto e : v) cudaEventDestroy(e);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// CSR pattern in the reference's insertion order + contribution lists
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Incident {
+  int dom;
+  long long e;
+  int i;
+};
+
+// Builds, for all rows in [r0, r1): row lengths / columns / per-slot
+// contributions.  Two passes: count (fill=false), then fill.
+struct PatternBuilder {
+  const fe_problem *P;
+  const std::vector<const int32_t *> *conn_h;
+  const int32_t *eqn_h;
+  // incidence of each dof: (domain, element, local i) in element order
+  std::vector<long long> inc_ptr;
+  std::vector<Incident> inc;
+
+  int32_t geq(const Domain &d, const int32_t *conn, long long e, int k) const {
+    int node = conn[e * d.nnode + d.local_node[k]];
+    return eqn_h[(long long)node * P->nval + d.local_val[k]];
+  }
+
+  void build_incidence() {
+    const long long n = P->n_dof;
+    std::vector<long long> cnt(n + 1, 0);
+    for (size_t di = 0; di < P->domains.size(); di++) {
+      const Domain &d = P->domains[di];
+      const int32_t *conn = (*conn_h)[di];
+      for (long long e = 0; e < d.n_elem; e++)
+        for (int i = 0; i < d.nlocal; i++) {
+          int32_t r = geq(d, conn, e, i);
+          if (r >= 0) cnt[r + 1]++;
+        }
+    }
+    for (long long r = 0; r < n; r++) cnt[r + 1] += cnt[r];
+    inc_ptr = cnt;
+    inc.resize(cnt[n]);
+    std::vector<long long> pos(cnt.begin(), cnt.end() - 1);
+    for (size_t di = 0; di < P->domains.size(); di++) {
+      const Domain &d = P->domains[di];
+      const int32_t *conn = (*conn_h)[di];
+      for (long long e = 0; e < d.n_elem; e++)
+        for (int i = 0; i < d.nlocal; i++) {
+          int32_t r = geq(d, conn, e, i);
+          if (r >= 0) inc[pos[r]++] = Incident{(int)di, e, i};
+        }
+    }
+  }
+
+  // per-row work.  marker: [n_dof] scratch (-1), slot_of: column -> local slot
+  void row(long long r, std::vector<int32_t> &marker, std::vector<int32_t> &cols,
+           std::vector<long long> &slot_cnt, bool fill, int32_t *colidx_out, long long *cptr_out,
+           unsigned *cidx_out, long long cbase, long long *row_len, long long *row_contrib) const {
+    cols.clear();
+    slot_cnt.clear();
+    long long ncontrib = 0;
+    for (long long k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
+      const Incident &I = inc[k];
+      const Domain &d = P->domains[I.dom];
+      const int32_t *conn = (*conn_h)[I.dom];
+      for (int j = 0; j < d.nlocal; j++) {
+        int32_t c = geq(d, conn, I.e, j);
+        if (c < 0) continue;
+        int32_t s = marker[c];
+        if (s < 0) {
+          s = (int32_t)cols.size();
+          marker[c] = s;
+          cols.push_back(c);
+          slot_cnt.push_back(0);
+        }
+        slot_cnt[s]++;
+        ncontrib++;
+      }
+    }
+    *row_len = (long long)cols.size();
+    *row_contrib = ncontrib;
+    if (fill) {
+      // columns and per-slot pointers
+      long long acc = cbase;
+      for (size_t s = 0; s < cols.size(); s++) {
+        colidx_out[s] = cols[s];
+        cptr_out[s] = acc;
+        acc += slot_cnt[s];
+      }
+      // contributions in element order per slot
+      std::vector<long long> wpos(cols.size());
+      for (size_t s = 0; s < cols.size(); s++) wpos[s] = cptr_out[s];
+      for (long long k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
+        const Incident &I = inc[k];
+        const Domain &d = P->domains[I.dom];
+        const int32_t *conn = (*conn_h)[I.dom];
+        const long long base = d.jbase + (I.e * d.nlocal + I.i) * (long long)d.nlocal;
+        for (int j = 0; j < d.nlocal; j++) {
+          int32_t c = geq(d, conn, I.e, j);
+          if (c < 0) continue;
+          cidx_out[wpos[marker[c]]++] = (unsigned)(base + j);
+        }
+      }
+    }
+    for (int32_t c : cols) marker[c] = -1;
+  }
+};
+
+int build_pattern(fe_problem *P, const std::vector<const int32_t *> &conn_h, const int32_t *eqn_h) {
+  PatternBuilder B;
+  B.P = P;
+  B.conn_h = &conn_h;
+  B.eqn_h = eqn_h;
+  B.build_incidence();
+  const long long n = P->n_dof;
+  unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  std::vector<long long> row_len(n), row_con(n);
+  auto pass = [&](bool fill, std::vector<int32_t> *colidx, std::vector<long long> *cptr,
+                  std::vector<unsigned> *cidx, const std::vector<long long> *rp,
+                  const std::vector<long long> *cp) {
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nthreads; t++) {
+      th.emplace_back([&, t]() {
+        std::vector<int32_t> marker(n > 0 ? n : 1, -1), cols;
+        std::vector<long long> slot_cnt;
+        long long lo = n * t / nthreads, hi = n * (t + 1) / nthreads;
+        for (long long r = lo; r < hi; r++) {
+          long long rl, rc;
+          if (!fill) {
+            B.row(r, marker, cols, slot_cnt, false, nullptr, nullptr, nullptr, 0, &rl, &rc);
+            row_len[r] = rl;
+            row_con[r] = rc;
+          } else {
+            long long o = (*rp)[r];
+            B.row(r, marker, cols, slot_cnt, true, colidx->data() + o, cptr->data() + o, cidx->data(),
+                  (*cp)[r], &rl, &rc);
+          }
+        }
+      });
+    }
+    for (auto &x : th) x.join();
+  };
+  pass(false, nullptr, nullptr, nullptr, nullptr, nullptr);
+  std::vector<long long> rp(n + 1, 0), cp(n + 1, 0);
+  for (long long r = 0; r < n; r++) {
+    rp[r + 1] = rp[r] + row_len[r];
+    cp[r + 1] = cp[r] + row_con[r];
+  }
+  const long long nnz = rp[n];
+  if (nnz > 0x7fffffffLL) return fail(FE_ERR_ARG, "nnz %lld exceeds int32 CSR", nnz);
+  std::vector<int32_t> colidx(nnz);
+  std::vector<long long> cptr(nnz + 1);
+  std::vector<unsigned> cidx(cp[n]);
+  pass(true, &colidx, &cptr, &cidx, &rp, &cp);
+  cptr[nnz] = cp[n];
+  P->nnz = nnz;
+  P->h_rowptr.resize(n + 1);
+  for (long long r = 0; r <= n; r++) P->h_rowptr[r] = (int32_t)rp[r];
+  P->h_colidx = colidx;
+  int rc;
+  if ((rc = P->rowptr.upload(P->h_rowptr.data(), sizeof(int32_t) * (n + 1)))) return rc;
+  if ((rc = P->colidx.upload(colidx.data(), sizeof(int32_t) * nnz))) return rc;
+  if ((rc = P->cptr.upload(cptr.data(), sizeof(long long) * (nnz + 1)))) return rc;
+  if ((rc = P->cidx.upload(cidx.data(), sizeof(unsigned) * cidx.size()))) return rc;
+  // residual contribution lists: incidence in element order
+  std::vector<long long> rptr(n + 1);
+  std::vector<unsigned> ridx(B.inc.size());
+  for (long long r = 0; r <= n; r++) rptr[r] = B.inc_ptr[r];
+  for (size_t k = 0; k < B.inc.size(); k++) {
+    const Incident &I = B.inc[k];
+    const Domain &d = P->domains[I.dom];
+    ridx[k] = (unsigned)(d.rbase + I.e * d.nlocal + I.i);
+  }
+  if ((rc = P->rptr.upload(rptr.data(), sizeof(long long) * (n + 1)))) return rc;
+  if ((rc = P->ridx.upload(ridx.data(), sizeof(unsigned) * ridx.size()))) return rc;
+  return FE_OK;
+}
+
+int launch_elements(fe_problem *p, int flag, cudaStream_t st) {
+  for (Domain &d : p->domains) {
+    if (d.n_elem == 0) continue;
+    FeElemArgs a;
+    a.x = p->x.as<double>();
+    a.conn = d.conn.as<int>();
+    a.values = p->values.as<double>();
+    a.params = p->params.as<double>();
+    a.tables = d.tables.as<double>();
+    a.rbuf = p->rbuf_all.as<double>() + d.rbase;
+    if (p->jac_prec == FE_JAC_F64)
+      a.jbuf = (void *)(p->jbuf_all.as<double>() + d.jbase);
+    else
+      a.jbuf = (void *)(p->jbuf_all.as<float>() + d.jbase);
+    a.n_elem = d.n_elem;
+    a.nval = p->nval;
+    a.flag = flag;
+    a.status = p->status.as<int>();
+    void *kp[] = {&a};
+    unsigned grid = (unsigned)((d.n_elem + d.epb - 1) / d.epb);
+    CUDA_TRY(cudaLaunchKernel((const void *)d.code->func, dim3(grid), dim3(d.threads), kp, (size_t)d.smem, st));
+  }
+  return FE_OK;
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------
+// C-ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char *fe_last_error(void) { return g_err.c_str(); }
+const char *fe_version(void) { return FE_VERSION; }
+
+int fe_device_info(int *sm_count, int *cc_major, int *cc_minor, size_t *free_bytes, size_t *total_bytes) {
+  int rc = ensure_context();
+  if (rc) return rc;
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (sm_count) CUDA_TRY(cudaDeviceGetAttribute(sm_count, cudaDevAttrMultiProcessorCount, dev));
+  if (cc_major) CUDA_TRY(cudaDeviceGetAttribute(cc_major, cudaDevAttrComputeCapabilityMajor, dev));
+  if (cc_minor) CUDA_TRY(cudaDeviceGetAttribute(cc_minor, cudaDevAttrComputeCapabilityMinor, dev));
+  size_t f = 0, t = 0;
+  CUDA_TRY(cudaMemGetInfo(&f, &t));
+  if (free_bytes) *free_bytes = f;
+  if (total_bytes) *total_bytes = t;
+  return FE_OK;
+}
+
+namespace {
+// nvrtc -> cubin (cached by source hash); no device needed.
+int build_cubin(const char *source, const char *kernel_name, const char *include_dir, const char *cache_dir,
+                std::string &cubin, char *log, size_t log_cap) {
+  if (log && log_cap) log[0] = 0;
+  const std::string arch = "--gpu-architecture=sm_103a";
+  std::string inc = std::string("--include-path=") + (include_dir ? include_dir : ".");
+  const std::string key_src = std::string(source) + "\n//" + kernel_name + arch + FE_VERSION;
+  char keyhex[32];
+  snprintf(keyhex, sizeof(keyhex), "%016llx", (unsigned long long)fnv1a(key_src));
+  std::string cache_path;
+  cubin.clear();
+  if (cache_dir && cache_dir[0]) {
+    cache_path = std::string(cache_dir) + "/" + kernel_name + "_" + keyhex + ".cubin";
+    read_file(cache_path, cubin);
+  }
+  if (!cubin.empty()) return FE_OK;
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, source, "fe_element.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+    return fail(FE_ERR_COMPILE, "nvrtcCreateProgram failed");
+  const char *opts[] = {arch.c_str(), inc.c_str(), "--std=c++17", "-default-device", "-lineinfo",
+                        "--fmad=true", "-DFE_NVRTC=1"};
+  nvrtcResult r = nvrtcCompileProgram(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+  size_t lsz = 0;
+  nvrtcGetProgramLogSize(prog, &lsz);
+  std::string lg(lsz, '\0');
+  if (lsz) nvrtcGetProgramLog(prog, &lg[0]);
+  if (log && log_cap) {
+    size_t n = std::min(log_cap - 1, lg.size());
+    memcpy(log, lg.data(), n);
+    log[n] = 0;
+  }
+  if (r != NVRTC_SUCCESS) {
+    nvrtcDestroyProgram(&prog);
+    return fail(FE_ERR_COMPILE, "nvrtc: %s\n%s", nvrtcGetErrorString(r), lg.substr(0, 800).c_str());
+  }
+  size_t csz = 0;
+  nvrtcGetCUBINSize(prog, &csz);
+  cubin.resize(csz);
+  nvrtcGetCUBIN(prog, &cubin[0]);
+  nvrtcDestroyProgram(&prog);
+  if (!cache_path.empty()) {
+    std::string tmp = cache_path + ".tmp" +
+                      std::to_string((unsigned long long)std::hash<std::thread::id>()(std::this_thread::get_id()));
+    std::ofstream f(tmp, std::ios::binary);
+    if (f) {
+      f.write(cubin.data(), (std::streamsize)cubin.size());
+      f.close();
+      std::rename(tmp.c_str(), cache_path.c_str());
+    }
+  }
+  return FE_OK;
+}
+} // namespace
+
+int fe_code_build(const char *source, const char *kernel_name, const char *include_dir, const char *cache_dir,
+                  size_t *cubin_bytes, char *log, size_t log_cap) {
+  if (!source || !kernel_name) return fail(FE_ERR_ARG, "fe_code_build: null argument");
+  std::string cubin;
+  int rc = build_cubin(source, kernel_name, include_dir, cache_dir, cubin, log, log_cap);
+  if (rc) return rc;
+  if (cubin_bytes) *cubin_bytes = cubin.size();
+  return FE_OK;
+}
+
+int fe_code_compile(const char *source, const char *kernel_name, const char *include_dir,
+                    const char *cache_dir, fe_code_t **out, char *log, size_t log_cap) {
+  if (!source || !kernel_name || !out) return fail(FE_ERR_ARG, "fe_code_compile: null argument");
+  *out = nullptr;
+  std::string cubin;
+  int rc = build_cubin(source, kernel_name, include_dir, cache_dir, cubin, log, log_cap);
+  if (rc) return rc;
+  rc = ensure_context();
+  if (rc) return rc;
+  std::unique_ptr<fe_code> c(new fe_code());
+  CUDA_TRY(cudaLibraryLoadData(&c->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
+  CUDA_TRY(cudaLibraryGetKernel(&c->func, c->lib, kernel_name));
+  c->name = kernel_name;
+  *out = c.release();
+  return FE_OK;
+}
+
+void fe_code_destroy(fe_code_t *code) { delete code; }
+
+int fe_problem_create(const fe_problem_desc_t *desc, fe_problem_t **out) {
+  if (!desc || !out) return fail(FE_ERR_ARG, "fe_problem_create: null argument");
+  *out = nullptr;
+  if (desc->dim < 1 || desc->dim > 3 || desc->nval < 1 || desc->n_nodes < 0 || desc->n_dof < 0 ||
+      desc->n_domains < 1 || !desc->domains || !desc->x || !desc->eqn)
+    return fail(FE_ERR_ARG, "fe_problem_create: bad sizes");
+  if (desc->jac_precision != FE_JAC_F64 && desc->jac_precision != FE_JAC_F32)
+    return fail(FE_ERR_ARG, "fe_problem_create: bad jac_precision %d", desc->jac_precision);
+  int rc = ensure_context();
+  if (rc) return rc;
+  std::unique_ptr<fe_problem> P(new fe_problem());
+  P->dim = desc->dim;
+  P->nval = desc->nval;
+  P->n_nodes = desc->n_nodes;
+  P->n_dof = desc->n_dof;
+  P->jac_prec = desc->jac_precision;
+  P->n_params = desc->n_params;
+  // equation numbers must be in range
+  for (long long k = 0; k < desc->n_nodes * desc->nval; k++)
+    if (desc->eqn[k] >= desc->n_dof) return fail(FE_ERR_ARG, "eqn[%lld]=%d >= n_dof", k, desc->eqn[k]);
+  std::vector<const int32_t *> conn_h;
+  long long jtot = 0, rtot = 0;
+  for (int di = 0; di < desc->n_domains; di++) {
+    const fe_domain_desc_t &dd = desc->domains[di];
+    if (!dd.code || dd.nnode_el < 1 || dd.nlocal < 1 || dd.n_elem < 0 || (!dd.conn && dd.n_elem) ||
+        !dd.local_node || !dd.local_val || dd.elems_per_block < 1 || dd.threads_per_block < 32 ||
+        dd.threads_per_block > 1024 || dd.smem_bytes < 0)
+      return fail(FE_ERR_ARG, "fe_problem_create: bad domain %d", di);
+    for (long long k = 0; k < dd.n_elem * dd.nnode_el; k++)
+      if (dd.conn[k] < 0 || dd.conn[k] >= desc->n_nodes)
+        return fail(FE_ERR_ARG, "domain %d: conn[%lld]=%d out of range", di, k, dd.conn[k]);
+    for (int k = 0; k < dd.nlocal; k++)
+      if (dd.local_node[k] < 0 || dd.local_node[k] >= dd.nnode_el || dd.local_val[k] < 0 ||
+          dd.local_val[k] >= desc->nval)
+        return fail(FE_ERR_ARG, "domain %d: bad local layout at %d", di, k);
+    Domain d;
+    d.code = dd.code;
+    d.nnode = dd.nnode_el;
+    d.nlocal = dd.nlocal;
+    d.n_elem = dd.n_elem;
+    d.epb = dd.elems_per_block;
+    d.threads = dd.threads_per_block;
+    d.smem = dd.smem_bytes;
+    d.local_node.assign(dd.local_node, dd.local_node + dd.nlocal);
+    d.local_val.assign(dd.local_val, dd.local_val + dd.nlocal);
+    d.jbase = jtot;
+    d.rbase = rtot;
+    jtot += dd.n_elem * (long long)dd.nlocal * dd.nlocal;
+    rtot += dd.n_elem * (long long)dd.nlocal;
+    if ((rc = d.conn.upload(dd.conn, sizeof(int32_t) * dd.n_elem * dd.nnode_el))) return rc;
+    if (dd.n_tables > 0 && (rc = d.tables.upload(dd.tables, sizeof(double) * dd.n_tables))) return rc;
+    if (d.smem > 48 * 1024)
+      CUDA_TRY(cudaFuncSetAttribute((const void *)d.code->func, cudaFuncAttributeMaxDynamicSharedMemorySize, d.smem));
+    conn_h.push_back(dd.conn);
+    P->domains.push_back(std::move(d));
+  }
+  if (jtot > 0xffffffffLL) return fail(FE_ERR_ARG, "element Jacobian space %lld exceeds 2^32 entries", jtot);
+  if ((rc = P->x.upload(desc->x, sizeof(double) * desc->n_nodes * desc->dim))) return rc;
+  if ((rc = P->eqn.upload(desc->eqn, sizeof(int32_t) * desc->n_nodes * desc->nval))) return rc;
+  if ((rc = P->values.alloc(sizeof(double) * desc->n_nodes * desc->nval))) return rc;
+  CUDA_TRY(cudaMemset(P->values.p, 0, P->values.bytes));
+  if ((rc = P->params.alloc(sizeof(double) * std::max(1, desc->n_params)))) return rc;
+  if (desc->n_params > 0)
+    CUDA_TRY(cudaMemcpy(P->params.p, desc->params, sizeof(double) * desc->n_params, cudaMemcpyHostToDevice));
+  if ((rc = P->status.alloc(sizeof(int) * 4))) return rc;
+  CUDA_TRY(cudaMemset(P->status.p, 0, P->status.bytes));
+  const size_t jel = P->jac_prec == FE_JAC_F64 ? sizeof(double) : sizeof(float);
+  if ((rc = P->jbuf_all.alloc(jel * std::max(1LL, jtot)))) return rc;
+  if ((rc = P->rbuf_all.alloc(sizeof(double) * std::max(1LL, rtot)))) return rc;
+  if ((rc = P->partial.alloc(sizeof(double) * 4096))) return rc;
+  if ((rc = build_pattern(P.get(), conn_h, desc->eqn))) return rc;
+  *out = P.release();
+  return FE_OK;
+}
+
+void fe_problem_destroy(fe_problem_t *p) { delete p; }
+
+int fe_problem_sizes(const fe_problem_t *p, int64_t *n_dof, int64_t *nnz) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  if (n_dof) *n_dof = p->n_dof;
+  if (nnz) *nnz = p->nnz;
+  return FE_OK;
+}
+
+int fe_problem_pattern(const fe_problem_t *p, int32_t *rowptr, int32_t *colidx) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  if (rowptr) memcpy(rowptr, p->h_rowptr.data(), sizeof(int32_t) * (p->n_dof + 1));
+  if (colidx) memcpy(colidx, p->h_colidx.data(), sizeof(int32_t) * p->nnz);
+  return FE_OK;
+}
+
+int fe_problem_pattern_device(const fe_problem_t *p, const int32_t **rowptr, const int32_t **colidx) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  if (rowptr) *rowptr = p->rowptr.as<int32_t>();
+  if (colidx) *colidx = p->colidx.as<int32_t>();
+  return FE_OK;
+}
+
+int fe_problem_set_values(fe_problem_t *p, const double *values_host) {
+  if (!p || !values_host) return fail(FE_ERR_ARG, "null argument");
+  CUDA_TRY(cudaMemcpy(p->values.p, values_host, p->values.bytes, cudaMemcpyHostToDevice));
+  return FE_OK;
+}
+
+int fe_problem_get_values(const fe_problem_t *p, double *values_host) {
+  if (!p || !values_host) return fail(FE_ERR_ARG, "null argument");
+  CUDA_TRY(cudaMemcpy(values_host, p->values.p, p->values.bytes, cudaMemcpyDeviceToHost));
+  return FE_OK;
+}
+
+int fe_problem_set_params(fe_problem_t *p, const double *params_host) {
+  if (!p || (!params_host && p->n_params)) return fail(FE_ERR_ARG, "null argument");
+  if (p->n_params)
+    CUDA_TRY(cudaMemcpy(p->params.p, params_host, sizeof(double) * p->n_params, cudaMemcpyHostToDevice));
+  return FE_OK;
+}
+
+int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags, void *stream) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  cudaStream_t st = (cudaStream_t)stream;
+  const bool want_r = flags & FE_ASSEMBLE_RESIDUAL, want_j = flags & FE_ASSEMBLE_JACOBIAN;
+  if ((want_r && !R) || (want_j && !J_vals)) return fail(FE_ERR_ARG, "fe_assemble: missing output");
+  const int sms = sm_count_cached();
+  std::vector<cudaEvent_t> ev;
+  if (p->timing) {
+    ev.resize(5);
+    for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
+    CUDA_TRY(cudaEventRecord(ev[0], st));
+  }
+  if (flags & FE_ASSEMBLE_VALUES_FROM_DOFS) {
+    if (!dofs) return fail(FE_ERR_ARG, "fe_assemble: missing dofs");
+    long long n = p->n_nodes * p->nval;
+    k_scatter_dofs<<<grid_for(n, 256, sms), 256, 0, st>>>(dofs, p->eqn.as<int>(), p->values.as<double>(), n);
+    CUDA_TRY(cudaGetLastError());
+  }
+  if (p->timing) CUDA_TRY(cudaEventRecord(ev[1], st));
+  int rc = launch_elements(p, want_j ? 1 : 0, st);
+  if (rc) return rc;
+  if (p->timing) CUDA_TRY(cudaEventRecord(ev[2], st));
+  if (want_r) {
+    k_gather_rows<<<grid_for(p->n_dof, 256, sms), 256, 0, st>>>(p->rptr.as<long long>(), p->ridx.as<unsigned>(),
+                                                               p->rbuf_all.as<double>(), R, p->n_dof);
+    CUDA_TRY(cudaGetLastError());
+  }
+  if (p->timing) CUDA_TRY(cudaEventRecord(ev[3], st));
+  if (want_j && p->nnz > 0) {
+    if (p->jac_prec == FE_JAC_F64)
+      k_gather_slots<double><<<grid_for(p->nnz, 256, sms), 256, 0, st>>>(
+          p->cptr.as<long long>(), p->cidx.as<unsigned>(), p->jbuf_all.as<double>(), (double *)J_vals, p->nnz);
+    else
+      k_gather_slots<float><<<grid_for(p->nnz, 256, sms), 256, 0, st>>>(
+          p->cptr.as<long long>(), p->cidx.as<unsigned>(), p->jbuf_all.as<float>(), (float *)J_vals, p->nnz);
+    CUDA_TRY(cudaGetLastError());
+  }
+  if (p->timing) {
+    CUDA_TRY(cudaEventRecord(ev[4], st));
+    p->pending.push_back(ev);
+  }
+  return FE_OK;
+}
+
+int fe_problem_set_timing(fe_problem_t *p, int enable) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  p->timing = enable != 0;
+  return FE_OK;
+}
+
+int fe_problem_stage_times(fe_problem_t *p, double *ms, int64_t *calls) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  for (auto &v : p->pending) {
+    CUDA_TRY(cudaEventSynchronize(v[4]));
+    for (int k = 0; k < 4; k++) {
+      float t = 0.f;
+      CUDA_TRY(cudaEventElapsedTime(&t, v[k], v[k + 1]));
+      p->stage_ms[k] += t;
+    }
+    for (auto e : v) cudaEventDestroy(e);
+    p->stage_calls++;
+  }
+  p->pending.clear();
+  if (ms)
+    for (int k = 0; k < 4; k++) ms[k] = p->stage_ms[k];
+  if (calls) *calls = p->stage_calls;
+  for (int k = 0; k < 4; k++) p->stage_ms[k] = 0;
+  p->stage_calls = 0;
+  return FE_OK;
+}
+
+int fe_assemble_host(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  DevBuf d_dofs, d_R, d_J;
+  int rc;
+  const size_t jel = p->jac_prec == FE_JAC_F64 ? sizeof(double) : sizeof(float);
+  if (flags & FE_ASSEMBLE_VALUES_FROM_DOFS) {
+    if (!dofs) return fail(FE_ERR_ARG, "missing dofs");
+    if ((rc = d_dofs.upload(dofs, sizeof(double) * p->n_dof))) return rc;
+  }
+  if ((flags & FE_ASSEMBLE_RESIDUAL) && (rc = d_R.alloc(sizeof(double) * std::max(1LL, p->n_dof)))) return rc;
+  if ((flags & FE_ASSEMBLE_JACOBIAN) && (rc = d_J.alloc(jel * std::max(1LL, p->nnz)))) return rc;
+  if ((rc = fe_assemble(p, d_dofs.as<double>(), d_R.as<double>(), d_J.p, flags, nullptr))) return rc;
+  if ((rc = fe_problem_check(p))) return rc;
+  if (flags & FE_ASSEMBLE_RESIDUAL) CUDA_TRY(cudaMemcpy(R, d_R.p, sizeof(double) * p->n_dof, cudaMemcpyDeviceToHost));
+  if (flags & FE_ASSEMBLE_JACOBIAN) CUDA_TRY(cudaMemcpy(J_vals, d_J.p, jel * p->nnz, cudaMemcpyDeviceToHost));
+  return FE_OK;
+}
+
+int fe_residual_max(fe_problem_t *p, const double *R, int64_t n, double *out, void *stream) {
+  if (!p || !out || (n > 0 && !R)) return fail(FE_ERR_ARG, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n <= 0) {
+    *out = 0.0;
+    return FE_OK;
+  }
+  const int sms = sm_count_cached();
+  int g = std::min(grid_for(n, 256, sms), 4000);
+  k_absmax_partial<<<g, 256, 0, st>>>(R, n, p->partial.as<double>());
+  k_absmax_partial<<<1, 1024, 0, st>>>(p->partial.as<double>(), g, p->partial.as<double>() + 4095);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(out, p->partial.as<double>() + 4095, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return FE_OK;
+}
+
+int fe_dof_update(fe_problem_t *p, double *x, const double *dx, int64_t n, void *stream) {
+  if (!p || (n > 0 && (!x || !dx))) return fail(FE_ERR_ARG, "null argument");
+  if (n <= 0) return FE_OK;
+  k_dof_update<<<grid_for(n, 256, sm_count_cached()), 256, 0, (cudaStream_t)stream>>>(x, dx, n);
+  CUDA_TRY(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_problem_check(fe_problem_t *p) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  CUDA_TRY(cudaDeviceSynchronize());
+  int st[4] = {0, 0, 0, 0};
+  CUDA_TRY(cudaMemcpy(st, p->status.p, sizeof(st), cudaMemcpyDeviceToHost));
+  if (st[0]) return fail(FE_ERR_DEVICE, "element kernel status %d (detail %d %d %d)", st[0], st[1], st[2], st[3]);
+  return FE_OK;
+}
+
+int fe_problem_launch_count(const fe_problem_t *p, int flags) {
+  if (!p) return -1;
+  int n = 0;
+  if (flags & FE_ASSEMBLE_VALUES_FROM_DOFS) n++;
+  for (const Domain &d : p->domains)
+    if (d.n_elem) n++;
+  if (flags & FE_ASSEMBLE_RESIDUAL) n++;
+  if ((flags & FE_ASSEMBLE_JACOBIAN) && p->nnz > 0) n++;
+  return n;
+}
+
+} // extern "C"

@@ -1,0 +1,213 @@
+"""Weak-form expression language, mirroring the names of pyoomph's
+``pyoomph.expressions`` (``generic.py``: ``var`` :137, ``grad`` :355,
+``weak`` :394, ``testfunction`` :647, ``material_derivative`` :564;
+``__init__.py:453`` ``var_and_test``) on top of sympy.
+
+A field value at an integration point is a sympy symbol; its spatial
+gradient is a vector of symbols.  ``weak(a, b)`` is the integrand
+``a : b`` times the coordinate-system measure (``2*pi*r`` for the
+axisymmetric system, ``expressions/coordsys.py:428-432``).  The code
+generator differentiates the summed integrand with respect to the test
+and trial components to obtain the pointwise residual coefficients and
+their Jacobian -- the role GiNaC plays in the reference.
+"""
+from __future__ import annotations
+
+from typing import Dict, List, Sequence, Tuple, Union
+
+import sympy as sp
+
+Expr = Union[sp.Expr, sp.MatrixBase, float, int]
+
+# coordinate symbols x0, x1, x2 (Eulerian position at the integration point)
+X = sp.symbols("x0:3", real=True)
+
+
+class _Registry:
+    """Symbols of the fields, their gradients and test functions."""
+
+    def __init__(self):
+        self.value: Dict[str, sp.Symbol] = {}
+        self.grad: Dict[str, Tuple[sp.Symbol, ...]] = {}
+        self.test: Dict[str, sp.Symbol] = {}
+        self.test_grad: Dict[str, Tuple[sp.Symbol, ...]] = {}
+        self.params: Dict[str, sp.Symbol] = {}
+        self.vector_fields: Dict[str, List[str]] = {}
+
+    def field(self, name: str):
+        if name not in self.value:
+            self.value[name] = sp.Symbol(f"U_{name}", real=True)
+            self.grad[name] = tuple(sp.Symbol(f"U_{name}__x{i}", real=True) for i in range(3))
+            self.test[name] = sp.Symbol(f"T_{name}", real=True)
+            self.test_grad[name] = tuple(sp.Symbol(f"T_{name}__x{i}", real=True) for i in range(3))
+        return self.value[name]
+
+
+REG = _Registry()
+_DIM = [2]
+
+
+def set_dimension(dim: int) -> None:
+    _DIM[0] = dim
+
+
+def dimension() -> int:
+    return _DIM[0]
+
+
+def register_vector_field(name: str, comps: List[str]) -> None:
+    REG.vector_fields[name] = comps
+
+
+def var(name: str) -> Expr:
+    """Field value (scalar symbol, or a column vector for a vector field)."""
+    if name in REG.vector_fields:
+        return sp.Matrix([REG.field(c) for c in REG.vector_fields[name]])
+    if name == "coordinate":
+        return sp.Matrix(X[:dimension()])
+    if name.startswith("coordinate_"):
+        return X["xyz".index(name[-1])]
+    return REG.field(name)
+
+
+def testfunction(name: str) -> Expr:
+    if name in REG.vector_fields:
+        comps = REG.vector_fields[name]
+        for c in comps:
+            REG.field(c)
+        return sp.Matrix([REG.test[c] for c in comps])
+    REG.field(name)
+    return REG.test[name]
+
+
+def var_and_test(name: str):
+    return var(name), testfunction(name)
+
+
+def parameter(name: str) -> sp.Symbol:
+    """A global parameter (read from the parameter array at run time)."""
+    if name not in REG.params:
+        REG.params[name] = sp.Symbol(f"P_{name}", real=True)
+    return REG.params[name]
+
+
+def _d_dx(e: sp.Expr, i: int) -> sp.Expr:
+    """d/dx_i of a pointwise expression by the chain rule through the
+    field symbols (value -> gradient component) and the coordinates."""
+    e = sp.sympify(e)
+    out = sp.Integer(0)
+    for s in e.free_symbols:
+        de = sp.diff(e, s)
+        if de == 0:
+            continue
+        nm = s.name
+        if nm.startswith("U_") and "__x" not in nm:
+            out += de * REG.grad[nm[2:]][i]
+        elif nm.startswith("T_") and "__x" not in nm:
+            out += de * REG.test_grad[nm[2:]][i]
+        elif s in X:
+            out += de * (1 if X.index(s) == i else 0)
+        elif nm.startswith("P_"):
+            continue
+        else:
+            raise NotImplementedError(f"second derivatives of {nm} are not supported")
+    return out
+
+
+def grad(e: Expr) -> Expr:
+    """Gradient.  Scalar -> column vector g_i = d e/dx_i; vector u ->
+    matrix G[i, j] = d u_j / d x_i (pyoomph's convention)."""
+    d = dimension()
+    if isinstance(e, sp.MatrixBase):
+        return sp.Matrix(d, e.shape[0], lambda i, j: _d_dx(e[j], i))
+    return sp.Matrix([_d_dx(e, i) for i in range(d)])
+
+
+def div(u: Expr) -> sp.Expr:
+    d = dimension()
+    return sum(_d_dx(u[i], i) for i in range(d))
+
+
+def transpose(A: sp.MatrixBase) -> sp.MatrixBase:
+    return A.T
+
+
+def sym(A: sp.MatrixBase) -> sp.MatrixBase:
+    return (A + A.T) / 2
+
+
+def identity_matrix() -> sp.MatrixBase:
+    return sp.eye(dimension())
+
+
+def dot(a: Expr, b: Expr) -> Expr:
+    """Contraction of the last index of a with the first of b."""
+    if isinstance(a, sp.MatrixBase) and isinstance(b, sp.MatrixBase):
+        if a.shape[1] == 1 and b.shape[1] == 1:
+            return (a.T * b)[0, 0]
+        if a.shape[1] == 1:  # vector . matrix
+            return (a.T * b).T
+        return a * b
+    return a * b
+
+
+def material_derivative(f: Expr, velocity: Expr) -> Expr:
+    """Steady part of the material derivative, (u . grad) f (the partial_t
+    term of generic.py:564 vanishes for the stationary solves here)."""
+    return dot(velocity, grad(f))
+
+
+class CoordinateSystem:
+    def measure(self) -> sp.Expr:
+        return sp.Integer(1)
+
+
+class CartesianCoordinateSystem(CoordinateSystem):
+    pass
+
+
+class AxisymmetricCoordinateSystem(CoordinateSystem):
+    """dx = 2*pi*r dr dz with r = x0 (coordsys.py:428-432)."""
+
+    def measure(self) -> sp.Expr:
+        return 2 * sp.pi * X[0]
+
+
+_COORDSYS = [CartesianCoordinateSystem()]
+
+
+def set_coordinate_system(cs: CoordinateSystem) -> None:
+    _COORDSYS[0] = cs
+
+
+def weak(a: Expr, b: Expr, coordinate_system: CoordinateSystem = None) -> sp.Expr:
+    """Integrand a : b (full contraction) times the measure."""
+    cs = coordinate_system or _COORDSYS[0]
+    if isinstance(a, sp.MatrixBase) or isinstance(b, sp.MatrixBase):
+        A = sp.Matrix(a)
+        B = sp.Matrix(b)
+        if A.shape != B.shape:
+            raise ValueError(f"weak: shape mismatch {A.shape} vs {B.shape}")
+        prod = sum(A[i] * B[i] for i in range(len(A)))
+    else:
+        prod = sp.sympify(a) * sp.sympify(b)
+    return prod * cs.measure()
+
+
+def exp(e: Expr) -> sp.Expr:
+    return sp.exp(e)
+
+
+def square_mag(v: Sequence) -> sp.Expr:
+    return sum(c * c for c in v)
+
+
+def gaussian_source(n: int, dim: int, prefix: str = "g") -> sp.Expr:
+    """sum_k A_k exp(-|x - c_k|^2 / (2 w_k^2)) with the centres, widths and
+    amplitudes as global parameters ``{prefix}{k}_c{i}``, ``_w``, ``_A``."""
+    f = sp.Integer(0)
+    for k in range(n):
+        r2 = sum((X[i] - parameter(f"{prefix}{k}_c{i}")) ** 2 for i in range(dim))
+        w = parameter(f"{prefix}{k}_w")
+        f += parameter(f"{prefix}{k}_A") * sp.exp(-r2 / (2 * w * w))
+    return f

@@ -1,0 +1,219 @@
+"""Structured mesh templates in pyoomph's node and element order.
+
+The order of nodes fixes the equation numbering and therefore the CSR
+pattern, so it must match the reference exactly:
+
+* ``RectangularQuadMesh.define_geometry`` (``pyoomph/meshes/simplemeshes.py:225-305``)
+  visits cells with ``ix`` outer and ``iy`` inner and adds the corner nodes
+  n00, n10, n01, n11 through ``add_node_unique`` (deduplication by position,
+  ``src/meshtemplate.cpp:1378``); split cells give the triangles
+  ``(n00,n10,n11),(n00,n11,n01)`` ("left") or ``(n01,n10,n11),(n00,n10,n01)``
+  ("right");
+* ``CuboidBrickMesh`` (``simplemeshes.py:515-545``) visits ``ix, iy, iz`` and
+  adds the corners in the order 000,100,010,110,001,101,011,111;
+* the conversion to the quadratic space then appends, element by element,
+  the midside/face/centre nodes in the call order of
+  ``convert_for_C2_space`` (``meshtemplate.cpp:401-409`` quad,
+  ``:494-499`` triangle, ``:579-621`` brick);
+* the mesh keeps template-index order (``src/mesh2d.hpp:265-300``).
+
+Every node sits on a half-cell lattice, so the generator computes the
+sequence of lattice keys in the reference's insertion order and numbers
+each key at its first occurrence, all in vectorised numpy.  A node's
+position is the one computed at its first insertion, with the reference's
+arithmetic (``0.5*(a+b)``, ``0.25*(a+b+c+d)``).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Union
+
+import numpy as np
+
+from .spaces import ELEMENT_TYPES, ElementType
+
+
+@dataclass
+class MeshData:
+    etype: ElementType
+    x: np.ndarray                # [n_nodes, dim]
+    conn: np.ndarray             # [n_elem, nnode] int32
+    is_vertex: np.ndarray        # [n_nodes] bool (C1 nodes)
+    boundaries: Dict[str, np.ndarray] = field(default_factory=dict)  # name -> bool mask over nodes
+    lattice: Optional[np.ndarray] = None  # [n_nodes, dim] int64 half-cell coordinates
+
+    @property
+    def n_nodes(self) -> int:
+        return self.x.shape[0]
+
+    @property
+    def n_elem(self) -> int:
+        return self.conn.shape[0]
+
+    @property
+    def dim(self) -> int:
+        return self.etype.dim
+
+
+def _number_first_touch(keys: np.ndarray):
+    """Node ids by order of first occurrence of each key."""
+    uniq, first, inv = np.unique(keys, return_index=True, return_inverse=True)
+    order = np.argsort(first, kind="stable")
+    rank = np.empty_like(order)
+    rank[order] = np.arange(len(order))
+    return rank[inv], first[order], len(uniq)
+
+
+class MeshTemplate:
+    domain_name = "domain"
+
+    def generate(self) -> MeshData:  # pragma: no cover - abstract
+        raise NotImplementedError
+
+
+class RectangularQuadMesh(MeshTemplate):
+    """Unit-square-style rectangle of Q2 quads, or of P2 triangles with
+    ``split_in_tris="left"|"right"``."""
+
+    def __init__(self, *, N: Union[int, List[int]] = 10, size: Union[float, List[float]] = 1.0,
+                 lower_left: Union[float, List[float]] = 0.0, split_in_tris: Union[bool, str] = False,
+                 name: str = "domain"):
+        self.N = [N, N] if isinstance(N, int) else list(N)
+        self.size = [size, size] if isinstance(size, (int, float)) else list(size)
+        self.lower_left = [lower_left, lower_left] if isinstance(lower_left, (int, float)) else list(lower_left)
+        if split_in_tris not in (False, "left", "right"):
+            raise ValueError("split_in_tris must be False, 'left' or 'right'")
+        self.split = split_in_tris
+        self.domain_name = name
+
+    def generate(self) -> MeshData:
+        nx, ny = self.N
+        lx, ly = self.size
+        x0, y0 = self.lower_left
+        LX = 2 * nx + 1
+        ix, iy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+        ix = ix.ravel().astype(np.int64)
+        iy = iy.ravel().astype(np.int64)  # cells in (ix outer, iy inner) order
+        corners = [(0, 0), (2, 0), (0, 2), (2, 2)]  # n00, n10, n01, n11
+        lat_c = np.stack([np.stack([2 * ix + a, 2 * iy + b], axis=1) for a, b in corners], axis=1)  # [cells,4,2]
+
+        def pos_vertex(lat):
+            # (ix * size) / N + lower_left, as the template computes it
+            return np.stack([(lat[..., 0] // 2) * lx / nx + x0, (lat[..., 1] // 2) * ly / ny + y0], axis=-1)
+
+        pc = pos_vertex(lat_c)
+        if not self.split:
+            et = ELEMENT_TYPES["Q2_QUAD"]
+            # C2 additions per element: n1=mid(0,1), n3=mid(0,2), n4=centre, n5=mid(1,3), n7=mid(2,3)
+            mids = [(0, 1), (0, 2), None, (1, 3), (2, 3)]
+            lat_m, pos_m = [], []
+            for m in mids:
+                if m is None:
+                    lat_m.append((lat_c[:, 0] + lat_c[:, 3]) // 2)
+                    pos_m.append(0.25 * (pc[:, 0] + pc[:, 1] + pc[:, 2] + pc[:, 3]))
+                else:
+                    a, b = m
+                    lat_m.append((lat_c[:, a] + lat_c[:, b]) // 2)
+                    pos_m.append(0.5 * (pc[:, a] + pc[:, b]))
+            lat_m = np.stack(lat_m, axis=1)
+            pos_m = np.stack(pos_m, axis=1)
+            # element slots: (n00, n1, n10, n3, n4, n5, n01, n7, n11)
+            slot_lat = np.stack([lat_c[:, 0], lat_m[:, 0], lat_c[:, 1], lat_m[:, 1], lat_m[:, 2], lat_m[:, 3],
+                                 lat_c[:, 2], lat_m[:, 4], lat_c[:, 3]], axis=1)
+            touch_lat = np.concatenate([lat_c.reshape(-1, 2), lat_m.reshape(-1, 2)])
+            touch_pos = np.concatenate([pc.reshape(-1, 2), pos_m.reshape(-1, 2)])
+        else:
+            et = ELEMENT_TYPES["P2_TRI"]
+            if self.split == "left":
+                tris = [(0, 1, 3), (0, 3, 2)]
+            else:
+                tris = [(2, 1, 3), (0, 1, 2)]
+            vlat = np.stack([np.stack([lat_c[:, a], lat_c[:, b], lat_c[:, c]], axis=1) for a, b, c in tris],
+                            axis=1).reshape(-1, 3, 2)  # [2*cells, 3, 2], element order
+            vpos = np.stack([np.stack([pc[:, a], pc[:, b], pc[:, c]], axis=1) for a, b, c in tris],
+                            axis=1).reshape(-1, 3, 2)
+            pairs = [(0, 1), (1, 2), (0, 2)]
+            lat_m = np.stack([(vlat[:, a] + vlat[:, b]) // 2 for a, b in pairs], axis=1)
+            pos_m = np.stack([0.5 * (vpos[:, a] + vpos[:, b]) for a, b in pairs], axis=1)
+            slot_lat = np.concatenate([vlat, lat_m], axis=1)
+            touch_lat = np.concatenate([lat_c.reshape(-1, 2), lat_m.reshape(-1, 2)])
+            touch_pos = np.concatenate([pc.reshape(-1, 2), pos_m.reshape(-1, 2)])
+        key = lambda lat: lat[..., 0] + LX * lat[..., 1]
+        ids, first, n_nodes = _number_first_touch(key(touch_lat))
+        x = touch_pos[first]
+        lat = touch_lat[first]
+        # element connectivity through the same numbering
+        uniq_keys = key(lat)
+        lut = np.full(LX * (2 * ny + 1), -1, dtype=np.int64)
+        lut[uniq_keys] = np.arange(n_nodes)
+        conn = lut[key(slot_lat)].astype(np.int32)
+        is_vertex = (lat[:, 0] % 2 == 0) & (lat[:, 1] % 2 == 0)
+        b = {"left": lat[:, 0] == 0, "right": lat[:, 0] == 2 * nx,
+             "bottom": lat[:, 1] == 0, "top": lat[:, 1] == 2 * ny}
+        return MeshData(et, x, conn, is_vertex, b, lat)
+
+
+_HEX_C2_ORDER = [1, 3, 4, 5, 7, 9, 11, 15, 17, 19, 21, 22, 23, 25, 10, 12, 14, 16, 13]
+
+
+class CuboidBrickMesh(MeshTemplate):
+    """Box of Q2 hexahedra (27 nodes each)."""
+
+    def __init__(self, *, N: Union[int, List[int]] = 10, size: Union[float, List[float]] = 1.0,
+                 lower_left: Union[float, List[float]] = 0.0, domain_name: str = "domain"):
+        self.N = [N, N, N] if isinstance(N, int) else list(N)
+        self.size = [size] * 3 if isinstance(size, (int, float)) else list(size)
+        self.lower_left = [lower_left] * 3 if isinstance(lower_left, (int, float)) else list(lower_left)
+        self.domain_name = domain_name
+
+    def generate(self) -> MeshData:
+        nx, ny, nz = self.N
+        L = self.size
+        ll = self.lower_left
+        LX, LY = 2 * nx + 1, 2 * ny + 1
+        g = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+        cell = [a.ravel().astype(np.int64) for a in g]  # (ix, iy, iz) with iz fastest
+        ncell = cell[0].size
+        # corner c = px + 2 py + 4 pz at element slot (2px, 2py, 2pz)
+        slot_ijk = np.array([[s % 3, (s // 3) % 3, s // 9] for s in range(27)])
+        corner_slots = [0, 2, 6, 8, 18, 20, 24, 26]
+        lat = np.zeros((ncell, 27, 3), dtype=np.int64)
+        for d in range(3):
+            lat[:, :, d] = 2 * cell[d][:, None] + slot_ijk[None, :, d]
+        P = np.zeros((ncell, 27, 3))
+        nn = [nx, ny, nz]
+        for s in corner_slots:
+            for d in range(3):
+                P[:, s, d] = (lat[:, s, d] // 2) * L[d] / nn[d] + ll[d]
+        # positions of the C2 nodes, in the reference's arithmetic
+        two = {1: (0, 2), 3: (0, 6), 5: (2, 8), 7: (6, 8), 9: (0, 18), 11: (2, 20), 15: (6, 24), 17: (8, 26),
+               19: (18, 20), 21: (18, 24), 23: (20, 26), 25: (24, 26), 10: (9, 11), 12: (9, 15), 14: (11, 17),
+               16: (15, 17)}
+        four = {4: (0, 2, 6, 8), 22: (18, 20, 24, 26), 13: (0, 8, 20, 24)}
+        for s in _HEX_C2_ORDER:
+            if s in two:
+                a, b = two[s]
+                P[:, s] = 0.5 * (P[:, a] + P[:, b])
+            else:
+                a, b, c, d = four[s]
+                P[:, s] = 0.25 * (P[:, a] + P[:, b] + P[:, c] + P[:, d])
+        touch_slots = corner_slots + _HEX_C2_ORDER
+        # vertex touches come first (all cells), then the C2 additions (all elements)
+        v_lat = lat[:, corner_slots].reshape(-1, 3)
+        v_pos = P[:, corner_slots].reshape(-1, 3)
+        m_lat = lat[:, _HEX_C2_ORDER].reshape(-1, 3)
+        m_pos = P[:, _HEX_C2_ORDER].reshape(-1, 3)
+        touch_lat = np.concatenate([v_lat, m_lat])
+        touch_pos = np.concatenate([v_pos, m_pos])
+        key = lambda q: q[..., 0] + LX * (q[..., 1] + LY * q[..., 2])
+        ids, first, n_nodes = _number_first_touch(key(touch_lat))
+        x = touch_pos[first]
+        nlat = touch_lat[first]
+        lut = np.full(LX * LY * (2 * nz + 1), -1, dtype=np.int64)
+        lut[key(nlat)] = np.arange(n_nodes)
+        conn = lut[key(lat)].astype(np.int32)
+        is_vertex = np.all(nlat % 2 == 0, axis=1)
+        b = {"left": nlat[:, 0] == 0, "right": nlat[:, 0] == 2 * nx, "bottom": nlat[:, 1] == 0,
+             "top": nlat[:, 1] == 2 * ny, "back": nlat[:, 2] == 0, "front": nlat[:, 2] == 2 * nz}
+        del touch_slots
+        return MeshData(ELEMENT_TYPES["Q2_HEX"], x, conn, is_vertex, b, nlat)

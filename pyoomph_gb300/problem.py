@@ -1,0 +1,398 @@
+"""Problem: the drop-in counterpart of pyoomph's ``Problem`` for the
+residual/Jacobian path (``pyoomph/generic/problem.py``: ``Problem`` :343,
+``initialise`` :2430, ``assemble_jacobian`` :711, ``solve`` :4721; Newton
+defaults :409-411).
+
+``initialise`` generates the meshes, numbers the equations
+(oomph ``Mesh::assign_global_eqn_numbers``, ``mesh.cc:686-708``: nodes in
+order, values in order, pinned values skipped), lowers the weak form to a
+CUDA element kernel (``codegen.generate_kernel``), JIT-compiles it for
+sm_103a and creates the resident device problem through the C-ABI.
+
+``solve`` is ``Problem::newton_solve`` (``problem.cc:8986-9300``): residual
+max-norm (NaN -> inf), stop below ``newton_solver_tolerance``, otherwise
+assemble R and J on the GPU, solve J dx = R (SuperLU through scipy, the
+reference's default serial solver, or a caller-supplied solver), x -= dx.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+from dataclasses import dataclass
+from typing import Callable, Dict, List, Optional, Tuple
+
+import numpy as np
+
+from . import _native as N
+from . import expressions as E
+from .codegen import KernelSpec, Pointwise, differentiate, generate_kernel
+from .equations import (SPACE_ORDER, BoundaryCondition, DirichletBC, EquationPart, Equations,
+                        PressureFixation, flatten)
+from .meshes import MeshData, MeshTemplate
+
+
+class NewtonSolverError(RuntimeError):
+    """Raised when Newton diverges or exceeds its iteration cap
+    (oomph's NewtonSolverError, problem.cc:9298)."""
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise N.FeError(N.FE_ERR_NOGPU, "pyoomph_gb300 needs a CUDA GPU (none visible)")
+    return torch
+
+
+@dataclass
+class AssemblyStats:
+    n_elem: int
+    n_dof: int
+    nnz: int
+    n_contrib: int
+
+
+class Problem:
+    def __init__(self):
+        self._meshes: List[MeshTemplate] = []
+        self._equations: List[EquationPart] = []
+        self.max_residuals = 1e10
+        self.max_newton_iterations = 10
+        self.newton_solver_tolerance = 1e-8
+        self.jacobian_precision = "fp64"   # or "fp32": FP32 Jacobian, FP64 residual
+        self.elems_per_block: Optional[int] = None
+        self.linear_solver: Optional[Callable] = None
+        self.verbose = False
+        self._initialised = False
+        self.newton_history: List[float] = []
+        self.timings: Dict[str, float] = {}
+
+    # -- building ------------------------------------------------------
+    def add_mesh(self, mesh: MeshTemplate) -> None:
+        if len(self._meshes) >= 1:
+            raise NotImplementedError("one bulk domain per problem")
+        self._meshes.append(mesh)
+
+    def add_equations(self, eqs: EquationPart) -> None:
+        self._equations.append(eqs)
+
+    def __iadd__(self, other):
+        if isinstance(other, MeshTemplate):
+            self.add_mesh(other)
+        elif isinstance(other, EquationPart):
+            self.add_equations(other)
+        else:
+            raise TypeError(f"cannot add {type(other).__name__} to a Problem")
+        return self
+
+    # -- initialise ----------------------------------------------------
+    def lower(self) -> KernelSpec:
+        """Generate the mesh and the element kernel source (no GPU needed):
+        fields in nodal-value order, the summed weak form, its pointwise
+        derivatives and the CUDA kernel (codegen.generate_kernel)."""
+        if getattr(self, "kernel", None) is not None:
+            return self.kernel
+        t0 = time.perf_counter()
+        if not self._meshes:
+            raise RuntimeError("no mesh added")
+        tmpl = self._meshes[0]
+        mesh = tmpl.generate()
+        self.mesh: MeshData = mesh
+        E.set_dimension(mesh.dim)
+        bulk: List[Equations] = []
+        bcs: List[Tuple[BoundaryCondition, Optional[List[str]]]] = []
+        for eq in self._equations:
+            for part, where in flatten(eq):
+                if isinstance(part, Equations):
+                    bulk.append(part)
+                elif isinstance(part, BoundaryCondition):
+                    bcs.append((part, where))
+                else:
+                    raise TypeError(type(part).__name__)
+        if not bulk:
+            raise RuntimeError("no bulk equations")
+        self._bcs = bcs
+        fields: List[Tuple[str, str]] = []
+        integrand = 0
+        params: Dict[str, float] = {}
+        for b in bulk:
+            b._fields, b._residual = [], 0
+            b.define_fields()
+            fields += b._fields
+        for b in bulk:
+            b.define_residuals()
+            integrand = integrand + b._residual
+            params.update(b.parameter_values())
+        # nodal value order: by space (C2TB, C2, C1TB, C1), then definition order
+        # (codegen.cpp:2367-2380, 2795-2810)
+        order = sorted(range(len(fields)), key=lambda i: (SPACE_ORDER[fields[i][1]], i))
+        fields = [fields[i] for i in order]
+        self.fields = fields
+        self.field_index = {n: i for i, (n, _) in enumerate(fields)}
+        # parameters referenced by the integrand, in a stable order
+        used = sorted({s.name[2:] for s in (integrand.free_symbols if hasattr(integrand, "free_symbols") else [])
+                       if s.name.startswith("P_")})
+        missing = [p for p in used if p not in params]
+        if missing:
+            raise RuntimeError(f"parameters without values: {missing}")
+        self.param_names = used
+        self.params = np.array([params[p] for p in used], dtype=np.float64)
+        t1 = time.perf_counter()
+        pw = differentiate(fields, mesh.dim, integrand, used)
+        prec = "f64" if self.jacobian_precision in ("fp64", "f64", "double") else "f32"
+        self._prec = prec
+        self.kernel: KernelSpec = generate_kernel(mesh.etype, pw, prec, epb=self.elems_per_block)
+        self.timings.update(setup_mesh_s=t1 - t0, codegen_s=time.perf_counter() - t1)
+        return self.kernel
+
+    def initialise(self) -> None:
+        if self._initialised:
+            return
+        torch = _torch()
+        self.lower()
+        mesh, fields, bcs, prec = self.mesh, self.fields, self._bcs, self._prec
+        t2 = time.perf_counter()
+        self.code = N.Code(self.kernel.source, self.kernel.name)
+        t3 = time.perf_counter()
+        # nodal values, pins and equation numbers
+        nval = len(fields)
+        n = mesh.n_nodes
+        present = np.zeros((n, nval), dtype=bool)
+        for f, (_, sp_) in enumerate(fields):
+            present[:, f] = True if sp_ == "C2" else mesh.is_vertex
+        pinned = np.zeros((n, nval), dtype=bool)
+        values = np.zeros((n, nval))
+        for bc, where in bcs:
+            if isinstance(bc, DirichletBC):
+                if where is None:
+                    raise RuntimeError("DirichletBC needs a boundary: DirichletBC(...) @ 'left'")
+                mask = np.zeros(n, dtype=bool)
+                for w in where:
+                    if w not in mesh.boundaries:
+                        raise KeyError(f"unknown boundary {w!r}; have {list(mesh.boundaries)}")
+                    mask |= mesh.boundaries[w]
+                for name, val in bc.values.items():
+                    names = E.REG.vector_fields.get(name, [name])
+                    for k, fname in enumerate(names):
+                        f = self.field_index[fname]
+                        m = mask & present[:, f]
+                        pinned[m, f] = True
+                        if callable(val):
+                            v = val(*[mesh.x[m, d] for d in range(mesh.dim)])
+                            v = v[k] if isinstance(v, (tuple, list)) and len(names) > 1 else v
+                            values[m, f] = v
+                        elif val is not None:
+                            vv = val[k] if isinstance(val, (tuple, list)) else val
+                            values[m, f] = vv
+            elif isinstance(bc, PressureFixation):
+                f = self.field_index[bc.name]
+                node0 = int(mesh.conn[0, 0])
+                pinned[node0, f] = True
+                if bc.value is not None:
+                    values[node0, f] = bc.value
+        free = present & ~pinned
+        eqn = np.full((n, nval), -1, dtype=np.int32)
+        flat = free.reshape(-1)
+        self.n_dof = int(flat.sum())
+        eqn.reshape(-1)[flat] = np.arange(self.n_dof, dtype=np.int32)
+        self.eqn = eqn
+        self.present = present
+        self.pinned = pinned
+        self._values0 = values
+        # device problem
+        L = N.load()
+        lay = self.kernel.layout
+        self._keep = dict(
+            conn=np.ascontiguousarray(mesh.conn, dtype=np.int32),
+            lnode=np.ascontiguousarray(lay.node, dtype=np.int32),
+            lval=np.ascontiguousarray(lay.val, dtype=np.int32),
+            tables=np.ascontiguousarray(self.kernel.tables, dtype=np.float64),
+            x=np.ascontiguousarray(mesh.x, dtype=np.float64),
+            eqn=np.ascontiguousarray(eqn),
+            params=np.ascontiguousarray(self.params if len(self.params) else np.zeros(1)),
+        )
+        k = self._keep
+        dd = N.DomainDesc(self.code.handle, mesh.etype.nnode, lay.n, mesh.n_elem, k["conn"].ctypes.data,
+                          k["lnode"].ctypes.data, k["lval"].ctypes.data, k["tables"].ctypes.data,
+                          k["tables"].size, self.kernel.epb, self.kernel.threads, self.kernel.smem_bytes)
+        self._domains = (N.DomainDesc * 1)(dd)
+        desc = N.ProblemDesc(mesh.dim, n, nval, k["x"].ctypes.data, k["eqn"].ctypes.data, self.n_dof, 1,
+                             self._domains, len(self.params), k["params"].ctypes.data,
+                             N.FE_JAC_F64 if prec == "f64" else N.FE_JAC_F32)
+        h = ctypes.c_void_p()
+        N.check(L.fe_problem_create(ctypes.byref(desc), ctypes.byref(h)))
+        self._h = h
+        N.check(L.fe_problem_set_values(h, values.ctypes.data))
+        nd = ctypes.c_int64()
+        nnz = ctypes.c_int64()
+        N.check(L.fe_problem_sizes(h, ctypes.byref(nd), ctypes.byref(nnz)))
+        self.nnz = nnz.value
+        self._jdtype = torch.float64 if prec == "f64" else torch.float32
+        dev = torch.device("cuda")
+        self.x_dev = torch.zeros(self.n_dof, dtype=torch.float64, device=dev)
+        self.R_dev = torch.zeros(max(self.n_dof, 1), dtype=torch.float64, device=dev)
+        self.J_dev = torch.zeros(max(self.nnz, 1), dtype=self._jdtype, device=dev)
+        self.x_dev.copy_(torch.from_numpy(self._dofs_from_values(values)))
+        t4 = time.perf_counter()
+        self.timings.update(jit_s=t3 - t2, device_setup_s=t4 - t3)
+        self._initialised = True
+
+    def _dofs_from_values(self, values: np.ndarray) -> np.ndarray:
+        x = np.zeros(self.n_dof)
+        m = self.eqn >= 0
+        x[self.eqn[m]] = values[m]
+        return x
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                N.load().fe_problem_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    # -- state ---------------------------------------------------------
+    def get_dofs(self) -> np.ndarray:
+        return self.x_dev.cpu().numpy()
+
+    def set_dofs(self, x: np.ndarray) -> None:
+        torch = _torch()
+        self.x_dev.copy_(torch.as_tensor(np.asarray(x, dtype=np.float64)))
+
+    def set_values(self, values: np.ndarray) -> None:
+        """Set every nodal value [n_nodes, nval] (pinned ones included) and
+        the dof vector that goes with it."""
+        v = np.ascontiguousarray(values, dtype=np.float64).reshape(self.mesh.n_nodes, len(self.fields))
+        N.check(N.load().fe_problem_set_values(self._h, v.ctypes.data))
+        self.set_dofs(self._dofs_from_values(v))
+
+    def get_values(self) -> np.ndarray:
+        """Nodal values [n_nodes, nval] (after the last assembly's dof scatter)."""
+        v = np.zeros((self.mesh.n_nodes, len(self.fields)))
+        N.check(N.load().fe_problem_get_values(self._h, v.ctypes.data))
+        return v
+
+    def set_parameters(self, **kw) -> None:
+        for k, v in kw.items():
+            self.params[self.param_names.index(k)] = float(v)
+        self._keep["params"][:len(self.params)] = self.params
+        N.check(N.load().fe_problem_set_params(self._h, self._keep["params"].ctypes.data))
+
+    def pattern(self) -> Tuple[np.ndarray, np.ndarray]:
+        rp = np.zeros(self.n_dof + 1, dtype=np.int32)
+        ci = np.zeros(max(self.nnz, 1), dtype=np.int32)
+        N.check(N.load().fe_problem_pattern(self._h, rp.ctypes.data, ci.ctypes.data))
+        return rp, ci[:self.nnz]
+
+    # -- assembly (device) ----------------------------------------------
+    def assemble_device(self, with_jacobian: bool = True, stream=None) -> None:
+        """R (and CSR J values) into self.R_dev / self.J_dev from self.x_dev."""
+        torch = _torch()
+        flags = N.FE_ASSEMBLE_RESIDUAL | N.FE_ASSEMBLE_VALUES_FROM_DOFS
+        if with_jacobian:
+            flags |= N.FE_ASSEMBLE_JACOBIAN
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        N.check(N.load().fe_assemble(self._h, self.x_dev.data_ptr(), self.R_dev.data_ptr(),
+                                     self.J_dev.data_ptr(), flags, ctypes.c_void_p(st)))
+
+    def launch_count(self, with_jacobian: bool = True) -> int:
+        flags = N.FE_ASSEMBLE_RESIDUAL | N.FE_ASSEMBLE_VALUES_FROM_DOFS
+        if with_jacobian:
+            flags |= N.FE_ASSEMBLE_JACOBIAN
+        return N.load().fe_problem_launch_count(self._h, flags)
+
+    def set_stage_timing(self, enable: bool) -> None:
+        N.check(N.load().fe_problem_set_timing(self._h, int(enable)))
+
+    def stage_times(self):
+        """Summed ms per stage (dof scatter, element kernels, residual gather,
+        Jacobian gather) since the last call, and the number of assemblies."""
+        ms = np.zeros(4)
+        calls = ctypes.c_int64()
+        N.check(N.load().fe_problem_stage_times(self._h, ms.ctypes.data, ctypes.byref(calls)))
+        return ms, calls.value
+
+    def check(self) -> None:
+        N.check(N.load().fe_problem_check(self._h))
+
+    # -- the reference-facing calls --------------------------------------
+    def get_residuals(self) -> np.ndarray:
+        """Problem::get_residuals (problem.cc:3810): R at the current dofs."""
+        self.initialise()
+        self.assemble_device(with_jacobian=False)
+        self.check()
+        return self.R_dev[:self.n_dof].cpu().numpy()
+
+    def get_jacobian(self):
+        """Problem::get_jacobian (problem.cc:4038): (R, scipy CSR J)."""
+        import scipy.sparse as sp
+        self.initialise()
+        self.assemble_device(with_jacobian=True)
+        self.check()
+        R = self.R_dev[:self.n_dof].cpu().numpy()
+        rp, ci = self.pattern()
+        vals = self.J_dev[:self.nnz].cpu().numpy()
+        return R, sp.csr_matrix((vals, ci, rp), shape=(self.n_dof, self.n_dof))
+
+    def assemble_jacobian(self):
+        """pyoomph's Problem.assemble_jacobian (problem.py:711)."""
+        return self.get_jacobian()
+
+    def residual_max(self) -> float:
+        out = ctypes.c_double()
+        torch = _torch()
+        N.check(N.load().fe_residual_max(self._h, self.R_dev.data_ptr(), self.n_dof, ctypes.byref(out),
+                                         ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        return out.value
+
+    # -- Newton ----------------------------------------------------------
+    def _solve_linear(self, R: np.ndarray) -> np.ndarray:
+        import scipy.sparse as sp
+        import scipy.sparse.linalg as spla
+        rp, ci = self._pattern_cache
+        vals = self.J_dev[:self.nnz].cpu().numpy().astype(np.float64)
+        A = sp.csr_matrix((vals, ci, rp), shape=(self.n_dof, self.n_dof))
+        if self.linear_solver is not None:
+            return self.linear_solver(A, R)
+        return spla.splu(A.tocsc()).solve(R)
+
+    def solve(self, **_ignored) -> List[float]:
+        """Stationary Newton solve; returns the residual max-norm history."""
+        torch = _torch()
+        self.initialise()
+        self._pattern_cache = self.pattern()
+        hist = []
+        t_asm = 0.0
+        t_lin = 0.0
+        t0 = time.perf_counter()
+        self.assemble_device(with_jacobian=False)
+        hist.append(self.residual_max())
+        it = 0
+        while hist[-1] >= self.newton_solver_tolerance:
+            if it >= self.max_newton_iterations:
+                raise NewtonSolverError(f"max Newton iterations ({self.max_newton_iterations}) reached; "
+                                        f"residuals {hist}")
+            if hist[-1] > self.max_residuals:
+                raise NewtonSolverError(f"max residuals ({self.max_residuals}) exceeded: {hist}")
+            ta = time.perf_counter()
+            self.assemble_device(with_jacobian=True)
+            self.check()
+            R = self.R_dev[:self.n_dof].cpu().numpy()
+            tb = time.perf_counter()
+            dx = self._solve_linear(R)
+            tc = time.perf_counter()
+            dxd = torch.as_tensor(dx, device=self.x_dev.device)
+            N.check(N.load().fe_dof_update(self._h, self.x_dev.data_ptr(), dxd.data_ptr(), self.n_dof,
+                                           ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+            self.assemble_device(with_jacobian=False)
+            hist.append(self.residual_max())
+            t_asm += tb - ta
+            t_lin += tc - tb
+            it += 1
+            if self.verbose:
+                print(f"Newton iteration {it}: max residual {hist[-1]:.3e}")
+        self.assemble_device(with_jacobian=False)  # leaves the nodal values at the solution
+        self.check()
+        self.newton_history = hist
+        self.timings.update(newton_total_s=time.perf_counter() - t0, newton_assembly_s=t_asm,
+                            newton_linear_solve_s=t_lin, newton_iterations=it)
+        return hist

@@ -1,0 +1,79 @@
+"""The synthetic workloads of the benchmark, built through the public API.
+
+* Poisson -Laplace(u) = f on the unit square, Q2 quads, u = 0 on the
+  boundary, f a sum of 8 Gaussians drawn from a seed;
+* steady incompressible Navier-Stokes, Taylor-Hood P2/P1 on a split
+  structured mesh, Re = 100 (rho = 1, mu = 1/100), lid u_x = 16x^2(1-x)^2
+  on top, no-slip elsewhere, one pressure pinned, dofs perturbed by
+  N(0, 1e-3) from a seed;
+* 3D nonlinear diffusion -div((1+u^2) grad u) = f on the unit cube, Q2
+  hexahedra, f a sum of 16 Gaussians from a seed.
+
+Gaussians: centres U[0,1]^dim, widths U[0.05, 0.2], amplitudes N(0,1),
+f(x) = sum_k A_k exp(-|x - c_k|^2 / (2 w_k^2)), numpy default_rng(seed).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .equations import (DirichletBC, NavierStokesEquations, NonlinearDiffusionEquation, PoissonEquation,
+                        PressureFixation)
+from .meshes import CuboidBrickMesh, RectangularQuadMesh
+from .problem import Problem
+
+
+def draw_gaussians(seed: int, n: int, dim: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(0.0, 1.0, (n, dim))
+    w = rng.uniform(0.05, 0.2, (n, 1))
+    A = rng.normal(0.0, 1.0, (n, 1))
+    return np.hstack([c, w, A])
+
+
+def lid_velocity(x, y):
+    return 16.0 * x * x * (1.0 - x) * (1.0 - x)
+
+
+def poisson_problem(N=64, seed: int = 0, gaussians: np.ndarray = None, split: str = None,
+                    jacobian_precision: str = "fp64") -> Problem:
+    g = draw_gaussians(seed, 8, 2) if gaussians is None else gaussians
+    P = Problem()
+    P.jacobian_precision = jacobian_precision
+    P += RectangularQuadMesh(N=N, split_in_tris=split or False)
+    P += (PoissonEquation(source=g) + DirichletBC(u=0.0) @ ["left", "right", "top", "bottom"]) @ "domain"
+    return P
+
+
+def nonlinear_diffusion_problem(N=48, seed: int = 0, gaussians: np.ndarray = None,
+                                jacobian_precision: str = "fp64", dim: int = 3) -> Problem:
+    g = draw_gaussians(seed, 16, dim) if gaussians is None else gaussians
+    P = Problem()
+    P.jacobian_precision = jacobian_precision
+    if dim == 3:
+        P += CuboidBrickMesh(N=N)
+        walls = ["left", "right", "top", "bottom", "back", "front"]
+    else:
+        P += RectangularQuadMesh(N=N)
+        walls = ["left", "right", "top", "bottom"]
+    P += (NonlinearDiffusionEquation(source=g) + DirichletBC(u=0.0) @ walls) @ "domain"
+    return P
+
+
+def navier_stokes_problem(N=256, Re: float = 100.0, split: str = "left",
+                          jacobian_precision: str = "fp64") -> Problem:
+    P = Problem()
+    P.jacobian_precision = jacobian_precision
+    P += RectangularQuadMesh(N=N, split_in_tris=split)
+    eqs = NavierStokesEquations(mass_density=1.0, dynamic_viscosity=1.0 / Re)
+    eqs += DirichletBC(velocity_x=lid_velocity, velocity_y=0.0) @ "top"
+    eqs += DirichletBC(velocity_x=0.0, velocity_y=0.0) @ ["left", "right", "bottom"]
+    eqs += PressureFixation("pressure", 0.0)
+    P += eqs @ "domain"
+    return P
+
+
+def perturb_dofs(P: Problem, seed: int, sigma: float = 1e-3) -> None:
+    """Add N(0, sigma) to every dof (from a seed)."""
+    x = P.get_dofs()
+    x = x + np.random.default_rng(seed).normal(0.0, sigma, x.size)
+    P.set_dofs(x)

@@ -1,0 +1,175 @@
+"""GPU parity: the CUDA assembly (through the C-ABI library) against the
+reference's own oomph-lib output (golden fixtures) and the CPU oracle.
+
+Contract (fp64 path): CSR rowptr/colidx bit-exact (structural pattern in
+first-insertion order), residual and Jacobian entries within 1e-12 of the
+max norm, converged Newton solutions within 1e-10.  FP32-Jacobian path:
+residual as above; Jacobian within 1e-5 relative (max norm) of the FP64
+oracle; Newton converges to the FP64 solution within 1e-10.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+CASES = [c for c in sorted(glob.glob(os.path.join(GOLD, "*_*.npz"))) if not c.endswith("oomph_tables.npz")]
+RTOL = 1e-12
+JTOL32 = 1e-5
+STOL = 1e-10
+
+
+def _product_for(g):
+    from pyoomph_gb300 import workloads as W
+    et, eq = int(g["etype"]), int(g["eq"])
+    nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
+    if eq == O.EQ_NAVIER_STOKES_TH:
+        P = W.navier_stokes_problem(N=[nx, ny], Re=1.0 / float(g["params"][1]),
+                                    split="left" if int(g["split"]) == 0 else "right")
+    else:
+        dim = 3 if et == O.Q2_HEX else 2
+        gauss = g["params"][1:].reshape(int(g["params"][0]), dim + 2)
+        if eq == O.EQ_POISSON:
+            P = W.poisson_problem(N=[nx, ny], gaussians=gauss, split=None if et == O.Q2_QUAD else "left")
+        else:
+            P = W.nonlinear_diffusion_problem(N=[nx, ny, nz] if dim == 3 else [nx, ny], gaussians=gauss, dim=dim)
+    P.initialise()
+    return P
+
+
+def _relmax(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+@pytest.mark.parametrize("path", CASES, ids=[os.path.basename(c)[:-4] for c in CASES])
+def test_golden_reference_parity(path):
+    g = np.load(path)
+    P = _product_for(g)
+    assert np.array_equal(P.eqn, g["eqn"])
+    P.set_values(g["values"])
+    R, J = P.get_jacobian()
+    assert np.array_equal(J.indptr, g["rowptr_st"])
+    assert np.array_equal(J.indices, g["colidx_st"])
+    assert _relmax(J.data, g["vals_st"]) <= RTOL
+    assert _relmax(R, g["R"]) <= RTOL
+
+
+@pytest.mark.parametrize("kind", ["poisson_q2", "poisson_p2", "ns_th", "nldiff_hex", "nldiff_q2"])
+def test_random_state_vs_oracle(kind):
+    from pyoomph_gb300 import workloads as W
+    rng = np.random.default_rng(11)
+    if kind == "ns_th":
+        P = W.navier_stokes_problem(N=[9, 7])
+        P.initialise()
+        m = O.mesh(O.P2_TRI, 9, 7)
+        OP = O.navier_stokes_problem(m, rho=1.0, mu=0.01)
+        x = OP.dofs() + rng.normal(0, 0.1, OP.n_dof)
+    else:
+        if kind == "nldiff_hex":
+            et, dim, nx = O.Q2_HEX, 3, [3, 4, 2]
+        elif kind == "poisson_p2":
+            et, dim, nx = O.P2_TRI, 2, [11, 6]
+        else:
+            et, dim, nx = O.Q2_QUAD, 2, [12, 9]
+        gauss = W.draw_gaussians(3, 8, dim)
+        eq = O.EQ_POISSON if kind.startswith("poisson") else O.EQ_NONLINEAR_DIFFUSION
+        if eq == O.EQ_POISSON:
+            P = W.poisson_problem(N=nx, gaussians=gauss, split="left" if et == O.P2_TRI else None)
+        else:
+            P = W.nonlinear_diffusion_problem(N=nx, gaussians=gauss, dim=dim)
+        P.initialise()
+        m = O.mesh(et, *(nx + [0] * (3 - len(nx))))
+        OP = O.poisson_problem(m, gauss, eq=eq)
+        x = rng.normal(0, 0.5, OP.n_dof)
+    assert P.n_dof == OP.n_dof and np.array_equal(P.eqn, OP.eqn)
+    OP.set_dofs(x)
+    P.set_dofs(x)
+    R0, rp, ci, v = O.assemble(OP, True, -1.0)
+    R, J = P.get_jacobian()
+    assert np.array_equal(J.indptr, rp) and np.array_equal(J.indices, ci)
+    assert _relmax(J.data, v) <= RTOL
+    assert _relmax(R, R0) <= RTOL
+    # residual-only assembly gives the same residual
+    assert np.array_equal(P.get_residuals(), R)
+
+
+def test_assembly_is_deterministic():
+    from pyoomph_gb300 import workloads as W
+    P = W.navier_stokes_problem(N=[10, 10])
+    P.initialise()
+    W.perturb_dofs(P, seed=5, sigma=0.05)
+    R1, J1 = P.get_jacobian()
+    R2, J2 = P.get_jacobian()
+    assert np.array_equal(R1, R2) and np.array_equal(J1.data, J2.data)
+
+
+@pytest.mark.parametrize("kind", ["nldiff_hex", "ns_th"])
+def test_fp32_jacobian_error_vs_fp64_oracle(kind):
+    from pyoomph_gb300 import workloads as W
+    rng = np.random.default_rng(5)
+    if kind == "ns_th":
+        P = W.navier_stokes_problem(N=[8, 8], jacobian_precision="fp32")
+        P.initialise()
+        OP = O.navier_stokes_problem(O.mesh(O.P2_TRI, 8, 8), rho=1.0, mu=0.01)
+        x = OP.dofs() + rng.normal(0, 0.1, OP.n_dof)
+    else:
+        gauss = W.draw_gaussians(4, 16, 3)
+        P = W.nonlinear_diffusion_problem(N=4, gaussians=gauss, jacobian_precision="fp32")
+        P.initialise()
+        OP = O.poisson_problem(O.mesh(O.Q2_HEX, 4, 4, 4), gauss, eq=O.EQ_NONLINEAR_DIFFUSION)
+        x = rng.normal(0, 0.5, OP.n_dof)
+    OP.set_dofs(x)
+    P.set_dofs(x)
+    R0, rp, ci, v = O.assemble(OP, True, -1.0)
+    R, J = P.get_jacobian()
+    assert J.data.dtype == np.float32
+    assert np.array_equal(J.indptr, rp) and np.array_equal(J.indices, ci)
+    err = _relmax(J.data.astype(np.float64), v)
+    assert err <= JTOL32, err
+    assert _relmax(R, R0) <= RTOL
+
+
+def test_newton_poisson_matches_oracle_solution():
+    from pyoomph_gb300 import workloads as W
+    gauss = W.draw_gaussians(0, 8, 2)
+    P = W.poisson_problem(N=16, gaussians=gauss)
+    P.newton_solver_tolerance = 1e-10
+    hist = P.solve()
+    assert hist[-1] < 1e-10
+    OP = O.poisson_problem(O.mesh(O.Q2_QUAD, 16, 16), gauss)
+    O.newton(OP, tol=1e-10)
+    assert _relmax(P.get_dofs(), OP.dofs()) <= STOL
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_newton_navier_stokes_matches_oracle_solution(prec):
+    from pyoomph_gb300 import workloads as W
+    P = W.navier_stokes_problem(N=[8, 8], jacobian_precision=prec)
+    P.newton_solver_tolerance = 1e-10
+    P.max_newton_iterations = 20
+    hist = P.solve()
+    assert hist[-1] < 1e-10
+    OP = O.navier_stokes_problem(O.mesh(O.P2_TRI, 8, 8), rho=1.0, mu=0.01)
+    O.newton(OP, tol=1e-10)
+    assert _relmax(P.get_dofs(), OP.dofs()) <= STOL
+
+
+def test_newton_nonlinear_diffusion_fp32_converges_to_fp64_solution():
+    from pyoomph_gb300 import workloads as W
+    gauss = W.draw_gaussians(1, 16, 3) * np.array([1, 1, 1, 1, 20.0])
+    P64 = W.nonlinear_diffusion_problem(N=3, gaussians=gauss)
+    P64.newton_solver_tolerance = 1e-10
+    P64.solve()
+    P32 = W.nonlinear_diffusion_problem(N=3, gaussians=gauss, jacobian_precision="fp32")
+    P32.newton_solver_tolerance = 1e-10
+    P32.max_newton_iterations = 20
+    P32.solve()
+    assert _relmax(P32.get_dofs(), P64.get_dofs()) <= STOL
+    OP = O.poisson_problem(O.mesh(O.Q2_HEX, 3, 3, 3), gauss, eq=O.EQ_NONLINEAR_DIFFUSION)
+    O.newton(OP, tol=1e-10)
+    assert _relmax(P64.get_dofs(), OP.dofs()) <= STOL
