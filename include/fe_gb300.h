@@ -127,6 +127,13 @@ typedef struct fe_problem_desc {
 int fe_problem_create(const fe_problem_desc_t *desc, fe_problem_t **out);
 void fe_problem_destroy(fe_problem_t *p);
 
+/*
+ * The same CSR pattern on the host only (no GPU; the domains' code may be
+ * NULL).  Call with rowptr = colidx = NULL to get *nnz, then again with
+ * buffers of n_dof+1 and nnz entries.
+ */
+int fe_pattern_host(const fe_problem_desc_t *desc, int64_t *nnz, int32_t *rowptr, int32_t *colidx);
+
 int fe_problem_sizes(const fe_problem_t *p, int64_t *n_dof, int64_t *nnz);
 /* Host copies of the CSR pattern. */
 int fe_problem_pattern(const fe_problem_t *p, int32_t *rowptr, int32_t *colidx);

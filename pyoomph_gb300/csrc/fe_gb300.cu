@@ -61,9 +61,28 @@ int fail(int code, const char *fmt, ...) {
 // ---------------------------------------------------------------------------
 // device buffers
 // ---------------------------------------------------------------------------
+// Owning device allocation: movable, not copyable (a copy would free the
+// same pointer twice).
 struct DevBuf {
   void *p = nullptr;
   size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept : p(o.p), bytes(o.bytes) {
+    o.p = nullptr;
+    o.bytes = 0;
+  }
+  DevBuf &operator=(DevBuf &&o) noexcept {
+    if (this != &o) {
+      if (p) cudaFree(p);
+      p = o.p;
+      bytes = o.bytes;
+      o.p = nullptr;
+      o.bytes = 0;
+    }
+    return *this;
+  }
   ~DevBuf() {
     if (p) cudaFree(p);
   }
@@ -260,49 +279,66 @@ struct Incident {
   int i;
 };
 
-// Builds, for all rows in [r0, r1): row lengths / columns / per-slot
-// contributions.  Two passes: count (fill=false), then fill.
+// Host description of the element blocks the pattern is built from.
+struct PatDomain {
+  const int32_t *conn;
+  int nnode, nlocal;
+  long long n_elem;
+  const int32_t *local_node, *local_val;
+  long long jbase, rbase; // offsets in the element-matrix / element-residual buffers
+};
+
+struct PatternOut {
+  std::vector<int32_t> rowptr, colidx;
+  std::vector<long long> cptr; // [nnz+1] per-slot contribution ranges
+  std::vector<unsigned> cidx;  // element-matrix entry of each contribution
+  std::vector<long long> rptr; // [n_dof+1] per-row residual contributions
+  std::vector<unsigned> ridx;
+};
+
+// The CSR pattern of Problem::sparse_assemble_row_or_column_compressed_with_
+// vectors_of_pairs (problem.cc:5459-5660) with every structural coupling kept:
+// row r lists, in order of first insertion over (element, local i, local j),
+// the columns of the elements that contain equation r.  Rows are built
+// independently (in parallel): the incidence of each equation (its elements,
+// in element order, with the local index) is gathered first, then each row
+// walks its incidence with a marker array for O(1) membership.
 struct PatternBuilder {
-  const fe_problem *P;
-  const std::vector<const int32_t *> *conn_h;
-  const int32_t *eqn_h;
-  // incidence of each dof: (domain, element, local i) in element order
+  long long n_dof;
+  int nval;
+  const int32_t *eqn;
+  const std::vector<PatDomain> *doms;
   std::vector<long long> inc_ptr;
   std::vector<Incident> inc;
 
-  int32_t geq(const Domain &d, const int32_t *conn, long long e, int k) const {
-    int node = conn[e * d.nnode + d.local_node[k]];
-    return eqn_h[(long long)node * P->nval + d.local_val[k]];
+  int32_t geq(const PatDomain &d, long long e, int k) const {
+    int node = d.conn[e * d.nnode + d.local_node[k]];
+    return eqn[(long long)node * nval + d.local_val[k]];
   }
 
   void build_incidence() {
-    const long long n = P->n_dof;
+    const long long n = n_dof;
     std::vector<long long> cnt(n + 1, 0);
-    for (size_t di = 0; di < P->domains.size(); di++) {
-      const Domain &d = P->domains[di];
-      const int32_t *conn = (*conn_h)[di];
+    for (const PatDomain &d : *doms)
       for (long long e = 0; e < d.n_elem; e++)
         for (int i = 0; i < d.nlocal; i++) {
-          int32_t r = geq(d, conn, e, i);
+          int32_t r = geq(d, e, i);
           if (r >= 0) cnt[r + 1]++;
         }
-    }
     for (long long r = 0; r < n; r++) cnt[r + 1] += cnt[r];
     inc_ptr = cnt;
     inc.resize(cnt[n]);
     std::vector<long long> pos(cnt.begin(), cnt.end() - 1);
-    for (size_t di = 0; di < P->domains.size(); di++) {
-      const Domain &d = P->domains[di];
-      const int32_t *conn = (*conn_h)[di];
+    for (size_t di = 0; di < doms->size(); di++) {
+      const PatDomain &d = (*doms)[di];
       for (long long e = 0; e < d.n_elem; e++)
         for (int i = 0; i < d.nlocal; i++) {
-          int32_t r = geq(d, conn, e, i);
+          int32_t r = geq(d, e, i);
           if (r >= 0) inc[pos[r]++] = Incident{(int)di, e, i};
         }
     }
   }
 
-  // per-row work.  marker: [n_dof] scratch (-1), slot_of: column -> local slot
   void row(long long r, std::vector<int32_t> &marker, std::vector<int32_t> &cols,
            std::vector<long long> &slot_cnt, bool fill, int32_t *colidx_out, long long *cptr_out,
            unsigned *cidx_out, long long cbase, long long *row_len, long long *row_contrib) const {
@@ -311,10 +347,9 @@ struct PatternBuilder {
     long long ncontrib = 0;
     for (long long k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
       const Incident &I = inc[k];
-      const Domain &d = P->domains[I.dom];
-      const int32_t *conn = (*conn_h)[I.dom];
+      const PatDomain &d = (*doms)[I.dom];
       for (int j = 0; j < d.nlocal; j++) {
-        int32_t c = geq(d, conn, I.e, j);
+        int32_t c = geq(d, I.e, j);
         if (c < 0) continue;
         int32_t s = marker[c];
         if (s < 0) {
@@ -330,23 +365,20 @@ struct PatternBuilder {
     *row_len = (long long)cols.size();
     *row_contrib = ncontrib;
     if (fill) {
-      // columns and per-slot pointers
       long long acc = cbase;
       for (size_t s = 0; s < cols.size(); s++) {
         colidx_out[s] = cols[s];
         cptr_out[s] = acc;
         acc += slot_cnt[s];
       }
-      // contributions in element order per slot
       std::vector<long long> wpos(cols.size());
       for (size_t s = 0; s < cols.size(); s++) wpos[s] = cptr_out[s];
       for (long long k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
         const Incident &I = inc[k];
-        const Domain &d = P->domains[I.dom];
-        const int32_t *conn = (*conn_h)[I.dom];
+        const PatDomain &d = (*doms)[I.dom];
         const long long base = d.jbase + (I.e * d.nlocal + I.i) * (long long)d.nlocal;
         for (int j = 0; j < d.nlocal; j++) {
-          int32_t c = geq(d, conn, I.e, j);
+          int32_t c = geq(d, I.e, j);
           if (c < 0) continue;
           cidx_out[wpos[marker[c]]++] = (unsigned)(base + j);
         }
@@ -356,18 +388,20 @@ struct PatternBuilder {
   }
 };
 
-int build_pattern(fe_problem *P, const std::vector<const int32_t *> &conn_h, const int32_t *eqn_h) {
+int build_pattern_host(long long n_dof, int nval, const int32_t *eqn, const std::vector<PatDomain> &doms,
+                       bool with_contributions, PatternOut &out) {
   PatternBuilder B;
-  B.P = P;
-  B.conn_h = &conn_h;
-  B.eqn_h = eqn_h;
+  B.n_dof = n_dof;
+  B.nval = nval;
+  B.eqn = eqn;
+  B.doms = &doms;
   B.build_incidence();
-  const long long n = P->n_dof;
+  const long long n = n_dof;
   unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  if (n < 4096) nthreads = 1;
   std::vector<long long> row_len(n), row_con(n);
-  auto pass = [&](bool fill, std::vector<int32_t> *colidx, std::vector<long long> *cptr,
-                  std::vector<unsigned> *cidx, const std::vector<long long> *rp,
-                  const std::vector<long long> *cp) {
+  std::vector<long long> rp(n + 1, 0), cp(n + 1, 0);
+  auto pass = [&](bool fill) {
     std::vector<std::thread> th;
     for (unsigned t = 0; t < nthreads; t++) {
       th.emplace_back([&, t]() {
@@ -381,48 +415,94 @@ int build_pattern(fe_problem *P, const std::vector<const int32_t *> &conn_h, con
             row_len[r] = rl;
             row_con[r] = rc;
           } else {
-            long long o = (*rp)[r];
-            B.row(r, marker, cols, slot_cnt, true, colidx->data() + o, cptr->data() + o, cidx->data(),
-                  (*cp)[r], &rl, &rc);
+            long long o = rp[r];
+            B.row(r, marker, cols, slot_cnt, with_contributions, out.colidx.data() + o,
+                  with_contributions ? out.cptr.data() + o : nullptr,
+                  with_contributions ? out.cidx.data() : nullptr, cp[r], &rl, &rc);
+            if (!with_contributions) {
+              // columns only: recompute cols for this row
+              for (size_t s = 0; s < cols.size(); s++) out.colidx[o + s] = cols[s];
+            }
           }
         }
       });
     }
     for (auto &x : th) x.join();
   };
-  pass(false, nullptr, nullptr, nullptr, nullptr, nullptr);
-  std::vector<long long> rp(n + 1, 0), cp(n + 1, 0);
+  pass(false);
   for (long long r = 0; r < n; r++) {
     rp[r + 1] = rp[r] + row_len[r];
     cp[r + 1] = cp[r] + row_con[r];
   }
   const long long nnz = rp[n];
   if (nnz > 0x7fffffffLL) return fail(FE_ERR_ARG, "nnz %lld exceeds int32 CSR", nnz);
-  std::vector<int32_t> colidx(nnz);
-  std::vector<long long> cptr(nnz + 1);
-  std::vector<unsigned> cidx(cp[n]);
-  pass(true, &colidx, &cptr, &cidx, &rp, &cp);
-  cptr[nnz] = cp[n];
-  P->nnz = nnz;
-  P->h_rowptr.resize(n + 1);
-  for (long long r = 0; r <= n; r++) P->h_rowptr[r] = (int32_t)rp[r];
-  P->h_colidx = colidx;
-  int rc;
-  if ((rc = P->rowptr.upload(P->h_rowptr.data(), sizeof(int32_t) * (n + 1)))) return rc;
-  if ((rc = P->colidx.upload(colidx.data(), sizeof(int32_t) * nnz))) return rc;
-  if ((rc = P->cptr.upload(cptr.data(), sizeof(long long) * (nnz + 1)))) return rc;
-  if ((rc = P->cidx.upload(cidx.data(), sizeof(unsigned) * cidx.size()))) return rc;
-  // residual contribution lists: incidence in element order
-  std::vector<long long> rptr(n + 1);
-  std::vector<unsigned> ridx(B.inc.size());
-  for (long long r = 0; r <= n; r++) rptr[r] = B.inc_ptr[r];
-  for (size_t k = 0; k < B.inc.size(); k++) {
-    const Incident &I = B.inc[k];
-    const Domain &d = P->domains[I.dom];
-    ridx[k] = (unsigned)(d.rbase + I.e * d.nlocal + I.i);
+  out.colidx.assign(nnz, 0);
+  if (with_contributions) {
+    out.cptr.assign(nnz + 1, 0);
+    out.cidx.assign(cp[n], 0);
   }
-  if ((rc = P->rptr.upload(rptr.data(), sizeof(long long) * (n + 1)))) return rc;
-  if ((rc = P->ridx.upload(ridx.data(), sizeof(unsigned) * ridx.size()))) return rc;
+  pass(true);
+  if (with_contributions) out.cptr[nnz] = cp[n];
+  out.rowptr.resize(n + 1);
+  for (long long r = 0; r <= n; r++) out.rowptr[r] = (int32_t)rp[r];
+  if (with_contributions) {
+    out.rptr.assign(B.inc_ptr.begin(), B.inc_ptr.end());
+    out.ridx.resize(B.inc.size());
+    for (size_t k = 0; k < B.inc.size(); k++) {
+      const Incident &I = B.inc[k];
+      const PatDomain &d = doms[I.dom];
+      out.ridx[k] = (unsigned)(d.rbase + I.e * d.nlocal + I.i);
+    }
+  }
+  return FE_OK;
+}
+
+int build_pattern(fe_problem *P, const std::vector<const int32_t *> &conn_h, const int32_t *eqn_h) {
+  std::vector<PatDomain> doms;
+  for (size_t di = 0; di < P->domains.size(); di++) {
+    const Domain &d = P->domains[di];
+    doms.push_back(PatDomain{conn_h[di], d.nnode, d.nlocal, d.n_elem, d.local_node.data(), d.local_val.data(),
+                             d.jbase, d.rbase});
+  }
+  PatternOut out;
+  int rc = build_pattern_host(P->n_dof, P->nval, eqn_h, doms, true, out);
+  if (rc) return rc;
+  const long long n = P->n_dof;
+  const long long nnz = (long long)out.colidx.size();
+  P->nnz = nnz;
+  P->h_rowptr = out.rowptr;
+  P->h_colidx = out.colidx;
+  if ((rc = P->rowptr.upload(out.rowptr.data(), sizeof(int32_t) * (n + 1)))) return rc;
+  if ((rc = P->colidx.upload(out.colidx.data(), sizeof(int32_t) * nnz))) return rc;
+  if ((rc = P->cptr.upload(out.cptr.data(), sizeof(long long) * (nnz + 1)))) return rc;
+  if ((rc = P->cidx.upload(out.cidx.data(), sizeof(unsigned) * out.cidx.size()))) return rc;
+  if ((rc = P->rptr.upload(out.rptr.data(), sizeof(long long) * (n + 1)))) return rc;
+  if ((rc = P->ridx.upload(out.ridx.data(), sizeof(unsigned) * out.ridx.size()))) return rc;
+  return FE_OK;
+}
+
+// validates the host parts of a problem description
+int validate_desc(const fe_problem_desc_t *desc, bool need_code) {
+  if (!desc) return fail(FE_ERR_ARG, "null problem description");
+  if (desc->dim < 1 || desc->dim > 3 || desc->nval < 1 || desc->n_nodes < 0 || desc->n_dof < 0 ||
+      desc->n_domains < 1 || !desc->domains || !desc->eqn)
+    return fail(FE_ERR_ARG, "problem description: bad sizes");
+  for (long long k = 0; k < desc->n_nodes * desc->nval; k++)
+    if (desc->eqn[k] >= desc->n_dof || desc->eqn[k] < -1)
+      return fail(FE_ERR_ARG, "eqn[%lld]=%d out of range", k, desc->eqn[k]);
+  for (int di = 0; di < desc->n_domains; di++) {
+    const fe_domain_desc_t &dd = desc->domains[di];
+    if ((need_code && !dd.code) || dd.nnode_el < 1 || dd.nlocal < 1 || dd.n_elem < 0 ||
+        (!dd.conn && dd.n_elem) || !dd.local_node || !dd.local_val)
+      return fail(FE_ERR_ARG, "bad domain %d", di);
+    for (long long k = 0; k < dd.n_elem * dd.nnode_el; k++)
+      if (dd.conn[k] < 0 || dd.conn[k] >= desc->n_nodes)
+        return fail(FE_ERR_ARG, "domain %d: conn[%lld]=%d out of range", di, k, dd.conn[k]);
+    for (int k = 0; k < dd.nlocal; k++)
+      if (dd.local_node[k] < 0 || dd.local_node[k] >= dd.nnode_el || dd.local_val[k] < 0 ||
+          dd.local_val[k] >= desc->nval)
+        return fail(FE_ERR_ARG, "domain %d: bad local layout at %d", di, k);
+  }
   return FE_OK;
 }
 
@@ -563,9 +643,9 @@ void fe_code_destroy(fe_code_t *code) { delete code; }
 int fe_problem_create(const fe_problem_desc_t *desc, fe_problem_t **out) {
   if (!desc || !out) return fail(FE_ERR_ARG, "fe_problem_create: null argument");
   *out = nullptr;
-  if (desc->dim < 1 || desc->dim > 3 || desc->nval < 1 || desc->n_nodes < 0 || desc->n_dof < 0 ||
-      desc->n_domains < 1 || !desc->domains || !desc->x || !desc->eqn)
-    return fail(FE_ERR_ARG, "fe_problem_create: bad sizes");
+  int rc0 = validate_desc(desc, true);
+  if (rc0) return rc0;
+  if (!desc->x) return fail(FE_ERR_ARG, "fe_problem_create: null positions");
   if (desc->jac_precision != FE_JAC_F64 && desc->jac_precision != FE_JAC_F32)
     return fail(FE_ERR_ARG, "fe_problem_create: bad jac_precision %d", desc->jac_precision);
   int rc = ensure_context();
@@ -577,24 +657,13 @@ int fe_problem_create(const fe_problem_desc_t *desc, fe_problem_t **out) {
   P->n_dof = desc->n_dof;
   P->jac_prec = desc->jac_precision;
   P->n_params = desc->n_params;
-  // equation numbers must be in range
-  for (long long k = 0; k < desc->n_nodes * desc->nval; k++)
-    if (desc->eqn[k] >= desc->n_dof) return fail(FE_ERR_ARG, "eqn[%lld]=%d >= n_dof", k, desc->eqn[k]);
   std::vector<const int32_t *> conn_h;
   long long jtot = 0, rtot = 0;
   for (int di = 0; di < desc->n_domains; di++) {
     const fe_domain_desc_t &dd = desc->domains[di];
-    if (!dd.code || dd.nnode_el < 1 || dd.nlocal < 1 || dd.n_elem < 0 || (!dd.conn && dd.n_elem) ||
-        !dd.local_node || !dd.local_val || dd.elems_per_block < 1 || dd.threads_per_block < 32 ||
-        dd.threads_per_block > 1024 || dd.smem_bytes < 0)
-      return fail(FE_ERR_ARG, "fe_problem_create: bad domain %d", di);
-    for (long long k = 0; k < dd.n_elem * dd.nnode_el; k++)
-      if (dd.conn[k] < 0 || dd.conn[k] >= desc->n_nodes)
-        return fail(FE_ERR_ARG, "domain %d: conn[%lld]=%d out of range", di, k, dd.conn[k]);
-    for (int k = 0; k < dd.nlocal; k++)
-      if (dd.local_node[k] < 0 || dd.local_node[k] >= dd.nnode_el || dd.local_val[k] < 0 ||
-          dd.local_val[k] >= desc->nval)
-        return fail(FE_ERR_ARG, "domain %d: bad local layout at %d", di, k);
+    if (dd.elems_per_block < 1 || dd.threads_per_block < 32 || dd.threads_per_block > 1024 || dd.smem_bytes < 0 ||
+        dd.smem_bytes > 227 * 1024)
+      return fail(FE_ERR_ARG, "fe_problem_create: bad launch shape in domain %d", di);
     Domain d;
     d.code = dd.code;
     d.nnode = dd.nnode_el;
@@ -636,6 +705,25 @@ int fe_problem_create(const fe_problem_desc_t *desc, fe_problem_t **out) {
 }
 
 void fe_problem_destroy(fe_problem_t *p) { delete p; }
+
+int fe_pattern_host(const fe_problem_desc_t *desc, int64_t *nnz, int32_t *rowptr, int32_t *colidx) {
+  int rc = validate_desc(desc, false);
+  if (rc) return rc;
+  std::vector<PatDomain> doms;
+  long long jb = 0, rb = 0;
+  for (int di = 0; di < desc->n_domains; di++) {
+    const fe_domain_desc_t &dd = desc->domains[di];
+    doms.push_back(PatDomain{dd.conn, dd.nnode_el, dd.nlocal, dd.n_elem, dd.local_node, dd.local_val, jb, rb});
+    jb += dd.n_elem * (long long)dd.nlocal * dd.nlocal;
+    rb += dd.n_elem * (long long)dd.nlocal;
+  }
+  PatternOut out;
+  if ((rc = build_pattern_host(desc->n_dof, desc->nval, desc->eqn, doms, false, out))) return rc;
+  if (nnz) *nnz = (int64_t)out.colidx.size();
+  if (rowptr) memcpy(rowptr, out.rowptr.data(), sizeof(int32_t) * out.rowptr.size());
+  if (colidx) memcpy(colidx, out.colidx.data(), sizeof(int32_t) * out.colidx.size());
+  return FE_OK;
+}
 
 int fe_problem_sizes(const fe_problem_t *p, int64_t *n_dof, int64_t *nnz) {
   if (!p) return fail(FE_ERR_ARG, "null problem");

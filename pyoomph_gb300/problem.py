@@ -142,17 +142,6 @@ class Problem:
         self._prec = prec
         self.kernel: KernelSpec = generate_kernel(mesh.etype, pw, prec, epb=self.elems_per_block)
         self.timings.update(setup_mesh_s=t1 - t0, codegen_s=time.perf_counter() - t1)
-        return self.kernel
-
-    def initialise(self) -> None:
-        if self._initialised:
-            return
-        torch = _torch()
-        self.lower()
-        mesh, fields, bcs, prec = self.mesh, self.fields, self._bcs, self._prec
-        t2 = time.perf_counter()
-        self.code = N.Code(self.kernel.source, self.kernel.name)
-        t3 = time.perf_counter()
         # nodal values, pins and equation numbers
         nval = len(fields)
         n = mesh.n_nodes
@@ -198,26 +187,21 @@ class Problem:
         self.present = present
         self.pinned = pinned
         self._values0 = values
+        return self.kernel
+
+    def initialise(self) -> None:
+        if self._initialised:
+            return
+        torch = _torch()
+        self.lower()
+        mesh, fields, prec = self.mesh, self.fields, self._prec
+        n, nval, values, eqn = mesh.n_nodes, len(fields), self._values0, self.eqn
+        t2 = time.perf_counter()
+        self.code = N.Code(self.kernel.source, self.kernel.name)
+        t3 = time.perf_counter()
         # device problem
         L = N.load()
-        lay = self.kernel.layout
-        self._keep = dict(
-            conn=np.ascontiguousarray(mesh.conn, dtype=np.int32),
-            lnode=np.ascontiguousarray(lay.node, dtype=np.int32),
-            lval=np.ascontiguousarray(lay.val, dtype=np.int32),
-            tables=np.ascontiguousarray(self.kernel.tables, dtype=np.float64),
-            x=np.ascontiguousarray(mesh.x, dtype=np.float64),
-            eqn=np.ascontiguousarray(eqn),
-            params=np.ascontiguousarray(self.params if len(self.params) else np.zeros(1)),
-        )
-        k = self._keep
-        dd = N.DomainDesc(self.code.handle, mesh.etype.nnode, lay.n, mesh.n_elem, k["conn"].ctypes.data,
-                          k["lnode"].ctypes.data, k["lval"].ctypes.data, k["tables"].ctypes.data,
-                          k["tables"].size, self.kernel.epb, self.kernel.threads, self.kernel.smem_bytes)
-        self._domains = (N.DomainDesc * 1)(dd)
-        desc = N.ProblemDesc(mesh.dim, n, nval, k["x"].ctypes.data, k["eqn"].ctypes.data, self.n_dof, 1,
-                             self._domains, len(self.params), k["params"].ctypes.data,
-                             N.FE_JAC_F64 if prec == "f64" else N.FE_JAC_F32)
+        desc, self._domains, self._keep = self._descriptors(with_code=True)
         h = ctypes.c_void_p()
         N.check(L.fe_problem_create(ctypes.byref(desc), ctypes.byref(h)))
         self._h = h
@@ -235,6 +219,41 @@ class Problem:
         t4 = time.perf_counter()
         self.timings.update(jit_s=t3 - t2, device_setup_s=t4 - t3)
         self._initialised = True
+
+    def _descriptors(self, with_code: bool):
+        mesh = self.mesh
+        lay = self.kernel.layout
+        keep = dict(
+            conn=np.ascontiguousarray(mesh.conn, dtype=np.int32),
+            lnode=np.ascontiguousarray(lay.node, dtype=np.int32),
+            lval=np.ascontiguousarray(lay.val, dtype=np.int32),
+            tables=np.ascontiguousarray(self.kernel.tables, dtype=np.float64),
+            x=np.ascontiguousarray(mesh.x, dtype=np.float64),
+            eqn=np.ascontiguousarray(self.eqn),
+            params=np.ascontiguousarray(self.params if len(self.params) else np.zeros(1)),
+        )
+        k = keep
+        dd = N.DomainDesc(self.code.handle if with_code else None, mesh.etype.nnode, lay.n, mesh.n_elem,
+                          k["conn"].ctypes.data, k["lnode"].ctypes.data, k["lval"].ctypes.data,
+                          k["tables"].ctypes.data, k["tables"].size, self.kernel.epb, self.kernel.threads,
+                          self.kernel.smem_bytes)
+        doms = (N.DomainDesc * 1)(dd)
+        desc = N.ProblemDesc(mesh.dim, mesh.n_nodes, len(self.fields), k["x"].ctypes.data, k["eqn"].ctypes.data,
+                             self.n_dof, 1, doms, len(self.params), k["params"].ctypes.data,
+                             N.FE_JAC_F64 if self._prec == "f64" else N.FE_JAC_F32)
+        return desc, doms, keep
+
+    def host_pattern(self) -> Tuple[np.ndarray, np.ndarray]:
+        """The CSR pattern built on the host only (fe_pattern_host; no GPU)."""
+        self.lower()
+        desc, doms, keep = self._descriptors(with_code=False)
+        L = N.load()
+        nnz = ctypes.c_int64()
+        N.check(L.fe_pattern_host(ctypes.byref(desc), ctypes.byref(nnz), None, None))
+        rp = np.zeros(self.n_dof + 1, dtype=np.int32)
+        ci = np.zeros(max(nnz.value, 1), dtype=np.int32)
+        N.check(L.fe_pattern_host(ctypes.byref(desc), None, rp.ctypes.data, ci.ctypes.data))
+        return rp, ci[:nnz.value]
 
     def _dofs_from_values(self, values: np.ndarray) -> np.ndarray:
         x = np.zeros(self.n_dof)

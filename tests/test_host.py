@@ -127,3 +127,51 @@ def test_pointwise_derivatives_match_finite_differences():
         assert abs(fd - exact) <= 1e-6 * max(1.0, abs(exact))
     # Taylor-Hood: 2 velocity comps x 3 + pressure x 3 test components
     assert pw.ntc == 9 and len(pw.d_entries) > 0
+
+
+def _product_for_golden(g):
+    from pyoomph_gb300 import workloads as W
+    et, eq = int(g["etype"]), int(g["eq"])
+    nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
+    if eq == O.EQ_NAVIER_STOKES_TH:
+        return W.navier_stokes_problem(N=[nx, ny], Re=1.0 / float(g["params"][1]),
+                                       split="left" if int(g["split"]) == 0 else "right")
+    dim = 3 if et == O.Q2_HEX else 2
+    gauss = g["params"][1:].reshape(int(g["params"][0]), dim + 2)
+    if eq == O.EQ_POISSON:
+        return W.poisson_problem(N=[nx, ny], gaussians=gauss, split=None if et == O.Q2_QUAD else "left")
+    return W.nonlinear_diffusion_problem(N=[nx, ny, nz] if dim == 3 else [nx, ny], gaussians=gauss, dim=dim)
+
+
+GOLD_CASES = [c for c in sorted(__import__("glob").glob(os.path.join(GOLD, "*_*.npz")))
+              if not c.endswith("oomph_tables.npz")]
+
+
+@pytest.mark.parametrize("path", GOLD_CASES, ids=[os.path.basename(c)[:-4] for c in GOLD_CASES])
+def test_host_pattern_and_numbering_bit_exact_vs_reference(path):
+    """The engine's CSR pattern (built by the C-ABI on the host) and equation
+    numbering against the reference's own oomph-lib (structural pattern)."""
+    g = np.load(path)
+    P = _product_for_golden(g)
+    P.lower()
+    assert np.array_equal(P.eqn, g["eqn"])
+    assert np.array_equal(P._values0[P.pinned], g["values"][P.pinned])
+    rp, ci = P.host_pattern()
+    assert np.array_equal(rp, g["rowptr_st"])
+    assert np.array_equal(ci, g["colidx_st"])
+
+
+@pytest.mark.parametrize("kind", ["ns", "hex"])
+def test_host_pattern_vs_oracle_larger(kind):
+    from pyoomph_gb300 import workloads as W
+    if kind == "ns":
+        P = W.navier_stokes_problem(N=[13, 11])
+        OP = O.navier_stokes_problem(O.mesh(O.P2_TRI, 13, 11))
+    else:
+        P = W.nonlinear_diffusion_problem(N=[4, 3, 5])
+        OP = O.poisson_problem(O.mesh(O.Q2_HEX, 4, 3, 5), np.array([[0.5, 0.5, 0.5, 0.1, 1.0]]),
+                               eq=O.EQ_NONLINEAR_DIFFUSION)
+    rp, ci = P.host_pattern()
+    assert np.array_equal(P.eqn, OP.eqn)
+    R, rp0, ci0, v0 = O.assemble(OP, True, -1.0)
+    assert np.array_equal(rp, rp0) and np.array_equal(ci, ci0)
