@@ -165,6 +165,32 @@ int fe_assemble_host(fe_problem_t *p, const double *dofs, double *R, void *J_val
 /* max |R| over n entries of a device vector, NaN -> +inf; result to host. */
 int fe_residual_max(fe_problem_t *p, const double *R, int64_t n, double *out, void *stream);
 
+/*
+ * Allocation-free residual max-norm.  No counterpart in the reference: it is
+ * an addition of this library for callers that cannot allocate device
+ * memory.  fe_residual_max needs a problem handle, and creating one
+ * allocates (mesh, CSR, element buffers).  A caller that only holds a
+ * residual vector in device memory and may not call cudaMalloc -- for
+ * example code that owns all device memory through its own pool, or code
+ * that must not allocate between set-up and shutdown -- uses this instead.
+ *
+ * Same result as fe_residual_max: max |R[i]| over n entries of the device
+ * vector R, NaN -> +inf, written to the host double *out; synchronises the
+ * stream (cudaStream_t, NULL = legacy default stream).
+ *
+ * It allocates nothing: its scratch is a static device array of 256 KiB
+ * that every GPU loading the library holds until the process exits.  n may
+ * be at most fe_residual_max_noalloc_limit() (268,427,264 entries); larger
+ * n is rejected with FE_ERR_ARG and a message.  The first call on a device
+ * looks up the array's device address with that device current; make that
+ * first call before any stream capture.  All calls share the array and the
+ * last call's contents stay in it: calls that overlap on the GPU (other
+ * streams or threads) race and must be serialised by the caller.
+ */
+int fe_residual_max_noalloc(const double *R, int64_t n, double *out, void *stream);
+/* Largest n fe_residual_max_noalloc accepts. */
+int64_t fe_residual_max_noalloc_limit(void);
+
 /* x[i] -= dx[i] for device vectors (the Newton update). */
 int fe_dof_update(fe_problem_t *p, double *x, const double *dx, int64_t n, void *stream);
 

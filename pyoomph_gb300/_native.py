@@ -25,7 +25,8 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_problem_create", "fe_problem_destroy", "fe_problem_sizes", "fe_problem_pattern",
            "fe_problem_pattern_device", "fe_problem_set_values", "fe_problem_get_values",
            "fe_problem_set_params", "fe_assemble", "fe_assemble_host", "fe_residual_max", "fe_dof_update",
-           "fe_problem_check", "fe_problem_launch_count", "fe_problem_set_timing", "fe_problem_stage_times", "fe_pattern_host"]
+           "fe_problem_check", "fe_problem_launch_count", "fe_problem_set_timing", "fe_problem_stage_times", "fe_pattern_host",
+           "fe_residual_max_noalloc", "fe_residual_max_noalloc_limit"]
 
 
 class FeError(RuntimeError):
@@ -114,6 +115,8 @@ def load(build_if_missing: bool = True):
         L.fe_problem_set_timing.argtypes = [vp, c_int]
         L.fe_problem_stage_times.argtypes = [vp, vp, vp]
         L.fe_pattern_host.argtypes = [ctypes.POINTER(ProblemDesc), vp, vp, vp]
+        L.fe_residual_max_noalloc.argtypes = [vp, i64, vp, vp]
+        L.fe_residual_max_noalloc_limit.restype = i64
         _lib = L
         return L
 

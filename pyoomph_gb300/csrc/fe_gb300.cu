@@ -25,6 +25,7 @@
 #include <cstring>
 #include <fstream>
 #include <memory>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <thread>
@@ -534,6 +535,79 @@ int launch_elements(fe_problem *p, int flag, cudaStream_t st) {
 } // namespace
 
 // ---------------------------------------------------------------------------
+// Allocation-free residual max-norm (fe_residual_max_noalloc).
+//
+// Its scratch (per-block partial maxima plus the result slot) is this
+// file-scope device array, so the call itself allocates nothing.  Every GPU
+// that loads the library holds these 256 KiB until the process exits.  All
+// calls share the array: calls that overlap on the GPU race on it.  The
+// kernels overwrite every partial they later read, so nothing has to be
+// cleared between calls.
+// ---------------------------------------------------------------------------
+#define FE_NOALLOC_SLOTS 32768             // doubles in the scratch array (256 KiB)
+#define FE_NOALLOC_ITEMS 8192              // residual entries reduced by one block
+#define FE_NOALLOC_MAX_N ((long long)(FE_NOALLOC_SLOTS - 1) * FE_NOALLOC_ITEMS)
+
+static __device__ __align__(256) double g_noalloc_scratch[FE_NOALLOC_SLOTS];
+
+__global__ void k_absmax_noalloc_blocks(const double *__restrict__ R, long long n, double *__restrict__ part) {
+  __shared__ double sm[32];
+  const long long b0 = (long long)blockIdx.x * FE_NOALLOC_ITEMS;
+  const long long b1 = b0 + FE_NOALLOC_ITEMS < n ? b0 + FE_NOALLOC_ITEMS : n;
+  double m = 0.0;
+  for (long long i = b0 + threadIdx.x; i < b1; i += blockDim.x) m = fmax(m, absnan(R[i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) part[blockIdx.x] = m;
+  }
+}
+
+__global__ void k_absmax_noalloc_final(const double *__restrict__ part, int nb, double *__restrict__ result) {
+  __shared__ double sm[32];
+  double m = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) m = fmax(m, part[i]);
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) *result = m;
+  }
+}
+
+namespace {
+// Device address of g_noalloc_scratch, looked up once per device with that
+// device current.  In host code the symbol itself is only a host-side
+// stand-in, never a device address.
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double *g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+int noalloc_scratch(double **ptr) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(FE_ERR_NOGPU, "no CUDA device: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return fail(FE_ERR_ARG, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(FE_ERR_CUDA, "cudaGetSymbolAddress(g_noalloc_scratch) on device %d: %s", dev,
+                  cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = static_cast<double *>(p);
+  }
+  *ptr = g_noalloc_ptr[dev];
+  return FE_OK;
+}
+} // namespace
+
+// ---------------------------------------------------------------------------
 // C-ABI
 // ---------------------------------------------------------------------------
 extern "C" {
@@ -870,6 +944,34 @@ int fe_residual_max(fe_problem_t *p, const double *R, int64_t n, double *out, vo
   CUDA_TRY(cudaStreamSynchronize(st));
   return FE_OK;
 }
+
+int fe_residual_max_noalloc(const double *R, int64_t n, double *out, void *stream) {
+  if (!out || (n > 0 && !R)) return fail(FE_ERR_ARG, "fe_residual_max_noalloc: null argument");
+  if (n < 0) return fail(FE_ERR_ARG, "fe_residual_max_noalloc: negative length %lld", (long long)n);
+  if (n > FE_NOALLOC_MAX_N)
+    return fail(FE_ERR_ARG,
+                "fe_residual_max_noalloc: n=%lld exceeds the maximum %lld of the static scratch; "
+                "use fe_residual_max",
+                (long long)n, FE_NOALLOC_MAX_N);
+  if (n == 0) {
+    *out = 0.0;
+    return FE_OK;
+  }
+  double *scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nb = (int)((n + FE_NOALLOC_ITEMS - 1) / FE_NOALLOC_ITEMS);
+  double *result = scratch + (FE_NOALLOC_SLOTS - 1);
+  k_absmax_noalloc_blocks<<<nb, 256, 0, st>>>(R, n, scratch);
+  k_absmax_noalloc_final<<<1, 1024, 0, st>>>(scratch, nb, result);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(out, result, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return FE_OK;
+}
+
+int64_t fe_residual_max_noalloc_limit(void) { return (int64_t)FE_NOALLOC_MAX_N; }
 
 int fe_dof_update(fe_problem_t *p, double *x, const double *dx, int64_t n, void *stream) {
   if (!p || (n > 0 && (!x || !dx))) return fail(FE_ERR_ARG, "null argument");
