@@ -131,6 +131,27 @@ def element_algorithmic_bytes(P) -> int:
                + m.n_elem * nl * 8 + m.n_elem * nl * nl * jb)
 
 
+def fp64_peak_tflops(torch) -> float:
+    """FP64 denominator measured in this run: cuBLAS DGEMM 4096^3, best of 5."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(5):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    return 2.0 * n ** 3 / best / 1e12
+
+
 def time_steps(torch, fn, steps: int, warmup: int):
     for _ in range(warmup):
         fn()
@@ -198,6 +219,8 @@ def run_gb300(args):
         torch.cuda.synchronize()
         results[prec] = dict(P=P, ms=ms, stage_ms=stage_ms, ms_e2e=ms_e2e, clocks=cs.summary(),
                              h2d=int(P.n_dof * 8), d2h=int(P.n_dof * 8 + P.nnz * P.J_dev.element_size()))
+    from pyoomph_gb300.codegen import estimate_flops
+    peak64 = fp64_peak_tflops(torch)
     main = results["fp64"]
     P = main["P"]
     n_elem = P.mesh.n_elem
@@ -229,6 +252,13 @@ def run_gb300(args):
         "roofline": {"bound": "hbm", "kernel": P.kernel.name, "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": abytes, "traffic": None},
+        "compute_roofline": {"pipe": "fp64", "kernel": P.kernel.name,
+                             "flops_per_element": estimate_flops(P.kernel, P.affine)["fp64"],
+                             "achieved": estimate_flops(P.kernel, P.affine)["fp64"] * n_elem / (elem_ms / 1e3) / 1e12,
+                             "peak": peak64, "unit": "TFLOP/s",
+                             "frac": estimate_flops(P.kernel, P.affine)["fp64"] * n_elem / (elem_ms / 1e3) / 1e12 / peak64,
+                             "peak_kind": "measured in this run: cuBLAS DGEMM 4096^3 (torch.matmul float64)",
+                             "flops": "counted from the generated kernel's operation structure, FMA = 2"},
         "e2e": {"value": n_elem * world / (main["ms_e2e"] / 1e3), "unit": "elements/s",
                 "h2d_bytes_per_step": main["h2d"], "d2h_bytes_per_step": main["d2h"],
                 "ms_per_step": main["ms_e2e"]},
@@ -236,8 +266,11 @@ def run_gb300(args):
         "clocks": main["clocks"],
     }
     r32 = results["fp32"]
+    f32 = estimate_flops(r32["P"].kernel, r32["P"].affine)
     line["fp32_jacobian"] = {"value": n_elem * world / (r32["ms"] / 1e3), "unit": "elements/s",
                              "ms_per_step": r32["ms"], "element_kernel_ms": float(r32["stage_ms"][1]),
+                             "fp64_tflops": f32["fp64"] * n_elem / (float(r32["stage_ms"][1]) / 1e3) / 1e12,
+                             "fp32_tflops": f32["jac"] * n_elem / (float(r32["stage_ms"][1]) / 1e3) / 1e12,
                              "e2e": {"value": n_elem * world / (r32["ms_e2e"] / 1e3),
                                      "h2d_bytes_per_step": r32["h2d"], "d2h_bytes_per_step": r32["d2h"]}}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -38,11 +38,19 @@ from .spaces import ElementType, Layout, make_layout
 
 
 class _Printer(C99CodePrinter):
-    """C printer: small integer powers as products, exp/sqrt as libm calls."""
+    """C printer: small integer powers as products, libm calls; with
+    ``fp32`` every literal and call is single precision."""
 
-    def __init__(self, names: Dict[sp.Symbol, str]):
+    def __init__(self, names: Dict[sp.Symbol, str], fp32: bool = False):
         super().__init__()
         self._names = names
+        self._fp32 = fp32
+
+    def _lit(self, v: float) -> str:
+        return f"{v!r}f" if self._fp32 else repr(v)
+
+    def _fn(self, name: str) -> str:
+        return name + "f" if self._fp32 else name
 
     def _print_Symbol(self, s):
         if s in self._names:
@@ -51,34 +59,49 @@ class _Printer(C99CodePrinter):
 
     def _print_Pow(self, e):
         b, x = e.args
+        one = self._lit(1.0)
         if x.is_Integer:
             n = int(x)
             if n == 2:
                 bs = self._print(b)
                 return f"(({bs})*({bs}))"
             if n == -1:
-                return f"(1.0/({self._print(b)}))"
+                return f"({one}/({self._print(b)}))"
             if n == -2:
                 bs = self._print(b)
-                return f"(1.0/(({bs})*({bs})))"
+                return f"({one}/(({bs})*({bs})))"
             if 2 < n <= 4:
                 bs = self._print(b)
                 return "(" + "*".join([f"({bs})"] * n) + ")"
         if x == sp.Rational(1, 2):
-            return f"sqrt({self._print(b)})"
-        return f"pow({self._print(b)}, {self._print(x)})"
+            return f"{self._fn('sqrt')}({self._print(b)})"
+        return f"{self._fn('pow')}({self._print(b)}, {self._print(x)})"
+
+    def _print_GaussianSum(self, e):
+        k0 = next(i for i, a in enumerate(e.args) if a.is_Integer)
+        n, dim = int(e.args[k0]), int(e.args[k0 + 1])
+        refs = [self._names.get(a, "") for a in e.args[k0 + 2:]]
+        idx = [int(r[r.index("[") + 1:-1]) if r.endswith("]") else -1 for r in refs]
+        if self._fp32 or len(idx) != n * (dim + 2) or idx != list(range(idx[0], idx[0] + len(idx))):
+            raise NotImplementedError("GaussianSum needs its parameters contiguous in the FP64 array")
+        base = refs[0][:refs[0].index("[")]
+        xq = self._names[E.X[0]][:self._names[E.X[0]].index("[")]
+        return f"fe_gauss_sum<{dim}>({xq}, {base} + {idx[0]}, {n})"
+
+    def _print_exp(self, e):
+        return f"{self._fn('exp')}({self._print(e.args[0])})"
 
     def _print_Rational(self, e):
-        return f"({float(e.p)!r}/{float(e.q)!r})"
+        return f"({self._lit(float(e.p))}/{self._lit(float(e.q))})"
 
     def _print_Float(self, e):
-        return repr(float(e))
+        return self._lit(float(e))
 
     def _print_Integer(self, e):
-        return f"{float(int(e))!r}"
+        return self._lit(float(int(e)))
 
     def _print_Pi(self, e):
-        return "3.141592653589793"
+        return self._lit(3.141592653589793)
 
 
 @dataclass
@@ -122,43 +145,73 @@ def differentiate(fields: List[Tuple[str, str]], dim: int, integrand: sp.Expr,
     return Pointwise(fields, dim, params, r_exprs, d_entries, uses_x)
 
 
-def _symbol_names(pw: Pointwise) -> Dict[sp.Symbol, str]:
+def _symbol_names(pw: Pointwise, prefix: str = "") -> Dict[sp.Symbol, str]:
     names = {}
     nc = 1 + pw.dim
     for f, (name, _) in enumerate(pw.fields):
-        names[E.REG.value[name]] = f"U[{f * nc}]"
+        names[E.REG.value[name]] = f"{prefix}U[{f * nc}]"
         for i in range(pw.dim):
-            names[E.REG.grad[name][i]] = f"U[{f * nc + 1 + i}]"
+            names[E.REG.grad[name][i]] = f"{prefix}U[{f * nc + 1 + i}]"
     for i in range(3):
-        names[E.X[i]] = f"Xq[{i}]"
+        names[E.X[i]] = f"{prefix}Xq[{i}]"
     for k, p in enumerate(pw.params):
-        names[E.parameter(p)] = f"P[{k}]"
+        names[E.parameter(p)] = f"{prefix}P[{k}]"
     return names
 
 
-def pointwise_source(pw: Pointwise) -> str:
-    """The generated device function fe_pointwise(U, Xq, P, r, D, flag)."""
-    names = _symbol_names(pw)
-    pr = _Printer(names)
-    lines = ["__device__ __forceinline__ void fe_pointwise(const double* __restrict__ U, "
-             "const double* __restrict__ Xq, const double* __restrict__ P, double* __restrict__ r, "
-             "double* __restrict__ D, int flag) {"]
-    exprs = list(pw.r_exprs)
-    n_r = len(exprs)
-    exprs += [d for (_, _, d) in pw.d_entries]
+def _emit(exprs, names, fp32: bool, outs, indent="  "):
+    real = "float" if fp32 else "double"
+    pr = _Printer(dict(names), fp32=fp32)
     repl, reduced = sp.cse(exprs, symbols=sp.numbered_symbols("t_"), optimizations="basic")
-    for s, e in repl:
-        names[s] = s.name
-    for s, e in repl:
-        lines.append(f"  const double {s.name} = {pr.doprint(e)};")
-    for k in range(n_r):
-        lines.append(f"  r[{k}] = {pr.doprint(reduced[k])};")
-    if pw.d_entries:
-        lines.append("  if (flag) {")
-        for k in range(len(pw.d_entries)):
-            lines.append(f"    D[{k}] = {pr.doprint(reduced[n_r + k])};")
-        lines.append("  }")
+    lines = []
+    for s_, e in repl:
+        pr._names[s_] = s_.name
+    for s_, e in repl:
+        lines.append(f"{indent}const {real} {s_.name} = {pr.doprint(e)};")
+    for o, e in zip(outs, reduced):
+        lines.append(f"{indent}{o} = {pr.doprint(e)};")
+    return lines
+
+
+def pointwise_source(pw: Pointwise, jreal: str = "double") -> str:
+    """The generated device functions.
+
+    ``fe_pointwise(U, Xq, P, r, D, flag)`` computes the residual coefficients
+    r in FP64 and, when jreal is double, the derivatives D too (sharing the
+    common subexpressions).  With jreal float, D comes from the separate
+    single-precision ``fe_pointwise_jac(U, Xq, P, D)``: the Jacobian then
+    costs no FP64 instructions."""
+    names = _symbol_names(pw)
+    nr = len(pw.r_exprs)
+    nd = len(pw.d_entries)
+    hdr = ("__device__ __forceinline__ void fe_pointwise(const double* __restrict__ U, "
+           "const double* __restrict__ Xq, const double* __restrict__ P, double* __restrict__ r, "
+           "jreal* __restrict__ D, int flag) {")
+    lines = [hdr]
+    if jreal == "double" and nd:
+        exprs = list(pw.r_exprs) + [d for (_, _, d) in pw.d_entries]
+        outs = [f"r[{k}]" for k in range(nr)] + [f"D[{k}]" for k in range(nd)]
+        body = _emit(exprs, names, False, outs, "  ")
+        # D assignments only when flag: move them under the branch
+        rl = [l for l in body if not l.strip().startswith("D[")]
+        dl = [l for l in body if l.strip().startswith("D[")]
+        lines += rl + ["  if (flag) {"] + ["  " + l for l in dl] + ["  }"]
+    else:
+        lines += _emit(list(pw.r_exprs), names, False, [f"r[{k}]" for k in range(nr)], "  ")
     lines.append("}")
+    if jreal != "double":
+        fl = _symbol_names(pw, prefix="f")
+        lines.append("__device__ __forceinline__ void fe_pointwise_jac(const double* __restrict__ U, "
+                     "const double* __restrict__ Xq, const double* __restrict__ P, float* __restrict__ D) {")
+        nc = 1 + pw.dim
+        lines.append(f"  float fU[{max(1, len(pw.fields) * nc)}]; float fXq[3]; float fP[{max(1, len(pw.params))}];")
+        lines.append(f"  #pragma unroll\n  for (int k = 0; k < {len(pw.fields) * nc}; ++k) fU[k] = (float)U[k];")
+        lines.append("  fXq[0] = (float)Xq[0]; fXq[1] = (float)Xq[1]; fXq[2] = (float)Xq[2];")
+        if pw.params:
+            lines.append(f"  #pragma unroll\n  for (int k = 0; k < {len(pw.params)}; ++k) fP[k] = (float)P[k];")
+        if nd:
+            lines += _emit([d for (_, _, d) in pw.d_entries], fl, True, [f"D[{k}]" for k in range(nd)], "  ")
+        lines.append("}")
     return "\n".join(lines)
 
 
@@ -181,7 +234,7 @@ class KernelSpec:
 
 
 def _launch_shape(et: ElementType, nloc: int, per_elem_bytes: int, table_bytes: int,
-                  smem_cap: int = 200 * 1024) -> Tuple[int, int]:
+                  smem_cap: int = 200 * 1024, max_threads: int = 512) -> Tuple[int, int]:
     """Elements per block and threads: keep both thread phases (element x
     integration point, element x row) busy in whole warps, within the
     shared-memory budget."""
@@ -192,7 +245,7 @@ def _launch_shape(et: ElementType, nloc: int, per_elem_bytes: int, table_bytes: 
             break
         work = max(epb * et.nq, epb * nloc)
         threads = ((work + 31) // 32) * 32
-        if threads > 1024:
+        if threads > max_threads:
             break
         # prefer whole-warp phases and larger blocks
         waste = (threads - epb * et.nq) / threads + (threads - epb * nloc) / threads
@@ -205,7 +258,21 @@ def _launch_shape(et: ElementType, nloc: int, per_elem_bytes: int, table_bytes: 
 
 
 def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
-                    name: str = None, epb: int = None) -> KernelSpec:
+                    name: str = None, epb: int = None, affine: bool = False) -> KernelSpec:
+    """Fused element kernel for one element type and weak form.
+
+    Thread phases (all in one launch, EPB elements per block):
+      0. stage reference tables and the elements' nodal positions/values in
+         shared memory;
+      G. (affine elements only) geometry once per element;
+      A. one thread per (element, integration point): geometry (unless
+         affine), interpolation, pointwise residual coefficients (FP64,
+         pulled back to reference coordinates) and derivatives D (Jacobian
+         precision), physical shape gradients for the Jacobian;
+      B. one thread per (element, local row), rows ordered field-major so a
+         warp shares its test field: R_i = sum_q rhat . phi_i and
+         J_ij = sum_q phi_i^T D psi_j, written to the element buffers.
+    """
     dim, nn, nn1, nq = et.dim, et.nnode, et.nnode_c1, et.nq
     fields = pw.fields
     nf = len(fields)
@@ -215,13 +282,15 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     layout = make_layout(et, spaces)
     nloc = layout.n
     nval = nf
-    has_c1 = any(s == "C1" for s in spaces)
+    has_c1 = any(s_ == "C1" for s_ in spaces)
     ndnz = max(1, len(pw.d_entries))
     jreal = "double" if jac_precision == "f64" else "float"
     jbytes = 8 if jac_precision == "f64" else 4
     table_doubles = nq + nq * nn + nq * nn * dim + nq * nn1 + nq * nn1 * dim
     table_bytes = table_doubles * 8
-    per_elem = (nn * dim + nn * nval + nq * ntc) * 8 + (nq * ndnz + nq * nn * dim + (nq * nn1 * dim if has_c1 else 0)) * jbytes
+    geo_doubles = (dim * dim + 1) if affine else 0
+    per_elem = ((nn * dim + nn * nval + nq * ntc + geo_doubles) * 8
+                + (nq * ndnz + nq * nn * dim + (nq * nn1 * dim if has_c1 else 0)) * jbytes)
     if epb is None:
         epb, threads = _launch_shape(et, nloc, per_elem, table_bytes)
     else:
@@ -229,10 +298,13 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     smem = table_bytes + epb * per_elem
     smem = (smem + 15) // 16 * 16
     if name is None:
-        h = hashlib.sha1((et.name + jac_precision + str(pw.r_exprs) + str(pw.d_entries)).encode()).hexdigest()[:10]
-        name = f"fe_elem_{et.name.lower()}_{jac_precision}_{h}"
+        h = hashlib.sha1((et.name + jac_precision + str(affine) + str(pw.r_exprs) + str(pw.d_entries)).encode()
+                         ).hexdigest()[:10]
+        name = f"fe_elem_{et.name.lower()}_{jac_precision}{'_aff' if affine else ''}_{h}"
 
-    # trial components that carry any D entry, per field
+    nsub = [nn if s_ == "C2" else nn1 for s_ in spaces]
+    loc_of_flat = [layout.loc_of[f][k] for f in range(nf) for k in range(nsub[f])]
+    loc_off = [sum(nsub[:f]) for f in range(nf)]
     used_ic = sorted({ic for (_, ic, _) in pw.d_entries})
     src = []
     w = src.append
@@ -240,13 +312,11 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w('#include "fe_device.cuh"')
     w(f"#define FE_DIM {dim}\n#define FE_NN {nn}\n#define FE_NN1 {nn1}\n#define FE_NQ {nq}")
     w(f"#define FE_NVAL {nval}\n#define FE_NLOC {nloc}\n#define FE_EPB {epb}\n#define FE_NT {threads}")
-    w(f"#define FE_NF {nf}\n#define FE_NTC {ntc}\n#define FE_NDNZ {ndnz}")
+    w(f"#define FE_NF {nf}\n#define FE_NTC {ntc}\n#define FE_NDNZ {ndnz}\n#define FE_AFFINE {1 if affine else 0}")
     w(f"typedef {jreal} jreal;")
-    w(f"__constant__ int c_loc_field[FE_NLOC] = {{{', '.join(map(str, layout.field))}}};")
-    w(f"__constant__ int c_loc_sub[FE_NLOC] = {{{', '.join(map(str, layout.sub))}}};")
-    w(f"__constant__ int c_fspace1[FE_NF] = {{{', '.join('1' if s == 'C1' else '0' for s in spaces)}}};")
+    w(f"__constant__ int c_loc_of[{len(loc_of_flat)}] = {{{', '.join(map(str, loc_of_flat))}}};")
     w(f"__constant__ int c_c1idx[FE_NN1] = {{{', '.join(map(str, et.c1_index))}}};")
-    w(pointwise_source(pw))
+    w(pointwise_source(pw, jreal))
     w(f'extern "C" __global__ void __launch_bounds__(FE_NT) {name}(const FeElemArgs a) {{')
     w("  extern __shared__ __align__(16) unsigned char fe_smem[];")
     w("  double* sW = reinterpret_cast<double*>(fe_smem);")
@@ -257,10 +327,11 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("  double* sX = sDps1 + FE_NQ * FE_NN1 * FE_DIM;")
     w("  double* sU = sX + FE_EPB * FE_NN * FE_DIM;")
     w("  double* sRh = sU + FE_EPB * FE_NN * FE_NVAL;")
-    w("  jreal* sD = reinterpret_cast<jreal*>(sRh + FE_EPB * FE_NQ * FE_NTC);")
+    w("  double* sG = sRh + FE_EPB * FE_NQ * FE_NTC;")
+    w(f"  jreal* sD = reinterpret_cast<jreal*>(sG + FE_EPB * {geo_doubles});")
     w("  jreal* sDx2 = sD + FE_EPB * FE_NQ * FE_NDNZ;")
     w("  jreal* sDx1 = sDx2 + FE_EPB * FE_NQ * FE_NN * FE_DIM;")
-    w("  (void)sDx1;")
+    w("  (void)sDx1; (void)sG;")
     w("  const long long e0 = (long long)blockIdx.x * FE_EPB;")
     w("  const long long rem = a.n_elem - e0;")
     w("  const int nel = rem < FE_EPB ? (int)rem : FE_EPB;")
@@ -275,28 +346,60 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    for (int v = 0; v < FE_NVAL; ++v) sU[k * FE_NVAL + v] = a.values[(long long)node * a.nval + v];")
     w("  }")
     w("  __syncthreads();")
+    if affine:
+        # ---------------- phase G: constant geometry of affine elements ----------------
+        w("  for (int el = threadIdx.x; el < nel; el += FE_NT) {")
+        w("    double g[FE_DIM][FE_DIM]; double J;")
+        w("    fe_metric_geometry<FE_DIM, FE_NN>(sX + el * FE_NN * FE_DIM, sDps2, g, J);")
+        w("    if (!(J > 0.0)) atomicExch(a.status, 1);")
+        w("    double* sg = sG + el * (FE_DIM * FE_DIM + 1);")
+        w("    #pragma unroll")
+        w("    for (int b = 0; b < FE_DIM; ++b)")
+        w("      #pragma unroll")
+        w("      for (int i = 0; i < FE_DIM; ++i) sg[b * FE_DIM + i] = g[b][i];")
+        w("    sg[FE_DIM * FE_DIM] = J;")
+        w("  }")
+        w("  __syncthreads();")
     # ---------------- phase A ----------------
     w("  for (int p = threadIdx.x; p < nel * FE_NQ; p += FE_NT) {")
     w("    const int el = p / FE_NQ, q = p - el * FE_NQ;")
     w("    const double* X = sX + el * FE_NN * FE_DIM;")
     w("    const double* dps = sDps2 + q * FE_NN * FE_DIM;")
     w("    double g[FE_DIM][FE_DIM]; double J;")
-    w("    fe_metric_geometry<FE_DIM, FE_NN>(X, dps, g, J);")
-    w("    if (!(J > 0.0)) atomicExch(a.status, 1);")
+    if affine:
+        w("    { const double* sg = sG + el * (FE_DIM * FE_DIM + 1);")
+        w("      #pragma unroll")
+        w("      for (int b = 0; b < FE_DIM; ++b)")
+        w("        #pragma unroll")
+        w("        for (int i = 0; i < FE_DIM; ++i) g[b][i] = sg[b * FE_DIM + i];")
+        w("      J = sg[FE_DIM * FE_DIM]; }")
+    else:
+        w("    fe_metric_geometry<FE_DIM, FE_NN>(X, dps, g, J);")
+        w("    if (!(J > 0.0)) atomicExch(a.status, 1);")
     w("    const double wq = sW[q] * J;")
     w("    double Xq[3] = {0.0, 0.0, 0.0};")
     if pw.uses_x:
-        w("    #pragma unroll")
-        w("    for (int l = 0; l < FE_NN; ++l) {")
-        w("      const double ps = sPsi2[q * FE_NN + l];")
-        w("      #pragma unroll")
-        w("      for (int i = 0; i < FE_DIM; ++i) Xq[i] += X[l * FE_DIM + i] * ps;")
-        w("    }")
+        if affine:
+            # the affine map is reproduced exactly by the vertex (C1) shapes
+            w("    #pragma unroll")
+            w("    for (int l = 0; l < FE_NN1; ++l) {")
+            w("      const double ps = sPsi1[q * FE_NN1 + l];")
+            w("      #pragma unroll")
+            w("      for (int i = 0; i < FE_DIM; ++i) Xq[i] += X[c_c1idx[l] * FE_DIM + i] * ps;")
+            w("    }")
+        else:
+            w("    #pragma unroll")
+            w("    for (int l = 0; l < FE_NN; ++l) {")
+            w("      const double ps = sPsi2[q * FE_NN + l];")
+            w("      #pragma unroll")
+            w("      for (int i = 0; i < FE_DIM; ++i) Xq[i] += X[l * FE_DIM + i] * ps;")
+            w("    }")
     w("    double U[FE_NTC];")
     for f, (fname, fsp) in enumerate(fields):
         base = f * nc
+        zeros = ", ".join(["0.0"] * dim)
+        w(f"    {{ double v = 0.0, gs[FE_DIM] = {{{zeros}}};")
         if fsp == "C2":
-            w(f"    {{ double v = 0.0, gs[FE_DIM] = {{{', '.join(['0.0'] * dim)}}};")
             w("      #pragma unroll")
             w("      for (int l = 0; l < FE_NN; ++l) {")
             w(f"        const double u = sU[(el * FE_NN + l) * FE_NVAL + {f}];")
@@ -305,7 +408,6 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w("        for (int b = 0; b < FE_DIM; ++b) gs[b] += u * dps[l * FE_DIM + b];")
             w("      }")
         else:
-            w(f"    {{ double v = 0.0, gs[FE_DIM] = {{{', '.join(['0.0'] * dim)}}};")
             w("      #pragma unroll")
             w("      for (int l = 0; l < FE_NN1; ++l) {")
             w(f"        const double u = sU[(el * FE_NN + c_c1idx[l]) * FE_NVAL + {f}];")
@@ -315,12 +417,12 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w("      }")
         w(f"      U[{base}] = v;")
         w("      #pragma unroll")
-        w(f"      for (int i = 0; i < FE_DIM; ++i) {{ double s = 0.0;")
+        w("      for (int i = 0; i < FE_DIM; ++i) { double s = 0.0;")
         w("        #pragma unroll")
-        w(f"        for (int b = 0; b < FE_DIM; ++b) s += g[b][i] * gs[b];")
+        w("        for (int b = 0; b < FE_DIM; ++b) s += g[b][i] * gs[b];")
         w(f"        U[{base} + 1 + i] = s; }}")
         w("    }")
-    w("    double r[FE_NTC]; double D[FE_NDNZ];")
+    w("    double r[FE_NTC]; jreal D[FE_NDNZ];")
     w("    fe_pointwise(U, Xq, a.params, r, D, flag);")
     w("    double* rh = sRh + (el * FE_NQ + q) * FE_NTC;")
     w("    #pragma unroll")
@@ -333,21 +435,31 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("        rh[f * (1 + FE_DIM) + 1 + b] = wq * s; }")
     w("    }")
     w("    if (flag) {")
+    if jreal == "float":
+        w("      fe_pointwise_jac(U, Xq, a.params, D);")
     w("      jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZ;")
+    w("      const jreal wj = (jreal)wq;")
     w("      #pragma unroll")
-    w("      for (int k = 0; k < FE_NDNZ; ++k) Dq[k] = (jreal)(wq * D[k]);")
+    w("      for (int k = 0; k < FE_NDNZ; ++k) Dq[k] = wj * D[k];")
     w("      fe_phys_grad<FE_DIM, FE_NN, jreal>(g, dps, sDx2 + (el * FE_NQ + q) * FE_NN * FE_DIM);")
     if has_c1:
         w("      fe_phys_grad<FE_DIM, FE_NN1, jreal>(g, sDps1 + q * FE_NN1 * FE_DIM, sDx1 + (el * FE_NQ + q) * FE_NN1 * FE_DIM);")
     w("    }")
     w("  }")
     w("  __syncthreads();")
-    # ---------------- phase B ----------------
+    # ---------------- phase B: field-major rows ----------------
     w("  for (int p = threadIdx.x; p < nel * FE_NLOC; p += FE_NT) {")
-    w("    const int el = p / FE_NLOC, i = p - el * FE_NLOC;")
-    w("    const int tf = c_loc_field[i], lt = c_loc_sub[i];")
-    w("    const int t1 = c_fspace1[tf];")
-    w("    const int tnn = t1 ? FE_NN1 : FE_NN;")
+    w("    int tf = 0, rel = p;")
+    for f in range(nf - 1):
+        w(f"    if (tf == {f} && rel >= nel * {nsub[f]}) {{ rel -= nel * {nsub[f]}; tf = {f + 1}; }}")
+    w("    int tn = 0, toff = 0;")
+    for f in range(nf):
+        w(f"    if (tf == {f}) {{ tn = {nsub[f]}; toff = {loc_off[f]}; }}")
+    w("    const int el = rel / tn, lt = rel - el * tn;")
+    w("    const int i = c_loc_of[toff + lt];")
+    w("    const int t1 = (tn == FE_NN1) && (FE_NN1 != FE_NN) ? 1 : 0;")
+    if not has_c1:
+        w("    (void)t1;")
     w("    const double* tpsi = t1 ? sPsi1 : sPsi2;")
     w("    const double* tdps = t1 ? sDps1 : sDps2;")
     w("    double Racc = 0.0;")
@@ -356,10 +468,10 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    for (int k = 0; k < FE_NLOC; ++k) Jr[k] = (jreal)0;")
     w("    for (int q = 0; q < FE_NQ; ++q) {")
     w("      const double* rh = sRh + (el * FE_NQ + q) * FE_NTC + tf * (1 + FE_DIM);")
-    w("      const double pv = tpsi[q * tnn + lt];")
+    w("      const double pv = tpsi[q * tn + lt];")
     w("      double racc = rh[0] * pv;")
     w("      #pragma unroll")
-    w("      for (int b = 0; b < FE_DIM; ++b) racc += rh[1 + b] * tdps[(q * tnn + lt) * FE_DIM + b];")
+    w("      for (int b = 0; b < FE_DIM; ++b) racc += rh[1 + b] * tdps[(q * tn + lt) * FE_DIM + b];")
     w("      Racc += racc;")
     w("      if (flag) {")
     w("        const jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZ;")
@@ -368,13 +480,17 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("        const jreal phi0 = (jreal)pv;")
     for d in range(dim):
         w(f"        const jreal phi{d + 1} = tdx[{d}];")
-    # a_ic accumulators
     for ic in used_ic:
         w(f"        jreal a{ic} = (jreal)0;")
-    for k, (tc, ic, _) in enumerate(pw.d_entries):
-        tfield, tcomp = divmod(tc, nc)
-        w(f"        a{ic} += (tf == {tfield}) ? phi{tcomp} * Dq[{k}] : (jreal)0;")
-    # j loop per trial field
+    # per test field: only its own D entries (warp-uniform branch)
+    for f in range(nf):
+        ents = [(k, tc, ic) for k, (tc, ic, _) in enumerate(pw.d_entries) if tc // nc == f]
+        if not ents:
+            continue
+        w(f"        if (tf == {f}) {{")
+        for k, tc, ic in ents:
+            w(f"          a{ic} += phi{tc % nc} * Dq[{k}];")
+        w("        }")
     for f, (fname, fsp) in enumerate(fields):
         comps = [ic for ic in used_ic if ic // nc == f]
         if not comps:
@@ -383,30 +499,22 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w("        {")
             w("          const double* psi = sPsi2 + q * FE_NN;")
             w("          const jreal* dx = sDx2 + (el * FE_NQ + q) * FE_NN * FE_DIM;")
-            for ls in range(nn):
-                terms = []
-                for ic in comps:
-                    c = ic % nc
-                    if c == 0:
-                        terms.append(f"a{ic} * (jreal)psi[{ls}]")
-                    else:
-                        terms.append(f"a{ic} * dx[{ls * dim + c - 1}]")
-                w(f"          Jr[{layout.loc_of[f][ls]}] += {' + '.join(terms)};")
-            w("        }")
+            cnt = nn
         else:
             w("        {")
             w("          const double* psi = sPsi1 + q * FE_NN1;")
             w("          const jreal* dx = sDx1 + (el * FE_NQ + q) * FE_NN1 * FE_DIM;")
-            for ls in range(nn1):
-                terms = []
-                for ic in comps:
-                    c = ic % nc
-                    if c == 0:
-                        terms.append(f"a{ic} * (jreal)psi[{ls}]")
-                    else:
-                        terms.append(f"a{ic} * dx[{ls * dim + c - 1}]")
-                w(f"          Jr[{layout.loc_of[f][ls]}] += {' + '.join(terms)};")
-            w("        }")
+            cnt = nn1
+        for ls in range(cnt):
+            terms = []
+            for ic in comps:
+                c = ic % nc
+                if c == 0:
+                    terms.append(f"a{ic} * (jreal)psi[{ls}]")
+                else:
+                    terms.append(f"a{ic} * dx[{ls * dim + c - 1}]")
+            w(f"          Jr[{layout.loc_of[f][ls]}] += {' + '.join(terms)};")
+        w("        }")
     w("      }")
     w("    }")
     w("    const long long row = (e0 + el) * FE_NLOC + i;")
@@ -422,3 +530,47 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     return KernelSpec(name=name, source=source, et=et, layout=layout, pointwise=pw, epb=epb,
                       threads=threads, smem_bytes=smem, jac_precision=jac_precision,
                       tables=et.packed_tables())
+
+
+def estimate_flops(ks: KernelSpec, affine: bool) -> Dict[str, float]:
+    """Floating-point operations per element of a generated kernel, counted
+    from its structure (an FMA counts 2).  Keys: ``fp64`` (geometry,
+    interpolation, pointwise residual, residual contraction; plus the
+    Jacobian when it is FP64) and ``jac`` (the Jacobian-only work, in the
+    Jacobian's precision)."""
+    et, pw, lay = ks.et, ks.pointwise, ks.layout
+    D, NN, N1, NQ = et.dim, et.nnode, et.nnode_c1, et.nq
+    nc = 1 + D
+    fields = pw.fields
+    geo = 2 * NN * D * D + 2 * D ** 3 + (D ** 3 + 10) + 2 * D ** 3 + 10
+    per_q = 0.0 if affine else geo
+    if pw.uses_x:
+        per_q += 2 * (N1 if affine else NN) * D
+    for _, s in fields:
+        n = NN if s == "C2" else N1
+        per_q += 2 * n * nc + 2 * D * D
+    ops_r = 0
+    for e in pw.r_exprs:
+        gs = list(e.atoms(E.GaussianSum))
+        for g in gs:
+            k0 = next(i for i, a in enumerate(g.args) if a.is_Integer)
+            ops_r += int(g.args[k0]) * (3 * D + 45)
+        ops_r += sp.count_ops(e.subs({g: 0 for g in gs}))
+    per_q += ops_r
+    per_q += len(fields) * (1 + 2 * D * D)
+    rows = lay.n
+    resid = rows * NQ * 2 * nc
+    fp64 = NQ * per_q + (geo if affine else 0) + resid
+    ops_d = sum(sp.count_ops(d) for (_, _, d) in pw.d_entries)
+    jac_q = ops_d + len(pw.d_entries) + 2 * NN * D * D + (2 * N1 * D * D if any(s == "C1" for _, s in fields) else 0)
+    used_ic = sorted({ic for (_, ic, _) in pw.d_entries})
+    per_row_q = 0.0
+    for f, (_, s) in enumerate(fields):
+        comps = [ic for ic in used_ic if ic // nc == f]
+        per_row_q += 2 * (NN if s == "C2" else N1) * len(comps)
+    a_ops = 2 * len(pw.d_entries) / max(1, len(fields))
+    jac = NQ * jac_q + rows * NQ * (per_row_q + a_ops)
+    out = {"fp64": float(fp64), "jac": float(jac)}
+    if ks.jac_precision == "f64":
+        out["fp64"] += out["jac"]
+    return out

@@ -46,22 +46,24 @@ __device__ __forceinline__ void fe_metric_geometry(const double *__restrict__ X,
     aup[0][0] = 1.0 / det;
   } else if constexpr (DIM == 2) {
     det = am[0][0] * am[1][1] - am[0][1] * am[1][0];
-    aup[0][0] = am[1][1] / det;
-    aup[0][1] = -am[0][1] / det;
-    aup[1][0] = -am[1][0] / det;
-    aup[1][1] = am[0][0] / det;
+    const double idet = 1.0 / det;
+    aup[0][0] = am[1][1] * idet;
+    aup[0][1] = -am[0][1] * idet;
+    aup[1][0] = -am[1][0] * idet;
+    aup[1][1] = am[0][0] * idet;
   } else {
     det = am[0][0] * am[1][1] * am[2][2] + am[0][1] * am[1][2] * am[2][0] + am[0][2] * am[1][0] * am[2][1] -
           am[0][0] * am[1][2] * am[2][1] - am[0][1] * am[1][0] * am[2][2] - am[0][2] * am[1][1] * am[2][0];
-    aup[0][0] = (am[1][1] * am[2][2] - am[1][2] * am[2][1]) / det;
-    aup[0][1] = -(am[0][1] * am[2][2] - am[0][2] * am[2][1]) / det;
-    aup[0][2] = (am[0][1] * am[1][2] - am[0][2] * am[1][1]) / det;
-    aup[1][0] = -(am[1][0] * am[2][2] - am[1][2] * am[2][0]) / det;
-    aup[1][1] = (am[0][0] * am[2][2] - am[0][2] * am[2][0]) / det;
-    aup[1][2] = -(am[0][0] * am[1][2] - am[0][2] * am[1][0]) / det;
-    aup[2][0] = (am[1][0] * am[2][1] - am[1][1] * am[2][0]) / det;
-    aup[2][1] = -(am[0][0] * am[2][1] - am[0][1] * am[2][0]) / det;
-    aup[2][2] = (am[0][0] * am[1][1] - am[0][1] * am[1][0]) / det;
+    const double idet = 1.0 / det;
+    aup[0][0] = (am[1][1] * am[2][2] - am[1][2] * am[2][1]) * idet;
+    aup[0][1] = -(am[0][1] * am[2][2] - am[0][2] * am[2][1]) * idet;
+    aup[0][2] = (am[0][1] * am[1][2] - am[0][2] * am[1][1]) * idet;
+    aup[1][0] = -(am[1][0] * am[2][2] - am[1][2] * am[2][0]) * idet;
+    aup[1][1] = (am[0][0] * am[2][2] - am[0][2] * am[2][0]) * idet;
+    aup[1][2] = -(am[0][0] * am[1][2] - am[0][2] * am[1][0]) * idet;
+    aup[2][0] = (am[1][0] * am[2][1] - am[1][1] * am[2][0]) * idet;
+    aup[2][1] = -(am[0][0] * am[2][1] - am[0][1] * am[2][0]) * idet;
+    aup[2][2] = (am[0][0] * am[1][1] - am[0][1] * am[1][0]) * idet;
   }
 #pragma unroll
   for (int b = 0; b < DIM; ++b)
@@ -98,6 +100,26 @@ __device__ __forceinline__ void fe_phys_grad(const double (&g)[DIM][DIM], const 
       out[l * DIM + i] = s;
     }
   }
+}
+
+// Sum of n Gaussians A exp(-|x-c|^2 / (2 w^2)); parameters per Gaussian:
+// c_0..c_{DIM-1}, w, A (contiguous).  A loop, not unrolled: it keeps the
+// element kernel's register footprint independent of n.
+template <int DIM>
+__device__ __noinline__ double fe_gauss_sum(const double *__restrict__ Xq, const double *__restrict__ g, int n) {
+  double f = 0.0;
+#pragma unroll 1
+  for (int k = 0; k < n; ++k, g += DIM + 2) {
+    double r2 = 0.0;
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      const double d = Xq[i] - g[i];
+      r2 += d * d;
+    }
+    const double w = g[DIM];
+    f += g[DIM + 1] * exp(-r2 / (2.0 * w * w));
+  }
+  return f;
 }
 
 #endif

@@ -202,12 +202,37 @@ def square_mag(v: Sequence) -> sp.Expr:
     return sum(c * c for c in v)
 
 
-def gaussian_source(n: int, dim: int, prefix: str = "g") -> sp.Expr:
-    """sum_k A_k exp(-|x - c_k|^2 / (2 w_k^2)) with the centres, widths and
-    amplitudes as global parameters ``{prefix}{k}_c{i}``, ``_w``, ``_A``."""
-    f = sp.Integer(0)
+class GaussianSum(sp.Function):
+    """sum_k A_k exp(-|x - c_k|^2 / (2 w_k^2)) over n Gaussians whose
+    centres, widths and amplitudes are the parameters g{k}_c{i}, g{k}_w,
+    g{k}_A (stored contiguously per Gaussian).  Arguments: the coordinate
+    symbols, n, dim, then the parameter symbols in array order.  The code
+    generator prints it as a call of the
+    device loop fe_gauss_sum<dim>, which keeps the kernel small; it depends
+    on the position only, so its derivative with respect to any field is 0."""
+
+    def fdiff(self, argindex=1):
+        raise NotImplementedError("GaussianSum has no coordinate derivative (fixed meshes only)")
+
+
+def gaussian_source(n: int, dim: int) -> sp.Expr:
+    ps = []
     for k in range(n):
-        r2 = sum((X[i] - parameter(f"{prefix}{k}_c{i}")) ** 2 for i in range(dim))
-        w = parameter(f"{prefix}{k}_w")
-        f += parameter(f"{prefix}{k}_A") * sp.exp(-r2 / (2 * w * w))
-    return f
+        for i in range(dim):
+            ps.append(parameter(f"g{k}_c{i}"))
+        ps.append(parameter(f"g{k}_w"))
+        ps.append(parameter(f"g{k}_A"))
+    return GaussianSum(*X[:dim], sp.Integer(n), sp.Integer(dim), *ps)
+
+
+_GAUSS_RE = __import__("re").compile(r"^g(\d+)_(c(\d)|w|A)$")
+
+
+def parameter_order_key(name: str):
+    """Array order of the global parameters: the Gaussian groups first,
+    each Gaussian's c_0..c_{d-1}, w, A contiguous; then the rest by name."""
+    m = _GAUSS_RE.match(name)
+    if m:
+        comp = {"w": 10, "A": 11}.get(m.group(2), int(m.group(3)) if m.group(3) is not None else 0)
+        return (0, int(m.group(1)), comp, "")
+    return (1, 0, 0, name)

@@ -66,8 +66,15 @@ def _number_first_touch(keys: np.ndarray):
 
 class MeshTemplate:
     domain_name = "domain"
+    transform = None  # optional callable x[n, dim] -> x[n, dim] applied to all nodes
 
-    def generate(self) -> MeshData:  # pragma: no cover - abstract
+    def generate(self) -> MeshData:
+        md = self._generate()
+        if self.transform is not None:
+            md.x = np.ascontiguousarray(self.transform(md.x.copy()), dtype=np.float64)
+        return md
+
+    def _generate(self) -> MeshData:  # pragma: no cover - abstract
         raise NotImplementedError
 
 
@@ -77,7 +84,8 @@ class RectangularQuadMesh(MeshTemplate):
 
     def __init__(self, *, N: Union[int, List[int]] = 10, size: Union[float, List[float]] = 1.0,
                  lower_left: Union[float, List[float]] = 0.0, split_in_tris: Union[bool, str] = False,
-                 name: str = "domain"):
+                 name: str = "domain", transform=None):
+        self.transform = transform
         self.N = [N, N] if isinstance(N, int) else list(N)
         self.size = [size, size] if isinstance(size, (int, float)) else list(size)
         self.lower_left = [lower_left, lower_left] if isinstance(lower_left, (int, float)) else list(lower_left)
@@ -86,7 +94,7 @@ class RectangularQuadMesh(MeshTemplate):
         self.split = split_in_tris
         self.domain_name = name
 
-    def generate(self) -> MeshData:
+    def _generate(self) -> MeshData:
         nx, ny = self.N
         lx, ly = self.size
         x0, y0 = self.lower_left
@@ -160,13 +168,14 @@ class CuboidBrickMesh(MeshTemplate):
     """Box of Q2 hexahedra (27 nodes each)."""
 
     def __init__(self, *, N: Union[int, List[int]] = 10, size: Union[float, List[float]] = 1.0,
-                 lower_left: Union[float, List[float]] = 0.0, domain_name: str = "domain"):
+                 lower_left: Union[float, List[float]] = 0.0, domain_name: str = "domain", transform=None):
+        self.transform = transform
         self.N = [N, N, N] if isinstance(N, int) else list(N)
         self.size = [size] * 3 if isinstance(size, (int, float)) else list(size)
         self.lower_left = [lower_left] * 3 if isinstance(lower_left, (int, float)) else list(lower_left)
         self.domain_name = domain_name
 
-    def generate(self) -> MeshData:
+    def _generate(self) -> MeshData:
         nx, ny, nz = self.N
         L = self.size
         ll = self.lower_left

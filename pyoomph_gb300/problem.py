@@ -31,6 +31,30 @@ from .equations import (SPACE_ORDER, BoundaryCondition, DirichletBC, EquationPar
 from .meshes import MeshData, MeshTemplate
 
 
+def mesh_is_affine(mesh: MeshData, rtol: float = 1e-12) -> bool:
+    """True if every element's map from reference to physical coordinates is
+    affine: the tangent vectors dx/ds are the same at all integration points
+    and the vertex (C1) interpolation reproduces the position.  Such elements
+    get their geometry computed once per element instead of once per
+    integration point (the values differ only by rounding)."""
+    et = mesh.etype
+    t = et.tables()
+    X = mesh.x[mesh.conn]                                   # [E, NN, D]
+    dps = t["DPS2"]                                         # [Q, NN, D]
+    scale = np.max(np.abs(mesh.x)) + 1e-300
+    E = X.shape[0]
+    for lo in range(0, E, 65536):
+        Xb = X[lo:lo + 65536]
+        tq = np.einsum("eli,qla->eqai", Xb, dps)            # tangents at every point
+        if np.max(np.abs(tq - tq[:, :1])) > rtol * np.max(np.abs(tq[:, :1]) + 1e-300) * 10:
+            return False
+        x2 = np.einsum("eli,ql->eqi", Xb, t["PSI2"])
+        x1 = np.einsum("eli,ql->eqi", Xb[:, list(et.c1_index)], t["PSI1"])
+        if np.max(np.abs(x2 - x1)) > 1e-13 * scale:
+            return False
+    return True
+
+
 class NewtonSolverError(RuntimeError):
     """Raised when Newton diverges or exceeds its iteration cap
     (oomph's NewtonSolverError, problem.cc:9298)."""
@@ -60,6 +84,8 @@ class Problem:
         self.newton_solver_tolerance = 1e-8
         self.jacobian_precision = "fp64"   # or "fp32": FP32 Jacobian, FP64 residual
         self.elems_per_block: Optional[int] = None
+        # "auto": detect affine elements (constant geometry per element) on the host
+        self.geometry = "auto"
         self.linear_solver: Optional[Callable] = None
         self.verbose = False
         self._initialised = False
@@ -130,7 +156,7 @@ class Problem:
         self.field_index = {n: i for i, (n, _) in enumerate(fields)}
         # parameters referenced by the integrand, in a stable order
         used = sorted({s.name[2:] for s in (integrand.free_symbols if hasattr(integrand, "free_symbols") else [])
-                       if s.name.startswith("P_")})
+                       if s.name.startswith("P_")}, key=E.parameter_order_key)
         missing = [p for p in used if p not in params]
         if missing:
             raise RuntimeError(f"parameters without values: {missing}")
@@ -140,7 +166,12 @@ class Problem:
         pw = differentiate(fields, mesh.dim, integrand, used)
         prec = "f64" if self.jacobian_precision in ("fp64", "f64", "double") else "f32"
         self._prec = prec
-        self.kernel: KernelSpec = generate_kernel(mesh.etype, pw, prec, epb=self.elems_per_block)
+        if self.geometry == "auto":
+            self.affine = mesh_is_affine(mesh)
+        else:
+            self.affine = self.geometry == "affine"
+        self.kernel: KernelSpec = generate_kernel(mesh.etype, pw, prec, epb=self.elems_per_block,
+                                                  affine=self.affine)
         self.timings.update(setup_mesh_s=t1 - t0, codegen_s=time.perf_counter() - t1)
         # nodal values, pins and equation numbers
         nval = len(fields)

@@ -35,41 +35,53 @@ def lid_velocity(x, y):
 
 
 def poisson_problem(N=64, seed: int = 0, gaussians: np.ndarray = None, split: str = None,
-                    jacobian_precision: str = "fp64") -> Problem:
+                    jacobian_precision: str = "fp64", transform=None) -> Problem:
     g = draw_gaussians(seed, 8, 2) if gaussians is None else gaussians
     P = Problem()
     P.jacobian_precision = jacobian_precision
-    P += RectangularQuadMesh(N=N, split_in_tris=split or False)
+    P += RectangularQuadMesh(N=N, split_in_tris=split or False, transform=transform)
     P += (PoissonEquation(source=g) + DirichletBC(u=0.0) @ ["left", "right", "top", "bottom"]) @ "domain"
     return P
 
 
 def nonlinear_diffusion_problem(N=48, seed: int = 0, gaussians: np.ndarray = None,
-                                jacobian_precision: str = "fp64", dim: int = 3) -> Problem:
+                                jacobian_precision: str = "fp64", dim: int = 3, transform=None) -> Problem:
     g = draw_gaussians(seed, 16, dim) if gaussians is None else gaussians
     P = Problem()
     P.jacobian_precision = jacobian_precision
     if dim == 3:
-        P += CuboidBrickMesh(N=N)
+        P += CuboidBrickMesh(N=N, transform=transform)
         walls = ["left", "right", "top", "bottom", "back", "front"]
     else:
-        P += RectangularQuadMesh(N=N)
+        P += RectangularQuadMesh(N=N, transform=transform)
         walls = ["left", "right", "top", "bottom"]
     P += (NonlinearDiffusionEquation(source=g) + DirichletBC(u=0.0) @ walls) @ "domain"
     return P
 
 
 def navier_stokes_problem(N=256, Re: float = 100.0, split: str = "left",
-                          jacobian_precision: str = "fp64") -> Problem:
+                          jacobian_precision: str = "fp64", transform=None) -> Problem:
     P = Problem()
     P.jacobian_precision = jacobian_precision
-    P += RectangularQuadMesh(N=N, split_in_tris=split)
+    P += RectangularQuadMesh(N=N, split_in_tris=split, transform=transform)
     eqs = NavierStokesEquations(mass_density=1.0, dynamic_viscosity=1.0 / Re)
     eqs += DirichletBC(velocity_x=lid_velocity, velocity_y=0.0) @ "top"
     eqs += DirichletBC(velocity_x=0.0, velocity_y=0.0) @ ["left", "right", "bottom"]
     eqs += PressureFixation("pressure", 0.0)
     P += eqs @ "domain"
     return P
+
+
+def wavy(amplitude: float = 0.02):
+    """A smooth non-affine deformation of the unit square/cube that keeps the
+    boundary in place: x_i += a sin(pi x_i) sin(2 pi x_j) for j != i."""
+    def f(x):
+        y = x.copy()
+        d = x.shape[1]
+        for i in range(d):
+            y[:, i] = x[:, i] + amplitude * np.sin(np.pi * x[:, i]) * np.sin(2 * np.pi * x[:, (i + 1) % d])
+        return y
+    return f
 
 
 def perturb_dofs(P: Problem, seed: int, sigma: float = 1e-3) -> None:

@@ -173,3 +173,48 @@ def test_newton_nonlinear_diffusion_fp32_converges_to_fp64_solution():
     OP = O.poisson_problem(O.mesh(O.Q2_HEX, 3, 3, 3), gauss, eq=O.EQ_NONLINEAR_DIFFUSION)
     O.newton(OP, tol=1e-10)
     assert _relmax(P64.get_dofs(), OP.dofs()) <= STOL
+
+
+@pytest.mark.parametrize("kind", ["ns_th", "nldiff_hex", "poisson_q2"])
+def test_curved_mesh_general_geometry_vs_oracle(kind):
+    """Non-affine (curved) elements take the per-integration-point geometry
+    path; the affine shortcut must not be selected."""
+    from pyoomph_gb300 import workloads as W
+    rng = np.random.default_rng(21)
+    T = W.wavy(0.03)
+    if kind == "ns_th":
+        P = W.navier_stokes_problem(N=[7, 6], transform=T)
+        P.initialise()
+        m = O.mesh(O.P2_TRI, 7, 6)
+        m.x = T(m.x.copy())
+        OP = O.navier_stokes_problem(m, rho=1.0, mu=0.01)
+        x = OP.dofs() + rng.normal(0, 0.1, OP.n_dof)
+    else:
+        et, dim, nx = (O.Q2_HEX, 3, [3, 2, 3]) if kind == "nldiff_hex" else (O.Q2_QUAD, 2, [6, 5])
+        gauss = W.draw_gaussians(8, 8, dim)
+        if kind == "nldiff_hex":
+            P = W.nonlinear_diffusion_problem(N=nx, gaussians=gauss, transform=T)
+            eq = O.EQ_NONLINEAR_DIFFUSION
+        else:
+            P = W.poisson_problem(N=nx, gaussians=gauss, transform=T)
+            eq = O.EQ_POISSON
+        P.initialise()
+        m = O.mesh(et, *(nx + [0] * (3 - len(nx))))
+        m.x = T(m.x.copy())
+        OP = O.poisson_problem(m, gauss, eq=eq)
+        x = rng.normal(0, 0.5, OP.n_dof)
+    assert not P.affine
+    OP.set_dofs(x)
+    P.set_dofs(x)
+    R0, rp, ci, v = O.assemble(OP, True, -1.0)
+    R, J = P.get_jacobian()
+    assert np.array_equal(J.indptr, rp) and np.array_equal(J.indices, ci)
+    assert _relmax(J.data, v) <= RTOL
+    assert _relmax(R, R0) <= RTOL
+
+
+def test_structured_workloads_take_the_affine_path():
+    from pyoomph_gb300 import workloads as W
+    for P in (W.poisson_problem(N=4), W.navier_stokes_problem(N=4), W.nonlinear_diffusion_problem(N=2)):
+        P.lower()
+        assert P.affine
