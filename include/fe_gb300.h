@@ -194,6 +194,16 @@ int64_t fe_residual_max_noalloc_limit(void);
 /* x[i] -= dx[i] for device vectors (the Newton update). */
 int fe_dof_update(fe_problem_t *p, double *x, const double *dx, int64_t n, void *stream);
 
+/*
+ * Element-level results of the last assembly of a domain (host copies):
+ * R_e [n_elem][nlocal] doubles, J_e [n_elem][nlocal][nlocal] in the Jacobian
+ * precision, local order node-major (either pointer may be NULL).  The
+ * element residual/Jacobian R_e, J_e of GeneralisedElement::get_jacobian
+ * (elements.h:990-999) that the reference checks against finite differences
+ * (BulkElementBase::debug_analytical_jacobian, elements.cpp:5880).
+ */
+int fe_problem_element_buffers(fe_problem_t *p, int domain, double *R_e, void *J_e);
+
 /* Synchronise the problem's work and report any kernel status error. */
 int fe_problem_check(fe_problem_t *p);
 

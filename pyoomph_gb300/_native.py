@@ -26,7 +26,19 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_problem_pattern_device", "fe_problem_set_values", "fe_problem_get_values",
            "fe_problem_set_params", "fe_assemble", "fe_assemble_host", "fe_residual_max", "fe_dof_update",
            "fe_problem_check", "fe_problem_launch_count", "fe_problem_set_timing", "fe_problem_stage_times", "fe_pattern_host",
-           "fe_residual_max_noalloc", "fe_residual_max_noalloc_limit"]
+           "fe_residual_max_noalloc", "fe_residual_max_noalloc_limit", "fe_problem_element_buffers"]
+
+
+def _header_stamp() -> str:
+    """Hash of the device headers the generated sources include, so that the
+    cubin cache (keyed by source text) never serves an image built against
+    an older header."""
+    import hashlib
+    h = hashlib.sha1()
+    for f in ("fe_device.cuh", "fe_abi.h"):
+        with open(os.path.join(INCLUDE_DIR, f), "rb") as fp:
+            h.update(fp.read())
+    return "// device headers " + h.hexdigest()[:16] + "\n"
 
 
 class FeError(RuntimeError):
@@ -116,6 +128,7 @@ def load(build_if_missing: bool = True):
         L.fe_problem_stage_times.argtypes = [vp, vp, vp]
         L.fe_pattern_host.argtypes = [ctypes.POINTER(ProblemDesc), vp, vp, vp]
         L.fe_residual_max_noalloc.argtypes = [vp, i64, vp, vp]
+        L.fe_problem_element_buffers.argtypes = [vp, c_int, vp, vp]
         L.fe_residual_max_noalloc_limit.restype = i64
         _lib = L
         return L
@@ -132,6 +145,7 @@ def code_build(source: str, name: str, cache_dir: str = CACHE_DIR) -> int:
     os.makedirs(cache_dir, exist_ok=True)
     n = ctypes.c_size_t()
     log = ctypes.create_string_buffer(1 << 16)
+    source = _header_stamp() + source
     rc = L.fe_code_build(source.encode(), name.encode(), INCLUDE_DIR.encode(), cache_dir.encode(),
                          ctypes.byref(n), log, len(log))
     if rc:
@@ -147,6 +161,7 @@ class Code:
         os.makedirs(cache_dir, exist_ok=True)
         h = ctypes.c_void_p()
         log = ctypes.create_string_buffer(1 << 16)
+        source = _header_stamp() + source
         rc = L.fe_code_compile(source.encode(), name.encode(), INCLUDE_DIR.encode(), cache_dir.encode(),
                                ctypes.byref(h), log, len(log))
         if rc:

@@ -315,7 +315,6 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w(f"#define FE_NF {nf}\n#define FE_NTC {ntc}\n#define FE_NDNZ {ndnz}\n#define FE_AFFINE {1 if affine else 0}")
     w(f"typedef {jreal} jreal;")
     w(f"__constant__ int c_loc_of[{len(loc_of_flat)}] = {{{', '.join(map(str, loc_of_flat))}}};")
-    w(f"__constant__ int c_c1idx[FE_NN1] = {{{', '.join(map(str, et.c1_index))}}};")
     w(pointwise_source(pw, jreal))
     w(f'extern "C" __global__ void __launch_bounds__(FE_NT) {name}(const FeElemArgs a) {{')
     w("  extern __shared__ __align__(16) unsigned char fe_smem[];")
@@ -381,12 +380,9 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     if pw.uses_x:
         if affine:
             # the affine map is reproduced exactly by the vertex (C1) shapes
-            w("    #pragma unroll")
-            w("    for (int l = 0; l < FE_NN1; ++l) {")
-            w("      const double ps = sPsi1[q * FE_NN1 + l];")
-            w("      #pragma unroll")
-            w("      for (int i = 0; i < FE_DIM; ++i) Xq[i] += X[c_c1idx[l] * FE_DIM + i] * ps;")
-            w("    }")
+            for l, node in enumerate(et.c1_index):
+                for i in range(dim):
+                    w(f"    Xq[{i}] += X[{node * dim + i}] * sPsi1[q * FE_NN1 + {l}];")
         else:
             w("    #pragma unroll")
             w("    for (int l = 0; l < FE_NN; ++l) {")
@@ -408,13 +404,15 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w("        for (int b = 0; b < FE_DIM; ++b) gs[b] += u * dps[l * FE_DIM + b];")
             w("      }")
         else:
-            w("      #pragma unroll")
-            w("      for (int l = 0; l < FE_NN1; ++l) {")
-            w(f"        const double u = sU[(el * FE_NN + c_c1idx[l]) * FE_NVAL + {f}];")
-            w("        v += u * sPsi1[q * FE_NN1 + l];")
-            w("        #pragma unroll")
-            w("        for (int b = 0; b < FE_DIM; ++b) gs[b] += u * sDps1[(q * FE_NN1 + l) * FE_DIM + b];")
-            w("      }")
+            # C1 nodes by literal element slot (no constant-memory index in the loop)
+            w("      const double* ps1 = sPsi1 + q * FE_NN1;")
+            w("      const double* dp1 = sDps1 + q * FE_NN1 * FE_DIM;")
+            for l, node in enumerate(et.c1_index):
+                w(f"      {{ const double u = sU[(el * FE_NN + {node}) * FE_NVAL + {f}];")
+                w(f"        v += u * ps1[{l}];")
+                for b in range(dim):
+                    w(f"        gs[{b}] += u * dp1[{l * dim + b}];")
+                w("      }")
         w(f"      U[{base}] = v;")
         w("      #pragma unroll")
         w("      for (int i = 0; i < FE_DIM; ++i) { double s = 0.0;")

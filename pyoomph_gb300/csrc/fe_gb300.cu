@@ -22,6 +22,7 @@
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <memory>
@@ -637,7 +638,17 @@ int build_cubin(const char *source, const char *kernel_name, const char *include
   if (log && log_cap) log[0] = 0;
   const std::string arch = "--gpu-architecture=sm_103a";
   std::string inc = std::string("--include-path=") + (include_dir ? include_dir : ".");
-  const std::string key_src = std::string(source) + "\n//" + kernel_name + arch + FE_VERSION;
+  // compiler options: the defaults, or PYOOMPH_GB300_NVRTC_OPTS (space separated)
+  std::vector<std::string> optv = {"--std=c++17", "-default-device", "-lineinfo", "--fmad=true", "-DFE_NVRTC=1"};
+  if (const char *env = getenv("PYOOMPH_GB300_NVRTC_OPTS")) {
+    optv.clear();
+    std::istringstream is(env);
+    std::string o;
+    while (is >> o) optv.push_back(o);
+  }
+  std::string optkey;
+  for (auto &o : optv) optkey += o + " ";
+  const std::string key_src = std::string(source) + "\n//" + kernel_name + arch + FE_VERSION + optkey;
   char keyhex[32];
   snprintf(keyhex, sizeof(keyhex), "%016llx", (unsigned long long)fnv1a(key_src));
   std::string cache_path;
@@ -650,9 +661,9 @@ int build_cubin(const char *source, const char *kernel_name, const char *include
   nvrtcProgram prog;
   if (nvrtcCreateProgram(&prog, source, "fe_element.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
     return fail(FE_ERR_COMPILE, "nvrtcCreateProgram failed");
-  const char *opts[] = {arch.c_str(), inc.c_str(), "--std=c++17", "-default-device", "-lineinfo",
-                        "--fmad=true", "-DFE_NVRTC=1"};
-  nvrtcResult r = nvrtcCompileProgram(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+  std::vector<const char *> opts = {arch.c_str(), inc.c_str()};
+  for (auto &o : optv) opts.push_back(o.c_str());
+  nvrtcResult r = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
   size_t lsz = 0;
   nvrtcGetProgramLogSize(prog, &lsz);
   std::string lg(lsz, '\0');
@@ -978,6 +989,20 @@ int fe_dof_update(fe_problem_t *p, double *x, const double *dx, int64_t n, void 
   if (n <= 0) return FE_OK;
   k_dof_update<<<grid_for(n, 256, sm_count_cached()), 256, 0, (cudaStream_t)stream>>>(x, dx, n);
   CUDA_TRY(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_problem_element_buffers(fe_problem_t *p, int domain, double *R_e, void *J_e) {
+  if (!p || domain < 0 || domain >= (int)p->domains.size()) return fail(FE_ERR_ARG, "bad problem/domain");
+  CUDA_TRY(cudaDeviceSynchronize());
+  const Domain &d = p->domains[domain];
+  const size_t jel = p->jac_prec == FE_JAC_F64 ? sizeof(double) : sizeof(float);
+  if (R_e)
+    CUDA_TRY(cudaMemcpy(R_e, p->rbuf_all.as<double>() + d.rbase, sizeof(double) * d.n_elem * d.nlocal,
+                        cudaMemcpyDeviceToHost));
+  if (J_e)
+    CUDA_TRY(cudaMemcpy(J_e, (const char *)p->jbuf_all.p + jel * d.jbase, jel * d.n_elem * d.nlocal * d.nlocal,
+                        cudaMemcpyDeviceToHost));
   return FE_OK;
 }
 

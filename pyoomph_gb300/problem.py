@@ -361,6 +361,14 @@ class Problem:
         N.check(N.load().fe_problem_stage_times(self._h, ms.ctypes.data, ctypes.byref(calls)))
         return ms, calls.value
 
+    def element_buffers(self):
+        """(R_e [E, nloc], J_e [E, nloc, nloc]) of the last assembly."""
+        E, n = self.mesh.n_elem, self.kernel.layout.n
+        R = np.zeros((E, n))
+        J = np.zeros((E, n, n), dtype=np.float64 if self._prec == "f64" else np.float32)
+        N.check(N.load().fe_problem_element_buffers(self._h, 0, R.ctypes.data, J.ctypes.data))
+        return R, J
+
     def check(self) -> None:
         N.check(N.load().fe_problem_check(self._h))
 

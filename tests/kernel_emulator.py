@@ -1,0 +1,93 @@
+"""CPU emulation of a generated element kernel (test infrastructure).
+
+The generated kernels run their phases as block-strided loops
+``for (p = threadIdx.x; p < n; p += FE_NT)`` separated by __syncthreads().
+Compiled as plain C++ with FE_NT = 1 and threadIdx = 0, one host thread runs
+every iteration of each phase in order, which is exactly the block's
+result.  This lets the CPU test suite check the generated code element by
+element against the oracle without a GPU.  It is never part of the product.
+"""
+from __future__ import annotations
+
+import ctypes
+import hashlib
+import os
+import re
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "pyoomph_gb300", "csrc")
+OUT = os.path.join(ROOT, "_build", "emu")
+
+PRELUDE = r"""
+#include <math.h>
+#include <cmath>
+#include <cstring>
+struct fe_emu_dim3 { unsigned x, y, z; };
+static fe_emu_dim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0};
+#define __global__
+#define __device__
+#define __host__
+#define __constant__ static
+#define __forceinline__ inline
+#define __noinline__
+#define __launch_bounds__(x)
+#define __restrict__ __restrict
+#define __align__(n) alignas(n)
+#define __syncthreads() do {} while (0)
+static inline int atomicExch(int *p, int v) { int o = *p; *p = v; return o; }
+alignas(16) unsigned char fe_smem[232448];
+"""
+
+
+class _Args(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_void_p), ("conn", ctypes.c_void_p), ("values", ctypes.c_void_p),
+                ("params", ctypes.c_void_p), ("tables", ctypes.c_void_p), ("rbuf", ctypes.c_void_p),
+                ("jbuf", ctypes.c_void_p), ("n_elem", ctypes.c_longlong), ("nval", ctypes.c_int),
+                ("flag", ctypes.c_int), ("status", ctypes.c_void_p)]
+
+
+def build(ks) -> ctypes.CDLL:
+    src = re.sub(r"#define FE_NT \d+", "#define FE_NT 1", ks.source)
+    src = src.replace("extern __shared__ __align__(16) unsigned char fe_smem[];", "")
+    body = PRELUDE + src + (
+        f'\nextern "C" void fe_emu_run(const FeElemArgs *a, int nblocks) {{\n'
+        f'  for (int b = 0; b < nblocks; ++b) {{\n'
+        f'    memset(fe_smem, 0xff, sizeof(fe_smem)); /* NaN garbage: uninitialised reads show */\n'
+        f'    blockIdx.x = b; {ks.name}(*a); }}\n}}\n')
+    h = hashlib.sha1(body.encode()).hexdigest()[:16]
+    os.makedirs(OUT, exist_ok=True)
+    so = os.path.join(OUT, f"emu_{h}.so")
+    if not os.path.exists(so):
+        cpp = os.path.join(OUT, f"emu_{h}.cpp")
+        with open(cpp, "w") as f:
+            f.write(body)
+        subprocess.run(["g++", "-std=c++17", "-O3", "-fPIC", "-shared", "-ffp-contract=off", "-I", CSRC, cpp,
+                        "-o", so + ".tmp"], check=True)
+        os.replace(so + ".tmp", so)
+    L = ctypes.CDLL(so)
+    L.fe_emu_run.argtypes = [ctypes.POINTER(_Args), ctypes.c_int]
+    return L
+
+
+def run(ks, x, conn, values, params, flag: int = 1):
+    """Element residuals [E, nloc] and matrices [E, nloc, nloc] of the
+    generated kernel ks on the given mesh data (host arrays)."""
+    L = build(ks)
+    E = conn.shape[0]
+    nloc = ks.layout.n
+    jt = np.float64 if ks.jac_precision == "f64" else np.float32
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    values = np.ascontiguousarray(values, dtype=np.float64)
+    params = np.ascontiguousarray(params if len(params) else np.zeros(1), dtype=np.float64)
+    tables = np.ascontiguousarray(ks.tables, dtype=np.float64)
+    rbuf = np.zeros((E, nloc))
+    jbuf = np.zeros((E, nloc, nloc), dtype=jt)
+    status = np.zeros(4, dtype=np.int32)
+    a = _Args(x.ctypes.data, conn.ctypes.data, values.ctypes.data, params.ctypes.data, tables.ctypes.data,
+              rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data)
+    L.fe_emu_run(ctypes.byref(a), (E + ks.epb - 1) // ks.epb)
+    return rbuf, jbuf, status

@@ -218,3 +218,19 @@ def test_structured_workloads_take_the_affine_path():
     for P in (W.poisson_problem(N=4), W.navier_stokes_problem(N=4), W.nonlinear_diffusion_problem(N=2)):
         P.lower()
         assert P.affine
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("geometry", ["affine", "general"])
+@pytest.mark.parametrize("kind", ["poisson_q2", "poisson_p2", "ns_th", "nldiff_hex", "nldiff_q2"])
+def test_element_level_parity_every_kernel_variant(kind, geometry, prec):
+    """Element residuals/matrices straight from the GPU element buffers
+    (fe_problem_element_buffers) against the oracle's, for every variant."""
+    import element_cases as C
+    P, ks, values, Rr, Jr = C.build(kind, geometry, prec)
+    P.initialise()
+    P.set_values(values)
+    P.get_jacobian()
+    Re, Je = P.element_buffers()
+    assert C.relmax(Re, Rr) <= RTOL
+    assert C.relmax(Je, Jr) <= (RTOL if prec == "fp64" else JTOL32)
