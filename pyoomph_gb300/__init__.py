@@ -11,9 +11,10 @@ from .equations import (DirichletBC, Equations, NavierStokesEquations, Nonlinear
 from .expressions import (div, dot, exp, gaussian_source, grad, identity_matrix, material_derivative,
                           parameter, sym, testfunction, var, var_and_test, weak)
 from .meshes import CuboidBrickMesh, RectangularQuadMesh
+from .assembly import CustomAssemblyBase, GB300Assembler
 from .problem import NewtonSolverError, Problem
 
-__all__ = ["Problem", "NewtonSolverError", "Equations", "PoissonEquation", "NonlinearDiffusionEquation",
+__all__ = ["CustomAssemblyBase", "GB300Assembler", "Problem", "NewtonSolverError", "Equations", "PoissonEquation", "NonlinearDiffusionEquation",
            "StokesEquations", "NavierStokesEquations", "DirichletBC", "PressureFixation", "RectangularQuadMesh",
            "CuboidBrickMesh", "var", "testfunction", "var_and_test", "grad", "div", "dot", "sym", "weak", "exp",
            "identity_matrix", "material_derivative", "parameter", "gaussian_source"]

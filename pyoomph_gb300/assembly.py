@@ -1,0 +1,97 @@
+"""The problem-level assembly plugin, mirroring pyoomph's
+``CustomAssemblyBase`` (``pyoomph/generic/assembly.py:36-88``) and its use
+by ``Problem.set_custom_assembler`` / ``get_custom_residuals_jacobian``
+(``pyoomph/generic/problem.py:1711-1745``).
+
+``GB300Assembler`` is the drop-in: a pyoomph ``Problem`` that calls
+``set_custom_assembler(GB300Assembler(engine_problem))`` gets its residual
+and CSR Jacobian from the GPU engine, in the reference's equation numbering
+and CSR order, with the dtypes pyoomph asserts (float64 residual, int32
+indptr/indices, float64 data).  The host problem's current dofs are read
+with ``get_current_dofs()[0]`` each call, as pyoomph's own assemblers do.
+"""
+from __future__ import annotations
+
+from typing import Callable, Optional, Tuple, Union
+
+import numpy as np
+
+
+class CustomAssemblyBase:
+    def __init__(self) -> None:
+        self.problem = None
+
+    def _set_problem(self, problem) -> None:
+        self.problem = problem
+
+    def has_custom_solve_routine(self) -> bool:
+        return False
+
+    def custom_solve_routine(self, solve_Jx_b: Callable[[np.ndarray], np.ndarray], b: np.ndarray) -> np.ndarray:
+        raise NotImplementedError("Custom solve routine not implemented")
+
+    def invalidate_cache(self) -> None:
+        pass
+
+    def actions_after_adapt(self) -> None:
+        self.invalidate_cache()
+
+    def actions_after_remeshing(self) -> None:
+        self.invalidate_cache()
+
+    def actions_after_equation_numbering(self) -> None:
+        self.invalidate_cache()
+
+    def actions_after_setting_initial_condition(self) -> None:
+        self.invalidate_cache()
+
+    def actions_after_successful_newton_solve(self) -> None:
+        pass
+
+    def initialize(self) -> None:
+        pass
+
+    def finalize(self) -> None:
+        pass
+
+    def get_residuals_and_jacobian(self, require_jacobian: bool, dparameter: Optional[str] = None):
+        raise RuntimeError("Must be implemented")
+
+    def get_last_mass_and_jacobian_matrices(self):
+        return None, None
+
+
+class GB300Assembler(CustomAssemblyBase):
+    """Residual and CSR Jacobian from the GB300 engine.
+
+    ``engine`` is a ``pyoomph_gb300.Problem`` describing the same mesh and
+    weak form as the host problem (same equation numbering).  If the host
+    problem is not set, the engine's own dof state is assembled."""
+
+    def __init__(self, engine) -> None:
+        super().__init__()
+        self.engine = engine
+
+    def initialize(self) -> None:
+        self.engine.initialise()
+
+    def _sync_dofs(self) -> None:
+        if self.problem is not None and hasattr(self.problem, "get_current_dofs"):
+            dofs = np.asarray(self.problem.get_current_dofs()[0], dtype=np.float64)
+            if dofs.shape[0] != self.engine.n_dof:
+                raise RuntimeError(f"host problem has {dofs.shape[0]} dofs, engine {self.engine.n_dof}")
+            self.engine.set_dofs(dofs)
+
+    def get_residuals_and_jacobian(self, require_jacobian: bool, dparameter: Optional[str] = None
+                                   ) -> Union[np.ndarray, Tuple[np.ndarray, "object"]]:
+        if dparameter is not None:
+            raise RuntimeError("Cannot derive the residual with respect to a parameter yet")
+        self.engine.initialise()
+        self._sync_dofs()
+        if not require_jacobian:
+            return np.ascontiguousarray(self.engine.get_residuals(), dtype=np.float64)
+        R, J = self.engine.get_jacobian()
+        J.data = J.data.astype(np.float64, copy=False)
+        J.indptr = J.indptr.astype(np.int32, copy=False)
+        J.indices = J.indices.astype(np.int32, copy=False)
+        return np.ascontiguousarray(R, dtype=np.float64), J

@@ -315,6 +315,23 @@ class Problem:
         N.check(N.load().fe_problem_set_values(self._h, v.ctypes.data))
         self.set_dofs(self._dofs_from_values(v))
 
+    def get_current_dofs(self):
+        """pyoomph's accessor: (dof vector, pinned values)."""
+        return self.get_dofs(), self._values0[self.pinned].copy() if hasattr(self, "pinned") else None
+
+    def set_current_dofs(self, dofs) -> None:
+        self.set_dofs(np.asarray(dofs, dtype=np.float64))
+
+    def set_custom_assembler(self, assembler) -> None:
+        """pyoomph's Problem.set_custom_assembler (problem.py:1711): the
+        assembler then provides residuals and Jacobians to solve()."""
+        if getattr(self, "_custom_assembler", None) is not None:
+            self._custom_assembler.finalize()
+        self._custom_assembler = assembler
+        if assembler is not None:
+            assembler._set_problem(self)
+            assembler.initialize()
+
     def get_values(self) -> np.ndarray:
         """Nodal values [n_nodes, nval] (after the last assembly's dof scatter)."""
         v = np.zeros((self.mesh.n_nodes, len(self.fields)))

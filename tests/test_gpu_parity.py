@@ -234,3 +234,34 @@ def test_element_level_parity_every_kernel_variant(kind, geometry, prec):
     Re, Je = P.element_buffers()
     assert C.relmax(Re, Rr) <= RTOL
     assert C.relmax(Je, Jr) <= (RTOL if prec == "fp64" else JTOL32)
+
+
+def test_custom_assembler_drop_in_contract():
+    """GB300Assembler through pyoomph's CustomAssemblyBase contract: float64
+    residual, CSR with int32 indptr/indices and float64 data, dofs taken
+    from the host problem's get_current_dofs()."""
+    from pyoomph_gb300 import GB300Assembler, workloads as W
+
+    class HostProblem:  # stands for the pyoomph Problem
+        def __init__(self, x):
+            self.x = x
+
+        def get_current_dofs(self):
+            return self.x, None
+
+    gauss = W.draw_gaussians(2, 8, 2)
+    eng = W.poisson_problem(N=6, gaussians=gauss)
+    asm = GB300Assembler(eng)
+    asm.initialize()
+    x = np.random.default_rng(1).normal(size=eng.n_dof)
+    asm._set_problem(HostProblem(x))
+    R = asm.get_residuals_and_jacobian(False)
+    R2, J = asm.get_residuals_and_jacobian(True)
+    assert R.dtype == np.float64 and J.data.dtype == np.float64
+    assert J.indptr.dtype == np.int32 and J.indices.dtype == np.int32
+    assert np.array_equal(R, R2)
+    OP = O.poisson_problem(O.mesh(O.Q2_QUAD, 6, 6), gauss)
+    OP.set_dofs(x)
+    R0, rp, ci, v = O.assemble(OP, True, -1.0)
+    assert np.array_equal(J.indptr, rp) and np.array_equal(J.indices, ci)
+    assert _relmax(J.data, v) <= RTOL and _relmax(R, R0) <= RTOL
