@@ -35,7 +35,44 @@ WORKLOADS = {
     "ns": ("navier_stokes_th_p2p1_split_left_Re100", 256),
     "poisson": ("poisson_q2_quad_8gaussians", 64),
     "hex": ("nonlinear_diffusion_q2_hex_16gaussians", 48),
+    "serving": ("serving_stream_poisson_ns_mixed", 128),
 }
+
+
+def run_serving(args):
+    """Serving stream: Poisson-process arrivals of Poisson / Navier-Stokes
+    assemble+Newton requests, sides log-uniform in [16, --size]; the
+    continuous-batching FP32-Jacobian server beside the plain FP64
+    one-request-at-a-time path, on the same stream."""
+    import copy
+    import torch
+    from pyoomph_gb300 import serving as S
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    reqs = S.make_stream(args.requests, rate=args.rate, seed=0, side_range=(16, args.size))
+    out = {}
+    for name, fn in (("batched_fp32", lambda r: S.Server(slots=4, jacobian_precision="fp32").run(r)),
+                     ("sequential_fp64", lambda r: S.serve_sequential(r, precision="fp64"))):
+        # warm-up: compile and build every mesh class once
+        t0 = time.perf_counter()
+        done = fn(copy.deepcopy(reqs))
+        wall = max(r.t_done for r in done)
+        out[name] = S.summary(done, wall)
+        out[name]["wall_s"] = time.perf_counter() - t0
+        out[name]["results"] = {r.rid: r.dofs for r in done}
+    # each request's dofs agree between the two paths (FP32 vs FP64 Jacobian Newton)
+    err = max(float(np.max(np.abs(out["batched_fp32"]["results"][k] - out["sequential_fp64"]["results"][k])) /
+                    max(1.0, float(np.max(np.abs(out["sequential_fp64"]["results"][k])))))
+              for k in out["sequential_fp64"]["results"])
+    for v in out.values():
+        v.pop("results")
+    b, s_ = out["batched_fp32"], out["sequential_fp64"]
+    line = {"metric": "p50/p99 assemble+Newton request latency (serving stream)", "value": b["p50_s"],
+            "unit": "s", "n_gpus": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 residual, f32 Jacobian", "data": "synthetic",
+            "config": {"workload": WORKLOADS["serving"][0], "requests": args.requests, "rate_per_s": args.rate,
+                       "side_range": [16, args.size], "slots_per_class": 4, "linear_solver": "SuperLU (scipy)"},
+            "batched_fp32": b, "sequential_fp64": s_, "max_rel_solution_difference": err}
+    print(json.dumps(line), flush=True)
 
 
 def _peaks():
@@ -373,12 +410,16 @@ def main():
     ap.add_argument("--workload", default="ns", choices=list(WORKLOADS))
     ap.add_argument("--size", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--rate", type=float, default=50.0)
     args = ap.parse_args()
     if args.size is None:
         args.size = WORKLOADS[args.workload][1]
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.workload == "serving":
+        run_serving(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

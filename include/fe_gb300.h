@@ -102,6 +102,8 @@ typedef struct fe_domain_desc {
   int elems_per_block;      /* launch shape chosen by the code generator / tuner */
   int threads_per_block;
   int smem_bytes;           /* dynamic shared memory per block */
+  int64_t replica_elems;    /* > 0: the elements are replicas of a mesh of this many elements,
+                               replica r reading params + r * params_stride (batched serving) */
 } fe_domain_desc_t;
 
 typedef struct fe_problem_desc {
@@ -116,6 +118,7 @@ typedef struct fe_problem_desc {
   int n_params;
   const double *params;     /* global parameters read by the element code */
   int jac_precision;        /* FE_JAC_F64 or FE_JAC_F32 */
+  int params_stride;        /* parameters per replica (0 = one set for all elements) */
 } fe_problem_desc_t;
 
 /*

@@ -61,6 +61,7 @@ class DomainDesc(ctypes.Structure):
         ("elems_per_block", ctypes.c_int),
         ("threads_per_block", ctypes.c_int),
         ("smem_bytes", ctypes.c_int),
+        ("replica_elems", ctypes.c_int64),
     ]
 
 
@@ -77,6 +78,7 @@ class ProblemDesc(ctypes.Structure):
         ("n_params", ctypes.c_int),
         ("params", ctypes.c_void_p),
         ("jac_precision", ctypes.c_int),
+        ("params_stride", ctypes.c_int),
     ]
 
 

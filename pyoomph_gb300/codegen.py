@@ -420,8 +420,9 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("        for (int b = 0; b < FE_DIM; ++b) s += g[b][i] * gs[b];")
         w(f"        U[{base} + 1 + i] = s; }}")
         w("    }")
+    w("    const double* Pe = a.params + (a.replica_elems > 0 ? ((e0 + el) / a.replica_elems) * a.params_stride : 0);")
     w("    double r[FE_NTC]; jreal D[FE_NDNZ];")
-    w("    fe_pointwise(U, Xq, a.params, r, D, flag);")
+    w("    fe_pointwise(U, Xq, Pe, r, D, flag);")
     w("    double* rh = sRh + (el * FE_NQ + q) * FE_NTC;")
     w("    #pragma unroll")
     w("    for (int f = 0; f < FE_NF; ++f) {")
@@ -434,7 +435,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    }")
     w("    if (flag) {")
     if jreal == "float":
-        w("      fe_pointwise_jac(U, Xq, a.params, D);")
+        w("      fe_pointwise_jac(U, Xq, Pe, D);")
     w("      jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZ;")
     w("      const jreal wj = (jreal)wq;")
     w("      #pragma unroll")

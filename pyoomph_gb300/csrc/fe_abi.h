@@ -17,6 +17,8 @@ struct FeElemArgs {
   int nval;
   int flag;             // 0: residual only, 1: residual and Jacobian
   int *status;          // device status word (0 = ok)
+  long long replica_elems; // > 0: the domain is a stack of replicas of this many elements each
+  int params_stride;       // parameters per replica (replica r reads params + r * params_stride)
 };
 
 #endif

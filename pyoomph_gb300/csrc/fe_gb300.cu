@@ -242,6 +242,7 @@ struct Domain {
   int nnode = 0, nlocal = 0;
   long long n_elem = 0;
   int epb = 1, threads = 128, smem = 0;
+  long long replica_elems = 0;
   DevBuf conn, tables, rbuf, jbuf;
   long long jbase = 0; // flat offset of this domain's entries in the global contribution space
   long long rbase = 0;
@@ -251,7 +252,7 @@ struct Domain {
 struct fe_problem {
   int dim = 0, nval = 0, jac_prec = FE_JAC_F64;
   long long n_nodes = 0, n_dof = 0, nnz = 0;
-  int n_params = 0;
+  int n_params = 0, params_stride = 0;
   std::vector<Domain> domains;
   DevBuf x, values, eqn, params, status;
   DevBuf rowptr, colidx, cptr, cidx, rptr, ridx;
@@ -526,6 +527,8 @@ int launch_elements(fe_problem *p, int flag, cudaStream_t st) {
     a.nval = p->nval;
     a.flag = flag;
     a.status = p->status.as<int>();
+    a.replica_elems = d.replica_elems;
+    a.params_stride = p->params_stride;
     void *kp[] = {&a};
     unsigned grid = (unsigned)((d.n_elem + d.epb - 1) / d.epb);
     CUDA_TRY(cudaLaunchKernel((const void *)d.code->func, dim3(grid), dim3(d.threads), kp, (size_t)d.smem, st));
@@ -742,6 +745,7 @@ int fe_problem_create(const fe_problem_desc_t *desc, fe_problem_t **out) {
   P->n_dof = desc->n_dof;
   P->jac_prec = desc->jac_precision;
   P->n_params = desc->n_params;
+  P->params_stride = desc->params_stride;
   std::vector<const int32_t *> conn_h;
   long long jtot = 0, rtot = 0;
   for (int di = 0; di < desc->n_domains; di++) {
@@ -757,6 +761,10 @@ int fe_problem_create(const fe_problem_desc_t *desc, fe_problem_t **out) {
     d.epb = dd.elems_per_block;
     d.threads = dd.threads_per_block;
     d.smem = dd.smem_bytes;
+    d.replica_elems = dd.replica_elems > 0 ? dd.replica_elems : 0;
+    if (d.replica_elems && (desc->params_stride < 0 ||
+                            (dd.n_elem / d.replica_elems) * (long long)desc->params_stride > desc->n_params))
+      return fail(FE_ERR_ARG, "domain %d: replica parameters exceed the parameter array", di);
     d.local_node.assign(dd.local_node, dd.local_node + dd.nlocal);
     d.local_val.assign(dd.local_val, dd.local_val + dd.nlocal);
     d.jbase = jtot;

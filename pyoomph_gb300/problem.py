@@ -86,6 +86,8 @@ class Problem:
         self.elems_per_block: Optional[int] = None
         # "auto": detect affine elements (constant geometry per element) on the host
         self.geometry = "auto"
+        # > 1: a stack of independent copies of the problem assembled together
+        self.replicas = 1
         self.linear_solver: Optional[Callable] = None
         self.verbose = False
         self._initialised = False
@@ -209,6 +211,22 @@ class Problem:
                 pinned[node0, f] = True
                 if bc.value is not None:
                     values[node0, f] = bc.value
+        R = int(self.replicas)
+        if R > 1:
+            # a stack of independent copies of the mesh (batched serving):
+            # replica r's nodes follow replica r-1's, so its equations are a
+            # contiguous block and the Jacobian is block diagonal
+            self.base_mesh = mesh
+            self.base_n_nodes, self.base_n_elem = n, mesh.n_elem
+            mesh = MeshData(mesh.etype, np.tile(mesh.x, (R, 1)),
+                            (mesh.conn[None, :, :] + (np.arange(R) * n)[:, None, None]).reshape(-1, mesh.conn.shape[1]).astype(np.int32),
+                            np.tile(mesh.is_vertex, R), {k: np.tile(v, R) for k, v in mesh.boundaries.items()})
+            self.mesh = mesh
+            present, pinned, values = np.tile(present, (R, 1)), np.tile(pinned, (R, 1)), np.tile(values, (R, 1))
+            n = mesh.n_nodes
+            self.replica_elems = self.base_n_elem
+            self.params_stride = len(self.params)
+            self.params = np.tile(self.params, R)
         free = present & ~pinned
         eqn = np.full((n, nval), -1, dtype=np.int32)
         flat = free.reshape(-1)
@@ -267,11 +285,12 @@ class Problem:
         dd = N.DomainDesc(self.code.handle if with_code else None, mesh.etype.nnode, lay.n, mesh.n_elem,
                           k["conn"].ctypes.data, k["lnode"].ctypes.data, k["lval"].ctypes.data,
                           k["tables"].ctypes.data, k["tables"].size, self.kernel.epb, self.kernel.threads,
-                          self.kernel.smem_bytes)
+                          self.kernel.smem_bytes, getattr(self, "replica_elems", 0))
         doms = (N.DomainDesc * 1)(dd)
         desc = N.ProblemDesc(mesh.dim, mesh.n_nodes, len(self.fields), k["x"].ctypes.data, k["eqn"].ctypes.data,
                              self.n_dof, 1, doms, len(self.params), k["params"].ctypes.data,
-                             N.FE_JAC_F64 if self._prec == "f64" else N.FE_JAC_F32)
+                             N.FE_JAC_F64 if self._prec == "f64" else N.FE_JAC_F32,
+                             getattr(self, "params_stride", 0))
         return desc, doms, keep
 
     def host_pattern(self) -> Tuple[np.ndarray, np.ndarray]:
@@ -338,9 +357,24 @@ class Problem:
         N.check(N.load().fe_problem_get_values(self._h, v.ctypes.data))
         return v
 
-    def set_parameters(self, **kw) -> None:
+    def set_parameters(self, replica: Optional[int] = None, **kw) -> None:
+        """Set global parameters by name (of one replica, or of all)."""
+        stride = len(self.param_names)
+        reps = range(int(self.replicas)) if replica is None else [replica]
         for k, v in kw.items():
-            self.params[self.param_names.index(k)] = float(v)
+            j = self.param_names.index(k)
+            for r in reps:
+                self.params[r * stride + j] = float(v)
+        self._keep["params"][:len(self.params)] = self.params
+        N.check(N.load().fe_problem_set_params(self._h, self._keep["params"].ctypes.data))
+
+    def set_parameter_vector(self, values: np.ndarray, replica: Optional[int] = None) -> None:
+        """Set every global parameter (array in param_names order)."""
+        stride = len(self.param_names)
+        v = np.asarray(values, dtype=np.float64).reshape(stride)
+        reps = range(int(self.replicas)) if replica is None else [replica]
+        for r in reps:
+            self.params[r * stride:(r + 1) * stride] = v
         self._keep["params"][:len(self.params)] = self.params
         N.check(N.load().fe_problem_set_params(self._h, self._keep["params"].ctypes.data))
 

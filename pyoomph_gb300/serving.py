@@ -1,0 +1,322 @@
+"""Serving: a continuous-batching loop of assemble + Newton-solve requests.
+
+Requests (a Poisson or a Navier-Stokes problem of some mesh side, with its
+own source or Reynolds number) arrive over time.  The server keeps, per mesh
+class (equation, side, Jacobian precision), one *batch*: a resident
+problem that stacks S independent replicas of the mesh (``Problem.replicas``),
+each replica reading its own parameters.  A request is admitted into a free
+replica slot of its class as soon as one is free and the device has the
+memory for the class (``fe_device_info`` free bytes, minus a reserve);
+otherwise it waits.  Admission happens at Newton-step boundaries, so
+requests join and leave a running batch continuously.
+
+One Newton step of a batch is one fused launch sequence for all its
+replicas (dof scatter, element kernel, residual and Jacobian scatter) on the
+batch's own CUDA stream, the per-replica residual max-norm on the device,
+and then, for each active replica, the linear solve J dx = R of its diagonal
+block on a CPU worker (SuperLU through scipy, the reference's default
+solver) -- so GPU assembly of one batch overlaps the solves of others.
+
+Results do not depend on the mix: every element, CSR slot and residual
+entry of a replica is computed from that replica's values only, in a fixed
+order, so a request gives bit-identical dofs alone or among others.
+
+Per-request latency = completion - arrival; the summary reports p50/p99 and
+solves/s.  ``serve_sequential`` is the plain path: one request at a time,
+one problem per request, FP64 Jacobian.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import ctypes
+import heapq
+import time
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+
+from . import _native as N
+from . import workloads as W
+
+
+@dataclass
+class Request:
+    rid: int
+    kind: str                   # "poisson" | "ns"
+    side: int
+    arrival: float              # seconds after the start of the stream
+    seed: int = 0
+    Re: float = 100.0
+    # results
+    dofs: Optional[np.ndarray] = None
+    t_admit: float = float("nan")
+    t_done: float = float("nan")
+    newton_iterations: int = 0
+    residuals: List[float] = field(default_factory=list)
+    error: Optional[str] = None
+
+    @property
+    def latency(self) -> float:
+        return self.t_done - self.arrival
+
+
+def make_stream(n: int, rate: float, seed: int = 0, side_range: Tuple[int, int] = (16, 512),
+                kinds=("poisson", "ns"), ns_side_max: Optional[int] = None) -> List[Request]:
+    """Poisson-process arrivals at `rate` per second; side log-uniform in
+    side_range; kind uniform over kinds; source seed / Re from the seed."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    out = []
+    for i in range(n):
+        kind = kinds[int(rng.integers(len(kinds)))]
+        side = int(round(np.exp(rng.uniform(np.log(side_range[0]), np.log(side_range[1])))))
+        if kind == "ns" and ns_side_max:
+            side = min(side, ns_side_max)
+        out.append(Request(i, kind, side, float(t[i]), seed=int(rng.integers(1 << 30)),
+                           Re=float(rng.uniform(10.0, 100.0))))
+    return out
+
+
+def _class_problem(kind: str, side: int, precision: str, replicas: int):
+    if kind == "poisson":
+        P = W.poisson_problem(N=side, seed=0, jacobian_precision=precision)
+    else:
+        P = W.navier_stokes_problem(N=side, Re=100.0, jacobian_precision=precision)
+    P.replicas = replicas
+    return P
+
+
+def _request_params(req: Request, P) -> np.ndarray:
+    """The parameter vector of one replica, in P.param_names order."""
+    names = P.param_names
+    v = np.zeros(len(names))
+    if req.kind == "poisson":
+        g = W.draw_gaussians(req.seed, 8, 2)
+        d = {}
+        for k in range(g.shape[0]):
+            d[f"g{k}_c0"], d[f"g{k}_c1"], d[f"g{k}_w"], d[f"g{k}_A"] = g[k]
+    else:
+        d = {"mass_density": 1.0, "dynamic_viscosity": 1.0 / req.Re}
+    for j, nm in enumerate(names):
+        v[j] = d[nm]
+    return v
+
+
+def estimate_bytes(P) -> int:
+    """Device memory of a lowered problem (element buffers, CSR values,
+    pattern and scatter lists, nodal arrays), before creating it."""
+    E = P.mesh.n_elem
+    nl = P.kernel.layout.n
+    jb = 8 if P._prec == "f64" else 4
+    nnz_est = E * nl * nl  # upper bound of the number of CSR slots
+    return int(E * nl * nl * (jb + 4) + nnz_est * (jb + 8 + 4) + E * nl * 12 + P.mesh.n_nodes * 64)
+
+
+class _Batch:
+    def __init__(self, key, P, slots: int, stream):
+        self.key = key
+        self.P = P
+        self.slots = slots
+        self.stream = stream
+        self.req: List[Optional[Request]] = [None] * slots
+        self.n_dof = P.n_dof // slots
+        self.nnz = P.nnz // slots
+        rp, ci = P.pattern()
+        self.rp0 = rp[:self.n_dof + 1].copy()
+        self.ci0 = ci[:self.nnz].copy()
+        self.x0 = P.get_dofs()[:self.n_dof].copy()
+        self.last_used = time.perf_counter()
+
+    def free_slot(self) -> int:
+        for s, r in enumerate(self.req):
+            if r is None:
+                return s
+        return -1
+
+    def active(self) -> bool:
+        return any(r is not None for r in self.req)
+
+
+class Server:
+    def __init__(self, slots: int = 4, jacobian_precision: str = "fp32", tol: float = 1e-10,
+                 max_newton: int = 20, workers: int = 8, hbm_reserve: float = 0.1):
+        import torch
+        self.torch = torch
+        self.slots = slots
+        self.precision = jacobian_precision
+        self.tol = tol
+        self.max_newton = max_newton
+        self.pool = cf.ThreadPoolExecutor(max_workers=workers)       # linear solves
+        self.stepper = cf.ThreadPoolExecutor(max_workers=16)         # one step per busy batch
+        self.hbm_reserve = hbm_reserve
+        self.batches: Dict[tuple, _Batch] = {}
+        self.launches = 0
+
+    # -- memory ------------------------------------------------------------
+    def _free_bytes(self) -> int:
+        f = ctypes.c_size_t()
+        t = ctypes.c_size_t()
+        N.check(N.load().fe_device_info(None, None, None, ctypes.byref(f), ctypes.byref(t)))
+        return int(f.value - self.hbm_reserve * t.value)
+
+    def _get_batch(self, req: Request) -> Optional[_Batch]:
+        key = (req.kind, req.side, self.precision)
+        b = self.batches.get(key)
+        if b is not None:
+            return b
+        P = _class_problem(req.kind, req.side, self.precision, self.slots)
+        P.lower()
+        need = estimate_bytes(P)
+        while need > self._free_bytes():
+            idle = [k for k, bb in self.batches.items() if not bb.active()]
+            if not idle:
+                return None  # admission refused for now: not enough HBM
+            victim = min(idle, key=lambda k: self.batches[k].last_used)
+            del self.batches[victim]
+            self.torch.cuda.synchronize()
+        P.initialise()
+        b = _Batch(key, P, self.slots, self.torch.cuda.Stream())
+        self.batches[key] = b
+        return b
+
+    def _admit(self, req: Request, now: float) -> bool:
+        b = self._get_batch(req)
+        if b is None:
+            return False
+        s = b.free_slot()
+        if s < 0:
+            return False
+        P = b.P
+        P.set_parameter_vector(_request_params(req, P), replica=s)
+        with self.torch.cuda.stream(b.stream):
+            P.x_dev[s * b.n_dof:(s + 1) * b.n_dof].copy_(self.torch.as_tensor(b.x0, device="cuda"))
+        b.req[s] = req
+        req.t_admit = now
+        return True
+
+    def _residual_norms(self, b: _Batch) -> List[float]:
+        out = []
+        for s in range(b.slots):
+            if b.req[s] is None:
+                out.append(0.0)
+                continue
+            v = ctypes.c_double()
+            ptr = b.P.R_dev.data_ptr() + 8 * s * b.n_dof
+            N.check(N.load().fe_residual_max(b.P._h, ptr, b.n_dof, ctypes.byref(v),
+                                             ctypes.c_void_p(b.stream.cuda_stream)))
+            out.append(v.value)
+        return out
+
+    def _solve(self, vals: np.ndarray, R: np.ndarray, b: _Batch) -> np.ndarray:
+        import scipy.sparse as sp
+        import scipy.sparse.linalg as spla
+        A = sp.csr_matrix((vals.astype(np.float64), b.ci0, b.rp0), shape=(b.n_dof, b.n_dof))
+        return spla.splu(A.tocsc()).solve(R)
+
+    def _step(self, b: _Batch, t0: float) -> List[Request]:
+        """One Newton step of every active replica of a batch."""
+        torch = self.torch
+        P = b.P
+        done = []
+        with torch.cuda.stream(b.stream):
+            P.assemble_device(with_jacobian=True, stream=b.stream.cuda_stream)
+            self.launches += P.launch_count(True)
+            norms = self._residual_norms(b)
+            R = P.R_dev[:P.n_dof].cpu().numpy() if any(r is not None for r in b.req) else None
+            J = P.J_dev[:P.nnz].cpu().numpy()
+        futs = {}
+        for s, req in enumerate(b.req):
+            if req is None:
+                continue
+            req.residuals.append(norms[s])
+            if norms[s] < self.tol or req.newton_iterations >= self.max_newton or not np.isfinite(norms[s]):
+                if norms[s] >= self.tol:
+                    req.error = f"Newton did not converge: {req.residuals}"
+                req.dofs = P.x_dev[s * b.n_dof:(s + 1) * b.n_dof].cpu().numpy()
+                req.t_done = time.perf_counter() - t0
+                b.req[s] = None
+                done.append(req)
+                continue
+            Rs = R[s * b.n_dof:(s + 1) * b.n_dof]
+            Js = J[s * b.nnz:(s + 1) * b.nnz]
+            futs[s] = self.pool.submit(self._solve, Js, Rs, b)
+        for s, f in futs.items():
+            dx = f.result()
+            with torch.cuda.stream(b.stream):
+                sl = P.x_dev[s * b.n_dof:(s + 1) * b.n_dof]
+                sl -= torch.as_tensor(dx, device="cuda")
+            b.req[s].newton_iterations += 1
+        b.last_used = time.perf_counter()
+        return done
+
+    def run(self, requests: List[Request], realtime: bool = True) -> List[Request]:
+        """Serve a stream; arrivals are honoured in real time."""
+        pending = sorted(requests, key=lambda r: r.arrival)
+        waiting: List[Request] = []
+        finished: List[Request] = []
+        t0 = time.perf_counter()
+        i = 0
+        while len(finished) < len(requests):
+            now = time.perf_counter() - t0
+            while i < len(pending) and (pending[i].arrival <= now or not realtime):
+                waiting.append(pending[i])
+                i += 1
+            still = []
+            for r in waiting:
+                if not self._admit(r, time.perf_counter() - t0):
+                    still.append(r)
+            waiting = still
+            busy = [b for b in self.batches.values() if b.active()]
+            if not busy:
+                if i < len(pending) and realtime:
+                    time.sleep(max(0.0, min(0.01, pending[i].arrival - now)))
+                elif waiting and not busy:
+                    raise RuntimeError("requests cannot be admitted (device memory)")
+                continue
+            # step every active batch; their GPU work runs on separate streams
+            steps = [self.stepper.submit(self._step, b, t0) for b in busy]
+            for f in steps:
+                finished += f.result()
+        self.torch.cuda.synchronize()
+        return finished
+
+
+def serve_sequential(requests: List[Request], precision: str = "fp64", tol: float = 1e-10,
+                     realtime: bool = True) -> List[Request]:
+    """The plain path: requests one at a time in arrival order, one problem
+    per request (resident meshes cached per class), Newton with SuperLU."""
+    cache: Dict[tuple, tuple] = {}
+    t0 = time.perf_counter()
+    for req in sorted(requests, key=lambda r: r.arrival):
+        now = time.perf_counter() - t0
+        if realtime and req.arrival > now:
+            time.sleep(req.arrival - now)
+        key = (req.kind, req.side)
+        if key not in cache:
+            P = _class_problem(req.kind, req.side, precision, 1)
+            P.initialise()
+            cache[key] = (P, P.get_dofs().copy())
+        P, x0 = cache[key]
+        req.t_admit = time.perf_counter() - t0
+        P.set_parameter_vector(_request_params(req, P))
+        P.set_dofs(x0)
+        P.newton_solver_tolerance = tol
+        P.max_newton_iterations = 20
+        try:
+            req.residuals = P.solve()
+            req.newton_iterations = len(req.residuals) - 1
+        except Exception as e:  # recorded per request
+            req.error = str(e)
+        req.dofs = P.get_dofs()
+        req.t_done = time.perf_counter() - t0
+    return requests
+
+
+def summary(reqs: List[Request], wall: float) -> dict:
+    lat = np.array([r.latency for r in reqs if r.error is None])
+    return {"requests": len(reqs), "errors": sum(r.error is not None for r in reqs),
+            "p50_s": float(np.percentile(lat, 50)) if lat.size else None,
+            "p99_s": float(np.percentile(lat, 99)) if lat.size else None,
+            "solves_per_s": len(reqs) / wall if wall > 0 else None,
+            "mean_newton_iterations": float(np.mean([r.newton_iterations for r in reqs]))}

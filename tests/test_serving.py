@@ -1,0 +1,51 @@
+"""Serving: continuous batching of assemble + Newton requests.
+
+A request's result is the same alone and in a mix (bit-identical dofs);
+every request converges to the FP64 oracle's solution within 1e-10; the
+stream summary reports p50/p99 latency."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_solution(req):
+    from pyoomph_gb300 import workloads as W
+    if req.kind == "poisson":
+        OP = O.poisson_problem(O.mesh(O.Q2_QUAD, req.side, req.side), W.draw_gaussians(req.seed, 8, 2))
+    else:
+        OP = O.navier_stokes_problem(O.mesh(O.P2_TRI, req.side, req.side), rho=1.0, mu=1.0 / req.Re)
+    O.newton(OP, tol=1e-10)
+    return OP.dofs()
+
+
+def test_request_alone_equals_request_in_mix_and_matches_oracle():
+    from pyoomph_gb300 import serving as S
+    probe = S.Request(0, "ns", 8, 0.0, seed=5, Re=70.0)
+    alone = S.Server(slots=3).run([probe], realtime=False)[0]
+    assert alone.error is None, alone.error
+    mix = [S.Request(1, "poisson", 8, 0.0, seed=1), S.Request(2, "ns", 8, 0.0, seed=2, Re=30.0),
+           S.Request(3, "poisson", 12, 0.0, seed=3), S.Request(4, "ns", 8, 0.0, seed=4, Re=90.0),
+           S.Request(0, "ns", 8, 0.0, seed=5, Re=70.0), S.Request(5, "poisson", 8, 0.0, seed=6)]
+    out = {r.rid: r for r in S.Server(slots=3).run(mix, realtime=False)}
+    assert all(r.error is None for r in out.values())
+    assert np.array_equal(out[0].dofs, alone.dofs)
+    for r in out.values():
+        x = _oracle_solution(r)
+        assert np.max(np.abs(r.dofs - x)) <= 1e-10 * max(1.0, np.max(np.abs(x)))
+
+
+def test_stream_summary_and_sequential_path_agree():
+    from pyoomph_gb300 import serving as S
+    reqs = S.make_stream(12, rate=200.0, seed=3, side_range=(8, 20))
+    import copy
+    seq = S.serve_sequential(copy.deepcopy(reqs), realtime=True)
+    bat = S.Server(slots=4).run(copy.deepcopy(reqs), realtime=True)
+    sb = {r.rid: r for r in bat}
+    for r in seq:
+        assert r.error is None and sb[r.rid].error is None
+        assert np.max(np.abs(r.dofs - sb[r.rid].dofs)) <= 1e-10 * max(1.0, np.max(np.abs(r.dofs)))
+    s = S.summary(bat, max(r.t_done for r in bat))
+    assert s["p50_s"] is not None and s["p99_s"] >= s["p50_s"] and s["errors"] == 0
