@@ -55,6 +55,10 @@ def mesh_is_affine(mesh: MeshData, rtol: float = 1e-12) -> bool:
     return True
 
 
+_KERNEL_CACHE: Dict[tuple, KernelSpec] = {}
+_CODE_CACHE: Dict[str, "N.Code"] = {}
+
+
 class NewtonSolverError(RuntimeError):
     """Raised when Newton diverges or exceeds its iteration cap
     (oomph's NewtonSolverError, problem.cc:9298)."""
@@ -165,15 +169,21 @@ class Problem:
         self.param_names = used
         self.params = np.array([params[p] for p in used], dtype=np.float64)
         t1 = time.perf_counter()
-        pw = differentiate(fields, mesh.dim, integrand, used)
         prec = "f64" if self.jacobian_precision in ("fp64", "f64", "double") else "f32"
         self._prec = prec
         if self.geometry == "auto":
             self.affine = mesh_is_affine(mesh)
         else:
             self.affine = self.geometry == "affine"
-        self.kernel: KernelSpec = generate_kernel(mesh.etype, pw, prec, epb=self.elems_per_block,
-                                                  affine=self.affine)
+        # the kernel depends on the weak form, element type, precision and
+        # geometry kind only -- not on the mesh size: cache it per process
+        key = (mesh.etype.name, tuple(fields), str(integrand), tuple(used), prec, self.affine, self.elems_per_block)
+        ks = _KERNEL_CACHE.get(key)
+        if ks is None:
+            pw = differentiate(fields, mesh.dim, integrand, used)
+            ks = generate_kernel(mesh.etype, pw, prec, epb=self.elems_per_block, affine=self.affine)
+            _KERNEL_CACHE[key] = ks
+        self.kernel: KernelSpec = ks
         self.timings.update(setup_mesh_s=t1 - t0, codegen_s=time.perf_counter() - t1)
         # nodal values, pins and equation numbers
         nval = len(fields)
@@ -246,7 +256,10 @@ class Problem:
         mesh, fields, prec = self.mesh, self.fields, self._prec
         n, nval, values, eqn = mesh.n_nodes, len(fields), self._values0, self.eqn
         t2 = time.perf_counter()
-        self.code = N.Code(self.kernel.source, self.kernel.name)
+        self.code = _CODE_CACHE.get(self.kernel.name)
+        if self.code is None:
+            self.code = N.Code(self.kernel.source, self.kernel.name)
+            _CODE_CACHE[self.kernel.name] = self.code
         t3 = time.perf_counter()
         # device problem
         L = N.load()
