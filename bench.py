@@ -50,7 +50,8 @@ def run_serving(args):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     reqs = S.make_stream(args.requests, rate=args.rate, seed=0, side_range=(16, args.size))
     out = {}
-    for name, fn in (("batched_fp32", lambda r: S.Server(slots=4, jacobian_precision="fp32").run(r)),
+    srv = S.Server(slots=4, jacobian_precision="fp32", workers=max(1, (os.cpu_count() or 2) - 2))
+    for name, fn in (("batched_fp32", lambda r: srv.run(r)),
                      ("sequential_fp64", lambda r: S.serve_sequential(r, precision="fp64"))):
         # warm-up: compile and build every mesh class once
         t0 = time.perf_counter()
@@ -59,6 +60,7 @@ def run_serving(args):
         out[name] = S.summary(done, wall)
         out[name]["wall_s"] = time.perf_counter() - t0
         out[name]["results"] = {r.rid: r.dofs for r in done}
+    srv.close()
     # each request's dofs agree between the two paths (FP32 vs FP64 Jacobian Newton)
     err = max(float(np.max(np.abs(out["batched_fp32"]["results"][k] - out["sequential_fp64"]["results"][k])) /
                     max(1.0, float(np.max(np.abs(out["sequential_fp64"]["results"][k])))))

@@ -14,8 +14,9 @@ One Newton step of a batch is one fused launch sequence for all its
 replicas (dof scatter, element kernel, residual and Jacobian scatter) on the
 batch's own CUDA stream, the per-replica residual max-norm on the device,
 and then, for each active replica, the linear solve J dx = R of its diagonal
-block on a CPU worker (SuperLU through scipy, the reference's default
-solver) -- so GPU assembly of one batch overlaps the solves of others.
+block in a worker process (SuperLU through scipy, the reference's default
+solver; processes because SuperLU holds the GIL) -- so the solves of all
+active requests run in parallel on the host cores while the GPU assembles.
 
 Results do not depend on the mix: every element, CSR slot and residual
 entry of a replica is computed from that replica's values only, in a fixed
@@ -29,7 +30,6 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import ctypes
-import heapq
 import time
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Tuple
@@ -113,6 +113,16 @@ def estimate_bytes(P) -> int:
     return int(E * nl * nl * (jb + 4) + nnz_est * (jb + 8 + 4) + E * nl * 12 + P.mesh.n_nodes * 64)
 
 
+def _splu_solve(vals: np.ndarray, colidx: np.ndarray, rowptr: np.ndarray, R: np.ndarray) -> np.ndarray:
+    """J dx = R with SuperLU (runs in a worker process: SuperLU holds the
+    GIL, so parallel solves need processes)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    n = R.shape[0]
+    A = sp.csr_matrix((vals.astype(np.float64), colidx, rowptr), shape=(n, n))
+    return spla.splu(A.tocsc()).solve(R)
+
+
 class _Batch:
     def __init__(self, key, P, slots: int, stream):
         self.key = key
@@ -147,7 +157,9 @@ class Server:
         self.precision = jacobian_precision
         self.tol = tol
         self.max_newton = max_newton
-        self.pool = cf.ThreadPoolExecutor(max_workers=workers)       # linear solves
+        import multiprocessing as mp
+        # linear solves in worker processes (spawned: safe after CUDA init)
+        self.pool = cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn"))
         self.stepper = cf.ThreadPoolExecutor(max_workers=16)         # one step per busy batch
         self.hbm_reserve = hbm_reserve
         self.batches: Dict[tuple, _Batch] = {}
@@ -208,12 +220,6 @@ class Server:
             out.append(v.value)
         return out
 
-    def _solve(self, vals: np.ndarray, R: np.ndarray, b: _Batch) -> np.ndarray:
-        import scipy.sparse as sp
-        import scipy.sparse.linalg as spla
-        A = sp.csr_matrix((vals.astype(np.float64), b.ci0, b.rp0), shape=(b.n_dof, b.n_dof))
-        return spla.splu(A.tocsc()).solve(R)
-
     def _step(self, b: _Batch, t0: float) -> List[Request]:
         """One Newton step of every active replica of a batch."""
         torch = self.torch
@@ -240,7 +246,7 @@ class Server:
                 continue
             Rs = R[s * b.n_dof:(s + 1) * b.n_dof]
             Js = J[s * b.nnz:(s + 1) * b.nnz]
-            futs[s] = self.pool.submit(self._solve, Js, Rs, b)
+            futs[s] = self.pool.submit(_splu_solve, Js, b.ci0, b.rp0, Rs)
         for s, f in futs.items():
             dx = f.result()
             with torch.cuda.stream(b.stream):
@@ -249,6 +255,10 @@ class Server:
             b.req[s].newton_iterations += 1
         b.last_used = time.perf_counter()
         return done
+
+    def close(self) -> None:
+        self.pool.shutdown(wait=True)
+        self.stepper.shutdown(wait=True)
 
     def run(self, requests: List[Request], realtime: bool = True) -> List[Request]:
         """Serve a stream; arrivals are honoured in real time."""
