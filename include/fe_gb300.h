@@ -119,6 +119,9 @@ typedef struct fe_problem_desc {
   const double *params;     /* global parameters read by the element code */
   int jac_precision;        /* FE_JAC_F64 or FE_JAC_F32 */
   int params_stride;        /* parameters per replica (0 = one set for all elements) */
+  int n_history;            /* previous time levels of the nodal values kept (BDF) */
+  const double *x0;         /* host [n_nodes * dim] Lagrangian positions (NULL: = x) */
+  int fused;                /* 1: every domain shares one fused code, run as one launch */
 } fe_problem_desc_t;
 
 /*
@@ -148,6 +151,15 @@ int fe_problem_pattern_device(const fe_problem_t *p, const int32_t **rowptr,
 int fe_problem_set_values(fe_problem_t *p, const double *values_host);
 /* Read the nodal values back to the host. */
 int fe_problem_get_values(const fe_problem_t *p, double *values_host);
+/* Time history (implicit time stepping, MultiTimeStepper of
+ * timestepper.hpp:46-108): level 0 is the previous step's values.
+ * set_history writes one level from the host; shift_history moves every
+ * level one step back and stores the current values as level 0. */
+int fe_problem_set_history(fe_problem_t *p, int level, const double *values_host);
+int fe_problem_shift_history(fe_problem_t *p);
+/* Overwrite the nodal positions (moving meshes keep them as dofs). */
+int fe_problem_set_positions(fe_problem_t *p, const double *x_host);
+
 /* Update the global parameters (host array, n_params values). */
 int fe_problem_set_params(fe_problem_t *p, const double *params_host);
 

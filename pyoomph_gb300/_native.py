@@ -26,7 +26,8 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_problem_pattern_device", "fe_problem_set_values", "fe_problem_get_values",
            "fe_problem_set_params", "fe_assemble", "fe_assemble_host", "fe_residual_max", "fe_dof_update",
            "fe_problem_check", "fe_problem_launch_count", "fe_problem_set_timing", "fe_problem_stage_times", "fe_pattern_host",
-           "fe_residual_max_noalloc", "fe_residual_max_noalloc_limit", "fe_problem_element_buffers"]
+           "fe_residual_max_noalloc", "fe_residual_max_noalloc_limit", "fe_problem_element_buffers",
+           "fe_problem_set_history", "fe_problem_shift_history", "fe_problem_set_positions"]
 
 
 def _header_stamp() -> str:
@@ -79,6 +80,9 @@ class ProblemDesc(ctypes.Structure):
         ("params", ctypes.c_void_p),
         ("jac_precision", ctypes.c_int),
         ("params_stride", ctypes.c_int),
+        ("n_history", ctypes.c_int),
+        ("x0", ctypes.c_void_p),
+        ("fused", ctypes.c_int),
     ]
 
 
@@ -131,6 +135,9 @@ def load(build_if_missing: bool = True):
         L.fe_pattern_host.argtypes = [ctypes.POINTER(ProblemDesc), vp, vp, vp]
         L.fe_residual_max_noalloc.argtypes = [vp, i64, vp, vp]
         L.fe_problem_element_buffers.argtypes = [vp, c_int, vp, vp]
+        L.fe_problem_set_history.argtypes = [vp, c_int, vp]
+        L.fe_problem_shift_history.argtypes = [vp]
+        L.fe_problem_set_positions.argtypes = [vp, vp]
         L.fe_residual_max_noalloc_limit.restype = i64
         _lib = L
         return L

@@ -19,6 +19,19 @@ struct FeElemArgs {
   int *status;          // device status word (0 = ok)
   long long replica_elems; // > 0: the domain is a stack of replicas of this many elements each
   int params_stride;       // parameters per replica (replica r reads params + r * params_stride)
+  const double *hist;      // [n_hist][n_nodes * nval] nodal values of previous time levels
+  const double *x0;        // [n_nodes * dim] Lagrangian (reference) positions
+  int n_hist;
+  long long hist_stride;    // entries per history level (n_nodes * nval)
+};
+
+// One launch over several domains (bulk, interface, contact line ...): block
+// b runs domain k for block_start[k] <= b < block_start[k+1].
+#define FE_MAX_FUSED 4
+struct FeFusedArgs {
+  FeElemArgs d[FE_MAX_FUSED];
+  int block_start[FE_MAX_FUSED + 1];
+  int n_domains;
 };
 
 #endif

@@ -252,9 +252,9 @@ struct Domain {
 struct fe_problem {
   int dim = 0, nval = 0, jac_prec = FE_JAC_F64;
   long long n_nodes = 0, n_dof = 0, nnz = 0;
-  int n_params = 0, params_stride = 0;
+  int n_params = 0, params_stride = 0, n_hist = 0, fused = 0;
   std::vector<Domain> domains;
-  DevBuf x, values, eqn, params, status;
+  DevBuf x, values, eqn, params, status, hist, x0;
   DevBuf rowptr, colidx, cptr, cidx, rptr, ridx;
   DevBuf partial;
   // the domain buffers are one allocation per kind, addressed by offsets:
@@ -509,26 +509,54 @@ int validate_desc(const fe_problem_desc_t *desc, bool need_code) {
   return FE_OK;
 }
 
+FeElemArgs domain_args(fe_problem *p, Domain &d, int flag) {
+  FeElemArgs a;
+  a.x = p->x.as<double>();
+  a.conn = d.conn.as<int>();
+  a.values = p->values.as<double>();
+  a.params = p->params.as<double>();
+  a.tables = d.tables.as<double>();
+  a.rbuf = p->rbuf_all.as<double>() + d.rbase;
+  if (p->jac_prec == FE_JAC_F64)
+    a.jbuf = (void *)(p->jbuf_all.as<double>() + d.jbase);
+  else
+    a.jbuf = (void *)(p->jbuf_all.as<float>() + d.jbase);
+  a.n_elem = d.n_elem;
+  a.nval = p->nval;
+  a.flag = flag;
+  a.status = p->status.as<int>();
+  a.replica_elems = d.replica_elems;
+  a.params_stride = p->params_stride;
+  a.hist = p->hist.as<double>();
+  a.x0 = p->x0.p ? p->x0.as<double>() : p->x.as<double>();
+  a.n_hist = p->n_hist;
+  a.hist_stride = (long long)p->n_nodes * p->nval;
+  return a;
+}
+
 int launch_elements(fe_problem *p, int flag, cudaStream_t st) {
+  if (p->fused) {
+    FeFusedArgs fa;
+    memset(&fa, 0, sizeof(fa));
+    int threads = 32, smem = 0, nb = 0, k = 0;
+    for (Domain &d : p->domains) {
+      fa.d[k] = domain_args(p, d, flag);
+      fa.block_start[k] = nb;
+      nb += (int)((d.n_elem + d.epb - 1) / d.epb);
+      threads = std::max(threads, d.threads);
+      smem = std::max(smem, d.smem);
+      k++;
+    }
+    fa.block_start[k] = nb;
+    fa.n_domains = k;
+    if (nb == 0) return FE_OK;
+    void *kp[] = {&fa};
+    CUDA_TRY(cudaLaunchKernel((const void *)p->domains[0].code->func, dim3(nb), dim3(threads), kp, (size_t)smem, st));
+    return FE_OK;
+  }
   for (Domain &d : p->domains) {
     if (d.n_elem == 0) continue;
-    FeElemArgs a;
-    a.x = p->x.as<double>();
-    a.conn = d.conn.as<int>();
-    a.values = p->values.as<double>();
-    a.params = p->params.as<double>();
-    a.tables = d.tables.as<double>();
-    a.rbuf = p->rbuf_all.as<double>() + d.rbase;
-    if (p->jac_prec == FE_JAC_F64)
-      a.jbuf = (void *)(p->jbuf_all.as<double>() + d.jbase);
-    else
-      a.jbuf = (void *)(p->jbuf_all.as<float>() + d.jbase);
-    a.n_elem = d.n_elem;
-    a.nval = p->nval;
-    a.flag = flag;
-    a.status = p->status.as<int>();
-    a.replica_elems = d.replica_elems;
-    a.params_stride = p->params_stride;
+    FeElemArgs a = domain_args(p, d, flag);
     void *kp[] = {&a};
     unsigned grid = (unsigned)((d.n_elem + d.epb - 1) / d.epb);
     CUDA_TRY(cudaLaunchKernel((const void *)d.code->func, dim3(grid), dim3(d.threads), kp, (size_t)d.smem, st));
@@ -746,6 +774,14 @@ int fe_problem_create(const fe_problem_desc_t *desc, fe_problem_t **out) {
   P->jac_prec = desc->jac_precision;
   P->n_params = desc->n_params;
   P->params_stride = desc->params_stride;
+  P->n_hist = std::max(0, desc->n_history);
+  P->fused = desc->fused ? 1 : 0;
+  if (P->fused) {
+    if (desc->n_domains > FE_MAX_FUSED) return fail(FE_ERR_ARG, "at most %d fused domains", FE_MAX_FUSED);
+    for (int di = 1; di < desc->n_domains; di++)
+      if (desc->domains[di].code != desc->domains[0].code)
+        return fail(FE_ERR_ARG, "fused domains must share one code");
+  }
   std::vector<const int32_t *> conn_h;
   long long jtot = 0, rtot = 0;
   for (int di = 0; di < desc->n_domains; di++) {
@@ -773,13 +809,25 @@ int fe_problem_create(const fe_problem_desc_t *desc, fe_problem_t **out) {
     rtot += dd.n_elem * (long long)dd.nlocal;
     if ((rc = d.conn.upload(dd.conn, sizeof(int32_t) * dd.n_elem * dd.nnode_el))) return rc;
     if (dd.n_tables > 0 && (rc = d.tables.upload(dd.tables, sizeof(double) * dd.n_tables))) return rc;
-    if (d.smem > 48 * 1024)
+    if (d.smem > 48 * 1024 && !P->fused)
       CUDA_TRY(cudaFuncSetAttribute((const void *)d.code->func, cudaFuncAttributeMaxDynamicSharedMemorySize, d.smem));
     conn_h.push_back(dd.conn);
     P->domains.push_back(std::move(d));
   }
   if (jtot > 0xffffffffLL) return fail(FE_ERR_ARG, "element Jacobian space %lld exceeds 2^32 entries", jtot);
+  if (P->fused) {
+    int smem = 0;
+    for (Domain &d : P->domains) smem = std::max(smem, d.smem);
+    if (smem > 48 * 1024)
+      CUDA_TRY(cudaFuncSetAttribute((const void *)P->domains[0].code->func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    smem));
+  }
   if ((rc = P->x.upload(desc->x, sizeof(double) * desc->n_nodes * desc->dim))) return rc;
+  if (desc->x0 && (rc = P->x0.upload(desc->x0, sizeof(double) * desc->n_nodes * desc->dim))) return rc;
+  if (P->n_hist > 0) {
+    if ((rc = P->hist.alloc(sizeof(double) * P->n_hist * desc->n_nodes * desc->nval))) return rc;
+    CUDA_TRY(cudaMemset(P->hist.p, 0, P->hist.bytes));
+  }
   if ((rc = P->eqn.upload(desc->eqn, sizeof(int32_t) * desc->n_nodes * desc->nval))) return rc;
   if ((rc = P->values.alloc(sizeof(double) * desc->n_nodes * desc->nval))) return rc;
   CUDA_TRY(cudaMemset(P->values.p, 0, P->values.bytes));
@@ -848,6 +896,29 @@ int fe_problem_set_values(fe_problem_t *p, const double *values_host) {
 int fe_problem_get_values(const fe_problem_t *p, double *values_host) {
   if (!p || !values_host) return fail(FE_ERR_ARG, "null argument");
   CUDA_TRY(cudaMemcpy(values_host, p->values.p, p->values.bytes, cudaMemcpyDeviceToHost));
+  return FE_OK;
+}
+
+int fe_problem_set_history(fe_problem_t *p, int level, const double *values_host) {
+  if (!p || !values_host || level < 0 || level >= p->n_hist) return fail(FE_ERR_ARG, "bad history level");
+  const size_t n = sizeof(double) * p->n_nodes * p->nval;
+  CUDA_TRY(cudaMemcpy(p->hist.as<char>() + n * level, values_host, n, cudaMemcpyHostToDevice));
+  return FE_OK;
+}
+
+int fe_problem_shift_history(fe_problem_t *p) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  if (p->n_hist == 0) return FE_OK;
+  const size_t n = sizeof(double) * p->n_nodes * p->nval;
+  for (int k = p->n_hist - 1; k >= 1; k--)
+    CUDA_TRY(cudaMemcpy(p->hist.as<char>() + n * k, p->hist.as<char>() + n * (k - 1), n, cudaMemcpyDeviceToDevice));
+  CUDA_TRY(cudaMemcpy(p->hist.p, p->values.p, n, cudaMemcpyDeviceToDevice));
+  return FE_OK;
+}
+
+int fe_problem_set_positions(fe_problem_t *p, const double *x_host) {
+  if (!p || !x_host) return fail(FE_ERR_ARG, "null argument");
+  CUDA_TRY(cudaMemcpy(p->x.p, x_host, p->x.bytes, cudaMemcpyHostToDevice));
   return FE_OK;
 }
 

@@ -19,8 +19,13 @@ import sympy as sp
 
 Expr = Union[sp.Expr, sp.MatrixBase, float, int]
 
-# coordinate symbols x0, x1, x2 (Eulerian position at the integration point)
+# coordinate symbols x0, x1, x2 (Eulerian position at the integration point;
+# on moving meshes these are the values of the position fields mesh_x/y/z)
 X = sp.symbols("x0:3", real=True)
+# Lagrangian (reference) coordinates and the interface normal
+LAG = sp.symbols("XL0:3", real=True)
+NORMAL = sp.symbols("N0:3", real=True)
+MESH_FIELDS = ("mesh_x", "mesh_y", "mesh_z")
 
 
 class _Registry:
@@ -33,6 +38,9 @@ class _Registry:
         self.test_grad: Dict[str, Tuple[sp.Symbol, ...]] = {}
         self.params: Dict[str, sp.Symbol] = {}
         self.vector_fields: Dict[str, List[str]] = {}
+        self.lgrad: Dict[str, Tuple[sp.Symbol, ...]] = {}
+        self.test_lgrad: Dict[str, Tuple[sp.Symbol, ...]] = {}
+        self.dt: Dict[str, sp.Symbol] = {}
 
     def field(self, name: str):
         if name not in self.value:
@@ -40,6 +48,9 @@ class _Registry:
             self.grad[name] = tuple(sp.Symbol(f"U_{name}__x{i}", real=True) for i in range(3))
             self.test[name] = sp.Symbol(f"T_{name}", real=True)
             self.test_grad[name] = tuple(sp.Symbol(f"T_{name}__x{i}", real=True) for i in range(3))
+            self.lgrad[name] = tuple(sp.Symbol(f"U_{name}__L{i}", real=True) for i in range(3))
+            self.test_lgrad[name] = tuple(sp.Symbol(f"T_{name}__L{i}", real=True) for i in range(3))
+            self.dt[name] = sp.Symbol(f"U_{name}__t", real=True)
         return self.value[name]
 
 
@@ -60,17 +71,28 @@ def register_vector_field(name: str, comps: List[str]) -> None:
 
 
 def var(name: str) -> Expr:
-    """Field value (scalar symbol, or a column vector for a vector field)."""
+    """Field value (scalar symbol, or a column vector for a vector field).
+    ``mesh``/``coordinate``: the Eulerian position; ``lagrangian``: the
+    reference position; ``normal``: the outward unit normal (interfaces)."""
     if name in REG.vector_fields:
         return sp.Matrix([REG.field(c) for c in REG.vector_fields[name]])
-    if name == "coordinate":
+    if name in ("coordinate", "mesh"):
         return sp.Matrix(X[:dimension()])
+    if name == "lagrangian":
+        return sp.Matrix(LAG[:dimension()])
+    if name == "normal":
+        return sp.Matrix(NORMAL[:dimension()])
     if name.startswith("coordinate_"):
         return X["xyz".index(name[-1])]
     return REG.field(name)
 
 
 def testfunction(name: str) -> Expr:
+    if name == "mesh":
+        comps = list(MESH_FIELDS[:dimension()])
+        for c in comps:
+            REG.field(c)
+        return sp.Matrix([REG.test[c] for c in comps])
     if name in REG.vector_fields:
         comps = REG.vector_fields[name]
         for c in comps:
@@ -89,6 +111,50 @@ def parameter(name: str) -> sp.Symbol:
     if name not in REG.params:
         REG.params[name] = sp.Symbol(f"P_{name}", real=True)
     return REG.params[name]
+
+
+def mesh_velocity() -> Expr:
+    """d x / d t at fixed Lagrangian position (BDF weights of the step)."""
+    return sp.Matrix([REG.dt[REG.field(c) and c] for c in MESH_FIELDS[:dimension()]])
+
+
+def partial_t(f: Expr) -> Expr:
+    """Time derivative at fixed node of a field (or vector of fields)."""
+    if isinstance(f, sp.MatrixBase):
+        return sp.Matrix([partial_t(c) for c in f])
+    f = sp.sympify(f)
+    out = sp.Integer(0)
+    for s_ in f.free_symbols:
+        nm = s_.name
+        if nm.startswith("U_") and "__" not in nm:
+            out += sp.diff(f, s_) * REG.dt[nm[2:]]
+        elif s_ in X:
+            out += sp.diff(f, s_) * REG.dt[MESH_FIELDS[X.index(s_)]]
+    return out
+
+
+def _d_dL(e: sp.Expr, i: int) -> sp.Expr:
+    """d/dxi_i (Lagrangian) of a pointwise expression."""
+    e = sp.sympify(e)
+    out = sp.Integer(0)
+    for s_ in e.free_symbols:
+        de = sp.diff(e, s_)
+        if de == 0:
+            continue
+        nm = s_.name
+        if nm.startswith("U_") and "__" not in nm:
+            out += de * REG.lgrad[nm[2:]][i]
+        elif nm.startswith("T_") and "__" not in nm:
+            out += de * REG.test_lgrad[nm[2:]][i]
+        elif s_ in X:
+            out += de * REG.lgrad[MESH_FIELDS[X.index(s_)]][i]
+        elif s_ in LAG:
+            out += de * (1 if LAG.index(s_) == i else 0)
+        elif nm.startswith("P_"):
+            continue
+        else:
+            raise NotImplementedError(f"Lagrangian derivative of {nm} is not supported")
+    return out
 
 
 def _d_dx(e: sp.Expr, i: int) -> sp.Expr:
@@ -114,18 +180,35 @@ def _d_dx(e: sp.Expr, i: int) -> sp.Expr:
     return out
 
 
-def grad(e: Expr) -> Expr:
+def grad(e: Expr, lagrangian: bool = False, coordsys=None) -> Expr:
     """Gradient.  Scalar -> column vector g_i = d e/dx_i; vector u ->
-    matrix G[i, j] = d u_j / d x_i (pyoomph's convention)."""
+    matrix G[i, j] = d u_j / d x_i (pyoomph's convention).  With
+    ``lagrangian`` the derivatives are with respect to the reference
+    position.  In the axisymmetric system a 2-vector (u_r, u_z) has the 3x3
+    gradient with the hoop entry G[2, 2] = u_r / r."""
     d = dimension()
+    dd = _d_dL if lagrangian else _d_dx
+    cs = coordsys or _COORDSYS[0]
     if isinstance(e, sp.MatrixBase):
-        return sp.Matrix(d, e.shape[0], lambda i, j: _d_dx(e[j], i))
-    return sp.Matrix([_d_dx(e, i) for i in range(d)])
+        G = sp.Matrix(d, e.shape[0], lambda i, j: dd(e[j], i))
+        if isinstance(cs, AxisymmetricCoordinateSystem) and e.shape[0] == 2:
+            r = LAG[0] if lagrangian else X[0]
+            G3 = sp.zeros(3, 3)
+            G3[:2, :2] = G
+            G3[2, 2] = e[0] / r
+            return G3
+        return G
+    return sp.Matrix([dd(e, i) for i in range(d)])
 
 
-def div(u: Expr) -> sp.Expr:
+def div(u: Expr, coordsys=None) -> sp.Expr:
+    """Divergence (axisymmetric: + u_r / r)."""
     d = dimension()
-    return sum(_d_dx(u[i], i) for i in range(d))
+    cs = coordsys or _COORDSYS[0]
+    out = sum(_d_dx(u[i], i) for i in range(d))
+    if isinstance(cs, AxisymmetricCoordinateSystem):
+        out += u[0] / X[0]
+    return out
 
 
 def transpose(A: sp.MatrixBase) -> sp.MatrixBase:
@@ -136,8 +219,12 @@ def sym(A: sp.MatrixBase) -> sp.MatrixBase:
     return (A + A.T) / 2
 
 
-def identity_matrix() -> sp.MatrixBase:
-    return sp.eye(dimension())
+def identity_matrix(n: int = None) -> sp.MatrixBase:
+    return sp.eye(n or dimension())
+
+
+def trace(A: sp.MatrixBase) -> sp.Expr:
+    return A.trace()
 
 
 def dot(a: Expr, b: Expr) -> Expr:
@@ -178,6 +265,35 @@ _COORDSYS = [CartesianCoordinateSystem()]
 
 def set_coordinate_system(cs: CoordinateSystem) -> None:
     _COORDSYS[0] = cs
+
+
+class LagrangianIntegrand:
+    """An integrand over the reference (Lagrangian) configuration (``Weak``)."""
+
+    def __init__(self, expr):
+        self.expr = sp.sympify(expr)
+
+    def __mul__(self, c):
+        return LagrangianIntegrand(self.expr * c)
+
+    __rmul__ = __mul__
+
+    def __neg__(self):
+        return LagrangianIntegrand(-self.expr)
+
+
+def Weak(a: Expr, b: Expr, coordinate_system: CoordinateSystem = None) -> LagrangianIntegrand:
+    """a : b integrated over the Lagrangian configuration dX."""
+    cs = coordinate_system or CartesianCoordinateSystem()
+    A, B = (sp.Matrix(a), sp.Matrix(b)) if isinstance(a, sp.MatrixBase) or isinstance(b, sp.MatrixBase) else (a, b)
+    if isinstance(A, sp.MatrixBase):
+        if A.shape != B.shape:
+            raise ValueError(f"Weak: shape mismatch {A.shape} vs {B.shape}")
+        prod = sum(A[i] * B[i] for i in range(len(A)))
+    else:
+        prod = sp.sympify(A) * sp.sympify(B)
+    meas = 2 * sp.pi * LAG[0] if isinstance(cs, AxisymmetricCoordinateSystem) else 1
+    return LagrangianIntegrand(prod * meas)
 
 
 def weak(a: Expr, b: Expr, coordinate_system: CoordinateSystem = None) -> sp.Expr:

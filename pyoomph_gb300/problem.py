@@ -303,7 +303,7 @@ class Problem:
         desc = N.ProblemDesc(mesh.dim, mesh.n_nodes, len(self.fields), k["x"].ctypes.data, k["eqn"].ctypes.data,
                              self.n_dof, 1, doms, len(self.params), k["params"].ctypes.data,
                              N.FE_JAC_F64 if self._prec == "f64" else N.FE_JAC_F32,
-                             getattr(self, "params_stride", 0))
+                             getattr(self, "params_stride", 0), 0, None, 0)
         return desc, doms, keep
 
     def host_pattern(self) -> Tuple[np.ndarray, np.ndarray]:

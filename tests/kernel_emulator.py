@@ -47,7 +47,8 @@ class _Args(ctypes.Structure):
                 ("params", ctypes.c_void_p), ("tables", ctypes.c_void_p), ("rbuf", ctypes.c_void_p),
                 ("jbuf", ctypes.c_void_p), ("n_elem", ctypes.c_longlong), ("nval", ctypes.c_int),
                 ("flag", ctypes.c_int), ("status", ctypes.c_void_p), ("replica_elems", ctypes.c_longlong),
-                ("params_stride", ctypes.c_int)]
+                ("params_stride", ctypes.c_int), ("hist", ctypes.c_void_p), ("x0", ctypes.c_void_p),
+                ("n_hist", ctypes.c_int), ("hist_stride", ctypes.c_longlong)]
 
 
 def build(ks) -> ctypes.CDLL:
@@ -89,6 +90,6 @@ def run(ks, x, conn, values, params, flag: int = 1):
     jbuf = np.zeros((E, nloc, nloc), dtype=jt)
     status = np.zeros(4, dtype=np.int32)
     a = _Args(x.ctypes.data, conn.ctypes.data, values.ctypes.data, params.ctypes.data, tables.ctypes.data,
-              rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data, 0, 0)
+              rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data, 0, 0, None, None, 0, 0)
     L.fe_emu_run(ctypes.byref(a), (E + ks.epb - 1) // ks.epb)
     return rbuf, jbuf, status
