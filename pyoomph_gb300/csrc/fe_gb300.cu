@@ -1098,8 +1098,13 @@ int fe_problem_launch_count(const fe_problem_t *p, int flags) {
   if (!p) return -1;
   int n = 0;
   if (flags & FE_ASSEMBLE_VALUES_FROM_DOFS) n++;
-  for (const Domain &d : p->domains)
-    if (d.n_elem) n++;
+  if (p->fused) {
+    for (const Domain &d : p->domains)
+      if (d.n_elem) { n++; break; }
+  } else {
+    for (const Domain &d : p->domains)
+      if (d.n_elem) n++;
+  }
   if (flags & FE_ASSEMBLE_RESIDUAL) n++;
   if ((flags & FE_ASSEMBLE_JACOBIAN) && p->nnz > 0) n++;
   return n;

@@ -93,3 +93,66 @@ def run(ks, x, conn, values, params, flag: int = 1):
               rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data, 0, 0, None, None, 0, 0)
     L.fe_emu_run(ctypes.byref(a), (E + ks.epb - 1) // ks.epb)
     return rbuf, jbuf, status
+
+
+class _FusedArgs(ctypes.Structure):
+    _fields_ = [("d", _Args * 4), ("block_start", ctypes.c_int * 5), ("n_domains", ctypes.c_int)]
+
+
+def build_fused(fk) -> ctypes.CDLL:
+    """Emulator library of a fused multi-domain kernel (pyoomph_gb300.ale)."""
+    src = re.sub(r"#define FE_NT \d+", "#define FE_NT 1", fk.source)
+    src = src.replace("extern __shared__ __align__(16) unsigned char fe_smem[];", "")
+    body = PRELUDE + src + (
+        f'\nextern "C" void fe_emu_run_fused(const FeFusedArgs *a, int nblocks) {{\n'
+        f'  for (int b = 0; b < nblocks; ++b) {{\n'
+        f'    memset(fe_smem, 0xff, sizeof(fe_smem));\n'
+        f'    blockIdx.x = b; {fk.name}(*a); }}\n}}\n')
+    h = hashlib.sha1(body.encode()).hexdigest()[:16]
+    os.makedirs(OUT, exist_ok=True)
+    so = os.path.join(OUT, f"emu_{h}.so")
+    if not os.path.exists(so):
+        cpp = os.path.join(OUT, f"emu_{h}.cpp")
+        with open(cpp, "w") as f:
+            f.write(body)
+        subprocess.run(["g++", "-std=c++17", "-O1", "-fPIC", "-shared", "-ffp-contract=off", "-I", CSRC, cpp,
+                        "-o", so + ".tmp"], check=True)
+        os.replace(so + ".tmp", so)
+    L = ctypes.CDLL(so)
+    L.fe_emu_run_fused.argtypes = [ctypes.POINTER(_FusedArgs), ctypes.c_int]
+    return L
+
+
+def run_fused(fk, conns, values, hist, x0, params, flag: int = 1):
+    """Element residuals and matrices of every domain of a fused kernel.
+    values, hist[k]: [n_nodes, nval]; x0: [n_nodes, dim]; conns: per domain
+    [E_k, nnode_k]."""
+    L = build_fused(fk)
+    nval = values.shape[1]
+    values = np.ascontiguousarray(values, dtype=np.float64)
+    hist_arr = np.ascontiguousarray(np.stack(hist), dtype=np.float64)
+    x0 = np.ascontiguousarray(x0, dtype=np.float64)
+    params = np.ascontiguousarray(params, dtype=np.float64)
+    status = np.zeros(4, dtype=np.int32)
+    fa = _FusedArgs()
+    keep, outs = [], []
+    nb = 0
+    jt = np.float64 if fk.jac_precision == "f64" else np.float32
+    for k, (dc, conn) in enumerate(zip(fk.domains, conns)):
+        conn = np.ascontiguousarray(conn, dtype=np.int32)
+        tables = np.ascontiguousarray(dc.dtype.tables(), dtype=np.float64)
+        E = conn.shape[0]
+        rbuf = np.zeros((E, dc.nloc))
+        jbuf = np.zeros((E, dc.nloc, dc.nloc), dtype=jt)
+        keep += [conn, tables]
+        outs.append((rbuf, jbuf))
+        fa.d[k] = _Args(x0.ctypes.data, conn.ctypes.data, values.ctypes.data, params.ctypes.data,
+                        tables.ctypes.data, rbuf.ctypes.data, jbuf.ctypes.data, E, nval, flag,
+                        status.ctypes.data, 0, 0, hist_arr.ctypes.data, x0.ctypes.data, len(hist),
+                        values.size)
+        fa.block_start[k] = nb
+        nb += (E + dc.epb - 1) // dc.epb
+    fa.block_start[len(fk.domains)] = nb
+    fa.n_domains = len(fk.domains)
+    L.fe_emu_run_fused(ctypes.byref(fa), nb)
+    return outs, status
