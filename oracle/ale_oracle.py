@@ -190,13 +190,15 @@ def bulk_residual(loc: np.ndarray, X0e: np.ndarray, p: Dict[str, float]) -> np.n
         t10 = xs @ dpsi[q, :, 1]
         t11 = ys @ dpsi[q, :, 1]
         det = t00 * t11 - t01 * t10
+        # weight: sqrt of the metric determinant (fill_shape_info_at_s), |det t|
+        Jw = np.sqrt((t00 * t00 + t01 * t01) * (t10 * t10 + t11 * t11) - (t00 * t10 + t01 * t11) ** 2)
         # dpsi/dx_i = sum_a inv(t)[i][a] dpsi/ds_a, inv(t) = [[t11, -t01], [-t10, t00]] / det
         dpx = (t11[:, None] * dpsi[q, :, 0] - t01[:, None] * dpsi[q, :, 1]) / det[:, None]
         dpy = (-t10[:, None] * dpsi[q, :, 0] + t00[:, None] * dpsi[q, :, 1]) / det[:, None]
         d1x = (t11[:, None] * dpsi1[q, :, 0] - t01[:, None] * dpsi1[q, :, 1]) / det[:, None]
         d1y = (-t10[:, None] * dpsi1[q, :, 0] + t00[:, None] * dpsi1[q, :, 1]) / det[:, None]
         r = xs @ psi[q]
-        W = w[q] * det * 2 * math.pi * r
+        W = w[q] * Jw * 2 * math.pi * r
         u0, u1 = ux @ psi[q], uy @ psi[q]
         du0dx, du0dy = (ux * dpx).sum(1), (ux * dpy).sum(1)
         du1dx, du1dy = (uy * dpx).sum(1), (uy * dpy).sum(1)
@@ -218,6 +220,7 @@ def bulk_residual(loc: np.ndarray, X0e: np.ndarray, p: Dict[str, float]) -> np.n
         T10 = X0e[:, :, 0] @ dpsi[q, :, 1]
         T11 = X0e[:, :, 1] @ dpsi[q, :, 1]
         detL = T00 * T11 - T01 * T10
+        JL = np.sqrt((T00 * T00 + T01 * T01) * (T10 * T10 + T11 * T11) - (T00 * T10 + T01 * T11) ** 2)
         dPx = (T11[:, None] * dpsi[q, :, 0] - T01[:, None] * dpsi[q, :, 1]) / detL[:, None]
         dPy = (-T10[:, None] * dpsi[q, :, 0] + T00[:, None] * dpsi[q, :, 1]) / detL[:, None]
         Dx = xs - X0e[:, :, 0]
@@ -229,7 +232,7 @@ def bulk_residual(loc: np.ndarray, X0e: np.ndarray, p: Dict[str, float]) -> np.n
         S_xx = lam * tr + 2 * mum * e_xx
         S_yy = lam * tr + 2 * mum * e_yy
         S_xy = 2 * mum * e_xy
-        WL = w[q] * detL
+        WL = w[q] * JL
         for l in range(6):
             R[:, 15 + 2 * l] += WL * (S_xx * dPx[:, l] + S_xy * dPy[:, l])
             R[:, 16 + 2 * l] += WL * (S_xy * dPx[:, l] + S_yy * dPy[:, l])

@@ -39,6 +39,7 @@ from __future__ import annotations
 import ctypes
 import hashlib
 import math
+import re
 import time
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Tuple
@@ -279,6 +280,7 @@ class DomainCode:
     smem: int = 0
     nk: int = 0
     rows_needed: int = 0
+    flops: float = 0.0          # FP64 operations per element (FMA = 2), counted from the generated code
 
     def layout(self):
         """Local order: the nodal values node by node (fields in order), then
@@ -295,6 +297,11 @@ class DomainCode:
                     lnode.append(l)
                     lval.append(vi)
         return lnode, lval, slot
+
+
+def _ops(c_expr: str) -> int:
+    """Binary arithmetic operations in a generated C expression."""
+    return c_expr.count(" * ") + c_expr.count(" + ") + c_expr.count(" - ")
 
 
 def _sub_nodes(dc: DomainCode, f: int) -> List[int]:
@@ -450,6 +457,16 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     keys = sorted(terms)
     NK = max(1, len(keys))
     dc.nk = len(keys)
+    # interpolated components the pointwise code and the Jacobian terms read
+    used_u = set()
+    for e_ in rEc + rLc:
+        used_u |= {usym[s_] for s_ in sp.sympify(e_).free_symbols if s_ in usym}
+    for key in keys:
+        for t_ in terms[key]:
+            used_u |= {int(m_) for m_ in re.findall(r"U\[(\d+)\]", t_)}
+    used_t = set(rEn) | set(rLn) | {tc for tc, _ in keys}
+    lagr = (any(d + 1 <= u_ % NCU <= 2 * d for u_ in used_u) or any(d + 1 <= t_ % NCT for t_ in used_t)
+            or any(d + 1 <= ic % NCU <= 2 * d for _, ic in keys))
     # ---- local layout
     lnode, lval, slot = dc.layout()
     nloc = len(lnode)
@@ -499,6 +516,11 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     for key, j in eN.items():
         exprs.append(DN[key])
         outs.append(f"dN[{j}]")
+    fl_point = 0
+    if exprs:
+        repl, red = sp.cse(exprs, symbols=sp.numbered_symbols("t_"), optimizations="basic")
+        fl_point = sum(sp.count_ops(e) for _, e in repl) + sum(sp.count_ops(e) for e in red)
+    fl_point += sum(_ops(" + ".join(terms[key])) for key in keys) + 2 * ntc
     if exprs:
         body = _emit(exprs, names, False, outs, "  ")
         dlines = [ln for ln in body if ln.strip().startswith(("dE[", "dL[", "dN["))]
@@ -519,6 +541,8 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
         w(f"    C[{kk}] = {' + '.join(terms[key])};")
     w("  }")
     w("}")
+    rowof = [slot[(f, l)] for f in range(nf) for l in _sub_nodes(dc, f)]
+    w(f"__constant__ int c_rowof[NLOC] = {{{', '.join(map(str, rowof))}}};")
     w("__device__ __forceinline__ void run(const FeElemArgs& a, int blk, double* __restrict__ sW) {")
     w("  double* sPsi2 = sW + NQ;")
     w("  double* sDps2 = sPsi2 + NQ * NN;")
@@ -569,7 +593,8 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     if ed == d:
         w("    { double J; fe_metric_geometry<DIM, NN>(Xe, dps, g, J); wE = sW[q] * J;")
         w("      if (!(J > 0.0)) atomicExch(a.status, 1); }")
-        w("    { double J; fe_metric_geometry<DIM, NN>(X0, dps, gl, J); wL = sW[q] * J; }")
+        if lagr:
+            w("    { double J; fe_metric_geometry<DIM, NN>(X0, dps, gl, J); wL = sW[q] * J; }")
     elif ed == 1:
         if d != 2:
             raise NotImplementedError("line elements are implemented in 2D")
@@ -580,40 +605,50 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
         w("      wE = sW[q] * J; tau[0] = t0 / J; tau[1] = t1 / J; Nn[0] = tau[1]; Nn[1] = -tau[0];")
         w("      g[0][0] = t0 / am; g[0][1] = t1 / am; }")
     w("    for (int l = 0; l < NN; ++l) for (int i = 0; i < DIM; ++i) {")
-    w("      double s1 = 0.0, s2 = 0.0;")
-    w("      for (int b = 0; b < ED; ++b) { s1 += g[b][i] * dps[l * ED + b]; s2 += gl[b][i] * dps[l * ED + b]; }")
-    w("      dx[l * DIM + i] = s1; dX[l * DIM + i] = s2; }")
+    w("      double s1 = 0.0;")
+    w("      for (int b = 0; b < ED; ++b) s1 += g[b][i] * dps[l * ED + b];")
+    w("      dx[l * DIM + i] = s1; }")
     w("    for (int l = 0; l < N1; ++l) for (int i = 0; i < DIM; ++i) {")
-    w("      double s1 = 0.0, s2 = 0.0;")
-    w("      for (int b = 0; b < ED; ++b) { s1 += g[b][i] * dps1[l * ED + b]; s2 += gl[b][i] * dps1[l * ED + b]; }")
-    w("      dx1[l * DIM + i] = s1; dX1[l * DIM + i] = s2; }")
+    w("      double s1 = 0.0;")
+    w("      for (int b = 0; b < ED; ++b) s1 += g[b][i] * dps1[l * ED + b];")
+    w("      dx1[l * DIM + i] = s1; }")
+    if lagr:
+        w("    for (int l = 0; l < NN; ++l) for (int i = 0; i < DIM; ++i) {")
+        w("      double s2 = 0.0;")
+        w("      for (int b = 0; b < ED; ++b) s2 += gl[b][i] * dps[l * ED + b];")
+        w("      dX[l * DIM + i] = s2; }")
+        w("    for (int l = 0; l < N1; ++l) for (int i = 0; i < DIM; ++i) {")
+        w("      double s2 = 0.0;")
+        w("      for (int b = 0; b < ED; ++b) s2 += gl[b][i] * dps1[l * ED + b];")
+        w("      dX1[l * DIM + i] = s2; }")
     w(f"    double U[{nf * NCU}];")
     w(f"    for (int c = 0; c < {nf * NCU}; ++c) U[c] = 0.0;")
+    interp = 0
     for f, (nm, space, vi, _) in enumerate(fields):
         b0 = ici(f, 0)
-        tder = bdf0 >= 0 and nh > 0
-        if space == "C2":
-            w("    for (int l = 0; l < NN; ++l) {")
-            w(f"      const double u = Uv[l * NVAL + {vi}];")
-            w(f"      U[{b0}] += u * ps[l];")
-            w(f"      for (int i = 0; i < DIM; ++i) {{ U[{b0 + 1} + i] += u * dx[l * DIM + i]; "
-              f"U[{b0 + 1 + d} + i] += u * dX[l * DIM + i]; }}")
+        want = [c for c in range(NCU) if b0 + c in used_u]
+        if not want:
+            continue
+        tder = bdf0 >= 0 and nh > 0 and (1 + 2 * d) in want
+        nodes = list(range(nn)) if space == "C2" else list(c1)
+        for s_, l in enumerate(nodes):
+            psv = f"ps[{l}]" if space == "C2" else f"sPsi1[q * N1 + {s_}]"
+            gxv = (lambda i: f"dx[{l * d + i}]") if space == "C2" else (lambda i: f"dx1[{s_ * d + i}]")
+            gXv = (lambda i: f"dX[{l * d + i}]") if space == "C2" else (lambda i: f"dX1[{s_ * d + i}]")
+            w(f"    {{ const double u = Uv[{l} * NVAL + {vi}];")
+            for c in want:
+                if c == 0:
+                    w(f"      U[{b0}] += u * {psv};")
+                elif c <= d:
+                    w(f"      U[{b0 + c}] += u * {gxv(c - 1)};")
+                elif c <= 2 * d:
+                    w(f"      U[{b0 + c}] += u * {gXv(c - 1 - d)};")
+                interp += 2 if c <= 2 * d else 0
             if tder:
-                w(f"      double ut = P[{bdf0}] * u;")
-                w(f"      for (int h = 0; h < NH; ++h) ut += P[{bdf0} + 1 + h] * Uv[(1 + h) * NN * NVAL + l * NVAL + {vi}];")
-                w(f"      U[{b0 + 1 + 2 * d}] += ut * ps[l];")
+                hs = " + ".join(f"P[{bdf0 + 1 + h}] * Uv[{(1 + h) * nn * nval + l * nval + vi}]" for h in range(nh))
+                w(f"      U[{b0 + 1 + 2 * d}] += (P[{bdf0}] * u + {hs}) * {psv};")
+                interp += 2 * (nh + 1) + 2
             w("    }")
-        else:
-            for s_, l in enumerate(c1):
-                w(f"    {{ const double u = Uv[{l} * NVAL + {vi}]; const double ps1 = sPsi1[q * N1 + {s_}];")
-                w(f"      U[{b0}] += u * ps1;")
-                w(f"      for (int i = 0; i < DIM; ++i) {{ U[{b0 + 1} + i] += u * dx1[{s_} * DIM + i]; "
-                  f"U[{b0 + 1 + d} + i] += u * dX1[{s_} * DIM + i]; }}")
-                if tder:
-                    w(f"      double ut = P[{bdf0}] * u;")
-                    w(f"      for (int h = 0; h < NH; ++h) ut += P[{bdf0} + 1 + h] * Uv[(1 + h) * NN * NVAL + {l} * NVAL + {vi}];")
-                    w(f"      U[{b0 + 1 + 2 * d}] += ut * ps1;")
-                w("    }")
     w("    double Xq[3] = {0.0, 0.0, 0.0}, XL[3] = {0.0, 0.0, 0.0};")
     w("    for (int l = 0; l < NN; ++l) for (int i = 0; i < DIM; ++i) "
       "{ Xq[i] += Xe[l * DIM + i] * ps[l]; XL[i] += X0[l * DIM + i] * ps[l]; }")
@@ -621,18 +656,28 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w("    misc[0] = tau[0]; misc[1] = tau[1];")
     w("  }")
     w("  __syncthreads();")
-    rf = [rows_f[i][0] for i in range(nloc)]
-    rs = [rows_f[i][1] for i in range(nloc)]
-    w(f"  constexpr int ROWF[NLOC] = {{{', '.join(map(str, rf))}}};")
-    w(f"  constexpr int ROWS[NLOC] = {{{', '.join(map(str, rs))}}};")
-    w("  for (int p = threadIdx.x; p < nel * NLOC; p += FE_NT) {")
-    w("    const int el = p / NLOC, i = p - el * NLOC;")
-    w("    const int tf = ROWF[i], ts = ROWS[i];")
+    # threads take rows field by field (all elements' rows of field 0, then
+    # field 1, ...) so that a warp runs one test field's code
+    nsubs = [len(_sub_nodes(dc, f)) for f in range(nf)]
+    w("  for (int p = threadIdx.x; p < EPB * NLOC; p += FE_NT) {")
+    w("    int tf, el, ts, i;")
+    off = 0
+    roff = 0
+    for f in range(nf):
+        cond = "if" if f == 0 else "} else if"
+        hi = off + epb * nsubs[f]
+        w(f"    {cond} (p < {hi}) {{")
+        w(f"      tf = {f}; el = (p - {off}) / {nsubs[f]}; ts = (p - {off}) - el * {nsubs[f]}; i = c_rowof[{roff} + ts];")
+        off = hi
+        roff += nsubs[f]
+    w("    } else { tf = 0; el = EPB; ts = 0; i = 0; }")
+    w("    if (el >= nel) continue;")
     w("    const double* ebq = sE + el * PER_EL + (1 + NH) * NN * NVAL + NN * DIM;")
     w("    double Racc = 0.0;")
     w("    double Jr[NLOC];")
     w("    for (int c = 0; c < NLOC; ++c) Jr[c] = 0.0;")
     w("    switch (tf) {")
+    fl_rows = 0
     for tf in range(nf):
         tsp = fields[tf][1]
         w(f"    case {tf}: {{")
@@ -642,23 +687,29 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
         w("        const double* dX1 = dx1 + N1 * DIM; const double* rc = dX1 + N1 * DIM; const double* C = rc + NTC;")
         w("        const double* ps = sPsi2 + q * NN;")
         w("        (void)dx; (void)dX; (void)dx1; (void)dX1; (void)ps; (void)C;")
-        w("        double phi[1 + 2 * DIM];")
-        if tsp == "C2":
-            w("        phi[0] = ps[ts];")
-            w("        for (int c = 0; c < DIM; ++c) { phi[1 + c] = dx[ts * DIM + c]; phi[1 + DIM + c] = dX[ts * DIM + c]; }")
-        else:
-            w("        phi[0] = sPsi1[q * N1 + ts];")
-            w("        for (int c = 0; c < DIM; ++c) { phi[1 + c] = dx1[ts * DIM + c]; phi[1 + DIM + c] = dX1[ts * DIM + c]; }")
-        rterms = [f"rc[{tci(tf, c)}] * phi[{c}]" for c in range(NCT) if (tci(tf, c) in rEn or tci(tf, c) in rLn)]
+        for c in range(NCT):
+            if tci(tf, c) not in used_t:
+                continue
+            if c == 0:
+                src_ = "ps[ts]" if tsp == "C2" else "sPsi1[q * N1 + ts]"
+            elif c <= d:
+                src_ = (f"dx[ts * DIM + {c - 1}]" if tsp == "C2" else f"dx1[ts * DIM + {c - 1}]")
+            else:
+                src_ = (f"dX[ts * DIM + {c - 1 - d}]" if tsp == "C2" else f"dX1[ts * DIM + {c - 1 - d}]")
+            w(f"        const double phi{c} = {src_};")
+        rterms = [f"rc[{tci(tf, c)}] * phi{c}" for c in range(NCT) if (tci(tf, c) in rEn or tci(tf, c) in rLn)]
+        n_rows_tf = sum(1 for r_ in rows_f if r_[0] == tf)
+        fl_tf = 2 * len(rterms)
         if rterms:
             w(f"        Racc += {' + '.join(rterms)};")
         w("        if (flag) {")
         av: Dict[int, List[str]] = {}
         for kk, (tc, ic) in enumerate(keys):
             if tc // NCT == tf:
-                av.setdefault(ic, []).append(f"phi[{tc - tf * NCT}] * C[{kk}]")
+                av.setdefault(ic, []).append(f"phi{tc - tf * NCT} * C[{kk}]")
         for ic, lst in sorted(av.items()):
             w(f"          const double av{ic} = {' + '.join(lst)};")
+            fl_tf += 2 * len(lst)
         for g_ in range(nf):
             gsp = fields[g_][1]
             for s_, l in enumerate(_sub_nodes(dc, g_)):
@@ -682,10 +733,17 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
                         parts.append(f"av{ic} * P[{bdf0}] * {val}")
                 if parts:
                     w(f"          Jr[{col}] += {' + '.join(parts)};")
+                    fl_tf += sum(_ops(x) for x in parts) + len(parts)
         w("        }")
         w("      }")
         w("      break;")
         w("    }")
+        fl_rows += n_rows_tf * fl_tf
+    # operation count per element: phase A per knot, phase B per (row, knot)
+    geo = (2 * (2 * nn * d * EDs + 2 * EDs * EDs * d + 2 * EDs * EDs * d + 12) if ed == d else
+           (4 * nn + 12 if ed == 1 else 0))
+    geo += (nn + n1) * d * EDs * 2 * (2 if lagr else 1) + 4 * nn * d
+    dc.flops = float(nq * (geo + interp + fl_point) + nq * fl_rows)
     w("    default: break;")
     w("    }")
     w("    const long long row = (e0 + el) * NLOC + i;")

@@ -13,8 +13,12 @@ from pyoomph_gb300 import ale
 PAR = {"dynamic_viscosity": 0.1, "surface_tension": 1.0}
 
 
-def _state(D, seed, amp=0.3, move=0.01):
+def _state(D, seed, amp=0.3, move=None):
+    """Random nodal values and previous positions; positions moved by
+    less than the element size allows (no inverted elements)."""
     rng = np.random.default_rng(seed)
+    n1d = int(round(np.sqrt(D.tri.shape[0] / 2)))
+    move = 0.04 / n1d ** 2 if move is None else move
     v = A.initial_values(D)
     v[:, 2:] = rng.normal(size=(v.shape[0], 4)) * amp
     v[:, 0:2] += rng.normal(size=(v.shape[0], 2)) * move
@@ -80,7 +84,8 @@ def test_droplet_mesh_matches_oracle():
         assert np.allclose(np.hypot(*D.x0[D.line.ravel()].T), 1.0)
 
 
-@pytest.mark.parametrize("N,theta,prec", [(3, 60.0, "fp64"), (4, 120.0, "fp64"), (4, 90.0, "fp32")])
+@pytest.mark.parametrize("N,theta,prec", [(3, 60.0, "fp64"), (4, 120.0, "fp64"), (6, 110.0, "fp64"),
+                                          (4, 90.0, "fp32")])
 def test_emulated_fused_kernel_matches_oracle(N, theta, prec):
     P = ale.DropletProblem(N=N, contact_angle_deg=theta, jacobian_precision=prec)
     fk = P.lower()
@@ -95,6 +100,26 @@ def test_emulated_fused_kernel_matches_oracle(N, theta, prec):
             assert np.max(np.abs(Re - Ro)) <= 1e-12 * np.max(np.abs(Ro))
             tol = 1e-12 if prec == "fp64" else 1e-6
             assert np.max(np.abs(Je.astype(np.float64) - Jo)) <= tol * np.max(np.abs(Jo))
+
+
+def test_emulated_inverted_elements_use_the_metric_weight():
+    """An inverted element (negative det dx/ds) is integrated with the weight
+    sqrt(det(t t^T)) = |det| of the metric formulation, in the kernel and in
+    the oracle alike."""
+    P = ale.DropletProblem(N=6, contact_angle_deg=110.0)
+    fk = P.lower()
+    D = A.droplet(6)
+    p = _params(110.0)
+    v, h0, h1 = _state(D, 7, move=0.01)
+    w, psi, dpsi, _, _ = A.tri_tables()
+    t = np.einsum("eli,la->eai", v[:, :2][D.tri], dpsi[0])
+    assert (t[:, 0, 0] * t[:, 1, 1] - t[:, 0, 1] * t[:, 1, 0]).min() < 0
+    outs, _ = KE.run_fused(fk, P.conns, v, [h0, h1], D.x0, _pvec(P, p))
+    ref = A.element_res_jac(D, v, [h0, h1], p)
+    # the folded elements are badly conditioned: rounding grows ~100x
+    for (Re, Je), (Ro, Jo) in zip(outs, ref):
+        assert np.max(np.abs(Re - Ro)) <= 1e-10 * np.max(np.abs(Ro))
+        assert np.max(np.abs(Je - Jo)) <= 1e-10 * np.max(np.abs(Jo))
 
 
 def test_emulated_residual_only_flag_leaves_jacobian_untouched():
@@ -227,13 +252,22 @@ def test_gpu_full_size_jacobian_is_the_derivative_of_the_residual():
     assert P.n_dof > 190_000
     P.set_params(__bdf0=1500.0, __bdf1=-2000.0, __bdf2=500.0)
     rng = np.random.default_rng(3)
+    v0 = P._values0
+    v = v0.copy()
+    v[:, 2:] = rng.normal(size=(v.shape[0], 4)) * 0.1
+    v[:, 0:2] += rng.normal(size=(v.shape[0], 2)) * 0.04 / 110 ** 2
+    v[P.pinned] = v0[P.pinned]
+    P.set_state(v, [v0, v0])
     x = P.x_dev[:P.n_dof].cpu().numpy().copy()
-    x += rng.normal(size=x.shape) * 1e-3
     d = rng.normal(size=x.shape)
-    P.x_dev[:P.n_dof].copy_(torch.from_numpy(x))
+    pos = np.zeros(x.shape, dtype=bool)
+    for c in (0, 1):
+        e = P.eqn[:, c]
+        pos[e[e >= 0]] = True
+    d[pos] *= 1.0 / 110 ** 2          # positions move by a fraction of the element size
     R, J = P.get_jacobian()
     Jd = J @ d
-    h = 1e-6
+    h = 1e-4
     P.x_dev[:P.n_dof].copy_(torch.from_numpy(x + h * d))
     Rp = P.get_residuals()
     P.x_dev[:P.n_dof].copy_(torch.from_numpy(x - h * d))
