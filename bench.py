@@ -479,10 +479,16 @@ def run_droplet(args):
         "clocks": m["clocks"],
     }
     r32 = res["fp32"]
-    line["fp32_jacobian_storage"] = {"value": n_elem / (r32["ms"] / 1e3), "unit": "elements/s",
-                                     "ms_per_step": r32["ms"], "element_kernel_ms": float(r32["stage_ms"][1]),
-                                     "e2e": {"value": n_elem / (r32["ms_e2e"] / 1e3),
-                                             "h2d_bytes_per_step": r32["h2d"], "d2h_bytes_per_step": r32["d2h"]}}
+    P32 = r32["P"]
+    k32 = float(r32["stage_ms"][1]) / 1e3
+    f64_32 = sum(dc.flops * c.shape[0] for dc, c in zip(P32.domains, P32.conns))
+    f32_32 = sum(dc.flops32 * c.shape[0] for dc, c in zip(P32.domains, P32.conns))
+    line["fp32_jacobian"] = {"value": n_elem / (r32["ms"] / 1e3), "unit": "elements/s",
+                             "ms_per_step": r32["ms"], "element_kernel_ms": k32 * 1e3,
+                             "fp64_tflops": f64_32 / k32 / 1e12, "fp32_tflops": f32_32 / k32 / 1e12,
+                             "fp64_frac_of_dgemm": f64_32 / k32 / 1e12 / peak64,
+                             "e2e": {"value": n_elem / (r32["ms_e2e"] / 1e3),
+                                     "h2d_bytes_per_step": r32["h2d"], "d2h_bytes_per_step": r32["d2h"]}}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = droplet_cpu_baseline(args.size)
     print(json.dumps(line), flush=True)

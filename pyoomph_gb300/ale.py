@@ -281,6 +281,7 @@ class DomainCode:
     nk: int = 0
     rows_needed: int = 0
     flops: float = 0.0          # FP64 operations per element (FMA = 2), counted from the generated code
+    flops32: float = 0.0        # FP32 operations per element (the Jacobian contraction of the f32 variant)
 
     def layout(self):
         """Local order: the nodal values node by node (fields in order), then
@@ -309,12 +310,14 @@ def _sub_nodes(dc: DomainCode, f: int) -> List[int]:
 
 
 def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: int, nh: int,
-                   smem_budget: int, nthreads_cap: int) -> str:
+                   smem_budget: int, nthreads_cap: int, f32: bool = False) -> str:
     """Device namespace dom{k} with ``run(a, blk, smem)`` evaluating one block
     of elements of this domain: stage tables and nodal data (phase 0), one
     thread per (element, knot) for geometry, interpolation and the pointwise
     weak form (phase A), one thread per (element, row) for R_e and J_e
-    (phase B)."""
+    (phase B).  With ``f32`` the Jacobian coefficients, the shape values and
+    gradients they are contracted with, and the accumulation are single
+    precision; geometry, pointwise weak form and residual stay FP64."""
     dt = dc.dtype
     ed, EDs = dt.el_dim, dt.ed
     nn, nq, c1 = dt.nnode, dt.nq, dt.c1_index
@@ -476,15 +479,19 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
         rows_f[i] = (f, _sub_nodes(dc, f).index(l))
     # ---- shared memory plan (doubles)
     tabd = nq + nq * nn + nq * nn * EDs + nq * n1 + nq * n1 * EDs
-    QB = 2 * nn * d + 2 * n1 * d + ntc + NK + 4
-    per_el = nn * nval * (1 + nh) + nn * d + nq * QB
+    tabf = nq * (nn + n1) if f32 else 0               # float copies of the shape values
+    tabfd = (tabf + 1) // 2
+    QB = 2 * nn * d + 2 * n1 * d + ntc + (0 if f32 else NK) + 4
+    FQB = NK + 2 * nn * d + 2 * n1 * d if f32 else 0  # floats per knot: C, dx, dX, dx1, dX1
+    FQB += FQB % 2
+    per_el = nn * nval * (1 + nh) + nn * d + nq * QB + nq * FQB // 2
     epb = 1
     for e_ in range(1, 65):
-        if max(e_ * nq, e_ * nloc) > nthreads_cap or (tabd + e_ * per_el) * 8 > smem_budget:
+        if max(e_ * nq, e_ * nloc) > nthreads_cap or (tabd + tabfd + e_ * per_el) * 8 > smem_budget:
             break
         epb = e_
     dc.epb = epb
-    dc.smem = ((tabd + epb * per_el) * 8 + 15) // 16 * 16
+    dc.smem = ((tabd + tabfd + epb * per_el) * 8 + 15) // 16 * 16
     dc.rows_needed = max(epb * nq, epb * nloc)
     # ---- source
     L: List[str] = []
@@ -492,10 +499,10 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w(f"namespace dom{k} {{")
     w(f"constexpr int NN = {nn}, NQ = {nq}, N1 = {n1}, ED = {EDs}, DIM = {d}, NVAL = {nval}, NH = {nh};")
     w(f"constexpr int NTC = {ntc}, NK = {NK}, NLOC = {nloc}, EPB = {epb};")
-    w(f"constexpr int TABD = {tabd}, QB = {QB}, PER_EL = {per_el};")
+    w(f"constexpr int TABD = {tabd}, TABFD = {tabfd}, QB = {QB}, FQB = {FQB}, PER_EL = {per_el};")
     w("__device__ __forceinline__ void pointwise(const double* __restrict__ U, const double* __restrict__ Xq,")
     w("    const double* __restrict__ XL, const double* __restrict__ Nn, const double* __restrict__ P,")
-    w("    const double* __restrict__ tau, double wE, double wL, double* __restrict__ rc, double* __restrict__ C,")
+    w("    const double* __restrict__ tau, double wE, double wL, double* __restrict__ rc, jreal* __restrict__ C,")
     w("    int flag) {")
     w(f"  double rE[{max(1, len(rEn))}], rL[{max(1, len(rLn))}];")
     w(f"  double dE[{max(1, len(eE))}], dL[{max(1, len(eL))}], dN[{max(1, len(eN))}];")
@@ -538,7 +545,7 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
         w(f"  rc[{tc}] = {' + '.join(parts) if parts else '0.0'};")
     w("  if (flag) {")
     for kk, key in enumerate(keys):
-        w(f"    C[{kk}] = {' + '.join(terms[key])};")
+        w(f"    C[{kk}] = (jreal)({' + '.join(terms[key])});")
     w("  }")
     w("}")
     rowof = [slot[(f, l)] for f in range(nf) for l in _sub_nodes(dc, f)]
@@ -548,7 +555,9 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w("  double* sDps2 = sPsi2 + NQ * NN;")
     w("  double* sPsi1 = sDps2 + NQ * NN * ED;")
     w("  double* sDps1 = sPsi1 + NQ * N1;")
-    w("  double* sE = sW + TABD;")
+    w("  double* sE = sW + TABD + TABFD;")
+    w("  float* sPsi2f = reinterpret_cast<float*>(sW + TABD); float* sPsi1f = sPsi2f + NQ * NN;")
+    w("  (void)sPsi2f; (void)sPsi1f;")
     w("  const long long e0 = (long long)blk * EPB;")
     w("  const long long rem = a.n_elem - e0;")
     w("  const int nel = rem < EPB ? (int)rem : EPB;")
@@ -556,6 +565,11 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w("  const double* __restrict__ P = a.params;")
     w("  (void)P; (void)sDps1;")
     w("  for (int k = threadIdx.x; k < TABD; k += FE_NT) sW[k] = a.tables[k];")
+    if f32:
+        w("  for (int k = threadIdx.x; k < NQ * NN; k += FE_NT) sPsi2f[k] = (float)a.tables[NQ + k];")
+        w("  for (int k = threadIdx.x; k < NQ * N1; k += FE_NT) sPsi1f[k] = (float)a.tables[NQ + NQ * NN * (1 + ED) + k];")
+    if bdf0 >= 0:
+        w(f"  const jreal w0j = (jreal)P[{bdf0}]; (void)w0j;")
     w("  for (int k = threadIdx.x; k < nel * NN; k += FE_NT) {")
     w("    const int el = k / NN, l = k - el * NN;")
     w("    const long long node = a.conn[(e0 + el) * NN + l];")
@@ -573,7 +587,13 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w("    const double* X0 = Uv + (1 + NH) * NN * NVAL;")
     w("    double* qb = sE + el * PER_EL + (1 + NH) * NN * NVAL + NN * DIM + q * QB;")
     w("    double* dx = qb; double* dX = dx + NN * DIM; double* dx1 = dX + NN * DIM; double* dX1 = dx1 + N1 * DIM;")
-    w("    double* rc = dX1 + N1 * DIM; double* C = rc + NTC; double* misc = C + NK;")
+    if f32:
+        w("    double* rc = dX1 + N1 * DIM; double* misc = rc + NTC;")
+        w("    float* C = reinterpret_cast<float*>(sE + el * PER_EL + (1 + NH) * NN * NVAL + NN * DIM + NQ * QB) + q * FQB;")
+        w("    float* fdx = C + NK; float* fdX = fdx + NN * DIM; float* fdx1 = fdX + NN * DIM; float* fdX1 = fdx1 + N1 * DIM;")
+        w("    (void)fdX; (void)fdX1;")
+    else:
+        w("    double* rc = dX1 + N1 * DIM; double* C = rc + NTC; double* misc = C + NK;")
     w("    const double* ps = sPsi2 + q * NN;")
     w("    const double* dps = sDps2 + q * NN * ED;")
     w("    const double* dps1 = sDps1 + q * N1 * ED;")
@@ -607,20 +627,20 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w("    for (int l = 0; l < NN; ++l) for (int i = 0; i < DIM; ++i) {")
     w("      double s1 = 0.0;")
     w("      for (int b = 0; b < ED; ++b) s1 += g[b][i] * dps[l * ED + b];")
-    w("      dx[l * DIM + i] = s1; }")
+    w("      dx[l * DIM + i] = s1;" + (" fdx[l * DIM + i] = (float)s1;" if f32 else "") + " }")
     w("    for (int l = 0; l < N1; ++l) for (int i = 0; i < DIM; ++i) {")
     w("      double s1 = 0.0;")
     w("      for (int b = 0; b < ED; ++b) s1 += g[b][i] * dps1[l * ED + b];")
-    w("      dx1[l * DIM + i] = s1; }")
+    w("      dx1[l * DIM + i] = s1;" + (" fdx1[l * DIM + i] = (float)s1;" if f32 else "") + " }")
     if lagr:
         w("    for (int l = 0; l < NN; ++l) for (int i = 0; i < DIM; ++i) {")
         w("      double s2 = 0.0;")
         w("      for (int b = 0; b < ED; ++b) s2 += gl[b][i] * dps[l * ED + b];")
-        w("      dX[l * DIM + i] = s2; }")
+        w("      dX[l * DIM + i] = s2;" + (" fdX[l * DIM + i] = (float)s2;" if f32 else "") + " }")
         w("    for (int l = 0; l < N1; ++l) for (int i = 0; i < DIM; ++i) {")
         w("      double s2 = 0.0;")
         w("      for (int b = 0; b < ED; ++b) s2 += gl[b][i] * dps1[l * ED + b];")
-        w("      dX1[l * DIM + i] = s2; }")
+        w("      dX1[l * DIM + i] = s2;" + (" fdX1[l * DIM + i] = (float)s2;" if f32 else "") + " }")
     w(f"    double U[{nf * NCU}];")
     w(f"    for (int c = 0; c < {nf * NCU}; ++c) U[c] = 0.0;")
     interp = 0
@@ -674,42 +694,57 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w("    if (el >= nel) continue;")
     w("    const double* ebq = sE + el * PER_EL + (1 + NH) * NN * NVAL + NN * DIM;")
     w("    double Racc = 0.0;")
-    w("    double Jr[NLOC];")
-    w("    for (int c = 0; c < NLOC; ++c) Jr[c] = 0.0;")
+    w("    jreal Jr[NLOC];")
+    w("    for (int c = 0; c < NLOC; ++c) Jr[c] = (jreal)0;")
     w("    switch (tf) {")
-    fl_rows = 0
+    fl_rows_r = fl_rows_j = 0
     for tf in range(nf):
         tsp = fields[tf][1]
         w(f"    case {tf}: {{")
         w("      for (int q = 0; q < NQ; ++q) {")
         w("        const double* qb = ebq + q * QB;")
         w("        const double* dx = qb; const double* dX = dx + NN * DIM; const double* dx1 = dX + NN * DIM;")
-        w("        const double* dX1 = dx1 + N1 * DIM; const double* rc = dX1 + N1 * DIM; const double* C = rc + NTC;")
+        w("        const double* dX1 = dx1 + N1 * DIM; const double* rc = dX1 + N1 * DIM;")
         w("        const double* ps = sPsi2 + q * NN;")
-        w("        (void)dx; (void)dX; (void)dx1; (void)dX1; (void)ps; (void)C;")
+        w("        (void)dx; (void)dX; (void)dx1; (void)dX1; (void)ps;")
+        if f32:
+            w("        const float* C = reinterpret_cast<const float*>(ebq + NQ * QB) + q * FQB;")
+            w("        const float* fdx = C + NK; const float* fdX = fdx + NN * DIM; const float* fdx1 = fdX + NN * DIM;")
+            w("        const float* fdX1 = fdx1 + N1 * DIM; const float* fps = sPsi2f + q * NN; const float* fps1 = sPsi1f + q * N1;")
+            w("        (void)fdx; (void)fdX; (void)fdx1; (void)fdX1; (void)fps; (void)fps1;")
+        else:
+            w("        const double* C = rc + NTC;")
+        w("        (void)C;")
+        jac_t = {tc - tf * NCT for tc, _ in keys if tc // NCT == tf}
         for c in range(NCT):
             if tci(tf, c) not in used_t:
                 continue
-            if c == 0:
-                src_ = "ps[ts]" if tsp == "C2" else "sPsi1[q * N1 + ts]"
-            elif c <= d:
-                src_ = (f"dx[ts * DIM + {c - 1}]" if tsp == "C2" else f"dx1[ts * DIM + {c - 1}]")
-            else:
-                src_ = (f"dX[ts * DIM + {c - 1 - d}]" if tsp == "C2" else f"dX1[ts * DIM + {c - 1 - d}]")
-            w(f"        const double phi{c} = {src_};")
+            for single in ((False, True) if f32 else (False,)):
+                pre = "f" if single else ""
+                if c == 0:
+                    src_ = (f"{pre}ps[ts]" if tsp == "C2" else
+                            ("fps1[ts]" if single else "sPsi1[q * N1 + ts]"))
+                elif c <= d:
+                    src_ = f"{pre}dx[ts * DIM + {c - 1}]" if tsp == "C2" else f"{pre}dx1[ts * DIM + {c - 1}]"
+                else:
+                    src_ = f"{pre}dX[ts * DIM + {c - 1 - d}]" if tsp == "C2" else f"{pre}dX1[ts * DIM + {c - 1 - d}]"
+                if single and c in jac_t:
+                    w(f"        const float fphi{c} = {src_};")
+                elif not single and (not f32 or tci(tf, c) in rEn or tci(tf, c) in rLn):
+                    w(f"        const double phi{c} = {src_};")
         rterms = [f"rc[{tci(tf, c)}] * phi{c}" for c in range(NCT) if (tci(tf, c) in rEn or tci(tf, c) in rLn)]
         n_rows_tf = sum(1 for r_ in rows_f if r_[0] == tf)
-        fl_tf = 2 * len(rterms)
+        fl_tr, fl_tj = 2 * len(rterms), 0
         if rterms:
             w(f"        Racc += {' + '.join(rterms)};")
         w("        if (flag) {")
         av: Dict[int, List[str]] = {}
         for kk, (tc, ic) in enumerate(keys):
             if tc // NCT == tf:
-                av.setdefault(ic, []).append(f"phi{tc - tf * NCT} * C[{kk}]")
+                av.setdefault(ic, []).append(f"{'f' if f32 else ''}phi{tc - tf * NCT} * C[{kk}]")
         for ic, lst in sorted(av.items()):
-            w(f"          const double av{ic} = {' + '.join(lst)};")
-            fl_tf += 2 * len(lst)
+            w(f"          const jreal av{ic} = {' + '.join(lst)};")
+            fl_tj += 2 * len(lst)
         for g_ in range(nf):
             gsp = fields[g_][1]
             for s_, l in enumerate(_sub_nodes(dc, g_)):
@@ -719,10 +754,12 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
                     gf, cc = divmod(ic, NCU)
                     if gf != g_:
                         continue
+                    pre = "f" if f32 else ""
                     if gsp == "C2":
-                        val, gx, gX = f"ps[{l}]", f"dx[{l * d} + {{i}}]", f"dX[{l * d} + {{i}}]"
+                        val, gx, gX = f"{pre}ps[{l}]", f"{pre}dx[{l * d} + {{i}}]", f"{pre}dX[{l * d} + {{i}}]"
                     else:
-                        val, gx, gX = (f"sPsi1[q * N1 + {s_}]", f"dx1[{s_ * d} + {{i}}]", f"dX1[{s_ * d} + {{i}}]")
+                        val = f"fps1[{s_}]" if f32 else f"sPsi1[q * N1 + {s_}]"
+                        gx, gX = f"{pre}dx1[{s_ * d} + {{i}}]", f"{pre}dX1[{s_ * d} + {{i}}]"
                     if cc == 0:
                         parts.append(f"av{ic} * {val}")
                     elif cc <= d:
@@ -730,27 +767,29 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
                     elif cc <= 2 * d:
                         parts.append(f"av{ic} * {gX.format(i=cc - 1 - d)}")
                     else:
-                        parts.append(f"av{ic} * P[{bdf0}] * {val}")
+                        parts.append(f"av{ic} * w0j * {val}")
                 if parts:
                     w(f"          Jr[{col}] += {' + '.join(parts)};")
-                    fl_tf += sum(_ops(x) for x in parts) + len(parts)
+                    fl_tj += sum(_ops(x) for x in parts) + len(parts)
         w("        }")
         w("      }")
         w("      break;")
         w("    }")
-        fl_rows += n_rows_tf * fl_tf
+        fl_rows_r += n_rows_tf * fl_tr
+        fl_rows_j += n_rows_tf * fl_tj
     # operation count per element: phase A per knot, phase B per (row, knot)
     geo = (2 * (2 * nn * d * EDs + 2 * EDs * EDs * d + 2 * EDs * EDs * d + 12) if ed == d else
            (4 * nn + 12 if ed == 1 else 0))
     geo += (nn + n1) * d * EDs * 2 * (2 if lagr else 1) + 4 * nn * d
-    dc.flops = float(nq * (geo + interp + fl_point) + nq * fl_rows)
+    dc.flops = float(nq * (geo + interp + fl_point + fl_rows_r + (0 if f32 else fl_rows_j)))
+    dc.flops32 = float(nq * fl_rows_j) if f32 else 0.0
     w("    default: break;")
     w("    }")
     w("    const long long row = (e0 + el) * NLOC + i;")
     w("    a.rbuf[row] = Racc;")
     w("    if (flag) {")
     w("      jreal* jb = reinterpret_cast<jreal*>(a.jbuf) + row * NLOC;")
-    w("      for (int c = 0; c < NLOC; ++c) jb[c] = (jreal)Jr[c];")
+    w("      for (int c = 0; c < NLOC; ++c) jb[c] = Jr[c];")
     w("    }")
     w("  }")
     w("}")
@@ -777,7 +816,7 @@ def generate_fused(domains: List[DomainCode], dim: int, params: List[str], nval:
     if len(domains) > 4:
         raise ValueError("at most 4 fused domains")
     jreal = "double" if jac_precision == "f64" else "float"
-    bodies = [_domain_source(k, dc, dim, params, nval, nh, smem_budget, nthreads_cap)
+    bodies = [_domain_source(k, dc, dim, params, nval, nh, smem_budget, nthreads_cap, jac_precision == "f32")
               for k, dc in enumerate(domains)]
     threads = max(32, max(((dc.rows_needed + 31) // 32) * 32 for dc in domains))
     smem = max(dc.smem for dc in domains)
