@@ -10,13 +10,15 @@ memory for the class (``fe_device_info`` free bytes, minus a reserve);
 otherwise it waits.  Admission happens at Newton-step boundaries, so
 requests join and leave a running batch continuously.
 
-One Newton step of a batch is one fused launch sequence for all its
-replicas (dof scatter, element kernel, residual and Jacobian scatter) on the
-batch's own CUDA stream, the per-replica residual max-norm on the device,
-and then, for each active replica, the linear solve J dx = R of its diagonal
-block in a worker process (SuperLU through scipy, the reference's default
-solver; processes because SuperLU holds the GIL) -- so the solves of all
-active requests run in parallel on the host cores while the GPU assembles.
+Each request advances on its own: assembly, residual check, the linear
+solve J dx = R of its diagonal block in a worker process (SuperLU through
+scipy, the reference's default solver; processes because SuperLU holds the
+GIL; the class's CSR pattern is published once in shared memory), update,
+next assembly.  The pending assemblies of a class are served by one launch
+sequence for all its replicas (dof scatter, element kernel, residual and
+Jacobian scatter) on the class's own CUDA stream, with the per-replica
+residual max-norms reduced on the device -- so the solves of all active
+requests run in parallel on the host cores while the GPU assembles.
 
 Results do not depend on the mix: every element, CSR slot and residual
 entry of a replica is computed from that replica's values only, in a fixed
@@ -113,28 +115,48 @@ def estimate_bytes(P) -> int:
     return int(E * nl * nl * (jb + 4) + nnz_est * (jb + 8 + 4) + E * nl * 12 + P.mesh.n_nodes * 64)
 
 
-def _splu_solve(vals: np.ndarray, colidx: np.ndarray, rowptr: np.ndarray, R: np.ndarray) -> np.ndarray:
-    """J dx = R with SuperLU (runs in a worker process: SuperLU holds the
-    GIL, so parallel solves need processes)."""
+_PATTERNS: Dict[str, tuple] = {}
+
+
+def _attach_pattern(name: str, n: int, nnz: int):
+    """The CSR pattern of a mesh class, published once in shared memory by
+    the server and attached (and cached) by each worker process."""
+    got = _PATTERNS.get(name)
+    if got is None:
+        from multiprocessing import shared_memory
+        shm = shared_memory.SharedMemory(name=name)
+        rp = np.ndarray((n + 1,), dtype=np.int32, buffer=shm.buf)
+        ci = np.ndarray((nnz,), dtype=np.int32, buffer=shm.buf, offset=4 * (n + 1))
+        got = _PATTERNS[name] = (shm, rp, ci)
+    return got[1], got[2]
+
+
+def _splu_solve(pattern: str, vals: np.ndarray, R: np.ndarray) -> np.ndarray:
+    """J dx = R with SuperLU in a worker process (SuperLU holds the GIL, so
+    parallel solves need processes); the pattern comes from shared memory."""
     import scipy.sparse as sp
     import scipy.sparse.linalg as spla
     n = R.shape[0]
-    A = sp.csr_matrix((vals.astype(np.float64), colidx, rowptr), shape=(n, n))
+    rp, ci = _attach_pattern(pattern, n, vals.shape[0])
+    A = sp.csr_matrix((vals.astype(np.float64), ci, rp), shape=(n, n))
     return spla.splu(A.tocsc()).solve(R)
 
 
 class _Batch:
     def __init__(self, key, P, slots: int, stream):
+        from multiprocessing import shared_memory
         self.key = key
         self.P = P
         self.slots = slots
         self.stream = stream
         self.req: List[Optional[Request]] = [None] * slots
+        self.state: List[str] = ["free"] * slots        # free | assemble | solving
         self.n_dof = P.n_dof // slots
         self.nnz = P.nnz // slots
         rp, ci = P.pattern()
-        self.rp0 = rp[:self.n_dof + 1].copy()
-        self.ci0 = ci[:self.nnz].copy()
+        self.shm = shared_memory.SharedMemory(create=True, size=4 * (self.n_dof + 1 + self.nnz))
+        np.ndarray((self.n_dof + 1,), dtype=np.int32, buffer=self.shm.buf)[:] = rp[:self.n_dof + 1]
+        np.ndarray((self.nnz,), dtype=np.int32, buffer=self.shm.buf, offset=4 * (self.n_dof + 1))[:] = ci[:self.nnz]
         self.x0 = P.get_dofs()[:self.n_dof].copy()
         self.last_used = time.perf_counter()
 
@@ -147,8 +169,19 @@ class _Batch:
     def active(self) -> bool:
         return any(r is not None for r in self.req)
 
+    def release(self) -> None:
+        try:
+            self.shm.close()
+            self.shm.unlink()
+        except Exception:
+            pass
+
 
 class Server:
+    """Continuous batching: each request advances on its own (assemble ->
+    solve in a worker -> update -> assemble ...); a class's pending
+    assemblies are served by one launch sequence for all its replicas."""
+
     def __init__(self, slots: int = 4, jacobian_precision: str = "fp32", tol: float = 1e-10,
                  max_newton: int = 20, workers: int = 8, hbm_reserve: float = 0.1):
         import torch
@@ -160,10 +193,11 @@ class Server:
         import multiprocessing as mp
         # linear solves in worker processes (spawned: safe after CUDA init)
         self.pool = cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn"))
-        self.stepper = cf.ThreadPoolExecutor(max_workers=16)         # one step per busy batch
         self.hbm_reserve = hbm_reserve
         self.batches: Dict[tuple, _Batch] = {}
         self.launches = 0
+        self.assemblies = 0
+        self.t_solve = 0.0
 
     # -- memory ------------------------------------------------------------
     def _free_bytes(self) -> int:
@@ -185,7 +219,7 @@ class Server:
             if not idle:
                 return None  # admission refused for now: not enough HBM
             victim = min(idle, key=lambda k: self.batches[k].last_used)
-            del self.batches[victim]
+            self.batches.pop(victim).release()
             self.torch.cuda.synchronize()
         P.initialise()
         b = _Batch(key, P, self.slots, self.torch.cuda.Stream())
@@ -204,67 +238,62 @@ class Server:
         with self.torch.cuda.stream(b.stream):
             P.x_dev[s * b.n_dof:(s + 1) * b.n_dof].copy_(self.torch.as_tensor(b.x0, device="cuda"))
         b.req[s] = req
+        b.state[s] = "assemble"
         req.t_admit = now
         return True
 
-    def _residual_norms(self, b: _Batch) -> List[float]:
-        out = []
-        for s in range(b.slots):
-            if b.req[s] is None:
-                out.append(0.0)
-                continue
-            v = ctypes.c_double()
-            ptr = b.P.R_dev.data_ptr() + 8 * s * b.n_dof
-            N.check(N.load().fe_residual_max(b.P._h, ptr, b.n_dof, ctypes.byref(v),
-                                             ctypes.c_void_p(b.stream.cuda_stream)))
-            out.append(v.value)
-        return out
-
-    def _step(self, b: _Batch, t0: float) -> List[Request]:
-        """One Newton step of every active replica of a batch."""
+    def _assemble(self, b: _Batch, t0: float, futs: dict) -> List[Request]:
+        """One launch sequence for every replica of the class; then, per
+        replica waiting for an assembly, the convergence check and either
+        completion or a solve submitted to the workers."""
         torch = self.torch
         P = b.P
         done = []
         with torch.cuda.stream(b.stream):
             P.assemble_device(with_jacobian=True, stream=b.stream.cuda_stream)
             self.launches += P.launch_count(True)
-            norms = self._residual_norms(b)
-            R = P.R_dev[:P.n_dof].cpu().numpy() if any(r is not None for r in b.req) else None
-            J = P.J_dev[:P.nnz].cpu().numpy()
-        futs = {}
+            self.assemblies += 1
+            Rv = P.R_dev[:P.n_dof].view(b.slots, b.n_dof)
+            norms = torch.nan_to_num(Rv.abs().amax(dim=1), nan=float("inf")).cpu().numpy()
+            R = Rv.cpu().numpy()
+            J = P.J_dev[:P.nnz].view(b.slots, b.nnz).cpu().numpy()
         for s, req in enumerate(b.req):
-            if req is None:
+            if req is None or b.state[s] != "assemble":
                 continue
-            req.residuals.append(norms[s])
+            req.residuals.append(float(norms[s]))
             if norms[s] < self.tol or req.newton_iterations >= self.max_newton or not np.isfinite(norms[s]):
                 if norms[s] >= self.tol:
                     req.error = f"Newton did not converge: {req.residuals}"
                 req.dofs = P.x_dev[s * b.n_dof:(s + 1) * b.n_dof].cpu().numpy()
                 req.t_done = time.perf_counter() - t0
                 b.req[s] = None
+                b.state[s] = "free"
                 done.append(req)
                 continue
-            Rs = R[s * b.n_dof:(s + 1) * b.n_dof]
-            Js = J[s * b.nnz:(s + 1) * b.nnz]
-            futs[s] = self.pool.submit(_splu_solve, Js, b.ci0, b.rp0, Rs)
-        for s, f in futs.items():
-            dx = f.result()
-            with torch.cuda.stream(b.stream):
-                sl = P.x_dev[s * b.n_dof:(s + 1) * b.n_dof]
-                sl -= torch.as_tensor(dx, device="cuda")
-            b.req[s].newton_iterations += 1
+            b.state[s] = "solving"
+            futs[self.pool.submit(_splu_solve, b.shm.name, J[s], R[s])] = (b, s, time.perf_counter())
         b.last_used = time.perf_counter()
         return done
 
+    def _apply(self, b: _Batch, s: int, dx: np.ndarray) -> None:
+        with self.torch.cuda.stream(b.stream):
+            sl = b.P.x_dev[s * b.n_dof:(s + 1) * b.n_dof]
+            sl -= self.torch.as_tensor(dx, device="cuda")
+        b.req[s].newton_iterations += 1
+        b.state[s] = "assemble"
+
     def close(self) -> None:
         self.pool.shutdown(wait=True)
-        self.stepper.shutdown(wait=True)
+        for b in self.batches.values():
+            b.release()
+        self.batches.clear()
 
     def run(self, requests: List[Request], realtime: bool = True) -> List[Request]:
         """Serve a stream; arrivals are honoured in real time."""
         pending = sorted(requests, key=lambda r: r.arrival)
         waiting: List[Request] = []
         finished: List[Request] = []
+        futs: Dict[cf.Future, tuple] = {}
         t0 = time.perf_counter()
         i = 0
         while len(finished) < len(requests):
@@ -272,22 +301,27 @@ class Server:
             while i < len(pending) and (pending[i].arrival <= now or not realtime):
                 waiting.append(pending[i])
                 i += 1
-            still = []
-            for r in waiting:
-                if not self._admit(r, time.perf_counter() - t0):
-                    still.append(r)
-            waiting = still
-            busy = [b for b in self.batches.values() if b.active()]
-            if not busy:
+            waiting = [r for r in waiting if not self._admit(r, time.perf_counter() - t0)]
+            ready = [b for b in self.batches.values() if "assemble" in b.state]
+            for b in ready:
+                finished += self._assemble(b, t0, futs)
+            if len(finished) >= len(requests):
+                break
+            if not futs and not ready:
                 if i < len(pending) and realtime:
                     time.sleep(max(0.0, min(0.01, pending[i].arrival - now)))
-                elif waiting and not busy:
+                    continue
+                if waiting:
                     raise RuntimeError("requests cannot be admitted (device memory)")
                 continue
-            # step every active batch; their GPU work runs on separate streams
-            steps = [self.stepper.submit(self._step, b, t0) for b in busy]
-            for f in steps:
-                finished += f.result()
+            if futs:
+                nxt = pending[i].arrival - (time.perf_counter() - t0) if (i < len(pending) and realtime) else None
+                timeout = None if nxt is None else max(0.0, nxt)
+                dn, _ = cf.wait(list(futs), timeout=timeout, return_when=cf.FIRST_COMPLETED)
+                for f in dn:
+                    b, s, ts = futs.pop(f)
+                    self.t_solve += time.perf_counter() - ts
+                    self._apply(b, s, f.result())
         self.torch.cuda.synchronize()
         return finished
 
