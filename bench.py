@@ -156,17 +156,20 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_problem(workload: str, size: int, precision: str):
+def make_problem(workload: str, size: int, precision: str, epb=None):
     from pyoomph_gb300 import workloads as W
     if workload == "ns":
         P = W.navier_stokes_problem(N=size, jacobian_precision=precision)
+        P.elems_per_block = epb
         P.initialise()
         W.perturb_dofs(P, seed=0, sigma=1e-3)
     elif workload == "poisson":
         P = W.poisson_problem(N=size, seed=0, jacobian_precision=precision)
+        P.elems_per_block = epb
         P.initialise()
     else:
         P = W.nonlinear_diffusion_problem(N=size, seed=0, jacobian_precision=precision)
+        P.elems_per_block = epb
         P.initialise()
         x = np.random.default_rng(0).normal(0.0, 0.1, P.n_dof)
         P.set_dofs(x)
@@ -233,8 +236,19 @@ def run_gb300(args):
         dist.init_process_group("nccl")
     hbm_peak, peak_kind = _peaks()
     results = {}
+    tuned = {}
     for prec in ("fp64", "fp32"):
-        P = make_problem(args.workload, args.size, prec)
+        epb = None
+        if args.autotune:
+            from pyoomph_gb300 import autotune as AT
+            P0 = make_problem(args.workload, args.size, prec)
+            cands = AT.epb_candidates(P0.mesh.etype.nq, P0.kernel.layout.n)
+            key = f"{args.workload}-{args.size}-{prec}-{P0.kernel.name}"
+            del P0
+            epb, table = AT.tune(key, lambda e: make_problem(args.workload, args.size, prec, e), cands,
+                                 use_cache=False)
+            tuned[prec] = {"elems_per_block": epb, "ms_per_assembly": table}
+        P = make_problem(args.workload, args.size, prec, epb)
         P.check()
         asm = lambda: P.assemble_device(with_jacobian=True)
         # device-resident throughput
@@ -270,7 +284,11 @@ def run_gb300(args):
 
         ms_e2e = time_steps(torch, e2e, max(3, args.steps), args.warmup)
         torch.cuda.synchronize()
-        results[prec] = dict(P=P, ms=ms, stage_ms=stage_ms, ms_e2e=ms_e2e, clocks=cs.summary(),
+        # the same assembly replayed as one CUDA graph
+        P.capture_assembly(with_jacobian=True)
+        ms_graph = time_steps(torch, P.assemble_graph, args.steps, args.warmup)
+        P.check()
+        results[prec] = dict(P=P, ms=ms, stage_ms=stage_ms, ms_e2e=ms_e2e, clocks=cs.summary(), ms_graph=ms_graph,
                              h2d=int(P.n_dof * 8), d2h=int(P.n_dof * 8 + P.nnz * P.J_dev.element_size()))
     from pyoomph_gb300.codegen import estimate_flops
     peak64 = fp64_peak_tflops(torch)
@@ -317,6 +335,10 @@ def run_gb300(args):
                 "ms_per_step": main["ms_e2e"]},
         "gpu_launches": launches * args.steps,
         "clocks": main["clocks"],
+        "cuda_graph": {"ms_per_step": main["ms_graph"], "value": n_elem * world / (main["ms_graph"] / 1e3),
+                       "launches_per_step": 1},
+        "launch_shape": {"elems_per_block": P.kernel.epb, "threads": P.kernel.threads,
+                         "smem_bytes": P.kernel.smem_bytes, "autotuned": tuned or None},
     }
     r32 = results["fp32"]
     f32 = estimate_flops(r32["P"].kernel, r32["P"].affine)
@@ -325,7 +347,9 @@ def run_gb300(args):
                              "fp64_tflops": f32["fp64"] * n_elem / (float(r32["stage_ms"][1]) / 1e3) / 1e12,
                              "fp32_tflops": f32["jac"] * n_elem / (float(r32["stage_ms"][1]) / 1e3) / 1e12,
                              "e2e": {"value": n_elem * world / (r32["ms_e2e"] / 1e3),
-                                     "h2d_bytes_per_step": r32["h2d"], "d2h_bytes_per_step": r32["d2h"]}}
+                                     "h2d_bytes_per_step": r32["h2d"], "d2h_bytes_per_step": r32["d2h"]},
+                             "cuda_graph_ms_per_step": r32["ms_graph"],
+                             "elems_per_block": r32["P"].kernel.epb}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, threads=1)
     if rank == 0:
@@ -391,7 +415,7 @@ def cpu_baseline(args, threads: int = 1, seconds: float = 10.0):
                       f"per core (oracle/fe_oracle.c, vectors-of-pairs)"}
 
 
-def droplet_problem(size: int, precision: str):
+def droplet_problem(size: int, precision: str, shape=None):
     """Droplet on its moving mesh (contact angle drawn from U[60, 120]
     degrees with seed 0) in a BDF2 step of dt = 1e-3: seeded velocities,
     pressures, multipliers and mesh displacements (a fraction of the element
@@ -400,6 +424,8 @@ def droplet_problem(size: int, precision: str):
     rng = np.random.default_rng(0)
     theta = float(rng.uniform(60.0, 120.0))
     P = ale.DropletProblem(N=size, contact_angle_deg=theta, jacobian_precision=precision)
+    if shape is not None:
+        P.nthreads_cap, P.smem_budget = shape
     P.initialise()
     v0 = P._values0
     v = v0.copy()
@@ -430,8 +456,16 @@ def run_droplet(args):
     torch.cuda.set_device(0)
     hbm_peak, peak_kind = _peaks()
     res = {}
+    tuned = {}
     for prec in ("fp64", "fp32"):
-        P, theta = droplet_problem(args.size, prec)
+        shape = None
+        if args.autotune:
+            from pyoomph_gb300 import autotune as AT
+            cands = [(128, 64 * 1024), (256, 100 * 1024), (256, 200 * 1024), (512, 200 * 1024)]
+            shape, table = AT.tune(f"droplet-{args.size}-{prec}", lambda c: droplet_problem(args.size, prec, c)[0],
+                                   cands, use_cache=False)
+            tuned[prec] = {"threads_cap_smem_budget": shape, "ms_per_assembly": table}
+        P, theta = droplet_problem(args.size, prec, shape)
         asm = lambda: P.assemble_device(with_jacobian=True)
         for _ in range(args.warmup):
             asm()
@@ -456,7 +490,10 @@ def run_droplet(args):
             Jh.copy_(P.J_dev[:P.nnz], non_blocking=True)
 
         ms_e2e = time_steps(torch, e2e, max(3, args.steps), args.warmup)
-        res[prec] = dict(P=P, ms=ms, stage_ms=stage_ms, ms_e2e=ms_e2e, clocks=cs.summary(),
+        P.capture_assembly(with_jacobian=True)
+        ms_graph = time_steps(torch, P.assemble_graph, args.steps, args.warmup)
+        P.check()
+        res[prec] = dict(P=P, ms=ms, stage_ms=stage_ms, ms_e2e=ms_e2e, clocks=cs.summary(), ms_graph=ms_graph,
                          h2d=int(P.n_dof * 8), d2h=int(P.n_dof * 8 + P.nnz * P.J_dev.element_size()))
     peak64 = fp64_peak_tflops(torch)
     m = res["fp64"]
@@ -490,6 +527,9 @@ def run_droplet(args):
                 "d2h_bytes_per_step": m["d2h"], "ms_per_step": m["ms_e2e"]},
         "gpu_launches": P.launch_count(True) * args.steps,
         "clocks": m["clocks"],
+        "cuda_graph": {"ms_per_step": m["ms_graph"], "value": n_elem / (m["ms_graph"] / 1e3), "launches_per_step": 1},
+        "launch_shape": {"threads": P.kernel.threads, "smem_bytes": P.kernel.smem_bytes,
+                         "elems_per_block": [dc.epb for dc in P.domains], "autotuned": tuned or None},
     }
     r32 = res["fp32"]
     P32 = r32["P"]
@@ -501,7 +541,8 @@ def run_droplet(args):
                              "fp64_tflops": f64_32 / k32 / 1e12, "fp32_tflops": f32_32 / k32 / 1e12,
                              "fp64_frac_of_dgemm": f64_32 / k32 / 1e12 / peak64,
                              "e2e": {"value": n_elem / (r32["ms_e2e"] / 1e3),
-                                     "h2d_bytes_per_step": r32["h2d"], "d2h_bytes_per_step": r32["d2h"]}}
+                                     "h2d_bytes_per_step": r32["h2d"], "d2h_bytes_per_step": r32["d2h"]},
+                             "cuda_graph_ms_per_step": r32["ms_graph"]}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = droplet_cpu_baseline(args.size)
     print(json.dumps(line), flush=True)
@@ -570,6 +611,7 @@ def main():
     ap.add_argument("--workload", default="ns", choices=list(WORKLOADS))
     ap.add_argument("--size", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--autotune", action="store_true", help="time the element kernels' launch shapes first")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--rates", default="10,20,50")
     args = ap.parse_args()

@@ -174,6 +174,19 @@ int fe_problem_set_params(fe_problem_t *p, const double *params_host);
 int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags,
                 void *stream);
 
+/*
+ * Record one fe_assemble (these pointers and flags) as a CUDA graph, and
+ * replay it: the Newton loop's assembly as a single graph launch instead of
+ * four kernel launches (no counterpart in the reference, whose assembly is
+ * a host loop; it replaces the launch sequence behind
+ * Problem::get_jacobian, problem.cc:4038).  The graph reads the dof vector
+ * and writes R / J_vals at the recorded addresses; parameters, history and
+ * values set later through the other calls are read at replay time.
+ * Capturing again replaces the recorded graph.
+ */
+int fe_problem_graph_capture(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags);
+int fe_problem_graph_launch(fe_problem_t *p, void *stream);
+
 /* The same with HOST buffers: copies in, assembles, copies out, synchronises. */
 int fe_assemble_host(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags);
 

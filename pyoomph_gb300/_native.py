@@ -27,7 +27,8 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_problem_set_params", "fe_assemble", "fe_assemble_host", "fe_residual_max", "fe_dof_update",
            "fe_problem_check", "fe_problem_launch_count", "fe_problem_set_timing", "fe_problem_stage_times", "fe_pattern_host",
            "fe_residual_max_noalloc", "fe_residual_max_noalloc_limit", "fe_problem_element_buffers",
-           "fe_problem_set_history", "fe_problem_shift_history", "fe_problem_set_positions"]
+           "fe_problem_set_history", "fe_problem_shift_history", "fe_problem_set_positions",
+           "fe_problem_graph_capture", "fe_problem_graph_launch"]
 
 
 def _header_stamp() -> str:
@@ -138,6 +139,8 @@ def load(build_if_missing: bool = True):
         L.fe_problem_set_history.argtypes = [vp, c_int, vp]
         L.fe_problem_shift_history.argtypes = [vp]
         L.fe_problem_set_positions.argtypes = [vp, vp]
+        L.fe_problem_graph_capture.argtypes = [vp, vp, vp, vp, c_int]
+        L.fe_problem_graph_launch.argtypes = [vp, vp]
         L.fe_residual_max_noalloc_limit.restype = i64
         _lib = L
         return L

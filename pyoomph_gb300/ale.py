@@ -928,6 +928,10 @@ class DropletProblem:
         self._initialised = False
         self.timings: Dict[str, float] = {}
         self.newton_history: List[float] = []
+        # launch shape of the fused kernel: thread cap and shared-memory budget
+        # per block (both decide elements per block; autotune.tune picks them)
+        self.nthreads_cap = 256
+        self.smem_budget = 100 * 1024
 
     # -- lowering (no GPU) ----------------------------------------------
     def lower(self) -> FusedKernel:
@@ -970,7 +974,8 @@ class DropletProblem:
         ]
         prec = "f64" if self.jacobian_precision in ("fp64", "f64") else "f32"
         self._prec = prec
-        self.kernel = generate_fused(self.domains, 2, self.param_names, nval, 2, prec)
+        self.kernel = generate_fused(self.domains, 2, self.param_names, nval, 2, prec,
+                                     smem_budget=self.smem_budget, nthreads_cap=self.nthreads_cap)
         self.conns = [m.conn, m.interface, m.contact_line]
         n = m.x.shape[0]
         present = np.ones((n, nval), dtype=bool)
@@ -1121,6 +1126,20 @@ class DropletProblem:
 
     def check(self) -> None:
         N.check(N.load().fe_problem_check(self._h))
+
+    def capture_assembly(self, with_jacobian: bool = True) -> None:
+        """Record the assembly from x_dev into R_dev / J_dev as a CUDA graph
+        (fe_problem_graph_capture); assemble_graph replays it."""
+        flags = N.FE_ASSEMBLE_RESIDUAL | N.FE_ASSEMBLE_VALUES_FROM_DOFS
+        if with_jacobian:
+            flags |= N.FE_ASSEMBLE_JACOBIAN
+        N.check(N.load().fe_problem_graph_capture(self._h, self.x_dev.data_ptr(), self.R_dev.data_ptr(),
+                                                  self.J_dev.data_ptr(), flags))
+
+    def assemble_graph(self, stream=None) -> None:
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        N.check(N.load().fe_problem_graph_launch(self._h, ctypes.c_void_p(st)))
 
     def launch_count(self, with_jacobian: bool = True) -> int:
         flags = N.FE_ASSEMBLE_RESIDUAL | N.FE_ASSEMBLE_VALUES_FROM_DOFS

@@ -297,9 +297,11 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         threads = ((max(epb * nq, epb * nloc) + 31) // 32) * 32
     smem = table_bytes + epb * per_elem
     smem = (smem + 15) // 16 * 16
+    if threads > 1024 or smem > 227 * 1024:
+        raise ValueError(f"{epb} elements per block do not fit a block ({threads} threads, {smem} B shared)")
     if name is None:
-        h = hashlib.sha1((et.name + jac_precision + str(affine) + str(pw.r_exprs) + str(pw.d_entries)).encode()
-                         ).hexdigest()[:10]
+        h = hashlib.sha1((et.name + jac_precision + str(affine) + str(epb) + str(pw.r_exprs) +
+                          str(pw.d_entries)).encode()).hexdigest()[:10]
         name = f"fe_elem_{et.name.lower()}_{jac_precision}{'_aff' if affine else ''}_{h}"
 
     nsub = [nn if s_ == "C2" else nn1 for s_ in spaces]

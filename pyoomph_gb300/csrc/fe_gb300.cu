@@ -265,9 +265,12 @@ struct fe_problem {
   std::vector<std::vector<cudaEvent_t>> pending; // per call: 5 events
   double stage_ms[4] = {0, 0, 0, 0};
   long long stage_calls = 0;
+  // one recorded assembly (fe_problem_graph_capture), replayed by fe_problem_graph_launch
+  cudaGraphExec_t graph = nullptr;
   ~fe_problem() {
     for (auto &v : pending)
       for (auto e : v) cudaEventDestroy(e);
+    if (graph) cudaGraphExecDestroy(graph);
   }
 };
 
@@ -970,6 +973,44 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
     CUDA_TRY(cudaEventRecord(ev[4], st));
     p->pending.push_back(ev);
   }
+  return FE_OK;
+}
+
+int fe_problem_graph_capture(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  if (p->graph) {
+    CUDA_TRY(cudaGraphExecDestroy(p->graph));
+    p->graph = nullptr;
+  }
+  cudaStream_t s;
+  CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  const bool timing = p->timing;
+  p->timing = false; // no events inside the recorded graph
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  int rc = FE_OK;
+  if (e == cudaSuccess) {
+    rc = fe_assemble(p, dofs, R, J_vals, flags, (void *)s);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(s, &g);
+    if (rc == FE_OK && e2 == cudaSuccess) {
+      e = cudaGraphInstantiate(&p->graph, g, 0);
+      if (e != cudaSuccess) p->graph = nullptr;
+    } else if (rc == FE_OK) {
+      e = e2;
+    }
+    if (g) cudaGraphDestroy(g);
+  }
+  p->timing = timing;
+  cudaStreamDestroy(s);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(FE_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  return FE_OK;
+}
+
+int fe_problem_graph_launch(fe_problem_t *p, void *stream) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  if (!p->graph) return fail(FE_ERR_ARG, "no recorded assembly (call fe_problem_graph_capture first)");
+  CUDA_TRY(cudaGraphLaunch(p->graph, (cudaStream_t)stream));
   return FE_OK;
 }
 

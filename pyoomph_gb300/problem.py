@@ -408,6 +408,20 @@ class Problem:
         N.check(N.load().fe_assemble(self._h, self.x_dev.data_ptr(), self.R_dev.data_ptr(),
                                      self.J_dev.data_ptr(), flags, ctypes.c_void_p(st)))
 
+    def capture_assembly(self, with_jacobian: bool = True) -> None:
+        """Record the assembly from x_dev into R_dev / J_dev as a CUDA graph
+        (fe_problem_graph_capture); assemble_graph replays it."""
+        flags = N.FE_ASSEMBLE_RESIDUAL | N.FE_ASSEMBLE_VALUES_FROM_DOFS
+        if with_jacobian:
+            flags |= N.FE_ASSEMBLE_JACOBIAN
+        N.check(N.load().fe_problem_graph_capture(self._h, self.x_dev.data_ptr(), self.R_dev.data_ptr(),
+                                                  self.J_dev.data_ptr(), flags))
+
+    def assemble_graph(self, stream=None) -> None:
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        N.check(N.load().fe_problem_graph_launch(self._h, ctypes.c_void_p(st)))
+
     def launch_count(self, with_jacobian: bool = True) -> int:
         flags = N.FE_ASSEMBLE_RESIDUAL | N.FE_ASSEMBLE_VALUES_FROM_DOFS
         if with_jacobian:
