@@ -50,7 +50,12 @@ enum {
 enum {
   FE_ASSEMBLE_RESIDUAL = 1, /* fill R (Problem::get_residuals) */
   FE_ASSEMBLE_JACOBIAN = 2, /* fill the CSR values of J (Problem::get_jacobian) */
-  FE_ASSEMBLE_VALUES_FROM_DOFS = 4 /* first scatter the dof vector into the nodal values */
+  FE_ASSEMBLE_VALUES_FROM_DOFS = 4, /* first scatter the dof vector into the nodal values */
+  /* fused (moving-mesh) code only, each in a call of its own: */
+  FE_ASSEMBLE_MASS = 8,   /* J_vals receives the mass matrix dR/d(du/dt) (flag 2 of the
+                             generated ResidualAndJacobian, jitbridge.h:285) */
+  FE_ASSEMBLE_DPARAM = 16 /* R receives dR/dp for the parameter of fe_problem_set_dparam
+                             (dResidual{i}dParameter_{k}, codegen.cpp:4743-4760) */
 };
 
 /* Jacobian value precision */
@@ -159,6 +164,9 @@ int fe_problem_set_history(fe_problem_t *p, int level, const double *values_host
 int fe_problem_shift_history(fe_problem_t *p);
 /* Overwrite the nodal positions (moving meshes keep them as dofs). */
 int fe_problem_set_positions(fe_problem_t *p, const double *x_host);
+
+/* Parameter of the next FE_ASSEMBLE_DPARAM assembly (index into params). */
+int fe_problem_set_dparam(fe_problem_t *p, int index);
 
 /* Update the global parameters (host array, n_params values). */
 int fe_problem_set_params(fe_problem_t *p, const double *params_host);

@@ -272,8 +272,8 @@ def point_residual(loc: np.ndarray, p: Dict[str, float]) -> np.ndarray:
     th, sig = p["contact_angle"], p["surface_tension"]
     r = loc[:, 2]
     R = np.zeros((loc.shape[0], 4), dtype=loc.dtype)
-    R[:, 0] = sig * (-math.cos(th)) * 2 * math.pi * r
-    R[:, 1] = sig * math.sin(th) * 2 * math.pi * r
+    R[:, 0] = sig * (-np.cos(th)) * 2 * math.pi * r
+    R[:, 1] = sig * np.sin(th) * 2 * math.pi * r
     return R
 
 
@@ -298,6 +298,60 @@ def element_res_jac(D: Droplet, vals: np.ndarray, hist: List[np.ndarray], p: Dic
     out.append(_complex_step(lambda z: line_residual(z, hx, p), _gather(vals, D.line, line_layout())))
     out.append(_complex_step(lambda z: point_residual(z, p), _gather(vals, D.point, point_layout())))
     return out
+
+
+def element_mass(D: Droplet, vals: np.ndarray, hist: List[np.ndarray], p: Dict[str, float]):
+    """Element mass matrices dR_e/d(du/dt): only the interface's kinematic
+    condition has a time derivative (of the positions).  Since
+    du/dt = b0 u + b1 u_prev + b2 u_prev2, dR/d(du/dt) = (dR/du_prev) / b1,
+    taken by complex steps in the previous positions."""
+    lay = line_layout()
+    loc = _gather(vals, D.line, lay)
+    h0 = hist[0][D.line][:, :, 0:2]
+    h1 = hist[1][D.line][:, :, 0:2]
+    M = np.zeros((D.line.shape[0], 15, 15))
+    for l in range(3):
+        for c in range(2):
+            z = h0.astype(np.complex128)
+            z[:, l, c] += 1j * H_CS
+            M[:, :, 9 + 2 * l + c] = line_residual(loc.astype(np.complex128), [z, h1], p).imag / H_CS / p["__bdf1"]
+    nb = D.tri.shape[0]
+    return [np.zeros((nb, 27, 27)), M, np.zeros((1, 4, 4))]
+
+
+def element_dparam(D: Droplet, vals: np.ndarray, hist: List[np.ndarray], p: Dict[str, float], name: str):
+    """Element residual derivatives dR_e/dp by a complex step in p."""
+    q = dict(p)
+    q[name] = p[name] + 1j * H_CS
+    hx = [h[D.line][:, :, 0:2] for h in hist]
+    out = [bulk_residual(_gather(vals, D.tri, bulk_layout()).astype(np.complex128), D.x0[D.tri], q),
+           line_residual(_gather(vals, D.line, line_layout()).astype(np.complex128), hx, q),
+           point_residual(_gather(vals, D.point, point_layout()).astype(np.complex128), q)]
+    return [o.imag / H_CS for o in out]
+
+
+def assemble_blocks(D: Droplet, blocks_R, blocks_J):
+    """Vectors-of-pairs assembly of given element vectors/matrices."""
+    conns = [D.tri, D.line, D.point]
+    lays = [bulk_layout(), line_layout(), point_layout()]
+    R = np.zeros(D.n_dof)
+    rows: List[Dict[int, float]] = [dict() for _ in range(D.n_dof)]
+    for Re, Je, conn, lay in zip(blocks_R, blocks_J, conns, lays):
+        for e in range(conn.shape[0]):
+            eq = [int(D.eqn[conn[e, l], v]) for (l, v) in lay]
+            for i, gi in enumerate(eq):
+                if gi < 0:
+                    continue
+                if Re is not None:
+                    R[gi] += Re[e, i]
+                if Je is None:
+                    continue
+                row = rows[gi]
+                for j, gj in enumerate(eq):
+                    if gj >= 0:
+                        row[gj] = row.get(gj, 0.0) + Je[e, i, j]
+    vals = np.fromiter((v for row in rows for v in row.values()), dtype=np.float64)
+    return R, vals
 
 
 def assemble(D: Droplet, vals: np.ndarray, hist: List[np.ndarray], p: Dict[str, float]):

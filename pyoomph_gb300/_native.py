@@ -13,6 +13,7 @@ from . import build as _build
 
 FE_OK, FE_ERR_ARG, FE_ERR_CUDA, FE_ERR_COMPILE, FE_ERR_NOMEM, FE_ERR_STATE, FE_ERR_DEVICE, FE_ERR_NOGPU = range(8)
 FE_ASSEMBLE_RESIDUAL, FE_ASSEMBLE_JACOBIAN, FE_ASSEMBLE_VALUES_FROM_DOFS = 1, 2, 4
+FE_ASSEMBLE_MASS, FE_ASSEMBLE_DPARAM = 8, 16
 FE_JAC_F64, FE_JAC_F32 = 0, 1
 
 INCLUDE_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc")
@@ -28,7 +29,7 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_problem_check", "fe_problem_launch_count", "fe_problem_set_timing", "fe_problem_stage_times", "fe_pattern_host",
            "fe_residual_max_noalloc", "fe_residual_max_noalloc_limit", "fe_problem_element_buffers",
            "fe_problem_set_history", "fe_problem_shift_history", "fe_problem_set_positions",
-           "fe_problem_graph_capture", "fe_problem_graph_launch"]
+           "fe_problem_graph_capture", "fe_problem_graph_launch", "fe_problem_set_dparam"]
 
 
 def _header_stamp() -> str:
@@ -141,6 +142,7 @@ def load(build_if_missing: bool = True):
         L.fe_problem_set_positions.argtypes = [vp, vp]
         L.fe_problem_graph_capture.argtypes = [vp, vp, vp, vp, c_int]
         L.fe_problem_graph_launch.argtypes = [vp, vp]
+        L.fe_problem_set_dparam.argtypes = [vp, c_int]
         L.fe_residual_max_noalloc_limit.restype = i64
         _lib = L
         return L

@@ -503,7 +503,7 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w("__device__ __forceinline__ void pointwise(const double* __restrict__ U, const double* __restrict__ Xq,")
     w("    const double* __restrict__ XL, const double* __restrict__ Nn, const double* __restrict__ P,")
     w("    const double* __restrict__ tau, double wE, double wL, double* __restrict__ rc, jreal* __restrict__ C,")
-    w("    int flag) {")
+    w("    int flag, int dparam) {")
     w(f"  double rE[{max(1, len(rEn))}], rL[{max(1, len(rLn))}];")
     w(f"  double dE[{max(1, len(eE))}], dL[{max(1, len(eL))}], dN[{max(1, len(eN))}];")
     w("  (void)U; (void)Xq; (void)XL; (void)Nn; (void)P; (void)tau; (void)rE; (void)rL; (void)dE; (void)dL; (void)dN;")
@@ -533,7 +533,7 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
         dlines = [ln for ln in body if ln.strip().startswith(("dE[", "dL[", "dN["))]
         rlines = [ln for ln in body if not ln.strip().startswith(("dE[", "dL[", "dN["))]
         L.extend(rlines)
-        w("  if (flag) {")
+        w("  if (flag == 1 || flag == 2) {")
         L.extend("  " + ln for ln in dlines)
         w("  }")
     for tc in range(ntc):
@@ -543,9 +543,34 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
         if tc in rLn:
             parts.append(f"wL * rL[{rLn[tc]}]")
         w(f"  rc[{tc}] = {' + '.join(parts) if parts else '0.0'};")
-    w("  if (flag) {")
+    w("  if (flag == 1 || flag == 2) {")
     for kk, key in enumerate(keys):
         w(f"    C[{kk}] = (jreal)({' + '.join(terms[key])});")
+    w("  }")
+    # flag 3: residual coefficients differentiated by one global parameter
+    w("  if (flag == 3) {")
+    w("    (void)dparam;")
+    w(f"    for (int k = 0; k < {ntc}; ++k) rc[k] = 0.0;")
+    w("    switch (dparam) {")
+    for j, pn in enumerate(params):
+        psym = E.parameter(pn)
+        pex, pouts = [], []
+        for tc in range(ntc):
+            dEp = sp.diff(rEc[tc], psym) if rEc[tc] != 0 else sp.Integer(0)
+            dLp = sp.diff(rLc[tc], psym) if rLc[tc] != 0 else sp.Integer(0)
+            if dEp != 0 or dLp != 0:
+                pex.append(dEp * sp.Symbol("WE") + dLp * sp.Symbol("WL"))
+                pouts.append(f"rc[{tc}]")
+        if not pex:
+            continue
+        w(f"    case {j}: {{")
+        pn_names = dict(names)
+        pn_names[sp.Symbol("WE")] = "wE"
+        pn_names[sp.Symbol("WL")] = "wL"
+        L.extend(_emit(pex, pn_names, False, pouts, "      "))
+        w("      break; }")
+    w("    default: break;")
+    w("    }")
     w("  }")
     w("}")
     rowof = [slot[(f, l)] for f in range(nf) for l in _sub_nodes(dc, f)]
@@ -672,7 +697,7 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w("    double Xq[3] = {0.0, 0.0, 0.0}, XL[3] = {0.0, 0.0, 0.0};")
     w("    for (int l = 0; l < NN; ++l) for (int i = 0; i < DIM; ++i) "
       "{ Xq[i] += Xe[l * DIM + i] * ps[l]; XL[i] += X0[l * DIM + i] * ps[l]; }")
-    w("    pointwise(U, Xq, XL, Nn, P, tau, wE, wL, rc, C, flag);")
+    w("    pointwise(U, Xq, XL, Nn, P, tau, wE, wL, rc, C, flag, a.aux);")
     w("    misc[0] = tau[0]; misc[1] = tau[1];")
     w("  }")
     w("  __syncthreads();")
@@ -737,7 +762,7 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
         fl_tr, fl_tj = 2 * len(rterms), 0
         if rterms:
             w(f"        Racc += {' + '.join(rterms)};")
-        w("        if (flag) {")
+        w("        if (flag == 1) {")
         av: Dict[int, List[str]] = {}
         for kk, (tc, ic) in enumerate(keys):
             if tc // NCT == tf:
@@ -772,6 +797,24 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
                     w(f"          Jr[{col}] += {' + '.join(parts)};")
                     fl_tj += sum(_ops(x) for x in parts) + len(parts)
         w("        }")
+        # mass matrix: the coefficients of the time-derivative components, basis psi
+        tics = sorted(ic for ic in av if ic % NCU == 1 + 2 * d)
+        if tics:
+            w("        if (flag == 2) {")
+            for ic in tics:
+                w(f"          const jreal av{ic} = {' + '.join(av[ic])};")
+            for g_ in range(nf):
+                ic = g_ * NCU + 1 + 2 * d
+                if ic not in tics:
+                    continue
+                for s_, l in enumerate(_sub_nodes(dc, g_)):
+                    col = slot[(g_, l)]
+                    if fields[g_][1] == "C2":
+                        val = f"{'f' if f32 else ''}ps[{l}]"
+                    else:
+                        val = f"fps1[{s_}]" if f32 else f"sPsi1[q * N1 + {s_}]"
+                    w(f"          Jr[{col}] += av{ic} * {val};")
+            w("        }")
         w("      }")
         w("      break;")
         w("    }")
@@ -787,7 +830,7 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w("    }")
     w("    const long long row = (e0 + el) * NLOC + i;")
     w("    a.rbuf[row] = Racc;")
-    w("    if (flag) {")
+    w("    if (flag == 1 || flag == 2) {")
     w("      jreal* jb = reinterpret_cast<jreal*>(a.jbuf) + row * NLOC;")
     w("      for (int c = 0; c < NLOC; ++c) jb[c] = Jr[c];")
     w("    }")
@@ -1180,6 +1223,33 @@ class DropletProblem:
         rp, ci = self._pattern_cache
         vals = self.J_dev[:self.nnz].cpu().numpy().astype(np.float64)
         return R, sps.csr_matrix((vals, ci, rp), shape=(self.n_dof, self.n_dof))
+
+    def get_mass_matrix(self):
+        """The mass matrix dR/d(du/dt) at the current dofs in the Jacobian's
+        CSR pattern (pyoomph's mass-matrix assembly, flag 2 of the generated
+        element code).  Leaves J_dev holding M."""
+        import scipy.sparse as sps
+        import torch
+        self.initialise()
+        st = torch.cuda.current_stream().cuda_stream
+        N.check(N.load().fe_assemble(self._h, self.x_dev.data_ptr(), self.R_dev.data_ptr(), self.J_dev.data_ptr(),
+                                     N.FE_ASSEMBLE_MASS | N.FE_ASSEMBLE_VALUES_FROM_DOFS, ctypes.c_void_p(st)))
+        self.check()
+        rp, ci = self._pattern_cache
+        vals = self.J_dev[:self.nnz].cpu().numpy().astype(np.float64)
+        return sps.csr_matrix((vals, ci, rp), shape=(self.n_dof, self.n_dof))
+
+    def get_parameter_derivative(self, name: str) -> np.ndarray:
+        """dR/dp of one global parameter at the current dofs
+        (dResidual{i}dParameter_{k} of pyoomph's generated code)."""
+        import torch
+        self.initialise()
+        N.check(N.load().fe_problem_set_dparam(self._h, self.param_names.index(name)))
+        st = torch.cuda.current_stream().cuda_stream
+        N.check(N.load().fe_assemble(self._h, self.x_dev.data_ptr(), self.R_dev.data_ptr(), self.J_dev.data_ptr(),
+                                     N.FE_ASSEMBLE_DPARAM | N.FE_ASSEMBLE_VALUES_FROM_DOFS, ctypes.c_void_p(st)))
+        self.check()
+        return self.R_dev[:self.n_dof].cpu().numpy()
 
     def residual_max(self) -> float:
         import torch

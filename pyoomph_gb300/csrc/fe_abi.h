@@ -23,6 +23,7 @@ struct FeElemArgs {
   const double *x0;        // [n_nodes * dim] Lagrangian (reference) positions
   int n_hist;
   long long hist_stride;    // entries per history level (n_nodes * nval)
+  int aux;                  // flag 3: index of the parameter of dR/dp
 };
 
 // One launch over several domains (bulk, interface, contact line ...): block

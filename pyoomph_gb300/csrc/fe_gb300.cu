@@ -252,7 +252,7 @@ struct Domain {
 struct fe_problem {
   int dim = 0, nval = 0, jac_prec = FE_JAC_F64;
   long long n_nodes = 0, n_dof = 0, nnz = 0;
-  int n_params = 0, params_stride = 0, n_hist = 0, fused = 0;
+  int n_params = 0, params_stride = 0, n_hist = 0, fused = 0, dparam = 0;
   std::vector<Domain> domains;
   DevBuf x, values, eqn, params, status, hist, x0;
   DevBuf rowptr, colidx, cptr, cidx, rptr, ridx;
@@ -534,6 +534,7 @@ FeElemArgs domain_args(fe_problem *p, Domain &d, int flag) {
   a.x0 = p->x0.p ? p->x0.as<double>() : p->x.as<double>();
   a.n_hist = p->n_hist;
   a.hist_stride = (long long)p->n_nodes * p->nval;
+  a.aux = p->dparam;
   return a;
 }
 
@@ -935,8 +936,14 @@ int fe_problem_set_params(fe_problem_t *p, const double *params_host) {
 int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags, void *stream) {
   if (!p) return fail(FE_ERR_ARG, "null problem");
   cudaStream_t st = (cudaStream_t)stream;
-  const bool want_r = flags & FE_ASSEMBLE_RESIDUAL, want_j = flags & FE_ASSEMBLE_JACOBIAN;
+  const bool want_m = flags & FE_ASSEMBLE_MASS, want_p = flags & FE_ASSEMBLE_DPARAM;
+  const bool want_r = (flags & FE_ASSEMBLE_RESIDUAL) || want_p, want_j = (flags & FE_ASSEMBLE_JACOBIAN) || want_m;
   if ((want_r && !R) || (want_j && !J_vals)) return fail(FE_ERR_ARG, "fe_assemble: missing output");
+  if ((want_m || want_p) && !p->fused)
+    return fail(FE_ERR_ARG, "fe_assemble: mass matrices and parameter derivatives need fused (moving-mesh) code");
+  if ((want_m && (flags & FE_ASSEMBLE_JACOBIAN)) || (want_p && (flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS))))
+    return fail(FE_ERR_ARG, "fe_assemble: Jacobian, mass matrix and parameter derivative are separate calls");
+  const int eflag = want_p ? 3 : want_m ? 2 : want_j ? 1 : 0;
   const int sms = sm_count_cached();
   std::vector<cudaEvent_t> ev;
   if (p->timing) {
@@ -951,7 +958,7 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
     CUDA_TRY(cudaGetLastError());
   }
   if (p->timing) CUDA_TRY(cudaEventRecord(ev[1], st));
-  int rc = launch_elements(p, want_j ? 1 : 0, st);
+  int rc = launch_elements(p, eflag, st);
   if (rc) return rc;
   if (p->timing) CUDA_TRY(cudaEventRecord(ev[2], st));
   if (want_r) {
@@ -1011,6 +1018,12 @@ int fe_problem_graph_launch(fe_problem_t *p, void *stream) {
   if (!p) return fail(FE_ERR_ARG, "null problem");
   if (!p->graph) return fail(FE_ERR_ARG, "no recorded assembly (call fe_problem_graph_capture first)");
   CUDA_TRY(cudaGraphLaunch(p->graph, (cudaStream_t)stream));
+  return FE_OK;
+}
+
+int fe_problem_set_dparam(fe_problem_t *p, int index) {
+  if (!p || index < 0 || index >= std::max(1, p->n_params)) return fail(FE_ERR_ARG, "bad parameter index");
+  p->dparam = index;
   return FE_OK;
 }
 
@@ -1146,8 +1159,8 @@ int fe_problem_launch_count(const fe_problem_t *p, int flags) {
     for (const Domain &d : p->domains)
       if (d.n_elem) n++;
   }
-  if (flags & FE_ASSEMBLE_RESIDUAL) n++;
-  if ((flags & FE_ASSEMBLE_JACOBIAN) && p->nnz > 0) n++;
+  if (flags & (FE_ASSEMBLE_RESIDUAL | FE_ASSEMBLE_DPARAM)) n++;
+  if ((flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS)) && p->nnz > 0) n++;
   return n;
 }
 

@@ -48,7 +48,7 @@ class _Args(ctypes.Structure):
                 ("jbuf", ctypes.c_void_p), ("n_elem", ctypes.c_longlong), ("nval", ctypes.c_int),
                 ("flag", ctypes.c_int), ("status", ctypes.c_void_p), ("replica_elems", ctypes.c_longlong),
                 ("params_stride", ctypes.c_int), ("hist", ctypes.c_void_p), ("x0", ctypes.c_void_p),
-                ("n_hist", ctypes.c_int), ("hist_stride", ctypes.c_longlong)]
+                ("n_hist", ctypes.c_int), ("hist_stride", ctypes.c_longlong), ("aux", ctypes.c_int)]
 
 
 def build(ks) -> ctypes.CDLL:
@@ -90,7 +90,7 @@ def run(ks, x, conn, values, params, flag: int = 1):
     jbuf = np.zeros((E, nloc, nloc), dtype=jt)
     status = np.zeros(4, dtype=np.int32)
     a = _Args(x.ctypes.data, conn.ctypes.data, values.ctypes.data, params.ctypes.data, tables.ctypes.data,
-              rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data, 0, 0, None, None, 0, 0)
+              rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data, 0, 0, None, None, 0, 0, 0)
     L.fe_emu_run(ctypes.byref(a), (E + ks.epb - 1) // ks.epb)
     return rbuf, jbuf, status
 
@@ -123,7 +123,7 @@ def build_fused(fk) -> ctypes.CDLL:
     return L
 
 
-def run_fused(fk, conns, values, hist, x0, params, flag: int = 1):
+def run_fused(fk, conns, values, hist, x0, params, flag: int = 1, aux: int = 0):
     """Element residuals and matrices of every domain of a fused kernel.
     values, hist[k]: [n_nodes, nval]; x0: [n_nodes, dim]; conns: per domain
     [E_k, nnode_k]."""
@@ -149,7 +149,7 @@ def run_fused(fk, conns, values, hist, x0, params, flag: int = 1):
         fa.d[k] = _Args(x0.ctypes.data, conn.ctypes.data, values.ctypes.data, params.ctypes.data,
                         tables.ctypes.data, rbuf.ctypes.data, jbuf.ctypes.data, E, nval, flag,
                         status.ctypes.data, 0, 0, hist_arr.ctypes.data, x0.ctypes.data, len(hist),
-                        values.size)
+                        values.size, aux)
         fa.block_start[k] = nb
         nb += (E + dc.epb - 1) // dc.epb
     fa.block_start[len(fk.domains)] = nb

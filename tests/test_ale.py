@@ -274,3 +274,47 @@ def test_gpu_full_size_jacobian_is_the_derivative_of_the_residual():
     Rm = P.get_residuals()
     fd = (Rp - Rm) / (2 * h)
     assert np.max(np.abs(fd - Jd)) <= 1e-6 * np.max(np.abs(Jd))
+
+
+# ---------------------------------------------------------------------------
+# mass matrices and parameter derivatives
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_emulated_mass_matrix_and_parameter_derivatives(prec):
+    P = ale.DropletProblem(N=4, contact_angle_deg=75.0, jacobian_precision=prec)
+    fk = P.lower()
+    D = A.droplet(4)
+    p = _params(75.0)
+    v, h0, h1 = _state(D, 2)
+    outs, status = KE.run_fused(fk, P.conns, v, [h0, h1], D.x0, _pvec(P, p), flag=2)
+    assert not status.any()
+    tol = 1e-12 if prec == "fp64" else 1e-6
+    for (_, Me), Mo in zip(outs, A.element_mass(D, v, [h0, h1], p)):
+        assert np.max(np.abs(Me.astype(np.float64) - Mo)) <= tol * max(1.0, np.max(np.abs(Mo)))
+    for name in ("dynamic_viscosity", "surface_tension", "contact_angle"):
+        outs, _ = KE.run_fused(fk, P.conns, v, [h0, h1], D.x0, _pvec(P, p), flag=3,
+                               aux=P.param_names.index(name))
+        for (Re, Je), Ro in zip(outs, A.element_dparam(D, v, [h0, h1], p, name)):
+            assert np.max(np.abs(Re - Ro)) <= 1e-12 * max(1.0, np.max(np.abs(Ro)))
+            assert not Je.any()
+
+
+@pytest.mark.gpu
+def test_gpu_mass_matrix_and_parameter_derivatives_match_oracle():
+    P = _gpu_problem(5, 65.0)
+    D = A.droplet(5)
+    p = _params(65.0)
+    P.set_params(**{k: p[k] for k in ("__bdf0", "__bdf1", "__bdf2")})
+    v, h0, h1 = _state(D, 9)
+    P.set_state(v, [h0, h1])
+    M = P.get_mass_matrix()
+    _, Mo = A.assemble_blocks(D, [None] * 3, A.element_mass(D, v, [h0, h1], p))
+    assert np.max(np.abs(M.data - Mo)) <= 1e-12 * np.max(np.abs(Mo))
+    for name in ("dynamic_viscosity", "surface_tension", "contact_angle"):
+        dR = P.get_parameter_derivative(name)
+        Ro, _ = A.assemble_blocks(D, A.element_dparam(D, v, [h0, h1], p, name), [None] * 3)
+        assert np.max(np.abs(dR - Ro)) <= 1e-12 * np.max(np.abs(Ro))
+    # the Jacobian path is unaffected afterwards
+    R, J = P.get_jacobian()
+    Ro, orp, oci, ov = A.assemble(D, v, [h0, h1], p)
+    assert np.max(np.abs(J.data - ov)) <= 1e-12 * np.max(np.abs(ov))
