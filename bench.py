@@ -176,6 +176,18 @@ def make_problem(workload: str, size: int, precision: str, epb=None):
     return P
 
 
+# DRAM bytes (read + write) per launch of the element kernel of each bench
+# workload at its default size, from one ncu capture per workload
+# (dram__bytes_read.sum + dram__bytes_write.sum, median of 21 launches;
+# profiles/dram_traffic_element_kernels.md gives the commands).
+MEASURED_TRAFFIC = {
+    ("ns", 256, "fp64"): 207.48e6, ("ns", 256, "fp32"): 86.00e6,
+    ("droplet", 110, "fp64"): 97.69e6, ("droplet", 110, "fp32"): 24.94e6,
+    ("hex", 48, "fp64"): 652.76e6, ("hex", 48, "fp32"): 333.92e6,
+    ("poisson", 64, "fp64"): 0.63e6, ("poisson", 64, "fp32"): 0.62e6,
+}
+
+
 def element_algorithmic_bytes(P) -> int:
     """Compulsory HBM bytes of one element-kernel launch: connectivity,
     nodal positions and values read once, element residuals and matrices
@@ -322,7 +334,8 @@ def run_gb300(args):
                      "residual_gather": float(main["stage_ms"][2]), "jacobian_gather": float(main["stage_ms"][3])},
         "roofline": {"bound": "hbm", "kernel": P.kernel.name, "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": abytes, "traffic": None},
+                     "algorithmic_bytes_per_launch": abytes,
+                     "traffic": MEASURED_TRAFFIC.get((args.workload, args.size, "fp64"))},
         "compute_roofline": {"pipe": "fp64", "kernel": P.kernel.name,
                              "flops_per_element": estimate_flops(P.kernel, P.affine)["fp64"],
                              "achieved": estimate_flops(P.kernel, P.affine)["fp64"] * n_elem / (elem_ms / 1e3) / 1e12,
@@ -517,7 +530,8 @@ def run_droplet(args):
                      "residual_gather": float(m["stage_ms"][2]), "jacobian_gather": float(m["stage_ms"][3])},
         "roofline": {"bound": "hbm", "kernel": P.kernel.name, "achieved": abytes / (elem_ms / 1e3) / 1e9,
                      "peak": hbm_peak, "unit": "GB/s", "frac": abytes / (elem_ms / 1e3) / 1e9 / hbm_peak,
-                     "peak_kind": peak_kind, "algorithmic_bytes_per_launch": abytes, "traffic": None},
+                     "peak_kind": peak_kind, "algorithmic_bytes_per_launch": abytes,
+                     "traffic": MEASURED_TRAFFIC.get(("droplet", args.size, "fp64"))},
         "compute_roofline": {"pipe": "fp64", "kernel": P.kernel.name, "flops_per_launch": flops,
                              "achieved": flops / (elem_ms / 1e3) / 1e12, "peak": peak64, "unit": "TFLOP/s",
                              "frac": flops / (elem_ms / 1e3) / 1e12 / peak64,
