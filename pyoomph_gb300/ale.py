@@ -51,6 +51,7 @@ from . import _native as N
 from . import expressions as E
 from .codegen import _emit
 from .meshes import RectangularQuadMesh
+from .problem import nvtx_range
 from .spaces import GAUSS_T2_KNOTS, GAUSS_T2_WEIGHTS, P2_TRI
 
 # TGauss<1,3> (oomph integral.cc:311-316) and TElement<1,3> shapes (Telements.h:347-366)
@@ -597,7 +598,8 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
         w(f"  const jreal w0j = (jreal)P[{bdf0}]; (void)w0j;")
     w("  for (int k = threadIdx.x; k < nel * NN; k += FE_NT) {")
     w("    const int el = k / NN, l = k - el * NN;")
-    w("    const long long node = a.conn[(e0 + el) * NN + l];")
+    w("    long long node = a.conn[(e0 + el) * NN + l];")
+    w("    FE_CHECK_NODE(node, e0 + el, a);")
     w("    double* eb = sE + el * PER_EL;")
     w("    for (int v = 0; v < NVAL; ++v) eb[l * NVAL + v] = a.values[node * NVAL + v];")
     w("    for (int h = 0; h < NH; ++h)")
@@ -975,6 +977,8 @@ class DropletProblem:
         # per block (both decide elements per block; autotune.tune picks them)
         self.nthreads_cap = 256
         self.smem_budget = 100 * 1024
+        # compile the element code with device-side bounds checks (status word 2)
+        self.bounds_check = False
 
     # -- lowering (no GPU) ----------------------------------------------
     def lower(self) -> FusedKernel:
@@ -1087,10 +1091,12 @@ class DropletProblem:
             raise N.FeError(N.FE_ERR_NOGPU, "pyoomph_gb300 needs a CUDA GPU (none visible)")
         self.lower()
         t0 = time.perf_counter()
-        self.code = _FUSED_CACHE.get(self.kernel.name)
+        ckey = self.kernel.name + ("+bounds" if self.bounds_check else "")
+        self.code = _FUSED_CACHE.get(ckey)
         if self.code is None:
-            self.code = N.Code(self.kernel.source, self.kernel.name)
-            _FUSED_CACHE[self.kernel.name] = self.code
+            src = ("#define FE_BOUNDS_CHECK 1\n" if self.bounds_check else "") + self.kernel.source
+            self.code = N.Code(src, self.kernel.name)
+            _FUSED_CACHE[ckey] = self.code
         t1 = time.perf_counter()
         L = N.load()
         desc, self._doms, self._keep = self._descriptors(with_code=True)
@@ -1274,13 +1280,15 @@ class DropletProblem:
             if it >= self.max_newton_iterations or hist[-1] > self.max_residuals:
                 raise RuntimeError(f"Newton failed: residuals {hist}")
             ta = time.perf_counter()
-            self.assemble_device(with_jacobian=True)
-            self.check()
-            R = self.R_dev[:self.n_dof].cpu().numpy()
-            vals = self.J_dev[:self.nnz].cpu().numpy().astype(np.float64)
+            with nvtx_range("fused assembly R+J"):
+                self.assemble_device(with_jacobian=True)
+                self.check()
+                R = self.R_dev[:self.n_dof].cpu().numpy()
+                vals = self.J_dev[:self.nnz].cpu().numpy().astype(np.float64)
             tb = time.perf_counter()
-            A = sps.csr_matrix((vals, ci, rp), shape=(self.n_dof, self.n_dof))
-            dx = self.linear_solver(A, R) if self.linear_solver else spla.splu(A.tocsc()).solve(R)
+            with nvtx_range("linear solve"):
+                A = sps.csr_matrix((vals, ci, rp), shape=(self.n_dof, self.n_dof))
+                dx = self.linear_solver(A, R) if self.linear_solver else spla.splu(A.tocsc()).solve(R)
             tc = time.perf_counter()
             dxd = torch.as_tensor(dx, device=self.x_dev.device)
             N.check(N.load().fe_dof_update(self._h, self.x_dev.data_ptr(), dxd.data_ptr(), self.n_dof,

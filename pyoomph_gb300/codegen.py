@@ -340,7 +340,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w(f"  for (int k = threadIdx.x; k < {table_doubles}; k += FE_NT) sW[k] = a.tables[k];")
     w("  for (int k = threadIdx.x; k < nel * FE_NN; k += FE_NT) {")
     w("    const int el = k / FE_NN, l = k - el * FE_NN;")
-    w("    const int node = a.conn[(e0 + el) * FE_NN + l];")
+    w("    int node = a.conn[(e0 + el) * FE_NN + l];")
+    w("    FE_CHECK_NODE(node, e0 + el, a);")
     w("    #pragma unroll")
     w("    for (int d = 0; d < FE_DIM; ++d) sX[k * FE_DIM + d] = a.x[(long long)node * FE_DIM + d];")
     w("    #pragma unroll")

@@ -24,6 +24,7 @@ struct FeElemArgs {
   int n_hist;
   long long hist_stride;    // entries per history level (n_nodes * nval)
   int aux;                  // flag 3: index of the parameter of dR/dp
+  long long n_nodes;        // nodes of the problem (bounds of conn entries)
 };
 
 // One launch over several domains (bulk, interface, contact line ...): block

@@ -5,6 +5,25 @@
 
 #include "fe_abi.h"
 
+// Bounds-checked build (compile the element code with -DFE_BOUNDS_CHECK=1):
+// a connectivity entry outside [0, n_nodes) is replaced by node 0, and the
+// kernel records status 2 with the element index instead of reading out of
+// bounds.  The check the sanitizer would make, as an error word.
+#if defined(FE_BOUNDS_CHECK) && FE_BOUNDS_CHECK
+#define FE_CHECK_NODE(node, elem, args)                                          \
+  do {                                                                           \
+    if ((node) < 0 || (long long)(node) >= (args).n_nodes) {                     \
+      atomicExch((args).status + 1, (int)(elem));                                \
+      atomicExch((args).status, 2);                                              \
+      (node) = 0;                                                                \
+    }                                                                            \
+  } while (0)
+#else
+#define FE_CHECK_NODE(node, elem, args) \
+  do {                                  \
+  } while (0)
+#endif
+
 // Geometry at one integration point through the metric tensor, the route of
 // BulkElementBase::fill_shape_info_at_s (src/elements.cpp:3593-3990):
 //   t[a][i]  = sum_l x_l,i dpsi_l/ds_a         (tangent vectors)

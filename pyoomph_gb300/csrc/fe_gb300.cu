@@ -535,6 +535,7 @@ FeElemArgs domain_args(fe_problem *p, Domain &d, int flag) {
   a.n_hist = p->n_hist;
   a.hist_stride = (long long)p->n_nodes * p->nval;
   a.aux = p->dparam;
+  a.n_nodes = p->n_nodes;
   return a;
 }
 

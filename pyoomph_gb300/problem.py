@@ -59,6 +59,19 @@ _KERNEL_CACHE: Dict[tuple, KernelSpec] = {}
 _CODE_CACHE: Dict[str, "N.Code"] = {}
 
 
+def nvtx_range(name: str):
+    """NVTX range around a host-side stage (assembly, linear solve) for
+    timeline profilers; a no-op context when torch has no CUDA."""
+    import contextlib
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return torch.cuda.nvtx.range(name)
+    except Exception:
+        pass
+    return contextlib.nullcontext()
+
+
 class NewtonSolverError(RuntimeError):
     """Raised when Newton diverges or exceeds its iteration cap
     (oomph's NewtonSolverError, problem.cc:9298)."""
@@ -93,6 +106,8 @@ class Problem:
         # > 1: a stack of independent copies of the problem assembled together
         self.replicas = 1
         self.linear_solver: Optional[Callable] = None
+        # compile the element code with device-side bounds checks (status word 2)
+        self.bounds_check = False
         self.verbose = False
         self._initialised = False
         self.newton_history: List[float] = []
@@ -256,10 +271,12 @@ class Problem:
         mesh, fields, prec = self.mesh, self.fields, self._prec
         n, nval, values, eqn = mesh.n_nodes, len(fields), self._values0, self.eqn
         t2 = time.perf_counter()
-        self.code = _CODE_CACHE.get(self.kernel.name)
+        ckey = self.kernel.name + ("+bounds" if self.bounds_check else "")
+        self.code = _CODE_CACHE.get(ckey)
         if self.code is None:
-            self.code = N.Code(self.kernel.source, self.kernel.name)
-            _CODE_CACHE[self.kernel.name] = self.code
+            src = ("#define FE_BOUNDS_CHECK 1\n" if self.bounds_check else "") + self.kernel.source
+            self.code = N.Code(src, self.kernel.name)
+            _CODE_CACHE[ckey] = self.code
         t3 = time.perf_counter()
         # device problem
         L = N.load()
@@ -510,11 +527,13 @@ class Problem:
             if hist[-1] > self.max_residuals:
                 raise NewtonSolverError(f"max residuals ({self.max_residuals}) exceeded: {hist}")
             ta = time.perf_counter()
-            self.assemble_device(with_jacobian=True)
-            self.check()
-            R = self.R_dev[:self.n_dof].cpu().numpy()
+            with nvtx_range("fe_assemble R+J"):
+                self.assemble_device(with_jacobian=True)
+                self.check()
+                R = self.R_dev[:self.n_dof].cpu().numpy()
             tb = time.perf_counter()
-            dx = self._solve_linear(R)
+            with nvtx_range("linear solve"):
+                dx = self._solve_linear(R)
             tc = time.perf_counter()
             dxd = torch.as_tensor(dx, device=self.x_dev.device)
             N.check(N.load().fe_dof_update(self._h, self.x_dev.data_ptr(), dxd.data_ptr(), self.n_dof,

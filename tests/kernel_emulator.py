@@ -48,7 +48,7 @@ class _Args(ctypes.Structure):
                 ("jbuf", ctypes.c_void_p), ("n_elem", ctypes.c_longlong), ("nval", ctypes.c_int),
                 ("flag", ctypes.c_int), ("status", ctypes.c_void_p), ("replica_elems", ctypes.c_longlong),
                 ("params_stride", ctypes.c_int), ("hist", ctypes.c_void_p), ("x0", ctypes.c_void_p),
-                ("n_hist", ctypes.c_int), ("hist_stride", ctypes.c_longlong), ("aux", ctypes.c_int)]
+                ("n_hist", ctypes.c_int), ("hist_stride", ctypes.c_longlong), ("aux", ctypes.c_int), ("n_nodes", ctypes.c_longlong)]
 
 
 def build(ks) -> ctypes.CDLL:
@@ -90,7 +90,8 @@ def run(ks, x, conn, values, params, flag: int = 1):
     jbuf = np.zeros((E, nloc, nloc), dtype=jt)
     status = np.zeros(4, dtype=np.int32)
     a = _Args(x.ctypes.data, conn.ctypes.data, values.ctypes.data, params.ctypes.data, tables.ctypes.data,
-              rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data, 0, 0, None, None, 0, 0, 0)
+              rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data, 0, 0, None, None, 0, 0, 0,
+              x.shape[0])
     L.fe_emu_run(ctypes.byref(a), (E + ks.epb - 1) // ks.epb)
     return rbuf, jbuf, status
 
@@ -99,11 +100,11 @@ class _FusedArgs(ctypes.Structure):
     _fields_ = [("d", _Args * 4), ("block_start", ctypes.c_int * 5), ("n_domains", ctypes.c_int)]
 
 
-def build_fused(fk) -> ctypes.CDLL:
+def build_fused(fk, defines=()) -> ctypes.CDLL:
     """Emulator library of a fused multi-domain kernel (pyoomph_gb300.ale)."""
     src = re.sub(r"#define FE_NT \d+", "#define FE_NT 1", fk.source)
     src = src.replace("extern __shared__ __align__(16) unsigned char fe_smem[];", "")
-    body = PRELUDE + src + (
+    body = "".join(f"#define {d_} 1\n" for d_ in defines) + PRELUDE + src + (
         f'\nextern "C" void fe_emu_run_fused(const FeFusedArgs *a, int nblocks) {{\n'
         f'  for (int b = 0; b < nblocks; ++b) {{\n'
         f'    memset(fe_smem, 0xff, sizeof(fe_smem));\n'
@@ -123,11 +124,11 @@ def build_fused(fk) -> ctypes.CDLL:
     return L
 
 
-def run_fused(fk, conns, values, hist, x0, params, flag: int = 1, aux: int = 0):
+def run_fused(fk, conns, values, hist, x0, params, flag: int = 1, aux: int = 0, defines=()):
     """Element residuals and matrices of every domain of a fused kernel.
     values, hist[k]: [n_nodes, nval]; x0: [n_nodes, dim]; conns: per domain
     [E_k, nnode_k]."""
-    L = build_fused(fk)
+    L = build_fused(fk, defines)
     nval = values.shape[1]
     values = np.ascontiguousarray(values, dtype=np.float64)
     hist_arr = np.ascontiguousarray(np.stack(hist), dtype=np.float64)
@@ -149,7 +150,7 @@ def run_fused(fk, conns, values, hist, x0, params, flag: int = 1, aux: int = 0):
         fa.d[k] = _Args(x0.ctypes.data, conn.ctypes.data, values.ctypes.data, params.ctypes.data,
                         tables.ctypes.data, rbuf.ctypes.data, jbuf.ctypes.data, E, nval, flag,
                         status.ctypes.data, 0, 0, hist_arr.ctypes.data, x0.ctypes.data, len(hist),
-                        values.size, aux)
+                        values.size, aux, values.shape[0])
         fa.block_start[k] = nb
         nb += (E + dc.epb - 1) // dc.epb
     fa.block_start[len(fk.domains)] = nb
