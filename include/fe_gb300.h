@@ -195,6 +195,21 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
 int fe_problem_graph_capture(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags);
 int fe_problem_graph_launch(fe_problem_t *p, void *stream);
 
+/*
+ * fe_assemble with HOST buffers, pipelined: the dof vector is copied in,
+ * the elements run in nchunks consecutive ranges, and after each range the
+ * rows it completed (every element touching them done) are gathered and
+ * copied to the host on a second stream while the next range computes.  R
+ * and J_vals are host buffers (pinned memory for overlap); results equal
+ * fe_assemble's bit for bit.  Asynchronous on `stream`: the copies have
+ * landed when the stream has completed.  Single-domain problems without
+ * replicas; flags RESIDUAL, JACOBIAN, VALUES_FROM_DOFS.  Replaces the same
+ * assembly calls as fe_assemble for a caller that keeps R and J on the host
+ * (oomph's Problem::get_jacobian, problem.cc:4038-4165).
+ */
+int fe_assemble_pipelined(fe_problem_t *p, const double *dofs_host, double *R_host, void *J_host, int flags,
+                          int nchunks, void *stream);
+
 /* The same with HOST buffers: copies in, assembles, copies out, synchronises. */
 int fe_assemble_host(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags);
 

@@ -29,7 +29,8 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_problem_check", "fe_problem_launch_count", "fe_problem_set_timing", "fe_problem_stage_times", "fe_pattern_host",
            "fe_residual_max_noalloc", "fe_residual_max_noalloc_limit", "fe_problem_element_buffers",
            "fe_problem_set_history", "fe_problem_shift_history", "fe_problem_set_positions",
-           "fe_problem_graph_capture", "fe_problem_graph_launch", "fe_problem_set_dparam"]
+           "fe_problem_graph_capture", "fe_problem_graph_launch", "fe_problem_set_dparam",
+           "fe_assemble_pipelined"]
 
 
 def _header_stamp() -> str:
@@ -143,6 +144,7 @@ def load(build_if_missing: bool = True):
         L.fe_problem_graph_capture.argtypes = [vp, vp, vp, vp, c_int]
         L.fe_problem_graph_launch.argtypes = [vp, vp]
         L.fe_problem_set_dparam.argtypes = [vp, c_int]
+        L.fe_assemble_pipelined.argtypes = [vp, vp, vp, vp, c_int, c_int, vp]
         L.fe_residual_max_noalloc_limit.restype = i64
         _lib = L
         return L

@@ -267,10 +267,27 @@ struct fe_problem {
   long long stage_calls = 0;
   // one recorded assembly (fe_problem_graph_capture), replayed by fe_problem_graph_launch
   cudaGraphExec_t graph = nullptr;
+  // pipelined host-buffer assembly (fe_assemble_pipelined): the last element
+  // touching each row (single-domain problems), the chunk plan, device
+  // staging buffers, a copy stream and one event per chunk
+  std::vector<int32_t> row_last;
+  int pipe_chunks = 0;
+  std::vector<long long> pipe_elem, pipe_row;
+  DevBuf pipe_dofs, pipe_R, pipe_J;
+  cudaStream_t pipe_copy = nullptr;
+  std::vector<cudaEvent_t> pipe_ev;
+  void pipe_release() {
+    for (auto e : pipe_ev) cudaEventDestroy(e);
+    pipe_ev.clear();
+    if (pipe_copy) cudaStreamDestroy(pipe_copy);
+    pipe_copy = nullptr;
+    pipe_chunks = 0;
+  }
   ~fe_problem() {
     for (auto &v : pending)
       for (auto e : v) cudaEventDestroy(e);
     if (graph) cudaGraphExecDestroy(graph);
+    pipe_release();
   }
 };
 
@@ -846,6 +863,18 @@ int fe_problem_create(const fe_problem_desc_t *desc, fe_problem_t **out) {
   if ((rc = P->rbuf_all.alloc(sizeof(double) * std::max(1LL, rtot)))) return rc;
   if ((rc = P->partial.alloc(sizeof(double) * 4096))) return rc;
   if ((rc = build_pattern(P.get(), conn_h, desc->eqn))) return rc;
+  if (!P->fused && P->domains.size() == 1 && P->domains[0].replica_elems == 0) {
+    // last element (in element order) contributing to each row
+    const Domain &d = P->domains[0];
+    const fe_domain_desc_t &dd = desc->domains[0];
+    P->row_last.assign((size_t)P->n_dof, -1);
+    for (long long e = 0; e < d.n_elem; e++)
+      for (int i = 0; i < d.nlocal; i++) {
+        const long long node = dd.conn[e * d.nnode + d.local_node[i]];
+        const int eq = desc->eqn[node * desc->nval + d.local_val[i]];
+        if (eq >= 0) P->row_last[eq] = (int32_t)e;
+      }
+  }
   *out = P.release();
   return FE_OK;
 }
@@ -1019,6 +1048,112 @@ int fe_problem_graph_launch(fe_problem_t *p, void *stream) {
   if (!p) return fail(FE_ERR_ARG, "null problem");
   if (!p->graph) return fail(FE_ERR_ARG, "no recorded assembly (call fe_problem_graph_capture first)");
   CUDA_TRY(cudaGraphLaunch(p->graph, (cudaStream_t)stream));
+  return FE_OK;
+}
+
+namespace {
+int plan_pipeline(fe_problem *p, int nchunks) {
+  const Domain &d = p->domains[0];
+  const long long units = (d.n_elem + d.epb - 1) / d.epb; // element blocks
+  nchunks = (int)std::max(1LL, std::min<long long>(nchunks, units));
+  if (p->pipe_copy) CUDA_TRY(cudaStreamSynchronize(p->pipe_copy)); // copies of the old plan
+  p->pipe_release();
+  p->pipe_elem.assign(nchunks + 1, 0);
+  for (int k = 0; k <= nchunks; k++)
+    p->pipe_elem[k] = std::min(d.n_elem, (units * k / nchunks) * d.epb);
+  // rows [0, pipe_row[k+1]) are complete after chunk k: the longest prefix
+  // of rows whose last contributing element lies in chunks <= k
+  p->pipe_row.assign(nchunks + 1, 0);
+  long long r = 0;
+  for (int k = 0; k < nchunks; k++) {
+    while (r < p->n_dof && p->row_last[r] < p->pipe_elem[k + 1]) r++;
+    p->pipe_row[k + 1] = r;
+  }
+  p->pipe_row[nchunks] = p->n_dof;
+  CUDA_TRY(cudaStreamCreateWithFlags(&p->pipe_copy, cudaStreamNonBlocking));
+  p->pipe_ev.resize(nchunks + 1);
+  for (auto &e : p->pipe_ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  p->pipe_chunks = nchunks;
+  return FE_OK;
+}
+} // namespace
+
+int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags, int nchunks,
+                          void *stream) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  if (p->row_last.empty() && p->n_dof > 0)
+    return fail(FE_ERR_ARG, "fe_assemble_pipelined: single-domain problems without replicas only");
+  const bool want_r = flags & FE_ASSEMBLE_RESIDUAL, want_j = flags & FE_ASSEMBLE_JACOBIAN;
+  if (flags & ~(FE_ASSEMBLE_RESIDUAL | FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_VALUES_FROM_DOFS))
+    return fail(FE_ERR_ARG, "fe_assemble_pipelined: residual and Jacobian flags only");
+  if ((want_r && !R) || (want_j && !J_vals) || ((flags & FE_ASSEMBLE_VALUES_FROM_DOFS) && !dofs))
+    return fail(FE_ERR_ARG, "fe_assemble_pipelined: missing buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc;
+  if (p->pipe_chunks != std::max(1, nchunks) && (rc = plan_pipeline(p, nchunks))) return rc;
+  const size_t jel = p->jac_prec == FE_JAC_F64 ? sizeof(double) : sizeof(float);
+  if (!p->pipe_dofs.p && ((rc = p->pipe_dofs.alloc(sizeof(double) * std::max(1LL, p->n_dof))) ||
+                          (rc = p->pipe_R.alloc(sizeof(double) * std::max(1LL, p->n_dof))) ||
+                          (rc = p->pipe_J.alloc(jel * std::max(1LL, p->nnz)))))
+    return rc;
+  const int sms = sm_count_cached();
+  // the previous call's copies read the staging buffers: finish them first
+  CUDA_TRY(cudaStreamWaitEvent(st, p->pipe_ev[p->pipe_chunks], 0));
+  if (flags & FE_ASSEMBLE_VALUES_FROM_DOFS) {
+    CUDA_TRY(cudaMemcpyAsync(p->pipe_dofs.p, dofs, sizeof(double) * p->n_dof, cudaMemcpyHostToDevice, st));
+    long long n = p->n_nodes * p->nval;
+    k_scatter_dofs<<<grid_for(n, 256, sms), 256, 0, st>>>(p->pipe_dofs.as<double>(), p->eqn.as<int>(),
+                                                          p->values.as<double>(), n);
+    CUDA_TRY(cudaGetLastError());
+  }
+  Domain &d = p->domains[0];
+  const int32_t *h_rp = p->h_rowptr.data();
+  for (int k = 0; k < p->pipe_chunks; k++) {
+    const long long e0 = p->pipe_elem[k], e1 = p->pipe_elem[k + 1];
+    if (e1 > e0) {
+      FeElemArgs a = domain_args(p, d, want_j ? 1 : 0);
+      a.conn += e0 * d.nnode;
+      a.rbuf += e0 * d.nlocal;
+      a.jbuf = (char *)a.jbuf + jel * (size_t)(e0 * (long long)d.nlocal * d.nlocal);
+      a.n_elem = e1 - e0;
+      void *kp[] = {&a};
+      unsigned grid = (unsigned)((a.n_elem + d.epb - 1) / d.epb);
+      CUDA_TRY(cudaLaunchKernel((const void *)d.code->func, dim3(grid), dim3(d.threads), kp, (size_t)d.smem, st));
+    }
+    const long long r0 = p->pipe_row[k], r1 = p->pipe_row[k + 1];
+    if (r1 > r0) {
+      const long long s0 = h_rp[r0], s1 = h_rp[r1];
+      if (want_r) {
+        k_gather_rows<<<grid_for(r1 - r0, 256, sms), 256, 0, st>>>(p->rptr.as<long long>() + r0, p->ridx.as<unsigned>(),
+                                                                  p->rbuf_all.as<double>(), p->pipe_R.as<double>() + r0,
+                                                                  r1 - r0);
+        CUDA_TRY(cudaGetLastError());
+      }
+      if (want_j && s1 > s0) {
+        if (p->jac_prec == FE_JAC_F64)
+          k_gather_slots<double><<<grid_for(s1 - s0, 256, sms), 256, 0, st>>>(
+              p->cptr.as<long long>() + s0, p->cidx.as<unsigned>(), p->jbuf_all.as<double>(),
+              p->pipe_J.as<double>() + s0, s1 - s0);
+        else
+          k_gather_slots<float><<<grid_for(s1 - s0, 256, sms), 256, 0, st>>>(
+              p->cptr.as<long long>() + s0, p->cidx.as<unsigned>(), p->jbuf_all.as<float>(),
+              p->pipe_J.as<float>() + s0, s1 - s0);
+        CUDA_TRY(cudaGetLastError());
+      }
+      // copy the finished rows to the host while the next chunk computes
+      CUDA_TRY(cudaEventRecord(p->pipe_ev[k], st));
+      CUDA_TRY(cudaStreamWaitEvent(p->pipe_copy, p->pipe_ev[k], 0));
+      if (want_r)
+        CUDA_TRY(cudaMemcpyAsync(R + r0, p->pipe_R.as<double>() + r0, sizeof(double) * (r1 - r0),
+                                 cudaMemcpyDeviceToHost, p->pipe_copy));
+      if (want_j && s1 > s0)
+        CUDA_TRY(cudaMemcpyAsync((char *)J_vals + jel * s0, (const char *)p->pipe_J.p + jel * s0, jel * (s1 - s0),
+                                 cudaMemcpyDeviceToHost, p->pipe_copy));
+    }
+  }
+  // the caller's stream completes only after the copies
+  CUDA_TRY(cudaEventRecord(p->pipe_ev[p->pipe_chunks], p->pipe_copy));
+  CUDA_TRY(cudaStreamWaitEvent(st, p->pipe_ev[p->pipe_chunks], 0));
   return FE_OK;
 }
 

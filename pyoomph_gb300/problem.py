@@ -425,6 +425,22 @@ class Problem:
         N.check(N.load().fe_assemble(self._h, self.x_dev.data_ptr(), self.R_dev.data_ptr(),
                                      self.J_dev.data_ptr(), flags, ctypes.c_void_p(st)))
 
+    def assemble_host(self, x_host, R_host, J_host, with_jacobian: bool = True, chunks: int = 8, stream=None) -> None:
+        """Assemble from a host dof vector into host R / CSR values
+        (fe_assemble_pipelined: the copies of finished rows overlap the
+        element chunks still computing).  Pass pinned tensors/arrays;
+        asynchronous on the stream."""
+        import torch
+        flags = N.FE_ASSEMBLE_RESIDUAL | N.FE_ASSEMBLE_VALUES_FROM_DOFS
+        if with_jacobian:
+            flags |= N.FE_ASSEMBLE_JACOBIAN
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+
+        def ptr(a):
+            return a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data
+        N.check(N.load().fe_assemble_pipelined(self._h, ptr(x_host), ptr(R_host), ptr(J_host), flags, int(chunks),
+                                               ctypes.c_void_p(st)))
+
     def capture_assembly(self, with_jacobian: bool = True) -> None:
         """Record the assembly from x_dev into R_dev / J_dev as a CUDA graph
         (fe_problem_graph_capture); assemble_graph replays it."""

@@ -85,3 +85,26 @@ def test_autotune_picks_a_measured_candidate(tmp_path):
     assert best in (2, 4, 8) and set(table) == {"2", "4", "8"}
     P = make(best)
     assert P.kernel.epb == best
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,prec,chunks", [("ns", "fp64", 1), ("ns", "fp64", 5), ("ns", "fp32", 8),
+                                               ("poisson", "fp64", 3)])
+def test_pipelined_host_assembly_equals_device_assembly(kind, prec, chunks):
+    import torch
+    from pyoomph_gb300 import workloads as W
+    P = (W.navier_stokes_problem(N=20, jacobian_precision=prec) if kind == "ns"
+         else W.poisson_problem(N=20, jacobian_precision=prec))
+    P.initialise()
+    W.perturb_dofs(P, seed=4, sigma=1e-2)
+    P.assemble_device(True)
+    R0 = P.R_dev[:P.n_dof].cpu()
+    J0 = P.J_dev[:P.nnz].cpu()
+    xh = P.x_dev[:P.n_dof].cpu().pin_memory()
+    Rh = torch.full((P.n_dof,), float("nan"), dtype=torch.float64).pin_memory()
+    Jh = torch.full((P.nnz,), float("nan"), dtype=P.J_dev.dtype).pin_memory()
+    for _ in range(2):                          # a second call reuses the plan and buffers
+        P.assemble_host(xh, Rh, Jh, chunks=chunks)
+        torch.cuda.current_stream().synchronize()
+        P.check()
+        assert torch.equal(Rh, R0) and torch.equal(Jh, J0)
