@@ -19,6 +19,7 @@
 #include <nvrtc.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
@@ -272,7 +273,8 @@ struct fe_problem {
   // staging buffers, a copy stream and one event per chunk
   std::vector<int32_t> row_last;
   int pipe_chunks = 0;
-  std::vector<long long> pipe_elem, pipe_row;
+  std::vector<long long> pipe_elem;
+  std::vector<std::vector<std::pair<long long, long long>>> pipe_runs; // per chunk: row ranges it completes
   DevBuf pipe_dofs, pipe_R, pipe_J;
   cudaStream_t pipe_copy = nullptr;
   std::vector<cudaEvent_t> pipe_ev;
@@ -1061,15 +1063,51 @@ int plan_pipeline(fe_problem *p, int nchunks) {
   p->pipe_elem.assign(nchunks + 1, 0);
   for (int k = 0; k <= nchunks; k++)
     p->pipe_elem[k] = std::min(d.n_elem, (units * k / nchunks) * d.epb);
-  // rows [0, pipe_row[k+1]) are complete after chunk k: the longest prefix
-  // of rows whose last contributing element lies in chunks <= k
-  p->pipe_row.assign(nchunks + 1, 0);
-  long long r = 0;
-  for (int k = 0; k < nchunks; k++) {
-    while (r < p->n_dof && p->row_last[r] < p->pipe_elem[k + 1]) r++;
-    p->pipe_row[k + 1] = r;
+  // a row is complete after the chunk holding its last contributing element;
+  // maximal runs of consecutive rows completed by the same chunk become one
+  // gather + copy each (structured meshes give a few runs per chunk: the
+  // vertex rows and the rows of the nodes added for the quadratic space)
+  std::vector<int> chunk_of(p->n_dof);
+  for (long long r = 0; r < p->n_dof; r++) {
+    const long long e = p->row_last[r];
+    int k = 0;
+    while (k + 1 < nchunks && e >= p->pipe_elem[k + 1]) k++;
+    chunk_of[r] = e < 0 ? 0 : k;
   }
-  p->pipe_row[nchunks] = p->n_dof;
+  std::vector<std::array<long long, 3>> runs; // chunk, r0, r1
+  for (long long r = 0; r < p->n_dof;) {
+    long long r1 = r + 1;
+    while (r1 < p->n_dof && chunk_of[r1] == chunk_of[r]) r1++;
+    runs.push_back({chunk_of[r], r, r1});
+    r = r1;
+  }
+  // short runs (the alternating rows of the element column a chunk boundary
+  // cuts) join the following run when that one completes no earlier: a row
+  // may always be gathered late, never early
+  {
+    const long long thr = std::max(1LL, p->n_dof / (16LL * nchunks));
+    std::vector<std::array<long long, 3>> m;
+    for (auto it = runs.rbegin(); it != runs.rend(); ++it) {
+      if (!m.empty() && (*it)[2] - (*it)[1] < thr && m.back()[0] >= (*it)[0])
+        m.back()[1] = (*it)[1];
+      else
+        m.push_back(*it);
+    }
+    runs.assign(m.rbegin(), m.rend());
+  }
+  // still too many runs: pairwise merges into the later chunk (safety net)
+  while ((long long)runs.size() > 8LL * nchunks) {
+    std::vector<std::array<long long, 3>> m;
+    for (size_t i = 0; i < runs.size(); i += 2) {
+      if (i + 1 < runs.size())
+        m.push_back({std::max(runs[i][0], runs[i + 1][0]), runs[i][1], runs[i + 1][2]});
+      else
+        m.push_back(runs[i]);
+    }
+    runs.swap(m);
+  }
+  p->pipe_runs.assign(nchunks, {});
+  for (auto &q : runs) p->pipe_runs[q[0]].push_back({q[1], q[2]});
   CUDA_TRY(cudaStreamCreateWithFlags(&p->pipe_copy, cudaStreamNonBlocking));
   p->pipe_ev.resize(nchunks + 1);
   for (auto &e : p->pipe_ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1120,8 +1158,8 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
       unsigned grid = (unsigned)((a.n_elem + d.epb - 1) / d.epb);
       CUDA_TRY(cudaLaunchKernel((const void *)d.code->func, dim3(grid), dim3(d.threads), kp, (size_t)d.smem, st));
     }
-    const long long r0 = p->pipe_row[k], r1 = p->pipe_row[k + 1];
-    if (r1 > r0) {
+    for (const auto &run : p->pipe_runs[k]) {
+      const long long r0 = run.first, r1 = run.second;
       const long long s0 = h_rp[r0], s1 = h_rp[r1];
       if (want_r) {
         k_gather_rows<<<grid_for(r1 - r0, 256, sms), 256, 0, st>>>(p->rptr.as<long long>() + r0, p->ridx.as<unsigned>(),
@@ -1140,9 +1178,14 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
               p->pipe_J.as<float>() + s0, s1 - s0);
         CUDA_TRY(cudaGetLastError());
       }
-      // copy the finished rows to the host while the next chunk computes
-      CUDA_TRY(cudaEventRecord(p->pipe_ev[k], st));
-      CUDA_TRY(cudaStreamWaitEvent(p->pipe_copy, p->pipe_ev[k], 0));
+    }
+    if (p->pipe_runs[k].empty()) continue;
+    // copy the finished rows to the host while the next chunk computes
+    CUDA_TRY(cudaEventRecord(p->pipe_ev[k], st));
+    CUDA_TRY(cudaStreamWaitEvent(p->pipe_copy, p->pipe_ev[k], 0));
+    for (const auto &run : p->pipe_runs[k]) {
+      const long long r0 = run.first, r1 = run.second;
+      const long long s0 = h_rp[r0], s1 = h_rp[r1];
       if (want_r)
         CUDA_TRY(cudaMemcpyAsync(R + r0, p->pipe_R.as<double>() + r0, sizeof(double) * (r1 - r0),
                                  cudaMemcpyDeviceToHost, p->pipe_copy));
