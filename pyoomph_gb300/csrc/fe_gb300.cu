@@ -272,7 +272,7 @@ struct fe_problem {
   // touching each row (single-domain problems), the chunk plan, device
   // staging buffers, a copy stream and one event per chunk
   std::vector<int32_t> row_last;
-  int pipe_chunks = 0;
+  int pipe_chunks = 0, pipe_requested = 0;
   std::vector<long long> pipe_elem;
   std::vector<std::vector<std::pair<long long, long long>>> pipe_runs; // per chunk: row ranges it completes
   DevBuf pipe_dofs, pipe_R, pipe_J;
@@ -284,6 +284,7 @@ struct fe_problem {
     if (pipe_copy) cudaStreamDestroy(pipe_copy);
     pipe_copy = nullptr;
     pipe_chunks = 0;
+    pipe_requested = 0;
   }
   ~fe_problem() {
     for (auto &v : pending)
@@ -1055,14 +1056,24 @@ int fe_problem_graph_launch(fe_problem_t *p, void *stream) {
 
 namespace {
 int plan_pipeline(fe_problem *p, int nchunks) {
+  const int requested = nchunks;
   const Domain &d = p->domains[0];
-  const long long units = (d.n_elem + d.epb - 1) / d.epb; // element blocks
-  nchunks = (int)std::max(1LL, std::min<long long>(nchunks, units));
+  // chunks hold whole waves of blocks (all SMs busy), so only the last one has a tail
+  int per_sm = 1;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)d.code->func, d.threads, d.smem));
+  const long long wave = (long long)std::max(1, per_sm) * sm_count_cached(); // blocks per wave
+  const long long blocks = (d.n_elem + d.epb - 1) / d.epb;
+  const long long waves = (blocks + wave - 1) / wave;
+  nchunks = (int)std::max(1LL, std::min<long long>(nchunks, waves));
+  const long long wave_per_chunk = (waves + nchunks - 1) / nchunks;
+  nchunks = (int)((waves + wave_per_chunk - 1) / wave_per_chunk);
+  const long long units = blocks;
   if (p->pipe_copy) CUDA_TRY(cudaStreamSynchronize(p->pipe_copy)); // copies of the old plan
   p->pipe_release();
   p->pipe_elem.assign(nchunks + 1, 0);
   for (int k = 0; k <= nchunks; k++)
-    p->pipe_elem[k] = std::min(d.n_elem, (units * k / nchunks) * d.epb);
+    p->pipe_elem[k] = std::min(d.n_elem, std::min(units, k * wave_per_chunk * wave) * d.epb);
+  p->pipe_elem[nchunks] = d.n_elem;
   // a row is complete after the chunk holding its last contributing element;
   // maximal runs of consecutive rows completed by the same chunk become one
   // gather + copy each (structured meshes give a few runs per chunk: the
@@ -1112,6 +1123,7 @@ int plan_pipeline(fe_problem *p, int nchunks) {
   p->pipe_ev.resize(nchunks + 1);
   for (auto &e : p->pipe_ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   p->pipe_chunks = nchunks;
+  p->pipe_requested = requested;
   return FE_OK;
 }
 } // namespace
@@ -1128,7 +1140,7 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
     return fail(FE_ERR_ARG, "fe_assemble_pipelined: missing buffer");
   cudaStream_t st = (cudaStream_t)stream;
   int rc;
-  if (p->pipe_chunks != std::max(1, nchunks) && (rc = plan_pipeline(p, nchunks))) return rc;
+  if (p->pipe_requested != std::max(1, nchunks) && (rc = plan_pipeline(p, std::max(1, nchunks)))) return rc;
   const size_t jel = p->jac_prec == FE_JAC_F64 ? sizeof(double) : sizeof(float);
   if (!p->pipe_dofs.p && ((rc = p->pipe_dofs.alloc(sizeof(double) * std::max(1LL, p->n_dof))) ||
                           (rc = p->pipe_R.alloc(sizeof(double) * std::max(1LL, p->n_dof))) ||
