@@ -213,6 +213,20 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs_host, double *R_ho
 /* The same with HOST buffers: copies in, assembles, copies out, synchronises. */
 int fe_assemble_host(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags);
 
+/*
+ * Device sparse kernels of the Newton linear solve (the reference solves on
+ * the host with SuperLU, pyoomph/solvers/scipy.py, src/pybind/solver.cpp:105;
+ * no counterpart on its assembly path).  DEVICE pointers: CSR rowptr/colidx
+ * (the problem's resident pattern, fe_problem_pattern_device), values in
+ * FE_JAC_F64 / FE_JAC_F32, FP64 vectors of length n.
+ *   fe_csr_spmv:     y = A x
+ *   fe_csr_diagonal: diag[i] = A(i, i)
+ */
+int fe_csr_spmv(const int32_t *rowptr, const int32_t *colidx, const void *vals, int val_precision, const double *x,
+                double *y, int64_t n, void *stream);
+int fe_csr_diagonal(const int32_t *rowptr, const int32_t *colidx, const void *vals, int val_precision, double *diag,
+                    int64_t n, void *stream);
+
 /* max |R| over n entries of a device vector, NaN -> +inf; result to host. */
 int fe_residual_max(fe_problem_t *p, const double *R, int64_t n, double *out, void *stream);
 

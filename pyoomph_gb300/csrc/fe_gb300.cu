@@ -176,6 +176,35 @@ __global__ void k_dof_update(double *__restrict__ x, const double *__restrict__ 
     x[i] -= dx[i];
 }
 
+// y = A x for a CSR matrix (FP64 or FP32 values, FP64 vectors): one warp
+// per row, lanes stride the row, a fixed shuffle tree sums them
+// (deterministic).  The Krylov solver of the device Newton path calls it.
+template <typename T>
+__global__ void k_csr_spmv(const int *__restrict__ rowptr, const int *__restrict__ colidx, const T *__restrict__ vals,
+                           const double *__restrict__ x, double *__restrict__ y, long long n) {
+  const int lane = threadIdx.x & 31;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += nw) {
+    double acc = 0.0;
+    const int e = rowptr[r + 1];
+    for (int k = rowptr[r] + lane; k < e; k += 32) acc += (double)vals[k] * x[colidx[k]];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[r] = acc;
+  }
+}
+
+template <typename T>
+__global__ void k_csr_diagonal(const int *__restrict__ rowptr, const int *__restrict__ colidx,
+                               const T *__restrict__ vals, double *__restrict__ diag, long long n) {
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
+    double v = 0.0;
+    for (int k = rowptr[r]; k < rowptr[r + 1]; k++)
+      if (colidx[k] == r) v += (double)vals[k];
+    diag[r] = v;
+  }
+}
+
 int grid_for(long long n, int threads, int sms) {
   long long g = (n + threads - 1) / threads;
   long long cap = (long long)sms * 16;
@@ -1307,6 +1336,33 @@ int fe_residual_max_noalloc(const double *R, int64_t n, double *out, void *strea
 }
 
 int64_t fe_residual_max_noalloc_limit(void) { return (int64_t)FE_NOALLOC_MAX_N; }
+
+int fe_csr_spmv(const int32_t *rowptr, const int32_t *colidx, const void *vals, int val_precision, const double *x,
+                double *y, int64_t n, void *stream) {
+  if (n <= 0) return FE_OK;
+  if (!rowptr || !colidx || !vals || !x || !y) return fail(FE_ERR_ARG, "fe_csr_spmv: null argument");
+  const int sms = sm_count_cached();
+  const int g = grid_for(n * 32, 256, sms);
+  if (val_precision == FE_JAC_F64)
+    k_csr_spmv<double><<<g, 256, 0, (cudaStream_t)stream>>>(rowptr, colidx, (const double *)vals, x, y, n);
+  else
+    k_csr_spmv<float><<<g, 256, 0, (cudaStream_t)stream>>>(rowptr, colidx, (const float *)vals, x, y, n);
+  CUDA_TRY(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_csr_diagonal(const int32_t *rowptr, const int32_t *colidx, const void *vals, int val_precision, double *diag,
+                    int64_t n, void *stream) {
+  if (n <= 0) return FE_OK;
+  if (!rowptr || !colidx || !vals || !diag) return fail(FE_ERR_ARG, "fe_csr_diagonal: null argument");
+  const int g = grid_for(n, 256, sm_count_cached());
+  if (val_precision == FE_JAC_F64)
+    k_csr_diagonal<double><<<g, 256, 0, (cudaStream_t)stream>>>(rowptr, colidx, (const double *)vals, diag, n);
+  else
+    k_csr_diagonal<float><<<g, 256, 0, (cudaStream_t)stream>>>(rowptr, colidx, (const float *)vals, diag, n);
+  CUDA_TRY(cudaGetLastError());
+  return FE_OK;
+}
 
 int fe_dof_update(fe_problem_t *p, double *x, const double *dx, int64_t n, void *stream) {
   if (!p || (n > 0 && (!x || !dx))) return fail(FE_ERR_ARG, "null argument");

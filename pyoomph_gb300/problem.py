@@ -108,6 +108,9 @@ class Problem:
         self.linear_solver: Optional[Callable] = None
         # compile the element code with device-side bounds checks (status word 2)
         self.bounds_check = False
+        # linear_solver = "bicgstab": J dx = R solved on the device (linsolve.py)
+        # to this relative tolerance; None: SuperLU on the host (the reference's default)
+        self.linear_solver_tolerance = 1e-13
         self.verbose = False
         self._initialised = False
         self.newton_history: List[float] = []
@@ -520,7 +523,7 @@ class Problem:
         rp, ci = self._pattern_cache
         vals = self.J_dev[:self.nnz].cpu().numpy().astype(np.float64)
         A = sp.csr_matrix((vals, ci, rp), shape=(self.n_dof, self.n_dof))
-        if self.linear_solver is not None:
+        if callable(self.linear_solver):
             return self.linear_solver(A, R)
         return spla.splu(A.tocsc()).solve(R)
 
@@ -543,15 +546,23 @@ class Problem:
             if hist[-1] > self.max_residuals:
                 raise NewtonSolverError(f"max residuals ({self.max_residuals}) exceeded: {hist}")
             ta = time.perf_counter()
+            device_solve = self.linear_solver == "bicgstab"
             with nvtx_range("fe_assemble R+J"):
                 self.assemble_device(with_jacobian=True)
                 self.check()
-                R = self.R_dev[:self.n_dof].cpu().numpy()
+                R = None if device_solve else self.R_dev[:self.n_dof].cpu().numpy()
             tb = time.perf_counter()
             with nvtx_range("linear solve"):
-                dx = self._solve_linear(R)
+                if device_solve:
+                    from .linsolve import DeviceCSR, bicgstab
+                    dxd, its = bicgstab(DeviceCSR.of_problem(self), self.R_dev[:self.n_dof],
+                                        tol=self.linear_solver_tolerance)
+                    self.timings["krylov_iterations"] = self.timings.get("krylov_iterations", 0) + its
+                else:
+                    dx = self._solve_linear(R)
             tc = time.perf_counter()
-            dxd = torch.as_tensor(dx, device=self.x_dev.device)
+            if not device_solve:
+                dxd = torch.as_tensor(dx, device=self.x_dev.device)
             N.check(N.load().fe_dof_update(self._h, self.x_dev.data_ptr(), dxd.data_ptr(), self.n_dof,
                                            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
             self.assemble_device(with_jacobian=False)
