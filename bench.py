@@ -377,6 +377,24 @@ def run_gb300(args):
                                      "h2d_bytes_per_step": r32["h2d"], "d2h_bytes_per_step": r32["d2h"]},
                              "cuda_graph_ms_per_step": r32["ms_graph"],
                              "elems_per_block": r32["P"].kernel.epb}
+    if args.workload in ("hex", "poisson") and world == 1:
+        # a whole Newton solve on the device (assembly + BiCGStab on the resident
+        # Jacobian), from the zero initial guess to max |R| < 1e-10
+        for prec in ("fp64", "fp32"):
+            PN = make_problem(args.workload, args.size, prec)
+            PN.set_dofs(np.zeros(PN.n_dof))
+            PN.linear_solver = "bicgstab"
+            PN.newton_solver_tolerance = 1e-10
+            PN.max_newton_iterations = 20
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            hist = PN.solve()
+            torch.cuda.synchronize()
+            line.setdefault("newton_device_solve", {})[prec] = {
+                "s": time.perf_counter() - t0, "n_dof": PN.n_dof, "newton_iterations": len(hist) - 1,
+                "krylov_iterations": PN.timings.get("krylov_iterations"), "residuals": hist,
+                "linear_solver": "BiCGStab + Jacobi on the device (fe_csr_spmv)"}
+            del PN
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, threads=1)
     if rank == 0:
