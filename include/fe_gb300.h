@@ -54,8 +54,13 @@ enum {
   /* fused (moving-mesh) code only, each in a call of its own: */
   FE_ASSEMBLE_MASS = 8,   /* J_vals receives the mass matrix dR/d(du/dt) (flag 2 of the
                              generated ResidualAndJacobian, jitbridge.h:285) */
-  FE_ASSEMBLE_DPARAM = 16 /* R receives dR/dp for the parameter of fe_problem_set_dparam
+  FE_ASSEMBLE_DPARAM = 16, /* R receives dR/dp for the parameter of fe_problem_set_dparam
                              (dResidual{i}dParameter_{k}, codegen.cpp:4743-4760) */
+  /* fixed-mesh code only, in a call of its own: */
+  FE_ASSEMBLE_HVP = 32     /* J_vals receives the Hessian-vector product
+                              H(y)_ij = sum_k d2R_i/du_j du_k y_k for the direction of
+                              fe_problem_set_direction (HessianVectorProduct{i},
+                              jitbridge.h:286, codegen.cpp:3646) */
 };
 
 /* Jacobian value precision */
@@ -164,6 +169,9 @@ int fe_problem_set_history(fe_problem_t *p, int level, const double *values_host
 int fe_problem_shift_history(fe_problem_t *p);
 /* Overwrite the nodal positions (moving meshes keep them as dofs). */
 int fe_problem_set_positions(fe_problem_t *p, const double *x_host);
+
+/* Direction y (DEVICE dof vector, n_dof) of FE_ASSEMBLE_HVP assemblies. */
+int fe_problem_set_direction(fe_problem_t *p, const double *y, void *stream);
 
 /* Parameter of the next FE_ASSEMBLE_DPARAM assembly (index into params). */
 int fe_problem_set_dparam(fe_problem_t *p, int index);

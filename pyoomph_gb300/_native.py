@@ -13,7 +13,7 @@ from . import build as _build
 
 FE_OK, FE_ERR_ARG, FE_ERR_CUDA, FE_ERR_COMPILE, FE_ERR_NOMEM, FE_ERR_STATE, FE_ERR_DEVICE, FE_ERR_NOGPU = range(8)
 FE_ASSEMBLE_RESIDUAL, FE_ASSEMBLE_JACOBIAN, FE_ASSEMBLE_VALUES_FROM_DOFS = 1, 2, 4
-FE_ASSEMBLE_MASS, FE_ASSEMBLE_DPARAM = 8, 16
+FE_ASSEMBLE_MASS, FE_ASSEMBLE_DPARAM, FE_ASSEMBLE_HVP = 8, 16, 32
 FE_JAC_F64, FE_JAC_F32 = 0, 1
 
 INCLUDE_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc")
@@ -30,7 +30,7 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_residual_max_noalloc", "fe_residual_max_noalloc_limit", "fe_problem_element_buffers",
            "fe_problem_set_history", "fe_problem_shift_history", "fe_problem_set_positions",
            "fe_problem_graph_capture", "fe_problem_graph_launch", "fe_problem_set_dparam",
-           "fe_assemble_pipelined", "fe_csr_spmv", "fe_csr_diagonal"]
+           "fe_assemble_pipelined", "fe_csr_spmv", "fe_csr_diagonal", "fe_problem_set_direction"]
 
 
 def _header_stamp() -> str:
@@ -147,6 +147,7 @@ def load(build_if_missing: bool = True):
         L.fe_assemble_pipelined.argtypes = [vp, vp, vp, vp, c_int, c_int, vp]
         L.fe_csr_spmv.argtypes = [vp, vp, vp, c_int, vp, vp, i64, vp]
         L.fe_csr_diagonal.argtypes = [vp, vp, vp, c_int, vp, i64, vp]
+        L.fe_problem_set_direction.argtypes = [vp, vp, vp]
         L.fe_residual_max_noalloc_limit.restype = i64
         _lib = L
         return L

@@ -199,6 +199,25 @@ def pointwise_source(pw: Pointwise, jreal: str = "double") -> str:
     else:
         lines += _emit(list(pw.r_exprs), names, False, [f"r[{k}]" for k in range(nr)], "  ")
     lines.append("}")
+    # Hessian-vector product: D'(U; V) = sum_c dD/dU_c V_c, V the interpolated direction
+    nc = 1 + pw.dim
+    usyms, vsyms = [], []
+    for f, (name, _) in enumerate(pw.fields):
+        usyms += [E.REG.value[name]] + list(E.REG.grad[name][:pw.dim])
+        vsyms += [sp.Symbol(f"V_{f}_{c}", real=True) for c in range(nc)]
+    hnames = dict(names)
+    for k, v in enumerate(vsyms):
+        hnames[v] = f"V[{k}]"
+    hexprs = [sum((sp.diff(d, u) * v for u, v in zip(usyms, vsyms)), sp.Integer(0)) for (_, _, d) in pw.d_entries]
+    lines.append("__device__ __forceinline__ void fe_pointwise_hvp(const double* __restrict__ U, "
+                 "const double* __restrict__ V, const double* __restrict__ Xq, const double* __restrict__ P, "
+                 "jreal* __restrict__ D) {")
+    lines.append("  (void)U; (void)V; (void)Xq; (void)P;")
+    if nd:
+        hl = _emit(hexprs, hnames, False, [f"D[{k}]" for k in range(nd)], "  ")
+        lines += [l.replace("] = ", "] = (jreal)(", 1) + ")" if l.strip().startswith("D[") else l for l in hl]
+        lines = [l[:-2] + ");" if l.strip().startswith("D[") and l.endswith(";)") else l for l in lines]
+    lines.append("}")
     if jreal != "double":
         fl = _symbol_names(pw, prefix="f")
         lines.append("__device__ __forceinline__ void fe_pointwise_jac(const double* __restrict__ U, "
@@ -289,7 +308,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     table_doubles = nq + nq * nn + nq * nn * dim + nq * nn1 + nq * nn1 * dim
     table_bytes = table_doubles * 8
     geo_doubles = (dim * dim + 1) if affine else 0
-    per_elem = ((nn * dim + nn * nval + nq * ntc + geo_doubles) * 8
+    per_elem = ((nn * dim + 2 * nn * nval + nq * ntc + geo_doubles) * 8
                 + (nq * ndnz + nq * nn * dim + (nq * nn1 * dim if has_c1 else 0)) * jbytes)
     if epb is None:
         epb, threads = _launch_shape(et, nloc, per_elem, table_bytes)
@@ -327,7 +346,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("  double* sDps1 = sPsi1 + FE_NQ * FE_NN1;")
     w("  double* sX = sDps1 + FE_NQ * FE_NN1 * FE_DIM;")
     w("  double* sU = sX + FE_EPB * FE_NN * FE_DIM;")
-    w("  double* sRh = sU + FE_EPB * FE_NN * FE_NVAL;")
+    w("  double* sY = sU + FE_EPB * FE_NN * FE_NVAL;  // direction of the Hessian-vector product (flag 4)")
+    w("  double* sRh = sY + FE_EPB * FE_NN * FE_NVAL;")
     w("  double* sG = sRh + FE_EPB * FE_NQ * FE_NTC;")
     w(f"  jreal* sD = reinterpret_cast<jreal*>(sG + FE_EPB * {geo_doubles});")
     w("  jreal* sDx2 = sD + FE_EPB * FE_NQ * FE_NDNZ;")
@@ -346,6 +366,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    for (int d = 0; d < FE_DIM; ++d) sX[k * FE_DIM + d] = a.x[(long long)node * FE_DIM + d];")
     w("    #pragma unroll")
     w("    for (int v = 0; v < FE_NVAL; ++v) sU[k * FE_NVAL + v] = a.values[(long long)node * a.nval + v];")
+    w("    if (flag == 4)")
+    w("      for (int v = 0; v < FE_NVAL; ++v) sY[k * FE_NVAL + v] = a.dir[(long long)node * a.nval + v];")
     w("  }")
     w("  __syncthreads();")
     if affine:
@@ -393,36 +415,39 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w("      #pragma unroll")
             w("      for (int i = 0; i < FE_DIM; ++i) Xq[i] += X[l * FE_DIM + i] * ps;")
             w("    }")
-    w("    double U[FE_NTC];")
-    for f, (fname, fsp) in enumerate(fields):
-        base = f * nc
-        zeros = ", ".join(["0.0"] * dim)
-        w(f"    {{ double v = 0.0, gs[FE_DIM] = {{{zeros}}};")
-        if fsp == "C2":
-            w("      #pragma unroll")
-            w("      for (int l = 0; l < FE_NN; ++l) {")
-            w(f"        const double u = sU[(el * FE_NN + l) * FE_NVAL + {f}];")
-            w("        v += u * sPsi2[q * FE_NN + l];")
-            w("        #pragma unroll")
-            w("        for (int b = 0; b < FE_DIM; ++b) gs[b] += u * dps[l * FE_DIM + b];")
-            w("      }")
-        else:
-            # C1 nodes by literal element slot (no constant-memory index in the loop)
-            w("      const double* ps1 = sPsi1 + q * FE_NN1;")
-            w("      const double* dp1 = sDps1 + q * FE_NN1 * FE_DIM;")
-            for l, node in enumerate(et.c1_index):
-                w(f"      {{ const double u = sU[(el * FE_NN + {node}) * FE_NVAL + {f}];")
-                w(f"        v += u * ps1[{l}];")
-                for b in range(dim):
-                    w(f"        gs[{b}] += u * dp1[{l * dim + b}];")
-                w("      }")
-        w(f"      U[{base}] = v;")
-        w("      #pragma unroll")
-        w("      for (int i = 0; i < FE_DIM; ++i) { double s = 0.0;")
-        w("        #pragma unroll")
-        w("        for (int b = 0; b < FE_DIM; ++b) s += g[b][i] * gs[b];")
-        w(f"        U[{base} + 1 + i] = s; }}")
-        w("    }")
+    def interp(dst, src, ind):
+        w(f"{ind}double {dst}[FE_NTC];")
+        for f, (fname, fsp) in enumerate(fields):
+            base = f * nc
+            zeros = ", ".join(["0.0"] * dim)
+            w(f"{ind}{{ double v = 0.0, gs[FE_DIM] = {{{zeros}}};")
+            if fsp == "C2":
+                w(f"{ind}  #pragma unroll")
+                w(f"{ind}  for (int l = 0; l < FE_NN; ++l) {{")
+                w(f"{ind}    const double u = {src}[(el * FE_NN + l) * FE_NVAL + {f}];")
+                w(f"{ind}    v += u * sPsi2[q * FE_NN + l];")
+                w(f"{ind}    #pragma unroll")
+                w(f"{ind}    for (int b = 0; b < FE_DIM; ++b) gs[b] += u * dps[l * FE_DIM + b];")
+                w(f"{ind}  }}")
+            else:
+                # C1 nodes by literal element slot (no constant-memory index in the loop)
+                w(f"{ind}  const double* ps1 = sPsi1 + q * FE_NN1;")
+                w(f"{ind}  const double* dp1 = sDps1 + q * FE_NN1 * FE_DIM;")
+                for l, node in enumerate(et.c1_index):
+                    w(f"{ind}  {{ const double u = {src}[(el * FE_NN + {node}) * FE_NVAL + {f}];")
+                    w(f"{ind}    v += u * ps1[{l}];")
+                    for b in range(dim):
+                        w(f"{ind}    gs[{b}] += u * dp1[{l * dim + b}];")
+                    w(f"{ind}  }}")
+            w(f"{ind}  {dst}[{base}] = v;")
+            w(f"{ind}  #pragma unroll")
+            w(f"{ind}  for (int i = 0; i < FE_DIM; ++i) {{ double s = 0.0;")
+            w(f"{ind}    #pragma unroll")
+            w(f"{ind}    for (int b = 0; b < FE_DIM; ++b) s += g[b][i] * gs[b];")
+            w(f"{ind}    {dst}[{base} + 1 + i] = s; }}")
+            w(f"{ind}}}")
+
+    interp("U", "sU", "    ")
     w("    const double* Pe = a.params + (a.replica_elems > 0 ? ((e0 + el) / a.replica_elems) * a.params_stride : 0);")
     w("    double r[FE_NTC]; jreal D[FE_NDNZ];")
     w("    fe_pointwise(U, Xq, Pe, r, D, flag);")
@@ -438,7 +463,11 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    }")
     w("    if (flag) {")
     if jreal == "float":
-        w("      fe_pointwise_jac(U, Xq, Pe, D);")
+        w("      if (flag != 4) fe_pointwise_jac(U, Xq, Pe, D);")
+    w("      if (flag == 4) {")
+    interp("V", "sY", "        ")
+    w("        fe_pointwise_hvp(U, V, Xq, Pe, D);")
+    w("      }")
     w("      jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZ;")
     w("      const jreal wj = (jreal)wq;")
     w("      #pragma unroll")

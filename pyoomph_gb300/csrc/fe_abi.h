@@ -25,6 +25,7 @@ struct FeElemArgs {
   long long hist_stride;    // entries per history level (n_nodes * nval)
   int aux;                  // flag 3: index of the parameter of dR/dp
   long long n_nodes;        // nodes of the problem (bounds of conn entries)
+  const double *dir;        // flag 4: nodal values of the direction y of the Hessian-vector product
 };
 
 // One launch over several domains (bulk, interface, contact line ...): block

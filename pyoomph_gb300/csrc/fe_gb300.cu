@@ -284,7 +284,7 @@ struct fe_problem {
   long long n_nodes = 0, n_dof = 0, nnz = 0;
   int n_params = 0, params_stride = 0, n_hist = 0, fused = 0, dparam = 0;
   std::vector<Domain> domains;
-  DevBuf x, values, eqn, params, status, hist, x0;
+  DevBuf x, values, eqn, params, status, hist, x0, dir;
   DevBuf rowptr, colidx, cptr, cidx, rptr, ridx;
   DevBuf partial;
   // the domain buffers are one allocation per kind, addressed by offsets:
@@ -585,6 +585,7 @@ FeElemArgs domain_args(fe_problem *p, Domain &d, int flag) {
   a.hist_stride = (long long)p->n_nodes * p->nval;
   a.aux = p->dparam;
   a.n_nodes = p->n_nodes;
+  a.dir = p->dir.p ? p->dir.as<double>() : p->values.as<double>();
   return a;
 }
 
@@ -999,13 +1000,18 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
   if (!p) return fail(FE_ERR_ARG, "null problem");
   cudaStream_t st = (cudaStream_t)stream;
   const bool want_m = flags & FE_ASSEMBLE_MASS, want_p = flags & FE_ASSEMBLE_DPARAM;
-  const bool want_r = (flags & FE_ASSEMBLE_RESIDUAL) || want_p, want_j = (flags & FE_ASSEMBLE_JACOBIAN) || want_m;
+  const bool want_h = flags & FE_ASSEMBLE_HVP;
+  const bool want_r = (flags & FE_ASSEMBLE_RESIDUAL) || want_p;
+  const bool want_j = (flags & FE_ASSEMBLE_JACOBIAN) || want_m || want_h;
+  if (want_h && (p->fused || !p->dir.p || (flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS | FE_ASSEMBLE_DPARAM))))
+    return fail(FE_ERR_ARG, "fe_assemble: the Hessian-vector product needs fixed-mesh code, a direction "
+                            "(fe_problem_set_direction) and a call of its own");
   if ((want_r && !R) || (want_j && !J_vals)) return fail(FE_ERR_ARG, "fe_assemble: missing output");
   if ((want_m || want_p) && !p->fused)
     return fail(FE_ERR_ARG, "fe_assemble: mass matrices and parameter derivatives need fused (moving-mesh) code");
   if ((want_m && (flags & FE_ASSEMBLE_JACOBIAN)) || (want_p && (flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS))))
     return fail(FE_ERR_ARG, "fe_assemble: Jacobian, mass matrix and parameter derivative are separate calls");
-  const int eflag = want_p ? 3 : want_m ? 2 : want_j ? 1 : 0;
+  const int eflag = want_h ? 4 : want_p ? 3 : want_m ? 2 : want_j ? 1 : 0;
   const int sms = sm_count_cached();
   std::vector<cudaEvent_t> ev;
   if (p->timing) {
@@ -1241,6 +1247,18 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
   return FE_OK;
 }
 
+int fe_problem_set_direction(fe_problem_t *p, const double *y, void *stream) {
+  if (!p || (!y && p->n_dof > 0)) return fail(FE_ERR_ARG, "null argument");
+  int rc;
+  const long long n = p->n_nodes * p->nval;
+  if (!p->dir.p && (rc = p->dir.alloc(sizeof(double) * std::max(1LL, n)))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(cudaMemsetAsync(p->dir.p, 0, sizeof(double) * n, st)); // pinned values: zero direction
+  k_scatter_dofs<<<grid_for(n, 256, sm_count_cached()), 256, 0, st>>>(y, p->eqn.as<int>(), p->dir.as<double>(), n);
+  CUDA_TRY(cudaGetLastError());
+  return FE_OK;
+}
+
 int fe_problem_set_dparam(fe_problem_t *p, int index) {
   if (!p || index < 0 || index >= std::max(1, p->n_params)) return fail(FE_ERR_ARG, "bad parameter index");
   p->dparam = index;
@@ -1407,7 +1425,7 @@ int fe_problem_launch_count(const fe_problem_t *p, int flags) {
       if (d.n_elem) n++;
   }
   if (flags & (FE_ASSEMBLE_RESIDUAL | FE_ASSEMBLE_DPARAM)) n++;
-  if ((flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS)) && p->nnz > 0) n++;
+  if ((flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS | FE_ASSEMBLE_HVP)) && p->nnz > 0) n++;
   return n;
 }
 

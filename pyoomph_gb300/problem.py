@@ -505,6 +505,23 @@ class Problem:
         vals = self.J_dev[:self.nnz].cpu().numpy()
         return R, sp.csr_matrix((vals, ci, rp), shape=(self.n_dof, self.n_dof))
 
+    def get_hessian_vector_product(self, y: np.ndarray):
+        """H(y)_ij = sum_k d2R_i/(du_j du_k) y_k at the current dofs, in the
+        Jacobian's CSR pattern (pyoomph's HessianVectorProduct, used by
+        bifurcation tracking).  Leaves J_dev holding H(y)."""
+        import scipy.sparse as sp
+        torch = _torch()
+        self.initialise()
+        st = torch.cuda.current_stream().cuda_stream
+        yd = torch.as_tensor(np.asarray(y, dtype=np.float64), device=self.x_dev.device)
+        N.check(N.load().fe_problem_set_direction(self._h, yd.data_ptr(), ctypes.c_void_p(st)))
+        N.check(N.load().fe_assemble(self._h, self.x_dev.data_ptr(), self.R_dev.data_ptr(), self.J_dev.data_ptr(),
+                                     N.FE_ASSEMBLE_HVP | N.FE_ASSEMBLE_VALUES_FROM_DOFS, ctypes.c_void_p(st)))
+        self.check()
+        rp, ci = self.pattern()
+        vals = self.J_dev[:self.nnz].cpu().numpy().astype(np.float64)
+        return sp.csr_matrix((vals, ci, rp), shape=(self.n_dof, self.n_dof))
+
     def assemble_jacobian(self):
         """pyoomph's Problem.assemble_jacobian (problem.py:711)."""
         return self.get_jacobian()

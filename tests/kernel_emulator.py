@@ -48,7 +48,7 @@ class _Args(ctypes.Structure):
                 ("jbuf", ctypes.c_void_p), ("n_elem", ctypes.c_longlong), ("nval", ctypes.c_int),
                 ("flag", ctypes.c_int), ("status", ctypes.c_void_p), ("replica_elems", ctypes.c_longlong),
                 ("params_stride", ctypes.c_int), ("hist", ctypes.c_void_p), ("x0", ctypes.c_void_p),
-                ("n_hist", ctypes.c_int), ("hist_stride", ctypes.c_longlong), ("aux", ctypes.c_int), ("n_nodes", ctypes.c_longlong)]
+                ("n_hist", ctypes.c_int), ("hist_stride", ctypes.c_longlong), ("aux", ctypes.c_int), ("n_nodes", ctypes.c_longlong), ("dir", ctypes.c_void_p)]
 
 
 def build(ks) -> ctypes.CDLL:
@@ -74,7 +74,7 @@ def build(ks) -> ctypes.CDLL:
     return L
 
 
-def run(ks, x, conn, values, params, flag: int = 1):
+def run(ks, x, conn, values, params, flag: int = 1, direction=None):
     """Element residuals [E, nloc] and matrices [E, nloc, nloc] of the
     generated kernel ks on the given mesh data (host arrays)."""
     L = build(ks)
@@ -89,9 +89,11 @@ def run(ks, x, conn, values, params, flag: int = 1):
     rbuf = np.zeros((E, nloc))
     jbuf = np.zeros((E, nloc, nloc), dtype=jt)
     status = np.zeros(4, dtype=np.int32)
+    if direction is not None:
+        direction = np.ascontiguousarray(direction, dtype=np.float64)
     a = _Args(x.ctypes.data, conn.ctypes.data, values.ctypes.data, params.ctypes.data, tables.ctypes.data,
               rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data, 0, 0, None, None, 0, 0, 0,
-              x.shape[0])
+              x.shape[0], values.ctypes.data if direction is None else direction.ctypes.data)
     L.fe_emu_run(ctypes.byref(a), (E + ks.epb - 1) // ks.epb)
     return rbuf, jbuf, status
 
@@ -150,7 +152,7 @@ def run_fused(fk, conns, values, hist, x0, params, flag: int = 1, aux: int = 0, 
         fa.d[k] = _Args(x0.ctypes.data, conn.ctypes.data, values.ctypes.data, params.ctypes.data,
                         tables.ctypes.data, rbuf.ctypes.data, jbuf.ctypes.data, E, nval, flag,
                         status.ctypes.data, 0, 0, hist_arr.ctypes.data, x0.ctypes.data, len(hist),
-                        values.size, aux, values.shape[0])
+                        values.size, aux, values.shape[0], values.ctypes.data)
         fa.block_start[k] = nb
         nb += (E + dc.epb - 1) // dc.epb
     fa.block_start[len(fk.domains)] = nb
