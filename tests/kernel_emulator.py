@@ -42,6 +42,16 @@ alignas(16) unsigned char fe_smem[232448];
 """
 
 
+def _headers() -> str:
+    """The device headers the generated code includes (part of the cache key:
+    a changed argument block must rebuild every emulator library)."""
+    out = ""
+    for f in ("fe_abi.h", "fe_device.cuh"):
+        with open(os.path.join(CSRC, f)) as fp:
+            out += fp.read()
+    return out
+
+
 class _Args(ctypes.Structure):
     _fields_ = [("x", ctypes.c_void_p), ("conn", ctypes.c_void_p), ("values", ctypes.c_void_p),
                 ("params", ctypes.c_void_p), ("tables", ctypes.c_void_p), ("rbuf", ctypes.c_void_p),
@@ -59,7 +69,7 @@ def build(ks) -> ctypes.CDLL:
         f'  for (int b = 0; b < nblocks; ++b) {{\n'
         f'    memset(fe_smem, 0xff, sizeof(fe_smem)); /* NaN garbage: uninitialised reads show */\n'
         f'    blockIdx.x = b; {ks.name}(*a); }}\n}}\n')
-    h = hashlib.sha1(body.encode()).hexdigest()[:16]
+    h = hashlib.sha1((body + _headers()).encode()).hexdigest()[:16]
     os.makedirs(OUT, exist_ok=True)
     so = os.path.join(OUT, f"emu_{h}.so")
     if not os.path.exists(so):
@@ -111,7 +121,7 @@ def build_fused(fk, defines=()) -> ctypes.CDLL:
         f'  for (int b = 0; b < nblocks; ++b) {{\n'
         f'    memset(fe_smem, 0xff, sizeof(fe_smem));\n'
         f'    blockIdx.x = b; {fk.name}(*a); }}\n}}\n')
-    h = hashlib.sha1(body.encode()).hexdigest()[:16]
+    h = hashlib.sha1((body + _headers()).encode()).hexdigest()[:16]
     os.makedirs(OUT, exist_ok=True)
     so = os.path.join(OUT, f"emu_{h}.so")
     if not os.path.exists(so):
