@@ -132,6 +132,14 @@ typedef struct fe_problem_desc {
   int n_history;            /* previous time levels of the nodal values kept (BDF) */
   const double *x0;         /* host [n_nodes * dim] Lagrangian positions (NULL: = x) */
   int fused;                /* 1: every domain shares one fused code, run as one launch */
+  /* hanging values (refined meshes; oomph's HangInfo, problem.cc / nodes.h:
+   * a constrained value has no equation and equals sum_m w_m * master_m):
+   * slot = node * nval + value index; masters are slots that do not hang */
+  int64_t n_hang;
+  const int64_t *hang_slot;   /* [n_hang] sorted */
+  const int64_t *hang_ptr;    /* [n_hang + 1] */
+  const int64_t *hang_master; /* [hang_ptr[n_hang]] */
+  const double *hang_weight;  /* [hang_ptr[n_hang]] */
 } fe_problem_desc_t;
 
 /*

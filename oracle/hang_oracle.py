@@ -1,0 +1,172 @@
+"""CPU oracle for assembly on refined meshes with hanging nodes.
+
+TEST INFRASTRUCTURE ONLY.  Imported by tests/ as the checker; never by the
+package ``pyoomph_gb300``.
+
+Restates, independently of the package's lattice-based generator:
+
+* one level of refinement of a Q2 quad mesh (oracle mesh of ``fe_oracle.c``
+  in pyoomph's order): each chosen element is replaced by its four children
+  (SW, SE, NW, NE) whose nodes are placed by the parent's isoparametric map;
+  new nodes are numbered in order of first appearance;
+* hanging nodes found geometrically: a child node strictly inside an edge of
+  an unrefined element takes the values interpolated along that edge by the
+  1D quadratic shapes (oomph's ``RefineableQElement<2>::setup_hang_for_value``),
+  and its values are constrained (no equation; ``Node::assign_eqn_numbers``,
+  ``nodes.cc:534-561``);
+* the element residuals/Jacobians of ``fe_oracle.c`` with the hanging values
+  interpolated, assembled with oomph's hanging-node rule (each local equation
+  of a hanging value adds, weighted, to its masters' equations, rows and
+  columns alike; ``jitbridge_hang.h`` master loops) in the vectors-of-pairs
+  order (element, local row, row master, local column, column master).
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Dict, List, Tuple
+
+import numpy as np
+
+import oracle as O
+
+
+def refine(m: O.Mesh, chosen) -> Tuple[np.ndarray, np.ndarray, Dict[int, List[Tuple[int, float]]], np.ndarray]:
+    """(x, conn, hang, on_boundary) of the refined mesh; ``chosen(cx, cy)``
+    selects the elements to split."""
+    L = O.lib()
+    x = [p for p in m.x]
+    conn: List[List[int]] = []
+    refined = []
+    for e in range(m.conn.shape[0]):
+        c = m.conn[e]
+        cx, cy = m.x[c[4]]
+        refined.append(bool(chosen(cx, cy)))
+    lookup: Dict[Tuple[float, float], int] = {(round(p[0], 12), round(p[1], 12)): k for k, p in enumerate(m.x)}
+    for e in range(m.conn.shape[0]):
+        c = m.conn[e]
+        if not refined[e]:
+            conn.append(list(c))
+            continue
+        Xe = m.x[c]
+        for (sx0, sy0) in ((-1.0, -1.0), (0.0, -1.0), (-1.0, 0.0), (0.0, 0.0)):
+            child = []
+            for j in range(3):
+                for i in range(3):
+                    s = np.array([sx0 + 0.5 * i, sy0 + 0.5 * j, 0.0])
+                    psi = np.zeros(9)
+                    dps = np.zeros((9, 2))
+                    L.ofe_shape_c2(O.Q2_QUAD, O._ptr(s), O._ptr(psi), O._ptr(dps))
+                    p = psi @ Xe
+                    k = lookup.get((round(p[0], 12), round(p[1], 12)))
+                    if k is None:
+                        k = len(x)
+                        x.append(p)
+                        lookup[(round(p[0], 12), round(p[1], 12))] = k
+                    child.append(k)
+            conn.append(child)
+    x = np.array(x)
+    conn = np.array(conn, dtype=np.int32)
+    # edges of the unrefined elements: (a, mid, b) node triples
+    edges = []
+    for e in range(m.conn.shape[0]):
+        if refined[e]:
+            continue
+        c = m.conn[e]
+        for a, mid, b in ((0, 1, 2), (6, 7, 8), (0, 3, 6), (2, 5, 8)):
+            edges.append((c[a], c[mid], c[b]))
+    hang: Dict[int, List[Tuple[int, float]]] = {}
+    child_nodes = set(conn[[k for k in range(conn.shape[0])]].ravel().tolist())
+    for k in sorted(child_nodes):
+        for a, mid, b in edges:
+            if k in (a, mid, b):
+                continue
+            pa, pb = x[a], x[b]
+            t = pb - pa
+            u = np.dot(x[k] - pa, t) / np.dot(t, t)
+            if 0.0 < u < 1.0 and np.linalg.norm(pa + u * t - x[k]) < 1e-12:
+                # the local coordinate along the edge on the refinement grid
+                # (exact in binary, as a quadtree's son coordinates are)
+                s = np.round((2.0 * u - 1.0) * 1024.0) / 1024.0
+                w = (0.5 * s * (s - 1.0), 1.0 - s * s, 0.5 * s * (s + 1.0))
+                hang[k] = [(a, w[0]), (mid, w[1]), (b, w[2])]
+                break
+    lo, hi = x.min(axis=0), x.max(axis=0)
+    on_b = (np.abs(x[:, 0] - lo[0]) < 1e-12) | (np.abs(x[:, 0] - hi[0]) < 1e-12) | \
+           (np.abs(x[:, 1] - lo[1]) < 1e-12) | (np.abs(x[:, 1] - hi[1]) < 1e-12)
+    return x, conn, hang, on_b
+
+
+class HangProblem:
+    """Scalar Q2 problem (Poisson / nonlinear diffusion) on a refined mesh,
+    u = 0 on the outer boundary."""
+
+    def __init__(self, N: int, chosen, gaussians: np.ndarray, eq: int = O.EQ_POISSON):
+        self.x, self.conn, self.hang, on_b = refine(O.mesh(O.Q2_QUAD, N, N), chosen)
+        n = self.x.shape[0]
+        self.eq = eq
+        self.params = O.gaussian_params(gaussians)
+        self.values = np.zeros(n)
+        self.eqn = np.full(n, -1, dtype=np.int64)
+        k = 0
+        for i in range(n):
+            if not on_b[i] and i not in self.hang:
+                self.eqn[i] = k
+                k += 1
+        self.n_dof = k
+
+    def dofs(self) -> np.ndarray:
+        m = self.eqn >= 0
+        out = np.zeros(self.n_dof)
+        out[self.eqn[m]] = self.values[m]
+        return out
+
+    def set_dofs(self, d: np.ndarray) -> None:
+        m = self.eqn >= 0
+        self.values[m] = d[self.eqn[m]]
+        for h, ms in self.hang.items():
+            self.values[h] = sum(w * self.values[mm] for mm, w in ms)
+
+    def expand(self, node: int) -> List[Tuple[int, float]]:
+        if node in self.hang:
+            return [(int(self.eqn[mm]), w) for mm, w in self.hang[node] if self.eqn[mm] >= 0]
+        return [(int(self.eqn[node]), 1.0)] if self.eqn[node] >= 0 else []
+
+    def assemble(self):
+        L = O.lib()
+        R = np.zeros(self.n_dof)
+        rows: List[Dict[int, float]] = [dict() for _ in range(self.n_dof)]
+        isv = np.zeros(self.x.shape[0], dtype=np.uint8)
+        vals = np.ascontiguousarray(self.values.reshape(-1, 1))
+        Re = np.zeros(9)
+        Je = np.zeros(81)
+        xx = np.ascontiguousarray(self.x)
+        for e in range(self.conn.shape[0]):
+            c = np.ascontiguousarray(self.conn[e])
+            L.ofe_element_res_jac(O.Q2_QUAD, self.eq, 2, O._ptr(xx), O._ptr(c), 1, O._ptr(vals), O._ptr(isv),
+                                  O._ptr(self.params), len(self.params), O._ptr(Re), O._ptr(Je))
+            J = Je.reshape(9, 9)
+            exp = [self.expand(int(n)) for n in c]
+            for i in range(9):
+                for (r, wr) in exp[i]:
+                    R[r] += wr * Re[i]
+                    row = rows[r]
+                    for j in range(9):
+                        for (cc, wc) in exp[j]:
+                            row[cc] = row.get(cc, 0.0) + wr * wc * J[i, j]
+        rp = np.zeros(self.n_dof + 1, dtype=np.int64)
+        for i, row in enumerate(rows):
+            rp[i + 1] = rp[i] + len(row)
+        ci = np.fromiter((k for row in rows for k in row), dtype=np.int64, count=int(rp[-1]))
+        v = np.fromiter((val for row in rows for val in row.values()), dtype=np.float64, count=int(rp[-1]))
+        return R, rp, ci, v
+
+    def newton(self, tol: float = 1e-11, max_iter: int = 20) -> np.ndarray:
+        import scipy.sparse as sps
+        import scipy.sparse.linalg as spla
+        for _ in range(max_iter):
+            R, rp, ci, v = self.assemble()
+            if np.max(np.abs(R)) < tol:
+                return self.dofs()
+            A = sps.csr_matrix((v, ci, rp), shape=(self.n_dof, self.n_dof))
+            self.set_dofs(self.dofs() - spla.splu(A.tocsc()).solve(R))
+        raise RuntimeError("oracle Newton did not converge")

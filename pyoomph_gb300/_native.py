@@ -86,6 +86,11 @@ class ProblemDesc(ctypes.Structure):
         ("n_history", ctypes.c_int),
         ("x0", ctypes.c_void_p),
         ("fused", ctypes.c_int),
+        ("n_hang", ctypes.c_int64),
+        ("hang_slot", ctypes.c_void_p),
+        ("hang_ptr", ctypes.c_void_p),
+        ("hang_master", ctypes.c_void_p),
+        ("hang_weight", ctypes.c_void_p),
     ]
 
 

@@ -151,6 +151,44 @@ __global__ void k_gather_rows(const long long *__restrict__ rptr, const unsigned
   }
 }
 
+// hanging values: values[slot] = sum_m w_m values[master_m]
+__global__ void k_hang_interp(const long long *__restrict__ slot, const long long *__restrict__ ptr,
+                              const long long *__restrict__ master, const double *__restrict__ w,
+                              double *__restrict__ values, long long n) {
+  for (long long h = blockIdx.x * (long long)blockDim.x + threadIdx.x; h < n; h += (long long)gridDim.x * blockDim.x) {
+    double v = 0.0;
+    for (long long m = ptr[h]; m < ptr[h + 1]; m++) v += w[m] * values[master[m]];
+    values[slot[h]] = v;
+  }
+}
+
+// weighted scatter (meshes with hanging values): the same fixed order, each
+// contribution times its weight
+template <typename T>
+__global__ void k_gather_slots_w(const long long *__restrict__ cptr, const unsigned *__restrict__ cidx,
+                                 const double *__restrict__ cw, const T *__restrict__ jbuf, T *__restrict__ out,
+                                 long long nnz) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nnz;
+       s += (long long)gridDim.x * blockDim.x) {
+    const long long b = cptr[s], e = cptr[s + 1];
+    T acc = (T)0;
+    for (long long k = b; k < e; k++) acc += (T)cw[k] * jbuf[cidx[k]];
+    out[s] = acc;
+  }
+}
+
+__global__ void k_gather_rows_w(const long long *__restrict__ rptr, const unsigned *__restrict__ ridx,
+                                const double *__restrict__ rw, const double *__restrict__ rbuf, double *__restrict__ R,
+                                long long n) {
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;
+       r += (long long)gridDim.x * blockDim.x) {
+    const long long b = rptr[r], e = rptr[r + 1];
+    double acc = 0.0;
+    for (long long k = b; k < e; k++) acc += rw[k] * rbuf[ridx[k]];
+    R[r] = acc;
+  }
+}
+
 // max |R| with NaN -> inf; one block per chunk, then a single finishing block
 __device__ __forceinline__ double absnan(double v) { return (v != v) ? __longlong_as_double(0x7ff0000000000000LL) : fabs(v); }
 
@@ -285,6 +323,8 @@ struct fe_problem {
   int n_params = 0, params_stride = 0, n_hist = 0, fused = 0, dparam = 0;
   std::vector<Domain> domains;
   DevBuf x, values, eqn, params, status, hist, x0, dir;
+  long long n_hang = 0;
+  DevBuf hang_slot, hang_ptr, hang_master, hang_weight, cw, rw; // weighted scatter when n_hang > 0
   DevBuf rowptr, colidx, cptr, cidx, rptr, ridx;
   DevBuf partial;
   // the domain buffers are one allocation per kind, addressed by offsets:
@@ -332,6 +372,7 @@ struct Incident {
   int dom;
   long long e;
   int i;
+  double w; // weight of the row's master (1 without hanging nodes)
 };
 
 // Host description of the element blocks the pattern is built from.
@@ -349,6 +390,19 @@ struct PatternOut {
   std::vector<unsigned> cidx;  // element-matrix entry of each contribution
   std::vector<long long> rptr; // [n_dof+1] per-row residual contributions
   std::vector<unsigned> ridx;
+  std::vector<double> cw, rw;  // contribution weights (hanging nodes), empty if all 1
+};
+
+// Hanging values (oomph's HangInfo, nodes.h; constrained values have no
+// equation): slot = node * nval + value, its masters and weights.
+struct HangMap {
+  std::vector<long long> slot_of;             // sorted hanging slots
+  const int64_t *ptr = nullptr, *master = nullptr;
+  const double *weight = nullptr;
+  long long find(long long slot) const {
+    auto it = std::lower_bound(slot_of.begin(), slot_of.end(), slot);
+    return (it != slot_of.end() && *it == slot) ? (long long)(it - slot_of.begin()) : -1;
+  }
 };
 
 // The CSR pattern of Problem::sparse_assemble_row_or_column_compressed_with_
@@ -363,12 +417,27 @@ struct PatternBuilder {
   int nval;
   const int32_t *eqn;
   const std::vector<PatDomain> *doms;
+  const HangMap *hang = nullptr;
   std::vector<long long> inc_ptr;
   std::vector<Incident> inc;
 
-  int32_t geq(const PatDomain &d, long long e, int k) const {
-    int node = d.conn[e * d.nnode + d.local_node[k]];
-    return eqn[(long long)node * nval + d.local_val[k]];
+  // the equations (and weights) a local value of an element stands for: its
+  // own equation, or the equations of its masters if it hangs
+  template <typename F> void expand(const PatDomain &d, long long e, int k, F &&f) const {
+    const long long node = d.conn[e * d.nnode + d.local_node[k]];
+    const long long slot = node * nval + d.local_val[k];
+    if (hang) {
+      const long long h = hang->find(slot);
+      if (h >= 0) {
+        for (long long m = hang->ptr[h]; m < hang->ptr[h + 1]; m++) {
+          const int32_t c = eqn[hang->master[m]];
+          if (c >= 0) f(c, hang->weight[m]);
+        }
+        return;
+      }
+    }
+    const int32_t c = eqn[slot];
+    if (c >= 0) f(c, 1.0);
   }
 
   void build_incidence() {
@@ -376,10 +445,7 @@ struct PatternBuilder {
     std::vector<long long> cnt(n + 1, 0);
     for (const PatDomain &d : *doms)
       for (long long e = 0; e < d.n_elem; e++)
-        for (int i = 0; i < d.nlocal; i++) {
-          int32_t r = geq(d, e, i);
-          if (r >= 0) cnt[r + 1]++;
-        }
+        for (int i = 0; i < d.nlocal; i++) expand(d, e, i, [&](int32_t r, double) { cnt[r + 1]++; });
     for (long long r = 0; r < n; r++) cnt[r + 1] += cnt[r];
     inc_ptr = cnt;
     inc.resize(cnt[n]);
@@ -387,35 +453,32 @@ struct PatternBuilder {
     for (size_t di = 0; di < doms->size(); di++) {
       const PatDomain &d = (*doms)[di];
       for (long long e = 0; e < d.n_elem; e++)
-        for (int i = 0; i < d.nlocal; i++) {
-          int32_t r = geq(d, e, i);
-          if (r >= 0) inc[pos[r]++] = Incident{(int)di, e, i};
-        }
+        for (int i = 0; i < d.nlocal; i++)
+          expand(d, e, i, [&](int32_t r, double w) { inc[pos[r]++] = Incident{(int)di, e, i, w}; });
     }
   }
 
   void row(long long r, std::vector<int32_t> &marker, std::vector<int32_t> &cols,
            std::vector<long long> &slot_cnt, bool fill, int32_t *colidx_out, long long *cptr_out,
-           unsigned *cidx_out, long long cbase, long long *row_len, long long *row_contrib) const {
+           unsigned *cidx_out, double *cw_out, long long cbase, long long *row_len, long long *row_contrib) const {
     cols.clear();
     slot_cnt.clear();
     long long ncontrib = 0;
     for (long long k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
       const Incident &I = inc[k];
       const PatDomain &d = (*doms)[I.dom];
-      for (int j = 0; j < d.nlocal; j++) {
-        int32_t c = geq(d, I.e, j);
-        if (c < 0) continue;
-        int32_t s = marker[c];
-        if (s < 0) {
-          s = (int32_t)cols.size();
-          marker[c] = s;
-          cols.push_back(c);
-          slot_cnt.push_back(0);
-        }
-        slot_cnt[s]++;
-        ncontrib++;
-      }
+      for (int j = 0; j < d.nlocal; j++)
+        expand(d, I.e, j, [&](int32_t c, double) {
+          int32_t s = marker[c];
+          if (s < 0) {
+            s = (int32_t)cols.size();
+            marker[c] = s;
+            cols.push_back(c);
+            slot_cnt.push_back(0);
+          }
+          slot_cnt[s]++;
+          ncontrib++;
+        });
     }
     *row_len = (long long)cols.size();
     *row_contrib = ncontrib;
@@ -432,11 +495,12 @@ struct PatternBuilder {
         const Incident &I = inc[k];
         const PatDomain &d = (*doms)[I.dom];
         const long long base = d.jbase + (I.e * d.nlocal + I.i) * (long long)d.nlocal;
-        for (int j = 0; j < d.nlocal; j++) {
-          int32_t c = geq(d, I.e, j);
-          if (c < 0) continue;
-          cidx_out[wpos[marker[c]]++] = (unsigned)(base + j);
-        }
+        for (int j = 0; j < d.nlocal; j++)
+          expand(d, I.e, j, [&](int32_t c, double w) {
+            const long long at = wpos[marker[c]]++;
+            cidx_out[at] = (unsigned)(base + j);
+            if (cw_out) cw_out[at] = I.w * w;
+          });
       }
     }
     for (int32_t c : cols) marker[c] = -1;
@@ -444,12 +508,14 @@ struct PatternBuilder {
 };
 
 int build_pattern_host(long long n_dof, int nval, const int32_t *eqn, const std::vector<PatDomain> &doms,
-                       bool with_contributions, PatternOut &out) {
+                       bool with_contributions, PatternOut &out, const HangMap *hang = nullptr) {
   PatternBuilder B;
   B.n_dof = n_dof;
   B.nval = nval;
   B.eqn = eqn;
   B.doms = &doms;
+  B.hang = hang;
+  const bool weighted = hang && !hang->slot_of.empty();
   B.build_incidence();
   const long long n = n_dof;
   unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -466,14 +532,15 @@ int build_pattern_host(long long n_dof, int nval, const int32_t *eqn, const std:
         for (long long r = lo; r < hi; r++) {
           long long rl, rc;
           if (!fill) {
-            B.row(r, marker, cols, slot_cnt, false, nullptr, nullptr, nullptr, 0, &rl, &rc);
+            B.row(r, marker, cols, slot_cnt, false, nullptr, nullptr, nullptr, nullptr, 0, &rl, &rc);
             row_len[r] = rl;
             row_con[r] = rc;
           } else {
             long long o = rp[r];
             B.row(r, marker, cols, slot_cnt, with_contributions, out.colidx.data() + o,
                   with_contributions ? out.cptr.data() + o : nullptr,
-                  with_contributions ? out.cidx.data() : nullptr, cp[r], &rl, &rc);
+                  with_contributions ? out.cidx.data() : nullptr,
+                  (with_contributions && weighted) ? out.cw.data() : nullptr, cp[r], &rl, &rc);
             if (!with_contributions) {
               // columns only: recompute cols for this row
               for (size_t s = 0; s < cols.size(); s++) out.colidx[o + s] = cols[s];
@@ -495,6 +562,7 @@ int build_pattern_host(long long n_dof, int nval, const int32_t *eqn, const std:
   if (with_contributions) {
     out.cptr.assign(nnz + 1, 0);
     out.cidx.assign(cp[n], 0);
+    if (weighted) out.cw.assign(cp[n], 0.0);
   }
   pass(true);
   if (with_contributions) out.cptr[nnz] = cp[n];
@@ -508,11 +576,16 @@ int build_pattern_host(long long n_dof, int nval, const int32_t *eqn, const std:
       const PatDomain &d = doms[I.dom];
       out.ridx[k] = (unsigned)(d.rbase + I.e * d.nlocal + I.i);
     }
+    if (weighted) {
+      out.rw.resize(B.inc.size());
+      for (size_t k = 0; k < B.inc.size(); k++) out.rw[k] = B.inc[k].w;
+    }
   }
   return FE_OK;
 }
 
-int build_pattern(fe_problem *P, const std::vector<const int32_t *> &conn_h, const int32_t *eqn_h) {
+int build_pattern(fe_problem *P, const std::vector<const int32_t *> &conn_h, const int32_t *eqn_h,
+                  const HangMap *hang) {
   std::vector<PatDomain> doms;
   for (size_t di = 0; di < P->domains.size(); di++) {
     const Domain &d = P->domains[di];
@@ -520,8 +593,12 @@ int build_pattern(fe_problem *P, const std::vector<const int32_t *> &conn_h, con
                              d.jbase, d.rbase});
   }
   PatternOut out;
-  int rc = build_pattern_host(P->n_dof, P->nval, eqn_h, doms, true, out);
+  int rc = build_pattern_host(P->n_dof, P->nval, eqn_h, doms, true, out, hang);
   if (rc) return rc;
+  if (!out.cw.empty()) {
+    if ((rc = P->cw.upload(out.cw.data(), sizeof(double) * out.cw.size()))) return rc;
+    if ((rc = P->rw.upload(out.rw.data(), sizeof(double) * out.rw.size()))) return rc;
+  }
   const long long n = P->n_dof;
   const long long nnz = (long long)out.colidx.size();
   P->nnz = nnz;
@@ -533,6 +610,34 @@ int build_pattern(fe_problem *P, const std::vector<const int32_t *> &conn_h, con
   if ((rc = P->cidx.upload(out.cidx.data(), sizeof(unsigned) * out.cidx.size()))) return rc;
   if ((rc = P->rptr.upload(out.rptr.data(), sizeof(long long) * (n + 1)))) return rc;
   if ((rc = P->ridx.upload(out.ridx.data(), sizeof(unsigned) * out.ridx.size()))) return rc;
+  return FE_OK;
+}
+
+// checks the hanging values of a description and indexes them
+int hang_map(const fe_problem_desc_t *desc, HangMap &h) {
+  h.slot_of.clear();
+  if (desc->n_hang <= 0) return FE_OK;
+  if (!desc->hang_slot || !desc->hang_ptr || !desc->hang_master || !desc->hang_weight)
+    return fail(FE_ERR_ARG, "hanging values: null arrays");
+  const long long nslots = desc->n_nodes * desc->nval;
+  h.slot_of.assign(desc->hang_slot, desc->hang_slot + desc->n_hang);
+  for (long long k = 0; k < desc->n_hang; k++) {
+    const long long s = h.slot_of[k];
+    if (s < 0 || s >= nslots || (k > 0 && s <= h.slot_of[k - 1]))
+      return fail(FE_ERR_ARG, "hanging values: slots must be sorted, unique and in range (entry %lld)", k);
+    if (desc->eqn[s] >= 0) return fail(FE_ERR_ARG, "hanging value %lld has an equation number", s);
+    if (desc->hang_ptr[k + 1] < desc->hang_ptr[k]) return fail(FE_ERR_ARG, "hanging values: bad hang_ptr");
+  }
+  if (desc->hang_ptr[0] != 0) return fail(FE_ERR_ARG, "hanging values: hang_ptr[0] != 0");
+  h.ptr = desc->hang_ptr;
+  h.master = desc->hang_master;
+  h.weight = desc->hang_weight;
+  for (long long m = 0; m < desc->hang_ptr[desc->n_hang]; m++) {
+    const long long s = desc->hang_master[m];
+    if (s < 0 || s >= nslots) return fail(FE_ERR_ARG, "hanging values: master %lld out of range", m);
+    if (h.find(s) >= 0) return fail(FE_ERR_ARG, "hanging values: master slot %lld hangs itself", s);
+    if (!(desc->hang_weight[m] == desc->hang_weight[m])) return fail(FE_ERR_ARG, "hanging values: NaN weight");
+  }
   return FE_OK;
 }
 
@@ -895,8 +1000,19 @@ int fe_problem_create(const fe_problem_desc_t *desc, fe_problem_t **out) {
   if ((rc = P->jbuf_all.alloc(jel * std::max(1LL, jtot)))) return rc;
   if ((rc = P->rbuf_all.alloc(sizeof(double) * std::max(1LL, rtot)))) return rc;
   if ((rc = P->partial.alloc(sizeof(double) * 4096))) return rc;
-  if ((rc = build_pattern(P.get(), conn_h, desc->eqn))) return rc;
-  if (!P->fused && P->domains.size() == 1 && P->domains[0].replica_elems == 0) {
+  HangMap hang;
+  if ((rc = hang_map(desc, hang))) return rc;
+  if ((rc = build_pattern(P.get(), conn_h, desc->eqn, &hang))) return rc;
+  P->n_hang = desc->n_hang;
+  if (P->n_hang > 0) {
+    const long long nm = desc->hang_ptr[desc->n_hang];
+    if ((rc = P->hang_slot.upload(desc->hang_slot, sizeof(int64_t) * P->n_hang)) ||
+        (rc = P->hang_ptr.upload(desc->hang_ptr, sizeof(int64_t) * (P->n_hang + 1))) ||
+        (rc = P->hang_master.upload(desc->hang_master, sizeof(int64_t) * std::max(1LL, nm))) ||
+        (rc = P->hang_weight.upload(desc->hang_weight, sizeof(double) * std::max(1LL, nm))))
+      return rc;
+  }
+  if (!P->fused && P->domains.size() == 1 && P->domains[0].replica_elems == 0 && desc->n_hang == 0) {
     // last element (in element order) contributing to each row
     const Domain &d = P->domains[0];
     const fe_domain_desc_t &dd = desc->domains[0];
@@ -926,7 +1042,9 @@ int fe_pattern_host(const fe_problem_desc_t *desc, int64_t *nnz, int32_t *rowptr
     rb += dd.n_elem * (long long)dd.nlocal;
   }
   PatternOut out;
-  if ((rc = build_pattern_host(desc->n_dof, desc->nval, desc->eqn, doms, false, out))) return rc;
+  HangMap hang;
+  if ((rc = hang_map(desc, hang))) return rc;
+  if ((rc = build_pattern_host(desc->n_dof, desc->nval, desc->eqn, doms, false, out, &hang))) return rc;
   if (nnz) *nnz = (int64_t)out.colidx.size();
   if (rowptr) memcpy(rowptr, out.rowptr.data(), sizeof(int32_t) * out.rowptr.size());
   if (colidx) memcpy(colidx, out.colidx.data(), sizeof(int32_t) * out.colidx.size());
@@ -1025,17 +1143,38 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
     k_scatter_dofs<<<grid_for(n, 256, sms), 256, 0, st>>>(dofs, p->eqn.as<int>(), p->values.as<double>(), n);
     CUDA_TRY(cudaGetLastError());
   }
+  if (p->n_hang > 0) {
+    k_hang_interp<<<grid_for(p->n_hang, 256, sms), 256, 0, st>>>(
+        p->hang_slot.as<long long>(), p->hang_ptr.as<long long>(), p->hang_master.as<long long>(),
+        p->hang_weight.as<double>(), p->values.as<double>(), p->n_hang);
+    CUDA_TRY(cudaGetLastError());
+  }
   if (p->timing) CUDA_TRY(cudaEventRecord(ev[1], st));
   int rc = launch_elements(p, eflag, st);
   if (rc) return rc;
   if (p->timing) CUDA_TRY(cudaEventRecord(ev[2], st));
-  if (want_r) {
+  if (want_r && p->rw.p) {
+    k_gather_rows_w<<<grid_for(p->n_dof, 256, sms), 256, 0, st>>>(p->rptr.as<long long>(), p->ridx.as<unsigned>(),
+                                                                 p->rw.as<double>(), p->rbuf_all.as<double>(), R,
+                                                                 p->n_dof);
+    CUDA_TRY(cudaGetLastError());
+  } else if (want_r) {
     k_gather_rows<<<grid_for(p->n_dof, 256, sms), 256, 0, st>>>(p->rptr.as<long long>(), p->ridx.as<unsigned>(),
                                                                p->rbuf_all.as<double>(), R, p->n_dof);
     CUDA_TRY(cudaGetLastError());
   }
   if (p->timing) CUDA_TRY(cudaEventRecord(ev[3], st));
-  if (want_j && p->nnz > 0) {
+  if (want_j && p->nnz > 0 && p->cw.p) {
+    if (p->jac_prec == FE_JAC_F64)
+      k_gather_slots_w<double><<<grid_for(p->nnz, 256, sms), 256, 0, st>>>(
+          p->cptr.as<long long>(), p->cidx.as<unsigned>(), p->cw.as<double>(), p->jbuf_all.as<double>(),
+          (double *)J_vals, p->nnz);
+    else
+      k_gather_slots_w<float><<<grid_for(p->nnz, 256, sms), 256, 0, st>>>(
+          p->cptr.as<long long>(), p->cidx.as<unsigned>(), p->cw.as<double>(), p->jbuf_all.as<float>(),
+          (float *)J_vals, p->nnz);
+    CUDA_TRY(cudaGetLastError());
+  } else if (want_j && p->nnz > 0) {
     if (p->jac_prec == FE_JAC_F64)
       k_gather_slots<double><<<grid_for(p->nnz, 256, sms), 256, 0, st>>>(
           p->cptr.as<long long>(), p->cidx.as<unsigned>(), p->jbuf_all.as<double>(), (double *)J_vals, p->nnz);

@@ -255,7 +255,45 @@ class Problem:
             self.replica_elems = self.base_n_elem
             self.params_stride = len(self.params)
             self.params = np.tile(self.params, R)
-        free = present & ~pinned
+        # hanging values (refined meshes): constrained, no equation; each is the
+        # weighted sum of its masters (oomph's HangInfo)
+        self.hang_slots = np.zeros(0, dtype=np.int64)
+        self.hang_ptr = np.zeros(1, dtype=np.int64)
+        self.hang_master = np.zeros(0, dtype=np.int64)
+        self.hang_weight = np.zeros(0)
+        constrained = np.zeros((n, nval), dtype=bool)
+        if getattr(mesh, "hang", None):
+            if R > 1:
+                raise NotImplementedError("replicas of meshes with hanging nodes")
+            if any(sp_ != "C2" for _, sp_ in fields):
+                raise NotImplementedError("hanging nodes with C1 fields")
+            slots, ptr, mas, wts = [], [0], [], []
+            for h, ms in mesh.hang.items():
+                for f in range(nval):
+                    slots.append(h * nval + f)
+                    for m, w in ms:
+                        mas.append(m * nval + f)
+                        wts.append(w)
+                    ptr.append(len(mas))
+                    constrained[h, f] = True
+            order = np.argsort(slots, kind="stable")
+            ptr_a = np.array(ptr, dtype=np.int64)
+            lens = np.diff(ptr_a)
+            mas_a, wts_a = np.array(mas, dtype=np.int64), np.array(wts)
+            new_m, new_w, new_p = [], [], [0]
+            for k in order:
+                new_m.append(mas_a[ptr_a[k]:ptr_a[k + 1]])
+                new_w.append(wts_a[ptr_a[k]:ptr_a[k + 1]])
+                new_p.append(new_p[-1] + lens[k])
+            self.hang_slots = np.array(slots, dtype=np.int64)[order]
+            self.hang_ptr = np.array(new_p, dtype=np.int64)
+            self.hang_master = np.concatenate(new_m).astype(np.int64)
+            self.hang_weight = np.concatenate(new_w)
+            flat_v = values.reshape(-1)
+            for k, s_ in enumerate(self.hang_slots):
+                a, b = self.hang_ptr[k], self.hang_ptr[k + 1]
+                flat_v[s_] = np.dot(self.hang_weight[a:b], flat_v[self.hang_master[a:b]])
+        free = present & ~pinned & ~constrained
         eqn = np.full((n, nval), -1, dtype=np.int32)
         flat = free.reshape(-1)
         self.n_dof = int(flat.sum())
@@ -313,6 +351,10 @@ class Problem:
             x=np.ascontiguousarray(mesh.x, dtype=np.float64),
             eqn=np.ascontiguousarray(self.eqn),
             params=np.ascontiguousarray(self.params if len(self.params) else np.zeros(1)),
+            hs=np.ascontiguousarray(self.hang_slots, dtype=np.int64),
+            hp=np.ascontiguousarray(self.hang_ptr, dtype=np.int64),
+            hm=np.ascontiguousarray(self.hang_master if self.hang_master.size else np.zeros(1, np.int64)),
+            hw=np.ascontiguousarray(self.hang_weight if self.hang_weight.size else np.zeros(1)),
         )
         k = keep
         dd = N.DomainDesc(self.code.handle if with_code else None, mesh.etype.nnode, lay.n, mesh.n_elem,
@@ -323,7 +365,9 @@ class Problem:
         desc = N.ProblemDesc(mesh.dim, mesh.n_nodes, len(self.fields), k["x"].ctypes.data, k["eqn"].ctypes.data,
                              self.n_dof, 1, doms, len(self.params), k["params"].ctypes.data,
                              N.FE_JAC_F64 if self._prec == "f64" else N.FE_JAC_F32,
-                             getattr(self, "params_stride", 0), 0, None, 0)
+                             getattr(self, "params_stride", 0), 0, None, 0,
+                             int(self.hang_slots.size), k["hs"].ctypes.data, k["hp"].ctypes.data,
+                             k["hm"].ctypes.data, k["hw"].ctypes.data)
         return desc, doms, keep
 
     def host_pattern(self) -> Tuple[np.ndarray, np.ndarray]:
