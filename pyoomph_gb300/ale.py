@@ -974,9 +974,12 @@ class DropletProblem:
         self.timings: Dict[str, float] = {}
         self.newton_history: List[float] = []
         # launch shape of the fused kernel: thread cap and shared-memory budget
-        # per block (both decide elements per block; autotune.tune picks them)
-        self.nthreads_cap = 256
-        self.smem_budget = 100 * 1024
+        # per block (both decide elements per block).  Defaults: the fastest
+        # shapes autotune.tune measured on GB300 for the droplet (FP64 J: 512
+        # threads / 200 KB, FP32 J: 128 threads / 64 KB)
+        f64 = jacobian_precision in ("fp64", "f64")
+        self.nthreads_cap = 512 if f64 else 128
+        self.smem_budget = (200 if f64 else 64) * 1024
         # compile the element code with device-side bounds checks (status word 2)
         self.bounds_check = False
 
