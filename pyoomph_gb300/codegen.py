@@ -277,7 +277,7 @@ def _launch_shape(et: ElementType, nloc: int, per_elem_bytes: int, table_bytes: 
 
 
 def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
-                    name: str = None, epb: int = None, affine: bool = False) -> KernelSpec:
+                    name: str = None, epb: int = None, affine: bool = False, jref: bool = None) -> KernelSpec:
     """Fused element kernel for one element type and weak form.
 
     Thread phases (all in one launch, EPB elements per block):
@@ -291,6 +291,14 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
       B. one thread per (element, local row), rows ordered field-major so a
          warp shares its test field: R_i = sum_q rhat . phi_i and
          J_ij = sum_q phi_i^T D psi_j, written to the element buffers.
+
+    With ``jref`` (default for 3D elements) the Jacobian is contracted in
+    reference coordinates too: phase A pulls D back, Dhat = T^T D T with
+    T = diag(1, g) per field (the same route as the residual's rhat), and
+    phase B contracts Dhat with the reference shape tables shared by all
+    elements.  Nothing of size (knots x nodes x dim) is kept per element, so
+    a block holds several times more elements (the Q2 hex element needs 27 x
+    27 x 3 physical gradients otherwise).
     """
     dim, nn, nn1, nq = et.dim, et.nnode, et.nnode_c1, et.nq
     fields = pw.fields
@@ -305,11 +313,32 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     ndnz = max(1, len(pw.d_entries))
     jreal = "double" if jac_precision == "f64" else "float"
     jbytes = 8 if jac_precision == "f64" else 4
+    if jref is None:
+        jref = dim == 3
+    # Dhat blocks (test field, trial field) -> rows/cols in reference components
+    blocks: Dict[Tuple[int, int], List[Tuple[int, int, int]]] = {}
+    for k, (tc, ic, _) in enumerate(pw.d_entries):
+        blocks.setdefault((tc // nc, ic // nc), []).append((tc % nc, ic % nc, k))
+    hat: List[Tuple[int, int, int, int]] = []
+    for (tf_, gf_), ents in sorted(blocks.items()):
+        rows_ = ([0] if any(a_ == 0 for a_, _, _ in ents) else []) + \
+            (list(range(1, nc)) if any(a_ >= 1 for a_, _, _ in ents) else [])
+        cols_ = ([0] if any(b_ == 0 for _, b_, _ in ents) else []) + \
+            (list(range(1, nc)) if any(b_ >= 1 for _, b_, _ in ents) else [])
+        for ah in rows_:
+            for bh in cols_:
+                hat.append((tf_, gf_, ah, bh))
+    ndnz_hat = max(1, len(hat))
     table_doubles = nq + nq * nn + nq * nn * dim + nq * nn1 + nq * nn1 * dim
     table_bytes = table_doubles * 8
+    tabf = (nq * nn * (1 + dim) + nq * nn1 * (1 + dim)) if (jref and jreal == "float") else 0
+    table_bytes += ((tabf * 4 + 15) // 16) * 16
     geo_doubles = (dim * dim + 1) if affine else 0
-    per_elem = ((nn * dim + 2 * nn * nval + nq * ntc + geo_doubles) * 8
-                + (nq * ndnz + nq * nn * dim + (nq * nn1 * dim if has_c1 else 0)) * jbytes)
+    if jref:
+        per_elem = (nn * dim + 2 * nn * nval + nq * ntc + geo_doubles) * 8 + nq * ndnz_hat * jbytes
+    else:
+        per_elem = ((nn * dim + 2 * nn * nval + nq * ntc + geo_doubles) * 8
+                    + (nq * ndnz + nq * nn * dim + (nq * nn1 * dim if has_c1 else 0)) * jbytes)
     if epb is None:
         epb, threads = _launch_shape(et, nloc, per_elem, table_bytes)
     else:
@@ -319,7 +348,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     if threads > 1024 or smem > 227 * 1024:
         raise ValueError(f"{epb} elements per block do not fit a block ({threads} threads, {smem} B shared)")
     if name is None:
-        h = hashlib.sha1((et.name + jac_precision + str(affine) + str(epb) + str(pw.r_exprs) +
+        h = hashlib.sha1((et.name + jac_precision + str(affine) + str(epb) + str(jref) + str(pw.r_exprs) +
                           str(pw.d_entries)).encode()).hexdigest()[:10]
         name = f"fe_elem_{et.name.lower()}_{jac_precision}{'_aff' if affine else ''}_{h}"
 
@@ -334,6 +363,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w(f"#define FE_DIM {dim}\n#define FE_NN {nn}\n#define FE_NN1 {nn1}\n#define FE_NQ {nq}")
     w(f"#define FE_NVAL {nval}\n#define FE_NLOC {nloc}\n#define FE_EPB {epb}\n#define FE_NT {threads}")
     w(f"#define FE_NF {nf}\n#define FE_NTC {ntc}\n#define FE_NDNZ {ndnz}\n#define FE_AFFINE {1 if affine else 0}")
+    w(f"#define FE_NDNZH {ndnz_hat}")
     w(f"typedef {jreal} jreal;")
     w(f"__constant__ int c_loc_of[{len(loc_of_flat)}] = {{{', '.join(map(str, loc_of_flat))}}};")
     w(pointwise_source(pw, jreal))
@@ -350,14 +380,30 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("  double* sRh = sY + FE_EPB * FE_NN * FE_NVAL;")
     w("  double* sG = sRh + FE_EPB * FE_NQ * FE_NTC;")
     w(f"  jreal* sD = reinterpret_cast<jreal*>(sG + FE_EPB * {geo_doubles});")
-    w("  jreal* sDx2 = sD + FE_EPB * FE_NQ * FE_NDNZ;")
-    w("  jreal* sDx1 = sDx2 + FE_EPB * FE_NQ * FE_NN * FE_DIM;")
-    w("  (void)sDx1; (void)sG;")
+    if jref:
+        w("  jreal* sEnd = sD + FE_EPB * FE_NQ * FE_NDNZH;")
+        if jreal == "float":
+            # single-precision copies of the reference tables (after the element data)
+            w("  float* sPsi2j = reinterpret_cast<float*>(sEnd);")
+            w("  float* sDps2j = sPsi2j + FE_NQ * FE_NN;")
+            w("  float* sPsi1j = sDps2j + FE_NQ * FE_NN * FE_DIM;")
+            w("  float* sDps1j = sPsi1j + FE_NQ * FE_NN1;")
+        else:
+            w("  (void)sEnd;")
+            w("  const double* sPsi2j = sPsi2; const double* sDps2j = sDps2;")
+            w("  const double* sPsi1j = sPsi1; const double* sDps1j = sDps1;")
+        w("  (void)sPsi1j; (void)sDps1j; (void)sG;")
+    else:
+        w("  jreal* sDx2 = sD + FE_EPB * FE_NQ * FE_NDNZ;")
+        w("  jreal* sDx1 = sDx2 + FE_EPB * FE_NQ * FE_NN * FE_DIM;")
+        w("  (void)sDx1; (void)sG;")
     w("  const long long e0 = (long long)blockIdx.x * FE_EPB;")
     w("  const long long rem = a.n_elem - e0;")
     w("  const int nel = rem < FE_EPB ? (int)rem : FE_EPB;")
     w("  const int flag = a.flag;")
     w(f"  for (int k = threadIdx.x; k < {table_doubles}; k += FE_NT) sW[k] = a.tables[k];")
+    if jref and jreal == "float":
+        w(f"  for (int k = threadIdx.x; k < {tabf}; k += FE_NT) sPsi2j[k] = (float)a.tables[FE_NQ + k];")
     w("  for (int k = threadIdx.x; k < nel * FE_NN; k += FE_NT) {")
     w("    const int el = k / FE_NN, l = k - el * FE_NN;")
     w("    int node = a.conn[(e0 + el) * FE_NN + l];")
@@ -468,13 +514,37 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     interp("V", "sY", "        ")
     w("        fe_pointwise_hvp(U, V, Xq, Pe, D);")
     w("      }")
-    w("      jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZ;")
     w("      const jreal wj = (jreal)wq;")
-    w("      #pragma unroll")
-    w("      for (int k = 0; k < FE_NDNZ; ++k) Dq[k] = wj * D[k];")
-    w("      fe_phys_grad<FE_DIM, FE_NN, jreal>(g, dps, sDx2 + (el * FE_NQ + q) * FE_NN * FE_DIM);")
-    if has_c1:
-        w("      fe_phys_grad<FE_DIM, FE_NN1, jreal>(g, sDps1 + q * FE_NN1 * FE_DIM, sDx1 + (el * FE_NQ + q) * FE_NN1 * FE_DIM);")
+    if jref:
+        # Dhat = T^T D T, T = diag(1, g) per field: d/dx_i = sum_b g[b][i] d/ds_b
+        w("      jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZH;")
+        w("      jreal T[FE_DIM][FE_DIM];")
+        w("      #pragma unroll")
+        w("      for (int i = 0; i < FE_DIM; ++i)")
+        w("        #pragma unroll")
+        w("        for (int b = 0; b < FE_DIM; ++b) T[i][b] = (jreal)g[b][i];")
+
+        def cT(a_, h_):
+            if a_ == 0 and h_ == 0:
+                return ""
+            if a_ == 0 or h_ == 0:
+                return None
+            return f"T[{a_ - 1}][{h_ - 1}]"
+        for kk, (tf_, gf_, ah, bh) in enumerate(hat):
+            terms = []
+            for a_, b_, k in blocks[(tf_, gf_)]:
+                ca, cb = cT(a_, ah), cT(b_, bh)
+                if ca is None or cb is None:
+                    continue
+                terms.append(" * ".join([x_ for x_ in (ca, f"D[{k}]", cb) if x_]))
+            w(f"      Dq[{kk}] = wj * ({' + '.join(terms) if terms else '(jreal)0'});")
+    else:
+        w("      jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZ;")
+        w("      #pragma unroll")
+        w("      for (int k = 0; k < FE_NDNZ; ++k) Dq[k] = wj * D[k];")
+        w("      fe_phys_grad<FE_DIM, FE_NN, jreal>(g, dps, sDx2 + (el * FE_NQ + q) * FE_NN * FE_DIM);")
+        if has_c1:
+            w("      fe_phys_grad<FE_DIM, FE_NN1, jreal>(g, sDps1 + q * FE_NN1 * FE_DIM, sDx1 + (el * FE_NQ + q) * FE_NN1 * FE_DIM);")
     w("    }")
     w("  }")
     w("  __syncthreads();")
@@ -504,48 +574,90 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("      #pragma unroll")
     w("      for (int b = 0; b < FE_DIM; ++b) racc += rh[1 + b] * tdps[(q * tn + lt) * FE_DIM + b];")
     w("      Racc += racc;")
-    w("      if (flag) {")
-    w("        const jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZ;")
-    w("        const jreal* tdx = t1 ? (sDx1 + ((el * FE_NQ + q) * FE_NN1 + lt) * FE_DIM)")
-    w("                             : (sDx2 + ((el * FE_NQ + q) * FE_NN + lt) * FE_DIM);")
-    w("        const jreal phi0 = (jreal)pv;")
-    for d in range(dim):
-        w(f"        const jreal phi{d + 1} = tdx[{d}];")
-    for ic in used_ic:
-        w(f"        jreal a{ic} = (jreal)0;")
-    # per test field: only its own D entries (warp-uniform branch)
-    for f in range(nf):
-        ents = [(k, tc, ic) for k, (tc, ic, _) in enumerate(pw.d_entries) if tc // nc == f]
-        if not ents:
-            continue
-        w(f"        if (tf == {f}) {{")
-        for k, tc, ic in ents:
-            w(f"          a{ic} += phi{tc % nc} * Dq[{k}];")
-        w("        }")
-    for f, (fname, fsp) in enumerate(fields):
-        comps = [ic for ic in used_ic if ic // nc == f]
-        if not comps:
-            continue
-        if fsp == "C2":
+    if jref:
+        w("      if (flag) {")
+        w("        const jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZH;")
+        w("        const jreal* tpj = t1 ? (sPsi1j + q * FE_NN1) : (sPsi2j + q * FE_NN);")
+        w("        const jreal* tdj = t1 ? (sDps1j + (q * FE_NN1 + lt) * FE_DIM) : (sDps2j + (q * FE_NN + lt) * FE_DIM);")
+        w("        const jreal phi0 = tpj[lt];")
+        for d in range(dim):
+            w(f"        const jreal phi{d + 1} = tdj[{d}];")
+        used_h = sorted({(gf_, bh) for (_, gf_, _, bh) in hat})
+        for gf_, bh in used_h:
+            w(f"        jreal h{gf_}_{bh} = (jreal)0;")
+        for f in range(nf):
+            ents = [(kk, ah, gf_, bh) for kk, (tf_, gf_, ah, bh) in enumerate(hat) if tf_ == f]
+            if not ents:
+                continue
+            w(f"        if (tf == {f}) {{")
+            for kk, ah, gf_, bh in ents:
+                w(f"          h{gf_}_{bh} += phi{ah} * Dq[{kk}];")
+            w("        }")
+        for f, (fname, fsp) in enumerate(fields):
+            comps = [bh for (gf_, bh) in used_h if gf_ == f]
+            if not comps:
+                continue
             w("        {")
-            w("          const double* psi = sPsi2 + q * FE_NN;")
-            w("          const jreal* dx = sDx2 + (el * FE_NQ + q) * FE_NN * FE_DIM;")
-            cnt = nn
-        else:
-            w("        {")
-            w("          const double* psi = sPsi1 + q * FE_NN1;")
-            w("          const jreal* dx = sDx1 + (el * FE_NQ + q) * FE_NN1 * FE_DIM;")
-            cnt = nn1
-        for ls in range(cnt):
-            terms = []
-            for ic in comps:
-                c = ic % nc
-                if c == 0:
-                    terms.append(f"a{ic} * (jreal)psi[{ls}]")
-                else:
-                    terms.append(f"a{ic} * dx[{ls * dim + c - 1}]")
-            w(f"          Jr[{layout.loc_of[f][ls]}] += {' + '.join(terms)};")
-        w("        }")
+            if fsp == "C2":
+                w("          const jreal* psi = sPsi2j + q * FE_NN;")
+                w("          const jreal* dps_ = sDps2j + q * FE_NN * FE_DIM;")
+                cnt = nn
+            else:
+                w("          const jreal* psi = sPsi1j + q * FE_NN1;")
+                w("          const jreal* dps_ = sDps1j + q * FE_NN1 * FE_DIM;")
+                cnt = nn1
+            for ls in range(cnt):
+                terms = []
+                for bh in comps:
+                    if bh == 0:
+                        terms.append(f"h{f}_0 * psi[{ls}]")
+                    else:
+                        terms.append(f"h{f}_{bh} * dps_[{ls * dim + bh - 1}]")
+                w(f"          Jr[{layout.loc_of[f][ls]}] += {' + '.join(terms)};")
+            w("        }")
+    else:
+        w("      if (flag) {")
+        w("        const jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZ;")
+        w("        const jreal* tdx = t1 ? (sDx1 + ((el * FE_NQ + q) * FE_NN1 + lt) * FE_DIM)")
+        w("                             : (sDx2 + ((el * FE_NQ + q) * FE_NN + lt) * FE_DIM);")
+        w("        const jreal phi0 = (jreal)pv;")
+        for d in range(dim):
+            w(f"        const jreal phi{d + 1} = tdx[{d}];")
+        for ic in used_ic:
+            w(f"        jreal a{ic} = (jreal)0;")
+        # per test field: only its own D entries (warp-uniform branch)
+        for f in range(nf):
+            ents = [(k, tc, ic) for k, (tc, ic, _) in enumerate(pw.d_entries) if tc // nc == f]
+            if not ents:
+                continue
+            w(f"        if (tf == {f}) {{")
+            for k, tc, ic in ents:
+                w(f"          a{ic} += phi{tc % nc} * Dq[{k}];")
+            w("        }")
+        for f, (fname, fsp) in enumerate(fields):
+            comps = [ic for ic in used_ic if ic // nc == f]
+            if not comps:
+                continue
+            if fsp == "C2":
+                w("        {")
+                w("          const double* psi = sPsi2 + q * FE_NN;")
+                w("          const jreal* dx = sDx2 + (el * FE_NQ + q) * FE_NN * FE_DIM;")
+                cnt = nn
+            else:
+                w("        {")
+                w("          const double* psi = sPsi1 + q * FE_NN1;")
+                w("          const jreal* dx = sDx1 + (el * FE_NQ + q) * FE_NN1 * FE_DIM;")
+                cnt = nn1
+            for ls in range(cnt):
+                terms = []
+                for ic in comps:
+                    c = ic % nc
+                    if c == 0:
+                        terms.append(f"a{ic} * (jreal)psi[{ls}]")
+                    else:
+                        terms.append(f"a{ic} * dx[{ls * dim + c - 1}]")
+                w(f"          Jr[{layout.loc_of[f][ls]}] += {' + '.join(terms)};")
+            w("        }")
     w("      }")
     w("    }")
     w("    const long long row = (e0 + el) * FE_NLOC + i;")

@@ -108,6 +108,9 @@ class Problem:
         self.linear_solver: Optional[Callable] = None
         # compile the element code with device-side bounds checks (status word 2)
         self.bounds_check = False
+        # contract the Jacobian in reference coordinates (None: the generator's
+        # default, on for 3D elements)
+        self.jacobian_reference: Optional[bool] = None
         # linear_solver = "bicgstab": J dx = R solved on the device (linsolve.py)
         # to this relative tolerance; None: SuperLU on the host (the reference's default)
         self.linear_solver_tolerance = 1e-13
@@ -195,11 +198,13 @@ class Problem:
             self.affine = self.geometry == "affine"
         # the kernel depends on the weak form, element type, precision and
         # geometry kind only -- not on the mesh size: cache it per process
-        key = (mesh.etype.name, tuple(fields), str(integrand), tuple(used), prec, self.affine, self.elems_per_block)
+        key = (mesh.etype.name, tuple(fields), str(integrand), tuple(used), prec, self.affine, self.elems_per_block,
+               self.jacobian_reference)
         ks = _KERNEL_CACHE.get(key)
         if ks is None:
             pw = differentiate(fields, mesh.dim, integrand, used)
-            ks = generate_kernel(mesh.etype, pw, prec, epb=self.elems_per_block, affine=self.affine)
+            ks = generate_kernel(mesh.etype, pw, prec, epb=self.elems_per_block, affine=self.affine,
+                                 jref=self.jacobian_reference)
             _KERNEL_CACHE[key] = ks
         self.kernel: KernelSpec = ks
         self.timings.update(setup_mesh_s=t1 - t0, codegen_s=time.perf_counter() - t1)

@@ -8,7 +8,7 @@ import oracle as O
 KINDS = ["poisson_q2", "poisson_p2", "ns_th", "nldiff_hex", "nldiff_q2"]
 
 
-def build(kind: str, geometry: str, prec: str, seed: int = 3):
+def build(kind: str, geometry: str, prec: str, seed: int = 3, jref=None):
     from pyoomph_gb300 import workloads as W
     rng = np.random.default_rng(seed)
     T = W.wavy(0.03) if geometry == "general" else None
@@ -30,6 +30,7 @@ def build(kind: str, geometry: str, prec: str, seed: int = 3):
             eq = O.EQ_NONLINEAR_DIFFUSION
         params = O.gaussian_params(gauss)
     P.geometry = geometry if geometry == "general" else "auto"
+    P.jacobian_reference = jref
     ks = P.lower()
     m = P.mesh
     values = P._values0.copy()

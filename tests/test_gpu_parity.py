@@ -220,14 +220,16 @@ def test_structured_workloads_take_the_affine_path():
         assert P.affine
 
 
+@pytest.mark.parametrize("jref", [False, True])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
 @pytest.mark.parametrize("geometry", ["affine", "general"])
 @pytest.mark.parametrize("kind", ["poisson_q2", "poisson_p2", "ns_th", "nldiff_hex", "nldiff_q2"])
-def test_element_level_parity_every_kernel_variant(kind, geometry, prec):
+def test_element_level_parity_every_kernel_variant(kind, geometry, prec, jref):
     """Element residuals/matrices straight from the GPU element buffers
-    (fe_problem_element_buffers) against the oracle's, for every variant."""
+    (fe_problem_element_buffers) against the oracle's, for every variant
+    (Jacobian contracted in physical or in reference coordinates)."""
     import element_cases as C
-    P, ks, values, Rr, Jr = C.build(kind, geometry, prec)
+    P, ks, values, Rr, Jr = C.build(kind, geometry, prec, jref=jref)
     P.initialise()
     P.set_values(values)
     P.get_jacobian()

@@ -177,15 +177,17 @@ def test_host_pattern_vs_oracle_larger(kind):
     assert np.array_equal(rp, rp0) and np.array_equal(ci, ci0)
 
 
+@pytest.mark.parametrize("jref", [False, True])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
 @pytest.mark.parametrize("geometry", ["affine", "general"])
 @pytest.mark.parametrize("kind", ["poisson_q2", "poisson_p2", "ns_th", "nldiff_hex", "nldiff_q2"])
-def test_generated_kernel_emulated_on_cpu_matches_oracle_elements(kind, geometry, prec):
-    """Every generated kernel variant, run on the CPU by the sequential
-    emulator, reproduces the oracle's element residuals and matrices."""
+def test_generated_kernel_emulated_on_cpu_matches_oracle_elements(kind, geometry, prec, jref):
+    """Every generated kernel variant (Jacobian contracted in physical or in
+    reference coordinates), run on the CPU by the sequential emulator,
+    reproduces the oracle's element residuals and matrices."""
     import element_cases as C
     import kernel_emulator as KE
-    P, ks, values, Rr, Jr = C.build(kind, geometry, prec)
+    P, ks, values, Rr, Jr = C.build(kind, geometry, prec, jref=jref)
     assert P.affine == (geometry == "affine")
     rb, jb, st = KE.run(ks, P.mesh.x, P.mesh.conn, values, P.params)
     assert st[0] == 0
