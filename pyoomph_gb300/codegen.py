@@ -292,7 +292,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
          warp shares its test field: R_i = sum_q rhat . phi_i and
          J_ij = sum_q phi_i^T D psi_j, written to the element buffers.
 
-    With ``jref`` (default for 3D elements) the Jacobian is contracted in
+    With ``jref`` (default: FP32 Jacobians, 3D elements, single-field
+    forms) the Jacobian is contracted in
     reference coordinates too: phase A pulls D back, Dhat = T^T D T with
     T = diag(1, g) per field (the same route as the residual's rhat), and
     phase B contracts Dhat with the reference shape tables shared by all
@@ -314,7 +315,10 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     jreal = "double" if jac_precision == "f64" else "float"
     jbytes = 8 if jac_precision == "f64" else 4
     if jref is None:
-        jref = dim == 3
+        # measured on GB300: faster for every FP32 Jacobian, for 3D elements
+        # and for single-field forms; slower for the FP64 Taylor-Hood
+        # Jacobian, whose pulled-back D is denser than D
+        jref = jac_precision == "f32" or dim == 3 or nf == 1
     # Dhat blocks (test field, trial field) -> rows/cols in reference components
     blocks: Dict[Tuple[int, int], List[Tuple[int, int, int]]] = {}
     for k, (tc, ic, _) in enumerate(pw.d_entries):
