@@ -338,8 +338,17 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     tabf = (nq * nn * (1 + dim) + nq * nn1 * (1 + dim)) if (jref and jreal == "float") else 0
     table_bytes += ((tabf * 4 + 15) // 16) * 16
     geo_doubles = (dim * dim + 1) if affine else 0
+    # sum factorisation of the Q2 hex Jacobian (tensor-product shapes and
+    # Gauss<3,3> knots): J_ij = sum_ab sum_q prod_d F^d_ab[q_d][i_d][j_d] Dhat_ab(q)
+    # contracted one direction at a time (3 x 81 + 3 x 243 + 3 x 729 multiply-adds
+    # per (a, b) block instead of 27 x 27 x 27)
+    sumfac = bool(jref and et.name == "Q2_HEX" and nf == 1 and spaces[0] == "C2")
+    if sumfac:
+        table_bytes += ((4 * 27 * jbytes + 15) // 16) * 16
     if jref:
         per_elem = (nn * dim + 2 * nn * nval + nq * ntc + geo_doubles) * 8 + nq * ndnz_hat * jbytes
+        if sumfac:
+            per_elem += (81 + 243 + 729) * jbytes
     else:
         per_elem = ((nn * dim + 2 * nn * nval + nq * ntc + geo_doubles) * 8
                     + (nq * ndnz + nq * nn * dim + (nq * nn1 * dim if has_c1 else 0)) * jbytes)
@@ -352,7 +361,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     if threads > 1024 or smem > 227 * 1024:
         raise ValueError(f"{epb} elements per block do not fit a block ({threads} threads, {smem} B shared)")
     if name is None:
-        h = hashlib.sha1((et.name + jac_precision + str(affine) + str(epb) + str(jref) + str(pw.r_exprs) +
+        h = hashlib.sha1((et.name + jac_precision + str(affine) + str(epb) + str(jref) + str(sumfac) + str(pw.r_exprs) +
                           str(pw.d_entries)).encode()).hexdigest()[:10]
         name = f"fe_elem_{et.name.lower()}_{jac_precision}{'_aff' if affine else ''}_{h}"
 
@@ -370,6 +379,12 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w(f"#define FE_NDNZH {ndnz_hat}")
     w(f"typedef {jreal} jreal;")
     w(f"__constant__ int c_loc_of[{len(loc_of_flat)}] = {{{', '.join(map(str, loc_of_flat))}}};")
+    if jref and et.name == "Q2_HEX" and nf == 1 and spaces[0] == "C2":
+        from .spaces import _G3_1D, _lag3
+        M_ = [np.array([_lag3(g)[0] for g in _G3_1D]), np.array([_lag3(g)[1] for g in _G3_1D])]
+        F_ = [repr(float(M_[c >> 1][q][i] * M_[c & 1][q][j]))
+              for c in range(4) for q in range(3) for i in range(3) for j in range(3)]
+        w(f"__constant__ double c_F[108] = {{{', '.join(F_)}}};")
     w(pointwise_source(pw, jreal))
     w(f'extern "C" __global__ void __launch_bounds__(FE_NT) {name}(const FeElemArgs a) {{')
     w("  extern __shared__ __align__(16) unsigned char fe_smem[];")
@@ -397,6 +412,13 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w("  const double* sPsi2j = sPsi2; const double* sDps2j = sDps2;")
             w("  const double* sPsi1j = sPsi1; const double* sDps1j = sDps1;")
         w("  (void)sPsi1j; (void)sDps1j; (void)sG;")
+        if sumfac:
+            # per element: stage buffers and the element matrix; per block: F tables
+            base = "sPsi2j + " + str(tabf) if jreal == "float" else "sEnd"
+            w(f"  jreal* sS1 = reinterpret_cast<jreal*>({base});")
+            w("  jreal* sS2 = sS1 + FE_EPB * 81;")
+            w("  jreal* sJe = sS2 + FE_EPB * 243;")
+            w("  jreal* sF = sJe + FE_EPB * 729;")
     else:
         w("  jreal* sDx2 = sD + FE_EPB * FE_NQ * FE_NDNZ;")
         w("  jreal* sDx1 = sDx2 + FE_EPB * FE_NQ * FE_NN * FE_DIM;")
@@ -408,6 +430,17 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w(f"  for (int k = threadIdx.x; k < {table_doubles}; k += FE_NT) sW[k] = a.tables[k];")
     if jref and jreal == "float":
         w(f"  for (int k = threadIdx.x; k < {tabf}; k += FE_NT) sPsi2j[k] = (float)a.tables[FE_NQ + k];")
+    if sumfac:
+        from .spaces import _G3_1D, _lag3
+        M = [np.array([_lag3(g)[0] for g in _G3_1D]), np.array([_lag3(g)[1] for g in _G3_1D])]
+        Fv = []
+        for c in range(4):
+            for q in range(3):
+                for i in range(3):
+                    for j in range(3):
+                        Fv.append(M[c >> 1][q][i] * M[c & 1][q][j])
+        w(f"  for (int k = threadIdx.x; k < 108; k += FE_NT) sF[k] = (jreal)c_F[k];")
+
     w("  for (int k = threadIdx.x; k < nel * FE_NN; k += FE_NT) {")
     w("    const int el = k / FE_NN, l = k - el * FE_NN;")
     w("    int node = a.conn[(e0 + el) * FE_NN + l];")
@@ -552,6 +585,40 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    }")
     w("  }")
     w("  __syncthreads();")
+    if sumfac:
+        # ---------------- phase B': sum-factorised Jacobian, one (a, b) block at a time ----------------
+        w("  if (flag) {")
+        for kk, (_, _, ah, bh) in enumerate(hat):
+            cx = 2 * (ah == 1) + (bh == 1)
+            cy = 2 * (ah == 2) + (bh == 2)
+            cz = 2 * (ah == 3) + (bh == 3)
+            w(f"    // block (a={ah}, b={bh})")
+            w("    for (int p = threadIdx.x; p < nel * 81; p += FE_NT) {")
+            w("      const int el = p / 81, o = p - el * 81, qxy = o / 9, izjz = o - qxy * 9;")
+            w("      const int iz = izjz / 3, jz = izjz - iz * 3;")
+            w("      const jreal* Dq = sD + (el * FE_NQ + 3 * qxy) * FE_NDNZH;")
+            w(f"      const jreal* F = sF + {cz * 27} + iz * 3 + jz;")
+            w(f"      sS1[p] = F[0] * Dq[{kk}] + F[9] * Dq[FE_NDNZH + {kk}] + F[18] * Dq[2 * FE_NDNZH + {kk}];")
+            w("    }")
+            w("    __syncthreads();")
+            w("    for (int p = threadIdx.x; p < nel * 243; p += FE_NT) {")
+            w("      const int el = p / 243, o = p - el * 243, qx = o / 81, r = o - qx * 81, iyjy = r / 9;")
+            w("      const int izjz = r - iyjy * 9, iy = iyjy / 3, jy = iyjy - iy * 3;")
+            w("      const jreal* S1 = sS1 + el * 81 + qx * 27 + izjz;")
+            w(f"      const jreal* F = sF + {cy * 27} + iy * 3 + jy;")
+            w("      sS2[p] = F[0] * S1[0] + F[9] * S1[9] + F[18] * S1[18];")
+            w("    }")
+            w("    __syncthreads();")
+            w("    for (int p = threadIdx.x; p < nel * 729; p += FE_NT) {")
+            w("      const int el = p / 729, o = p - el * 729, i = o / 27, j = o - i * 27;")
+            w("      const int ix = i % 3, iy = (i / 3) % 3, iz = i / 9, jx = j % 3, jy = (j / 3) % 3, jz = j / 9;")
+            w("      const jreal* S2 = sS2 + el * 243 + (iy * 3 + jy) * 9 + iz * 3 + jz;")
+            w(f"      const jreal* F = sF + {cx * 27} + ix * 3 + jx;")
+            w(f"      const jreal v = F[0] * S2[0] + F[9] * S2[81] + F[18] * S2[162];")
+            w(f"      sJe[p] {'=' if kk == 0 else '+='} v;")
+            w("    }")
+            w("    __syncthreads();")
+        w("  }")
     # ---------------- phase B: field-major rows ----------------
     w("  for (int p = threadIdx.x; p < nel * FE_NLOC; p += FE_NT) {")
     w("    int tf = 0, rel = p;")
@@ -578,7 +645,9 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("      #pragma unroll")
     w("      for (int b = 0; b < FE_DIM; ++b) racc += rh[1 + b] * tdps[(q * tn + lt) * FE_DIM + b];")
     w("      Racc += racc;")
-    if jref:
+    if sumfac:
+        pass
+    elif jref:
         w("      if (flag) {")
         w("        const jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZH;")
         w("        const jreal* tpj = t1 ? (sPsi1j + q * FE_NN1) : (sPsi2j + q * FE_NN);")
@@ -662,14 +731,19 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                         terms.append(f"a{ic} * dx[{ls * dim + c - 1}]")
                 w(f"          Jr[{layout.loc_of[f][ls]}] += {' + '.join(terms)};")
             w("        }")
-    w("      }")
+    if not sumfac:
+        w("      }")
     w("    }")
     w("    const long long row = (e0 + el) * FE_NLOC + i;")
     w("    a.rbuf[row] = Racc;")
     w("    if (flag) {")
     w("      jreal* jb = reinterpret_cast<jreal*>(a.jbuf) + row * FE_NLOC;")
-    w("      #pragma unroll")
-    w("      for (int k = 0; k < FE_NLOC; ++k) jb[k] = Jr[k];")
+    if sumfac:
+        w("      const jreal* Jrow = sJe + el * 729 + i * 27;")
+        w("      for (int k = 0; k < FE_NLOC; ++k) jb[k] = Jrow[k];")
+    else:
+        w("      #pragma unroll")
+        w("      for (int k = 0; k < FE_NLOC; ++k) jb[k] = Jr[k];")
     w("    }")
     w("  }")
     w("}")
