@@ -246,6 +246,7 @@ class KernelSpec:
     smem_bytes: int
     jac_precision: str
     tables: np.ndarray = field(repr=False, default=None)
+    sumfac_blocks: int = 0       # > 0: sum-factorised Jacobian with this many (a, b) blocks
 
     @property
     def key(self) -> str:
@@ -342,7 +343,9 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     # Gauss<3,3> knots): J_ij = sum_ab sum_q prod_d F^d_ab[q_d][i_d][j_d] Dhat_ab(q)
     # contracted one direction at a time (3 x 81 + 3 x 243 + 3 x 729 multiply-adds
     # per (a, b) block instead of 27 x 27 x 27)
-    sumfac = bool(jref and et.name == "Q2_HEX" and nf == 1 and spaces[0] == "C2")
+    # (FP64 Jacobians only: for FP32 the contraction is cheap on the FP32 pipe
+    # and the staged form measured slower on GB300)
+    sumfac = bool(jref and et.name == "Q2_HEX" and nf == 1 and spaces[0] == "C2" and jac_precision == "f64")
     if sumfac:
         table_bytes += ((4 * 27 * jbytes + 15) // 16) * 16
     if jref:
@@ -379,7 +382,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w(f"#define FE_NDNZH {ndnz_hat}")
     w(f"typedef {jreal} jreal;")
     w(f"__constant__ int c_loc_of[{len(loc_of_flat)}] = {{{', '.join(map(str, loc_of_flat))}}};")
-    if jref and et.name == "Q2_HEX" and nf == 1 and spaces[0] == "C2":
+    if sumfac:
         from .spaces import _G3_1D, _lag3
         M_ = [np.array([_lag3(g)[0] for g in _G3_1D]), np.array([_lag3(g)[1] for g in _G3_1D])]
         F_ = [repr(float(M_[c >> 1][q][i] * M_[c & 1][q][j]))
@@ -750,7 +753,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     source = "\n".join(src) + "\n"
     return KernelSpec(name=name, source=source, et=et, layout=layout, pointwise=pw, epb=epb,
                       threads=threads, smem_bytes=smem, jac_precision=jac_precision,
-                      tables=et.packed_tables())
+                      tables=et.packed_tables(), sumfac_blocks=len(hat) if sumfac else 0)
 
 
 def estimate_flops(ks: KernelSpec, affine: bool) -> Dict[str, float]:
@@ -791,6 +794,9 @@ def estimate_flops(ks: KernelSpec, affine: bool) -> Dict[str, float]:
         per_row_q += 2 * (NN if s == "C2" else N1) * len(comps)
     a_ops = 2 * len(pw.d_entries) / max(1, len(fields))
     jac = NQ * jac_q + rows * NQ * (per_row_q + a_ops)
+    if ks.sumfac_blocks:
+        # pulled-back D per knot, then per (a, b) block 3 x (81 + 243 + 729) multiply-adds
+        jac = NQ * (ops_d + 4 * ks.sumfac_blocks) + ks.sumfac_blocks * 2 * 3 * (81 + 243 + 729)
     out = {"fp64": float(fp64), "jac": float(jac)}
     if ks.jac_precision == "f64":
         out["fp64"] += out["jac"]
