@@ -93,6 +93,21 @@ def bicgstab(A: DeviceCSR, b, tol: float = 1e-13, maxiter: int = 20000, check_ev
     rho_old = torch.ones((), dtype=torch.float64, device=dev)
     alpha = torch.ones((), dtype=torch.float64, device=dev)
     omega = torch.ones((), dtype=torch.float64, device=dev)
+    x_good = x.clone()
+    restarts = 0
+
+    def restart():
+        # from the last checked iterate, with the true residual as shadow vector
+        nonlocal r, rhat, rho_old, alpha, omega
+        A.matvec(x, t, st)
+        r = b - t
+        rhat = r.clone()
+        p.zero_()
+        v.zero_()
+        rho_old = torch.ones((), dtype=torch.float64, device=dev)
+        alpha = torch.ones((), dtype=torch.float64, device=dev)
+        omega = torch.ones((), dtype=torch.float64, device=dev)
+
     for it in range(1, maxiter + 1):
         rho = torch.dot(rhat, r)
         beta = (rho / rho_old) * (alpha / omega)
@@ -109,18 +124,19 @@ def bicgstab(A: DeviceCSR, b, tol: float = 1e-13, maxiter: int = 20000, check_ev
         rho_old = rho
         if it % check_every == 0:
             rn = float(r.abs().max())
-            if rn != rn:
-                raise LinearSolverError(f"BiCGStab broke down (NaN) after {it} iterations")
+            if not (rn == rn) or not bool(torch.isfinite(x).all()):
+                # breakdown (rho or omega ~ 0): back to the last good iterate and restart
+                restarts += 1
+                if restarts > 20:
+                    raise LinearSolverError(f"BiCGStab broke down repeatedly ({it} iterations)")
+                x.copy_(x_good)
+                restart()
+                continue
+            x_good.copy_(x)
             if rn <= target:
                 A.matvec(x, t, st)
                 true = float((b - t).abs().max())
                 if true <= target * 10:
                     return x, it
-                r = b - t            # restart from the true residual
-                rhat = r.clone()
-                p.zero_()
-                v.zero_()
-                rho_old = torch.ones((), dtype=torch.float64, device=dev)
-                alpha = torch.ones((), dtype=torch.float64, device=dev)
-                omega = torch.ones((), dtype=torch.float64, device=dev)
+                restart()
     raise LinearSolverError(f"BiCGStab did not reach {tol} in {maxiter} iterations")
