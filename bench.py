@@ -181,9 +181,9 @@ def make_problem(workload: str, size: int, precision: str, epb=None):
 # (dram__bytes_read.sum + dram__bytes_write.sum, median of 21 launches;
 # profiles/dram_traffic_element_kernels.md gives the commands).
 MEASURED_TRAFFIC = {
-    ("ns", 256, "fp64"): 207.48e6, ("ns", 256, "fp32"): 86.00e6,
-    ("droplet", 110, "fp64"): 97.69e6, ("droplet", 110, "fp32"): 24.94e6,
-    ("hex", 48, "fp64"): 652.76e6, ("hex", 48, "fp32"): 333.92e6,
+    ("ns", 256, "fp64"): 207.56e6,
+    ("droplet", 110, "fp64"): 96.67e6, ("droplet", 110, "fp32"): 24.00e6,
+    ("hex", 48, "fp64"): 675.25e6,
     ("poisson", 64, "fp64"): 0.63e6, ("poisson", 64, "fp32"): 0.62e6,
 }
 
