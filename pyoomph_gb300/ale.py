@@ -870,12 +870,18 @@ def generate_fused(domains: List[DomainCode], dim: int, params: List[str], nval:
     src = "\n".join(head + bodies)
     h = hashlib.sha1(src.encode()).hexdigest()[:12]
     name = f"fe_fused_{jac_precision}_{h}"
+    # persistent: the grid is sized to the SMs' resident blocks and each block
+    # walks the element blocks of every domain (bulk first, then the small
+    # interface and contact-line domains) with a static stride
     tail = [f'extern "C" __global__ void __launch_bounds__(FE_NT) {name}(const FeFusedArgs fa) {{',
             "  extern __shared__ __align__(16) unsigned char fe_smem[];",
             "  double* sW = reinterpret_cast<double*>(fe_smem);",
-            "  const int b = blockIdx.x;"]
+            "  for (int b = blockIdx.x; b < fa.block_start[fa.n_domains]; b += gridDim.x) {"]
     for k in range(len(domains)):
-        tail.append(f"  if (b < fa.block_start[{k + 1}]) {{ dom{k}::run(fa.d[{k}], b - fa.block_start[{k}], sW); return; }}")
+        cond = "if" if k == 0 else "else if"
+        tail.append(f"    {cond} (b < fa.block_start[{k + 1}]) dom{k}::run(fa.d[{k}], b - fa.block_start[{k}], sW);")
+    tail.append("    __syncthreads();  // the next element block reuses the shared memory")
+    tail.append("  }")
     tail.append("}")
     src = src + "\n" + "\n".join(tail) + "\n"
     return FusedKernel(src, name, threads, smem, domains, params, jac_precision)

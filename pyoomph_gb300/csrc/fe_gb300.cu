@@ -321,6 +321,7 @@ struct fe_problem {
   int dim = 0, nval = 0, jac_prec = FE_JAC_F64;
   long long n_nodes = 0, n_dof = 0, nnz = 0;
   int n_params = 0, params_stride = 0, n_hist = 0, fused = 0, dparam = 0;
+  int fused_grid_cap = 0; // resident blocks of the fused kernel (persistent launch)
   std::vector<Domain> domains;
   DevBuf x, values, eqn, params, status, hist, x0, dir;
   long long n_hang = 0;
@@ -710,8 +711,17 @@ int launch_elements(fe_problem *p, int flag, cudaStream_t st) {
     fa.block_start[k] = nb;
     fa.n_domains = k;
     if (nb == 0) return FE_OK;
+    // persistent launch: as many blocks as the SMs hold at once (the kernel
+    // strides over the element blocks of all domains)
+    if (p->fused_grid_cap == 0) {
+      int per_sm = 1;
+      CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)p->domains[0].code->func, threads,
+                                                             (size_t)smem));
+      p->fused_grid_cap = std::max(1, per_sm) * sm_count_cached();
+    }
+    const int grid = std::min(nb, p->fused_grid_cap);
     void *kp[] = {&fa};
-    CUDA_TRY(cudaLaunchKernel((const void *)p->domains[0].code->func, dim3(nb), dim3(threads), kp, (size_t)smem, st));
+    CUDA_TRY(cudaLaunchKernel((const void *)p->domains[0].code->func, dim3(grid), dim3(threads), kp, (size_t)smem, st));
     return FE_OK;
   }
   for (Domain &d : p->domains) {

@@ -26,7 +26,7 @@ PRELUDE = r"""
 #include <cmath>
 #include <cstring>
 struct fe_emu_dim3 { unsigned x, y, z; };
-static fe_emu_dim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0};
+static fe_emu_dim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, gridDim = {1, 1, 1};
 #define __global__
 #define __device__
 #define __host__
@@ -120,7 +120,7 @@ def build_fused(fk, defines=()) -> ctypes.CDLL:
         f'\nextern "C" void fe_emu_run_fused(const FeFusedArgs *a, int nblocks) {{\n'
         f'  for (int b = 0; b < nblocks; ++b) {{\n'
         f'    memset(fe_smem, 0xff, sizeof(fe_smem));\n'
-        f'    blockIdx.x = b; {fk.name}(*a); }}\n}}\n')
+        f'    blockIdx.x = b; gridDim.x = nblocks; {fk.name}(*a); }}\n}}\n')
     h = hashlib.sha1((body + _headers()).encode()).hexdigest()[:16]
     os.makedirs(OUT, exist_ok=True)
     so = os.path.join(OUT, f"emu_{h}.so")
