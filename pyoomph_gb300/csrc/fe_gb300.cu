@@ -1134,7 +1134,8 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
   if (want_h && (p->fused || !p->dir.p || (flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS | FE_ASSEMBLE_DPARAM))))
     return fail(FE_ERR_ARG, "fe_assemble: the Hessian-vector product needs fixed-mesh code, a direction "
                             "(fe_problem_set_direction) and a call of its own");
-  if ((want_r && !R) || (want_j && !J_vals)) return fail(FE_ERR_ARG, "fe_assemble: missing output");
+  if ((want_r && !R && p->n_dof > 0) || (want_j && !J_vals && p->nnz > 0))
+    return fail(FE_ERR_ARG, "fe_assemble: missing output");
   if ((want_m || want_p) && !p->fused)
     return fail(FE_ERR_ARG, "fe_assemble: mass matrices and parameter derivatives need fused (moving-mesh) code");
   if ((want_m && (flags & FE_ASSEMBLE_JACOBIAN)) || (want_p && (flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS))))
@@ -1148,7 +1149,7 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
     CUDA_TRY(cudaEventRecord(ev[0], st));
   }
   if (flags & FE_ASSEMBLE_VALUES_FROM_DOFS) {
-    if (!dofs) return fail(FE_ERR_ARG, "fe_assemble: missing dofs");
+    if (!dofs && p->n_dof > 0) return fail(FE_ERR_ARG, "fe_assemble: missing dofs");
     long long n = p->n_nodes * p->nval;
     k_scatter_dofs<<<grid_for(n, 256, sms), 256, 0, st>>>(dofs, p->eqn.as<int>(), p->values.as<double>(), n);
     CUDA_TRY(cudaGetLastError());
@@ -1320,7 +1321,8 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
   const bool want_r = flags & FE_ASSEMBLE_RESIDUAL, want_j = flags & FE_ASSEMBLE_JACOBIAN;
   if (flags & ~(FE_ASSEMBLE_RESIDUAL | FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_VALUES_FROM_DOFS))
     return fail(FE_ERR_ARG, "fe_assemble_pipelined: residual and Jacobian flags only");
-  if ((want_r && !R) || (want_j && !J_vals) || ((flags & FE_ASSEMBLE_VALUES_FROM_DOFS) && !dofs))
+  if ((want_r && !R && p->n_dof > 0) || (want_j && !J_vals && p->nnz > 0) ||
+      ((flags & FE_ASSEMBLE_VALUES_FROM_DOFS) && !dofs && p->n_dof > 0))
     return fail(FE_ERR_ARG, "fe_assemble_pipelined: missing buffer");
   cudaStream_t st = (cudaStream_t)stream;
   int rc;
