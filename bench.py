@@ -544,7 +544,11 @@ def run_droplet(args):
         P.capture_assembly(with_jacobian=True)
         ms_graph = time_steps(torch, P.assemble_graph, args.steps, args.warmup)
         P.check()
-        res[prec] = dict(P=P, ms=ms, stage_ms=stage_ms, ms_e2e=ms_e2e, clocks=cs.summary(), ms_graph=ms_graph,
+        P.set_persistent(True)
+        ms_persistent = time_steps(torch, asm, args.steps, args.warmup)
+        P.set_persistent(False)
+        P.check()
+        res[prec] = dict(ms_persistent=ms_persistent, P=P, ms=ms, stage_ms=stage_ms, ms_e2e=ms_e2e, clocks=cs.summary(), ms_graph=ms_graph,
                          h2d=int(P.n_dof * 8), d2h=int(P.n_dof * 8 + P.nnz * P.J_dev.element_size()))
     peak64 = fp64_peak_tflops(torch)
     m = res["fp64"]
@@ -580,6 +584,7 @@ def run_droplet(args):
         "gpu_launches": P.launch_count(True) * args.steps,
         "clocks": m["clocks"],
         "cuda_graph": {"ms_per_step": m["ms_graph"], "value": n_elem / (m["ms_graph"] / 1e3), "launches_per_step": 1},
+        "persistent_fused_launch_ms_per_step": {"fp64": m["ms_persistent"], "fp32": res["fp32"]["ms_persistent"]},
         "launch_shape": {"threads": P.kernel.threads, "smem_bytes": P.kernel.smem_bytes,
                          "elems_per_block": [dc.epb for dc in P.domains], "autotuned": tuned or None},
     }

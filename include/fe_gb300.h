@@ -181,6 +181,11 @@ int fe_problem_set_positions(fe_problem_t *p, const double *x_host);
 /* Direction y (DEVICE dof vector, n_dof) of FE_ASSEMBLE_HVP assemblies. */
 int fe_problem_set_direction(fe_problem_t *p, const double *y, void *stream);
 
+/* Fused problems: launch the element kernel persistently (a grid of the
+ * blocks the SMs hold at once, striding over all domains' element blocks)
+ * instead of one block per element block.  Off by default. */
+int fe_problem_set_persistent(fe_problem_t *p, int enable);
+
 /* Parameter of the next FE_ASSEMBLE_DPARAM assembly (index into params). */
 int fe_problem_set_dparam(fe_problem_t *p, int index);
 

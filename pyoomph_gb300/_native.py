@@ -30,7 +30,8 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_residual_max_noalloc", "fe_residual_max_noalloc_limit", "fe_problem_element_buffers",
            "fe_problem_set_history", "fe_problem_shift_history", "fe_problem_set_positions",
            "fe_problem_graph_capture", "fe_problem_graph_launch", "fe_problem_set_dparam",
-           "fe_assemble_pipelined", "fe_csr_spmv", "fe_csr_diagonal", "fe_problem_set_direction"]
+           "fe_assemble_pipelined", "fe_csr_spmv", "fe_csr_diagonal", "fe_problem_set_direction",
+           "fe_problem_set_persistent"]
 
 
 def _header_stamp() -> str:
@@ -153,6 +154,7 @@ def load(build_if_missing: bool = True):
         L.fe_csr_spmv.argtypes = [vp, vp, vp, c_int, vp, vp, i64, vp]
         L.fe_csr_diagonal.argtypes = [vp, vp, vp, c_int, vp, i64, vp]
         L.fe_problem_set_direction.argtypes = [vp, vp, vp]
+        L.fe_problem_set_persistent.argtypes = [vp, c_int]
         L.fe_residual_max_noalloc_limit.restype = i64
         _lib = L
         return L

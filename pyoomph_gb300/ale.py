@@ -1185,6 +1185,12 @@ class DropletProblem:
     def check(self) -> None:
         N.check(N.load().fe_problem_check(self._h))
 
+    def set_persistent(self, enable: bool) -> None:
+        """Persistent fused launch (grid of resident blocks) or one block per
+        element block (default)."""
+        self.initialise()
+        N.check(N.load().fe_problem_set_persistent(self._h, int(enable)))
+
     def capture_assembly(self, with_jacobian: bool = True) -> None:
         """Record the assembly from x_dev into R_dev / J_dev as a CUDA graph
         (fe_problem_graph_capture); assemble_graph replays it."""

@@ -322,6 +322,7 @@ struct fe_problem {
   long long n_nodes = 0, n_dof = 0, nnz = 0;
   int n_params = 0, params_stride = 0, n_hist = 0, fused = 0, dparam = 0;
   int fused_grid_cap = 0; // resident blocks of the fused kernel (persistent launch)
+  int persistent = 0;
   std::vector<Domain> domains;
   DevBuf x, values, eqn, params, status, hist, x0, dir;
   long long n_hang = 0;
@@ -711,15 +712,16 @@ int launch_elements(fe_problem *p, int flag, cudaStream_t st) {
     fa.block_start[k] = nb;
     fa.n_domains = k;
     if (nb == 0) return FE_OK;
-    // persistent launch: as many blocks as the SMs hold at once (the kernel
-    // strides over the element blocks of all domains)
-    if (p->fused_grid_cap == 0) {
+    // persistent launch (optional): as many blocks as the SMs hold at once, the
+    // kernel striding over the element blocks of all domains; otherwise one
+    // block per element block (the stride loop then runs once)
+    if (p->persistent && p->fused_grid_cap == 0) {
       int per_sm = 1;
       CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)p->domains[0].code->func, threads,
                                                              (size_t)smem));
       p->fused_grid_cap = std::max(1, per_sm) * sm_count_cached();
     }
-    const int grid = std::min(nb, p->fused_grid_cap);
+    const int grid = p->persistent ? std::min(nb, p->fused_grid_cap) : nb;
     void *kp[] = {&fa};
     CUDA_TRY(cudaLaunchKernel((const void *)p->domains[0].code->func, dim3(grid), dim3(threads), kp, (size_t)smem, st));
     return FE_OK;
@@ -1407,6 +1409,12 @@ int fe_problem_set_direction(fe_problem_t *p, const double *y, void *stream) {
   CUDA_TRY(cudaMemsetAsync(p->dir.p, 0, sizeof(double) * n, st)); // pinned values: zero direction
   k_scatter_dofs<<<grid_for(n, 256, sm_count_cached()), 256, 0, st>>>(y, p->eqn.as<int>(), p->dir.as<double>(), n);
   CUDA_TRY(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_problem_set_persistent(fe_problem_t *p, int enable) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  p->persistent = enable != 0;
   return FE_OK;
 }
 
