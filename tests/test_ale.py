@@ -318,3 +318,17 @@ def test_gpu_mass_matrix_and_parameter_derivatives_match_oracle():
     R, J = P.get_jacobian()
     Ro, orp, oci, ov = A.assemble(D, v, [h0, h1], p)
     assert np.max(np.abs(J.data - ov)) <= 1e-12 * np.max(np.abs(ov))
+
+
+@pytest.mark.gpu
+def test_gpu_persistent_fused_launch_gives_identical_results():
+    P = _gpu_problem(9, 100.0)
+    D = A.droplet(9)
+    v, h0, h1 = _state(D, 13)
+    P.set_params(__bdf0=1500.0, __bdf1=-2000.0, __bdf2=500.0)
+    P.set_state(v, [h0, h1])
+    R1, J1 = P.get_jacobian()
+    P.set_persistent(True)
+    R2, J2 = P.get_jacobian()
+    P.set_persistent(False)
+    assert np.array_equal(R1, R2) and np.array_equal(J1.data, J2.data)
