@@ -65,7 +65,8 @@ def run_serving(args):
         wall = time.perf_counter() - t0
         sm = S.summary(done, wall)
         sm.update(wall_s=wall, assemblies=srv.assemblies, gpu_launches=srv.launches,
-                  mean_solve_s=srv.t_solve / max(1, sum(r.newton_iterations for r in done)))
+                  mean_solve_s=srv.t_solve / max(1, sum(r.newton_iterations for r in done)),
+                  device_solves=srv.device_solves)
         per_rate[str(rate)] = sm
         if rate == rates[0]:
             results["batched"] = {r.rid: r.dofs for r in done}
@@ -84,7 +85,9 @@ def run_serving(args):
             "dtype": "f64 residual, f32 Jacobian", "data": "synthetic",
             "config": {"workload": WORKLOADS["serving"][0], "requests": args.requests, "rates_per_s": rates,
                        "headline_rate_per_s": rates[min(1, len(rates) - 1)], "side_range": [16, args.size],
-                       "slots_per_class": 4, "linear_solver": f"SuperLU (scipy), {workers} worker processes"},
+                       "slots_per_class": 4,
+                       "linear_solver": f"Poisson: BiCGStab on the device; Navier-Stokes: SuperLU (scipy), "
+                                        f"{workers} worker processes"},
             "batched_fp32_by_rate": per_rate, "sequential_fp64_at_first_rate": s_,
             "max_rel_solution_difference_batched_vs_sequential": err,
             "gpu_launches": sum(v["gpu_launches"] for v in per_rate.values())}

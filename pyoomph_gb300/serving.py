@@ -159,6 +159,11 @@ class _Batch:
         np.ndarray((self.nnz,), dtype=np.int32, buffer=self.shm.buf, offset=4 * (self.n_dof + 1))[:] = ci[:self.nnz]
         self.x0 = P.get_dofs()[:self.n_dof].copy()
         self.last_used = time.perf_counter()
+        # one replica's CSR pattern on the device (every replica has the same
+        # block): the device solver works on a replica's block alone
+        import torch
+        self.rp_dev = torch.as_tensor(self.rp0, device="cuda")
+        self.ci_dev = torch.as_tensor(self.ci0, device="cuda")
 
     def free_slot(self) -> int:
         for s, r in enumerate(self.req):
@@ -183,7 +188,7 @@ class Server:
     assemblies are served by one launch sequence for all its replicas."""
 
     def __init__(self, slots: int = 4, jacobian_precision: str = "fp32", tol: float = 1e-10,
-                 max_newton: int = 20, workers: int = 8, hbm_reserve: float = 0.1):
+                 max_newton: int = 20, workers: int = 8, hbm_reserve: float = 0.1, device_solver: bool = True):
         import torch
         self.torch = torch
         self.slots = slots
@@ -194,6 +199,11 @@ class Server:
         # linear solves in worker processes (spawned: safe after CUDA init)
         self.pool = cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn"))
         self.hbm_reserve = hbm_reserve
+        # Poisson requests: J dx = R by BiCGStab on the device (per replica
+        # block, so a request's iterates never depend on its neighbours);
+        # Navier-Stokes (saddle point) requests: SuperLU in the workers
+        self.device_solver = device_solver
+        self.device_solves = 0
         self.batches: Dict[tuple, _Batch] = {}
         self.launches = 0
         self.assemblies = 0
@@ -270,6 +280,18 @@ class Server:
                 b.state[s] = "free"
                 done.append(req)
                 continue
+            if self.device_solver and b.key[0] == "poisson":
+                from .linsolve import DeviceCSR, bicgstab
+                ts = time.perf_counter()
+                with torch.cuda.stream(b.stream):
+                    A = DeviceCSR(b.rp_dev.data_ptr(), b.ci_dev.data_ptr(),
+                                  P.J_dev[s * b.nnz:(s + 1) * b.nnz], b.n_dof)
+                    dx, _ = bicgstab(A, P.R_dev[s * b.n_dof:(s + 1) * b.n_dof], tol=1e-13)
+                    P.x_dev[s * b.n_dof:(s + 1) * b.n_dof] -= dx
+                self.t_solve += time.perf_counter() - ts
+                self.device_solves += 1
+                req.newton_iterations += 1
+                continue                              # stays "assemble": next round re-assembles
             b.state[s] = "solving"
             futs[self.pool.submit(_splu_solve, b.shm.name, J[s], R[s])] = (b, s, time.perf_counter())
         b.last_used = time.perf_counter()
