@@ -154,6 +154,8 @@ class _Batch:
         self.n_dof = P.n_dof // slots
         self.nnz = P.nnz // slots
         rp, ci = P.pattern()
+        self.rp0 = np.ascontiguousarray(rp[:self.n_dof + 1], dtype=np.int32)
+        self.ci0 = np.ascontiguousarray(ci[:self.nnz], dtype=np.int32)
         self.shm = shared_memory.SharedMemory(create=True, size=4 * (self.n_dof + 1 + self.nnz))
         np.ndarray((self.n_dof + 1,), dtype=np.int32, buffer=self.shm.buf)[:] = rp[:self.n_dof + 1]
         np.ndarray((self.nnz,), dtype=np.int32, buffer=self.shm.buf, offset=4 * (self.n_dof + 1))[:] = ci[:self.nnz]
