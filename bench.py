@@ -86,8 +86,7 @@ def run_serving(args):
             "config": {"workload": WORKLOADS["serving"][0], "requests": args.requests, "rates_per_s": rates,
                        "headline_rate_per_s": rates[min(1, len(rates) - 1)], "side_range": [16, args.size],
                        "slots_per_class": 4,
-                       "linear_solver": f"Poisson: BiCGStab on the device; Navier-Stokes: SuperLU (scipy), "
-                                        f"{workers} worker processes"},
+                       "linear_solver": f"SuperLU (scipy), {workers} worker processes"},
             "batched_fp32_by_rate": per_rate, "sequential_fp64_at_first_rate": s_,
             "max_rel_solution_difference_batched_vs_sequential": err,
             "gpu_launches": sum(v["gpu_launches"] for v in per_rate.values())}

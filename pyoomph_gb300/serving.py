@@ -190,7 +190,7 @@ class Server:
     assemblies are served by one launch sequence for all its replicas."""
 
     def __init__(self, slots: int = 4, jacobian_precision: str = "fp32", tol: float = 1e-10,
-                 max_newton: int = 20, workers: int = 8, hbm_reserve: float = 0.1, device_solver: bool = True):
+                 max_newton: int = 20, workers: int = 8, hbm_reserve: float = 0.1, device_solver: bool = False):
         import torch
         self.torch = torch
         self.slots = slots
@@ -201,9 +201,11 @@ class Server:
         # linear solves in worker processes (spawned: safe after CUDA init)
         self.pool = cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn"))
         self.hbm_reserve = hbm_reserve
-        # Poisson requests: J dx = R by BiCGStab on the device (per replica
-        # block, so a request's iterates never depend on its neighbours);
-        # Navier-Stokes (saddle point) requests: SuperLU in the workers
+        # device_solver: Poisson requests solve J dx = R by BiCGStab on the
+        # device (per replica block, so a request's iterates never depend on
+        # its neighbours) instead of SuperLU in the workers.  Off by default:
+        # the Krylov solves run on the serving thread and delay every other
+        # request's assembly (measured: p50 at 20 requests/s 0.14 s -> 5.9 s)
         self.device_solver = device_solver
         self.device_solves = 0
         self.batches: Dict[tuple, _Batch] = {}

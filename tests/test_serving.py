@@ -50,3 +50,17 @@ def test_stream_summary_and_sequential_path_agree():
         assert np.max(np.abs(r.dofs - sb[r.rid].dofs)) <= 1e-10 * max(1.0, np.max(np.abs(r.dofs)))
     s = S.summary(bat, max(r.t_done for r in bat))
     assert s["p50_s"] is not None and s["p99_s"] >= s["p50_s"] and s["errors"] == 0
+
+
+def test_device_solver_option_gives_the_same_solutions():
+    from pyoomph_gb300 import serving as S
+    mix = [S.Request(1, "poisson", 10, 0.0, seed=1), S.Request(2, "ns", 8, 0.0, seed=2, Re=30.0),
+           S.Request(3, "poisson", 10, 0.0, seed=3)]
+    srv = S.Server(slots=2, tol=1e-12, device_solver=True)
+    out = {r.rid: r for r in srv.run(mix, realtime=False)}
+    srv.close()
+    assert srv.device_solves > 0
+    for r in out.values():
+        assert r.error is None
+        x = _oracle_solution(r)
+        assert np.max(np.abs(r.dofs - x)) <= 1e-10 * max(1.0, np.max(np.abs(x)))
