@@ -59,12 +59,12 @@ def run_serving(args):
     results = {}
     for rate in rates:
         reqs = S.make_stream(args.requests, rate=rate, seed=0, side_range=(16, args.size))
-        srv = S.Server(slots=4, jacobian_precision="fp32", workers=workers)
+        srv = S.Server(slots=4, jacobian_precision="fp32", workers=workers, device_solver=args.device_solver)
         t0 = time.perf_counter()
         done = srv.run(copy.deepcopy(reqs))
         wall = time.perf_counter() - t0
         sm = S.summary(done, wall)
-        sm.update(wall_s=wall, assemblies=srv.assemblies, gpu_launches=srv.launches,
+        sm.update(wall_s=wall, assemblies=srv.assemblies, gpu_launches=srv.launches + srv.solver_launches,
                   mean_solve_s=srv.t_solve / max(1, sum(r.newton_iterations for r in done)),
                   device_solves=srv.device_solves)
         per_rate[str(rate)] = sm
@@ -86,7 +86,9 @@ def run_serving(args):
             "config": {"workload": WORKLOADS["serving"][0], "requests": args.requests, "rates_per_s": rates,
                        "headline_rate_per_s": rates[min(1, len(rates) - 1)], "side_range": [16, args.size],
                        "slots_per_class": 4,
-                       "linear_solver": f"SuperLU (scipy), {workers} worker processes"},
+                       "linear_solver": (f"Poisson: native batched BiCGStab on the device; Navier-Stokes: SuperLU "
+                                         f"(scipy), {workers} worker processes") if args.device_solver else
+                                        f"SuperLU (scipy), {workers} worker processes"},
             "batched_fp32_by_rate": per_rate, "sequential_fp64_at_first_rate": s_,
             "max_rel_solution_difference_batched_vs_sequential": err,
             "gpu_launches": sum(v["gpu_launches"] for v in per_rate.values())}
@@ -398,11 +400,46 @@ def run_gb300(args):
             t0 = time.perf_counter()
             hist = PN.solve()
             torch.cuda.synchronize()
+            t_solve = time.perf_counter() - t0
+            kinfo = PN._krylov.info()
+            # the CSR SpMV alone on the converged Jacobian: algorithmic bytes =
+            # values + column indices + row pointers + x + y, once
+            from pyoomph_gb300.linsolve import DeviceCSR
+            A = DeviceCSR.of_problem(PN)
+            xs = torch.ones(PN.n_dof, dtype=torch.float64, device="cuda")
+            ys = torch.empty_like(xs)
+            st = torch.cuda.current_stream().cuda_stream
+
+            def time_spmv(fn, reps=20):
+                for _ in range(3):
+                    fn()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    fn()
+                e1.record()
+                torch.cuda.synchronize()
+                return e0.elapsed_time(e1) / reps
+            spmv_ms = time_spmv(lambda: PN._krylov.matvec(xs, ys))          # the solver's tiled kernel
+            spmv_rows_ms = time_spmv(lambda: A.matvec(xs, ys, st))           # fe_csr_spmv (lane group per row)
+            jb = 8 if prec == "fp64" else 4
+            spmv_bytes = PN.nnz * (jb + 4) + (PN.n_dof + 1) * 4 + 2 * PN.n_dof * 8
+            kits = PN.timings.get("krylov_iterations") or 0
             line.setdefault("newton_device_solve", {})[prec] = {
-                "s": time.perf_counter() - t0, "n_dof": PN.n_dof, "newton_iterations": len(hist) - 1,
-                "krylov_iterations": PN.timings.get("krylov_iterations"), "residuals": hist,
-                "linear_solver": "BiCGStab + Jacobi on the device (fe_csr_spmv)"}
-            del PN
+                "s": t_solve, "n_dof": PN.n_dof, "newton_iterations": len(hist) - 1,
+                "krylov_iterations": kits, "residuals": hist,
+                "linear_solve_s": PN.timings.get("newton_linear_solve_s"),
+                "ms_per_krylov_iteration": (1e3 * PN.timings["newton_linear_solve_s"] / kits) if kits else None,
+                "solver_launches": kinfo["launches"], "solver_graph_replays": kinfo["graph_replays"],
+                "spmv": {"kernel": "k_csr_spmv_tiled (fe_krylov_matvec)", "ms": spmv_ms,
+                         "algorithmic_bytes": spmv_bytes, "gbs": spmv_bytes / spmv_ms / 1e6,
+                         "row_group_kernel_ms": spmv_rows_ms,
+                         "frac_of_hbm": spmv_bytes / spmv_ms / 1e6 / hbm_peak if hbm_peak else None,
+                         "l2": "matrix > L2 (streamed once per product)" if spmv_bytes > 129e6 else
+                               "matrix fits in L2 (warm repeats)"},
+                "linear_solver": "native batched Jacobi-BiCGStab (fe_krylov_solve: fe_csr_spmv + fused "
+                                 "vector kernels, CUDA-graph blocks of 8 iterations)"}
+            del PN, A
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, threads=1)
     if rank == 0:
@@ -673,6 +710,8 @@ def main():
     ap.add_argument("--autotune", action="store_true", help="time the element kernels' launch shapes first")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--rates", default="10,20,50")
+    ap.add_argument("--device-solver", action="store_true",
+                    help="serving: solve the Poisson requests' Newton systems on the device")
     args = ap.parse_args()
     if args.size is None:
         args.size = WORKLOADS[args.workload][1]

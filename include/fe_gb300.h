@@ -43,7 +43,8 @@ enum {
   FE_ERR_NOMEM = 4,   /* device or host allocation refused */
   FE_ERR_STATE = 5,   /* call out of order */
   FE_ERR_DEVICE = 6,  /* a kernel reported an error in its status word */
-  FE_ERR_NOGPU = 7    /* no usable CUDA device */
+  FE_ERR_NOGPU = 7,   /* no usable CUDA device */
+  FE_ERR_SOLVER = 8   /* linear solver: not applicable, broke down or did not converge */
 };
 
 /* flags of fe_assemble */
@@ -240,13 +241,55 @@ int fe_assemble_host(fe_problem_t *p, const double *dofs, double *R, void *J_val
  * no counterpart on its assembly path).  DEVICE pointers: CSR rowptr/colidx
  * (the problem's resident pattern, fe_problem_pattern_device), values in
  * FE_JAC_F64 / FE_JAC_F32, FP64 vectors of length n.
- *   fe_csr_spmv:     y = A x
+ *   fe_csr_spmv:     y = A x; nnz = rowptr[n] (host copy): 4 lanes share
+ *                    a row (32 when rows average over 128 entries), one
+ *                    FMA per stored entry; the summation order depends only
+ *                    on the row and that choice
  *   fe_csr_diagonal: diag[i] = A(i, i)
  */
 int fe_csr_spmv(const int32_t *rowptr, const int32_t *colidx, const void *vals, int val_precision, const double *x,
-                double *y, int64_t n, void *stream);
+                double *y, int64_t n, int64_t nnz, void *stream);
 int fe_csr_diagonal(const int32_t *rowptr, const int32_t *colidx, const void *vals, int val_precision, double *diag,
                     int64_t n, void *stream);
+
+/*
+ * Batched device Newton linear solve: Jacobi-preconditioned BiCGStab on the
+ * `blocks` diagonal blocks of a stacked CSR matrix (block s owns rows
+ * s*n/blocks .. (s+1)*n/blocks and couples only to them: the replicas of a
+ * problem; blocks = 1 for one system).  Replaces the host SuperLU solve of
+ * the reference's Newton step (pyoomph/solvers/scipy.py,
+ * src/pybind/solver.cpp:105) for diffusion-type Jacobians.
+ *
+ * Every scalar and every reduction is per block, the reductions run over
+ * fixed chunks of a block's rows in a fixed order, and a block stops at the
+ * iteration its own residual reaches tol * ||b_s||_inf: a block's solution
+ * is bit-identical whatever the other blocks hold.  Iterations run on the
+ * solver's own stream (ordered after and before `stream` by events), in
+ * blocks of check_every iterations replayed as one CUDA graph (use_graph);
+ * the host reads the per-block state words between blocks.  A converged
+ * block is confirmed by its true residual (<= 10 * target, else it
+ * restarts); a breakdown restores the block's iterate from the last check
+ * and restarts it (at most max_restarts times).
+ *
+ * create: DEVICE rowptr/colidx/vals stay owned by the caller and must stay
+ *         valid (values may change between solves).
+ * solve:  DEVICE b (n) and x (n, written for every block: inactive blocks
+ *         get 0); HOST active[blocks] (NULL = all) and iterations[blocks]
+ *         (may be NULL).  FE_ERR_SOLVER for a zero diagonal entry in an
+ *         active block (saddle-point systems), a non-finite right-hand
+ *         side, repeated breakdown or no convergence in maxiter.
+ */
+typedef struct fe_krylov fe_krylov_t;
+int fe_krylov_create(const int32_t *rowptr, const int32_t *colidx, const void *vals, int val_precision, int64_t n,
+                     int64_t nnz, int32_t blocks, int32_t check_every, int32_t use_graph, fe_krylov_t **out);
+int fe_krylov_solve(fe_krylov_t *k, const double *b, const uint8_t *active, double tol, int64_t maxiter,
+                    int32_t max_restarts, double *x, int64_t *iterations, void *stream);
+/* y = A x (every row, DEVICE vectors of n) with the solver's matrix and
+ * SpMV kernel (that of fe_csr_spmv).  Ordered on `stream`. */
+int fe_krylov_matvec(fe_krylov_t *k, const double *x, double *y, void *stream);
+/* kernel launches (graph nodes included), graph replays, restarts so far. */
+int fe_krylov_info(const fe_krylov_t *k, int64_t *launches, int64_t *graph_replays, int64_t *restarts);
+void fe_krylov_destroy(fe_krylov_t *k);
 
 /* max |R| over n entries of a device vector, NaN -> +inf; result to host. */
 int fe_residual_max(fe_problem_t *p, const double *R, int64_t n, double *out, void *stream);

@@ -11,7 +11,8 @@ import threading
 
 from . import build as _build
 
-FE_OK, FE_ERR_ARG, FE_ERR_CUDA, FE_ERR_COMPILE, FE_ERR_NOMEM, FE_ERR_STATE, FE_ERR_DEVICE, FE_ERR_NOGPU = range(8)
+(FE_OK, FE_ERR_ARG, FE_ERR_CUDA, FE_ERR_COMPILE, FE_ERR_NOMEM, FE_ERR_STATE, FE_ERR_DEVICE, FE_ERR_NOGPU,
+ FE_ERR_SOLVER) = range(9)
 FE_ASSEMBLE_RESIDUAL, FE_ASSEMBLE_JACOBIAN, FE_ASSEMBLE_VALUES_FROM_DOFS = 1, 2, 4
 FE_ASSEMBLE_MASS, FE_ASSEMBLE_DPARAM, FE_ASSEMBLE_HVP = 8, 16, 32
 FE_JAC_F64, FE_JAC_F32 = 0, 1
@@ -30,7 +31,8 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_residual_max_noalloc", "fe_residual_max_noalloc_limit", "fe_problem_element_buffers",
            "fe_problem_set_history", "fe_problem_shift_history", "fe_problem_set_positions",
            "fe_problem_graph_capture", "fe_problem_graph_launch", "fe_problem_set_dparam",
-           "fe_assemble_pipelined", "fe_csr_spmv", "fe_csr_diagonal", "fe_problem_set_direction",
+           "fe_assemble_pipelined", "fe_csr_spmv", "fe_csr_diagonal", "fe_krylov_create", "fe_krylov_solve",
+           "fe_krylov_matvec", "fe_krylov_info", "fe_krylov_destroy", "fe_problem_set_direction",
            "fe_problem_set_persistent"]
 
 
@@ -151,8 +153,14 @@ def load(build_if_missing: bool = True):
         L.fe_problem_graph_launch.argtypes = [vp, vp]
         L.fe_problem_set_dparam.argtypes = [vp, c_int]
         L.fe_assemble_pipelined.argtypes = [vp, vp, vp, vp, c_int, c_int, vp]
-        L.fe_csr_spmv.argtypes = [vp, vp, vp, c_int, vp, vp, i64, vp]
+        L.fe_csr_spmv.argtypes = [vp, vp, vp, c_int, vp, vp, i64, i64, vp]
         L.fe_csr_diagonal.argtypes = [vp, vp, vp, c_int, vp, i64, vp]
+        L.fe_krylov_create.argtypes = [vp, vp, vp, c_int, i64, i64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, vp]
+        L.fe_krylov_solve.argtypes = [vp, vp, vp, ctypes.c_double, i64, ctypes.c_int32, vp, vp, vp]
+        L.fe_krylov_info.argtypes = [vp, vp, vp, vp]
+        L.fe_krylov_matvec.argtypes = [vp, vp, vp, vp]
+        L.fe_krylov_destroy.argtypes = [vp]
+        L.fe_krylov_destroy.restype = None
         L.fe_problem_set_direction.argtypes = [vp, vp, vp]
         L.fe_problem_set_persistent.argtypes = [vp, c_int]
         L.fe_residual_max_noalloc_limit.restype = i64

@@ -217,18 +217,67 @@ __global__ void k_dof_update(double *__restrict__ x, const double *__restrict__ 
 // y = A x for a CSR matrix (FP64 or FP32 values, FP64 vectors): one warp
 // per row, lanes stride the row, a fixed shuffle tree sums them
 // (deterministic).  The Krylov solver of the device Newton path calls it.
-template <typename T>
-__global__ void k_csr_spmv(const int *__restrict__ rowptr, const int *__restrict__ colidx, const T *__restrict__ vals,
-                           const double *__restrict__ x, double *__restrict__ y, long long n) {
-  const int lane = threadIdx.x & 31;
-  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += nw) {
-    double acc = 0.0;
+// FP32 -> FP64 by integer operations (exact: binary32 -> binary64 moves the
+// sign, rebiases the exponent by 1023 - 127 = 896 and shifts the fraction by
+// 29 bits).  On GB300 the FP64 pipe bounds the SpMV, and the conversion
+// instruction would occupy it once per stored value; the integer pipe is
+// idle.  Zeros keep their sign; subnormal, infinite and NaN inputs take the
+// ordinary conversion.
+__device__ __forceinline__ double fe_widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  if (e - 1u < 254u)
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 896u) << 52) |
+                                            ((unsigned long long)(u & 0x7fffffu) << 29)));
+  if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)sign);
+  return (double)f;
+}
+__device__ __forceinline__ double fe_widen(double d) { return d; }
+
+// y = A x with L lanes per row.  GB300 issues FP64 at ~1/64 of the FP32
+// rate, so the kernel is shaped to spend one FMA per stored entry and as
+// little else as possible on the FP64 pipe: L = 4 lanes per row (a lane
+// group's load of 4 consecutive entries fills a 32-byte sector for FP64
+// values) accumulate with FMAs into two partial sums, and only log2(L) = 2
+// adds per lane fold the group (a 32-lane group would spend 5 adds on every
+// lane for every row, more than the row's own FMAs).  The matrix streams
+// through once (evict-first loads), x stays in L2; four entries per lane
+// are loaded before they are used.  Rows are assigned to lane groups in a
+// grid-stride loop; a group's lanes share the row, so the shuffle mask is
+// the group's own lanes.  With bstate, only the rows of diagonal blocks (of
+// nb rows) whose state word is `want` are computed (the batched solver skips
+// blocks that stopped).  The summation order depends on the row alone.
+template <typename T, int L>
+__global__ void __launch_bounds__(256) k_csr_spmv(const int *__restrict__ rowptr, const int *__restrict__ colidx,
+                                                  const T *__restrict__ vals, const double *__restrict__ x,
+                                                  double *__restrict__ y, long long n,
+                                                  const int *__restrict__ bstate = nullptr, int want = 0,
+                                                  long long nb = 1) {
+  const int sub = threadIdx.x & (L - 1);
+  const unsigned gmask = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << ((threadIdx.x & 31) & ~(L - 1)));
+  const long long ng = ((long long)gridDim.x * blockDim.x) / L;
+  for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / L; r < n; r += ng) {
+    if (bstate && bstate[r / nb] != want) continue;
     const int e = rowptr[r + 1];
-    for (int k = rowptr[r] + lane; k < e; k += 32) acc += (double)vals[k] * x[colidx[k]];
+    int k = rowptr[r] + sub;
+    double a0 = 0.0, a1 = 0.0;
+    for (; k + 3 * L < e; k += 4 * L) {
+      const T v0 = __ldcs(vals + k), v1 = __ldcs(vals + k + L), v2 = __ldcs(vals + k + 2 * L),
+              v3 = __ldcs(vals + k + 3 * L);
+      const int c0 = __ldcs(colidx + k), c1 = __ldcs(colidx + k + L), c2 = __ldcs(colidx + k + 2 * L),
+                c3 = __ldcs(colidx + k + 3 * L);
+      const double x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
+      a0 = fma(fe_widen(v0), x0, a0);
+      a1 = fma(fe_widen(v1), x1, a1);
+      a0 = fma(fe_widen(v2), x2, a0);
+      a1 = fma(fe_widen(v3), x3, a1);
+    }
+    for (; k < e; k += L) a0 = fma(fe_widen(__ldcs(vals + k)), x[__ldcs(colidx + k)], a0);
+    double acc = a0 + a1;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) y[r] = acc;
+    for (int o = L / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o);
+    if (sub == 0) y[r] = acc;
   }
 }
 
@@ -249,6 +298,28 @@ int grid_for(long long n, int threads, int sms) {
   if (g > cap) g = cap;
   if (g < 1) g = 1;
   return (int)g;
+}
+
+int sm_count_cached();
+
+// y = A x (rows of blocks whose state word is `want` only, with bstate):
+// 4 lanes per row (32 for rows averaging over 128 entries), so the
+// summation order depends only on the row and that choice.
+void launch_csr_spmv(const int *rowptr, const int *colidx, const void *vals, int prec, const double *x, double *y,
+                     long long n, long long nnz, const int *bstate, int want, long long nb, cudaStream_t st) {
+  const int L = (double)nnz > 128.0 * (double)n ? 32 : 4;
+  const int g = grid_for(n * L, 256, sm_count_cached());
+#define FE_SPMV_LAUNCH(T)                                                                                      \
+  if (L == 4)                                                                                                  \
+    k_csr_spmv<T, 4><<<g, 256, 0, st>>>(rowptr, colidx, (const T *)vals, x, y, n, bstate, want, nb);           \
+  else                                                                                                         \
+    k_csr_spmv<T, 32><<<g, 256, 0, st>>>(rowptr, colidx, (const T *)vals, x, y, n, bstate, want, nb);
+  if (prec == FE_JAC_F64) {
+    FE_SPMV_LAUNCH(double)
+  } else {
+    FE_SPMV_LAUNCH(float)
+  }
+#undef FE_SPMV_LAUNCH
 }
 
 // ---------------------------------------------------------------------------
@@ -1515,15 +1586,10 @@ int fe_residual_max_noalloc(const double *R, int64_t n, double *out, void *strea
 int64_t fe_residual_max_noalloc_limit(void) { return (int64_t)FE_NOALLOC_MAX_N; }
 
 int fe_csr_spmv(const int32_t *rowptr, const int32_t *colidx, const void *vals, int val_precision, const double *x,
-                double *y, int64_t n, void *stream) {
+                double *y, int64_t n, int64_t nnz, void *stream) {
   if (n <= 0) return FE_OK;
-  if (!rowptr || !colidx || !vals || !x || !y) return fail(FE_ERR_ARG, "fe_csr_spmv: null argument");
-  const int sms = sm_count_cached();
-  const int g = grid_for(n * 32, 256, sms);
-  if (val_precision == FE_JAC_F64)
-    k_csr_spmv<double><<<g, 256, 0, (cudaStream_t)stream>>>(rowptr, colidx, (const double *)vals, x, y, n);
-  else
-    k_csr_spmv<float><<<g, 256, 0, (cudaStream_t)stream>>>(rowptr, colidx, (const float *)vals, x, y, n);
+  if (!rowptr || !colidx || !vals || !x || !y || nnz < 0) return fail(FE_ERR_ARG, "fe_csr_spmv: null argument");
+  launch_csr_spmv(rowptr, colidx, vals, val_precision, x, y, n, nnz, nullptr, 0, 1, (cudaStream_t)stream);
   CUDA_TRY(cudaGetLastError());
   return FE_OK;
 }
@@ -1589,3 +1655,5 @@ int fe_problem_launch_count(const fe_problem_t *p, int flags) {
 }
 
 } // extern "C"
+
+#include "fe_krylov.cuh"

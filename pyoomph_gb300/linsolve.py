@@ -4,21 +4,33 @@ resident CSR Jacobian.
 The reference solves J dx = R on the host with SuperLU
 (``pyoomph/solvers/scipy.py``, ``src/pybind/solver.cpp:105``), which needs
 the Jacobian copied to the host every Newton step and dominates the solve
-time at large sizes.  Here the Jacobian never leaves the device: the
-matrix-vector products run in the library's CSR kernel (``fe_csr_spmv``, one
-warp per row) on the assembled values, the vector algebra in torch, and the
-only host synchronisation is the convergence check every few iterations.
+time at large sizes.  Here the Jacobian never leaves the device: the native
+solver (``fe_krylov_*`` in the C-ABI) runs the matrix-vector products in the
+library's CSR kernel (``fe_csr_spmv``: 4..32 lanes per row by the mean row
+length) on the assembled values and the vector algebra in its own fused
+kernels, replays blocks of iterations as one CUDA graph on its own stream,
+and synchronises with the host only at the convergence checks between
+blocks.
 
 BiCGStab (van der Vorst 1992) with the diagonal as right preconditioner
 suits the diffusion-type Jacobians of Poisson and nonlinear diffusion (also
 the non-symmetric ones); saddle-point systems with a zero diagonal block
 (Taylor-Hood Navier-Stokes) are rejected -- they keep the host SuperLU path.
+
+``BatchedBiCGStab`` iterates S independent diagonal blocks of one stacked
+matrix together (the replicas of a problem: block s owns rows s*n..(s+1)*n
+and couples only to them).  Every scalar is per block, every reduction runs
+over fixed chunks of one block's rows in a fixed order, and a block stops
+(its iterate frozen) at the iteration its own residual reaches the target,
+so a block's solution is bit-identical whatever slot it occupies and
+whatever the other blocks hold.
 """
 from __future__ import annotations
 
 import ctypes
 from dataclasses import dataclass
-from typing import Optional
+
+import numpy as np
 
 from . import _native as N
 
@@ -34,13 +46,14 @@ class DeviceCSR:
     colidx: int
     vals: "object"       # torch tensor on the device
     n: int
+    nnz: int
 
     @classmethod
     def of_problem(cls, P, vals=None) -> "DeviceCSR":
         rp = ctypes.c_void_p()
         ci = ctypes.c_void_p()
         N.check(N.load().fe_problem_pattern_device(P._h, ctypes.byref(rp), ctypes.byref(ci)))
-        return cls(rp.value, ci.value, P.J_dev if vals is None else vals, P.n_dof)
+        return cls(rp.value, ci.value, P.J_dev if vals is None else vals, P.n_dof, P.nnz)
 
     @property
     def precision(self) -> int:
@@ -51,7 +64,7 @@ class DeviceCSR:
         N.check(N.load().fe_csr_spmv(ctypes.c_void_p(self.rowptr), ctypes.c_void_p(self.colidx),
                                      ctypes.c_void_p(self.vals.data_ptr()), self.precision,
                                      ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()), self.n,
-                                     ctypes.c_void_p(stream)))
+                                     self.nnz, ctypes.c_void_p(stream)))
 
     def diagonal(self, out, stream) -> None:
         N.check(N.load().fe_csr_diagonal(ctypes.c_void_p(self.rowptr), ctypes.c_void_p(self.colidx),
@@ -59,84 +72,80 @@ class DeviceCSR:
                                          ctypes.c_void_p(out.data_ptr()), self.n, ctypes.c_void_p(stream)))
 
 
+class BatchedBiCGStab:
+    """The native batched solver (``fe_krylov_create`` / ``fe_krylov_solve``)
+    bound to a DeviceCSR whose values buffer stays in place (the values may
+    change between solves: the next Newton step's Jacobian)."""
+
+    def __init__(self, A: DeviceCSR, blocks: int = 1, check_every: int = 8, graph: bool = True):
+        import torch
+        if blocks < 1 or A.n % blocks:
+            raise ValueError(f"{A.n} rows do not split into {blocks} equal blocks")
+        self.torch = torch
+        self.A = A
+        self.S = blocks
+        self.n = A.n // blocks
+        self.check_every = int(check_every)
+        h = ctypes.c_void_p()
+        N.check(N.load().fe_krylov_create(ctypes.c_void_p(A.rowptr), ctypes.c_void_p(A.colidx),
+                                          ctypes.c_void_p(A.vals.data_ptr()), A.precision, A.n, A.nnz, blocks,
+                                          self.check_every, int(bool(graph)), ctypes.byref(h)))
+        self._h = h
+        self.x = torch.zeros((self.S, self.n), dtype=torch.float64, device=A.vals.device)
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                N.load().fe_krylov_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        N.check(N.load().fe_krylov_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"launches": a.value, "graph_replays": b.value, "restarts": c.value}
+
+    def matvec(self, x, y) -> None:
+        """y = A x with the solver's tiled SpMV, on the current stream."""
+        N.check(N.load().fe_krylov_matvec(self._h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                                          ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)))
+
+    @property
+    def graph_replays(self) -> int:
+        return self.info()["graph_replays"]
+
+    def solve(self, b, active=None, tol: float = 1e-13, maxiter: int = 20000, max_restarts: int = 20):
+        """Solve A_s x_s = b_s for the active blocks s (all by default); b is
+        the stacked right-hand side (S*n,) or (S, n) on the device.  Stops a
+        block when ||r_s||_inf <= tol * ||b_s||_inf.  Returns (x, iterations):
+        x the (S, n) result (inactive blocks hold 0), iterations per block
+        (multiples of check_every)."""
+        torch = self.torch
+        b = b.reshape(-1)
+        if b.numel() != self.S * self.n or b.dtype != torch.float64 or not b.is_contiguous():
+            raise ValueError("b must be a contiguous float64 vector of the matrix's size")
+        act = None
+        if active is not None:
+            act = np.ascontiguousarray(np.asarray(active, dtype=bool).astype(np.uint8))
+            if act.shape != (self.S,):
+                raise ValueError(f"active must have {self.S} entries")
+        its = np.zeros(self.S, dtype=np.int64)
+        rc = N.load().fe_krylov_solve(self._h, ctypes.c_void_p(b.data_ptr()),
+                                      None if act is None else act.ctypes.data_as(ctypes.c_void_p),
+                                      float(tol), int(maxiter), int(max_restarts),
+                                      ctypes.c_void_p(self.x.data_ptr()), its.ctypes.data_as(ctypes.c_void_p),
+                                      ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        if rc == N.FE_ERR_SOLVER:
+            raise LinearSolverError(N.load().fe_last_error().decode(errors="replace"))
+        N.check(rc)
+        return self.x, its
+
+
 def bicgstab(A: DeviceCSR, b, tol: float = 1e-13, maxiter: int = 20000, check_every: int = 8,
-             x0=None):
-    """Solve A x = b on the device; stop when ||b - A x||_inf <= tol *
-    ||b||_inf (checked every `check_every` iterations with the recursively
-    updated residual, confirmed with a true residual).  Returns (x,
-    iterations)."""
-    import torch
-    st = torch.cuda.current_stream().cuda_stream
-    n = A.n
-    dev = b.device
-    diag = torch.empty(n, dtype=torch.float64, device=dev)
-    A.diagonal(diag, st)
-    if bool((diag == 0).any()):
-        raise LinearSolverError("zero diagonal entry: Jacobi-preconditioned BiCGStab does not apply "
-                                "(saddle-point system); use the host solver")
-    minv = 1.0 / diag
-    x = torch.zeros(n, dtype=torch.float64, device=dev) if x0 is None else x0.clone()
-    r = b.clone()
-    if x0 is not None:
-        t = torch.empty_like(b)
-        A.matvec(x, t, st)
-        r -= t
-    bnorm = float(b.abs().max())
-    if bnorm == 0.0:
-        return x, 0
-    target = tol * bnorm
-    rhat = r.clone()
-    p = torch.zeros_like(r)
-    v = torch.zeros_like(r)
-    s = torch.empty_like(r)
-    t = torch.empty_like(r)
-    rho_old = torch.ones((), dtype=torch.float64, device=dev)
-    alpha = torch.ones((), dtype=torch.float64, device=dev)
-    omega = torch.ones((), dtype=torch.float64, device=dev)
-    x_good = x.clone()
-    restarts = 0
-
-    def restart():
-        # from the last checked iterate, with the true residual as shadow vector
-        nonlocal r, rhat, rho_old, alpha, omega
-        A.matvec(x, t, st)
-        r = b - t
-        rhat = r.clone()
-        p.zero_()
-        v.zero_()
-        rho_old = torch.ones((), dtype=torch.float64, device=dev)
-        alpha = torch.ones((), dtype=torch.float64, device=dev)
-        omega = torch.ones((), dtype=torch.float64, device=dev)
-
-    for it in range(1, maxiter + 1):
-        rho = torch.dot(rhat, r)
-        beta = (rho / rho_old) * (alpha / omega)
-        p.sub_(omega * v).mul_(beta).add_(r)
-        phat = p * minv
-        A.matvec(phat, v, st)
-        alpha = rho / torch.dot(rhat, v)
-        torch.sub(r, alpha * v, out=s)
-        shat = s * minv
-        A.matvec(shat, t, st)
-        omega = torch.dot(t, s) / torch.dot(t, t)
-        x.add_(alpha * phat).add_(omega * shat)
-        torch.sub(s, omega * t, out=r)
-        rho_old = rho
-        if it % check_every == 0:
-            rn = float(r.abs().max())
-            if not (rn == rn) or not bool(torch.isfinite(x).all()):
-                # breakdown (rho or omega ~ 0): back to the last good iterate and restart
-                restarts += 1
-                if restarts > 20:
-                    raise LinearSolverError(f"BiCGStab broke down repeatedly ({it} iterations)")
-                x.copy_(x_good)
-                restart()
-                continue
-            x_good.copy_(x)
-            if rn <= target:
-                A.matvec(x, t, st)
-                true = float((b - t).abs().max())
-                if true <= target * 10:
-                    return x, it
-                restart()
-    raise LinearSolverError(f"BiCGStab did not reach {tol} in {maxiter} iterations")
+             graph: bool = True):
+    """Solve A x = b on the device (one block); stop when ||b - A x||_inf <=
+    tol * ||b||_inf.  Returns (x, iterations)."""
+    solver = BatchedBiCGStab(A, 1, check_every=check_every, graph=graph)
+    x, its = solver.solve(b, tol=tol, maxiter=maxiter)
+    return x.view(-1).clone(), int(its[0])

@@ -340,6 +340,7 @@ class Problem:
         self.x_dev = torch.zeros(self.n_dof, dtype=torch.float64, device=dev)
         self.R_dev = torch.zeros(max(self.n_dof, 1), dtype=torch.float64, device=dev)
         self.J_dev = torch.zeros(max(self.nnz, 1), dtype=self._jdtype, device=dev)
+        self._krylov = None   # device linear solver state, bound to J_dev
         self.x_dev.copy_(torch.from_numpy(self._dofs_from_values(values)))
         t4 = time.perf_counter()
         self.timings.update(jit_s=t3 - t2, device_setup_s=t4 - t3)
@@ -620,10 +621,13 @@ class Problem:
             tb = time.perf_counter()
             with nvtx_range("linear solve"):
                 if device_solve:
-                    from .linsolve import DeviceCSR, bicgstab
-                    dxd, its = bicgstab(DeviceCSR.of_problem(self), self.R_dev[:self.n_dof],
-                                        tol=self.linear_solver_tolerance)
-                    self.timings["krylov_iterations"] = self.timings.get("krylov_iterations", 0) + its
+                    from .linsolve import BatchedBiCGStab, DeviceCSR
+                    if getattr(self, "_krylov", None) is None:
+                        # one block per replica: each replica's solve is its own
+                        self._krylov = BatchedBiCGStab(DeviceCSR.of_problem(self), blocks=self.replicas)
+                    dx2, its = self._krylov.solve(self.R_dev[:self.n_dof], tol=self.linear_solver_tolerance)
+                    dxd = dx2.view(-1)
+                    self.timings["krylov_iterations"] = self.timings.get("krylov_iterations", 0) + int(its.max())
                 else:
                     dx = self._solve_linear(R)
             tc = time.perf_counter()

@@ -18,7 +18,10 @@ next assembly.  The pending assemblies of a class are served by one launch
 sequence for all its replicas (dof scatter, element kernel, residual and
 Jacobian scatter) on the class's own CUDA stream, with the per-replica
 residual max-norms reduced on the device -- so the solves of all active
-requests run in parallel on the host cores while the GPU assembles.
+requests run in parallel on the host cores while the GPU assembles.  With
+``device_solver=True`` the Poisson requests of a class are solved on the
+device instead: one batched Jacobi-BiCGStab over the class's replicas
+(``linsolve.BatchedBiCGStab``, CUDA-graph blocks of iterations).
 
 Results do not depend on the mix: every element, CSR slot and residual
 entry of a replica is computed from that replica's values only, in a fixed
@@ -154,18 +157,12 @@ class _Batch:
         self.n_dof = P.n_dof // slots
         self.nnz = P.nnz // slots
         rp, ci = P.pattern()
-        self.rp0 = np.ascontiguousarray(rp[:self.n_dof + 1], dtype=np.int32)
-        self.ci0 = np.ascontiguousarray(ci[:self.nnz], dtype=np.int32)
         self.shm = shared_memory.SharedMemory(create=True, size=4 * (self.n_dof + 1 + self.nnz))
         np.ndarray((self.n_dof + 1,), dtype=np.int32, buffer=self.shm.buf)[:] = rp[:self.n_dof + 1]
         np.ndarray((self.nnz,), dtype=np.int32, buffer=self.shm.buf, offset=4 * (self.n_dof + 1))[:] = ci[:self.nnz]
         self.x0 = P.get_dofs()[:self.n_dof].copy()
         self.last_used = time.perf_counter()
-        # one replica's CSR pattern on the device (every replica has the same
-        # block): the device solver works on a replica's block alone
-        import torch
-        self.rp_dev = torch.as_tensor(self.rp0, device="cuda")
-        self.ci_dev = torch.as_tensor(self.ci0, device="cuda")
+        self.krylov = None      # device solver of the class (device_solver=True)
 
     def free_slot(self) -> int:
         for s, r in enumerate(self.req):
@@ -201,13 +198,13 @@ class Server:
         # linear solves in worker processes (spawned: safe after CUDA init)
         self.pool = cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn"))
         self.hbm_reserve = hbm_reserve
-        # device_solver: Poisson requests solve J dx = R by BiCGStab on the
-        # device (per replica block, so a request's iterates never depend on
-        # its neighbours) instead of SuperLU in the workers.  Off by default:
-        # the Krylov solves run on the serving thread and delay every other
-        # request's assembly (measured: p50 at 20 requests/s 0.14 s -> 5.9 s)
+        # device_solver: Poisson requests solve J dx = R on the device, one
+        # batched BiCGStab per class and round (a block per replica, so a
+        # request's iterates never depend on its neighbours), instead of
+        # SuperLU in the workers
         self.device_solver = device_solver
         self.device_solves = 0
+        self.solver_launches = 0      # kernel launches of the device solver
         self.batches: Dict[tuple, _Batch] = {}
         self.launches = 0
         self.assemblies = 0
@@ -263,6 +260,7 @@ class Server:
         torch = self.torch
         P = b.P
         done = []
+        dev_solve: List[int] = []
         with torch.cuda.stream(b.stream):
             P.assemble_device(with_jacobian=True, stream=b.stream.cuda_stream)
             self.launches += P.launch_count(True)
@@ -285,19 +283,29 @@ class Server:
                 done.append(req)
                 continue
             if self.device_solver and b.key[0] == "poisson":
-                from .linsolve import DeviceCSR, bicgstab
-                ts = time.perf_counter()
-                with torch.cuda.stream(b.stream):
-                    A = DeviceCSR(b.rp_dev.data_ptr(), b.ci_dev.data_ptr(),
-                                  P.J_dev[s * b.nnz:(s + 1) * b.nnz], b.n_dof)
-                    dx, _ = bicgstab(A, P.R_dev[s * b.n_dof:(s + 1) * b.n_dof], tol=1e-13)
-                    P.x_dev[s * b.n_dof:(s + 1) * b.n_dof] -= dx
-                self.t_solve += time.perf_counter() - ts
-                self.device_solves += 1
-                req.newton_iterations += 1
-                continue                              # stays "assemble": next round re-assembles
+                dev_solve.append(s)
+                continue
             b.state[s] = "solving"
             futs[self.pool.submit(_splu_solve, b.shm.name, J[s], R[s])] = (b, s, time.perf_counter())
+        if dev_solve:
+            # one batched BiCGStab for every replica that needs a step: one
+            # block per replica, each with its own scalars and stopping point
+            from .linsolve import BatchedBiCGStab, DeviceCSR
+            ts = time.perf_counter()
+            with torch.cuda.stream(b.stream):
+                if b.krylov is None:
+                    b.krylov = BatchedBiCGStab(DeviceCSR.of_problem(P), blocks=b.slots)
+                mask = np.zeros(b.slots, dtype=bool)
+                mask[dev_solve] = True
+                l0 = b.krylov.info()["launches"]
+                dx, _ = b.krylov.solve(P.R_dev[:P.n_dof], active=mask, tol=1e-13)
+                self.solver_launches += b.krylov.info()["launches"] - l0
+                xv = P.x_dev[:P.n_dof].view(b.slots, b.n_dof)
+                for s in dev_solve:
+                    xv[s] -= dx[s]
+                    b.req[s].newton_iterations += 1     # stays "assemble": re-assembled next round
+            self.t_solve += time.perf_counter() - ts
+            self.device_solves += len(dev_solve)
         b.last_used = time.perf_counter()
         return done
 

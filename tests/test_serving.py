@@ -52,14 +52,22 @@ def test_stream_summary_and_sequential_path_agree():
     assert s["p50_s"] is not None and s["p99_s"] >= s["p50_s"] and s["errors"] == 0
 
 
-def test_device_solver_option_gives_the_same_solutions():
+def test_device_solver_alone_equals_mix_and_matches_oracle():
+    """Poisson requests solved on the device (one batched BiCGStab per class
+    round): a request's dofs are bit-identical alone or in a mix, and every
+    request converges to the oracle's solution within 1e-10."""
     from pyoomph_gb300 import serving as S
+    srv = S.Server(slots=3, tol=1e-12, device_solver=True)
+    alone = srv.run([S.Request(0, "poisson", 10, 0.0, seed=7)], realtime=False)[0]
+    srv.close()
+    assert alone.error is None, alone.error
     mix = [S.Request(1, "poisson", 10, 0.0, seed=1), S.Request(2, "ns", 8, 0.0, seed=2, Re=30.0),
-           S.Request(3, "poisson", 10, 0.0, seed=3)]
-    srv = S.Server(slots=2, tol=1e-12, device_solver=True)
+           S.Request(0, "poisson", 10, 0.0, seed=7), S.Request(3, "poisson", 10, 0.0, seed=3)]
+    srv = S.Server(slots=3, tol=1e-12, device_solver=True)
     out = {r.rid: r for r in srv.run(mix, realtime=False)}
     srv.close()
     assert srv.device_solves > 0
+    assert np.array_equal(out[0].dofs, alone.dofs)
     for r in out.values():
         assert r.error is None
         x = _oracle_solution(r)
