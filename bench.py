@@ -253,7 +253,7 @@ def run_gb300(args):
     hbm_peak, peak_kind = _peaks()
     results = {}
     tuned = {}
-    for prec in ("fp64", "fp32"):
+    for prec in ("fp64", "fp32", "df64"):
         epb = None
         if args.autotune:
             from pyoomph_gb300 import autotune as AT
@@ -381,6 +381,28 @@ def run_gb300(args):
                                      "h2d_bytes_per_step": r32["h2d"], "d2h_bytes_per_step": r32["d2h"]},
                              "cuda_graph_ms_per_step": r32["ms_graph"],
                              "elems_per_block": r32["P"].kernel.epb}
+    rdf = results["df64"]
+    fdf = estimate_flops(rdf["P"].kernel, rdf["P"].affine)
+    kdf = float(rdf["stage_ms"][1]) / 1e3
+    # full-size parity of the double-float Jacobian against the FP64 one (same
+    # state, same pattern): max |J_df64 - J_fp64| / max |J_fp64|
+    Pdf = rdf["P"]
+    Pdf.assemble_device(with_jacobian=True)
+    P.assemble_device(with_jacobian=True)
+    jdiff = float((Pdf.J_dev[:P.nnz] - P.J_dev[:P.nnz]).abs().max() / P.J_dev[:P.nnz].abs().max())
+    rdiff = float((Pdf.R_dev[:P.n_dof] - P.R_dev[:P.n_dof]).abs().max() / P.R_dev[:P.n_dof].abs().max())
+    line["df64_jacobian"] = {
+        "what": "FP64 residual and FP64 Jacobian values; the Jacobian's contraction (phase B) in double-float "
+                "(hi + lo pairs of FP32, ~2^-48 relative per operation) on the FP32 pipes",
+        "value": n_elem * world / (rdf["ms"] / 1e3), "unit": "elements/s", "ms_per_step": rdf["ms"],
+        "element_kernel_ms": kdf * 1e3, "kernel": Pdf.kernel.name,
+        "fp64_tflops": fdf["fp64"] * n_elem / kdf / 1e12,
+        "df64_contraction_tflops_fp64_equivalent": fdf.get("df64", 0.0) * n_elem / kdf / 1e12,
+        "max_rel_jacobian_difference_vs_fp64": jdiff, "max_rel_residual_difference_vs_fp64": rdiff,
+        "e2e": {"value": n_elem * world / (rdf["ms_e2e"] / 1e3), "unit": "elements/s",
+                "h2d_bytes_per_step": rdf["h2d"], "d2h_bytes_per_step": rdf["d2h"], "ms_per_step": rdf["ms_e2e"]},
+        "cuda_graph_ms_per_step": rdf["ms_graph"], "elems_per_block": Pdf.kernel.epb,
+        "threads": Pdf.kernel.threads, "smem_bytes": Pdf.kernel.smem_bytes}
     if args.workload in ("hex", "poisson") and world == 1:
         # a whole Newton solve on the device (assembly + BiCGStab on the resident
         # Jacobian), from the zero initial guess to max |R| < 1e-10; a small

@@ -42,7 +42,7 @@ def _header_stamp() -> str:
     an older header."""
     import hashlib
     h = hashlib.sha1()
-    for f in ("fe_device.cuh", "fe_abi.h"):
+    for f in ("fe_device.cuh", "fe_abi.h", "fe_df64.cuh"):
         with open(os.path.join(INCLUDE_DIR, f), "rb") as fp:
             h.update(fp.read())
     return "// device headers " + h.hexdigest()[:16] + "\n"

@@ -254,10 +254,11 @@ class KernelSpec:
 
 
 def _launch_shape(et: ElementType, nloc: int, per_elem_bytes: int, table_bytes: int,
-                  smem_cap: int = 200 * 1024, max_threads: int = 512) -> Tuple[int, int]:
+                  smem_cap: int = 200 * 1024, max_threads: int = 512,
+                  largest: bool = False) -> Tuple[int, int]:
     """Elements per block and threads: keep both thread phases (element x
     integration point, element x row) busy in whole warps, within the
-    shared-memory budget."""
+    shared-memory budget (or, with `largest`, the most elements that fit)."""
     best = None
     for epb in range(1, 65):
         smem = table_bytes + epb * per_elem_bytes
@@ -269,7 +270,7 @@ def _launch_shape(et: ElementType, nloc: int, per_elem_bytes: int, table_bytes: 
             break
         # prefer whole-warp phases and larger blocks
         waste = (threads - epb * et.nq) / threads + (threads - epb * nloc) / threads
-        score = (-waste, epb)
+        score = (epb,) if largest else (-waste, epb)
         if best is None or score > best[0]:
             best = (score, epb, threads)
     if best is None:
@@ -313,8 +314,20 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     nval = nf
     has_c1 = any(s_ == "C1" for s_ in spaces)
     ndnz = max(1, len(pw.d_entries))
-    jreal = "double" if jac_precision == "f64" else "float"
-    jbytes = 8 if jac_precision == "f64" else 4
+    if jac_precision not in ("f64", "f32", "df64"):
+        raise ValueError(f"unknown Jacobian precision {jac_precision!r}")
+    df64 = jac_precision == "df64"
+    # jreal: phase A (pointwise D and its pull-back); jacc: phase B (the
+    # contraction that builds J) -- for df64 D is formed in FP64 and the
+    # contraction runs in double-float on the FP32 pipes (fe_df64.cuh)
+    jreal = "float" if jac_precision == "f32" else "double"
+    jacc = "fe_df64" if df64 else jreal
+    jstore = "float" if jac_precision == "f32" else "double"
+    jbytes = 4 if jac_precision == "f32" else 8
+    if df64:
+        if jref is False:
+            raise ValueError("the df64 Jacobian is built in reference coordinates (jref)")
+        jref = True
     if jref is None:
         # measured on GB300: faster for every FP32 Jacobian, for 3D elements
         # and for single-field forms; slower for the FP64 Taylor-Hood
@@ -336,8 +349,10 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     ndnz_hat = max(1, len(hat))
     table_doubles = nq + nq * nn + nq * nn * dim + nq * nn1 + nq * nn1 * dim
     table_bytes = table_doubles * 8
-    tabf = (nq * nn * (1 + dim) + nq * nn1 * (1 + dim)) if (jref and jreal == "float") else 0
-    table_bytes += ((tabf * 4 + 15) // 16) * 16
+    tab_copy = bool(jref and (jreal == "float" or df64))   # reference tables in the contraction type
+    tabt = jacc if tab_copy else "double"
+    tabf = (nq * nn * (1 + dim) + nq * nn1 * (1 + dim)) if tab_copy else 0
+    table_bytes += ((tabf * (8 if df64 else 4) + 15) // 16) * 16
     geo_doubles = (dim * dim + 1) if affine else 0
     # sum factorisation of the Q2 hex Jacobian (tensor-product shapes and
     # Gauss<3,3> knots): J_ij = sum_ab sum_q prod_d F^d_ab[q_d][i_d][j_d] Dhat_ab(q)
@@ -345,7 +360,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     # per (a, b) block instead of 27 x 27 x 27)
     # (FP64 Jacobians only: for FP32 the contraction is cheap on the FP32 pipe
     # and the staged form measured slower on GB300)
-    sumfac = bool(jref and et.name == "Q2_HEX" and nf == 1 and spaces[0] == "C2" and jac_precision == "f64")
+    sumfac = bool(jref and et.name == "Q2_HEX" and nf == 1 and spaces[0] == "C2" and jac_precision in ("f64", "df64"))
     if sumfac:
         table_bytes += ((4 * 27 * jbytes + 15) // 16) * 16
     if jref:
@@ -356,7 +371,12 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         per_elem = ((nn * dim + 2 * nn * nval + nq * ntc + geo_doubles) * 8
                     + (nq * ndnz + nq * nn * dim + (nq * nn1 * dim if has_c1 else 0)) * jbytes)
     if epb is None:
-        epb, threads = _launch_shape(et, nloc, per_elem, table_bytes)
+        # df64: at most 352 threads (GB300 sweeps: the Q2 hex kernel runs
+        # fastest with 12-13 elements per block, the P2 triangle is flat
+        # between 16 and 64)
+        epb, threads = _launch_shape(et, nloc, per_elem, table_bytes,
+                                     smem_cap=224 * 1024 if df64 else 200 * 1024,
+                                     max_threads=352 if df64 else 512, largest=df64)
     else:
         threads = ((max(epb * nq, epb * nloc) + 31) // 32) * 32
     smem = table_bytes + epb * per_elem
@@ -381,6 +401,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w(f"#define FE_NF {nf}\n#define FE_NTC {ntc}\n#define FE_NDNZ {ndnz}\n#define FE_AFFINE {1 if affine else 0}")
     w(f"#define FE_NDNZH {ndnz_hat}")
     w(f"typedef {jreal} jreal;")
+    w(f"typedef {jacc} jacc;")
+    w(f"typedef {jstore} jstore;")
     w(f"__constant__ int c_loc_of[{len(loc_of_flat)}] = {{{', '.join(map(str, loc_of_flat))}}};")
     if sumfac:
         from .spaces import _G3_1D, _lag3
@@ -401,15 +423,15 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("  double* sY = sU + FE_EPB * FE_NN * FE_NVAL;  // direction of the Hessian-vector product (flag 4)")
     w("  double* sRh = sY + FE_EPB * FE_NN * FE_NVAL;")
     w("  double* sG = sRh + FE_EPB * FE_NQ * FE_NTC;")
-    w(f"  jreal* sD = reinterpret_cast<jreal*>(sG + FE_EPB * {geo_doubles});")
+    w(f"  jacc* sD = reinterpret_cast<jacc*>(sG + FE_EPB * {geo_doubles});")
     if jref:
-        w("  jreal* sEnd = sD + FE_EPB * FE_NQ * FE_NDNZH;")
-        if jreal == "float":
-            # single-precision copies of the reference tables (after the element data)
-            w("  float* sPsi2j = reinterpret_cast<float*>(sEnd);")
-            w("  float* sDps2j = sPsi2j + FE_NQ * FE_NN;")
-            w("  float* sPsi1j = sDps2j + FE_NQ * FE_NN * FE_DIM;")
-            w("  float* sDps1j = sPsi1j + FE_NQ * FE_NN1;")
+        w("  jacc* sEnd = sD + FE_EPB * FE_NQ * FE_NDNZH;")
+        if tab_copy:
+            # copies of the reference tables in the contraction type (after the element data)
+            w("  jacc* sPsi2j = sEnd;")
+            w("  jacc* sDps2j = sPsi2j + FE_NQ * FE_NN;")
+            w("  jacc* sPsi1j = sDps2j + FE_NQ * FE_NN * FE_DIM;")
+            w("  jacc* sDps1j = sPsi1j + FE_NQ * FE_NN1;")
         else:
             w("  (void)sEnd;")
             w("  const double* sPsi2j = sPsi2; const double* sDps2j = sDps2;")
@@ -417,11 +439,11 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("  (void)sPsi1j; (void)sDps1j; (void)sG;")
         if sumfac:
             # per element: stage buffers and the element matrix; per block: F tables
-            base = "sPsi2j + " + str(tabf) if jreal == "float" else "sEnd"
-            w(f"  jreal* sS1 = reinterpret_cast<jreal*>({base});")
-            w("  jreal* sS2 = sS1 + FE_EPB * 81;")
-            w("  jreal* sJe = sS2 + FE_EPB * 243;")
-            w("  jreal* sF = sJe + FE_EPB * 729;")
+            base = "sPsi2j + " + str(tabf) if tab_copy else "sEnd"
+            w(f"  jacc* sS1 = {base};")
+            w("  jacc* sS2 = sS1 + FE_EPB * 81;")
+            w("  jacc* sJe = sS2 + FE_EPB * 243;")
+            w("  jacc* sF = sJe + FE_EPB * 729;")
     else:
         w("  jreal* sDx2 = sD + FE_EPB * FE_NQ * FE_NDNZ;")
         w("  jreal* sDx1 = sDx2 + FE_EPB * FE_NQ * FE_NN * FE_DIM;")
@@ -431,8 +453,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("  const int nel = rem < FE_EPB ? (int)rem : FE_EPB;")
     w("  const int flag = a.flag;")
     w(f"  for (int k = threadIdx.x; k < {table_doubles}; k += FE_NT) sW[k] = a.tables[k];")
-    if jref and jreal == "float":
-        w(f"  for (int k = threadIdx.x; k < {tabf}; k += FE_NT) sPsi2j[k] = (float)a.tables[FE_NQ + k];")
+    if tab_copy:
+        w(f"  for (int k = threadIdx.x; k < {tabf}; k += FE_NT) sPsi2j[k] = (jacc)a.tables[FE_NQ + k];")
     if sumfac:
         from .spaces import _G3_1D, _lag3
         M = [np.array([_lag3(g)[0] for g in _G3_1D]), np.array([_lag3(g)[1] for g in _G3_1D])]
@@ -442,7 +464,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                 for i in range(3):
                     for j in range(3):
                         Fv.append(M[c >> 1][q][i] * M[c & 1][q][j])
-        w(f"  for (int k = threadIdx.x; k < 108; k += FE_NT) sF[k] = (jreal)c_F[k];")
+        w(f"  for (int k = threadIdx.x; k < 108; k += FE_NT) sF[k] = (jacc)c_F[k];")
 
     w("  for (int k = threadIdx.x; k < nel * FE_NN; k += FE_NT) {")
     w("    const int el = k / FE_NN, l = k - el * FE_NN;")
@@ -557,12 +579,22 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("      const jreal wj = (jreal)wq;")
     if jref:
         # Dhat = T^T D T, T = diag(1, g) per field: d/dx_i = sum_b g[b][i] d/ds_b
-        w("      jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZH;")
-        w("      jreal T[FE_DIM][FE_DIM];")
+        # (df64: the pull-back itself in double-float -- D, g and the weight
+        # are converted once, the products run on the FP32 pipes)
+        w("      jacc* Dq = sD + (el * FE_NQ + q) * FE_NDNZH;")
+        tT = "jacc" if df64 else "jreal"
+        w(f"      {tT} T[FE_DIM][FE_DIM];")
         w("      #pragma unroll")
         w("      for (int i = 0; i < FE_DIM; ++i)")
         w("        #pragma unroll")
-        w("        for (int b = 0; b < FE_DIM; ++b) T[i][b] = (jreal)g[b][i];")
+        w(f"        for (int b = 0; b < FE_DIM; ++b) T[i][b] = ({tT})g[b][i];")
+        dsym = "D"
+        if df64:
+            w("      jacc Dd[FE_NDNZ];")
+            w("      #pragma unroll")
+            w("      for (int k = 0; k < FE_NDNZ; ++k) Dd[k] = (jacc)D[k];")
+            w("      const jacc wjd = (jacc)wq;")
+            dsym = "Dd"
 
         def cT(a_, h_):
             if a_ == 0 and h_ == 0:
@@ -576,8 +608,11 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                 ca, cb = cT(a_, ah), cT(b_, bh)
                 if ca is None or cb is None:
                     continue
-                terms.append(" * ".join([x_ for x_ in (ca, f"D[{k}]", cb) if x_]))
-            w(f"      Dq[{kk}] = wj * ({' + '.join(terms) if terms else '(jreal)0'});")
+                terms.append(" * ".join([x_ for x_ in (ca, f"{dsym}[{k}]", cb) if x_]))
+            if df64:
+                w(f"      Dq[{kk}] = {'wjd * (' + ' + '.join(terms) + ')' if terms else '(jacc)0'};")
+            else:
+                w(f"      Dq[{kk}] = (jacc)(wj * ({' + '.join(terms) if terms else '(jreal)0'}));")
     else:
         w("      jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZ;")
         w("      #pragma unroll")
@@ -599,26 +634,40 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w("    for (int p = threadIdx.x; p < nel * 81; p += FE_NT) {")
             w("      const int el = p / 81, o = p - el * 81, qxy = o / 9, izjz = o - qxy * 9;")
             w("      const int iz = izjz / 3, jz = izjz - iz * 3;")
-            w("      const jreal* Dq = sD + (el * FE_NQ + 3 * qxy) * FE_NDNZH;")
-            w(f"      const jreal* F = sF + {cz * 27} + iz * 3 + jz;")
-            w(f"      sS1[p] = F[0] * Dq[{kk}] + F[9] * Dq[FE_NDNZH + {kk}] + F[18] * Dq[2 * FE_NDNZH + {kk}];")
+            w("      const jacc* Dq = sD + (el * FE_NQ + 3 * qxy) * FE_NDNZH;")
+            w(f"      const jacc* F = sF + {cz * 27} + iz * 3 + jz;")
+            if df64:
+                w(f"      jacc t = (jacc)0; fe_mac(t, F[0], Dq[{kk}]); fe_mac(t, F[9], Dq[FE_NDNZH + {kk}]);")
+                w(f"      fe_mac(t, F[18], Dq[2 * FE_NDNZH + {kk}]); sS1[p] = fe_norm(t);")
+            else:
+                w(f"      sS1[p] = F[0] * Dq[{kk}] + F[9] * Dq[FE_NDNZH + {kk}] + F[18] * Dq[2 * FE_NDNZH + {kk}];")
             w("    }")
             w("    __syncthreads();")
             w("    for (int p = threadIdx.x; p < nel * 243; p += FE_NT) {")
             w("      const int el = p / 243, o = p - el * 243, qx = o / 81, r = o - qx * 81, iyjy = r / 9;")
             w("      const int izjz = r - iyjy * 9, iy = iyjy / 3, jy = iyjy - iy * 3;")
-            w("      const jreal* S1 = sS1 + el * 81 + qx * 27 + izjz;")
-            w(f"      const jreal* F = sF + {cy * 27} + iy * 3 + jy;")
-            w("      sS2[p] = F[0] * S1[0] + F[9] * S1[9] + F[18] * S1[18];")
+            w("      const jacc* S1 = sS1 + el * 81 + qx * 27 + izjz;")
+            w(f"      const jacc* F = sF + {cy * 27} + iy * 3 + jy;")
+            if df64:
+                w("      jacc t = (jacc)0; fe_mac(t, F[0], S1[0]); fe_mac(t, F[9], S1[9]); fe_mac(t, F[18], S1[18]);")
+                w("      sS2[p] = fe_norm(t);")
+            else:
+                w("      sS2[p] = F[0] * S1[0] + F[9] * S1[9] + F[18] * S1[18];")
             w("    }")
             w("    __syncthreads();")
             w("    for (int p = threadIdx.x; p < nel * 729; p += FE_NT) {")
             w("      const int el = p / 729, o = p - el * 729, i = o / 27, j = o - i * 27;")
             w("      const int ix = i % 3, iy = (i / 3) % 3, iz = i / 9, jx = j % 3, jy = (j / 3) % 3, jz = j / 9;")
-            w("      const jreal* S2 = sS2 + el * 243 + (iy * 3 + jy) * 9 + iz * 3 + jz;")
-            w(f"      const jreal* F = sF + {cx * 27} + ix * 3 + jx;")
-            w(f"      const jreal v = F[0] * S2[0] + F[9] * S2[81] + F[18] * S2[162];")
-            w(f"      sJe[p] {'=' if kk == 0 else '+='} v;")
+            w("      const jacc* S2 = sS2 + el * 243 + (iy * 3 + jy) * 9 + iz * 3 + jz;")
+            w(f"      const jacc* F = sF + {cx * 27} + ix * 3 + jx;")
+            if df64:
+                # one accumulator over all (a, b) blocks: each thread owns its entries
+                w(f"      jacc v = {'(jacc)0' if kk == 0 else 'sJe[p]'};")
+                w("      fe_mac(v, F[0], S2[0]); fe_mac(v, F[9], S2[81]); fe_mac(v, F[18], S2[162]);")
+                w("      sJe[p] = v;")
+            else:
+                w(f"      const jacc v = F[0] * S2[0] + F[9] * S2[81] + F[18] * S2[162];")
+                w(f"      sJe[p] {'=' if kk == 0 else '+='} v;")
             w("    }")
             w("    __syncthreads();")
         w("  }")
@@ -638,9 +687,9 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    const double* tpsi = t1 ? sPsi1 : sPsi2;")
     w("    const double* tdps = t1 ? sDps1 : sDps2;")
     w("    double Racc = 0.0;")
-    w("    jreal Jr[FE_NLOC];")
+    w("    jacc Jr[FE_NLOC];")
     w("    #pragma unroll")
-    w("    for (int k = 0; k < FE_NLOC; ++k) Jr[k] = (jreal)0;")
+    w("    for (int k = 0; k < FE_NLOC; ++k) Jr[k] = (jacc)0;")
     w("    for (int q = 0; q < FE_NQ; ++q) {")
     w("      const double* rh = sRh + (el * FE_NQ + q) * FE_NTC + tf * (1 + FE_DIM);")
     w("      const double pv = tpsi[q * tn + lt];")
@@ -652,44 +701,53 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         pass
     elif jref:
         w("      if (flag) {")
-        w("        const jreal* Dq = sD + (el * FE_NQ + q) * FE_NDNZH;")
-        w("        const jreal* tpj = t1 ? (sPsi1j + q * FE_NN1) : (sPsi2j + q * FE_NN);")
-        w("        const jreal* tdj = t1 ? (sDps1j + (q * FE_NN1 + lt) * FE_DIM) : (sDps2j + (q * FE_NN + lt) * FE_DIM);")
-        w("        const jreal phi0 = tpj[lt];")
+        w("        const jacc* Dq = sD + (el * FE_NQ + q) * FE_NDNZH;")
+        w(f"        const {tabt}* tpj = t1 ? (sPsi1j + q * FE_NN1) : (sPsi2j + q * FE_NN);")
+        w(f"        const {tabt}* tdj = t1 ? (sDps1j + (q * FE_NN1 + lt) * FE_DIM) : (sDps2j + (q * FE_NN + lt) * FE_DIM);")
+        w("        const jacc phi0 = (jacc)tpj[lt];")
         for d in range(dim):
-            w(f"        const jreal phi{d + 1} = tdj[{d}];")
+            w(f"        const jacc phi{d + 1} = (jacc)tdj[{d}];")
         used_h = sorted({(gf_, bh) for (_, gf_, _, bh) in hat})
         for gf_, bh in used_h:
-            w(f"        jreal h{gf_}_{bh} = (jreal)0;")
+            w(f"        jacc h{gf_}_{bh} = (jacc)0;")
         for f in range(nf):
             ents = [(kk, ah, gf_, bh) for kk, (tf_, gf_, ah, bh) in enumerate(hat) if tf_ == f]
             if not ents:
                 continue
             w(f"        if (tf == {f}) {{")
             for kk, ah, gf_, bh in ents:
-                w(f"          h{gf_}_{bh} += phi{ah} * Dq[{kk}];")
+                if df64:
+                    w(f"          fe_mac(h{gf_}_{bh}, phi{ah}, Dq[{kk}]);")
+                else:
+                    w(f"          h{gf_}_{bh} += phi{ah} * Dq[{kk}];")
             w("        }")
+        if df64:
+            for gf_, bh in used_h:
+                w(f"        h{gf_}_{bh} = fe_norm(h{gf_}_{bh});")
         for f, (fname, fsp) in enumerate(fields):
             comps = [bh for (gf_, bh) in used_h if gf_ == f]
             if not comps:
                 continue
             w("        {")
             if fsp == "C2":
-                w("          const jreal* psi = sPsi2j + q * FE_NN;")
-                w("          const jreal* dps_ = sDps2j + q * FE_NN * FE_DIM;")
+                w(f"          const {tabt}* psi = sPsi2j + q * FE_NN;")
+                w(f"          const {tabt}* dps_ = sDps2j + q * FE_NN * FE_DIM;")
                 cnt = nn
             else:
-                w("          const jreal* psi = sPsi1j + q * FE_NN1;")
-                w("          const jreal* dps_ = sDps1j + q * FE_NN1 * FE_DIM;")
+                w(f"          const {tabt}* psi = sPsi1j + q * FE_NN1;")
+                w(f"          const {tabt}* dps_ = sDps1j + q * FE_NN1 * FE_DIM;")
                 cnt = nn1
             for ls in range(cnt):
                 terms = []
                 for bh in comps:
                     if bh == 0:
-                        terms.append(f"h{f}_0 * psi[{ls}]")
+                        terms.append((f"h{f}_0", f"(jacc)psi[{ls}]"))
                     else:
-                        terms.append(f"h{f}_{bh} * dps_[{ls * dim + bh - 1}]")
-                w(f"          Jr[{layout.loc_of[f][ls]}] += {' + '.join(terms)};")
+                        terms.append((f"h{f}_{bh}", f"(jacc)dps_[{ls * dim + bh - 1}]"))
+                if df64:
+                    w("          " + " ".join(f"fe_mac(Jr[{layout.loc_of[f][ls]}], {x_}, {y_});" for x_, y_ in terms))
+                else:
+                    w(f"          Jr[{layout.loc_of[f][ls]}] += {' + '.join(f'{x_} * {y_}' for x_, y_ in terms)};")
             w("        }")
     else:
         w("      if (flag) {")
@@ -740,13 +798,13 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    const long long row = (e0 + el) * FE_NLOC + i;")
     w("    a.rbuf[row] = Racc;")
     w("    if (flag) {")
-    w("      jreal* jb = reinterpret_cast<jreal*>(a.jbuf) + row * FE_NLOC;")
+    w("      jstore* jb = reinterpret_cast<jstore*>(a.jbuf) + row * FE_NLOC;")
     if sumfac:
-        w("      const jreal* Jrow = sJe + el * 729 + i * 27;")
-        w("      for (int k = 0; k < FE_NLOC; ++k) jb[k] = Jrow[k];")
+        w("      const jacc* Jrow = sJe + el * 729 + i * 27;")
+        w("      for (int k = 0; k < FE_NLOC; ++k) jb[k] = fe_jstore(Jrow[k]);")
     else:
         w("      #pragma unroll")
-        w("      for (int k = 0; k < FE_NLOC; ++k) jb[k] = Jr[k];")
+        w("      for (int k = 0; k < FE_NLOC; ++k) jb[k] = fe_jstore(Jr[k]);")
     w("    }")
     w("  }")
     w("}")
@@ -760,8 +818,9 @@ def estimate_flops(ks: KernelSpec, affine: bool) -> Dict[str, float]:
     """Floating-point operations per element of a generated kernel, counted
     from its structure (an FMA counts 2).  Keys: ``fp64`` (geometry,
     interpolation, pointwise residual, residual contraction; plus the
-    Jacobian when it is FP64) and ``jac`` (the Jacobian-only work, in the
-    Jacobian's precision)."""
+    Jacobian when it is FP64, its D and pull-back when it is df64), ``jac``
+    (the Jacobian-only work) and, for df64, ``df64`` (the contraction done in
+    double-float)."""
     et, pw, lay = ks.et, ks.pointwise, ks.layout
     D, NN, N1, NQ = et.dim, et.nnode, et.nnode_c1, et.nq
     nc = 1 + D
@@ -793,11 +852,18 @@ def estimate_flops(ks: KernelSpec, affine: bool) -> Dict[str, float]:
         comps = [ic for ic in used_ic if ic // nc == f]
         per_row_q += 2 * (NN if s == "C2" else N1) * len(comps)
     a_ops = 2 * len(pw.d_entries) / max(1, len(fields))
-    jac = NQ * jac_q + rows * NQ * (per_row_q + a_ops)
+    jac_a = NQ * jac_q                              # D and its pull-back, per knot
+    jac_b = rows * NQ * (per_row_q + a_ops)         # the contraction into J
     if ks.sumfac_blocks:
         # pulled-back D per knot, then per (a, b) block 3 x (81 + 243 + 729) multiply-adds
-        jac = NQ * (ops_d + 4 * ks.sumfac_blocks) + ks.sumfac_blocks * 2 * 3 * (81 + 243 + 729)
-    out = {"fp64": float(fp64), "jac": float(jac)}
+        jac_a = NQ * (ops_d + 4 * ks.sumfac_blocks)
+        jac_b = ks.sumfac_blocks * 2 * 3 * (81 + 243 + 729)
+    out = {"fp64": float(fp64), "jac": float(jac_a + jac_b)}
     if ks.jac_precision == "f64":
         out["fp64"] += out["jac"]
+    elif ks.jac_precision == "df64":
+        # D in FP64; the contraction in double-float on the FP32 pipes
+        # (counted as the FP64 flops it replaces)
+        out["fp64"] += float(jac_a)
+        out["df64"] = float(jac_b)
     return out

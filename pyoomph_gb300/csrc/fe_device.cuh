@@ -4,6 +4,7 @@
 #define FE_DEVICE_CUH
 
 #include "fe_abi.h"
+#include "fe_df64.cuh"
 
 // Bounds-checked build (compile the element code with -DFE_BOUNDS_CHECK=1):
 // a connectivity entry outside [0, n_nodes) is replaced by node 0, and the

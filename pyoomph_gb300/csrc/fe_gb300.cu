@@ -35,6 +35,7 @@
 
 #include "../../include/fe_gb300.h"
 #include "fe_abi.h"
+#include "fe_df64.cuh"
 
 #define FE_VERSION "fe_gb300 0.1.0 (sm_103a)"
 
@@ -217,23 +218,7 @@ __global__ void k_dof_update(double *__restrict__ x, const double *__restrict__ 
 // y = A x for a CSR matrix (FP64 or FP32 values, FP64 vectors): one warp
 // per row, lanes stride the row, a fixed shuffle tree sums them
 // (deterministic).  The Krylov solver of the device Newton path calls it.
-// FP32 -> FP64 by integer operations (exact: binary32 -> binary64 moves the
-// sign, rebiases the exponent by 1023 - 127 = 896 and shifts the fraction by
-// 29 bits).  On GB300 the FP64 pipe bounds the SpMV, and the conversion
-// instruction would occupy it once per stored value; the integer pipe is
-// idle.  Zeros keep their sign; subnormal, infinite and NaN inputs take the
-// ordinary conversion.
-__device__ __forceinline__ double fe_widen(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned e = (u >> 23) & 0xffu;
-  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
-  if (e - 1u < 254u)
-    return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 896u) << 52) |
-                                            ((unsigned long long)(u & 0x7fffffu) << 29)));
-  if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)sign);
-  return (double)f;
-}
-__device__ __forceinline__ double fe_widen(double d) { return d; }
+// fe_widen: exact FP32 -> FP64 on the integer pipe (fe_df64.cuh)
 
 // y = A x with L lanes per row.  GB300 issues FP64 at ~1/64 of the FP32
 // rate, so the kernel is shaped to spend one FMA per stored entry and as

@@ -149,3 +149,45 @@ def bicgstab(A: DeviceCSR, b, tol: float = 1e-13, maxiter: int = 20000, check_ev
     solver = BatchedBiCGStab(A, 1, check_every=check_every, graph=graph)
     x, its = solver.solve(b, tol=tol, maxiter=maxiter)
     return x.view(-1).clone(), int(its[0])
+
+
+def _main(argv=None) -> None:
+    """SpMV micro-benchmark on an assembled Jacobian:
+    ``python -m pyoomph_gb300.linsolve [hex|poisson|ns] [side] [fp64|fp32]``.
+    Prints the kernel time (CUDA events, 20 repeats after 3) and the
+    algorithmic bandwidth (values + column indices + row pointers + x + y)."""
+    import argparse
+    import torch
+    from . import workloads as W
+    ap = argparse.ArgumentParser(prog="python -m pyoomph_gb300.linsolve")
+    ap.add_argument("workload", nargs="?", default="hex", choices=["hex", "poisson", "ns"])
+    ap.add_argument("side", nargs="?", type=int, default=32)
+    ap.add_argument("precision", nargs="?", default="fp64", choices=["fp64", "fp32"])
+    a = ap.parse_args(argv)
+    make = {"hex": lambda: W.nonlinear_diffusion_problem(N=a.side, seed=2, jacobian_precision=a.precision),
+            "poisson": lambda: W.poisson_problem(N=a.side, seed=2, jacobian_precision=a.precision),
+            "ns": lambda: W.navier_stokes_problem(N=a.side, jacobian_precision=a.precision)}
+    P = make[a.workload]()
+    P.initialise()
+    P.assemble_device(with_jacobian=True)
+    A = DeviceCSR.of_problem(P)
+    x = torch.ones(P.n_dof, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    st = torch.cuda.current_stream().cuda_stream
+    for _ in range(3):
+        A.matvec(x, y, st)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(20):
+        A.matvec(x, y, st)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 20
+    jb = 8 if a.precision == "fp64" else 4
+    nbytes = P.nnz * (jb + 4) + (P.n_dof + 1) * 4 + 16 * P.n_dof
+    print(f"{a.workload} side {a.side} {a.precision}: n={P.n_dof} nnz={P.nnz} spmv {ms:.4f} ms, "
+          f"{nbytes / ms / 1e6:.0f} GB/s algorithmic")
+
+
+if __name__ == "__main__":
+    _main()

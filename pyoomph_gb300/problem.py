@@ -99,7 +99,9 @@ class Problem:
         self.max_residuals = 1e10
         self.max_newton_iterations = 10
         self.newton_solver_tolerance = 1e-8
-        self.jacobian_precision = "fp64"   # or "fp32": FP32 Jacobian, FP64 residual
+        # "fp64"; "fp32": FP32 Jacobian, FP64 residual; "df64": FP64 Jacobian
+        # values contracted in double-float (~2^-48) on the FP32 pipes
+        self.jacobian_precision = "fp64"
         self.elems_per_block: Optional[int] = None
         # "auto": detect affine elements (constant geometry per element) on the host
         self.geometry = "auto"
@@ -190,20 +192,30 @@ class Problem:
         self.param_names = used
         self.params = np.array([params[p] for p in used], dtype=np.float64)
         t1 = time.perf_counter()
-        prec = "f64" if self.jacobian_precision in ("fp64", "f64", "double") else "f32"
+        jp = self.jacobian_precision
+        if jp in ("fp64", "f64", "double"):
+            kprec = "f64"
+        elif jp in ("fp32", "f32", "float"):
+            kprec = "f32"
+        elif jp == "df64":
+            kprec = "df64"   # FP64 storage; contraction in double-float on the FP32 pipes
+        else:
+            raise ValueError(f"jacobian_precision must be fp64, fp32 or df64, not {jp!r}")
+        prec = "f32" if kprec == "f32" else "f64"   # storage of the Jacobian values
         self._prec = prec
+        self._kprec = kprec
         if self.geometry == "auto":
             self.affine = mesh_is_affine(mesh)
         else:
             self.affine = self.geometry == "affine"
         # the kernel depends on the weak form, element type, precision and
         # geometry kind only -- not on the mesh size: cache it per process
-        key = (mesh.etype.name, tuple(fields), str(integrand), tuple(used), prec, self.affine, self.elems_per_block,
+        key = (mesh.etype.name, tuple(fields), str(integrand), tuple(used), kprec, self.affine, self.elems_per_block,
                self.jacobian_reference)
         ks = _KERNEL_CACHE.get(key)
         if ks is None:
             pw = differentiate(fields, mesh.dim, integrand, used)
-            ks = generate_kernel(mesh.etype, pw, prec, epb=self.elems_per_block, affine=self.affine,
+            ks = generate_kernel(mesh.etype, pw, kprec, epb=self.elems_per_block, affine=self.affine,
                                  jref=self.jacobian_reference)
             _KERNEL_CACHE[key] = ks
         self.kernel: KernelSpec = ks

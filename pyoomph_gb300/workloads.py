@@ -89,3 +89,43 @@ def perturb_dofs(P: Problem, seed: int, sigma: float = 1e-3) -> None:
     x = P.get_dofs()
     x = x + np.random.default_rng(seed).normal(0.0, sigma, x.size)
     P.set_dofs(x)
+
+
+def _main(argv=None) -> None:
+    """Repeated R+J assemblies of one workload (a small driver for profiling
+    the element kernel): ``python -m pyoomph_gb300.workloads ns 128 df64 5``
+    = Navier-Stokes side 128, double-float Jacobian, 5 assemblies after one
+    warm-up."""
+    import argparse
+    import torch
+    ap = argparse.ArgumentParser(prog="python -m pyoomph_gb300.workloads")
+    ap.add_argument("workload", choices=["ns", "poisson", "hex"])
+    ap.add_argument("side", type=int)
+    ap.add_argument("precision", choices=["fp64", "fp32", "df64"])
+    ap.add_argument("repeat", type=int, nargs="?", default=3)
+    ap.add_argument("--epb", type=int, default=None, help="elements per block (default: the generator's)")
+    a = ap.parse_args(argv)
+    if a.workload == "ns":
+        P = navier_stokes_problem(N=a.side, jacobian_precision=a.precision)
+    elif a.workload == "poisson":
+        P = poisson_problem(N=a.side, seed=0, jacobian_precision=a.precision)
+    else:
+        P = nonlinear_diffusion_problem(N=a.side, seed=0, jacobian_precision=a.precision)
+    P.elems_per_block = a.epb
+    P.initialise()
+    perturb_dofs(P, seed=0, sigma=1e-3)
+    P.assemble_device(with_jacobian=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.repeat):
+        P.assemble_device(with_jacobian=True)
+    e1.record()
+    torch.cuda.synchronize()
+    P.check()
+    print(f"{a.workload} side {a.side} {a.precision}: {P.mesh.n_elem} elements, kernel {P.kernel.name}, "
+          f"{e0.elapsed_time(e1) / a.repeat:.4f} ms per assembly")
+
+
+if __name__ == "__main__":
+    _main()

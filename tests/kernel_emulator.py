@@ -38,6 +38,14 @@ static fe_emu_dim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, gridDim = {1, 1,
 #define __align__(n) alignas(n)
 #define __syncthreads() do {} while (0)
 static inline int atomicExch(int *p, int v) { int o = *p; *p = v; return o; }
+static inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
+static inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
+static inline long long __double_as_longlong(double d) { long long u; std::memcpy(&u, &d, 8); return u; }
+static inline double __longlong_as_double(long long u) { double d; std::memcpy(&d, &u, 8); return d; }
+static inline float __fadd_rn(float a, float b) { return a + b; }
+static inline float __fsub_rn(float a, float b) { return a - b; }
+static inline float __fmul_rn(float a, float b) { return a * b; }
+static inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }
 alignas(16) unsigned char fe_smem[232448];
 """
 
@@ -46,7 +54,7 @@ def _headers() -> str:
     """The device headers the generated code includes (part of the cache key:
     a changed argument block must rebuild every emulator library)."""
     out = ""
-    for f in ("fe_abi.h", "fe_device.cuh"):
+    for f in ("fe_abi.h", "fe_device.cuh", "fe_df64.cuh"):
         with open(os.path.join(CSRC, f)) as fp:
             out += fp.read()
     return out
@@ -90,7 +98,7 @@ def run(ks, x, conn, values, params, flag: int = 1, direction=None):
     L = build(ks)
     E = conn.shape[0]
     nloc = ks.layout.n
-    jt = np.float64 if ks.jac_precision == "f64" else np.float32
+    jt = np.float32 if ks.jac_precision == "f32" else np.float64
     x = np.ascontiguousarray(x, dtype=np.float64)
     conn = np.ascontiguousarray(conn, dtype=np.int32)
     values = np.ascontiguousarray(values, dtype=np.float64)

@@ -59,12 +59,15 @@ def test_golden_reference_parity(path):
     assert _relmax(R, g["R"]) <= RTOL
 
 
+@pytest.mark.parametrize("prec", ["fp64", "df64"])
 @pytest.mark.parametrize("kind", ["poisson_q2", "poisson_p2", "ns_th", "nldiff_hex", "nldiff_q2"])
-def test_random_state_vs_oracle(kind):
+def test_random_state_vs_oracle(kind, prec):
+    """Full CSR assembly (pattern bit-exact, values within 1e-12) for the FP64
+    Jacobian and for the double-float contraction (df64)."""
     from pyoomph_gb300 import workloads as W
     rng = np.random.default_rng(11)
     if kind == "ns_th":
-        P = W.navier_stokes_problem(N=[9, 7])
+        P = W.navier_stokes_problem(N=[9, 7], jacobian_precision=prec)
         P.initialise()
         m = O.mesh(O.P2_TRI, 9, 7)
         OP = O.navier_stokes_problem(m, rho=1.0, mu=0.01)
@@ -79,9 +82,10 @@ def test_random_state_vs_oracle(kind):
         gauss = W.draw_gaussians(3, 8, dim)
         eq = O.EQ_POISSON if kind.startswith("poisson") else O.EQ_NONLINEAR_DIFFUSION
         if eq == O.EQ_POISSON:
-            P = W.poisson_problem(N=nx, gaussians=gauss, split="left" if et == O.P2_TRI else None)
+            P = W.poisson_problem(N=nx, gaussians=gauss, split="left" if et == O.P2_TRI else None,
+                                  jacobian_precision=prec)
         else:
-            P = W.nonlinear_diffusion_problem(N=nx, gaussians=gauss, dim=dim)
+            P = W.nonlinear_diffusion_problem(N=nx, gaussians=gauss, dim=dim, jacobian_precision=prec)
         P.initialise()
         m = O.mesh(et, *(nx + [0] * (3 - len(nx))))
         OP = O.poisson_problem(m, gauss, eq=eq)
@@ -146,7 +150,7 @@ def test_newton_poisson_matches_oracle_solution():
     assert _relmax(P.get_dofs(), OP.dofs()) <= STOL
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "df64"])
 def test_newton_navier_stokes_matches_oracle_solution(prec):
     from pyoomph_gb300 import workloads as W
     P = W.navier_stokes_problem(N=[8, 8], jacobian_precision=prec)
@@ -267,3 +271,18 @@ def test_custom_assembler_drop_in_contract():
     R0, rp, ci, v = O.assemble(OP, True, -1.0)
     assert np.array_equal(J.indptr, rp) and np.array_equal(J.indices, ci)
     assert _relmax(J.data, v) <= RTOL and _relmax(R, R0) <= RTOL
+
+
+@pytest.mark.parametrize("geometry", ["affine", "general"])
+@pytest.mark.parametrize("kind", ["poisson_q2", "poisson_p2", "ns_th", "nldiff_hex", "nldiff_q2"])
+def test_df64_element_level_parity(kind, geometry):
+    """The double-float Jacobian's element matrices from the GPU element
+    buffers against the oracle's, within the FP64 contract."""
+    import element_cases as C
+    P, ks, values, Rr, Jr = C.build(kind, geometry, "df64")
+    P.initialise()
+    P.set_values(values)
+    P.get_jacobian()
+    Re, Je = P.element_buffers()
+    assert C.relmax(Re, Rr) <= RTOL
+    assert C.relmax(Je, Jr) <= RTOL

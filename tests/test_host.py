@@ -53,14 +53,16 @@ def test_null_arguments_are_rejected():
     assert L.fe_assemble(None, None, None, None, 3, None) == N.FE_ERR_ARG
 
 
-@pytest.mark.parametrize("kind", ["poisson", "poisson_p2", "ns", "ns32", "hex", "hex32"])
+@pytest.mark.parametrize("kind", ["poisson", "poisson_p2", "ns", "ns32", "nsdf", "hex", "hex32", "hexdf"])
 def test_generated_kernels_compile_for_sm103a(kind, tmp_path):
     from pyoomph_gb300 import _native as N
     from pyoomph_gb300 import workloads as W
     P = {"poisson": lambda: W.poisson_problem(N=4), "poisson_p2": lambda: W.poisson_problem(N=4, split="left"),
          "ns": lambda: W.navier_stokes_problem(N=4), "ns32": lambda: W.navier_stokes_problem(N=4, jacobian_precision="fp32"),
          "hex": lambda: W.nonlinear_diffusion_problem(N=2),
-         "hex32": lambda: W.nonlinear_diffusion_problem(N=2, jacobian_precision="fp32")}[kind]()
+         "hex32": lambda: W.nonlinear_diffusion_problem(N=2, jacobian_precision="fp32"),
+         "nsdf": lambda: W.navier_stokes_problem(N=4, jacobian_precision="df64"),
+         "hexdf": lambda: W.nonlinear_diffusion_problem(N=2, jacobian_precision="df64")}[kind]()
     ks = P.lower()
     assert ks.smem_bytes <= 227 * 1024 and ks.threads % 32 == 0 and ks.threads <= 1024
     assert N.code_build(ks.source, ks.name, str(tmp_path)) > 0
@@ -193,3 +195,22 @@ def test_generated_kernel_emulated_on_cpu_matches_oracle_elements(kind, geometry
     assert st[0] == 0
     assert C.relmax(rb, Rr) <= 1e-12
     assert C.relmax(jb, Jr) <= (1e-12 if prec == "fp64" else 1e-5)
+
+
+@pytest.mark.parametrize("geometry", ["affine", "general"])
+@pytest.mark.parametrize("kind", ["poisson_q2", "poisson_p2", "ns_th", "nldiff_hex", "nldiff_q2"])
+def test_df64_jacobian_emulated_on_cpu_matches_oracle_elements(kind, geometry):
+    """The double-float Jacobian (FP64 D, contraction in pairs of FP32 on the
+    FP32 pipes, FP64 storage) reproduces the oracle's element matrices
+    within the FP64 contract; its error sits near 2^-48, far below the
+    FP32 Jacobian's."""
+    import element_cases as C
+    import kernel_emulator as KE
+    P, ks, values, Rr, Jr = C.build(kind, geometry, "df64")
+    assert ks.jac_precision == "df64" and "fe_df64" in ks.source
+    rb, jb, st = KE.run(ks, P.mesh.x, P.mesh.conn, values, P.params)
+    assert st[0] == 0
+    assert C.relmax(rb, Rr) <= 1e-12
+    err = C.relmax(jb, Jr)
+    print(kind, geometry, "df64 J rel err", err)
+    assert err <= 1e-12
