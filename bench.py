@@ -180,6 +180,8 @@ def make_problem(workload: str, size: int, precision: str, epb=None):
     return P
 
 
+TUNED_EPB = {("ns", 256, "df64"): 48}
+
 # DRAM bytes (read + write) per launch of the element kernel of each bench
 # workload at its default size, from one ncu capture per workload
 # (dram__bytes_read.sum + dram__bytes_write.sum, median of 21 launches;
@@ -254,7 +256,10 @@ def run_gb300(args):
     results = {}
     tuned = {}
     for prec in ("fp64", "fp32", "df64"):
-        epb = None
+        # launch shapes --autotune measured fastest on GB300 where they differ
+        # from the generator's default (NS 256^2 df64: 48 elements/block
+        # 1.04 ms, default 46: 1.10 ms -- whole waves of 152 blocks)
+        epb = TUNED_EPB.get((args.workload, args.size, prec))
         if args.autotune:
             from pyoomph_gb300 import autotune as AT
             P0 = make_problem(args.workload, args.size, prec)
@@ -569,7 +574,7 @@ def run_droplet(args):
     hbm_peak, peak_kind = _peaks()
     res = {}
     tuned = {}
-    for prec in ("fp64", "fp32"):
+    for prec in ("fp64", "fp32", "df64"):
         shape = None
         if args.autotune:
             from pyoomph_gb300 import autotune as AT
@@ -661,6 +666,28 @@ def run_droplet(args):
                              "e2e": {"value": n_elem / (r32["ms_e2e"] / 1e3),
                                      "h2d_bytes_per_step": r32["h2d"], "d2h_bytes_per_step": r32["d2h"]},
                              "cuda_graph_ms_per_step": r32["ms_graph"]}
+    rdf = res["df64"]
+    Pdf = rdf["P"]
+    kdf = float(rdf["stage_ms"][1]) / 1e3
+    f64_df = sum(dc.flops * c.shape[0] for dc, c in zip(Pdf.domains, Pdf.conns))
+    fdf_df = sum(dc.flops_df64 * c.shape[0] for dc, c in zip(Pdf.domains, Pdf.conns))
+    # full-size parity against the FP64 kernel on the same state
+    Pdf.assemble_device(with_jacobian=True)
+    P.assemble_device(with_jacobian=True)
+    jdiff = float((Pdf.J_dev[:P.nnz] - P.J_dev[:P.nnz]).abs().max() / P.J_dev[:P.nnz].abs().max())
+    rdiff = float((Pdf.R_dev[:P.n_dof] - P.R_dev[:P.n_dof]).abs().max() / P.R_dev[:P.n_dof].abs().max())
+    line["df64_jacobian"] = {
+        "what": "FP64 residual, geometry and coefficients; the Jacobian contraction in double-float "
+                "(hi + lo pairs of FP32) on the FP32 pipes; FP64 Jacobian values",
+        "value": n_elem / (rdf["ms"] / 1e3), "unit": "elements/s", "ms_per_step": rdf["ms"],
+        "element_kernel_ms": kdf * 1e3, "kernel": Pdf.kernel.name,
+        "fp64_tflops": f64_df / kdf / 1e12, "df64_contraction_tflops_fp64_equivalent": fdf_df / kdf / 1e12,
+        "max_rel_jacobian_difference_vs_fp64": jdiff, "max_rel_residual_difference_vs_fp64": rdiff,
+        "e2e": {"value": n_elem / (rdf["ms_e2e"] / 1e3), "unit": "elements/s",
+                "h2d_bytes_per_step": rdf["h2d"], "d2h_bytes_per_step": rdf["d2h"], "ms_per_step": rdf["ms_e2e"]},
+        "cuda_graph_ms_per_step": rdf["ms_graph"],
+        "launch_shape": {"threads": Pdf.kernel.threads, "smem_bytes": Pdf.kernel.smem_bytes,
+                         "elems_per_block": [dc.epb for dc in Pdf.domains]}}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = droplet_cpu_baseline(args.size)
     print(json.dumps(line), flush=True)

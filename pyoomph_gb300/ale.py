@@ -283,6 +283,7 @@ class DomainCode:
     rows_needed: int = 0
     flops: float = 0.0          # FP64 operations per element (FMA = 2), counted from the generated code
     flops32: float = 0.0        # FP32 operations per element (the Jacobian contraction of the f32 variant)
+    flops_df64: float = 0.0     # FP64-equivalent operations of the df64 variant's contraction
 
     def layout(self):
         """Local order: the nodal values node by node (fields in order), then
@@ -311,7 +312,7 @@ def _sub_nodes(dc: DomainCode, f: int) -> List[int]:
 
 
 def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: int, nh: int,
-                   smem_budget: int, nthreads_cap: int, f32: bool = False) -> str:
+                   smem_budget: int, nthreads_cap: int, f32: bool = False, df64: bool = False) -> str:
     """Device namespace dom{k} with ``run(a, blk, smem)`` evaluating one block
     of elements of this domain: stage tables and nodal data (phase 0), one
     thread per (element, knot) for geometry, interpolation and the pointwise
@@ -480,12 +481,19 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
         rows_f[i] = (f, _sub_nodes(dc, f).index(l))
     # ---- shared memory plan (doubles)
     tabd = nq + nq * nn + nq * nn * EDs + nq * n1 + nq * n1 * EDs
-    tabf = nq * (nn + n1) if f32 else 0               # float copies of the shape values
-    tabfd = (tabf + 1) // 2
-    QB = 2 * nn * d + 2 * n1 * d + ntc + (0 if f32 else NK) + 4
-    FQB = NK + 2 * nn * d + 2 * n1 * d if f32 else 0  # floats per knot: C, dx, dX, dx1, dX1
-    FQB += FQB % 2
-    per_el = nn * nval * (1 + nh) + nn * d + nq * QB + nq * FQB // 2
+    # the Jacobian contraction reads copies in its own type: float (f32) or
+    # double-float pairs (df64, 8 bytes) of the shape values, the gradients
+    # and the coefficients; FP64 reads the FP64 originals
+    lowp = f32 or df64
+    lt = "fe_df64" if df64 else "float"
+    per8 = 1 if df64 else 2                           # low-precision values per 8 bytes
+    tabf = nq * (nn + n1) if lowp else 0               # copies of the shape values
+    tabfd = (tabf + per8 - 1) // per8
+    QB = 2 * nn * d + 2 * n1 * d + ntc + (0 if lowp else NK) + 4
+    FQB = NK + 2 * nn * d + 2 * n1 * d if lowp else 0  # per knot: C, dx, dX, dx1, dX1
+    if f32:
+        FQB += FQB % 2
+    per_el = nn * nval * (1 + nh) + nn * d + nq * QB + nq * FQB // per8
     epb = 1
     for e_ in range(1, 65):
         if max(e_ * nq, e_ * nloc) > nthreads_cap or (tabd + tabfd + e_ * per_el) * 8 > smem_budget:
@@ -582,7 +590,7 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w("  double* sPsi1 = sDps2 + NQ * NN * ED;")
     w("  double* sDps1 = sPsi1 + NQ * N1;")
     w("  double* sE = sW + TABD + TABFD;")
-    w("  float* sPsi2f = reinterpret_cast<float*>(sW + TABD); float* sPsi1f = sPsi2f + NQ * NN;")
+    w(f"  {lt}* sPsi2f = reinterpret_cast<{lt}*>(sW + TABD); {lt}* sPsi1f = sPsi2f + NQ * NN;")
     w("  (void)sPsi2f; (void)sPsi1f;")
     w("  const long long e0 = (long long)blk * EPB;")
     w("  const long long rem = a.n_elem - e0;")
@@ -591,9 +599,9 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w("  const double* __restrict__ P = a.params;")
     w("  (void)P; (void)sDps1;")
     w("  for (int k = threadIdx.x; k < TABD; k += FE_NT) sW[k] = a.tables[k];")
-    if f32:
-        w("  for (int k = threadIdx.x; k < NQ * NN; k += FE_NT) sPsi2f[k] = (float)a.tables[NQ + k];")
-        w("  for (int k = threadIdx.x; k < NQ * N1; k += FE_NT) sPsi1f[k] = (float)a.tables[NQ + NQ * NN * (1 + ED) + k];")
+    if lowp:
+        w(f"  for (int k = threadIdx.x; k < NQ * NN; k += FE_NT) sPsi2f[k] = ({lt})a.tables[NQ + k];")
+        w(f"  for (int k = threadIdx.x; k < NQ * N1; k += FE_NT) sPsi1f[k] = ({lt})a.tables[NQ + NQ * NN * (1 + ED) + k];")
     if bdf0 >= 0:
         w(f"  const jreal w0j = (jreal)P[{bdf0}]; (void)w0j;")
     w("  for (int k = threadIdx.x; k < nel * NN; k += FE_NT) {")
@@ -614,10 +622,10 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w("    const double* X0 = Uv + (1 + NH) * NN * NVAL;")
     w("    double* qb = sE + el * PER_EL + (1 + NH) * NN * NVAL + NN * DIM + q * QB;")
     w("    double* dx = qb; double* dX = dx + NN * DIM; double* dx1 = dX + NN * DIM; double* dX1 = dx1 + N1 * DIM;")
-    if f32:
+    if lowp:
         w("    double* rc = dX1 + N1 * DIM; double* misc = rc + NTC;")
-        w("    float* C = reinterpret_cast<float*>(sE + el * PER_EL + (1 + NH) * NN * NVAL + NN * DIM + NQ * QB) + q * FQB;")
-        w("    float* fdx = C + NK; float* fdX = fdx + NN * DIM; float* fdx1 = fdX + NN * DIM; float* fdX1 = fdx1 + N1 * DIM;")
+        w(f"    {lt}* C = reinterpret_cast<{lt}*>(sE + el * PER_EL + (1 + NH) * NN * NVAL + NN * DIM + NQ * QB) + q * FQB;")
+        w(f"    {lt}* fdx = C + NK; {lt}* fdX = fdx + NN * DIM; {lt}* fdx1 = fdX + NN * DIM; {lt}* fdX1 = fdx1 + N1 * DIM;")
         w("    (void)fdX; (void)fdX1;")
     else:
         w("    double* rc = dX1 + N1 * DIM; double* C = rc + NTC; double* misc = C + NK;")
@@ -654,20 +662,20 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     w("    for (int l = 0; l < NN; ++l) for (int i = 0; i < DIM; ++i) {")
     w("      double s1 = 0.0;")
     w("      for (int b = 0; b < ED; ++b) s1 += g[b][i] * dps[l * ED + b];")
-    w("      dx[l * DIM + i] = s1;" + (" fdx[l * DIM + i] = (float)s1;" if f32 else "") + " }")
+    w("      dx[l * DIM + i] = s1;" + (f" fdx[l * DIM + i] = ({lt})s1;" if lowp else "") + " }")
     w("    for (int l = 0; l < N1; ++l) for (int i = 0; i < DIM; ++i) {")
     w("      double s1 = 0.0;")
     w("      for (int b = 0; b < ED; ++b) s1 += g[b][i] * dps1[l * ED + b];")
-    w("      dx1[l * DIM + i] = s1;" + (" fdx1[l * DIM + i] = (float)s1;" if f32 else "") + " }")
+    w("      dx1[l * DIM + i] = s1;" + (f" fdx1[l * DIM + i] = ({lt})s1;" if lowp else "") + " }")
     if lagr:
         w("    for (int l = 0; l < NN; ++l) for (int i = 0; i < DIM; ++i) {")
         w("      double s2 = 0.0;")
         w("      for (int b = 0; b < ED; ++b) s2 += gl[b][i] * dps[l * ED + b];")
-        w("      dX[l * DIM + i] = s2;" + (" fdX[l * DIM + i] = (float)s2;" if f32 else "") + " }")
+        w("      dX[l * DIM + i] = s2;" + (f" fdX[l * DIM + i] = ({lt})s2;" if lowp else "") + " }")
         w("    for (int l = 0; l < N1; ++l) for (int i = 0; i < DIM; ++i) {")
         w("      double s2 = 0.0;")
         w("      for (int b = 0; b < ED; ++b) s2 += gl[b][i] * dps1[l * ED + b];")
-        w("      dX1[l * DIM + i] = s2;" + (" fdX1[l * DIM + i] = (float)s2;" if f32 else "") + " }")
+        w("      dX1[l * DIM + i] = s2;" + (f" fdX1[l * DIM + i] = ({lt})s2;" if lowp else "") + " }")
     w(f"    double U[{nf * NCU}];")
     w(f"    for (int c = 0; c < {nf * NCU}; ++c) U[c] = 0.0;")
     interp = 0
@@ -734,10 +742,10 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
         w("        const double* dX1 = dx1 + N1 * DIM; const double* rc = dX1 + N1 * DIM;")
         w("        const double* ps = sPsi2 + q * NN;")
         w("        (void)dx; (void)dX; (void)dx1; (void)dX1; (void)ps;")
-        if f32:
-            w("        const float* C = reinterpret_cast<const float*>(ebq + NQ * QB) + q * FQB;")
-            w("        const float* fdx = C + NK; const float* fdX = fdx + NN * DIM; const float* fdx1 = fdX + NN * DIM;")
-            w("        const float* fdX1 = fdx1 + N1 * DIM; const float* fps = sPsi2f + q * NN; const float* fps1 = sPsi1f + q * N1;")
+        if lowp:
+            w(f"        const {lt}* C = reinterpret_cast<const {lt}*>(ebq + NQ * QB) + q * FQB;")
+            w(f"        const {lt}* fdx = C + NK; const {lt}* fdX = fdx + NN * DIM; const {lt}* fdx1 = fdX + NN * DIM;")
+            w(f"        const {lt}* fdX1 = fdx1 + N1 * DIM; const {lt}* fps = sPsi2f + q * NN; const {lt}* fps1 = sPsi1f + q * N1;")
             w("        (void)fdx; (void)fdX; (void)fdx1; (void)fdX1; (void)fps; (void)fps1;")
         else:
             w("        const double* C = rc + NTC;")
@@ -746,7 +754,7 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
         for c in range(NCT):
             if tci(tf, c) not in used_t:
                 continue
-            for single in ((False, True) if f32 else (False,)):
+            for single in ((False, True) if lowp else (False,)):
                 pre = "f" if single else ""
                 if c == 0:
                     src_ = (f"{pre}ps[ts]" if tsp == "C2" else
@@ -756,8 +764,8 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
                 else:
                     src_ = f"{pre}dX[ts * DIM + {c - 1 - d}]" if tsp == "C2" else f"{pre}dX1[ts * DIM + {c - 1 - d}]"
                 if single and c in jac_t:
-                    w(f"        const float fphi{c} = {src_};")
-                elif not single and (not f32 or tci(tf, c) in rEn or tci(tf, c) in rLn):
+                    w(f"        const {lt} fphi{c} = {src_};")
+                elif not single and (not lowp or tci(tf, c) in rEn or tci(tf, c) in rLn):
                     w(f"        const double phi{c} = {src_};")
         rterms = [f"rc[{tci(tf, c)}] * phi{c}" for c in range(NCT) if (tci(tf, c) in rEn or tci(tf, c) in rLn)]
         n_rows_tf = sum(1 for r_ in rows_f if r_[0] == tf)
@@ -766,11 +774,21 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
             w(f"        Racc += {' + '.join(rterms)};")
         w("        if (flag == 1) {")
         av: Dict[int, List[str]] = {}
+        avp: Dict[int, List[Tuple[str, str]]] = {}
         for kk, (tc, ic) in enumerate(keys):
             if tc // NCT == tf:
-                av.setdefault(ic, []).append(f"{'f' if f32 else ''}phi{tc - tf * NCT} * C[{kk}]")
+                av.setdefault(ic, []).append(f"{'f' if lowp else ''}phi{tc - tf * NCT} * C[{kk}]")
+                avp.setdefault(ic, []).append((f"{'f' if lowp else ''}phi{tc - tf * NCT}", f"C[{kk}]"))
+
+        def emit_av(ic, ind):
+            # df64: compensated multiply-adds, renormalised once
+            if df64:
+                w(f"{ind}jreal av{ic} = (jreal)0; " + " ".join(f"fe_mac(av{ic}, {x_}, {y_});" for x_, y_ in avp[ic])
+                  + f" av{ic} = fe_norm(av{ic});")
+            else:
+                w(f"{ind}const jreal av{ic} = {' + '.join(av[ic])};")
         for ic, lst in sorted(av.items()):
-            w(f"          const jreal av{ic} = {' + '.join(lst)};")
+            emit_av(ic, "          ")
             fl_tj += 2 * len(lst)
         for g_ in range(nf):
             gsp = fields[g_][1]
@@ -781,30 +799,33 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
                     gf, cc = divmod(ic, NCU)
                     if gf != g_:
                         continue
-                    pre = "f" if f32 else ""
+                    pre = "f" if lowp else ""
                     if gsp == "C2":
                         val, gx, gX = f"{pre}ps[{l}]", f"{pre}dx[{l * d} + {{i}}]", f"{pre}dX[{l * d} + {{i}}]"
                     else:
-                        val = f"fps1[{s_}]" if f32 else f"sPsi1[q * N1 + {s_}]"
+                        val = f"fps1[{s_}]" if lowp else f"sPsi1[q * N1 + {s_}]"
                         gx, gX = f"{pre}dx1[{s_ * d} + {{i}}]", f"{pre}dX1[{s_ * d} + {{i}}]"
                     if cc == 0:
-                        parts.append(f"av{ic} * {val}")
+                        parts.append((f"av{ic}", val))
                     elif cc <= d:
-                        parts.append(f"av{ic} * {gx.format(i=cc - 1)}")
+                        parts.append((f"av{ic}", gx.format(i=cc - 1)))
                     elif cc <= 2 * d:
-                        parts.append(f"av{ic} * {gX.format(i=cc - 1 - d)}")
+                        parts.append((f"av{ic}", gX.format(i=cc - 1 - d)))
                     else:
-                        parts.append(f"av{ic} * w0j * {val}")
+                        parts.append((f"av{ic} * w0j", val))
                 if parts:
-                    w(f"          Jr[{col}] += {' + '.join(parts)};")
-                    fl_tj += sum(_ops(x) for x in parts) + len(parts)
+                    if df64:
+                        w("          " + " ".join(f"fe_mac(Jr[{col}], {x_}, {y_});" for x_, y_ in parts))
+                    else:
+                        w(f"          Jr[{col}] += {' + '.join(f'{x_} * {y_}' for x_, y_ in parts)};")
+                    fl_tj += sum(_ops(f"{x_} * {y_}") for x_, y_ in parts) + len(parts)
         w("        }")
         # mass matrix: the coefficients of the time-derivative components, basis psi
         tics = sorted(ic for ic in av if ic % NCU == 1 + 2 * d)
         if tics:
             w("        if (flag == 2) {")
             for ic in tics:
-                w(f"          const jreal av{ic} = {' + '.join(av[ic])};")
+                emit_av(ic, "          ")
             for g_ in range(nf):
                 ic = g_ * NCU + 1 + 2 * d
                 if ic not in tics:
@@ -812,10 +833,13 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
                 for s_, l in enumerate(_sub_nodes(dc, g_)):
                     col = slot[(g_, l)]
                     if fields[g_][1] == "C2":
-                        val = f"{'f' if f32 else ''}ps[{l}]"
+                        val = f"{'f' if lowp else ''}ps[{l}]"
                     else:
-                        val = f"fps1[{s_}]" if f32 else f"sPsi1[q * N1 + {s_}]"
-                    w(f"          Jr[{col}] += av{ic} * {val};")
+                        val = f"fps1[{s_}]" if lowp else f"sPsi1[q * N1 + {s_}]"
+                    if df64:
+                        w(f"          fe_mac(Jr[{col}], av{ic}, {val});")
+                    else:
+                        w(f"          Jr[{col}] += av{ic} * {val};")
             w("        }")
         w("      }")
         w("      break;")
@@ -826,15 +850,16 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     geo = (2 * (2 * nn * d * EDs + 2 * EDs * EDs * d + 2 * EDs * EDs * d + 12) if ed == d else
            (4 * nn + 12 if ed == 1 else 0))
     geo += (nn + n1) * d * EDs * 2 * (2 if lagr else 1) + 4 * nn * d
-    dc.flops = float(nq * (geo + interp + fl_point + fl_rows_r + (0 if f32 else fl_rows_j)))
+    dc.flops = float(nq * (geo + interp + fl_point + fl_rows_r + (0 if lowp else fl_rows_j)))
     dc.flops32 = float(nq * fl_rows_j) if f32 else 0.0
+    dc.flops_df64 = float(nq * fl_rows_j) if df64 else 0.0
     w("    default: break;")
     w("    }")
     w("    const long long row = (e0 + el) * NLOC + i;")
     w("    a.rbuf[row] = Racc;")
     w("    if (flag == 1 || flag == 2) {")
-    w("      jreal* jb = reinterpret_cast<jreal*>(a.jbuf) + row * NLOC;")
-    w("      for (int c = 0; c < NLOC; ++c) jb[c] = Jr[c];")
+    w("      jstore* jb = reinterpret_cast<jstore*>(a.jbuf) + row * NLOC;")
+    w("      for (int c = 0; c < NLOC; ++c) jb[c] = fe_jstore(Jr[c]);")
     w("    }")
     w("  }")
     w("}")
@@ -860,13 +885,17 @@ def generate_fused(domains: List[DomainCode], dim: int, params: List[str], nval:
     [block_start[k], block_start[k+1]) of the runtime's FeFusedArgs holds b."""
     if len(domains) > 4:
         raise ValueError("at most 4 fused domains")
-    jreal = "double" if jac_precision == "f64" else "float"
-    bodies = [_domain_source(k, dc, dim, params, nval, nh, smem_budget, nthreads_cap, jac_precision == "f32")
+    if jac_precision not in ("f64", "f32", "df64"):
+        raise ValueError(f"unknown Jacobian precision {jac_precision!r}")
+    jreal = {"f64": "double", "f32": "float", "df64": "fe_df64"}[jac_precision]
+    jstore = "float" if jac_precision == "f32" else "double"
+    bodies = [_domain_source(k, dc, dim, params, nval, nh, smem_budget, nthreads_cap, jac_precision == "f32",
+                             jac_precision == "df64")
               for k, dc in enumerate(domains)]
     threads = max(32, max(((dc.rows_needed + 31) // 32) * 32 for dc in domains))
     smem = max(dc.smem for dc in domains)
     head = ["// generated fused multi-domain element kernel", '#include "fe_device.cuh"',
-            f"typedef {jreal} jreal;", f"#define FE_NT {threads}"]
+            f"typedef {jreal} jreal;", f"typedef {jstore} jstore;", f"#define FE_NT {threads}"]
     src = "\n".join(head + bodies)
     h = hashlib.sha1(src.encode()).hexdigest()[:12]
     name = f"fe_fused_{jac_precision}_{h}"
@@ -983,7 +1012,7 @@ class DropletProblem:
         # per block (both decide elements per block).  Defaults: the fastest
         # shapes autotune.tune measured on GB300 for the droplet (FP64 J: 512
         # threads / 200 KB, FP32 J: 128 threads / 64 KB)
-        f64 = jacobian_precision in ("fp64", "f64")
+        f64 = jacobian_precision in ("fp64", "f64", "df64")
         self.nthreads_cap = 512 if f64 else 128
         self.smem_budget = (200 if f64 else 64) * 1024
         # compile the element code with device-side bounds checks (status word 2)
@@ -1028,9 +1057,11 @@ class DropletProblem:
             dom(LINE3, surf_eqs, vel + [("_kin_bc", "C2")] + pos),
             dom(POINT1, pt_eqs, vel + pos),
         ]
-        prec = "f64" if self.jacobian_precision in ("fp64", "f64") else "f32"
+        jp = self.jacobian_precision
+        kprec = "df64" if jp == "df64" else ("f64" if jp in ("fp64", "f64") else "f32")
+        prec = "f32" if kprec == "f32" else "f64"   # storage of the Jacobian values
         self._prec = prec
-        self.kernel = generate_fused(self.domains, 2, self.param_names, nval, 2, prec,
+        self.kernel = generate_fused(self.domains, 2, self.param_names, nval, 2, kprec,
                                      smem_budget=self.smem_budget, nthreads_cap=self.nthreads_cap)
         self.conns = [m.conn, m.interface, m.contact_line]
         n = m.x.shape[0]

@@ -371,12 +371,13 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         per_elem = ((nn * dim + 2 * nn * nval + nq * ntc + geo_doubles) * 8
                     + (nq * ndnz + nq * nn * dim + (nq * nn1 * dim if has_c1 else 0)) * jbytes)
     if epb is None:
-        # df64: at most 352 threads (GB300 sweeps: the Q2 hex kernel runs
-        # fastest with 12-13 elements per block, the P2 triangle is flat
-        # between 16 and 64)
+        # df64: the most elements that fit 720 threads and 224 KB (GB300
+        # sweeps: the Q2 hex kernel is fastest at 12 elements per block, the
+        # largest that fits the shared memory; the P2 Taylor-Hood kernel at
+        # 48, 720 threads)
         epb, threads = _launch_shape(et, nloc, per_elem, table_bytes,
                                      smem_cap=224 * 1024 if df64 else 200 * 1024,
-                                     max_threads=352 if df64 else 512, largest=df64)
+                                     max_threads=720 if df64 else 512, largest=df64)
     else:
         threads = ((max(epb * nq, epb * nloc) + 31) // 32) * 32
     smem = table_bytes + epb * per_elem

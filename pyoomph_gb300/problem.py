@@ -218,6 +218,18 @@ class Problem:
             ks = generate_kernel(mesh.etype, pw, kprec, epb=self.elems_per_block, affine=self.affine,
                                  jref=self.jacobian_reference)
             _KERNEL_CACHE[key] = ks
+        if kprec == "df64" and self.elems_per_block is None and mesh.n_elem < 128 * ks.epb:
+            # the df64 kernels take the largest blocks that fit; a small mesh
+            # then leaves SMs idle: keep at least 128 blocks (Poisson Q2 64^2
+            # on GB300: 64 elements/block 85 us, 32: 56 us)
+            epb = max(8, mesh.n_elem // 128)
+            if epb < ks.epb:
+                key2 = key[:-2] + (epb, self.jacobian_reference)
+                ks = _KERNEL_CACHE.get(key2)
+                if ks is None:
+                    ks = generate_kernel(mesh.etype, differentiate(fields, mesh.dim, integrand, used), kprec,
+                                         epb=epb, affine=self.affine, jref=self.jacobian_reference)
+                    _KERNEL_CACHE[key2] = ks
         self.kernel: KernelSpec = ks
         self.timings.update(setup_mesh_s=t1 - t0, codegen_s=time.perf_counter() - t1)
         # nodal values, pins and equation numbers

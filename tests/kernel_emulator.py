@@ -158,7 +158,7 @@ def run_fused(fk, conns, values, hist, x0, params, flag: int = 1, aux: int = 0, 
     fa = _FusedArgs()
     keep, outs = [], []
     nb = 0
-    jt = np.float64 if fk.jac_precision == "f64" else np.float32
+    jt = np.float32 if fk.jac_precision == "f32" else np.float64
     for k, (dc, conn) in enumerate(zip(fk.domains, conns)):
         conn = np.ascontiguousarray(conn, dtype=np.int32)
         tables = np.ascontiguousarray(dc.dtype.tables(), dtype=np.float64)

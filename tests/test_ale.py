@@ -85,7 +85,7 @@ def test_droplet_mesh_matches_oracle():
 
 
 @pytest.mark.parametrize("N,theta,prec", [(3, 60.0, "fp64"), (4, 120.0, "fp64"), (6, 110.0, "fp64"),
-                                          (4, 90.0, "fp32")])
+                                          (4, 90.0, "fp32"), (4, 90.0, "df64"), (6, 110.0, "df64")])
 def test_emulated_fused_kernel_matches_oracle(N, theta, prec):
     P = ale.DropletProblem(N=N, contact_angle_deg=theta, jacobian_precision=prec)
     fk = P.lower()
@@ -98,7 +98,7 @@ def test_emulated_fused_kernel_matches_oracle(N, theta, prec):
         ref = A.element_res_jac(D, v, [h0, h1], p)
         for (Re, Je), (Ro, Jo) in zip(outs, ref):
             assert np.max(np.abs(Re - Ro)) <= 1e-12 * np.max(np.abs(Ro))
-            tol = 1e-12 if prec == "fp64" else 1e-6
+            tol = 1e-6 if prec == "fp32" else 1e-12
             assert np.max(np.abs(Je.astype(np.float64) - Jo)) <= tol * np.max(np.abs(Jo))
 
 
@@ -217,6 +217,25 @@ def test_gpu_time_steps_match_oracle():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("N,theta", [(3, 60.0), (6, 110.0)])
+def test_gpu_df64_assembly_matches_oracle(N, theta):
+    """The double-float Jacobian of the fused moving-mesh kernel: pattern
+    bit-exact, R and J within the FP64 contract."""
+    P = _gpu_problem(N, theta, "df64")
+    D = A.droplet(N)
+    p = _params(theta)
+    P.set_params(**{k: p[k] for k in ("__bdf0", "__bdf1", "__bdf2")})
+    v, h0, h1 = _state(D, 7)
+    P.set_state(v, [h0, h1])
+    R, J = P.get_jacobian()
+    Ro, orp, oci, ov = A.assemble(D, v, [h0, h1], p)
+    rp, ci = P.pattern()
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    assert np.max(np.abs(R - Ro)) <= 1e-12 * np.max(np.abs(Ro))
+    assert np.max(np.abs(J.data - ov)) <= 1e-12 * np.max(np.abs(ov))
+
+
+@pytest.mark.gpu
 def test_gpu_fp32_jacobian_converges_to_fp64_solution():
     N, theta, dt = 6, 110.0, 1e-3
     P64 = _gpu_problem(N, theta, "fp64")
@@ -279,7 +298,7 @@ def test_gpu_full_size_jacobian_is_the_derivative_of_the_residual():
 # ---------------------------------------------------------------------------
 # mass matrices and parameter derivatives
 # ---------------------------------------------------------------------------
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "df64"])
 def test_emulated_mass_matrix_and_parameter_derivatives(prec):
     P = ale.DropletProblem(N=4, contact_angle_deg=75.0, jacobian_precision=prec)
     fk = P.lower()
@@ -288,7 +307,7 @@ def test_emulated_mass_matrix_and_parameter_derivatives(prec):
     v, h0, h1 = _state(D, 2)
     outs, status = KE.run_fused(fk, P.conns, v, [h0, h1], D.x0, _pvec(P, p), flag=2)
     assert not status.any()
-    tol = 1e-12 if prec == "fp64" else 1e-6
+    tol = 1e-6 if prec == "fp32" else 1e-12
     for (_, Me), Mo in zip(outs, A.element_mass(D, v, [h0, h1], p)):
         assert np.max(np.abs(Me.astype(np.float64) - Mo)) <= tol * max(1.0, np.max(np.abs(Mo)))
     for name in ("dynamic_viscosity", "surface_tension", "contact_angle"):
