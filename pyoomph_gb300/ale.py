@@ -816,8 +816,15 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
                 if parts:
                     if df64:
                         w("          " + " ".join(f"fe_mac(Jr[{col}], {x_}, {y_});" for x_, y_ in parts))
-                    else:
+                    elif f32:
                         w(f"          Jr[{col}] += {' + '.join(f'{x_} * {y_}' for x_, y_ in parts)};")
+                    else:
+                        # FP64: nested FMAs into the accumulator, one FP64 add
+                        # fewer per update (the pipe that bounds the kernel)
+                        ch = f"Jr[{col}]"
+                        for x_, y_ in parts:
+                            ch = f"fe_fma({x_}, {y_}, {ch})"
+                        w(f"          Jr[{col}] = {ch};")
                     fl_tj += sum(_ops(f"{x_} * {y_}") for x_, y_ in parts) + len(parts)
         w("        }")
         # mass matrix: the coefficients of the time-derivative components, basis psi
@@ -838,8 +845,10 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
                         val = f"fps1[{s_}]" if lowp else f"sPsi1[q * N1 + {s_}]"
                     if df64:
                         w(f"          fe_mac(Jr[{col}], av{ic}, {val});")
-                    else:
+                    elif f32:
                         w(f"          Jr[{col}] += av{ic} * {val};")
+                    else:
+                        w(f"          Jr[{col}] = fe_fma(av{ic}, {val}, Jr[{col}]);")
             w("        }")
         w("      }")
         w("      break;")
