@@ -104,6 +104,8 @@ def _main(argv=None) -> None:
     ap.add_argument("precision", choices=["fp64", "fp32", "df64"])
     ap.add_argument("repeat", type=int, nargs="?", default=3)
     ap.add_argument("--epb", type=int, default=None, help="elements per block (default: the generator's)")
+    ap.add_argument("--jref", type=int, choices=[0, 1], default=None,
+                    help="1: contract the Jacobian in reference coordinates, 0: physical (default: the generator's)")
     a = ap.parse_args(argv)
     if a.workload == "ns":
         P = navier_stokes_problem(N=a.side, jacobian_precision=a.precision)
@@ -112,6 +114,8 @@ def _main(argv=None) -> None:
     else:
         P = nonlinear_diffusion_problem(N=a.side, seed=0, jacobian_precision=a.precision)
     P.elems_per_block = a.epb
+    if a.jref is not None:
+        P.jacobian_reference = bool(a.jref)
     P.initialise()
     perturb_dofs(P, seed=0, sigma=1e-3)
     P.assemble_device(with_jacobian=True)

@@ -53,6 +53,28 @@ def test_null_arguments_are_rejected():
     assert L.fe_assemble(None, None, None, None, 3, None) == N.FE_ERR_ARG
 
 
+def test_krylov_solver_arguments_are_checked_before_any_device_call():
+    """fe_krylov_* reject bad arguments with FE_ERR_ARG (no GPU needed):
+    null handles and buffers, an empty matrix, rows that do not split into
+    the blocks, an unknown value precision, a check interval out of range."""
+    from pyoomph_gb300 import _native as N
+    L = N.load()
+    out = ctypes.c_void_p()
+    fake = ctypes.c_void_p(16)   # never dereferenced: the checks fail first
+    assert L.fe_krylov_create(None, None, None, N.FE_JAC_F64, 10, 10, 1, 8, 1, ctypes.byref(out)) == N.FE_ERR_ARG
+    assert L.fe_krylov_create(fake, fake, fake, N.FE_JAC_F64, 0, 10, 1, 8, 1, ctypes.byref(out)) == N.FE_ERR_ARG
+    assert L.fe_krylov_create(fake, fake, fake, N.FE_JAC_F64, 10, 10, 3, 8, 1, ctypes.byref(out)) == N.FE_ERR_ARG
+    assert "equal blocks" in L.fe_last_error().decode()
+    assert L.fe_krylov_create(fake, fake, fake, 7, 10, 10, 1, 8, 1, ctypes.byref(out)) == N.FE_ERR_ARG
+    assert L.fe_krylov_create(fake, fake, fake, N.FE_JAC_F64, 10, 10, 1, 0, 1, ctypes.byref(out)) == N.FE_ERR_ARG
+    assert L.fe_krylov_create(fake, fake, fake, N.FE_JAC_F64, 10, 10, 1, 8, 1, None) == N.FE_ERR_ARG
+    assert L.fe_krylov_solve(None, None, None, 1e-12, 10, 1, None, None, None) == N.FE_ERR_ARG
+    assert L.fe_krylov_matvec(None, None, None, None) == N.FE_ERR_ARG
+    assert L.fe_krylov_info(None, None, None, None) == N.FE_ERR_ARG
+    L.fe_krylov_destroy(None)
+    assert L.fe_csr_spmv(None, None, None, N.FE_JAC_F64, None, None, 10, 10, None) == N.FE_ERR_ARG
+
+
 @pytest.mark.parametrize("kind", ["poisson", "poisson_p2", "ns", "ns32", "nsdf", "hex", "hex32", "hexdf"])
 def test_generated_kernels_compile_for_sm103a(kind, tmp_path):
     from pyoomph_gb300 import _native as N

@@ -165,3 +165,22 @@ def test_fp32_values_widen_exactly():
     y = torch.empty_like(x)
     A.matvec(x, y, torch.cuda.current_stream().cuda_stream)
     assert np.array_equal(y.cpu().numpy(), vals32.astype(np.float64), equal_nan=True)
+
+
+def test_non_finite_right_hand_side_is_an_error():
+    import torch
+    from pyoomph_gb300 import workloads as W
+    from pyoomph_gb300.linsolve import BatchedBiCGStab, DeviceCSR, LinearSolverError
+    P = W.poisson_problem(N=8, seed=3)
+    P.initialise()
+    P.get_jacobian()
+    b = P.R_dev[:P.n_dof].clone()
+    b[5] = float("nan")
+    with pytest.raises(LinearSolverError, match="non-finite"):
+        BatchedBiCGStab(DeviceCSR.of_problem(P)).solve(b, tol=1e-13)
+    # the solver object stays usable after the error
+    K = BatchedBiCGStab(DeviceCSR.of_problem(P))
+    with pytest.raises(LinearSolverError):
+        K.solve(b)
+    x, its = K.solve(P.R_dev[:P.n_dof], tol=1e-13)
+    assert torch.isfinite(x).all() and its[0] > 0
