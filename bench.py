@@ -58,7 +58,8 @@ def run_serving(args):
     per_rate = {}
     results = {}
     for rate in rates:
-        reqs = S.make_stream(args.requests, rate=rate, seed=0, side_range=(16, args.size))
+        reqs = S.make_stream(args.requests, rate=rate, seed=0, side_range=(16, args.size),
+                             ns_side_max=args.ns_side_max)
         srv = S.Server(slots=4, jacobian_precision="fp32", workers=workers, device_solver=args.device_solver)
         t0 = time.perf_counter()
         done = srv.run(copy.deepcopy(reqs))
@@ -71,9 +72,10 @@ def run_serving(args):
         if rate == rates[0]:
             results["batched"] = {r.rid: r.dofs for r in done}
         srv.close()
-    reqs = S.make_stream(args.requests, rate=rates[0], seed=0, side_range=(16, args.size))
+    reqs = S.make_stream(args.requests, rate=rates[0], seed=0, side_range=(16, args.size),
+                         ns_side_max=args.ns_side_max)
     t0 = time.perf_counter()
-    seq = S.serve_sequential(copy.deepcopy(reqs), precision="fp64")
+    seq = S.serve_sequential(copy.deepcopy(reqs), precision="fp64", device_solver=args.device_solver)
     wall = time.perf_counter() - t0
     s_ = S.summary(seq, wall)
     s_["wall_s"] = wall
@@ -85,6 +87,7 @@ def run_serving(args):
             "dtype": "f64 residual, f32 Jacobian", "data": "synthetic",
             "config": {"workload": WORKLOADS["serving"][0], "requests": args.requests, "rates_per_s": rates,
                        "headline_rate_per_s": rates[min(1, len(rates) - 1)], "side_range": [16, args.size],
+                       "ns_side_max": args.ns_side_max,
                        "slots_per_class": 4,
                        "linear_solver": (f"Poisson: native batched BiCGStab on the device; Navier-Stokes: SuperLU "
                                          f"(scipy), {workers} worker processes") if args.device_solver else
@@ -759,6 +762,8 @@ def main():
     ap.add_argument("--autotune", action="store_true", help="time the element kernels' launch shapes first")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--rates", default="10,20,50")
+    ap.add_argument("--ns-side-max", type=int, default=None,
+                    help="serving: cap the Navier-Stokes requests' sides (their solves stay on the host)")
     ap.add_argument("--device-solver", action="store_true",
                     help="serving: solve the Poisson requests' Newton systems on the device")
     args = ap.parse_args()

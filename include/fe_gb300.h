@@ -262,7 +262,9 @@ int fe_csr_diagonal(const int32_t *rowptr, const int32_t *colidx, const void *va
  *
  * Every scalar and every reduction is per block, the reductions run over
  * fixed chunks of a block's rows in a fixed order, and a block stops at the
- * iteration its own residual reaches tol * ||b_s||_inf: a block's solution
+ * iteration its own residual reaches max(tol * ||b_s||_inf, atol) (atol:
+ * an absolute floor, e.g. a fraction of a Newton tolerance; a block whose
+ * ||b_s|| is already below it returns x_s = 0): a block's solution
  * is bit-identical whatever the other blocks hold.  Iterations run on the
  * solver's own stream (ordered after and before `stream` by events), in
  * blocks of check_every iterations replayed as one CUDA graph (use_graph);
@@ -282,8 +284,8 @@ int fe_csr_diagonal(const int32_t *rowptr, const int32_t *colidx, const void *va
 typedef struct fe_krylov fe_krylov_t;
 int fe_krylov_create(const int32_t *rowptr, const int32_t *colidx, const void *vals, int val_precision, int64_t n,
                      int64_t nnz, int32_t blocks, int32_t check_every, int32_t use_graph, fe_krylov_t **out);
-int fe_krylov_solve(fe_krylov_t *k, const double *b, const uint8_t *active, double tol, int64_t maxiter,
-                    int32_t max_restarts, double *x, int64_t *iterations, void *stream);
+int fe_krylov_solve(fe_krylov_t *k, const double *b, const uint8_t *active, double tol, double atol,
+                    int64_t maxiter, int32_t max_restarts, double *x, int64_t *iterations, void *stream);
 /* y = A x (every row, DEVICE vectors of n) with the solver's matrix and
  * SpMV kernel (that of fe_csr_spmv).  Ordered on `stream`. */
 int fe_krylov_matvec(fe_krylov_t *k, const double *x, double *y, void *stream);

@@ -156,7 +156,7 @@ def load(build_if_missing: bool = True):
         L.fe_csr_spmv.argtypes = [vp, vp, vp, c_int, vp, vp, i64, i64, vp]
         L.fe_csr_diagonal.argtypes = [vp, vp, vp, c_int, vp, i64, vp]
         L.fe_krylov_create.argtypes = [vp, vp, vp, c_int, i64, i64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, vp]
-        L.fe_krylov_solve.argtypes = [vp, vp, vp, ctypes.c_double, i64, ctypes.c_int32, vp, vp, vp]
+        L.fe_krylov_solve.argtypes = [vp, vp, vp, ctypes.c_double, ctypes.c_double, i64, ctypes.c_int32, vp, vp, vp]
         L.fe_krylov_info.argtypes = [vp, vp, vp, vp]
         L.fe_krylov_matvec.argtypes = [vp, vp, vp, vp]
         L.fe_krylov_destroy.argtypes = [vp]

@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(KR_T) k_kr_init(KrView k) {
 }
 
 // status RESTART (active) or IDLE on entry
-__global__ void __launch_bounds__(KR_T) k_kr_init_sc(KrView k, double tol) {
+__global__ void __launch_bounds__(KR_T) k_kr_init_sc(KrView k, double tol, double atol) {
   __shared__ double sh[KR_T / 32];
   const int blk = blockIdx.x;
   if (k.status[blk] != KR_RESTART) return;
@@ -174,8 +174,9 @@ __global__ void __launch_bounds__(KR_T) k_kr_init_sc(KrView k, double tol) {
     if (zero > 0.0) e |= KE_ZERO_DIAG;
     if (bad > 0.0) e |= KE_NONFINITE_B;
     k.err[blk] = e;
-    k.target[blk] = tol * bmax;
-    if (e || bmax == 0.0) k.status[blk] = KR_IDLE;  // b_s = 0: x_s = 0
+    const double t = fmax(tol * bmax, atol);
+    k.target[blk] = t;
+    if (e || bmax == 0.0 || bmax <= t) k.status[blk] = KR_IDLE;  // x_s = 0 already meets the target
   }
 }
 
@@ -549,7 +550,7 @@ int fe_krylov_info(const fe_krylov_t *k, int64_t *launches, int64_t *graph_repla
 }
 
 namespace {
-int krylov_solve(fe_krylov_t *K, const double *b, const uint8_t *active, double tol, int64_t maxiter,
+int krylov_solve(fe_krylov_t *K, const double *b, const uint8_t *active, double tol, double atol, int64_t maxiter,
                  int32_t max_restarts, double *x, int64_t *iterations) {
   KrView &k = K->k;
   const int S = k.S;
@@ -565,7 +566,7 @@ int krylov_solve(fe_krylov_t *K, const double *b, const uint8_t *active, double 
   else
     k_csr_diagonal<float><<<gd, 256, 0, st>>>(K->rowptr, K->colidx, (const float *)K->vals, k.t, K->n_total);
   k_kr_init<<<K->vgrid(), KR_T, 0, st>>>(k);
-  k_kr_init_sc<<<S, KR_T, 0, st>>>(k, tol);
+  k_kr_init_sc<<<S, KR_T, 0, st>>>(k, tol, atol);
   K->launches += 3;
   K->restart_sequence();
   CUDA_TRY(cudaGetLastError());
@@ -625,14 +626,14 @@ int krylov_solve(fe_krylov_t *K, const double *b, const uint8_t *active, double 
 }
 } // namespace
 
-int fe_krylov_solve(fe_krylov_t *K, const double *b, const uint8_t *active, double tol, int64_t maxiter,
-                    int32_t max_restarts, double *x, int64_t *iterations, void *stream) {
+int fe_krylov_solve(fe_krylov_t *K, const double *b, const uint8_t *active, double tol, double atol,
+                    int64_t maxiter, int32_t max_restarts, double *x, int64_t *iterations, void *stream) {
   if (!K || !b || !x) return fail(FE_ERR_ARG, "fe_krylov_solve: null argument");
-  if (!(tol >= 0.0)) return fail(FE_ERR_ARG, "fe_krylov_solve: tol must be >= 0");
+  if (!(tol >= 0.0) || !(atol >= 0.0)) return fail(FE_ERR_ARG, "fe_krylov_solve: tolerances must be >= 0");
   cudaStream_t ust = (cudaStream_t)stream;
   CUDA_TRY(cudaEventRecord(K->ev_in, ust));
   CUDA_TRY(cudaStreamWaitEvent(K->st, K->ev_in, 0));
-  int rc = krylov_solve(K, b, active, tol, maxiter, max_restarts, x, iterations);
+  int rc = krylov_solve(K, b, active, tol, atol, maxiter, max_restarts, x, iterations);
   if (rc) {
     cudaStreamSynchronize(K->st);  // nothing of a failed solve stays in flight
     return rc;

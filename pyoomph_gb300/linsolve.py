@@ -115,12 +115,16 @@ class BatchedBiCGStab:
     def graph_replays(self) -> int:
         return self.info()["graph_replays"]
 
-    def solve(self, b, active=None, tol: float = 1e-13, maxiter: int = 20000, max_restarts: int = 20):
+    def solve(self, b, active=None, tol: float = 1e-13, maxiter: int = 20000, max_restarts: int = 20,
+              stream=None, atol: float = 0.0):
         """Solve A_s x_s = b_s for the active blocks s (all by default); b is
         the stacked right-hand side (S*n,) or (S, n) on the device.  Stops a
-        block when ||r_s||_inf <= tol * ||b_s||_inf.  Returns (x, iterations):
+        block when ||r_s||_inf <= max(tol * ||b_s||_inf, atol).  Returns (x, iterations):
         x the (S, n) result (inactive blocks hold 0), iterations per block
-        (multiples of check_every)."""
+        (multiples of check_every).  `stream` (a CUDA stream handle, default
+        the current stream) orders the solve after the work that produced b
+        and the work that reads x after it; the call releases the GIL while
+        it iterates, so other threads keep running."""
         torch = self.torch
         b = b.reshape(-1)
         if b.numel() != self.S * self.n or b.dtype != torch.float64 or not b.is_contiguous():
@@ -133,9 +137,10 @@ class BatchedBiCGStab:
         its = np.zeros(self.S, dtype=np.int64)
         rc = N.load().fe_krylov_solve(self._h, ctypes.c_void_p(b.data_ptr()),
                                       None if act is None else act.ctypes.data_as(ctypes.c_void_p),
-                                      float(tol), int(maxiter), int(max_restarts),
+                                      float(tol), float(atol), int(maxiter), int(max_restarts),
                                       ctypes.c_void_p(self.x.data_ptr()), its.ctypes.data_as(ctypes.c_void_p),
-                                      ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+                                      ctypes.c_void_p(torch.cuda.current_stream().cuda_stream
+                                                      if stream is None else stream))
         if rc == N.FE_ERR_SOLVER:
             raise LinearSolverError(N.load().fe_last_error().decode(errors="replace"))
         N.check(rc)

@@ -116,6 +116,9 @@ class Problem:
         # linear_solver = "bicgstab": J dx = R solved on the device (linsolve.py)
         # to this relative tolerance; None: SuperLU on the host (the reference's default)
         self.linear_solver_tolerance = 1e-13
+        # absolute floor of the device solve's residual (0: relative only);
+        # e.g. 0.1 x newton_solver_tolerance for an inexact Newton step
+        self.linear_solver_atol = 0.0
         self.verbose = False
         self._initialised = False
         self.newton_history: List[float] = []
@@ -649,7 +652,8 @@ class Problem:
                     if getattr(self, "_krylov", None) is None:
                         # one block per replica: each replica's solve is its own
                         self._krylov = BatchedBiCGStab(DeviceCSR.of_problem(self), blocks=self.replicas)
-                    dx2, its = self._krylov.solve(self.R_dev[:self.n_dof], tol=self.linear_solver_tolerance)
+                    dx2, its = self._krylov.solve(self.R_dev[:self.n_dof], tol=self.linear_solver_tolerance,
+                                                  atol=self.linear_solver_atol)
                     dxd = dx2.view(-1)
                     self.timings["krylov_iterations"] = self.timings.get("krylov_iterations", 0) + int(its.max())
                 else:

@@ -68,7 +68,7 @@ def test_krylov_solver_arguments_are_checked_before_any_device_call():
     assert L.fe_krylov_create(fake, fake, fake, 7, 10, 10, 1, 8, 1, ctypes.byref(out)) == N.FE_ERR_ARG
     assert L.fe_krylov_create(fake, fake, fake, N.FE_JAC_F64, 10, 10, 1, 0, 1, ctypes.byref(out)) == N.FE_ERR_ARG
     assert L.fe_krylov_create(fake, fake, fake, N.FE_JAC_F64, 10, 10, 1, 8, 1, None) == N.FE_ERR_ARG
-    assert L.fe_krylov_solve(None, None, None, 1e-12, 10, 1, None, None, None) == N.FE_ERR_ARG
+    assert L.fe_krylov_solve(None, None, None, 1e-12, 0.0, 10, 1, None, None, None) == N.FE_ERR_ARG
     assert L.fe_krylov_matvec(None, None, None, None) == N.FE_ERR_ARG
     assert L.fe_krylov_info(None, None, None, None) == N.FE_ERR_ARG
     L.fe_krylov_destroy(None)

@@ -184,3 +184,26 @@ def test_non_finite_right_hand_side_is_an_error():
         K.solve(b)
     x, its = K.solve(P.R_dev[:P.n_dof], tol=1e-13)
     assert torch.isfinite(x).all() and its[0] > 0
+
+
+def test_absolute_tolerance_is_per_block():
+    """atol is an absolute floor per block: a block whose right-hand side is
+    already below it returns x = 0 and takes no iteration; the others stop
+    at max(tol |b_s|, atol), each independently of the others."""
+    import torch
+    from pyoomph_gb300.linsolve import BatchedBiCGStab, DeviceCSR
+    P = _replicated_poisson(10, 2)
+    P.get_jacobian()
+    n = P.n_dof // 2
+    b = P.R_dev[:P.n_dof].clone().view(2, n)
+    b[1] *= 1e-14                       # block 1: |b| far below atol
+    K = BatchedBiCGStab(DeviceCSR.of_problem(P), blocks=2)
+    atol = 1e-9 * float(b[0].abs().max())
+    x, its = K.solve(b, tol=1e-13, atol=atol)
+    assert its[1] == 0 and not x[1].any()
+    assert its[0] > 0
+    # the true residual of block 0 meets the absolute floor (10x, the confirmation margin)
+    y = torch.empty(P.n_dof, dtype=torch.float64, device="cuda")
+    DeviceCSR.of_problem(P).matvec(x.reshape(-1), y, torch.cuda.current_stream().cuda_stream)
+    r0 = (b[0] - y.view(2, n)[0]).abs().max()
+    assert float(r0) <= 10 * atol
