@@ -356,6 +356,24 @@ class Server:
         b.req[s].newton_iterations += 1
         b.state[s] = "assemble"
 
+    def _fail(self, b: _Batch, slots, exc: BaseException, t0: float, device: bool) -> List[Request]:
+        """End the requests of `slots` with the solve's error; free their slots."""
+        out = []
+        for s in slots:
+            req = b.req[s]
+            req.error = f"linear solve failed: {exc}"
+            req.dofs = b.P.x_dev[s * b.n_dof:(s + 1) * b.n_dof].cpu().numpy()
+            req.t_done = time.perf_counter() - t0
+            b.req[s] = None
+            b.state[s] = "free"
+            out.append(req)
+        if device:
+            b.inflight = False
+            for k, st_ in enumerate(b.state):
+                if st_ == "wait":
+                    b.state[k] = "assemble"
+        return out
+
     def close(self) -> None:
         self.pool.shutdown(wait=True)
         if self.tpool is not None:
@@ -397,7 +415,12 @@ class Server:
                 for f in dn:
                     b, s, ts = futs.pop(f)
                     self.t_solve += time.perf_counter() - ts
-                    if isinstance(s, tuple):
+                    exc = f.exception()
+                    if exc is not None:
+                        # a failed solve ends its requests with the error; the server goes on
+                        finished += self._fail(b, s if isinstance(s, tuple) else (s,), exc, t0,
+                                               device=isinstance(s, tuple))
+                    elif isinstance(s, tuple):
                         self._apply_device(b, s, f.result())
                     else:
                         self._apply(b, s, f.result())

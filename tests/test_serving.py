@@ -72,3 +72,31 @@ def test_device_solver_alone_equals_mix_and_matches_oracle():
         assert r.error is None
         x = _oracle_solution(r)
         assert np.max(np.abs(r.dofs - x)) <= 1e-10 * max(1.0, np.max(np.abs(x)))
+
+
+def test_failed_device_solve_ends_only_its_requests(monkeypatch):
+    """A device solve that raises (a fake of the failing call, on the host)
+    ends the requests of that solve with the error; the other requests of
+    the stream still complete and match the oracle."""
+    from pyoomph_gb300 import serving as S
+    from pyoomph_gb300.linsolve import LinearSolverError
+    real = S.Server._device_solve
+    calls = {"n": 0}
+
+    def flaky(self, b, mask, atol):
+        calls["n"] += 1
+        if calls["n"] == 1:
+            raise LinearSolverError("injected failure")
+        return real(self, b, mask, atol)
+    monkeypatch.setattr(S.Server, "_device_solve", flaky)
+    srv = S.Server(slots=2, tol=1e-12, device_solver=True)
+    reqs = [S.Request(1, "poisson", 10, 0.0, seed=1), S.Request(2, "ns", 8, 0.0, seed=2, Re=30.0),
+            S.Request(3, "poisson", 12, 0.0, seed=3)]
+    out = {r.rid: r for r in srv.run(reqs, realtime=False)}
+    srv.close()
+    failed = [r for r in out.values() if r.error]
+    assert len(out) == 3 and failed and all("injected failure" in r.error for r in failed)
+    for r in out.values():
+        if r.error is None:
+            x = _oracle_solution(r)
+            assert np.max(np.abs(r.dofs - x)) <= 1e-10 * max(1.0, np.max(np.abs(x)))
