@@ -86,7 +86,7 @@ class _Printer(C99CodePrinter):
             raise NotImplementedError("GaussianSum needs its parameters contiguous in the FP64 array")
         base = refs[0][:refs[0].index("[")]
         xq = self._names[E.X[0]][:self._names[E.X[0]].index("[")]
-        return f"fe_gauss_sum<{dim}>({xq}, {base} + {idx[0]}, {n})"
+        return f"FE_GAUSS({dim}, {xq}, {base} + {idx[0]}, {n})"
 
     def _print_exp(self, e):
         return f"{self._fn('exp')}({self._print(e.args[0])})"
@@ -186,8 +186,8 @@ def pointwise_source(pw: Pointwise, jreal: str = "double") -> str:
     nd = len(pw.d_entries)
     hdr = ("__device__ __forceinline__ void fe_pointwise(const double* __restrict__ U, "
            "const double* __restrict__ Xq, const double* __restrict__ P, double* __restrict__ r, "
-           "jreal* __restrict__ D, int flag) {")
-    lines = [hdr]
+           "jreal* __restrict__ D, int flag, const double* __restrict__ gsT, const int* __restrict__ gsI) {")
+    lines = [hdr, "  (void)gsT; (void)gsI;"]
     if jreal == "double" and nd:
         exprs = list(pw.r_exprs) + [d for (_, _, d) in pw.d_entries]
         outs = [f"r[{k}]" for k in range(nr)] + [f"D[{k}]" for k in range(nd)]
@@ -247,6 +247,7 @@ class KernelSpec:
     jac_precision: str
     tables: np.ndarray = field(repr=False, default=None)
     sumfac_blocks: int = 0       # > 0: sum-factorised Jacobian with this many (a, b) blocks
+    gauss_sep: int = 0           # > 0: this many Gaussians of the source evaluated separably per element
 
     @property
     def key(self) -> str:
@@ -279,7 +280,8 @@ def _launch_shape(et: ElementType, nloc: int, per_elem_bytes: int, table_bytes: 
 
 
 def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
-                    name: str = None, epb: int = None, affine: bool = False, jref: bool = None) -> KernelSpec:
+                    name: str = None, epb: int = None, affine: bool = False, jref: bool = None,
+                    gauss_sep: bool = False) -> KernelSpec:
     """Fused element kernel for one element type and weak form.
 
     Thread phases (all in one launch, EPB elements per block):
@@ -354,6 +356,21 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     tabf = (nq * nn * (1 + dim) + nq * nn1 * (1 + dim)) if tab_copy else 0
     table_bytes += ((tabf * (8 if df64 else 4) + 15) // 16) * 16
     geo_doubles = (dim * dim + 1) if affine else 0
+    # separable Gaussian source (axis-aligned affine Q2 elements, the caller
+    # checks the alignment): the element's per-axis factors in shared memory
+    gs_atoms = set()
+    for e_ in pw.r_exprs:
+        gs_atoms |= e_.atoms(E.GaussianSum)
+    gsep = bool(gauss_sep and affine and et.name in ("Q2_QUAD", "Q2_HEX") and len(gs_atoms) == 1)
+    gs_n = gs_base = 0
+    if gsep:
+        ga = next(iter(gs_atoms))
+        k0 = next(i for i, a_ in enumerate(ga.args) if a_.is_Integer)
+        gs_n, gdim = int(ga.args[k0]), int(ga.args[k0 + 1])
+        ref0 = _symbol_names(pw)[ga.args[k0 + 2]]
+        gs_base = int(ref0[ref0.index("[") + 1:-1])
+        gsep = gdim == dim
+    gsd = gs_n * dim * 3 if gsep else 0          # doubles per element
     # sum factorisation of the Q2 hex Jacobian (tensor-product shapes and
     # Gauss<3,3> knots): J_ij = sum_ab sum_q prod_d F^d_ab[q_d][i_d][j_d] Dhat_ab(q)
     # contracted one direction at a time (3 x 81 + 3 x 243 + 3 x 729 multiply-adds
@@ -364,11 +381,11 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     if sumfac:
         table_bytes += ((4 * 27 * jbytes + 15) // 16) * 16
     if jref:
-        per_elem = (nn * dim + 2 * nn * nval + nq * ntc + geo_doubles) * 8 + nq * ndnz_hat * jbytes
+        per_elem = (nn * dim + 2 * nn * nval + nq * ntc + geo_doubles + gsd) * 8 + nq * ndnz_hat * jbytes
         if sumfac:
             per_elem += (81 + 243 + 729) * jbytes
     else:
-        per_elem = ((nn * dim + 2 * nn * nval + nq * ntc + geo_doubles) * 8
+        per_elem = ((nn * dim + 2 * nn * nval + nq * ntc + geo_doubles + gsd) * 8
                     + (nq * ndnz + nq * nn * dim + (nq * nn1 * dim if has_c1 else 0)) * jbytes)
     if epb is None:
         # df64: the most elements that fit 720 threads and 224 KB (GB300
@@ -376,7 +393,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         # largest that fits the shared memory; the P2 Taylor-Hood kernel at
         # 48, 720 threads)
         epb, threads = _launch_shape(et, nloc, per_elem, table_bytes,
-                                     smem_cap=224 * 1024 if df64 else 200 * 1024,
+                                     smem_cap=224 * 1024 if df64 else 216 * 1024,
                                      max_threads=720 if df64 else 512, largest=df64)
     else:
         threads = ((max(epb * nq, epb * nloc) + 31) // 32) * 32
@@ -385,7 +402,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     if threads > 1024 or smem > 227 * 1024:
         raise ValueError(f"{epb} elements per block do not fit a block ({threads} threads, {smem} B shared)")
     if name is None:
-        h = hashlib.sha1((et.name + jac_precision + str(affine) + str(epb) + str(jref) + str(sumfac) + str(pw.r_exprs) +
+        h = hashlib.sha1((et.name + jac_precision + str(affine) + str(epb) + str(jref) + str(sumfac) + str(gsep) +
+                          str(pw.r_exprs) +
                           str(pw.d_entries)).encode()).hexdigest()[:10]
         name = f"fe_elem_{et.name.lower()}_{jac_precision}{'_aff' if affine else ''}_{h}"
 
@@ -411,6 +429,10 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         F_ = [repr(float(M_[c >> 1][q][i] * M_[c & 1][q][j]))
               for c in range(4) for q in range(3) for i in range(3) for j in range(3)]
         w(f"__constant__ double c_F[108] = {{{', '.join(F_)}}};")
+    if gsep:
+        w("#define FE_GAUSS(d, x, g, n) fe_gauss_sep<d>(gsT, gsI, g, n)")
+    else:
+        w("#define FE_GAUSS(d, x, g, n) fe_gauss_sum<d>(x, g, n)")
     w(pointwise_source(pw, jreal))
     w(f'extern "C" __global__ void __launch_bounds__(FE_NT) {name}(const FeElemArgs a) {{')
     w("  extern __shared__ __align__(16) unsigned char fe_smem[];")
@@ -424,7 +446,9 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("  double* sY = sU + FE_EPB * FE_NN * FE_NVAL;  // direction of the Hessian-vector product (flag 4)")
     w("  double* sRh = sY + FE_EPB * FE_NN * FE_NVAL;")
     w("  double* sG = sRh + FE_EPB * FE_NQ * FE_NTC;")
-    w(f"  jacc* sD = reinterpret_cast<jacc*>(sG + FE_EPB * {geo_doubles});")
+    w(f"  double* sGe = sG + FE_EPB * {geo_doubles};  // separable Gaussian factors, {gsd} per element")
+    w(f"  jacc* sD = reinterpret_cast<jacc*>(sGe + FE_EPB * {gsd});")
+    w("  (void)sGe;")
     if jref:
         w("  jacc* sEnd = sD + FE_EPB * FE_NQ * FE_NDNZH;")
         if tab_copy:
@@ -493,6 +517,25 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("    sg[FE_DIM * FE_DIM] = J;")
         w("  }")
         w("  __syncthreads();")
+    if gsep:
+        # ---------------- phase S: the separable Gaussian factors ----------------
+        # one thread per (element, Gaussian, axis, knot coordinate): x_d at the
+        # knot with index i along axis d and 0 along the others, formed as
+        # phase A forms Xq (vertex shapes of the affine map)
+        w(f"  for (int p = threadIdx.x; p < nel * {gsd}; p += FE_NT) {{")
+        w(f"    const int el = p / {gsd}, o = p - el * {gsd};")
+        w("    const int i = o % 3, kd = o / 3, d = kd % FE_DIM, k = kd / FE_DIM;")
+        w(f"    const int q = i * (FE_DIM == 3 ? (d == 0 ? 9 : d == 1 ? 3 : 1) : (d == 0 ? 3 : 1));")
+        w("    const double* X = sX + el * FE_NN * FE_DIM;")
+        w("    double xd = 0.0;")
+        for l, node in enumerate(et.c1_index):
+            w(f"    xd += X[{node} * FE_DIM + d] * sPsi1[q * FE_NN1 + {l}];")
+        w("    const double* Pe = a.params + (a.replica_elems > 0 ? ((e0 + el) / a.replica_elems) * a.params_stride : 0);")
+        w(f"    const double* g = Pe + {gs_base} + k * (FE_DIM + 2);")
+        w("    const double dd = xd - g[d], w = g[FE_DIM];")
+        w("    sGe[el * " + str(gsd) + " + o] = exp(-(dd * dd) / (2.0 * w * w));")
+        w("  }")
+        w("  __syncthreads();")
     # ---------------- phase A ----------------
     w("  for (int p = threadIdx.x; p < nel * FE_NQ; p += FE_NT) {")
     w("    const int el = p / FE_NQ, q = p - el * FE_NQ;")
@@ -559,7 +602,14 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     interp("U", "sU", "    ")
     w("    const double* Pe = a.params + (a.replica_elems > 0 ? ((e0 + el) / a.replica_elems) * a.params_stride : 0);")
     w("    double r[FE_NTC]; jreal D[FE_NDNZ];")
-    w("    fe_pointwise(U, Xq, Pe, r, D, flag);")
+    if gsep:
+        w("    int qI[FE_DIM];")
+        w("    { int qq = q;")
+        w("      #pragma unroll")
+        w("      for (int d = FE_DIM - 1; d >= 0; --d) { qI[d] = qq % 3; qq /= 3; } }")
+        w(f"    fe_pointwise(U, Xq, Pe, r, D, flag, sGe + el * {gsd}, qI);")
+    else:
+        w("    fe_pointwise(U, Xq, Pe, r, D, flag, nullptr, nullptr);")
     w("    double* rh = sRh + (el * FE_NQ + q) * FE_NTC;")
     w("    #pragma unroll")
     w("    for (int f = 0; f < FE_NF; ++f) {")
@@ -813,7 +863,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     source = "\n".join(src) + "\n"
     return KernelSpec(name=name, source=source, et=et, layout=layout, pointwise=pw, epb=epb,
                       threads=threads, smem_bytes=smem, jac_precision=jac_precision,
-                      tables=et.packed_tables(), sumfac_blocks=len(hat) if sumfac else 0)
+                      tables=et.packed_tables(), sumfac_blocks=len(hat) if sumfac else 0,
+                      gauss_sep=gs_n if gsep else 0)
 
 
 def _jacc_update(terms, acc: str, jacc: str) -> str:
@@ -854,13 +905,18 @@ def estimate_flops(ks: KernelSpec, affine: bool) -> Dict[str, float]:
         gs = list(e.atoms(E.GaussianSum))
         for g in gs:
             k0 = next(i for i, a in enumerate(g.args) if a.is_Integer)
-            ops_r += int(g.args[k0]) * (3 * D + 45)
+            # separable: D products and a sum per Gaussian and knot (the
+            # factors are counted per element below)
+            ops_r += int(g.args[k0]) * ((D + 1) if ks.gauss_sep else (3 * D + 45))
         ops_r += sp.count_ops(e.subs({g: 0 for g in gs}))
     per_q += ops_r
     per_q += len(fields) * (1 + 2 * D * D)
     rows = lay.n
     resid = rows * NQ * 2 * nc
     fp64 = NQ * per_q + (geo if affine else 0) + resid
+    if ks.gauss_sep:
+        # per element: 3 D factors per Gaussian (the affine map along the axis, exp)
+        fp64 += ks.gauss_sep * D * 3 * (2 * N1 + 48)
     ops_d = sum(sp.count_ops(d) for (_, _, d) in pw.d_entries)
     jac_q = ops_d + len(pw.d_entries) + 2 * NN * D * D + (2 * N1 * D * D if any(s == "C1" for _, s in fields) else 0)
     used_ic = sorted({ic for (_, ic, _) in pw.d_entries})

@@ -142,4 +142,23 @@ __device__ __noinline__ double fe_gauss_sum(const double *__restrict__ Xq, const
   return f;
 }
 
+// The same sum on an axis-aligned affine tensor-product element, separably:
+// exp(-|x-c|^2/(2w^2)) = prod_d exp(-(x_d-c_d)^2/(2w^2)), and along axis d
+// the knots take only three coordinates, so the element's factors
+// T[k][d][i] are evaluated once per element (3 DIM exponentials per
+// Gaussian instead of one per knot); qi = the knot's index along each axis.
+template <int DIM>
+__device__ __forceinline__ double fe_gauss_sep(const double *__restrict__ T, const int *__restrict__ qi,
+                                               const double *__restrict__ g, int n) {
+  double f = 0.0;
+#pragma unroll 1
+  for (int k = 0; k < n; ++k, g += DIM + 2, T += DIM * 3) {
+    double p = g[DIM + 1];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) p *= T[d * 3 + qi[d]];
+    f += p;
+  }
+  return f;
+}
+
 #endif

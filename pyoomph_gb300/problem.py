@@ -31,6 +31,23 @@ from .equations import (SPACE_ORDER, BoundaryCondition, DirichletBC, EquationPar
 from .meshes import MeshData, MeshTemplate
 
 
+def mesh_is_axis_aligned(mesh: MeshData, rtol: float = 1e-14) -> bool:
+    """True if every element's reference axis a maps onto physical axis a
+    alone (the affine map's Jacobian dx/ds is diagonal at the element
+    centre, off-diagonal entries below rtol of the diagonal): the
+    structured rectangle and cuboid meshes.  Tensor-product elements of such
+    a mesh take three coordinates per axis at their 3^dim Gauss points."""
+    et = mesh.etype
+    if et.name not in ("Q2_QUAD", "Q2_HEX"):
+        return False
+    _, d1 = et.shape_c1(np.zeros(mesh.dim))
+    Xv = mesh.x[mesh.conn[:, list(et.c1_index)]]                 # [E, vertices, D]
+    A = np.einsum("eld,la->eda", Xv, d1)                        # [E, physical, reference]
+    diag = np.abs(np.einsum("edd->ed", A))
+    off = np.abs(A).sum(axis=2) - diag
+    return bool(np.all(off <= rtol * diag) and np.all(diag > 0))
+
+
 def mesh_is_affine(mesh: MeshData, rtol: float = 1e-12) -> bool:
     """True if every element's map from reference to physical coordinates is
     affine: the tangent vectors dx/ds are the same at all integration points
@@ -116,6 +133,11 @@ class Problem:
         # linear_solver = "bicgstab": J dx = R solved on the device (linsolve.py)
         # to this relative tolerance; None: SuperLU on the host (the reference's default)
         self.linear_solver_tolerance = 1e-13
+        # Gaussian source terms on axis-aligned affine Q2 meshes: evaluate the
+        # per-axis factors once per element (3 dim exponentials per Gaussian
+        # instead of one per knot); the values differ from the per-knot
+        # evaluation by rounding only
+        self.separable_source = True
         # absolute floor of the device solve's residual (0: relative only);
         # e.g. 0.1 x newton_solver_tolerance for an inexact Newton step
         self.linear_solver_atol = 0.0
@@ -213,13 +235,14 @@ class Problem:
             self.affine = self.geometry == "affine"
         # the kernel depends on the weak form, element type, precision and
         # geometry kind only -- not on the mesh size: cache it per process
-        key = (mesh.etype.name, tuple(fields), str(integrand), tuple(used), kprec, self.affine, self.elems_per_block,
-               self.jacobian_reference)
+        gsep = bool(self.separable_source and self.affine and mesh_is_axis_aligned(mesh))
+        key = (mesh.etype.name, tuple(fields), str(integrand), tuple(used), kprec, self.affine, gsep,
+               self.elems_per_block, self.jacobian_reference)
         ks = _KERNEL_CACHE.get(key)
         if ks is None:
             pw = differentiate(fields, mesh.dim, integrand, used)
             ks = generate_kernel(mesh.etype, pw, kprec, epb=self.elems_per_block, affine=self.affine,
-                                 jref=self.jacobian_reference)
+                                 jref=self.jacobian_reference, gauss_sep=gsep)
             _KERNEL_CACHE[key] = ks
         if kprec == "df64" and self.elems_per_block is None and mesh.n_elem < 128 * ks.epb:
             # the df64 kernels take the largest blocks that fit; a small mesh
@@ -231,7 +254,8 @@ class Problem:
                 ks = _KERNEL_CACHE.get(key2)
                 if ks is None:
                     ks = generate_kernel(mesh.etype, differentiate(fields, mesh.dim, integrand, used), kprec,
-                                         epb=epb, affine=self.affine, jref=self.jacobian_reference)
+                                         epb=epb, affine=self.affine, jref=self.jacobian_reference,
+                                         gauss_sep=gsep)
                     _KERNEL_CACHE[key2] = ks
         self.kernel: KernelSpec = ks
         self.timings.update(setup_mesh_s=t1 - t0, codegen_s=time.perf_counter() - t1)
