@@ -31,6 +31,23 @@ from .equations import (SPACE_ORDER, BoundaryCondition, DirichletBC, EquationPar
 from .meshes import MeshData, MeshTemplate
 
 
+def _sm_count() -> int:
+    """Streaming multiprocessors of device 0 (152 on GB300; also the value
+    used where no device is visible, so that the generated kernels are the
+    same with and without one)."""
+    global _SMS
+    if _SMS is None:
+        try:
+            n = ctypes.c_int()
+            _SMS = n.value if N.load().fe_device_info(ctypes.byref(n), None, None, None, None) == 0 else 152
+        except Exception:
+            _SMS = 152
+    return _SMS
+
+
+_SMS = None
+
+
 def mesh_is_axis_aligned(mesh: MeshData, rtol: float = 1e-14) -> bool:
     """True if every element's reference axis a maps onto physical axis a
     alone (the affine map's Jacobian dx/ds is diagonal at the element
@@ -244,19 +261,25 @@ class Problem:
             ks = generate_kernel(mesh.etype, pw, kprec, epb=self.elems_per_block, affine=self.affine,
                                  jref=self.jacobian_reference, gauss_sep=gsep)
             _KERNEL_CACHE[key] = ks
-        if kprec == "df64" and self.elems_per_block is None and mesh.n_elem < 128 * ks.epb:
-            # the df64 kernels take the largest blocks that fit; a small mesh
-            # then leaves SMs idle: keep at least 128 blocks (Poisson Q2 64^2
-            # on GB300: 64 elements/block 85 us, 32: 56 us)
-            epb = max(8, mesh.n_elem // 128)
+        if self.elems_per_block is None:
+            # balance the waves: with W = ceil(E / (SMs x EPB)) waves of one
+            # block per SM, EPB' = ceil(E / (SMs x W)) fills every wave as
+            # evenly (small meshes: Poisson Q2 64^2, 4,096 elements, 32 per
+            # block = 128 blocks on 152 SMs; 27 per block = one full wave,
+            # 10% faster on GB300; large meshes keep their shape)
+            sms = _sm_count()
+            n_el = mesh.n_elem * max(1, int(self.replicas))     # one launch covers every replica
+            waves = -(-n_el // (sms * ks.epb))
+            epb = max(1, -(-n_el // (sms * waves)))
             if epb < ks.epb:
                 key2 = key[:-2] + (epb, self.jacobian_reference)
-                ks = _KERNEL_CACHE.get(key2)
-                if ks is None:
-                    ks = generate_kernel(mesh.etype, differentiate(fields, mesh.dim, integrand, used), kprec,
-                                         epb=epb, affine=self.affine, jref=self.jacobian_reference,
-                                         gauss_sep=gsep)
-                    _KERNEL_CACHE[key2] = ks
+                ks2 = _KERNEL_CACHE.get(key2)
+                if ks2 is None:
+                    ks2 = generate_kernel(mesh.etype, differentiate(fields, mesh.dim, integrand, used), kprec,
+                                          epb=epb, affine=self.affine, jref=self.jacobian_reference,
+                                          gauss_sep=gsep)
+                    _KERNEL_CACHE[key2] = ks2
+                ks = ks2
         self.kernel: KernelSpec = ks
         self.timings.update(setup_mesh_s=t1 - t0, codegen_s=time.perf_counter() - t1)
         # nodal values, pins and equation numbers
