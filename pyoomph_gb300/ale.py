@@ -815,7 +815,8 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
                         parts.append((f"av{ic} * w0j", val))
                 if parts:
                     if df64:
-                        w("          " + " ".join(f"fe_mac(Jr[{col}], {x_}, {y_});" for x_, y_ in parts))
+                        w("          " + " ".join(f"fe_mac(Jr[{col}], {x_}, {y_});" for x_, y_ in parts)
+                          + f" Jr[{col}] = fe_norm(Jr[{col}]);")
                     elif f32:
                         w(f"          Jr[{col}] += {' + '.join(f'{x_} * {y_}' for x_, y_ in parts)};")
                     else:
@@ -844,7 +845,7 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
                     else:
                         val = f"fps1[{s_}]" if lowp else f"sPsi1[q * N1 + {s_}]"
                     if df64:
-                        w(f"          fe_mac(Jr[{col}], av{ic}, {val});")
+                        w(f"          fe_mac(Jr[{col}], av{ic}, {val}); Jr[{col}] = fe_norm(Jr[{col}]);")
                     elif f32:
                         w(f"          Jr[{col}] += av{ic} * {val};")
                     else:

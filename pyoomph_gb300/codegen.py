@@ -715,7 +715,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                 # one accumulator over all (a, b) blocks: each thread owns its entries
                 w(f"      jacc v = {'(jacc)0' if kk == 0 else 'sJe[p]'};")
                 w("      fe_mac(v, F[0], S2[0]); fe_mac(v, F[9], S2[81]); fe_mac(v, F[18], S2[162]);")
-                w("      sJe[p] = v;")
+                w("      sJe[p] = fe_norm(v);")
             elif kk == 0:
                 w("      sJe[p] = F[0] * S2[0] + F[9] * S2[81] + F[18] * S2[162];")
             else:
@@ -797,7 +797,12 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                     else:
                         terms.append((f"h{f}_{bh}", f"(jacc)dps_[{ls * dim + bh - 1}]"))
                 if df64:
-                    w("          " + " ".join(f"fe_mac(Jr[{layout.loc_of[f][ls]}], {x_}, {y_});" for x_, y_ in terms))
+                    # renormalised after each group of multiply-adds: the
+                    # compensation word's error then grows linearly, not
+                    # quadratically, with the number of knots
+                    col = layout.loc_of[f][ls]
+                    w("          " + " ".join(f"fe_mac(Jr[{col}], {x_}, {y_});" for x_, y_ in terms)
+                      + f" Jr[{col}] = fe_norm(Jr[{col}]);")
                 else:
                     w(f"          Jr[{layout.loc_of[f][ls]}] {_jacc_update(terms, f'Jr[{layout.loc_of[f][ls]}]', jacc)};")
             w("        }")

@@ -100,8 +100,11 @@ __device__ __forceinline__ fe_df64 &operator+=(fe_df64 &a, fe_df64 b) {
 // error, the exact two-sum of the running high part and the product forms
 // the sum's error, and both errors accumulate in acc.lo without a
 // renormalisation per step (12 FP32 instructions instead of 18).  acc.lo then
-// holds up to ~(terms) ulp(acc.hi); fe_norm restores |lo| <= ulp(hi) / 2
-// before the value is used as an operand.
+// holds up to ~(terms) ulp(acc.hi), and the rounding of the additions into it
+// grows as (terms)^2 u^2 (u = 2^-24); fe_norm restores |lo| <= ulp(hi) / 2.
+// The generated contractions renormalise after every group of a few
+// multiply-adds (one knot's terms of one entry), which keeps the error
+// bound linear in the number of groups: n m u^2 sum|terms| for n groups of m.
 __device__ __forceinline__ void fe_mac(fe_df64 &acc, fe_df64 b, fe_df64 c) {
   const float p = __fmul_rn(b.hi, c.hi);
   float pe = __fmaf_rn(b.hi, c.hi, -p);
