@@ -248,6 +248,7 @@ class KernelSpec:
     tables: np.ndarray = field(repr=False, default=None)
     sumfac_blocks: int = 0       # > 0: sum-factorised Jacobian with this many (a, b) blocks
     gauss_sep: int = 0           # > 0: this many Gaussians of the source evaluated separably per element
+    sum_fact_interp: bool = False  # interpolation and residual contraction sum-factorised (Q2 hex)
 
     @property
     def key(self) -> str:
@@ -380,6 +381,12 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     sumfac = bool(jref and et.name == "Q2_HEX" and nf == 1 and spaces[0] == "C2" and jac_precision in ("f64", "df64"))
     if sumfac:
         table_bytes += ((4 * 27 * jbytes + 15) // 16) * 16
+    # sum factorisation of the interpolation (value and reference gradient
+    # at the 27 knots) and of the residual's test-function contraction of the
+    # Q2 hex: one axis at a time, 729 multiply-adds each instead of 27 x 27 x 4
+    sfi = bool(jref and et.name == "Q2_HEX" and nf == 1 and spaces[0] == "C2"
+               and list(layout.loc_of[0]) == list(range(nn)))
+    sfi_own = sfi and not sumfac            # buffers of its own (else the Jacobian's stage buffers)
     if jref:
         per_elem = (nn * dim + 2 * nn * nval + nq * ntc + geo_doubles + gsd) * 8 + nq * ndnz_hat * jbytes
         if sumfac:
@@ -387,6 +394,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     else:
         per_elem = ((nn * dim + 2 * nn * nval + nq * ntc + geo_doubles + gsd) * 8
                     + (nq * ndnz + nq * nn * dim + (nq * nn1 * dim if has_c1 else 0)) * jbytes)
+    if sfi_own:
+        per_elem += (54 + 81 + 108) * 8
     if epb is None:
         # df64: the most elements that fit 720 threads and 224 KB (GB300
         # sweeps: the Q2 hex kernel is fastest at 12 elements per block, the
@@ -403,6 +412,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         raise ValueError(f"{epb} elements per block do not fit a block ({threads} threads, {smem} B shared)")
     if name is None:
         h = hashlib.sha1((et.name + jac_precision + str(affine) + str(epb) + str(jref) + str(sumfac) + str(gsep) +
+                          str(sfi) +
                           str(pw.r_exprs) +
                           str(pw.d_entries)).encode()).hexdigest()[:10]
         name = f"fe_elem_{et.name.lower()}_{jac_precision}{'_aff' if affine else ''}_{h}"
@@ -433,6 +443,10 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("#define FE_GAUSS(d, x, g, n) fe_gauss_sep<d>(gsT, gsI, g, n)")
     else:
         w("#define FE_GAUSS(d, x, g, n) fe_gauss_sum<d>(x, g, n)")
+    if sfi:
+        from .spaces import _G3_1D, _lag3
+        Mv = [repr(float(_lag3(g)[c][i])) for c in range(2) for g in _G3_1D for i in range(3)]
+        w(f"__constant__ double c_M[18] = {{{', '.join(Mv)}}};")
     w(pointwise_source(pw, jreal))
     w(f'extern "C" __global__ void __launch_bounds__(FE_NT) {name}(const FeElemArgs a) {{')
     w("  extern __shared__ __align__(16) unsigned char fe_smem[];")
@@ -469,6 +483,19 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w("  jacc* sS2 = sS1 + FE_EPB * 81;")
             w("  jacc* sJe = sS2 + FE_EPB * 243;")
             w("  jacc* sF = sJe + FE_EPB * 729;")
+        if sfi:
+            if sumfac:
+                w("  double* sIa = reinterpret_cast<double*>(sS1);  // interpolation / residual stages")
+                w("  double* sIb = reinterpret_cast<double*>(sS2);")
+                w("  double* sIc = reinterpret_cast<double*>(sJe);")
+                sfs = (81, 243, 729)
+            else:
+                assert not tab_copy or (tabf * (8 if df64 else 4)) % 8 == 0, "stage buffers must be 8-byte aligned"
+                base = f"sPsi2j + {tabf}" if tab_copy else "sEnd"
+                w(f"  double* sIa = reinterpret_cast<double*>({base});  // interpolation / residual stages")
+                w("  double* sIb = sIa + FE_EPB * 54;")
+                w("  double* sIc = sIb + FE_EPB * 81;")
+                sfs = (54, 81, 108)
     else:
         w("  jreal* sDx2 = sD + FE_EPB * FE_NQ * FE_NDNZ;")
         w("  jreal* sDx1 = sDx2 + FE_EPB * FE_NQ * FE_NN * FE_DIM;")
@@ -480,6 +507,10 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w(f"  for (int k = threadIdx.x; k < {table_doubles}; k += FE_NT) sW[k] = a.tables[k];")
     if tab_copy:
         w(f"  for (int k = threadIdx.x; k < {tabf}; k += FE_NT) sPsi2j[k] = (jacc)a.tables[FE_NQ + k];")
+    if sfi:
+        # 1D Lagrange values M0[q][i] and derivatives M1[q][i] at the 1D Gauss points
+        w("  __shared__ double sM[18];")
+        w("  for (int k = threadIdx.x; k < 18; k += FE_NT) sM[k] = c_M[k];")
     if sumfac:
         from .spaces import _G3_1D, _lag3
         M = [np.array([_lag3(g)[0] for g in _G3_1D]), np.array([_lag3(g)[1] for g in _G3_1D])]
@@ -534,6 +565,46 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w(f"    const double* g = Pe + {gs_base} + k * (FE_DIM + 2);")
         w("    const double dd = xd - g[d], w = g[FE_DIM];")
         w("    sGe[el * " + str(gsd) + " + o] = exp(-(dd * dd) / (2.0 * w * w));")
+        w("  }")
+        w("  __syncthreads();")
+    if sfi:
+        SA, SB, SC = sfs
+        # ---------------- phase I: sum-factorised interpolation ----------------
+        # u at node l = i0 + 3 i1 + 9 i2; knot q = 9 q0 + 3 q1 + q2; shapes
+        # psi_l(q) = M0[q0][i0] M0[q1][i1] M0[q2][i2] (M1: derivatives)
+        w("  for (int p = threadIdx.x; p < nel * 27; p += FE_NT) {  // axis 0: A, B [i1][i2][q0]")
+        w("    const int el = p / 27, o = p - el * 27, i1 = o / 9, i2 = (o / 3) % 3, q0 = o % 3;")
+        w("    const double* u = sU + el * FE_NN * FE_NVAL + (3 * i1 + 9 * i2) * FE_NVAL;")
+        w("    double a_ = 0.0, b_ = 0.0;")
+        w("    #pragma unroll")
+        w("    for (int i0 = 0; i0 < 3; ++i0) {")
+        w("      const double uu = u[i0 * FE_NVAL];")
+        w("      a_ = fma(uu, sM[q0 * 3 + i0], a_); b_ = fma(uu, sM[9 + q0 * 3 + i0], b_); }")
+        w(f"    sIa[el * {SA} + o] = a_; sIa[el * {SA} + 27 + o] = b_;")
+        w("  }")
+        w("  __syncthreads();")
+        w("  for (int p = threadIdx.x; p < nel * 27; p += FE_NT) {  // axis 1: AA, AB, BA [i2][q0][q1]")
+        w("    const int el = p / 27, o = p - el * 27, i2 = o / 9, q0 = (o / 3) % 3, q1 = o % 3;")
+        w(f"    const double* A = sIa + el * {SA} + i2 * 3 + q0;")
+        w("    double aa = 0.0, ab = 0.0, ba = 0.0;")
+        w("    #pragma unroll")
+        w("    for (int i1 = 0; i1 < 3; ++i1) {")
+        w("      const double av = A[i1 * 9], bv = A[27 + i1 * 9];")
+        w("      aa = fma(av, sM[q1 * 3 + i1], aa); ab = fma(av, sM[9 + q1 * 3 + i1], ab); ba = fma(bv, sM[q1 * 3 + i1], ba); }")
+        w(f"    sIb[el * {SB} + o] = aa; sIb[el * {SB} + 27 + o] = ab; sIb[el * {SB} + 54 + o] = ba;")
+        w("  }")
+        w("  __syncthreads();")
+        w("  for (int p = threadIdx.x; p < nel * 27; p += FE_NT) {  // axis 2: value, d0, d1, d2 at knot q")
+        w("    const int el = p / 27, q = p - el * 27, q0 = q / 9, q1 = (q / 3) % 3, q2 = q % 3;")
+        w(f"    const double* B = sIb + el * {SB} + q0 * 3 + q1;")
+        w("    double v = 0.0, d0 = 0.0, d1 = 0.0, d2 = 0.0;")
+        w("    #pragma unroll")
+        w("    for (int i2 = 0; i2 < 3; ++i2) {")
+        w("      const double aa = B[i2 * 9], ab = B[27 + i2 * 9], ba = B[54 + i2 * 9];")
+        w("      const double m0 = sM[q2 * 3 + i2], m1 = sM[9 + q2 * 3 + i2];")
+        w("      v = fma(aa, m0, v); d2 = fma(aa, m1, d2); d1 = fma(ab, m0, d1); d0 = fma(ba, m0, d0); }")
+        w(f"    double* C = sIc + el * {SC} + q;")
+        w("    C[0] = v; C[27] = d0; C[54] = d1; C[81] = d2;")
         w("  }")
         w("  __syncthreads();")
     # ---------------- phase A ----------------
@@ -599,7 +670,19 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w(f"{ind}    {dst}[{base} + 1 + i] = s; }}")
             w(f"{ind}}}")
 
-    interp("U", "sU", "    ")
+    if sfi:
+        w("    double U[FE_NTC];")
+        w(f"    {{ const double* C = sIc + el * {SC} + q;")
+        w("      const double gs[3] = {C[27], C[54], C[81]};")
+        w("      U[0] = C[0];")
+        w("      #pragma unroll")
+        w("      for (int i = 0; i < FE_DIM; ++i) { double s = 0.0;")
+        w("        #pragma unroll")
+        w("        for (int b = 0; b < FE_DIM; ++b) s += g[b][i] * gs[b];")
+        w("        U[1 + i] = s; }")
+        w("    }")
+    else:
+        interp("U", "sU", "    ")
     w("    const double* Pe = a.params + (a.replica_elems > 0 ? ((e0 + el) / a.replica_elems) * a.params_stride : 0);")
     w("    double r[FE_NTC]; jreal D[FE_NDNZ];")
     if gsep:
@@ -674,6 +757,43 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    }")
     w("  }")
     w("  __syncthreads();")
+    if sfi:
+        SA, SB, SC = sfs
+        # ---------------- phase R: sum-factorised residual ----------------
+        # R_l = sum_q [rh0 psi_l + rh1 d0psi_l + rh2 d1psi_l + rh3 d2psi_l], one axis at a time
+        w("  for (int p = threadIdx.x; p < nel * 27; p += FE_NT) {  // knot axis 2 -> node i2: T0, T1, T2 [q0][q1][i2]")
+        w("    const int el = p / 27, o = p - el * 27, q0 = o / 9, q1 = (o / 3) % 3, i2 = o % 3;")
+        w("    const double* rh = sRh + (el * FE_NQ + q0 * 9 + q1 * 3) * FE_NTC;")
+        w("    double t0 = 0.0, t1 = 0.0, t2 = 0.0;")
+        w("    #pragma unroll")
+        w("    for (int q2 = 0; q2 < 3; ++q2) {")
+        w("      const double* r = rh + q2 * FE_NTC;")
+        w("      const double m0 = sM[q2 * 3 + i2], m1 = sM[9 + q2 * 3 + i2];")
+        w("      t0 = fma(r[0], m0, fma(r[3], m1, t0)); t1 = fma(r[1], m0, t1); t2 = fma(r[2], m0, t2); }")
+        w(f"    sIb[el * {SB} + o] = t0; sIb[el * {SB} + 27 + o] = t1; sIb[el * {SB} + 54 + o] = t2;")
+        w("  }")
+        w("  __syncthreads();")
+        w("  for (int p = threadIdx.x; p < nel * 27; p += FE_NT) {  // knot axis 1 -> node i1: S0, S1 [q0][i1][i2]")
+        w("    const int el = p / 27, o = p - el * 27, q0 = o / 9, i1 = (o / 3) % 3, i2 = o % 3;")
+        w(f"    const double* T = sIb + el * {SB} + q0 * 9 + i2;")
+        w("    double s0 = 0.0, s1 = 0.0;")
+        w("    #pragma unroll")
+        w("    for (int q1 = 0; q1 < 3; ++q1) {")
+        w("      const double m0 = sM[q1 * 3 + i1], m1 = sM[9 + q1 * 3 + i1];")
+        w("      s0 = fma(T[q1 * 3], m0, fma(T[54 + q1 * 3], m1, s0)); s1 = fma(T[27 + q1 * 3], m0, s1); }")
+        w(f"    sIa[el * {SA} + o] = s0; sIa[el * {SA} + 27 + o] = s1;")
+        w("  }")
+        w("  __syncthreads();")
+        w("  for (int p = threadIdx.x; p < nel * 27; p += FE_NT) {  // knot axis 0 -> node i0: R at node l")
+        w("    const int el = p / 27, l = p - el * 27, i0 = l % 3, i1 = (l / 3) % 3, i2 = l / 9;")
+        w(f"    const double* S = sIa + el * {SA} + i1 * 3 + i2;")
+        w("    double r = 0.0;")
+        w("    #pragma unroll")
+        w("    for (int q0 = 0; q0 < 3; ++q0)")
+        w("      r = fma(S[q0 * 9], sM[q0 * 3 + i0], fma(S[27 + q0 * 9], sM[9 + q0 * 3 + i0], r));")
+        w("    a.rbuf[(e0 + el) * FE_NLOC + l] = r;")
+        w("  }")
+        w("  __syncthreads();")
     if sumfac:
         # ---------------- phase B': sum-factorised Jacobian, one (a, b) block at a time ----------------
         w("  if (flag) {")
@@ -742,13 +862,17 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    jacc Jr[FE_NLOC];")
     w("    #pragma unroll")
     w("    for (int k = 0; k < FE_NLOC; ++k) Jr[k] = (jacc)0;")
-    w("    for (int q = 0; q < FE_NQ; ++q) {")
-    w("      const double* rh = sRh + (el * FE_NQ + q) * FE_NTC + tf * (1 + FE_DIM);")
-    w("      const double pv = tpsi[q * tn + lt];")
-    w("      double racc = rh[0] * pv;")
-    w("      #pragma unroll")
-    w("      for (int b = 0; b < FE_DIM; ++b) racc += rh[1 + b] * tdps[(q * tn + lt) * FE_DIM + b];")
-    w("      Racc += racc;")
+    if sfi:
+        w("    (void)Racc; (void)tpsi; (void)tdps;")
+    # (sum-factorised Jacobian and residual: nothing is left per knot here)
+    w(f"    for (int q = 0; q < {'0' if (sfi and sumfac) else 'FE_NQ'}; ++q) {{")
+    if not sfi:
+        w("      const double* rh = sRh + (el * FE_NQ + q) * FE_NTC + tf * (1 + FE_DIM);")
+        w("      const double pv = tpsi[q * tn + lt];")
+        w("      double racc = rh[0] * pv;")
+        w("      #pragma unroll")
+        w("      for (int b = 0; b < FE_DIM; ++b) racc += rh[1 + b] * tdps[(q * tn + lt) * FE_DIM + b];")
+        w("      Racc += racc;")
     if sumfac:
         pass
     elif jref:
@@ -853,7 +977,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("      }")
     w("    }")
     w("    const long long row = (e0 + el) * FE_NLOC + i;")
-    w("    a.rbuf[row] = Racc;")
+    if not sfi:
+        w("    a.rbuf[row] = Racc;")
     w("    if (flag) {")
     w("      jstore* jb = reinterpret_cast<jstore*>(a.jbuf) + row * FE_NLOC;")
     if sumfac:
@@ -869,7 +994,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     return KernelSpec(name=name, source=source, et=et, layout=layout, pointwise=pw, epb=epb,
                       threads=threads, smem_bytes=smem, jac_precision=jac_precision,
                       tables=et.packed_tables(), sumfac_blocks=len(hat) if sumfac else 0,
-                      gauss_sep=gs_n if gsep else 0)
+                      gauss_sep=gs_n if gsep else 0, sum_fact_interp=sfi)
 
 
 def _jacc_update(terms, acc: str, jacc: str) -> str:
@@ -904,7 +1029,8 @@ def estimate_flops(ks: KernelSpec, affine: bool) -> Dict[str, float]:
         per_q += 2 * (N1 if affine else NN) * D
     for _, s in fields:
         n = NN if s == "C2" else N1
-        per_q += 2 * n * nc + 2 * D * D
+        # sum-factorised: the interpolation stages are counted per element below
+        per_q += (0 if ks.sum_fact_interp else 2 * n * nc) + 2 * D * D
     ops_r = 0
     for e in pw.r_exprs:
         gs = list(e.atoms(E.GaussianSum))
@@ -917,7 +1043,9 @@ def estimate_flops(ks: KernelSpec, affine: bool) -> Dict[str, float]:
     per_q += ops_r
     per_q += len(fields) * (1 + 2 * D * D)
     rows = lay.n
-    resid = rows * NQ * 2 * nc
+    # residual contraction; sum-factorised: 3 stages of 27 x (12, 9, 6) FMAs,
+    # plus the 3 interpolation stages of 27 x (6, 9, 12) FMAs
+    resid = 2 * 27 * (12 + 9 + 6) * 2 if ks.sum_fact_interp else rows * NQ * 2 * nc
     fp64 = NQ * per_q + (geo if affine else 0) + resid
     if ks.gauss_sep:
         # per element: 3 D factors per Gaussian (the affine map along the axis, exp)

@@ -37,6 +37,7 @@ static fe_emu_dim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, gridDim = {1, 1,
 #define __restrict__ __restrict
 #define __align__(n) alignas(n)
 #define __syncthreads() do {} while (0)
+#define __shared__
 static inline int atomicExch(int *p, int v) { int o = *p; *p = v; return o; }
 static inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
 static inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
