@@ -107,7 +107,7 @@ class BatchedBiCGStab:
         return {"launches": a.value, "graph_replays": b.value, "restarts": c.value}
 
     def matvec(self, x, y) -> None:
-        """y = A x with the solver's tiled SpMV, on the current stream."""
+        """y = A x with the solver's matrix and SpMV kernel, on the current stream."""
         N.check(N.load().fe_krylov_matvec(self._h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()),
                                           ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)))
 
