@@ -311,7 +311,7 @@ def run_gb300(args):
         # of finished rows overlapping the element chunks still running; the
         # chunk count (rounded to whole waves by the library) is chosen by timing
         e2e_by_chunks = {}
-        for nc in (2, 4, 8):
+        for nc in (2, 4, 8, 16):
             e2e_by_chunks[nc] = time_steps(torch, lambda: P.assemble_host(xh, Rh, Jh, True, chunks=nc),
                                            max(3, args.steps), args.warmup)
         chunks = min(e2e_by_chunks, key=e2e_by_chunks.get)
