@@ -261,14 +261,16 @@ class Problem:
             ks = generate_kernel(mesh.etype, pw, kprec, epb=self.elems_per_block, affine=self.affine,
                                  jref=self.jacobian_reference, gauss_sep=gsep)
             _KERNEL_CACHE[key] = ks
-        if self.elems_per_block is None:
+        if self.elems_per_block is None and int(self.replicas) == 1:
             # balance the waves: with W = ceil(E / (SMs x EPB)) waves of one
             # block per SM, EPB' = ceil(E / (SMs x W)) fills every wave as
             # evenly (small meshes: Poisson Q2 64^2, 4,096 elements, 32 per
             # block = 128 blocks on 152 SMs; 27 per block = one full wave,
-            # 10% faster on GB300; large meshes keep their shape)
+            # 10% faster on GB300; large meshes keep their shape).  Not for
+            # replicated problems: serving classes of many sizes then share
+            # one kernel instead of compiling one per size.
             sms = _sm_count()
-            n_el = mesh.n_elem * max(1, int(self.replicas))     # one launch covers every replica
+            n_el = mesh.n_elem
             waves = -(-n_el // (sms * ks.epb))
             epb = max(1, -(-n_el // (sms * waves)))
             if epb < ks.epb:

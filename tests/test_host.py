@@ -242,7 +242,8 @@ def test_launch_shapes_balance_the_waves():
     """Elements per block follow EPB' = ceil(E / (SMs x W)), W the waves of
     the generator's shape on 152 SMs: a small mesh fills one wave (Poisson
     Q2 64^2: 4,096 elements -> 27 per block = 152 blocks), a large one keeps
-    its shape, replicas count as elements of the launch."""
+    its shape, replicated problems (serving classes of many sizes) keep the
+    generator's shape so that they share one kernel."""
     from pyoomph_gb300 import problem as PR
     from pyoomph_gb300 import workloads as W
     PR._SMS = 152
@@ -250,8 +251,8 @@ def test_launch_shapes_balance_the_waves():
     assert ks.epb == 27 and -(-4096 // ks.epb) == 152
     assert W.navier_stokes_problem(N=256).lower().epb == 32
     P = W.poisson_problem(N=16)
-    P.replicas = 4                        # 4 x 256 elements in one launch
-    assert P.lower().epb == -(-1024 // 152)
+    P.replicas = 4
+    assert P.lower().epb == 32            # the generator's shape for the Poisson Q2 kernel
     P = W.poisson_problem(N=64)
     P.elems_per_block = 32                # an explicit shape is kept
     assert P.lower().epb == 32
