@@ -52,11 +52,13 @@ enum {
   FE_ASSEMBLE_RESIDUAL = 1, /* fill R (Problem::get_residuals) */
   FE_ASSEMBLE_JACOBIAN = 2, /* fill the CSR values of J (Problem::get_jacobian) */
   FE_ASSEMBLE_VALUES_FROM_DOFS = 4, /* first scatter the dof vector into the nodal values */
-  /* fused (moving-mesh) code only, each in a call of its own: */
-  FE_ASSEMBLE_MASS = 8,   /* J_vals receives the mass matrix dR/d(du/dt) (flag 2 of the
-                             generated ResidualAndJacobian, jitbridge.h:285) */
+  /* each in a call of its own: */
+  FE_ASSEMBLE_MASS = 8,   /* fused (moving-mesh) code only: J_vals receives the mass matrix
+                             dR/d(du/dt) (flag 2 of the generated ResidualAndJacobian,
+                             jitbridge.h:285) */
   FE_ASSEMBLE_DPARAM = 16, /* R receives dR/dp for the parameter of fe_problem_set_dparam
-                             (dResidual{i}dParameter_{k}, codegen.cpp:4743-4760) */
+                             (dResidual{i}dParameter_{k}, codegen.cpp:4743-4760); fixed-mesh
+                             and fused code */
   /* fixed-mesh code only, in a call of its own: */
   FE_ASSEMBLE_HVP = 32     /* J_vals receives the Hessian-vector product
                               H(y)_ij = sum_k d2R_i/du_j du_k y_k for the direction of

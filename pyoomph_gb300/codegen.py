@@ -173,6 +173,54 @@ def _emit(exprs, names, fp32: bool, outs, indent="  "):
     return lines
 
 
+def dparam_source(pw: Pointwise) -> str:
+    """``fe_pointwise_dparam(U, Xq, P, r, dparam)``: the residual
+    coefficients differentiated by the global parameter P[dparam]
+    (dResidual{i}dParameter_{k} of pyoomph's generated code,
+    codegen.cpp:4743-4760).  Parameters inside a Gaussian source enter by
+    the chain rule through the sum's closed-form derivatives
+    (fe_gauss_dparam)."""
+    names = _symbol_names(pw)
+    nr = len(pw.r_exprs)
+    atoms = sorted({g for e in pw.r_exprs for g in e.atoms(E.GaussianSum)}, key=str)
+    gsyms = [sp.Symbol(f"FE_GS{a}", real=True) for a in range(len(atoms))]
+    ginfo = []
+    for a, ga in enumerate(atoms):
+        k0 = next(i for i, x_ in enumerate(ga.args) if x_.is_Integer)
+        n, dim = int(ga.args[k0]), int(ga.args[k0 + 1])
+        pars = list(ga.args[k0 + 2:])
+        ref0 = names[pars[0]]
+        base = int(ref0[ref0.index("[") + 1:-1])
+        names[gsyms[a]] = f"fe_gauss_sum<{dim}>(Xq, P + {base}, {n})"
+        ginfo.append((dim, base, pars))
+    subs = dict(zip(atoms, gsyms))
+    rs = [e.subs(subs) for e in pw.r_exprs]
+    lines = ["__device__ __forceinline__ void fe_pointwise_dparam(const double* __restrict__ U, "
+             "const double* __restrict__ Xq, const double* __restrict__ P, double* __restrict__ r, int dparam) {",
+             "  (void)U; (void)Xq; (void)P;",
+             f"  for (int k = 0; k < {nr}; ++k) r[k] = 0.0;",
+             "  switch (dparam) {"]
+    for j, pname in enumerate(pw.params):
+        psym = E.parameter(pname)
+        exprs = []
+        for e in rs:
+            d = sp.diff(e, psym)
+            for a, (dim, base, pars) in enumerate(ginfo):
+                if psym in pars:
+                    dg = sp.Symbol(f"FE_DG{a}_{j}", real=True)
+                    names[dg] = f"fe_gauss_dparam<{dim}>(Xq, P + {base}, {j - base})"
+                    d = d + sp.diff(e, gsyms[a]) * dg
+            exprs.append(sp.simplify(d) if d != 0 else d)
+        if all(d == 0 for d in exprs):
+            continue
+        lines.append(f"    case {j}: {{")
+        keep = [(k, d) for k, d in enumerate(exprs) if d != 0]
+        lines += _emit([d for _, d in keep], names, False, [f"r[{k}]" for k, _ in keep], "      ")
+        lines.append("      break; }")
+    lines += ["    default: break;", "  }", "}"]
+    return "\n".join(lines)
+
+
 def pointwise_source(pw: Pointwise, jreal: str = "double") -> str:
     """The generated device functions.
 
@@ -448,6 +496,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         Mv = [repr(float(_lag3(g)[c][i])) for c in range(2) for g in _G3_1D for i in range(3)]
         w(f"__constant__ double c_M[18] = {{{', '.join(Mv)}}};")
     w(pointwise_source(pw, jreal))
+    w(dparam_source(pw))
     w(f'extern "C" __global__ void __launch_bounds__(FE_NT) {name}(const FeElemArgs a) {{')
     w("  extern __shared__ __align__(16) unsigned char fe_smem[];")
     w("  double* sW = reinterpret_cast<double*>(fe_smem);")
@@ -503,7 +552,10 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("  const long long e0 = (long long)blockIdx.x * FE_EPB;")
     w("  const long long rem = a.n_elem - e0;")
     w("  const int nel = rem < FE_EPB ? (int)rem : FE_EPB;")
-    w("  const int flag = a.flag;")
+    # flag 3 (dR/dp of global parameter a.aux): the residual path with the
+    # differentiated coefficients, no Jacobian
+    w("  const int flag = a.flag == 3 ? 0 : a.flag;")
+    w("  const bool dpar = a.flag == 3;")
     w(f"  for (int k = threadIdx.x; k < {table_doubles}; k += FE_NT) sW[k] = a.tables[k];")
     if tab_copy:
         w(f"  for (int k = threadIdx.x; k < {tabf}; k += FE_NT) sPsi2j[k] = (jacc)a.tables[FE_NQ + k];")
@@ -690,9 +742,11 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("    { int qq = q;")
         w("      #pragma unroll")
         w("      for (int d = FE_DIM - 1; d >= 0; --d) { qI[d] = qq % 3; qq /= 3; } }")
-        w(f"    fe_pointwise(U, Xq, Pe, r, D, flag, sGe + el * {gsd}, qI);")
+        w(f"    if (dpar) fe_pointwise_dparam(U, Xq, Pe, r, a.aux);")
+        w(f"    else fe_pointwise(U, Xq, Pe, r, D, flag, sGe + el * {gsd}, qI);")
     else:
-        w("    fe_pointwise(U, Xq, Pe, r, D, flag, nullptr, nullptr);")
+        w("    if (dpar) fe_pointwise_dparam(U, Xq, Pe, r, a.aux);")
+        w("    else fe_pointwise(U, Xq, Pe, r, D, flag, nullptr, nullptr);")
     w("    double* rh = sRh + (el * FE_NQ + q) * FE_NTC;")
     w("    #pragma unroll")
     w("    for (int f = 0; f < FE_NF; ++f) {")

@@ -142,6 +142,26 @@ __device__ __noinline__ double fe_gauss_sum(const double *__restrict__ Xq, const
   return f;
 }
 
+// d/dg_j of the same sum for one parameter, j = k (DIM + 2) + m of Gaussian
+// k: m < DIM (centre c_m): A E (x_m - c_m) / w^2; m = DIM (width): A E r^2 /
+// w^3; m = DIM + 1 (amplitude): E, with E = exp(-r^2 / (2 w^2)).
+template <int DIM>
+__device__ __noinline__ double fe_gauss_dparam(const double *__restrict__ Xq, const double *__restrict__ g, int j) {
+  const int k = j / (DIM + 2), m = j - k * (DIM + 2);
+  const double *gk = g + k * (DIM + 2);
+  double r2 = 0.0;
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) {
+    const double d = Xq[i] - gk[i];
+    r2 += d * d;
+  }
+  const double w = gk[DIM], e = exp(-r2 / (2.0 * w * w));
+  if (m == DIM + 1) return e;
+  const double a = gk[DIM + 1];
+  if (m == DIM) return a * e * r2 / (w * w * w);
+  return a * e * (Xq[m] - gk[m]) / (w * w);
+}
+
 // The same sum on an axis-aligned affine tensor-product element, separably:
 // exp(-|x-c|^2/(2w^2)) = prod_d exp(-(x_d-c_d)^2/(2w^2)), and along axis d
 // the knots take only three coordinates, so the element's factors

@@ -631,6 +631,23 @@ class Problem:
         vals = self.J_dev[:self.nnz].cpu().numpy()
         return R, sp.csr_matrix((vals, ci, rp), shape=(self.n_dof, self.n_dof))
 
+    def get_parameter_derivative(self, name: str) -> np.ndarray:
+        """dR/dp of one global parameter at the current dofs
+        (dResidual{i}dParameter_{k} of pyoomph's generated code,
+        codegen.cpp:4743-4760; used by continuation and bifurcation
+        tracking).  With replicas, each replica's residual by its own copy
+        of the parameter."""
+        torch = _torch()
+        self.initialise()
+        if name not in self.param_names:
+            raise KeyError(f"unknown parameter {name!r}; have {self.param_names}")
+        N.check(N.load().fe_problem_set_dparam(self._h, self.param_names.index(name)))
+        st = torch.cuda.current_stream().cuda_stream
+        N.check(N.load().fe_assemble(self._h, self.x_dev.data_ptr(), self.R_dev.data_ptr(), self.J_dev.data_ptr(),
+                                     N.FE_ASSEMBLE_DPARAM | N.FE_ASSEMBLE_VALUES_FROM_DOFS, ctypes.c_void_p(st)))
+        self.check()
+        return self.R_dev[:self.n_dof].cpu().numpy()
+
     def get_hessian_vector_product(self, y: np.ndarray):
         """H(y)_ij = sum_k d2R_i/(du_j du_k) y_k at the current dofs, in the
         Jacobian's CSR pattern (pyoomph's HessianVectorProduct, used by

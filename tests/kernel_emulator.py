@@ -93,7 +93,7 @@ def build(ks) -> ctypes.CDLL:
     return L
 
 
-def run(ks, x, conn, values, params, flag: int = 1, direction=None):
+def run(ks, x, conn, values, params, flag: int = 1, direction=None, aux: int = 0):
     """Element residuals [E, nloc] and matrices [E, nloc, nloc] of the
     generated kernel ks on the given mesh data (host arrays)."""
     L = build(ks)
@@ -111,7 +111,7 @@ def run(ks, x, conn, values, params, flag: int = 1, direction=None):
     if direction is not None:
         direction = np.ascontiguousarray(direction, dtype=np.float64)
     a = _Args(x.ctypes.data, conn.ctypes.data, values.ctypes.data, params.ctypes.data, tables.ctypes.data,
-              rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data, 0, 0, None, None, 0, 0, 0,
+              rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data, 0, 0, None, None, 0, 0, aux,
               x.shape[0], values.ctypes.data if direction is None else direction.ctypes.data)
     L.fe_emu_run(ctypes.byref(a), (E + ks.epb - 1) // ks.epb)
     return rbuf, jbuf, status
