@@ -82,12 +82,37 @@ class GB300Assembler(CustomAssemblyBase):
                 raise RuntimeError(f"host problem has {dofs.shape[0]} dofs, engine {self.engine.n_dof}")
             self.engine.set_dofs(dofs)
 
+    def _sync_params(self) -> None:
+        """Copy the host problem's global parameters that the engine's weak
+        form reads (by name: pyoomph's Problem.get_global_parameter_names /
+        get_global_parameter(name).value, src/pybind/problem.cpp:515-517)
+        into the engine when they changed, e.g. under arclength
+        continuation."""
+        if self.problem is None or not hasattr(self.problem, "get_global_parameter_names"):
+            return
+        stride = len(self.engine.param_names)
+        changed = {}
+        for name in self.problem.get_global_parameter_names():
+            if name in self.engine.param_names:
+                v = float(self.problem.get_global_parameter(name).value)
+                if v != self.engine.params[self.engine.param_names.index(name) % stride]:
+                    changed[name] = v
+        if changed:
+            self.engine.set_parameters(**changed)
+
     def get_residuals_and_jacobian(self, require_jacobian: bool, dparameter: Optional[str] = None
                                    ) -> Union[np.ndarray, Tuple[np.ndarray, "object"]]:
-        if dparameter is not None:
-            raise RuntimeError("Cannot derive the residual with respect to a parameter yet")
+        """R (float64[n]), or (R, J) with J a CSR matrix of int32 indices and
+        float64 values; with ``dparameter`` and no Jacobian, dR/dp of that
+        global parameter (problem.py:1739-1744 of pyoomph asks for it so; a
+        Jacobian derived by a parameter is refused there as here)."""
+        if dparameter is not None and require_jacobian:
+            raise RuntimeError("Cannot derive custom Jacobian with respect to a parameter yet")
         self.engine.initialise()
+        self._sync_params()
         self._sync_dofs()
+        if dparameter is not None:
+            return np.ascontiguousarray(self.engine.get_parameter_derivative(dparameter), dtype=np.float64)
         if not require_jacobian:
             return np.ascontiguousarray(self.engine.get_residuals(), dtype=np.float64)
         R, J = self.engine.get_jacobian()

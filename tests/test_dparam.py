@@ -77,3 +77,86 @@ def test_gpu_parameter_derivative_matches_central_differences(kind):
     assert np.array_equal(P.get_residuals(), R0)
     with pytest.raises(KeyError):
         P.get_parameter_derivative("no_such_parameter")
+
+
+class _Param:
+    def __init__(self, v):
+        self.value = v
+
+
+class _HostProblem:
+    """Stands for a pyoomph Problem: current dofs and named global parameters."""
+
+    def __init__(self, x, params):
+        self.x = x
+        self.params = {k: _Param(v) for k, v in params.items()}
+
+    def get_current_dofs(self):
+        return self.x, None
+
+    def get_global_parameter_names(self):
+        return list(self.params)
+
+    def get_global_parameter(self, name):
+        return self.params[name]
+
+
+def test_assembler_copies_changed_host_parameters_into_the_engine():
+    """Host logic of the drop-in assembler: parameters the weak form reads
+    follow the host problem (arclength continuation changes them between
+    solves); others are ignored; nothing is uploaded when nothing changed;
+    a Jacobian derived by a parameter is refused as pyoomph refuses it."""
+    from pyoomph_gb300 import GB300Assembler
+
+    class Engine:
+        param_names = ["dynamic_viscosity", "mass_density"]
+        params = np.array([0.01, 1.0])
+        n_dof = 3
+        uploads = []
+
+        def initialise(self):
+            pass
+
+        def set_parameters(self, **kw):
+            self.uploads.append(dict(kw))
+            for k, v in kw.items():
+                self.params[self.param_names.index(k)] = v
+
+        def set_dofs(self, x):
+            self.x = x
+
+        def get_parameter_derivative(self, name):
+            return np.full(self.n_dof, float(self.param_names.index(name)))
+
+    eng = Engine()
+    asm = GB300Assembler(eng)
+    host = _HostProblem(np.zeros(3), {"dynamic_viscosity": 0.01, "mass_density": 1.0, "unrelated": 7.0})
+    asm._set_problem(host)
+    assert np.array_equal(asm.get_residuals_and_jacobian(False, "mass_density"), np.ones(3))
+    assert eng.uploads == []
+    host.params["dynamic_viscosity"].value = 0.02
+    asm.get_residuals_and_jacobian(False, "dynamic_viscosity")
+    assert eng.uploads == [{"dynamic_viscosity": 0.02}] and eng.params[0] == 0.02
+    with pytest.raises(RuntimeError):
+        asm.get_residuals_and_jacobian(True, "dynamic_viscosity")
+
+
+@pytest.mark.gpu
+def test_gpu_assembler_parameter_derivative_and_sync():
+    """Through pyoomph's CustomAssemblyBase contract: dR/dp from
+    get_residuals_and_jacobian(False, name) equals the engine's, and a
+    parameter changed on the host reaches the next residual."""
+    from pyoomph_gb300 import GB300Assembler, workloads as W
+    eng = W.navier_stokes_problem(N=6, Re=50.0)
+    asm = GB300Assembler(eng)
+    asm.initialize()
+    x = np.random.default_rng(2).normal(0.0, 0.3, eng.n_dof)
+    host = _HostProblem(x, {"dynamic_viscosity": 0.02, "mass_density": 1.0})
+    asm._set_problem(host)
+    R1 = asm.get_residuals_and_jacobian(False)
+    D = asm.get_residuals_and_jacobian(False, "dynamic_viscosity")
+    assert D.dtype == np.float64 and D.shape == (eng.n_dof,)
+    host.params["dynamic_viscosity"].value = 0.03
+    R2 = asm.get_residuals_and_jacobian(False)
+    # R is linear in the viscosity
+    assert np.max(np.abs(R2 - R1 - 0.01 * D)) <= 1e-12 * max(1.0, np.max(np.abs(R1)))
