@@ -53,9 +53,10 @@ enum {
   FE_ASSEMBLE_JACOBIAN = 2, /* fill the CSR values of J (Problem::get_jacobian) */
   FE_ASSEMBLE_VALUES_FROM_DOFS = 4, /* first scatter the dof vector into the nodal values */
   /* each in a call of its own: */
-  FE_ASSEMBLE_MASS = 8,   /* fused (moving-mesh) code only: J_vals receives the mass matrix
-                             dR/d(du/dt) (flag 2 of the generated ResidualAndJacobian,
-                             jitbridge.h:285) */
+  FE_ASSEMBLE_MASS = 8,   /* J_vals receives the mass matrix dR/d(du/dt) (flag 2 of the
+                             generated ResidualAndJacobian, jitbridge.h:285); code of a
+                             transient form: fused code, or fixed-mesh code of a problem
+                             created with n_history > 0 */
   FE_ASSEMBLE_DPARAM = 16, /* R receives dR/dp for the parameter of fe_problem_set_dparam
                              (dResidual{i}dParameter_{k}, codegen.cpp:4743-4760); fixed-mesh
                              and fused code */
@@ -132,7 +133,8 @@ typedef struct fe_problem_desc {
   const double *params;     /* global parameters read by the element code */
   int jac_precision;        /* FE_JAC_F64 or FE_JAC_F32 */
   int params_stride;        /* parameters per replica (0 = one set for all elements) */
-  int n_history;            /* previous time levels of the nodal values kept (BDF) */
+  int n_history;            /* previous time levels of the nodal values kept (BDF; the generated
+                               code of a transient form reads levels 0 and 1 = u_{n-1}, u_{n-2}) */
   const double *x0;         /* host [n_nodes * dim] Lagrangian positions (NULL: = x) */
   int fused;                /* 1: every domain shares one fused code, run as one launch */
   /* hanging values (refined meshes; oomph's HangInfo, problem.cc / nodes.h:

@@ -510,6 +510,38 @@ int ofe_element_res_jac(int etype, int eq, int dim, const double *x, const int32
   return element_rj(etype, eq, dim, x, conn_e, nval, values, params, &L, R, J, 1);
 }
 
+/* Element mass matrix of the time-derivative term: M_e(i, j) = coeff *
+ * int psi_i psi_j dx between equal time-differentiated values (the velocity
+ * components for Navier-Stokes, coeff = rho: rho partial_t(u) of
+ * navier_stokes.py:481-503 through generic.py:564; the field of a scalar
+ * equation, coeff = temporal_factor: DiffusionEquation, poisson.py:153-180).
+ * These forms are linear in du/dt with a coefficient independent of u, so
+ * the transient element residual is R_e(u) + M_e udot_e and its Jacobian
+ * J_e + w0 M_e, udot the BDF combination of the nodal time levels and w0
+ * its weight of the current level; M_e is flag 2 of the generated code
+ * (jitbridge.h:285). */
+int ofe_element_mass(int etype, int eq, int dim, const double *x, const int32_t *conn_e, double coeff,
+                     double *M) {
+  layout_t L;
+  make_layout(etype, eq, &L);
+  const int nn = etype_nnode(etype), nq = ofe_n_intpt(etype), n = L.n;
+  const int nt = eq == OFE_EQ_NAVIER_STOKES_TH ? 2 : 1;
+  double X[27 * 3];
+  for (int l = 0; l < nn; l++)
+    for (int i = 0; i < dim; i++) X[l * dim + i] = x[(int64_t)conn_e[l] * dim + i];
+  memset(M, 0, sizeof(double) * n * n);
+  shapeinfo_t si;
+  for (int ipt = 0; ipt < nq; ipt++) {
+    fill_shape_info(etype, X, ipt, &si);
+    for (int lt = 0; lt < nn; lt++)
+      for (int ls = 0; ls < nn; ls++) {
+        const double m = coeff * si.psi2[lt] * si.psi2[ls] * si.w;
+        for (int k = 0; k < nt; k++) M[L.loc[lt][k] * n + L.loc[ls][k]] += m;
+      }
+  }
+  return n;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Global assembly: Problem::sparse_assemble_row_or_column_compressed_with_ */
 /* vectors_of_pairs (problem.cc:5332-5666), compressed-row branch.          */

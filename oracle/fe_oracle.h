@@ -78,6 +78,12 @@ int ofe_element_res_jac(int etype, int eq, int dim, const double *x, const int32
                         int nval, const double *values, const uint8_t *is_vertex,
                         const double *params, int nparams, double *R, double *J);
 
+/* Element mass matrix of the time-derivative term (coeff * int psi_i psi_j
+ * between equal time-differentiated values), in the same local order.
+ * Returns the local size. */
+int ofe_element_mass(int etype, int eq, int dim, const double *x, const int32_t *conn_e, double coeff,
+                     double *M);
+
 /* Local-size helper: number of local values of one element. */
 int ofe_element_nlocal(int etype, int eq, const int32_t *conn_e, int nval,
                        const uint8_t *is_vertex);

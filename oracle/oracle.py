@@ -74,6 +74,7 @@ def lib():
         L.ofe_csr_free.argtypes = [ctypes.POINTER(_CSR)]
         L.ofe_element_res_jac.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, p, p, ctypes.c_int,
                                           p, p, p, ctypes.c_int, p, p]
+        L.ofe_element_mass.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, p, p, ctypes.c_double, p]
         L.ofe_n_intpt.argtypes = [ctypes.c_int]
         L.ofe_intpt.argtypes = [ctypes.c_int, ctypes.c_int, p, p]
         L.ofe_shape_c2.argtypes = [ctypes.c_int, p, p, p]

@@ -104,6 +104,17 @@ class _Printer(C99CodePrinter):
         return self._lit(3.141592653589793)
 
 
+# the BDF weights of the current step (time derivative at a node:
+# du/dt = w0 u + w1 u_{n-1} + w2 u_{n-2}), appended to the parameter array
+# of a transient problem (the timestepper weights of pyoomph's shape buffer,
+# elements.cpp:4577-4656)
+BDF_PARAMS = ("_bdf_w0", "_bdf_w1", "_bdf_w2")
+
+
+def time_derivative_symbols(fields: List[Tuple[str, str]]) -> List[sp.Symbol]:
+    return [E.REG.dt[name] for name, _ in fields]
+
+
 @dataclass
 class Pointwise:
     """Result of differentiating a weak form at one integration point."""
@@ -113,36 +124,59 @@ class Pointwise:
     r_exprs: List[sp.Expr]                 # [NTC]
     d_entries: List[Tuple[int, int, sp.Expr]]  # (tc, ic, expr), nonzero only
     uses_x: bool
+    dt_fields: List[int] = None            # fields whose time derivative the form reads
+    m_entries: List[Tuple[int, sp.Expr]] = None  # (index into d_entries, dr/d(du/dt))
 
     @property
     def ntc(self) -> int:
         return len(self.fields) * (1 + self.dim)
 
+    @property
+    def transient(self) -> bool:
+        return bool(self.dt_fields)
+
 
 def differentiate(fields: List[Tuple[str, str]], dim: int, integrand: sp.Expr,
                   params: List[str]) -> Pointwise:
     """r_tc = d(integrand)/d(test component tc); D[tc, ic] = d r_tc / d(field
-    component ic).  Components per field: value, d/dx_0 .. d/dx_{dim-1}."""
+    component ic).  Components per field: value, d/dx_0 .. d/dx_{dim-1}.
+
+    A time derivative du/dt of a field (partial_t) is one more pointwise
+    input; since du/dt = w0 u + (history), its derivative enters the value
+    column as w0 dr/d(du/dt) (w0 the first BDF weight, a parameter), and
+    dr/d(du/dt) alone is the mass matrix's coefficient (flag 2 of the
+    generated ResidualAndJacobian, jitbridge.h:285)."""
     integrand = sp.expand(integrand) if integrand.has(sp.Symbol) else integrand
+    nc = 1 + dim
     tsyms, usyms = [], []
     for name, _ in fields:
         E.REG.field(name)
         tsyms += [E.REG.test[name]] + list(E.REG.test_grad[name][:dim])
         usyms += [E.REG.value[name]] + list(E.REG.grad[name][:dim])
+    dsyms = time_derivative_symbols(fields)
+    dt_fields = [f for f, s_ in enumerate(dsyms) if sp.sympify(integrand).has(s_)]
+    if dt_fields and BDF_PARAMS[0] not in params:
+        raise ValueError("a transient form needs the BDF weights among its parameters")
+    w0 = E.parameter(BDF_PARAMS[0]) if dt_fields else None
     r_exprs = []
     for t in tsyms:
         r = sp.diff(integrand, t)
         if any(r.has(tt) for tt in tsyms):
             raise ValueError("residual is not linear in the test functions")
         r_exprs.append(sp.simplify(r) if r.count_ops() < 40 else r)
-    d_entries = []
+    d_entries, m_entries = [], []
     for tc, r in enumerate(r_exprs):
         for ic, u in enumerate(usyms):
             d = sp.diff(r, u)
+            m = sp.diff(r, dsyms[ic // nc]) if (ic % nc == 0 and ic // nc in dt_fields) else sp.Integer(0)
+            if m != 0:
+                d = d + w0 * m
             if d != 0:
+                if m != 0:
+                    m_entries.append((len(d_entries), m))
                 d_entries.append((tc, ic, d))
     uses_x = any(any(e.has(x) for x in E.X) for e in r_exprs)
-    return Pointwise(fields, dim, params, r_exprs, d_entries, uses_x)
+    return Pointwise(fields, dim, params, r_exprs, d_entries, uses_x, dt_fields, m_entries)
 
 
 def _symbol_names(pw: Pointwise, prefix: str = "") -> Dict[sp.Symbol, str]:
@@ -152,6 +186,8 @@ def _symbol_names(pw: Pointwise, prefix: str = "") -> Dict[sp.Symbol, str]:
         names[E.REG.value[name]] = f"{prefix}U[{f * nc}]"
         for i in range(pw.dim):
             names[E.REG.grad[name][i]] = f"{prefix}U[{f * nc + 1 + i}]"
+        if pw.dt_fields and f in pw.dt_fields:
+            names[E.REG.dt[name]] = f"{prefix}U[{pw.ntc + f}]"
     for i in range(3):
         names[E.X[i]] = f"{prefix}Xq[{i}]"
     for k, p in enumerate(pw.params):
@@ -201,6 +237,8 @@ def dparam_source(pw: Pointwise) -> str:
              f"  for (int k = 0; k < {nr}; ++k) r[k] = 0.0;",
              "  switch (dparam) {"]
     for j, pname in enumerate(pw.params):
+        if pname in BDF_PARAMS:
+            continue
         psym = E.parameter(pname)
         exprs = []
         for e in rs:
@@ -236,6 +274,7 @@ def pointwise_source(pw: Pointwise, jreal: str = "double") -> str:
            "const double* __restrict__ Xq, const double* __restrict__ P, double* __restrict__ r, "
            "jreal* __restrict__ D, int flag, const double* __restrict__ gsT, const int* __restrict__ gsI) {")
     lines = [hdr, "  (void)gsT; (void)gsI;"]
+    mass = _mass_lines(pw, names, False) if pw.transient else []
     if jreal == "double" and nd:
         exprs = list(pw.r_exprs) + [d for (_, _, d) in pw.d_entries]
         outs = [f"r[{k}]" for k in range(nr)] + [f"D[{k}]" for k in range(nd)]
@@ -243,7 +282,11 @@ def pointwise_source(pw: Pointwise, jreal: str = "double") -> str:
         # D assignments only when flag: move them under the branch
         rl = [l for l in body if not l.strip().startswith("D[")]
         dl = [l for l in body if l.strip().startswith("D[")]
-        lines += rl + ["  if (flag) {"] + ["  " + l for l in dl] + ["  }"]
+        lines += rl
+        if mass:
+            lines += ["  if (flag == 2) {"] + mass + ["  } else if (flag) {"] + ["  " + l for l in dl] + ["  }"]
+        else:
+            lines += ["  if (flag) {"] + ["  " + l for l in dl] + ["  }"]
     else:
         lines += _emit(list(pw.r_exprs), names, False, [f"r[{k}]" for k in range(nr)], "  ")
     lines.append("}")
@@ -256,7 +299,12 @@ def pointwise_source(pw: Pointwise, jreal: str = "double") -> str:
     hnames = dict(names)
     for k, v in enumerate(vsyms):
         hnames[v] = f"V[{k}]"
-    hexprs = [sum((sp.diff(d, u) * v for u, v in zip(usyms, vsyms)), sp.Integer(0)) for (_, _, d) in pw.d_entries]
+    # a transient form: the direction moves du/dt by w0 times its value component
+    dsyms = time_derivative_symbols(pw.fields)
+    w0 = E.parameter(BDF_PARAMS[0]) if pw.transient else None
+    hexprs = [sum((sp.diff(d, u) * v for u, v in zip(usyms, vsyms)), sp.Integer(0)) +
+              sum((sp.diff(d, dsyms[f]) * w0 * vsyms[f * nc] for f in (pw.dt_fields or [])), sp.Integer(0))
+              for (_, _, d) in pw.d_entries]
     lines.append("__device__ __forceinline__ void fe_pointwise_hvp(const double* __restrict__ U, "
                  "const double* __restrict__ V, const double* __restrict__ Xq, const double* __restrict__ P, "
                  "jreal* __restrict__ D) {")
@@ -269,17 +317,32 @@ def pointwise_source(pw: Pointwise, jreal: str = "double") -> str:
     if jreal != "double":
         fl = _symbol_names(pw, prefix="f")
         lines.append("__device__ __forceinline__ void fe_pointwise_jac(const double* __restrict__ U, "
-                     "const double* __restrict__ Xq, const double* __restrict__ P, float* __restrict__ D) {")
+                     "const double* __restrict__ Xq, const double* __restrict__ P, float* __restrict__ D, int flag) {")
+        lines.append("  (void)flag;")
         nc = 1 + pw.dim
-        lines.append(f"  float fU[{max(1, len(pw.fields) * nc)}]; float fXq[3]; float fP[{max(1, len(pw.params))}];")
-        lines.append(f"  #pragma unroll\n  for (int k = 0; k < {len(pw.fields) * nc}; ++k) fU[k] = (float)U[k];")
+        nu = len(pw.fields) * nc + (len(pw.fields) if pw.transient else 0)
+        lines.append(f"  float fU[{max(1, nu)}]; float fXq[3]; float fP[{max(1, len(pw.params))}];")
+        lines.append(f"  #pragma unroll\n  for (int k = 0; k < {nu}; ++k) fU[k] = (float)U[k];")
         lines.append("  fXq[0] = (float)Xq[0]; fXq[1] = (float)Xq[1]; fXq[2] = (float)Xq[2];")
         if pw.params:
             lines.append(f"  #pragma unroll\n  for (int k = 0; k < {len(pw.params)}; ++k) fP[k] = (float)P[k];")
         if nd:
-            lines += _emit([d for (_, _, d) in pw.d_entries], fl, True, [f"D[{k}]" for k in range(nd)], "  ")
+            dl = _emit([d for (_, _, d) in pw.d_entries], fl, True, [f"D[{k}]" for k in range(nd)], "  ")
+            if pw.transient:
+                lines += ["  if (flag == 2) {"] + _mass_lines(pw, fl, True) + ["    return;", "  }"]
+            lines += dl
         lines.append("}")
     return "\n".join(lines)
+
+
+def _mass_lines(pw: Pointwise, names, fp32: bool) -> List[str]:
+    """Flag 2: D holds dr/d(du/dt) (the mass matrix's pointwise coefficients)
+    at the value columns of the time-differentiated fields, 0 elsewhere."""
+    real = "float" if fp32 else "double"
+    lines = [f"    #pragma unroll\n    for (int k = 0; k < {max(1, len(pw.d_entries))}; ++k) D[k] = ({real})0;"]
+    if pw.m_entries:
+        lines += _emit([m for _, m in pw.m_entries], names, fp32, [f"D[{k}]" for k, _ in pw.m_entries], "    ")
+    return lines
 
 
 @dataclass
@@ -433,7 +496,12 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     # at the 27 knots) and of the residual's test-function contraction of the
     # Q2 hex: one axis at a time, 729 multiply-adds each instead of 27 x 27 x 4
     sfi = bool(jref and et.name == "Q2_HEX" and nf == 1 and spaces[0] == "C2"
-               and list(layout.loc_of[0]) == list(range(nn)))
+               and list(layout.loc_of[0]) == list(range(nn)) and not pw.transient)
+    # transient forms: nodal du/dt = w0 u + w1 u_{n-1} + w2 u_{n-2} staged per
+    # element beside the values, interpolated as one more input per field
+    transient = pw.transient
+    nu = ntc + (nf if transient else 0)
+    bdf_idx = [pw.params.index(n_) for n_ in BDF_PARAMS] if transient else []
     sfi_own = sfi and not sumfac            # buffers of its own (else the Jacobian's stage buffers)
     if jref:
         per_elem = (nn * dim + 2 * nn * nval + nq * ntc + geo_doubles + gsd) * 8 + nq * ndnz_hat * jbytes
@@ -444,6 +512,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                     + (nq * ndnz + nq * nn * dim + (nq * nn1 * dim if has_c1 else 0)) * jbytes)
     if sfi_own:
         per_elem += (54 + 81 + 108) * 8
+    if transient:
+        per_elem += nn * nval * 8
     if epb is None:
         # df64: the most elements that fit 720 threads and 224 KB (GB300
         # sweeps: the Q2 hex kernel is fastest at 12 elements per block, the
@@ -460,7 +530,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         raise ValueError(f"{epb} elements per block do not fit a block ({threads} threads, {smem} B shared)")
     if name is None:
         h = hashlib.sha1((et.name + jac_precision + str(affine) + str(epb) + str(jref) + str(sumfac) + str(gsep) +
-                          str(sfi) +
+                          str(sfi) + (str(pw.m_entries) if transient else "") +
                           str(pw.r_exprs) +
                           str(pw.d_entries)).encode()).hexdigest()[:10]
         name = f"fe_elem_{et.name.lower()}_{jac_precision}{'_aff' if affine else ''}_{h}"
@@ -507,7 +577,11 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("  double* sX = sDps1 + FE_NQ * FE_NN1 * FE_DIM;")
     w("  double* sU = sX + FE_EPB * FE_NN * FE_DIM;")
     w("  double* sY = sU + FE_EPB * FE_NN * FE_NVAL;  // direction of the Hessian-vector product (flag 4)")
-    w("  double* sRh = sY + FE_EPB * FE_NN * FE_NVAL;")
+    if transient:
+        w("  double* sUt = sY + FE_EPB * FE_NN * FE_NVAL;  // nodal du/dt (BDF weights of the step)")
+        w("  double* sRh = sUt + FE_EPB * FE_NN * FE_NVAL;")
+    else:
+        w("  double* sRh = sY + FE_EPB * FE_NN * FE_NVAL;")
     w("  double* sG = sRh + FE_EPB * FE_NQ * FE_NTC;")
     w(f"  double* sGe = sG + FE_EPB * {geo_doubles};  // separable Gaussian factors, {gsd} per element")
     w(f"  jacc* sD = reinterpret_cast<jacc*>(sGe + FE_EPB * {gsd});")
@@ -584,6 +658,16 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    for (int v = 0; v < FE_NVAL; ++v) sU[k * FE_NVAL + v] = a.values[(long long)node * a.nval + v];")
     w("    if (flag == 4)")
     w("      for (int v = 0; v < FE_NVAL; ++v) sY[k * FE_NVAL + v] = a.dir[(long long)node * a.nval + v];")
+    if transient:
+        w("    { const double* Pe0 = a.params + (a.replica_elems > 0 ? ((e0 + el) / a.replica_elems) * a.params_stride : 0);")
+        w(f"      const double w0 = Pe0[{bdf_idx[0]}], w1 = Pe0[{bdf_idx[1]}], w2 = Pe0[{bdf_idx[2]}];")
+        w("      #pragma unroll")
+        w("      for (int v = 0; v < FE_NVAL; ++v) {")
+        w("        double ut = w0 * sU[k * FE_NVAL + v];")
+        w("        if (a.n_hist > 0) ut += w1 * a.hist[(long long)node * a.nval + v];")
+        w("        if (a.n_hist > 1) ut += w2 * a.hist[a.hist_stride + (long long)node * a.nval + v];")
+        w("        sUt[k * FE_NVAL + v] = ut;")
+        w("      } }")
     w("  }")
     w("  __syncthreads();")
     if affine:
@@ -690,17 +774,21 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w("      #pragma unroll")
             w("      for (int i = 0; i < FE_DIM; ++i) Xq[i] += X[l * FE_DIM + i] * ps;")
             w("    }")
-    def interp(dst, src, ind):
-        w(f"{ind}double {dst}[FE_NTC];")
+    def interp(dst, src, ind, with_dt=False):
+        with_dt = with_dt and transient
+        w(f"{ind}double {dst}[{nu if with_dt else 'FE_NTC'}];")
         for f, (fname, fsp) in enumerate(fields):
             base = f * nc
             zeros = ", ".join(["0.0"] * dim)
-            w(f"{ind}{{ double v = 0.0, gs[FE_DIM] = {{{zeros}}};")
+            fdt = with_dt and f in pw.dt_fields
+            w(f"{ind}{{ double v = 0.0, gs[FE_DIM] = {{{zeros}}};" + (" double vt = 0.0;" if fdt else ""))
             if fsp == "C2":
                 w(f"{ind}  #pragma unroll")
                 w(f"{ind}  for (int l = 0; l < FE_NN; ++l) {{")
                 w(f"{ind}    const double u = {src}[(el * FE_NN + l) * FE_NVAL + {f}];")
                 w(f"{ind}    v += u * sPsi2[q * FE_NN + l];")
+                if fdt:
+                    w(f"{ind}    vt += sUt[(el * FE_NN + l) * FE_NVAL + {f}] * sPsi2[q * FE_NN + l];")
                 w(f"{ind}    #pragma unroll")
                 w(f"{ind}    for (int b = 0; b < FE_DIM; ++b) gs[b] += u * dps[l * FE_DIM + b];")
                 w(f"{ind}  }}")
@@ -711,10 +799,14 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                 for l, node in enumerate(et.c1_index):
                     w(f"{ind}  {{ const double u = {src}[(el * FE_NN + {node}) * FE_NVAL + {f}];")
                     w(f"{ind}    v += u * ps1[{l}];")
+                    if fdt:
+                        w(f"{ind}    vt += sUt[(el * FE_NN + {node}) * FE_NVAL + {f}] * ps1[{l}];")
                     for b in range(dim):
                         w(f"{ind}    gs[{b}] += u * dp1[{l * dim + b}];")
                     w(f"{ind}  }}")
             w(f"{ind}  {dst}[{base}] = v;")
+            if fdt:
+                w(f"{ind}  {dst}[{ntc + f}] = vt;")
             w(f"{ind}  #pragma unroll")
             w(f"{ind}  for (int i = 0; i < FE_DIM; ++i) {{ double s = 0.0;")
             w(f"{ind}    #pragma unroll")
@@ -734,7 +826,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("        U[1 + i] = s; }")
         w("    }")
     else:
-        interp("U", "sU", "    ")
+        interp("U", "sU", "    ", with_dt=True)
     w("    const double* Pe = a.params + (a.replica_elems > 0 ? ((e0 + el) / a.replica_elems) * a.params_stride : 0);")
     w("    double r[FE_NTC]; jreal D[FE_NDNZ];")
     if gsep:
@@ -759,7 +851,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    }")
     w("    if (flag) {")
     if jreal == "float":
-        w("      if (flag != 4) fe_pointwise_jac(U, Xq, Pe, D);")
+        w("      if (flag != 4) fe_pointwise_jac(U, Xq, Pe, D, flag);")
     w("      if (flag == 4) {")
     interp("V", "sY", "        ")
     w("        fe_pointwise_hvp(U, V, Xq, Pe, D);")

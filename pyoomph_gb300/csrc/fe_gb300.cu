@@ -1194,9 +1194,9 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
                             "(fe_problem_set_direction) and a call of its own");
   if ((want_r && !R && p->n_dof > 0) || (want_j && !J_vals && p->nnz > 0))
     return fail(FE_ERR_ARG, "fe_assemble: missing output");
-  if (want_m && !p->fused)
-    return fail(FE_ERR_ARG, "fe_assemble: mass matrices need fused (moving-mesh) code (the fixed-mesh forms are "
-                            "steady)");
+  if (want_m && !p->fused && p->n_hist == 0)
+    return fail(FE_ERR_ARG, "fe_assemble: a mass matrix needs code of a transient form (fused code, or "
+                            "fixed-mesh code with history levels, n_history > 0)");
   if ((want_m && (flags & FE_ASSEMBLE_JACOBIAN)) || (want_p && (flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS))))
     return fail(FE_ERR_ARG, "fe_assemble: Jacobian, mass matrix and parameter derivative are separate calls");
   const int eflag = want_h ? 4 : want_p ? 3 : want_m ? 2 : want_j ? 1 : 0;

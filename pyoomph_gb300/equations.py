@@ -25,8 +25,8 @@ import numpy as np
 import sympy as sp
 
 from . import expressions as E
-from .expressions import (div, dot, grad, identity_matrix, material_derivative, sym, testfunction, var,
-                          var_and_test, weak)
+from .expressions import (div, dot, grad, identity_matrix, material_derivative, partial_t, sym, testfunction,
+                          var, var_and_test, weak)
 
 SPACE_ORDER = {"C2TB": 0, "C2": 1, "C1TB": 2, "C1": 3}
 
@@ -144,14 +144,31 @@ class PoissonEquation(Equations):
             self.add_residual(-weak(_source_expr(self, self.source), u_test))
 
 
-class NonlinearDiffusionEquation(Equations):
-    """-div((1+u^2) grad u) = f."""
+class DiffusionEquation(PoissonEquation):
+    """temporal_factor partial_t(u) - div(diffusivity grad(u)) = f
+    (pyoomph/equations/poisson.py:153-180): the Poisson form plus
+    weak(temporal_factor partial_t(u), v)."""
 
-    def __init__(self, name: str = "u", *, space: str = "C2", source=None):
+    def __init__(self, name: str = "u", *, space: str = "C2", source=None, diffusivity=1, temporal_factor=1):
+        super().__init__(name, space=space, source=source, coefficient=diffusivity)
+        self.temporal_factor = temporal_factor
+
+    def define_residuals(self):
+        super().define_residuals()
+        u, v = var_and_test(self.name)
+        self.add_residual(weak(self.temporal_factor * partial_t(u), v))
+
+
+class NonlinearDiffusionEquation(Equations):
+    """temporal_factor partial_t(u) - div((1+u^2) grad u) = f (steady by
+    default: temporal_factor 0)."""
+
+    def __init__(self, name: str = "u", *, space: str = "C2", source=None, temporal_factor=0):
         super().__init__()
         self.name = name
         self.space = space
         self.source = source
+        self.temporal_factor = temporal_factor
 
     def define_fields(self):
         self.define_scalar_field(self.name, self.space)
@@ -161,6 +178,8 @@ class NonlinearDiffusionEquation(Equations):
         self.add_residual(weak((1 + u * u) * grad(u), grad(v)))
         if self.source is not None:
             self.add_residual(-weak(_source_expr(self, self.source), v))
+        if self.temporal_factor:
+            self.add_residual(weak(self.temporal_factor * partial_t(u), v))
 
 
 class StokesEquations(Equations):
@@ -190,8 +209,9 @@ class StokesEquations(Equations):
 
 
 class NavierStokesEquations(StokesEquations):
-    """Steady incompressible Navier-Stokes (navier_stokes.py:481-503):
-    Stokes part plus weak(rho (u.grad) u, v)."""
+    """Incompressible Navier-Stokes (navier_stokes.py:481-503): Stokes part
+    plus weak(rho (partial_t u + (u.grad) u), v); the partial_t term
+    vanishes in a steady solve."""
 
     def __init__(self, *, mass_density: float = 1.0, dynamic_viscosity: float = 1.0, **kw):
         super().__init__(dynamic_viscosity=dynamic_viscosity, **kw)

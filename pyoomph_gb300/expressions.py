@@ -239,9 +239,9 @@ def dot(a: Expr, b: Expr) -> Expr:
 
 
 def material_derivative(f: Expr, velocity: Expr) -> Expr:
-    """Steady part of the material derivative, (u . grad) f (the partial_t
-    term of generic.py:564 vanishes for the stationary solves here)."""
-    return dot(velocity, grad(f))
+    """partial_t f + (u . grad) f (generic.py:564); the partial_t term
+    vanishes in a steady solve."""
+    return partial_t(f) + dot(velocity, grad(f))
 
 
 class CoordinateSystem:

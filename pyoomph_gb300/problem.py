@@ -22,10 +22,11 @@ from dataclasses import dataclass
 from typing import Callable, Dict, List, Optional, Tuple
 
 import numpy as np
+import sympy as sp
 
 from . import _native as N
 from . import expressions as E
-from .codegen import KernelSpec, Pointwise, differentiate, generate_kernel
+from .codegen import BDF_PARAMS, KernelSpec, Pointwise, differentiate, generate_kernel, time_derivative_symbols
 from .equations import (SPACE_ORDER, BoundaryCondition, DirichletBC, EquationPart, Equations,
                         PressureFixation, flatten)
 from .meshes import MeshData, MeshTemplate
@@ -158,6 +159,15 @@ class Problem:
         # absolute floor of the device solve's residual (0: relative only);
         # e.g. 0.1 x newton_solver_tolerance for an inexact Newton step
         self.linear_solver_atol = 0.0
+        # time-dependent solve: the weak form's partial_t terms are kept (BDF
+        # weights of the step as parameters, two previous time levels on the
+        # device); False: they vanish (the steady ResidualAndJacobianSteady
+        # of pyoomph's generated code).  Switched on by the first
+        # unsteady_newton_solve.
+        self.transient = False
+        self.time = 0.0
+        self.steps_done = 0
+        self.dt_prev: Optional[float] = None
         self.verbose = False
         self._initialised = False
         self.newton_history: List[float] = []
@@ -219,6 +229,10 @@ class Problem:
             b.define_residuals()
             integrand = integrand + b._residual
             params.update(b.parameter_values())
+        dsyms = time_derivative_symbols(fields)
+        self.is_transient = bool(self.transient) and any(sp.sympify(integrand).has(s_) for s_ in dsyms)
+        if not self.is_transient and hasattr(integrand, "subs"):
+            integrand = integrand.subs({s_: 0 for s_ in dsyms})
         # nodal value order: by space (C2TB, C2, C1TB, C1), then definition order
         # (codegen.cpp:2367-2380, 2795-2810)
         order = sorted(range(len(fields)), key=lambda i: (SPACE_ORDER[fields[i][1]], i))
@@ -231,6 +245,10 @@ class Problem:
         missing = [p for p in used if p not in params]
         if missing:
             raise RuntimeError(f"parameters without values: {missing}")
+        if self.is_transient:
+            # the BDF weights of the step, last (set by unsteady_newton_solve)
+            used = used + list(BDF_PARAMS)
+            params.update({k: 0.0 for k in BDF_PARAMS})
         self.param_names = used
         self.params = np.array([params[p] for p in used], dtype=np.float64)
         t1 = time.perf_counter()
@@ -254,7 +272,7 @@ class Problem:
         # geometry kind only -- not on the mesh size: cache it per process
         gsep = bool(self.separable_source and self.affine and mesh_is_axis_aligned(mesh))
         key = (mesh.etype.name, tuple(fields), str(integrand), tuple(used), kprec, self.affine, gsep,
-               self.elems_per_block, self.jacobian_reference)
+               self.is_transient, self.elems_per_block, self.jacobian_reference)
         ks = _KERNEL_CACHE.get(key)
         if ks is None:
             pw = differentiate(fields, mesh.dim, integrand, used)
@@ -447,7 +465,7 @@ class Problem:
         desc = N.ProblemDesc(mesh.dim, mesh.n_nodes, len(self.fields), k["x"].ctypes.data, k["eqn"].ctypes.data,
                              self.n_dof, 1, doms, len(self.params), k["params"].ctypes.data,
                              N.FE_JAC_F64 if self._prec == "f64" else N.FE_JAC_F32,
-                             getattr(self, "params_stride", 0), 0, None, 0,
+                             getattr(self, "params_stride", 0), 2 if self.is_transient else 0, None, 0,
                              int(self.hang_slots.size), k["hs"].ctypes.data, k["hp"].ctypes.data,
                              k["hm"].ctypes.data, k["hw"].ctypes.data)
         return desc, doms, keep
@@ -492,6 +510,15 @@ class Problem:
         v = np.ascontiguousarray(values, dtype=np.float64).reshape(self.mesh.n_nodes, len(self.fields))
         N.check(N.load().fe_problem_set_values(self._h, v.ctypes.data))
         self.set_dofs(self._dofs_from_values(v))
+
+    def set_history_values(self, level: int, values: np.ndarray) -> None:
+        """Nodal values [n_nodes, nval] of a previous time level of a
+        transient problem (0: u_{n-1}, 1: u_{n-2}); unsteady_newton_solve
+        fills them itself."""
+        if not self.is_transient:
+            raise RuntimeError("a steady problem keeps no time levels")
+        v = np.ascontiguousarray(values, dtype=np.float64).reshape(self.mesh.n_nodes, len(self.fields))
+        N.check(N.load().fe_problem_set_history(self._h, int(level), v.ctypes.data))
 
     def get_current_dofs(self):
         """pyoomph's accessor: (dof vector, pinned values)."""
@@ -686,6 +713,73 @@ class Problem:
         if callable(self.linear_solver):
             return self.linear_solver(A, R)
         return spla.splu(A.tocsc()).solve(R)
+
+    # -- time stepping ---------------------------------------------------
+    def unsteady_newton_solve(self, dt: float) -> List[float]:
+        """One implicit time step of size dt (pyoomph's
+        Problem.unsteady_newton_solve): the current values become the
+        previous time level (and the previous one the one before), the BDF
+        weights of the step are set -- BDF1 on the first step, BDF2 with
+        variable steps after it (the degraded start of pyoomph's BDF2,
+        timestepper.hpp:46-108) -- and Newton solves for the new level.
+        The first call on a steady problem switches it to its transient form
+        (a new kernel; the dofs are kept).  Returns the Newton residual
+        history."""
+        from .ale import bdf_weights
+        if dt <= 0.0:
+            raise ValueError("dt must be positive")
+        if not self.transient:
+            self.make_transient()
+        self.initialise()
+        if not self.is_transient:
+            raise RuntimeError("the weak form has no time derivative (partial_t)")
+        self.assemble_device(with_jacobian=False)      # nodal values = the current dofs
+        N.check(N.load().fe_problem_shift_history(self._h))
+        if self.steps_done == 0:
+            N.check(N.load().fe_problem_shift_history(self._h))   # both levels = the initial state
+        w = bdf_weights(1 if self.steps_done == 0 else 2, dt, self.dt_prev)
+        self.set_parameters(**dict(zip(BDF_PARAMS, w)))
+        hist = self.solve()
+        self.steps_done += 1
+        self.dt_prev = dt
+        self.time += dt
+        return hist
+
+    def make_transient(self) -> None:
+        """Keep the partial_t terms from now on.  An initialised problem is
+        rebuilt with its transient kernel; its dofs carry over."""
+        if self.transient:
+            return
+        dofs = self.get_dofs() if self._initialised else None
+        self.transient = True
+        if self._initialised:
+            if getattr(self, "_h", None):
+                N.load().fe_problem_destroy(self._h)
+                self._h = None
+            self._initialised = False
+        self.kernel = None
+        self.initialise()
+        if dofs is not None:
+            self.set_dofs(dofs)
+
+    def get_mass_matrix(self):
+        """The mass matrix M = dR/d(du/dt) on the Jacobian's CSR pattern (flag
+        2 of pyoomph's generated ResidualAndJacobian; the eigenproblem
+        J v = lambda M v of Problem.get_eigenvalues).  A steady problem is
+        switched to its transient form first."""
+        import scipy.sparse as sps
+        torch = _torch()
+        if not self.transient:
+            self.make_transient()
+        self.initialise()
+        M = torch.zeros_like(self.J_dev)
+        st = torch.cuda.current_stream().cuda_stream
+        N.check(N.load().fe_assemble(self._h, self.x_dev.data_ptr(), self.R_dev.data_ptr(), M.data_ptr(),
+                                     N.FE_ASSEMBLE_MASS | N.FE_ASSEMBLE_VALUES_FROM_DOFS, ctypes.c_void_p(st)))
+        self.check()
+        rp, ci = self.pattern()
+        return sps.csr_matrix((M[:self.nnz].cpu().numpy().astype(np.float64), ci, rp),
+                              shape=(self.n_dof, self.n_dof))
 
     def solve(self, **_ignored) -> List[float]:
         """Stationary Newton solve; returns the residual max-norm history."""

@@ -16,8 +16,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from .equations import (DirichletBC, NavierStokesEquations, NonlinearDiffusionEquation, PoissonEquation,
-                        PressureFixation)
+from .equations import (DiffusionEquation, DirichletBC, NavierStokesEquations, NonlinearDiffusionEquation,
+                        PoissonEquation, PressureFixation)
 from .meshes import CuboidBrickMesh, RectangularQuadMesh
 from .problem import Problem
 
@@ -35,34 +35,41 @@ def lid_velocity(x, y):
 
 
 def poisson_problem(N=64, seed: int = 0, gaussians: np.ndarray = None, split: str = None,
-                    jacobian_precision: str = "fp64", transform=None) -> Problem:
+                    jacobian_precision: str = "fp64", transform=None, transient: bool = False) -> Problem:
+    """transient: the diffusion equation du/dt - Laplace(u) = f instead."""
     g = draw_gaussians(seed, 8, 2) if gaussians is None else gaussians
     P = Problem()
     P.jacobian_precision = jacobian_precision
+    P.transient = transient
     P += RectangularQuadMesh(N=N, split_in_tris=split or False, transform=transform)
-    P += (PoissonEquation(source=g) + DirichletBC(u=0.0) @ ["left", "right", "top", "bottom"]) @ "domain"
+    eq = DiffusionEquation(source=g) if transient else PoissonEquation(source=g)
+    P += (eq + DirichletBC(u=0.0) @ ["left", "right", "top", "bottom"]) @ "domain"
     return P
 
 
 def nonlinear_diffusion_problem(N=48, seed: int = 0, gaussians: np.ndarray = None,
-                                jacobian_precision: str = "fp64", dim: int = 3, transform=None) -> Problem:
+                                jacobian_precision: str = "fp64", dim: int = 3, transform=None,
+                                transient: bool = False) -> Problem:
+    """transient: du/dt - div((1+u^2) grad u) = f instead."""
     g = draw_gaussians(seed, 16, dim) if gaussians is None else gaussians
     P = Problem()
     P.jacobian_precision = jacobian_precision
+    P.transient = transient
     if dim == 3:
         P += CuboidBrickMesh(N=N, transform=transform)
         walls = ["left", "right", "top", "bottom", "back", "front"]
     else:
         P += RectangularQuadMesh(N=N, transform=transform)
         walls = ["left", "right", "top", "bottom"]
-    P += (NonlinearDiffusionEquation(source=g) + DirichletBC(u=0.0) @ walls) @ "domain"
+    P += (NonlinearDiffusionEquation(source=g, temporal_factor=1 if transient else 0) + DirichletBC(u=0.0) @ walls) @ "domain"
     return P
 
 
 def navier_stokes_problem(N=256, Re: float = 100.0, split: str = "left",
-                          jacobian_precision: str = "fp64", transform=None) -> Problem:
+                          jacobian_precision: str = "fp64", transform=None, transient: bool = False) -> Problem:
     P = Problem()
     P.jacobian_precision = jacobian_precision
+    P.transient = transient
     P += RectangularQuadMesh(N=N, split_in_tris=split, transform=transform)
     eqs = NavierStokesEquations(mass_density=1.0, dynamic_viscosity=1.0 / Re)
     eqs += DirichletBC(velocity_x=lid_velocity, velocity_y=0.0) @ "top"

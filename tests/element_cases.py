@@ -8,12 +8,12 @@ import oracle as O
 KINDS = ["poisson_q2", "poisson_p2", "ns_th", "nldiff_hex", "nldiff_q2"]
 
 
-def build(kind: str, geometry: str, prec: str, seed: int = 3, jref=None):
+def build(kind: str, geometry: str, prec: str, seed: int = 3, jref=None, transient: bool = False):
     from pyoomph_gb300 import workloads as W
     rng = np.random.default_rng(seed)
     T = W.wavy(0.03) if geometry == "general" else None
     if kind == "ns_th":
-        P = W.navier_stokes_problem(N=[4, 3], transform=T, jacobian_precision=prec)
+        P = W.navier_stokes_problem(N=[4, 3], transform=T, jacobian_precision=prec, transient=transient)
         et, eq, n3 = O.P2_TRI, O.EQ_NAVIER_STOKES_TH, (4, 3, 0)
         params = np.array([1.0, 0.01])
     else:
@@ -23,10 +23,11 @@ def build(kind: str, geometry: str, prec: str, seed: int = 3, jref=None):
         nx = list(n3[:dim])
         if kind.startswith("poisson"):
             P = W.poisson_problem(N=nx, gaussians=gauss, split="left" if et == O.P2_TRI else None, transform=T,
-                                  jacobian_precision=prec)
+                                  jacobian_precision=prec, transient=transient)
             eq = O.EQ_POISSON
         else:
-            P = W.nonlinear_diffusion_problem(N=nx, gaussians=gauss, dim=dim, transform=T, jacobian_precision=prec)
+            P = W.nonlinear_diffusion_problem(N=nx, gaussians=gauss, dim=dim, transform=T, jacobian_precision=prec,
+                                              transient=transient)
             eq = O.EQ_NONLINEAR_DIFFUSION
         params = O.gaussian_params(gauss)
     P.geometry = geometry if geometry == "general" else "auto"

@@ -93,9 +93,10 @@ def build(ks) -> ctypes.CDLL:
     return L
 
 
-def run(ks, x, conn, values, params, flag: int = 1, direction=None, aux: int = 0):
+def run(ks, x, conn, values, params, flag: int = 1, direction=None, aux: int = 0, hist=None):
     """Element residuals [E, nloc] and matrices [E, nloc, nloc] of the
-    generated kernel ks on the given mesh data (host arrays)."""
+    generated kernel ks on the given mesh data (host arrays); ``hist``
+    [levels, n_nodes, nval]: previous time levels of the values."""
     L = build(ks)
     E = conn.shape[0]
     nloc = ks.layout.n
@@ -110,8 +111,14 @@ def run(ks, x, conn, values, params, flag: int = 1, direction=None, aux: int = 0
     status = np.zeros(4, dtype=np.int32)
     if direction is not None:
         direction = np.ascontiguousarray(direction, dtype=np.float64)
+    nh = 0
+    if hist is not None:
+        hist = np.ascontiguousarray(hist, dtype=np.float64)
+        assert hist.shape[1:] == values.shape
+        nh = hist.shape[0]
     a = _Args(x.ctypes.data, conn.ctypes.data, values.ctypes.data, params.ctypes.data, tables.ctypes.data,
-              rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data, 0, 0, None, None, 0, 0, aux,
+              rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data, 0, 0,
+              None if hist is None else hist.ctypes.data, None, nh, values.size, aux,
               x.shape[0], values.ctypes.data if direction is None else direction.ctypes.data)
     L.fe_emu_run(ctypes.byref(a), (E + ks.epb - 1) // ks.epb)
     return rbuf, jbuf, status

@@ -75,7 +75,8 @@ def test_krylov_solver_arguments_are_checked_before_any_device_call():
     assert L.fe_csr_spmv(None, None, None, N.FE_JAC_F64, None, None, 10, 10, None) == N.FE_ERR_ARG
 
 
-@pytest.mark.parametrize("kind", ["poisson", "poisson_p2", "ns", "ns32", "nsdf", "hex", "hex32", "hexdf"])
+@pytest.mark.parametrize("kind", ["poisson", "poisson_p2", "ns", "ns32", "nsdf", "hex", "hex32", "hexdf",
+                                  "ns_t", "ns32_t", "hexdf_t"])
 def test_generated_kernels_compile_for_sm103a(kind, tmp_path):
     from pyoomph_gb300 import _native as N
     from pyoomph_gb300 import workloads as W
@@ -84,7 +85,10 @@ def test_generated_kernels_compile_for_sm103a(kind, tmp_path):
          "hex": lambda: W.nonlinear_diffusion_problem(N=2),
          "hex32": lambda: W.nonlinear_diffusion_problem(N=2, jacobian_precision="fp32"),
          "nsdf": lambda: W.navier_stokes_problem(N=4, jacobian_precision="df64"),
-         "hexdf": lambda: W.nonlinear_diffusion_problem(N=2, jacobian_precision="df64")}[kind]()
+         "hexdf": lambda: W.nonlinear_diffusion_problem(N=2, jacobian_precision="df64"),
+         "ns_t": lambda: W.navier_stokes_problem(N=4, transient=True),
+         "ns32_t": lambda: W.navier_stokes_problem(N=4, jacobian_precision="fp32", transient=True),
+         "hexdf_t": lambda: W.nonlinear_diffusion_problem(N=2, jacobian_precision="df64", transient=True)}[kind]()
     ks = P.lower()
     assert ks.smem_bytes <= 227 * 1024 and ks.threads % 32 == 0 and ks.threads <= 1024
     assert N.code_build(ks.source, ks.name, str(tmp_path)) > 0
@@ -124,7 +128,7 @@ def test_pointwise_derivatives_match_finite_differences():
     """D = dr/du from the code generator against central differences of r."""
     import sympy as sp
     from pyoomph_gb300 import expressions as E
-    from pyoomph_gb300.codegen import differentiate
+    from pyoomph_gb300.codegen import differentiate, time_derivative_symbols
     from pyoomph_gb300.equations import NavierStokesEquations
     E.set_dimension(2)
     eq = NavierStokesEquations(mass_density=1.3, dynamic_viscosity=0.07)
@@ -133,7 +137,9 @@ def test_pointwise_derivatives_match_finite_differences():
     eq.define_residuals()
     fields = sorted(eq._fields, key=lambda f: {"C2": 0, "C1": 1}[f[1]])
     params = sorted(eq.parameter_values())
-    pw = differentiate(fields, 2, eq._residual, params)
+    # the steady form (partial_t terms vanish)
+    steady = eq._residual.subs({s_: 0 for s_ in time_derivative_symbols(fields)})
+    pw = differentiate(fields, 2, steady, params)
     usyms = []
     for name, _ in fields:
         usyms += [E.REG.value[name]] + list(E.REG.grad[name][:2])

@@ -1,0 +1,191 @@
+"""Time-dependent forms on fixed meshes: partial_t terms with BDF weights
+(pyoomph's DiffusionEquation, poisson.py:153-180, and the rho partial_t(u)
+of Navier-Stokes, navier_stokes.py:481-503), the mass matrix (flag 2 of the
+generated ResidualAndJacobian, jitbridge.h:285) and the BDF1/BDF2 time
+stepping of Problem.unsteady_newton_solve.
+
+These forms are linear in du/dt with a coefficient c independent of u, so
+the oracle's transient element residual is R_e(u) + M_e udot_e and its
+Jacobian J_e + w0 M_e, with M_e = c int psi_i psi_j (ofe_element_mass) and
+udot the BDF combination of the nodal time levels."""
+import numpy as np
+import pytest
+
+import element_cases as C
+import oracle as O
+
+# BDF2 with a variable step (dt = 0.1 after 0.07)
+_OM = 0.1 / 0.07
+W_BDF2 = ((1.0 + 2.0 * _OM) / ((1.0 + _OM) * 0.1), -(1.0 + _OM) / 0.1, _OM * _OM / ((1.0 + _OM) * 0.1))
+
+
+def _oracle_mass(kind, P, ks):
+    et = {"ns_th": O.P2_TRI, "poisson_q2": O.Q2_QUAD, "poisson_p2": O.P2_TRI, "nldiff_hex": O.Q2_HEX,
+          "nldiff_q2": O.Q2_QUAD}[kind]
+    eq = {"ns_th": O.EQ_NAVIER_STOKES_TH, "poisson_q2": O.EQ_POISSON, "poisson_p2": O.EQ_POISSON,
+          "nldiff_hex": O.EQ_NONLINEAR_DIFFUSION, "nldiff_q2": O.EQ_NONLINEAR_DIFFUSION}[kind]
+    coeff = 1.0  # rho = 1 (Navier-Stokes), temporal factor 1
+    m = P.mesh
+    n = ks.layout.n
+    out = []
+    for e in range(m.n_elem):
+        M = np.zeros(n * n)
+        O.lib().ofe_element_mass(et, eq, m.dim, O._ptr(np.ascontiguousarray(m.x)),
+                                 O._ptr(np.ascontiguousarray(m.conn[e])), coeff, O._ptr(M))
+        out.append(M.reshape(n, n))
+    return np.array(out)
+
+
+def _local(ks, conn, nodal):
+    """Nodal values [n_nodes, nval] -> element-local vectors [E, nloc]."""
+    lay = ks.layout
+    return nodal[conn[:, lay.node], lay.val]
+
+
+@pytest.mark.parametrize("geometry", ["affine", "general"])
+@pytest.mark.parametrize("kind,prec", [(k, "fp64") for k in C.KINDS] + [("ns_th", "df64"), ("poisson_q2", "fp32"),
+                                                                       ("nldiff_hex", "df64")])
+def test_emulated_transient_element_matches_oracle(kind, geometry, prec):
+    import kernel_emulator as KE
+    P, ks, values, Rr, Jr = C.build(kind, geometry, prec, transient=True)
+    assert ks.pointwise.transient and P.param_names[-3:] == ["_bdf_w0", "_bdf_w1", "_bdf_w2"]
+    m = P.mesh
+    rng = np.random.default_rng(11)
+    hist = np.stack([values + rng.normal(0.0, 0.2, values.shape), values + rng.normal(0.0, 0.2, values.shape)])
+    params = P.params.copy()
+    params[-3:] = W_BDF2
+    rb, jb, st = KE.run(ks, m.x, m.conn, values, params, flag=1, hist=hist)
+    assert not st.any()
+    _, mb, st = KE.run(ks, m.x, m.conn, values, params, flag=2, hist=hist)
+    assert not st.any()
+    Me = _oracle_mass(kind, P, ks)
+    udot = W_BDF2[0] * values + W_BDF2[1] * hist[0] + W_BDF2[2] * hist[1]
+    ue = _local(ks, m.conn, udot)
+    Rt = Rr + np.einsum("eij,ej->ei", Me, ue)
+    Jt = Jr + W_BDF2[0] * Me
+    jtol = 1e-5 if prec == "fp32" else 1e-12
+    assert C.relmax(rb, Rt) <= 1e-12
+    assert C.relmax(jb, Jt) <= jtol
+    assert C.relmax(mb, Me) <= jtol
+    # the time term is really there: the transient residual differs from the steady one
+    assert C.relmax(Rr, Rt) > 1e-3
+
+
+def test_steady_lowering_drops_the_time_derivative():
+    """A steady problem generates the steady kernel (no history, no BDF
+    weights), even where the form has partial_t terms (Navier-Stokes)."""
+    from pyoomph_gb300 import workloads as W
+    P = W.navier_stokes_problem(N=4)
+    ks = P.lower()
+    assert not ks.pointwise.transient and "_bdf_w0" not in P.param_names and "sUt" not in ks.source
+    Pt = W.navier_stokes_problem(N=4, transient=True)
+    kt = Pt.lower()
+    assert kt.pointwise.transient and "sUt" in kt.source and kt.name != ks.name
+    # BDF weights: BDF1, and BDF2 reproducing d/dt of a quadratic in time exactly
+    from pyoomph_gb300.ale import bdf_weights
+    w = bdf_weights(2, 0.1, 0.07)
+    t = np.array([0.17, 0.07, 0.0])
+    f = 3.0 + 2.0 * t - 5.0 * t * t
+    assert abs(np.dot(w, f) - (2.0 - 10.0 * 0.17)) < 1e-12
+    assert np.allclose(bdf_weights(1, 0.1), (10.0, -10.0, 0.0))
+
+
+def _engine_and_oracle(kind, prec, n=6):
+    from pyoomph_gb300 import workloads as W
+    if kind == "ns":
+        P = W.navier_stokes_problem(N=n, Re=50.0, jacobian_precision=prec, transient=True)
+        OP = O.navier_stokes_problem(O.mesh(O.P2_TRI, n, n), rho=1.0, mu=0.02)
+        et, eq = O.P2_TRI, O.EQ_NAVIER_STOKES_TH
+    elif kind == "poisson":
+        g = W.draw_gaussians(4, 8, 2)
+        P = W.poisson_problem(N=n, gaussians=g, jacobian_precision=prec, transient=True)
+        OP = O.poisson_problem(O.mesh(O.Q2_QUAD, n, n), g)
+        et, eq = O.Q2_QUAD, O.EQ_POISSON
+    else:
+        g = W.draw_gaussians(4, 16, 3)
+        P = W.nonlinear_diffusion_problem(N=3, gaussians=g, jacobian_precision=prec, transient=True)
+        OP = O.poisson_problem(O.mesh(O.Q2_HEX, 3, 3, 3), g, eq=O.EQ_NONLINEAR_DIFFUSION)
+        et, eq = O.Q2_HEX, O.EQ_NONLINEAR_DIFFUSION
+    return P, OP, et, eq
+
+
+def _oracle_time_term(P, et, eq, udot):
+    """Global sum_e M_e udot_e (free rows) and the free-free block of the
+    assembled mass matrix, dense (small meshes)."""
+    m, lay = P.mesh, P.kernel.layout
+    n = lay.n
+    R = np.zeros(P.n_dof)
+    M = np.zeros((P.n_dof, P.n_dof))
+    for e in range(m.n_elem):
+        Me = np.zeros(n * n)
+        O.lib().ofe_element_mass(et, eq, m.dim, O._ptr(np.ascontiguousarray(m.x)),
+                                 O._ptr(np.ascontiguousarray(m.conn[e])), 1.0, O._ptr(Me))
+        Me = Me.reshape(n, n)
+        g = P.eqn[m.conn[e, lay.node], lay.val]
+        r = Me @ udot[m.conn[e, lay.node], lay.val]
+        f = g >= 0
+        np.add.at(R, g[f], r[f])
+        M[np.ix_(g[f], g[f])] += Me[np.ix_(f, f)]
+    return R, M
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,prec", [("poisson", "fp64"), ("ns", "fp64"), ("ns", "df64"), ("hex", "fp64"),
+                                       ("hex", "fp32")])
+def test_gpu_transient_assembly_matches_oracle(kind, prec):
+    P, OP, et, eq = _engine_and_oracle(kind, prec)
+    P.initialise()
+    rng = np.random.default_rng(8)
+    free = P.eqn >= 0
+    levels = []
+    for _ in range(3):
+        v = P._values0.copy()
+        v[free] += rng.normal(0.0, 0.3, free.sum())
+        levels.append(v)
+    P.set_values(levels[0])
+    P.set_history_values(0, levels[1])
+    P.set_history_values(1, levels[2])
+    P.set_parameters(**dict(zip(["_bdf_w0", "_bdf_w1", "_bdf_w2"], W_BDF2)))
+    R, J = P.get_jacobian()
+    Mm = P.get_mass_matrix()
+    x = P.get_dofs()
+    OP.set_dofs(x)
+    R0, rp, ci, v0 = O.assemble(OP, True, -1.0)
+    prp, pci = P.pattern()
+    assert np.array_equal(prp, rp) and np.array_equal(pci, ci)
+    udot = W_BDF2[0] * levels[0] + W_BDF2[1] * levels[1] + W_BDF2[2] * levels[2]
+    Rt, Md = _oracle_time_term(P, et, eq, udot)
+    rows = np.repeat(np.arange(P.n_dof), np.diff(rp))
+    Mv = Md[rows, ci]
+    jtol = 1e-5 if prec == "fp32" else 1e-12
+    assert C.relmax(R, R0 + Rt) <= 1e-12
+    assert C.relmax(J.data, v0 + W_BDF2[0] * Mv) <= jtol
+    assert np.array_equal(Mm.indptr, rp) and np.array_equal(Mm.indices, ci)
+    assert C.relmax(Mm.data, Mv) <= jtol
+
+
+@pytest.mark.gpu
+def test_gpu_heat_equation_known_answer_second_order_in_time():
+    """du/dt = Laplace(u) on the unit square, u = 0 on the boundary,
+    u(0) = sin(pi x) sin(pi y): u(t) = exp(-2 pi^2 t) sin(pi x) sin(pi y).
+    BDF2 (BDF1 first step) through unsteady_newton_solve: the error at
+    t = 0.1 falls by ~4 when dt halves."""
+    from pyoomph_gb300 import DiffusionEquation, DirichletBC, Problem, RectangularQuadMesh
+    errs = []
+    for nsteps in (10, 20):
+        P = Problem()
+        P += RectangularQuadMesh(N=24)
+        P += (DiffusionEquation() + DirichletBC(u=0.0) @ ["left", "right", "top", "bottom"]) @ "domain"
+        P.initialise()
+        x = P.mesh.x
+        u0 = (np.sin(np.pi * x[:, 0]) * np.sin(np.pi * x[:, 1]))[:, None]
+        P.set_values(u0)
+        dt = 0.1 / nsteps
+        for _ in range(nsteps):
+            hist = P.unsteady_newton_solve(dt)
+            assert hist[-1] < 1e-10
+        assert P.is_transient and abs(P.time - 0.1) < 1e-12
+        exact = np.exp(-2.0 * np.pi ** 2 * 0.1) * u0[:, 0]
+        errs.append(np.max(np.abs(P.get_values()[:, 0] - exact)))
+    assert errs[1] < 2e-3
+    assert 3.2 < errs[0] / errs[1] < 4.8, errs
