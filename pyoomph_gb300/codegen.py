@@ -496,7 +496,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     # at the 27 knots) and of the residual's test-function contraction of the
     # Q2 hex: one axis at a time, 729 multiply-adds each instead of 27 x 27 x 4
     sfi = bool(jref and et.name == "Q2_HEX" and nf == 1 and spaces[0] == "C2"
-               and list(layout.loc_of[0]) == list(range(nn)) and not pw.transient)
+               and list(layout.loc_of[0]) == list(range(nn)))
     # transient forms: nodal du/dt = w0 u + w1 u_{n-1} + w2 u_{n-2} staged per
     # element beside the values, interpolated as one more input per field
     transient = pw.transient
@@ -519,9 +519,11 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         # sweeps: the Q2 hex kernel is fastest at 12 elements per block, the
         # largest that fits the shared memory; the P2 Taylor-Hood kernel at
         # 48, 720 threads)
+        # (the sum-factorised Q2 hex kernels are fastest at the largest block
+        # that fits too: the steady FP64 one at 13 elements)
         epb, threads = _launch_shape(et, nloc, per_elem, table_bytes,
                                      smem_cap=224 * 1024 if df64 else 216 * 1024,
-                                     max_threads=720 if df64 else 512, largest=df64)
+                                     max_threads=720 if df64 else 512, largest=df64 or sumfac)
     else:
         threads = ((max(epb * nq, epb * nloc) + 31) // 32) * 32
     smem = table_bytes + epb * per_elem
@@ -815,7 +817,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w(f"{ind}}}")
 
     if sfi:
-        w("    double U[FE_NTC];")
+        w(f"    double U[{nu if transient else 'FE_NTC'}];")
         w(f"    {{ const double* C = sIc + el * {SC} + q;")
         w("      const double gs[3] = {C[27], C[54], C[81]};")
         w("      U[0] = C[0];")
@@ -825,6 +827,12 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("        for (int b = 0; b < FE_DIM; ++b) s += g[b][i] * gs[b];")
         w("        U[1 + i] = s; }")
         w("    }")
+        if transient:
+            # du/dt at the knot: the value only, one plain pass over the nodes
+            w("    { double vt = 0.0;")
+            w("      #pragma unroll")
+            w("      for (int l = 0; l < FE_NN; ++l) vt += sUt[(el * FE_NN + l) * FE_NVAL] * sPsi2[q * FE_NN + l];")
+            w(f"      U[{ntc}] = vt; }}")
     else:
         interp("U", "sU", "    ", with_dt=True)
     w("    const double* Pe = a.params + (a.replica_elems > 0 ? ((e0 + el) / a.replica_elems) * a.params_stride : 0);")

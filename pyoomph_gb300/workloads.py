@@ -113,18 +113,26 @@ def _main(argv=None) -> None:
     ap.add_argument("--epb", type=int, default=None, help="elements per block (default: the generator's)")
     ap.add_argument("--jref", type=int, choices=[0, 1], default=None,
                     help="1: contract the Jacobian in reference coordinates, 0: physical (default: the generator's)")
+    ap.add_argument("--transient", action="store_true",
+                    help="the transient form (BDF2 weights of dt = 1e-3, both previous levels = the current values)")
     a = ap.parse_args(argv)
     if a.workload == "ns":
-        P = navier_stokes_problem(N=a.side, jacobian_precision=a.precision)
+        P = navier_stokes_problem(N=a.side, jacobian_precision=a.precision, transient=a.transient)
     elif a.workload == "poisson":
-        P = poisson_problem(N=a.side, seed=0, jacobian_precision=a.precision)
+        P = poisson_problem(N=a.side, seed=0, jacobian_precision=a.precision, transient=a.transient)
     else:
-        P = nonlinear_diffusion_problem(N=a.side, seed=0, jacobian_precision=a.precision)
+        P = nonlinear_diffusion_problem(N=a.side, seed=0, jacobian_precision=a.precision, transient=a.transient)
     P.elems_per_block = a.epb
     if a.jref is not None:
         P.jacobian_reference = bool(a.jref)
     P.initialise()
     perturb_dofs(P, seed=0, sigma=1e-3)
+    if a.transient:
+        from .ale import bdf_weights
+        P.assemble_device(with_jacobian=False)
+        P.set_history_values(0, P.get_values())
+        P.set_history_values(1, P.get_values())
+        P.set_parameters(**dict(zip(("_bdf_w0", "_bdf_w1", "_bdf_w2"), bdf_weights(2, 1e-3, 1e-3))))
     P.assemble_device(with_jacobian=True)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
