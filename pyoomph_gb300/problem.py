@@ -107,6 +107,32 @@ def nvtx_range(name: str):
     return contextlib.nullcontext()
 
 
+def solve_generalized_eigenproblem(J, M, n: int, shift=0.0, sort: bool = True, which: str = "LM", v0=None,
+                                   target=None):
+    """(-J) v = lambda M v for sparse J, M (host): all eigenpairs densely when
+    n covers the system, else n of them by shift-invert Arnoldi about
+    `shift` (scipy's eigs, as pyoomph's scipy eigensolver, solvers/scipy.py:166-190).
+    Sorted by descending real part, or by distance to `target`; infinite
+    eigenvalues (rows without mass: constraints, pressure) dropped in the
+    dense branch.  Returns (eigenvalues, eigenvectors as rows)."""
+    import scipy.linalg as sla
+    import scipy.sparse.linalg as spla_
+    A = -J.astype(np.float64)
+    N_ = A.shape[0]
+    if n <= 0 or n >= N_ - 1:
+        ev, vec = sla.eig(A.toarray(), b=M.toarray())
+        keep = np.isfinite(ev)
+        ev, vec = ev[keep], vec[:, keep]
+    else:
+        ev, vec = spla_.eigs(A.tocsc(), k=n, M=M.tocsc(), sigma=shift, which=which, v0=v0)
+    if sort:
+        order = np.argsort(np.abs(ev - target)) if target is not None else np.argsort(-ev.real, kind="stable")
+        ev, vec = ev[order], vec[:, order]
+    if n > 0:
+        ev, vec = ev[:n], vec[:, :n]
+    return ev, vec.T
+
+
 class NewtonSolverError(RuntimeError):
     """Raised when Newton diverges or exceeds its iteration cap
     (oomph's NewtonSolverError, problem.cc:9298)."""
@@ -780,6 +806,38 @@ class Problem:
         rp, ci = self.pattern()
         return sps.csr_matrix((M[:self.nnz].cpu().numpy().astype(np.float64), ci, rp),
                               shape=(self.n_dof, self.n_dof))
+
+    def solve_eigenproblem(self, n: int, shift=0.0, sort: bool = True, which: str = "LM", v0=None,
+                           target=None):
+        """Eigenvalues lambda and eigenvectors v of (-J) v = lambda M v at the
+        current dofs, J the steady Jacobian and M the mass matrix, both
+        assembled on the device (pyoomph's Problem.solve_eigenproblem with
+        its scipy eigensolver: solvers/generic.py:377-383 negates J,
+        solvers/scipy.py:166-190 solves shift-inverted).  Returns
+        (eigenvalues [n], eigenvectors [n, n_dof]), also kept for
+        get_last_eigenvalues / get_last_eigenvectors."""
+        M = self.get_mass_matrix()
+        # the steady Jacobian: BDF weights 0 for the assembly
+        keep = None
+        if self.is_transient:
+            idx = [self.param_names.index(k) for k in BDF_PARAMS]
+            keep = self.params[idx].copy()
+            self.set_parameters(**{k: 0.0 for k in BDF_PARAMS})
+        try:
+            _, J = self.get_jacobian()
+        finally:
+            if keep is not None:
+                self.set_parameters(**dict(zip(BDF_PARAMS, keep)))
+        ev, vec = solve_generalized_eigenproblem(J, M, n, shift=shift, sort=sort, which=which, v0=v0,
+                                                 target=target)
+        self._last_eigen = (ev, vec)
+        return ev, vec
+
+    def get_last_eigenvalues(self) -> np.ndarray:
+        return self._last_eigen[0] if getattr(self, "_last_eigen", None) else np.zeros(0, dtype=complex)
+
+    def get_last_eigenvectors(self) -> np.ndarray:
+        return self._last_eigen[1] if getattr(self, "_last_eigen", None) else np.zeros((0, 0), dtype=complex)
 
     def solve(self, **_ignored) -> List[float]:
         """Stationary Newton solve; returns the residual max-norm history."""

@@ -199,3 +199,60 @@ def test_gpu_heat_equation_known_answer_second_order_in_time():
             y.append(-(w[1] * y[-1] + w[2] * y[-2]) / (w[0] + lam))
         model = abs(y[-1] - np.exp(-lam * 0.1))
         assert abs(err - model) <= 0.01 * model, (nsteps, err, model)
+
+
+def test_generalized_eigensolver_host_logic():
+    """(-J) v = lambda M v: the shift-invert branch agrees with the dense
+    one; rows without mass (constraints) give infinite eigenvalues that the
+    dense branch drops; eigenpairs satisfy the equation."""
+    import scipy.sparse as sps
+    from pyoomph_gb300.problem import solve_generalized_eigenproblem
+    n = 40
+    h = 1.0 / (n + 1)
+    K = sps.diags([-np.ones(n - 1), 2 * np.ones(n), -np.ones(n - 1)], [-1, 0, 1]) / h     # 1D P1 stiffness
+    M = sps.diags([np.ones(n - 1), 4 * np.ones(n), np.ones(n - 1)], [-1, 0, 1]) * h / 6   # and mass
+    J = K.tocsr()                       # du/dt = u'' -> J = K, eigenvalues of -K: -(k pi)^2 approx
+    ev_d, vec_d = solve_generalized_eigenproblem(J, M.tocsr(), 0)
+    ev_s, vec_s = solve_generalized_eigenproblem(J, M.tocsr(), 4, shift=0.0)
+    assert np.allclose(ev_s, ev_d[:4], rtol=1e-10)
+    assert abs(ev_d[0].real + np.pi ** 2) < 1e-2 * np.pi ** 2
+    for lam, v in zip(ev_s, vec_s):
+        assert np.linalg.norm(-J @ v - lam * (M @ v)) <= 1e-8 * np.linalg.norm(J @ v)
+    # a constraint row (no mass) has an infinite eigenvalue
+    M2 = M.tolil()
+    M2[0, :] = 0.0
+    ev2, _ = solve_generalized_eigenproblem(J, M2.tocsr(), 0)
+    assert np.all(np.isfinite(ev2)) and len(ev2) == n - 1
+
+
+@pytest.mark.gpu
+def test_gpu_eigenvalues_of_the_laplacian():
+    """The heat equation on the unit square with u = 0 on the boundary: the
+    leading eigenvalues of (-J) v = lambda M v approximate -pi^2 (k^2 + l^2)
+    (-2 pi^2, -5 pi^2 twice, -8 pi^2).  Q2 elements with the 3 x 3 Gauss
+    rule are the exact tensor product of 1D P2 ones (stiffness
+    (1/3h)[7 -8 1; -8 16 -8; 1 -8 7], mass (h/30)[4 2 -1; 2 16 2; -1 2 4]),
+    so the discrete eigenvalues are exactly -(mu_k + mu_l) of the 1D P2
+    problem: checked to 1e-9, and to the continuous ones within 5e-5."""
+    import scipy.linalg as sla
+    from pyoomph_gb300 import DiffusionEquation, DirichletBC, Problem, RectangularQuadMesh
+    P = Problem()
+    P += RectangularQuadMesh(N=16)
+    P += (DiffusionEquation() + DirichletBC(u=0.0) @ ["left", "right", "top", "bottom"]) @ "domain"
+    P.initialise()
+    ev, vec = P.solve_eigenproblem(4, shift=0.0)
+    N, h = 16, 1.0 / 16
+    Ke = np.array([[7, -8, 1], [-8, 16, -8], [1, -8, 7]]) / (3 * h)
+    Me = np.array([[4, 2, -1], [2, 16, 2], [-1, 2, 4]]) * h / 30
+    K1, M1 = np.zeros((2 * N + 1, 2 * N + 1)), np.zeros((2 * N + 1, 2 * N + 1))
+    for e in range(N):
+        ix = np.ix_([2 * e, 2 * e + 1, 2 * e + 2], [2 * e, 2 * e + 1, 2 * e + 2])
+        K1[ix] += Ke
+        M1[ix] += Me
+    mu = np.sort(sla.eigh(K1[1:-1, 1:-1], M1[1:-1, 1:-1], eigvals_only=True))
+    discrete = -np.array([mu[0] + mu[0], mu[0] + mu[1], mu[0] + mu[1], mu[1] + mu[1]])
+    assert np.max(np.abs(ev.real - discrete) / np.abs(discrete)) < 1e-9, (ev, discrete)
+    exact = -np.pi ** 2 * np.array([2.0, 5.0, 5.0, 8.0])
+    assert np.max(np.abs(ev.real - exact) / np.abs(exact)) < 5e-5, ev
+    assert np.max(np.abs(ev.imag)) < 1e-8
+    assert vec.shape == (4, P.n_dof) and np.array_equal(P.get_last_eigenvalues(), ev)
