@@ -133,6 +133,34 @@ def solve_generalized_eigenproblem(J, M, n: int, shift=0.0, sort: bool = True, w
     return ev, vec.T
 
 
+class _ProblemContinuationOps:
+    """The continuation's operations on a Problem (device assembly)."""
+
+    def __init__(self, P: "Problem", name: str):
+        self.P, self.name = P, name
+        self.n_dof = P.n_dof
+        self.k = P.param_names.index(name)
+
+    def get_dofs(self):
+        return self.P.get_dofs()
+
+    def set_dofs(self, x):
+        self.P.set_dofs(x)
+
+    def get_parameter(self):
+        return float(self.P.params[self.k])
+
+    def set_parameter(self, v):
+        self.P.set_parameters(**{self.name: float(v)})
+
+    def residual_and_jacobian(self):
+        R, J = self.P.get_jacobian()
+        return np.asarray(R, dtype=np.float64), J
+
+    def parameter_derivative(self):
+        return self.P.get_parameter_derivative(self.name)
+
+
 class NewtonSolverError(RuntimeError):
     """Raised when Newton diverges or exceeds its iteration cap
     (oomph's NewtonSolverError, problem.cc:9298)."""
@@ -806,6 +834,38 @@ class Problem:
         rp, ci = self.pattern()
         return sps.csr_matrix((M[:self.nnz].cpu().numpy().astype(np.float64), ci, rp),
                               shape=(self.n_dof, self.n_dof))
+
+    def arclength_continuation(self, parameter: str, step: float, *, max_ds: Optional[float] = None,
+                               max_newton_iterations: Optional[int] = None,
+                               newton_solver_tolerance: Optional[float] = None,
+                               min_ds: Optional[float] = None) -> float:
+        """One pseudo-arclength step of (signed) length `step` in a global
+        parameter from the current solution (pyoomph's
+        Problem.arclength_continuation, problem.py:3508; the algorithm is in
+        continuation.py).  R and J come from the device assembly, dR/dp from
+        the kernels' parameter derivative.  Consecutive calls with the same
+        parameter continue along the path (the tangent is kept); returns the
+        suggested next step.  reset_arc_length_parameters() forgets the
+        path."""
+        from .continuation import arclength_step
+        self.initialise()
+        if int(self.replicas) != 1:
+            raise NotImplementedError("continuation of replicated problems")
+        if parameter not in self.param_names:
+            raise KeyError(f"unknown parameter {parameter!r}; have {self.param_names}")
+        st = self._arclength if getattr(self, "_arclength_param", None) == parameter else None
+        new, nds = arclength_step(
+            _ProblemContinuationOps(self, parameter), st, float(step),
+            tol=self.newton_solver_tolerance if newton_solver_tolerance is None else newton_solver_tolerance,
+            max_newton_iterations=self.max_newton_iterations if max_newton_iterations is None
+            else max_newton_iterations,
+            min_ds=1e-8 if min_ds is None else min_ds, max_ds=max_ds)
+        self._arclength, self._arclength_param = new, parameter
+        self.assemble_device(with_jacobian=False)      # nodal values at the new point
+        return nds
+
+    def reset_arc_length_parameters(self) -> None:
+        self._arclength = self._arclength_param = None
 
     def solve_eigenproblem(self, n: int, shift=0.0, sort: bool = True, which: str = "LM", v0=None,
                            target=None):
