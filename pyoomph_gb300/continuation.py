@@ -129,9 +129,29 @@ def arclength_step(ops: ContinuationOps, state: Optional[ContinuationState], ds:
     return new, nds
 
 
-def fold_from_three(s, p):
-    """Parameter at the turning point of the parabola through three points
-    (s_i, p_i) of the path (s the arclength)."""
-    A = np.vstack([np.asarray(s) ** 2, np.asarray(s), np.ones(3)]).T
-    a, b, c = np.linalg.solve(A, np.asarray(p, dtype=np.float64))
-    return c - b * b / (4.0 * a)
+def locate_fold(ops: ContinuationOps, before: ContinuationState, ds: float, *, rel_tol: float = 1e-6,
+                **step_kw) -> ContinuationState:
+    """The turning point between `before` and the point a step ds from it,
+    whose tangents' parameter components p' differ in sign: bisection on
+    the step length from `before`, each trial a full corrector solve, until
+    the bracket is rel_tol * |ds| wide.  The parameter is stationary there,
+    so its error is quadratic in the bracket.  Leaves ops at the returned
+    point (the last trial on the near side)."""
+    if before.dp == 0.0:
+        return before
+    lo, hi = 0.0, float(ds)
+    best = before
+    step_kw = dict(step_kw)
+    step_kw.pop("max_ds", None)
+    while abs(hi - lo) > rel_tol * abs(ds):
+        mid = 0.5 * (lo + hi)
+        st, _ = arclength_step(ops, before, mid, **step_kw)
+        if st.ds != mid:               # the step was shortened to converge
+            mid = st.ds
+        if np.sign(st.dp) == np.sign(before.dp):
+            lo, best = mid, st
+        else:
+            hi = mid
+    ops.set_dofs(best.u0)
+    ops.set_parameter(best.p0)
+    return best

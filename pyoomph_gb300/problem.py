@@ -854,6 +854,7 @@ class Problem:
         if parameter not in self.param_names:
             raise KeyError(f"unknown parameter {parameter!r}; have {self.param_names}")
         st = self._arclength if getattr(self, "_arclength_param", None) == parameter else None
+        self._arclength_prev = st
         new, nds = arclength_step(
             _ProblemContinuationOps(self, parameter), st, float(step),
             tol=self.newton_solver_tolerance if newton_solver_tolerance is None else newton_solver_tolerance,
@@ -865,7 +866,21 @@ class Problem:
         return nds
 
     def reset_arc_length_parameters(self) -> None:
-        self._arclength = self._arclength_param = None
+        self._arclength = self._arclength_param = self._arclength_prev = None
+
+    def locate_fold(self, rel_tol: float = 1e-6) -> float:
+        """After an arclength step that passed a fold (the parameter turned):
+        bisect that step down to the turning point, leave the problem there
+        and return the parameter's value (continuation.locate_fold)."""
+        from .continuation import locate_fold
+        prev, last = getattr(self, "_arclength_prev", None), getattr(self, "_arclength", None)
+        if prev is None or last is None or np.sign(prev.dp) == np.sign(last.dp):
+            raise RuntimeError("the last arclength step did not pass a fold")
+        st = locate_fold(_ProblemContinuationOps(self, self._arclength_param), prev, last.ds, rel_tol=rel_tol,
+                         tol=self.newton_solver_tolerance, max_newton_iterations=self.max_newton_iterations)
+        self._arclength = st
+        self.assemble_device(with_jacobian=False)
+        return st.p0
 
     def solve_eigenproblem(self, n: int, shift=0.0, sort: bool = True, which: str = "LM", v0=None,
                            target=None):

@@ -7,23 +7,17 @@ dR/dlambda (the kernels' parameter derivative, flag 3)."""
 import numpy as np
 import pytest
 
-from pyoomph_gb300.continuation import ContinuationError, arclength_step, fold_from_three
+from pyoomph_gb300.continuation import ContinuationError, arclength_step, locate_fold
 
 
-def _follow_to_fold(step_fn, p_of, max_steps=60):
-    """Step until the parameter turns; the fold from a parabola through the
-    last three points (s, p)."""
-    s, pts, state = 0.0, [], None
+def _follow_to_fold(step_fn, max_steps=60):
+    """Step until the parameter turns; returns the states before and after."""
+    prev, state = None, None
     for _ in range(max_steps):
-        state = step_fn(state)
-        s += state.ds
-        pts.append((s, p_of(state)))
+        prev, state = state, step_fn(state)
         if state.dp < 0.0:
-            break
-    else:
-        raise AssertionError("no fold reached")
-    (s0, p0), (s1, p1), (s2, p2) = pts[-3:]
-    return fold_from_three([s0, s1, s2], [p0, p1, p2]), pts
+            return prev, state
+    raise AssertionError("no fold reached")
 
 
 class _Bratu1D:
@@ -58,29 +52,31 @@ class _Bratu1D:
         return -np.exp(self.u)
 
 
-def test_continuation_rounds_the_fold_of_the_1d_bratu_problem():
+@pytest.mark.parametrize("max_ds", [0.25, 0.5, 1.0])
+def test_continuation_rounds_the_fold_of_the_1d_bratu_problem(max_ds):
+    """Finite differences, 200 points: the discrete fold, 3.51378547, lies
+    4.5e-5 below the continuum's 3.513830719 (second order in h); located
+    by bisection to 1e-8 whatever the step sizes that reached it."""
     ops = _Bratu1D(200)
     ds = [0.5]
 
     def step(state):
-        new, ds[0] = arclength_step(ops, state, ds[0], tol=1e-10, max_ds=0.5)
-        step.last = new
+        new, ds[0] = arclength_step(ops, state, ds[0], tol=1e-10, max_ds=max_ds)
         return new
 
-    lam_fold, pts = _follow_to_fold(step, lambda st: st.p0)
-    print("1D Bratu fold", lam_fold, "after", len(pts), "steps")
-    assert abs(lam_fold - 3.513830719) < 2e-3, (lam_fold, pts[-4:])
-    # every point on the path solves R = 0
-    R, _ = ops.residual_and_jacobian()
-    assert np.max(np.abs(R)) < 1e-8
+    before, after = _follow_to_fold(step)
     # beyond the fold the path continues on the upper branch: lambda falls, u grows
-    lam, umax = [pts[-1][1]], [np.max(ops.get_dofs())]
-    st = step.last
+    lam, umax, st = [after.p0], [np.max(after.u0)], after
     for _ in range(3):
-        st, ds[0] = arclength_step(ops, st, ds[0], tol=1e-10, max_ds=0.5)
+        st, ds[0] = arclength_step(ops, st, ds[0], tol=1e-10, max_ds=max_ds)
         lam.append(st.p0)
         umax.append(np.max(st.u0))
     assert np.all(np.diff(lam) < 0) and np.all(np.diff(umax) > 0), (lam, umax)
+    fold = locate_fold(ops, before, after.ds, tol=1e-10)
+    print("1D Bratu fold", fold.p0, "max_ds", max_ds)
+    assert abs(fold.p0 - 3.51378547) < 1e-8 and 3e-5 < 3.513830719 - fold.p0 < 6e-5
+    R, _ = ops.residual_and_jacobian()
+    assert np.max(np.abs(R)) < 1e-8 and abs(fold.dp) < 1e-2
 
 
 def test_failed_step_restores_the_last_point():
@@ -116,6 +112,8 @@ def test_gpu_continuation_finds_the_fold_of_the_2d_bratu_problem():
         ds[0] = P.arclength_continuation("lambda", ds[0], max_ds=0.5)
         return P._arclength
 
-    lam_fold, pts = _follow_to_fold(step, lambda st: st.p0)
-    assert abs(lam_fold - 6.808124) < 2e-3, (lam_fold, pts[-4:])
+    _follow_to_fold(step)
+    lam_fold = P.locate_fold()
+    print("2D Bratu fold", lam_fold)
+    assert abs(lam_fold - 6.808124) < 1e-3, lam_fold
     assert np.max(np.abs(P.get_residuals())) < 1e-9
