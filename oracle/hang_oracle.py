@@ -96,12 +96,114 @@ def refine(m: O.Mesh, chosen) -> Tuple[np.ndarray, np.ndarray, Dict[int, List[Tu
     return x, conn, hang, on_b
 
 
+def _shape(s0: float, s1: float) -> np.ndarray:
+    psi = np.zeros(9)
+    dps = np.zeros((9, 2))
+    O.lib().ofe_shape_c2(O.Q2_QUAD, O._ptr(np.array([s0, s1, 0.0])), O._ptr(psi), O._ptr(dps))
+    return psi
+
+
+def _complete(hang: Dict[int, List[Tuple[int, float]]], min_weight: float = 1e-8):
+    """oomph-lib's complete_hanging_nodes (refineable_mesh.cc:2214-2320) as
+    written there: nodes in order; for each hanging node the recursive list
+    of (master, weight) -- a hanging master contributes its own masters'
+    list, each weight then multiplied by the master's weight -- built on
+    the hang infos as completed so far, merged in a map (|w| <= min_weight
+    dropped, repeats summed) that replaces the node's hang info.  The map's
+    order is the node number here (oomph's is the node's address)."""
+    hang = {k: list(v) for k, v in hang.items()}
+
+    def rec(node, masters, weights):
+        if node in hang:
+            for m, w in hang[node]:
+                first = len(masters)
+                rec(m, masters, weights)
+                for k in range(first, len(masters)):
+                    weights[k] = w * weights[k]
+        else:
+            masters.append(node)
+            weights.append(1.0)
+
+    for node in sorted(hang):
+        masters: List[int] = []
+        weights: List[float] = []
+        rec(node, masters, weights)
+        merged: Dict[int, float] = {}
+        for m, w in zip(masters, weights):
+            if abs(w) > min_weight:
+                merged[m] = merged.get(m, 0.0) + w
+        hang[node] = [(m, merged[m]) for m in sorted(merged)]
+    return hang
+
+
+def refine_levels(m: O.Mesh, chosen, max_level: int):
+    """(x, conn, hang, on_boundary) of a quadtree refinement to several
+    levels: an element (a map X(s) of the reference square) is split into
+    its sons SW, SE, NW, NE -- son maps composed with the parent's -- while
+    ``chosen(cx, cy, level)`` holds at its centre node and level <
+    max_level; leaves in tree order; nodes found by position and numbered
+    by first encounter over the leaves' local nodes (oomph-lib's
+    Mesh::reorder_nodes, mesh.cc:541-640, called after every adapt);
+    hanging nodes found geometrically on the leaves' edges and completed
+    recursively (``_complete``)."""
+    leaves = []   # per leaf: its 9 node positions
+
+    def split(nodes9: np.ndarray, level: int):
+        c = nodes9[4]
+        if level < max_level and chosen(c[0], c[1], level):
+            for (sx0, sy0) in ((-1.0, -1.0), (0.0, -1.0), (-1.0, 0.0), (0.0, 0.0)):
+                son = np.array([_shape(sx0 + 0.5 * i, sy0 + 0.5 * j) @ nodes9 for j in range(3) for i in range(3)])
+                split(son, level + 1)
+        else:
+            leaves.append(nodes9)
+
+    for e in range(m.conn.shape[0]):
+        split(m.x[m.conn[e]].copy(), 0)
+    ids: Dict[Tuple[float, float], int] = {}
+    x: List[np.ndarray] = []
+    conn = []
+    for nodes9 in leaves:
+        row = []
+        for p in nodes9:
+            k = (round(float(p[0]), 12), round(float(p[1]), 12))
+            if k not in ids:
+                ids[k] = len(x)
+                x.append(p)
+            row.append(ids[k])
+        conn.append(row)
+    x = np.array(x)
+    conn = np.array(conn, dtype=np.int32)
+    hang: Dict[int, List[Tuple[int, float]]] = {}
+    edges = [(c[a], c[mid], c[b]) for c in conn for a, mid, b in ((0, 1, 2), (6, 7, 8), (0, 3, 6), (2, 5, 8))]
+    for k in range(x.shape[0]):
+        for a, mid, b in edges:
+            if k in (a, mid, b):
+                continue
+            pa, pb = x[a], x[b]
+            t = pb - pa
+            u = np.dot(x[k] - pa, t) / np.dot(t, t)
+            if 0.0 < u < 1.0 and np.linalg.norm(pa + u * t - x[k]) < 1e-12:
+                s = np.round((2.0 * u - 1.0) * 2.0 ** 20) / 2.0 ** 20   # dyadic, as the tree's coordinates
+                w = (0.5 * s * (s - 1.0), 1.0 - s * s, 0.5 * s * (s + 1.0))
+                hang[k] = [(a, w[0]), (mid, w[1]), (b, w[2])]
+                break
+    hang = _complete(hang)
+    lo, hi = x.min(axis=0), x.max(axis=0)
+    on_b = (np.abs(x[:, 0] - lo[0]) < 1e-12) | (np.abs(x[:, 0] - hi[0]) < 1e-12) | \
+           (np.abs(x[:, 1] - lo[1]) < 1e-12) | (np.abs(x[:, 1] - hi[1]) < 1e-12)
+    return x, conn, hang, on_b
+
+
 class HangProblem:
     """Scalar Q2 problem (Poisson / nonlinear diffusion) on a refined mesh,
-    u = 0 on the outer boundary."""
+    u = 0 on the outer boundary (one level: ``refine``; with max_level:
+    ``refine_levels``)."""
 
-    def __init__(self, N: int, chosen, gaussians: np.ndarray, eq: int = O.EQ_POISSON):
-        self.x, self.conn, self.hang, on_b = refine(O.mesh(O.Q2_QUAD, N, N), chosen)
+    def __init__(self, N: int, chosen, gaussians: np.ndarray, eq: int = O.EQ_POISSON, max_level=None):
+        if max_level is None:
+            self.x, self.conn, self.hang, on_b = refine(O.mesh(O.Q2_QUAD, N, N), chosen)
+        else:
+            self.x, self.conn, self.hang, on_b = refine_levels(O.mesh(O.Q2_QUAD, N, N), chosen, max_level)
         n = self.x.shape[0]
         self.eq = eq
         self.params = O.gaussian_params(gaussians)

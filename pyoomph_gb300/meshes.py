@@ -325,3 +325,155 @@ class RefinedQuadMesh(MeshTemplate):
         md = MeshData(ELEMENT_TYPES["Q2_QUAD"], x, np.array(conn, dtype=np.int32), is_vertex, b, ql)
         md.hang = {k: hang[k] for k in sorted(hang)}
         return md
+
+
+def complete_hanging(hang: Dict[int, List[Tuple[int, float]]], min_weight: float = 1e-8
+                     ) -> Dict[int, List[Tuple[int, float]]]:
+    """Hang infos whose masters do not hang (oomph-lib's
+    TreeBasedRefineableMeshBase::complete_hanging_nodes, refineable_mesh.cc:
+    2214-2320): a master that hangs is replaced by its own masters, weights
+    multiplied, recursively; then the list is merged -- entries with
+    |weight| <= min_weight dropped, repeated masters summed.  oomph merges in
+    a map keyed by the node's address; here the masters are ordered by node
+    number (the nodes' order of creation, which addresses follow in a
+    fresh allocation)."""
+    def expand(n: int, w: float, out: List[Tuple[int, float]], depth: int = 0) -> None:
+        if depth > 64:
+            raise ValueError("cyclic hanging-node dependencies")
+        if n in hang:
+            for m, wm in hang[n]:
+                expand(m, w * wm, out, depth + 1)
+        else:
+            out.append((n, w))
+
+    done: Dict[int, List[Tuple[int, float]]] = {}
+    for h in sorted(hang):
+        lst: List[Tuple[int, float]] = []
+        for m, w in hang[h]:
+            expand(m, w, lst)
+        merged: Dict[int, float] = {}
+        for m, w in lst:
+            if abs(w) > min_weight:
+                merged[m] = merged.get(m, 0.0) + w
+        done[h] = [(m, merged[m]) for m in sorted(merged)]
+    return done
+
+
+class AdaptiveQuadMesh(MeshTemplate):
+    """A RectangularQuadMesh of Q2 quads refined by quadtrees to several
+    levels: an element at level l (the base elements at 0) is split into its
+    four sons SW, SE, NW, NE while ``refine(centre_x, centre_y, l)`` holds
+    and l < max_level.  No 2:1 balance is imposed.
+
+    As oomph-lib's refineable meshes after ``adapt``: the elements are the
+    leaves of the forest in tree order (base elements in order, sons in
+    order, depth first); the nodes are numbered by first encounter over the
+    elements' local nodes (``Mesh::reorder_nodes``, mesh.cc:517-640); a node
+    strictly inside an edge of a coarser neighbour (and not one of its
+    nodes) hangs on that edge's three nodes with the 1D quadratic Lagrange
+    weights at its position (``RefineableQElement<2>::setup_hang_for_value``);
+    masters that hang themselves are resolved recursively
+    (``complete_hanging``).  Positions are the base element's isoparametric
+    map at the node's local coordinate."""
+
+    def __init__(self, *, N: int = 8, refine=None, max_level: int = 2, size: float = 1.0, name: str = "domain",
+                 transform=None):
+        self.N = int(N)
+        self.refine = refine or (lambda x, y, level: x < 0.5 ** (level + 1))
+        self.max_level = int(max_level)
+        if self.max_level < 0 or self.max_level > 12:
+            raise ValueError("max_level must be in 0..12")
+        self.size = float(size)
+        self.domain_name = name
+        self.transform = None
+        self._post = transform
+
+    def generate(self) -> MeshData:
+        md = self._generate()
+        if self._post is not None:
+            md.x = np.ascontiguousarray(self._post(md.x.copy()), dtype=np.float64)
+        return md
+
+    def _generate(self) -> MeshData:
+        from .spaces import Q2_QUAD
+        N, L = self.N, self.max_level
+        S = 2 ** (L + 1)                     # fine-lattice units per base cell (node spacing at level L)
+        base = RectangularQuadMesh(N=N, size=self.size).generate()
+        conn0, x0, lat0 = base.conn, base.x, base.lattice
+        hcell = self.size / N
+        leaves: List[Tuple[int, int, int, int]] = []   # (base element, qx0, qy0, span)
+
+        def split(e: int, qx: int, qy: int, span: int, level: int) -> None:
+            cx = (qx + 0.5 * span) * hcell / S
+            cy = (qy + 0.5 * span) * hcell / S
+            if level < L and bool(self.refine(cx, cy, level)):
+                h = span // 2
+                for dy, dx in ((0, 0), (0, 1), (1, 0), (1, 1)):          # SW, SE, NW, NE
+                    split(e, qx + dx * h, qy + dy * h, h, level + 1)
+            else:
+                leaves.append((e, qx, qy, span))
+
+        for e in range(conn0.shape[0]):
+            ix, iy = int(lat0[conn0[e, 0]][0]) // 2, int(lat0[conn0[e, 0]][1]) // 2
+            split(e, ix * S, iy * S, S, 0)
+        Q = N * S + 1
+        key = lambda qx, qy: int(qx) + Q * int(qy)
+        node_of: Dict[int, int] = {}
+        xs: List[np.ndarray] = []
+        qlat: List[Tuple[int, int]] = []
+        conn: List[List[int]] = []
+        for e, qx0, qy0, span in leaves:
+            Xe = x0[conn0[e]]
+            bx, by = (qx0 // S) * S, (qy0 // S) * S
+            h = span // 2
+            child = []
+            for j in range(3):
+                for i in range(3):
+                    qx, qy = qx0 + i * h, qy0 + j * h
+                    k = key(qx, qy)
+                    if k not in node_of:
+                        s = np.array([2.0 * (qx - bx) / S - 1.0, 2.0 * (qy - by) / S - 1.0])
+                        psi, _ = Q2_QUAD.shape_c2(s)
+                        node_of[k] = len(xs)
+                        xs.append(psi @ Xe)
+                        qlat.append((qx, qy))
+                    child.append(node_of[k])
+            conn.append(child)
+        x = np.array(xs)
+        ql = np.array(qlat, dtype=np.int64)
+        n = x.shape[0]
+        # leaf edges by line: horizontal (y, x_start, x_end), vertical (x, y_start, y_end)
+        hor: Dict[int, List[Tuple[int, int]]] = {}
+        ver: Dict[int, List[Tuple[int, int]]] = {}
+        for _, qx0, qy0, span in leaves:
+            for y in (qy0, qy0 + span):
+                hor.setdefault(y, []).append((qx0, qx0 + span))
+            for xq in (qx0, qx0 + span):
+                ver.setdefault(xq, []).append((qy0, qy0 + span))
+        hang: Dict[int, List[Tuple[int, float]]] = {}
+        for k in range(n):
+            qx, qy = int(ql[k, 0]), int(ql[k, 1])
+            found = None
+            for a, b in hor.get(qy, ()):
+                if a < qx < b and 2 * qx != a + b:
+                    found = ((a, qy), ((a + b) // 2, qy), (b, qy), 2.0 * (qx - a) / (b - a) - 1.0)
+                    break
+            if found is None:
+                for a, b in ver.get(qx, ()):
+                    if a < qy < b and 2 * qy != a + b:
+                        found = ((qx, a), (qx, (a + b) // 2), (qx, b), 2.0 * (qy - a) / (b - a) - 1.0)
+                        break
+            if found is not None:
+                pa, pm, pb, s = found
+                w = (0.5 * s * (s - 1.0), 1.0 - s * s, 0.5 * s * (s + 1.0))
+                hang[k] = [(node_of[key(*pa)], w[0]), (node_of[key(*pm)], w[1]), (node_of[key(*pb)], w[2])]
+        hang = complete_hanging(hang)
+        is_vertex = np.zeros(n, dtype=bool)
+        for c in conn:
+            for s_ in (0, 2, 6, 8):
+                is_vertex[c[s_]] = True
+        top = N * S
+        b = {"left": ql[:, 0] == 0, "right": ql[:, 0] == top, "bottom": ql[:, 1] == 0, "top": ql[:, 1] == top}
+        md = MeshData(ELEMENT_TYPES["Q2_QUAD"], x, np.array(conn, dtype=np.int32), is_vertex, b, ql)
+        md.hang = hang
+        return md

@@ -7,7 +7,7 @@ import pytest
 import hang_oracle as H
 from pyoomph_gb300 import _native as N
 from pyoomph_gb300.equations import DirichletBC, NonlinearDiffusionEquation, PoissonEquation
-from pyoomph_gb300.meshes import RefinedQuadMesh
+from pyoomph_gb300.meshes import AdaptiveQuadMesh, RefinedQuadMesh
 from pyoomph_gb300.problem import Problem
 from pyoomph_gb300.workloads import draw_gaussians
 
@@ -24,6 +24,66 @@ def _problem(n, region, eq="poisson", seed=5, prec="fp64"):
     P += (E(source=g) + DirichletBC(u=0.0) @ ["left", "right", "top", "bottom"]) @ "domain"
     HP = H.HangProblem(n, REGIONS[region], g, eq=H.O.EQ_POISSON if eq == "poisson" else H.O.EQ_NONLINEAR_DIFFUSION)
     return P, HP
+
+
+def _around(px, py, n):
+    """Refine the cells that contain (px, py), at every level."""
+    return lambda x, y, level: abs(x - px) < 0.5 / n / 2 ** level and abs(y - py) < 0.5 / n / 2 ** level
+
+
+# multi-level refinements without 2:1 balance: "point" refines towards a
+# point just inside a base-cell corner, so that three levels meet and some
+# masters hang themselves (completed recursively)
+LEVELS = {"point": (4, lambda n: _around(0.26, 0.26, n), 4),
+          "ring": (4, lambda n: (lambda x, y, l: abs(np.hypot(x - 0.5, y - 0.5) - 0.3) < 0.2 / 2 ** l), 3),
+          "two_points": (6, lambda n: (lambda x, y, l: _around(0.2, 0.7, n)(x, y, l) or _around(0.55, 0.3, n)(x, y, l)), 3)}
+
+
+def _problem_levels(case, eq="poisson", seed=5, prec="fp64"):
+    n, mk, L = LEVELS[case]
+    g = draw_gaussians(seed, 8, 2)
+    P = Problem()
+    P.jacobian_precision = prec
+    P += AdaptiveQuadMesh(N=n, refine=mk(n), max_level=L)
+    E = PoissonEquation if eq == "poisson" else NonlinearDiffusionEquation
+    P += (E(source=g) + DirichletBC(u=0.0) @ ["left", "right", "top", "bottom"]) @ "domain"
+    HP = H.HangProblem(n, mk(n), g, eq=H.O.EQ_POISSON if eq == "poisson" else H.O.EQ_NONLINEAR_DIFFUSION,
+                       max_level=L)
+    return P, HP
+
+
+@pytest.mark.parametrize("case", list(LEVELS))
+def test_multilevel_mesh_numbering_and_pattern_match_the_oracle(case):
+    """Several refinement levels: leaves in tree order, first-encounter
+    node numbering (oomph's reorder_nodes), hang infos completed through
+    hanging masters (oomph's complete_hanging_nodes), equation numbers and
+    the weighted CSR pattern, all against the oracle's geometric
+    restatement."""
+    P, HP = _problem_levels(case)
+    P.lower()
+    assert np.array_equal(P.mesh.conn, HP.conn)
+    assert np.max(np.abs(P.mesh.x - HP.x)) <= 1e-15
+    assert P.mesh.hang == HP.hang and len(HP.hang) > 0
+    assert np.array_equal(P.eqn[:, 0], HP.eqn)
+    rp, ci = P.host_pattern()
+    _, orp, oci, _ = HP.assemble()
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    if case == "point":
+        assert max(len(v) for v in HP.hang.values()) == 5       # masters of masters
+    for h, ms in P.mesh.hang.items():                               # linear fields are reproduced
+        assert abs(sum(w for _, w in ms) - 1.0) < 1e-14
+        assert np.allclose(sum(w * P.mesh.x[m] for m, w in ms), P.mesh.x[h], atol=1e-14, rtol=0)
+
+
+def test_completion_restates_oomph():
+    """complete_hanging against the oracle's literal restatement on a
+    hand-made chain: c hangs on (a, b), b hangs on (a, d); weights multiply,
+    repeats add, zero weights drop."""
+    from pyoomph_gb300.meshes import complete_hanging
+    hang = {2: [(0, 0.25), (1, 0.75)], 1: [(0, 0.5), (3, 0.5)], 5: [(4, 1.0), (2, 0.0)]}
+    got = complete_hanging(hang)
+    assert got == H._complete(hang)
+    assert got[2] == [(0, 0.625), (3, 0.375)] and got[1] == [(0, 0.5), (3, 0.5)] and got[5] == [(4, 1.0)]
 
 
 @pytest.mark.parametrize("region", list(REGIONS))
@@ -121,3 +181,36 @@ def test_refinement_improves_a_manufactured_solution():
         errs[name] = (tot, left)
     assert errs["refined"][0] < errs["coarse"][0]
     assert errs["refined"][1] < 0.25 * errs["coarse"][1]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case,eq,prec", [("point", "poisson", "fp64"), ("two_points", "nldiff", "fp64"),
+                                          ("ring", "nldiff", "fp32")])
+def test_gpu_multilevel_assembly_matches_the_oracle(case, eq, prec):
+    """Several levels, masters completed through hanging masters: R, the
+    CSR pattern and J from the device against the oracle's hanging-node
+    assembly."""
+    P, HP = _problem_levels(case, eq=eq, prec=prec)
+    P.initialise()
+    d = np.random.default_rng(4).normal(0.0, 0.3, P.n_dof)
+    P.set_dofs(d)
+    R, J = P.get_jacobian()
+    HP.set_dofs(d)
+    Ro, orp, oci, ov = HP.assemble()
+    rp, ci = P.pattern()
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    assert np.max(np.abs(R - Ro)) <= 1e-12 * np.max(np.abs(Ro))
+    tol = 1e-12 if prec == "fp64" else 1e-5
+    assert np.max(np.abs(J.data - ov)) <= tol * np.max(np.abs(ov))
+
+
+@pytest.mark.gpu
+def test_gpu_newton_on_a_multilevel_mesh_matches_the_oracle():
+    P, HP = _problem_levels("two_points", eq="nldiff")
+    P.newton_solver_tolerance = 1e-11
+    P.solve()
+    x = HP.newton(tol=1e-11)
+    assert np.max(np.abs(P.get_dofs() - x)) <= 1e-10 * max(1.0, np.max(np.abs(x)))
+    v = P.get_values()[:, 0]
+    for h, ms in P.mesh.hang.items():
+        assert abs(v[h] - sum(w * v[m] for m, w in ms)) < 1e-14
