@@ -71,6 +71,7 @@ class GB300Assembler(CustomAssemblyBase):
     def __init__(self, engine) -> None:
         super().__init__()
         self.engine = engine
+        self._last_J = None
 
     def initialize(self) -> None:
         self.engine.initialise()
@@ -119,4 +120,18 @@ class GB300Assembler(CustomAssemblyBase):
         J.data = J.data.astype(np.float64, copy=False)
         J.indptr = J.indptr.astype(np.int32, copy=False)
         J.indices = J.indices.astype(np.int32, copy=False)
+        self._last_J = J
         return np.ascontiguousarray(R, dtype=np.float64), J
+
+    def get_last_mass_and_jacobian_matrices(self):
+        """(M, J): J as returned by the last Jacobian assembly, M = dR/d(du/dt)
+        from the engine's mass-matrix assembly at the current state
+        (pyoomph's hook, assembly.py:87, read by utils/lyapunov.py:83).
+        (None, None) before any Jacobian or for a steady engine: the caller
+        then assembles them itself."""
+        if self._last_J is None or not getattr(self.engine, "is_transient", False):
+            return None, None
+        return self.engine.get_mass_matrix(), self._last_J
+
+    def invalidate_cache(self) -> None:
+        self._last_J = None

@@ -256,3 +256,39 @@ def test_gpu_eigenvalues_of_the_laplacian():
     assert np.max(np.abs(ev.real - exact) / np.abs(exact)) < 5e-5, ev
     assert np.max(np.abs(ev.imag)) < 1e-8
     assert vec.shape == (4, P.n_dof) and np.array_equal(P.get_last_eigenvalues(), ev)
+
+
+def test_assembler_last_mass_and_jacobian_host_logic():
+    """GB300Assembler.get_last_mass_and_jacobian_matrices (pyoomph's hook,
+    read by its Lyapunov-exponent tool): nothing before a Jacobian or for a
+    steady engine; the last J and the engine's mass matrix otherwise."""
+    import scipy.sparse as sps
+    from pyoomph_gb300 import GB300Assembler
+
+    class Engine:
+        is_transient = False
+        n_dof = 2
+
+        def initialise(self):
+            pass
+
+        def set_dofs(self, x):
+            pass
+
+        def get_jacobian(self):
+            return np.zeros(2), sps.csr_matrix(np.array([[2.0, 0.0], [1.0, 3.0]], dtype=np.float32))
+
+        def get_mass_matrix(self):
+            return sps.identity(2, format="csr")
+
+    eng = Engine()
+    asm = GB300Assembler(eng)
+    assert asm.get_last_mass_and_jacobian_matrices() == (None, None)
+    _, J = asm.get_residuals_and_jacobian(True)
+    assert J.data.dtype == np.float64 and J.indptr.dtype == np.int32
+    assert asm.get_last_mass_and_jacobian_matrices() == (None, None)      # steady engine
+    eng.is_transient = True
+    M, J2 = asm.get_last_mass_and_jacobian_matrices()
+    assert J2 is J and (M != sps.identity(2)).nnz == 0
+    asm.invalidate_cache()
+    assert asm.get_last_mass_and_jacobian_matrices() == (None, None)
