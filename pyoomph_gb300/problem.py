@@ -219,6 +219,7 @@ class Problem:
         # of pyoomph's generated code).  Switched on by the first
         # unsteady_newton_solve.
         self.transient = False
+        self.is_transient = False      # set by lower(): the lowered form keeps partial_t terms
         self.time = 0.0
         self.steps_done = 0
         self.dt_prev: Optional[float] = None
