@@ -70,12 +70,19 @@ def register_vector_field(name: str, comps: List[str]) -> None:
     REG.vector_fields[name] = comps
 
 
+TIME_PARAM = "_time"
+
+
 def var(name: str) -> Expr:
     """Field value (scalar symbol, or a column vector for a vector field).
-    ``mesh``/``coordinate``: the Eulerian position; ``lagrangian``: the
+    ``time``: the current time; ``mesh``/``coordinate``: the Eulerian position; ``lagrangian``: the
     reference position; ``normal``: the outward unit normal (interfaces)."""
     if name in REG.vector_fields:
         return sp.Matrix([REG.field(c) for c in REG.vector_fields[name]])
+    if name == "time":
+        # the time of the solve (t_{n+1} within a time step): a run-time
+        # parameter the time stepper sets
+        return parameter(TIME_PARAM)
     if name in ("coordinate", "mesh"):
         return sp.Matrix(X[:dimension()])
     if name == "lagrangian":

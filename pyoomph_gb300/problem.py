@@ -107,6 +107,23 @@ def nvtx_range(name: str):
     return contextlib.nullcontext()
 
 
+def _bc_takes_time(fn) -> bool:
+    import inspect
+    try:
+        return "t" in inspect.signature(fn).parameters
+    except (TypeError, ValueError):
+        return False
+
+
+def _bc_value(fn, x: np.ndarray, k: int, ncomp: int, t: float):
+    """A Dirichlet value function at nodes x [n, dim]: fn(x0, x1[, x2]) or,
+    time-dependent, fn(x0, x1[, x2], t=...); a vector field's function
+    returns one array per component."""
+    args = [x[:, d] for d in range(x.shape[1])]
+    v = fn(*args, t=t) if _bc_takes_time(fn) else fn(*args)
+    return v[k] if isinstance(v, (tuple, list)) and ncomp > 1 else v
+
+
 def solve_generalized_eigenproblem(J, M, n: int, shift=0.0, sort: bool = True, which: str = "LM", v0=None,
                                    target=None):
     """(-J) v = lambda M v for sparse J, M (host): all eigenpairs densely when
@@ -297,6 +314,8 @@ class Problem:
         # parameters referenced by the integrand, in a stable order
         used = sorted({s.name[2:] for s in (integrand.free_symbols if hasattr(integrand, "free_symbols") else [])
                        if s.name.startswith("P_")}, key=E.parameter_order_key)
+        if E.TIME_PARAM in used:
+            params[E.TIME_PARAM] = float(self.time)
         missing = [p for p in used if p not in params]
         if missing:
             raise RuntimeError(f"parameters without values: {missing}")
@@ -365,6 +384,7 @@ class Problem:
             present[:, f] = True if sp_ == "C2" else mesh.is_vertex
         pinned = np.zeros((n, nval), dtype=bool)
         values = np.zeros((n, nval))
+        self._timed_bcs = []     # (node mask, value index, callable, component, components) of f(x, ..., t=)
         for bc, where in bcs:
             if isinstance(bc, DirichletBC):
                 if where is None:
@@ -381,9 +401,9 @@ class Problem:
                         m = mask & present[:, f]
                         pinned[m, f] = True
                         if callable(val):
-                            v = val(*[mesh.x[m, d] for d in range(mesh.dim)])
-                            v = v[k] if isinstance(v, (tuple, list)) and len(names) > 1 else v
-                            values[m, f] = v
+                            values[m, f] = _bc_value(val, mesh.x[m], k, len(names), self.time)
+                            if _bc_takes_time(val):
+                                self._timed_bcs.append((m, f, val, k, len(names)))
                         elif val is not None:
                             vv = val[k] if isinstance(val, (tuple, list)) else val
                             values[m, f] = vv
@@ -794,11 +814,32 @@ class Problem:
             N.check(N.load().fe_problem_shift_history(self._h))   # both levels = the initial state
         w = bdf_weights(1 if self.steps_done == 0 else 2, dt, self.dt_prev)
         self.set_parameters(**dict(zip(BDF_PARAMS, w)))
+        self.set_time(self.time + dt)            # var("time") and timed boundary values at t_{n+1}
         hist = self.solve()
         self.steps_done += 1
         self.dt_prev = dt
-        self.time += dt
         return hist
+
+    def set_time(self, t: float) -> None:
+        """Set the current time: the parameter var("time") reads and the
+        Dirichlet values given as functions with a keyword ``t``
+        (re-evaluated at the pinned nodes and uploaded; the free values keep
+        the current dofs)."""
+        self.time = float(t)
+        if not self._initialised:
+            return
+        if E.TIME_PARAM in self.param_names:
+            self.set_parameters(**{E.TIME_PARAM: self.time})
+        if getattr(self, "_timed_bcs", None):
+            R = int(self.replicas)
+            n0 = self.mesh.n_nodes // R
+            vals = self._values0
+            for m, f, fn, k, ncomp in self._timed_bcs:
+                v = _bc_value(fn, self.mesh.x[:n0][m[:n0]], k, ncomp, self.time)
+                vals[:n0][m[:n0], f] = v
+                for r in range(1, R):
+                    vals[r * n0:(r + 1) * n0][m[:n0], f] = v
+            N.check(N.load().fe_problem_set_values(self._h, np.ascontiguousarray(vals).ctypes.data))
 
     def make_transient(self) -> None:
         """Keep the partial_t terms from now on.  An initialised problem is

@@ -292,3 +292,84 @@ def test_assembler_last_mass_and_jacobian_host_logic():
     assert J2 is J and (M != sps.identity(2)).nnz == 0
     asm.invalidate_cache()
     assert asm.get_last_mass_and_jacobian_matrices() == (None, None)
+
+
+def _time_form_problem(source):
+    from pyoomph_gb300 import DirichletBC, Equations, Problem, RectangularQuadMesh, grad, var_and_test, weak
+
+    class Heat(Equations):
+        def define_fields(self):
+            self.define_scalar_field("u", "C2")
+
+        def define_residuals(self):
+            u, v = var_and_test("u")
+            self.add_residual(weak(grad(u), grad(v)) - weak(source(), v))
+
+    P = Problem()
+    P += RectangularQuadMesh(N=3)
+    P += (Heat() + DirichletBC(u=0.0) @ ["left", "right"]) @ "domain"
+    return P
+
+
+def test_emulated_time_symbol_reads_the_time_parameter():
+    """var("time") is a run-time parameter: the kernel of a form with
+    sin(t) x y at t = 0.3 gives the residual of the form with the number
+    sin(0.3) in its place."""
+    import kernel_emulator as KE
+    import sympy as sp
+    from pyoomph_gb300 import expressions as E
+    from pyoomph_gb300 import var
+    Pt = _time_form_problem(lambda: sp.sin(var("time")) * E.X[0] * E.X[1])
+    Pt.time = 0.3
+    kt = Pt.lower()
+    assert Pt.param_names == ["_time"] and Pt.params[0] == 0.3
+    Pc = _time_form_problem(lambda: sp.Float(np.sin(0.3)) * E.X[0] * E.X[1])
+    kc = Pc.lower()
+    m = Pt.mesh
+    vals = Pt._values0 + np.random.default_rng(1).normal(0.0, 0.2, Pt._values0.shape)
+    rt, jt, st = KE.run(kt, m.x, m.conn, vals, Pt.params)
+    rc, jc, sc = KE.run(kc, m.x, m.conn, vals, np.zeros(1))
+    assert not st.any() and not sc.any()
+    assert np.max(np.abs(rt - rc)) <= 1e-14 * np.max(np.abs(rc)) and np.array_equal(jt, jc)
+    # another time, another source
+    p2 = Pt.params.copy()
+    p2[0] = 1.1
+    r2, _, _ = KE.run(kt, m.x, m.conn, vals, p2)
+    assert np.max(np.abs(r2 - rt)) > 1e-3
+
+
+def test_time_dependent_dirichlet_values(monkeypatch):
+    """Dirichlet values given as f(x, y, t=...) are evaluated at lowering
+    (at Problem.time) and again by set_time, which uploads the nodal
+    values; constant and time-independent values stay as they are."""
+    from pyoomph_gb300 import DirichletBC, PoissonEquation, Problem, RectangularQuadMesh
+    from pyoomph_gb300 import problem as PR
+    P = Problem()
+    P += RectangularQuadMesh(N=4)
+    P += (PoissonEquation() + DirichletBC(u=lambda x, y, t: np.sin(np.pi * x) * np.exp(-t)) @ "top" +
+          DirichletBC(u=lambda x, y: x) @ "bottom" + DirichletBC(u=2.0) @ "left") @ "domain"
+    P.time = 0.5
+    P.lower()
+    top = P.mesh.boundaries["top"] & ~P.mesh.boundaries["left"]
+    x = P.mesh.x
+    assert np.allclose(P._values0[top, 0], np.sin(np.pi * x[top, 0]) * np.exp(-0.5))
+    assert len(P._timed_bcs) == 1
+    uploads = []
+
+    class Lib:
+        def fe_problem_set_values(self, h, ptr):
+            uploads.append(np.ctypeslib.as_array((PR.ctypes.c_double * P._values0.size).from_address(ptr)).copy())
+            return 0
+
+    monkeypatch.setattr(PR.N, "load", lambda: Lib())
+    P._initialised, P._h = True, object()
+    P.set_time(1.25)
+    assert P.time == 1.25 and len(uploads) == 1
+    up = uploads[0].reshape(P._values0.shape)
+    assert np.allclose(up[top, 0], np.sin(np.pi * x[top, 0]) * np.exp(-1.25))
+    bottom = P.mesh.boundaries["bottom"] & ~P.mesh.boundaries["left"]
+    assert np.allclose(up[bottom, 0], x[bottom, 0])
+    b = P.mesh.boundaries
+    assert np.all(up[b["left"] & ~b["top"] & ~b["bottom"], 0] == 2.0)
+    assert np.array_equal(up[~top, 0], P._values0[~top, 0])       # only the timed values change
+    P._initialised, P._h = False, None
