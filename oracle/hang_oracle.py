@@ -17,12 +17,14 @@ Restates, independently of the package's lattice-based generator:
 * the element residuals/Jacobians of ``fe_oracle.c`` with the hanging values
   interpolated, assembled with oomph's hanging-node rule (each local equation
   of a hanging value adds, weighted, to its masters' equations, rows and
-  columns alike; ``jitbridge_hang.h`` master loops) in the vectors-of-pairs
-  order (element, local row, row master, local column, column master).
+  columns alike; ``jitbridge_hang.h`` master loops) into the element matrix
+  over oomph's local equations (own values, then outside masters), inserted
+  in the vectors-of-pairs order (element, local equation i, local equation j).
 """
 from __future__ import annotations
 
 import ctypes
+import os
 from typing import Dict, List, Tuple
 
 import numpy as np
@@ -103,14 +105,16 @@ def _shape(s0: float, s1: float) -> np.ndarray:
     return psi
 
 
-def _complete(hang: Dict[int, List[Tuple[int, float]]], min_weight: float = 1e-8):
+def _complete(hang: Dict[int, List[Tuple[int, float]]], min_weight: float = 1e-8, rank=None):
     """oomph-lib's complete_hanging_nodes (refineable_mesh.cc:2214-2320) as
     written there: nodes in order; for each hanging node the recursive list
     of (master, weight) -- a hanging master contributes its own masters'
     list, each weight then multiplied by the master's weight -- built on
     the hang infos as completed so far, merged in a map (|w| <= min_weight
     dropped, repeats summed) that replaces the node's hang info.  The map's
-    order is the node number here (oomph's is the node's address)."""
+    order is the node's address in oomph: ``rank`` gives the nodes' order of
+    creation, which the addresses follow in a fresh allocation (default:
+    the node number)."""
     hang = {k: list(v) for k, v in hang.items()}
 
     def rec(node, masters, weights):
@@ -132,7 +136,7 @@ def _complete(hang: Dict[int, List[Tuple[int, float]]], min_weight: float = 1e-8
         for m, w in zip(masters, weights):
             if abs(w) > min_weight:
                 merged[m] = merged.get(m, 0.0) + w
-        hang[node] = [(m, merged[m]) for m in sorted(merged)]
+        hang[node] = [(m, merged[m]) for m in sorted(merged, key=(lambda q: rank[q]) if rank else None)]
     return hang
 
 
@@ -147,12 +151,15 @@ def refine_levels(m: O.Mesh, chosen, max_level: int):
     hanging nodes found geometrically on the leaves' edges and completed
     recursively (``_complete``)."""
     leaves = []   # per leaf: its 9 node positions
+    sons_at = []  # (level, [4 x 9 positions]) of every split, in tree order
 
     def split(nodes9: np.ndarray, level: int):
         c = nodes9[4]
         if level < max_level and chosen(c[0], c[1], level):
-            for (sx0, sy0) in ((-1.0, -1.0), (0.0, -1.0), (-1.0, 0.0), (0.0, 0.0)):
-                son = np.array([_shape(sx0 + 0.5 * i, sy0 + 0.5 * j) @ nodes9 for j in range(3) for i in range(3)])
+            sons = [np.array([_shape(sx0 + 0.5 * i, sy0 + 0.5 * j) @ nodes9 for j in range(3) for i in range(3)])
+                    for (sx0, sy0) in ((-1.0, -1.0), (0.0, -1.0), (-1.0, 0.0), (0.0, 0.0))]
+            sons_at.append((level, sons))
+            for son in sons:
                 split(son, level + 1)
         else:
             leaves.append(nodes9)
@@ -187,11 +194,99 @@ def refine_levels(m: O.Mesh, chosen, max_level: int):
                 w = (0.5 * s * (s - 1.0), 1.0 - s * s, 0.5 * s * (s + 1.0))
                 hang[k] = [(a, w[0]), (mid, w[1]), (b, w[2])]
                 break
-    hang = _complete(hang)
+    # order of creation in oomph: the base mesh's nodes in its own order,
+    # then one adapt per level, each building the new sons in tree order,
+    # nodes in local order (a node already there is shared)
+    key = lambda p: (round(float(p[0]), 12), round(float(p[1]), 12))
+    rank = {ids[key(p)]: g for g, p in enumerate(m.x)}
+    for level in range(max_level):
+        for lv, sons in sons_at:
+            if lv == level:
+                for son in sons:
+                    for p in son:
+                        rank.setdefault(ids[key(p)], len(rank))
+    hang = _complete(hang, rank=rank)
     lo, hi = x.min(axis=0), x.max(axis=0)
     on_b = (np.abs(x[:, 0] - lo[0]) < 1e-12) | (np.abs(x[:, 0] - hi[0]) < 1e-12) | \
            (np.abs(x[:, 1] - lo[1]) < 1e-12) | (np.abs(x[:, 1] - hi[1]) < 1e-12)
     return x, conn, hang, on_b
+
+
+def refinement_plan(m: O.Mesh, chosen, max_level: int):
+    """(level, centre x, centre y) of every element that ``refine_levels``
+    splits, in tree order."""
+    plan = []
+
+    def split(nodes9: np.ndarray, level: int):
+        c = nodes9[4]
+        if level < max_level and chosen(c[0], c[1], level):
+            plan.append((level, float(c[0]), float(c[1])))
+            for (sx0, sy0) in ((-1.0, -1.0), (0.0, -1.0), (-1.0, 0.0), (0.0, 0.0)):
+                split(np.array([_shape(sx0 + 0.5 * i, sy0 + 0.5 * j) @ nodes9 for j in range(3) for i in range(3)]),
+                      level + 1)
+
+    for e in range(m.conn.shape[0]):
+        split(m.x[m.conn[e]].copy(), 0)
+    return plan
+
+
+REF_HANG_DRIVER = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_ref", "oomph_hang_driver")
+
+
+def ref_hang_available() -> bool:
+    return os.path.exists(REF_HANG_DRIVER)
+
+
+def ref_hang_run(N: int, chosen, max_level: int, gaussians: np.ndarray, dofs=None) -> dict:
+    """oomph-lib's own refinement, hanging nodes, numbering and
+    Problem::get_jacobian on the refined oracle mesh (oracle/ref/
+    oomph_hang_driver.cc, compiled from the reference tree).  ``dofs``:
+    the free values in oomph's equation order (default 0)."""
+    import subprocess
+    import tempfile
+    m = O.mesh(O.Q2_QUAD, N, N)
+    plan = np.array(refinement_plan(m, chosen, max_level), dtype=np.float64).reshape(-1, 3)
+    g = np.asarray(gaussians, dtype=np.float64)
+    params = np.concatenate([[g.shape[0]], g.reshape(-1)])
+    with tempfile.TemporaryDirectory() as td:
+        fin, fd, fout = (os.path.join(td, n) for n in ("in.bin", "dofs.bin", "out.bin"))
+        with open(fin, "wb") as f:
+            np.array([m.x.shape[0], m.conn.shape[0], plan.shape[0], params.size], dtype=np.int32).tofile(f)
+            np.ascontiguousarray(m.x, dtype=np.float64).tofile(f)
+            np.ascontiguousarray(m.conn, dtype=np.int32).tofile(f)
+            np.ascontiguousarray(m.bmask, dtype=np.uint32).tofile(f)
+            plan.tofile(f)
+            params.tofile(f)
+        if dofs is not None:
+            np.ascontiguousarray(dofs, dtype=np.float64).tofile(fd)
+        subprocess.run([REF_HANG_DRIVER, fin, fd if dofs is not None else "", fout], check=True)
+        b = open(fout, "rb").read()
+    off = 0
+
+    def take(dt, n):
+        nonlocal off
+        a = np.frombuffer(b, dtype=dt, count=n, offset=off)
+        off += a.nbytes
+        return a.copy()
+
+    nn, ne, nd, nnz = (int(v) for v in take(np.int32, 4))
+    x = take(np.float64, 2 * nn).reshape(nn, 2)
+    conn = take(np.int32, 9 * ne).reshape(ne, 9)
+    eqn = take(np.int32, nn)
+    hang = {}
+    for i in range(nn):
+        k = int(take(np.int32, 1)[0])
+        ms = []
+        for _ in range(k):
+            mm = int(take(np.int32, 1)[0])
+            ms.append((mm, float(take(np.float64, 1)[0])))
+        if k:
+            hang[i] = ms
+    rp = take(np.int32, nd + 1)
+    ci = take(np.int32, nnz)
+    v = take(np.float64, nnz)
+    R = take(np.float64, nd)
+    return dict(x=x, conn=conn, eqn=eqn, hang=hang, rowptr=rp, colidx=ci, vals=v, R=R)
 
 
 class HangProblem:
@@ -248,13 +343,32 @@ class HangProblem:
                                   O._ptr(self.params), len(self.params), O._ptr(Re), O._ptr(Je))
             J = Je.reshape(9, 9)
             exp = [self.expand(int(n)) for n in c]
+            # oomph's local equations of the element: its own non-hanging
+            # values in local order, then the masters of its hanging values
+            # that are not its own nodes, by first appearance
+            # (RefineableElement::assign_hanging_local_eqn_numbers)
+            dofs = [int(self.eqn[n]) for n in c if int(n) not in self.hang and self.eqn[n] >= 0]
+            own = set(int(n) for n in c)
+            for n in c:
+                for mm, _ in self.hang.get(int(n), []):
+                    q = int(self.eqn[mm])
+                    if mm not in own and q >= 0 and q not in dofs:
+                        dofs.append(q)
+            pos = {q: a for a, q in enumerate(dofs)}
+            Jl = np.zeros((len(dofs), len(dofs)))
+            Rl = np.zeros(len(dofs))
             for i in range(9):
                 for (r, wr) in exp[i]:
-                    R[r] += wr * Re[i]
-                    row = rows[r]
+                    Rl[pos[r]] += wr * Re[i]
                     for j in range(9):
                         for (cc, wc) in exp[j]:
-                            row[cc] = row.get(cc, 0.0) + wr * wc * J[i, j]
+                            Jl[pos[r], pos[cc]] += wr * wc * J[i, j]
+            # the vectors-of-pairs insertion: (local equation i, local equation j)
+            for a, r in enumerate(dofs):
+                R[r] += Rl[a]
+                row = rows[r]
+                for b, cc in enumerate(dofs):
+                    row[cc] = row.get(cc, 0.0) + Jl[a, b]
         rp = np.zeros(self.n_dof + 1, dtype=np.int64)
         for i, row in enumerate(rows):
             rp[i + 1] = rp[i] + len(row)

@@ -465,11 +465,16 @@ struct HangMap {
 
 // The CSR pattern of Problem::sparse_assemble_row_or_column_compressed_with_
 // vectors_of_pairs (problem.cc:5459-5660) with every structural coupling kept:
-// row r lists, in order of first insertion over (element, local i, local j),
-// the columns of the elements that contain equation r.  Rows are built
-// independently (in parallel): the incidence of each equation (its elements,
-// in element order, with the local index) is gathered first, then each row
-// walks its incidence with a marker array for O(1) membership.
+// row r lists, in order of first insertion over (element, local equation i,
+// local equation j), the columns of the elements that contain equation r.
+// An element's local equations are oomph's: its own values' equations in
+// local order, then -- with hanging values -- the equations of their masters
+// that are not values of the element, in order of first appearance over
+// (hanging value, master) (RefineableElement::assign_hanging_local_eqn_numbers,
+// refineable_elements.cc:312-450).  Rows are built independently (in
+// parallel): the incidence of each equation (its elements, in element order,
+// with the local index) is gathered first, then each row walks its incidence
+// with a marker array for O(1) membership.
 struct PatternBuilder {
   long long n_dof;
   int nval;
@@ -496,6 +501,31 @@ struct PatternBuilder {
     }
     const int32_t c = eqn[slot];
     if (c >= 0) f(c, 1.0);
+  }
+
+  // the element's local equations in oomph's order (see above)
+  template <typename F> void element_dofs(const PatDomain &d, long long e, F &&f) const {
+    const bool hanging = hang && !hang->slot_of.empty();
+    for (int k = 0; k < d.nlocal; k++) {
+      const long long slot = (long long)d.conn[e * d.nnode + d.local_node[k]] * nval + d.local_val[k];
+      if (hanging && hang->find(slot) >= 0) continue;
+      if (eqn[slot] >= 0) f(eqn[slot]);
+    }
+    if (!hanging) return;
+    // (a master met twice is passed twice: the caller keeps the first)
+    for (int k = 0; k < d.nlocal; k++) {
+      const long long slot = (long long)d.conn[e * d.nnode + d.local_node[k]] * nval + d.local_val[k];
+      const long long h = hang->find(slot);
+      if (h < 0) continue;
+      for (long long m = hang->ptr[h]; m < hang->ptr[h + 1]; m++) {
+        const long long ms = hang->master[m];
+        bool own = false;   // a value of this element: numbered in the first pass (or pinned)
+        for (int k2 = 0; k2 < d.nlocal && !own; k2++)
+          own = (long long)d.conn[e * d.nnode + d.local_node[k2]] * nval + d.local_val[k2] == ms;
+        const int32_t c = eqn[ms];
+        if (!own && c >= 0) f(c);
+      }
+    }
   }
 
   void build_incidence() {
@@ -525,16 +555,18 @@ struct PatternBuilder {
     for (long long k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
       const Incident &I = inc[k];
       const PatDomain &d = (*doms)[I.dom];
+      // columns in the element's local-equation order (new ones appended)
+      element_dofs(d, I.e, [&](int32_t c) {
+        if (marker[c] < 0) {
+          marker[c] = (int32_t)cols.size();
+          cols.push_back(c);
+          slot_cnt.push_back(0);
+        }
+      });
+      // contributions of this incidence: every (local j, master) of the element
       for (int j = 0; j < d.nlocal; j++)
         expand(d, I.e, j, [&](int32_t c, double) {
-          int32_t s = marker[c];
-          if (s < 0) {
-            s = (int32_t)cols.size();
-            marker[c] = s;
-            cols.push_back(c);
-            slot_cnt.push_back(0);
-          }
-          slot_cnt[s]++;
+          slot_cnt[marker[c]]++;
           ncontrib++;
         });
     }

@@ -327,16 +327,15 @@ class RefinedQuadMesh(MeshTemplate):
         return md
 
 
-def complete_hanging(hang: Dict[int, List[Tuple[int, float]]], min_weight: float = 1e-8
-                     ) -> Dict[int, List[Tuple[int, float]]]:
+def complete_hanging(hang: Dict[int, List[Tuple[int, float]]], min_weight: float = 1e-8,
+                     rank: Optional[Dict[int, int]] = None) -> Dict[int, List[Tuple[int, float]]]:
     """Hang infos whose masters do not hang (oomph-lib's
     TreeBasedRefineableMeshBase::complete_hanging_nodes, refineable_mesh.cc:
     2214-2320): a master that hangs is replaced by its own masters, weights
     multiplied, recursively; then the list is merged -- entries with
     |weight| <= min_weight dropped, repeated masters summed.  oomph merges in
-    a map keyed by the node's address; here the masters are ordered by node
-    number (the nodes' order of creation, which addresses follow in a
-    fresh allocation)."""
+    a map keyed by the node's address, i.e. in the order the nodes were
+    created; ``rank`` gives that order (default: the node number)."""
     def expand(n: int, w: float, out: List[Tuple[int, float]], depth: int = 0) -> None:
         if depth > 64:
             raise ValueError("cyclic hanging-node dependencies")
@@ -355,7 +354,8 @@ def complete_hanging(hang: Dict[int, List[Tuple[int, float]]], min_weight: float
         for m, w in lst:
             if abs(w) > min_weight:
                 merged[m] = merged.get(m, 0.0) + w
-        done[h] = [(m, merged[m]) for m in sorted(merged)]
+        key = (lambda m: rank[m]) if rank is not None else None
+        done[h] = [(m, merged[m]) for m in sorted(merged, key=key)]
     return done
 
 
@@ -374,7 +374,10 @@ class AdaptiveQuadMesh(MeshTemplate):
     weights at its position (``RefineableQElement<2>::setup_hang_for_value``);
     masters that hang themselves are resolved recursively
     (``complete_hanging``).  Positions are the base element's isoparametric
-    map at the node's local coordinate."""
+    map at the node's local coordinate.  The masters of a hang info are
+    ordered as oomph creates the nodes: the base mesh's in template order,
+    then, adapt by adapt (one level each), the new sons' in tree order and
+    local node order, a node shared with an existing one created once."""
 
     def __init__(self, *, N: int = 8, refine=None, max_level: int = 2, size: float = 1.0, name: str = "domain",
                  transform=None):
@@ -402,11 +405,13 @@ class AdaptiveQuadMesh(MeshTemplate):
         conn0, x0, lat0 = base.conn, base.x, base.lattice
         hcell = self.size / N
         leaves: List[Tuple[int, int, int, int]] = []   # (base element, qx0, qy0, span)
+        splits: List[Tuple[int, int, int, int]] = []   # (level, qx0, qy0, span) of split elements, tree order
 
         def split(e: int, qx: int, qy: int, span: int, level: int) -> None:
             cx = (qx + 0.5 * span) * hcell / S
             cy = (qy + 0.5 * span) * hcell / S
             if level < L and bool(self.refine(cx, cy, level)):
+                splits.append((level, qx, qy, span))
                 h = span // 2
                 for dy, dx in ((0, 0), (0, 1), (1, 0), (1, 1)):          # SW, SE, NW, NE
                     split(e, qx + dx * h, qy + dy * h, h, level + 1)
@@ -467,7 +472,25 @@ class AdaptiveQuadMesh(MeshTemplate):
                 pa, pm, pb, s = found
                 w = (0.5 * s * (s - 1.0), 1.0 - s * s, 0.5 * s * (s + 1.0))
                 hang[k] = [(node_of[key(*pa)], w[0]), (node_of[key(*pm)], w[1]), (node_of[key(*pb)], w[2])]
-        hang = complete_hanging(hang)
+        # creation order: base nodes (template order), then adapt by adapt
+        # the new sons' nodes in tree order and local node order
+        rank: Dict[int, int] = {}
+        for g in range(x0.shape[0]):
+            rank[node_of[key(int(lat0[g][0]) * S // 2, int(lat0[g][1]) * S // 2)]] = g
+        nxt = x0.shape[0]
+        for level in range(L):
+            for lv, qx0, qy0, span in splits:
+                if lv != level:
+                    continue
+                h = span // 2
+                for dy, dx in ((0, 0), (0, 1), (1, 0), (1, 1)):
+                    for j in range(3):
+                        for i in range(3):
+                            k = node_of[key(qx0 + dx * h + i * (h // 2), qy0 + dy * h + j * (h // 2))]
+                            if k not in rank:
+                                rank[k] = nxt
+                                nxt += 1
+        hang = complete_hanging(hang, rank=rank)
         is_vertex = np.zeros(n, dtype=bool)
         for c in conn:
             for s_ in (0, 2, 6, 8):

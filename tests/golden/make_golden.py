@@ -12,6 +12,13 @@ vals) from Problem::get_jacobian with the vectors-of-pairs assembler, for
 both the default zero filter (threshold 0.0) and the structural pattern
 (threshold -1, every coupling kept).  It also stores oomph's integration
 knots, weights and shape tables per element type.
+
+The hang/*.npz cases come from oracle/_ref/oomph_hang_driver: Q2 meshes refined
+by oomph's own quadtrees (several levels, no 2:1 balance), with the
+refinement plan (level and centre of every split element), oomph's node
+positions, elements, equation numbers, completed hang infos (masters in
+oomph's order), and the structural CSR Jacobian and residual of the Poisson
+form with Gaussian sources at given dofs.
 """
 import os
 import sys
@@ -31,6 +38,40 @@ CASES = [
     ("ns_th_4x3_left", O.P2_TRI, O.EQ_NAVIER_STOKES_TH, 4, 3, 0, 0),
     ("ns_th_3x3_right", O.P2_TRI, O.EQ_NAVIER_STOKES_TH, 3, 3, 0, 1),
 ]
+
+
+def _around(px, py, n):
+    return lambda x, y, level: abs(x - px) < 0.5 / n / 2 ** level and abs(y - py) < 0.5 / n / 2 ** level
+
+
+HANG_CASES = [
+    # name, N, max level, refinement predicate (centre x, centre y, level)
+    ("hang_point_4_L4", 4, 4, _around(0.26, 0.26, 4)),
+    ("hang_ring_4_L3", 4, 3, lambda x, y, l: abs(np.hypot(x - 0.5, y - 0.5) - 0.3) < 0.2 / 2 ** l),
+    ("hang_two_points_6_L3", 6, 3, lambda x, y, l: _around(0.2, 0.7, 6)(x, y, l) or _around(0.55, 0.3, 6)(x, y, l)),
+]
+
+
+def hang_cases():
+    import hang_oracle as H
+    if not H.ref_hang_available():
+        raise SystemExit("oracle/_ref/oomph_hang_driver missing: build it with make -C oracle/ref")
+    for k, (name, N, L, chosen) in enumerate(HANG_CASES):
+        rng = np.random.default_rng(2000 + k)
+        g = gaussians(rng, 2)
+        plan = np.array(H.refinement_plan(O.mesh(O.Q2_QUAD, N, N), chosen, L)).reshape(-1, 3)
+        r0 = H.ref_hang_run(N, chosen, L, g)
+        dofs = rng.normal(0.0, 0.3, r0["R"].size)
+        r = H.ref_hang_run(N, chosen, L, g, dofs=dofs)
+        hn = np.array(sorted(r["hang"]), dtype=np.int64)
+        hp = np.cumsum([0] + [len(r["hang"][h]) for h in hn]).astype(np.int64)
+        hm = np.array([m for h in hn for m, _ in r["hang"][h]], dtype=np.int64)
+        hw = np.array([w for h in hn for _, w in r["hang"][h]])
+        os.makedirs(os.path.join(HERE, "hang"), exist_ok=True)
+        np.savez_compressed(os.path.join(HERE, "hang", name + ".npz"), N=N, L=L, plan=plan, gaussians=g, dofs=dofs,
+                            x=r["x"], conn=r["conn"], eqn=r["eqn"], hang_node=hn, hang_ptr=hp, hang_master=hm,
+                            hang_weight=hw, rowptr=r["rowptr"], colidx=r["colidx"], vals=r["vals"], R=r["R"])
+        print(name, r["R"].size, r["colidx"].size, len(hn))
 
 
 def gaussians(rng, dim, n=8):
@@ -70,6 +111,7 @@ def main():
         for key, val in t.items():
             tabs[f"{et}_{key}"] = val
     np.savez_compressed(os.path.join(HERE, "oomph_tables.npz"), **tabs)
+    hang_cases()
 
 
 if __name__ == "__main__":
