@@ -382,11 +382,12 @@ def assemble(D: Droplet, vals: np.ndarray, hist: List[np.ndarray], p: Dict[str, 
 
 
 def bdf_weights(order: int, dt: float, dt_prev: Optional[float] = None) -> Tuple[float, float, float]:
-    """BDF1 / variable-step BDF2 weights of d/dt (current, previous, before)."""
+    """BDF1, or BDF2 for variable steps, with the expressions of pyoomph's
+    MultiTimeStepper::set_weights (src/timestepper.cpp:32-52)."""
     if order == 1:
         return 1.0 / dt, -1.0 / dt, 0.0
-    om = dt / (dt_prev or dt)
-    return (1 + 2 * om) / ((1 + om) * dt), -(1 + om) / dt, om * om / ((1 + om) * dt)
+    dtprev = dt_prev if dt_prev else dt
+    return 1.0 / dt + 1.0 / (dt + dtprev), -(dt + dtprev) / (dt * dtprev), dt / ((dt + dtprev) * dtprev)
 
 
 def newton(D: Droplet, vals: np.ndarray, hist: List[np.ndarray], p: Dict[str, float], tol: float = 1e-10,

@@ -973,11 +973,14 @@ def droplet_mesh(N: int, radius: float = 1.0) -> DropletMesh:
 
 def bdf_weights(order: int, dt: float, dt_prev: Optional[float] = None) -> Tuple[float, float, float]:
     """d/dt weights of (current, previous, before previous) values: BDF1, or
-    BDF2 for variable steps (omega = dt / dt_prev)."""
+    BDF2 for variable steps, with the expressions of pyoomph's
+    MultiTimeStepper::set_weights (src/timestepper.cpp:32-52, as oomph's
+    BDF<2>::set_weights, timesteppers.cc:232-245), so that the weights are
+    the reference's to the bit."""
     if order == 1:
         return 1.0 / dt, -1.0 / dt, 0.0
-    om = dt / (dt_prev if dt_prev else dt)
-    return (1.0 + 2.0 * om) / ((1.0 + om) * dt), -(1.0 + om) / dt, om * om / ((1.0 + om) * dt)
+    dtprev = dt_prev if dt_prev else dt
+    return (1.0 / dt + 1.0 / (dt + dtprev), -(dt + dtprev) / (dt * dtprev), dt / ((dt + dtprev) * dtprev))
 
 
 # ---------------------------------------------------------------------------

@@ -373,3 +373,21 @@ def test_time_dependent_dirichlet_values(monkeypatch):
     assert np.all(up[b["left"] & ~b["top"] & ~b["bottom"], 0] == 2.0)
     assert np.array_equal(up[~top, 0], P._values0[~top, 0])       # only the timed values change
     P._initialised, P._h = False, None
+
+
+def test_bdf_weights_are_the_references():
+    """pyoomph's MultiTimeStepper::set_weights (src/timestepper.cpp:32-52):
+    BDF1 1/dt, -1/dt; BDF2 1/dt + 1/(dt+dtp), -(dt+dtp)/(dt dtp),
+    dt/((dt+dtp) dtp) -- the same expressions, so the same bits; and
+    consistent with d/dt of quadratics in time."""
+    from pyoomph_gb300.ale import bdf_weights
+    import ale_oracle as AO
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        dt, dtp = 10.0 ** rng.uniform(-5, 0, 2)
+        ref = (1.0 / dt + 1.0 / (dt + dtp), -(dt + dtp) / (dt * dtp), dt / ((dt + dtp) * dtp))
+        assert bdf_weights(2, dt, dtp) == ref == AO.bdf_weights(2, dt, dtp)
+        assert bdf_weights(1, dt) == (1.0 / dt, -1.0 / dt, 0.0)
+        t = np.array([dt + dtp, dtp, 0.0])
+        f = 1.0 + 3.0 * t - 2.0 * t * t
+        assert abs(np.dot(ref, f) - (3.0 - 4.0 * (dt + dtp))) <= 1e-9 * max(1.0, 1.0 / dt)
