@@ -5,14 +5,16 @@ package ``pyoomph_gb300``.
 
 Restates, independently of the package's lattice-based generator:
 
-* one level of refinement of a Q2 quad mesh (oracle mesh of ``fe_oracle.c``
-  in pyoomph's order): each chosen element is replaced by its four children
-  (SW, SE, NW, NE) whose nodes are placed by the parent's isoparametric map;
-  new nodes are numbered in order of first appearance;
-* hanging nodes found geometrically: a child node strictly inside an edge of
-  an unrefined element takes the values interpolated along that edge by the
-  1D quadratic shapes (oomph's ``RefineableQElement<2>::setup_hang_for_value``),
-  and its values are constrained (no equation; ``Node::assign_eqn_numbers``,
+* quadtree refinement of a Q2 quad mesh (oracle mesh of ``fe_oracle.c`` in
+  pyoomph's order) to one or several levels: each chosen element is replaced
+  by its four sons (SW, SE, NW, NE) whose nodes are placed by the parent's
+  isoparametric map; the leaves in tree order; the nodes numbered by first
+  encounter over the leaves (oomph's ``Mesh::reorder_nodes`` after adapt);
+* hanging nodes found geometrically: a node strictly inside an edge of a
+  coarser leaf takes the values interpolated along that edge by the 1D
+  quadratic shapes (oomph's ``RefineableQElement<2>::setup_hang_for_value``),
+  completed through hanging masters (``complete_hanging_nodes``), and its
+  values are constrained (no equation; ``Node::assign_eqn_numbers``,
   ``nodes.cc:534-561``);
 * the element residuals/Jacobians of ``fe_oracle.c`` with the hanging values
   interpolated, assembled with oomph's hanging-node rule (each local equation
@@ -30,72 +32,6 @@ from typing import Dict, List, Tuple
 import numpy as np
 
 import oracle as O
-
-
-def refine(m: O.Mesh, chosen) -> Tuple[np.ndarray, np.ndarray, Dict[int, List[Tuple[int, float]]], np.ndarray]:
-    """(x, conn, hang, on_boundary) of the refined mesh; ``chosen(cx, cy)``
-    selects the elements to split."""
-    L = O.lib()
-    x = [p for p in m.x]
-    conn: List[List[int]] = []
-    refined = []
-    for e in range(m.conn.shape[0]):
-        c = m.conn[e]
-        cx, cy = m.x[c[4]]
-        refined.append(bool(chosen(cx, cy)))
-    lookup: Dict[Tuple[float, float], int] = {(round(p[0], 12), round(p[1], 12)): k for k, p in enumerate(m.x)}
-    for e in range(m.conn.shape[0]):
-        c = m.conn[e]
-        if not refined[e]:
-            conn.append(list(c))
-            continue
-        Xe = m.x[c]
-        for (sx0, sy0) in ((-1.0, -1.0), (0.0, -1.0), (-1.0, 0.0), (0.0, 0.0)):
-            child = []
-            for j in range(3):
-                for i in range(3):
-                    s = np.array([sx0 + 0.5 * i, sy0 + 0.5 * j, 0.0])
-                    psi = np.zeros(9)
-                    dps = np.zeros((9, 2))
-                    L.ofe_shape_c2(O.Q2_QUAD, O._ptr(s), O._ptr(psi), O._ptr(dps))
-                    p = psi @ Xe
-                    k = lookup.get((round(p[0], 12), round(p[1], 12)))
-                    if k is None:
-                        k = len(x)
-                        x.append(p)
-                        lookup[(round(p[0], 12), round(p[1], 12))] = k
-                    child.append(k)
-            conn.append(child)
-    x = np.array(x)
-    conn = np.array(conn, dtype=np.int32)
-    # edges of the unrefined elements: (a, mid, b) node triples
-    edges = []
-    for e in range(m.conn.shape[0]):
-        if refined[e]:
-            continue
-        c = m.conn[e]
-        for a, mid, b in ((0, 1, 2), (6, 7, 8), (0, 3, 6), (2, 5, 8)):
-            edges.append((c[a], c[mid], c[b]))
-    hang: Dict[int, List[Tuple[int, float]]] = {}
-    child_nodes = set(conn[[k for k in range(conn.shape[0])]].ravel().tolist())
-    for k in sorted(child_nodes):
-        for a, mid, b in edges:
-            if k in (a, mid, b):
-                continue
-            pa, pb = x[a], x[b]
-            t = pb - pa
-            u = np.dot(x[k] - pa, t) / np.dot(t, t)
-            if 0.0 < u < 1.0 and np.linalg.norm(pa + u * t - x[k]) < 1e-12:
-                # the local coordinate along the edge on the refinement grid
-                # (exact in binary, as a quadtree's son coordinates are)
-                s = np.round((2.0 * u - 1.0) * 1024.0) / 1024.0
-                w = (0.5 * s * (s - 1.0), 1.0 - s * s, 0.5 * s * (s + 1.0))
-                hang[k] = [(a, w[0]), (mid, w[1]), (b, w[2])]
-                break
-    lo, hi = x.min(axis=0), x.max(axis=0)
-    on_b = (np.abs(x[:, 0] - lo[0]) < 1e-12) | (np.abs(x[:, 0] - hi[0]) < 1e-12) | \
-           (np.abs(x[:, 1] - lo[1]) < 1e-12) | (np.abs(x[:, 1] - hi[1]) < 1e-12)
-    return x, conn, hang, on_b
 
 
 def _shape(s0: float, s1: float) -> np.ndarray:
@@ -291,12 +227,13 @@ def ref_hang_run(N: int, chosen, max_level: int, gaussians: np.ndarray, dofs=Non
 
 class HangProblem:
     """Scalar Q2 problem (Poisson / nonlinear diffusion) on a refined mesh,
-    u = 0 on the outer boundary (one level: ``refine``; with max_level:
-    ``refine_levels``)."""
+    u = 0 on the outer boundary (``refine_levels``; without max_level one
+    level, ``chosen(cx, cy)``)."""
 
     def __init__(self, N: int, chosen, gaussians: np.ndarray, eq: int = O.EQ_POISSON, max_level=None):
-        if max_level is None:
-            self.x, self.conn, self.hang, on_b = refine(O.mesh(O.Q2_QUAD, N, N), chosen)
+        if max_level is None:   # one level, chosen(cx, cy)
+            self.x, self.conn, self.hang, on_b = refine_levels(O.mesh(O.Q2_QUAD, N, N),
+                                                               lambda x, y, level: chosen(x, y), 1)
         else:
             self.x, self.conn, self.hang, on_b = refine_levels(O.mesh(O.Q2_QUAD, N, N), chosen, max_level)
         n = self.x.shape[0]

@@ -231,102 +231,6 @@ class CuboidBrickMesh(MeshTemplate):
 
 # 1D quadratic shapes at the quarter points of an edge (nodes at s = -1, 0, 1):
 # psi(-1/2) = (3/8, 3/4, -1/8), psi(1/2) = (-1/8, 3/4, 3/8)
-_QUARTER_WEIGHTS = {1: (0.375, 0.75, -0.125), 3: (-0.125, 0.75, 0.375)}
-
-
-class RefinedQuadMesh(MeshTemplate):
-    """A RectangularQuadMesh of Q2 quads in which the elements chosen by
-    ``refine(centre_x, centre_y) -> bool`` are split once into four children
-    (SW, SE, NW, NE, replacing the parent in the element list, as the leaves
-    of oomph's quadtree refinement follow their parent).  Nodes of the
-    children on an edge shared with an unrefined neighbour, at a quarter of
-    that edge, hang: their values are the neighbour's quadratic
-    interpolation along the edge (oomph's HangInfo, built by
-    ``RefineableQElement<2>::setup_hang_for_value``), and they carry no
-    equation.  The original nodes keep their numbers; new nodes are numbered
-    in order of first appearance (children in order, nodes in element order)."""
-
-    def __init__(self, *, N: int = 8, refine=None, size: float = 1.0, name: str = "domain", transform=None):
-        self.N = int(N)
-        self.refine = refine or (lambda x, y: x < 0.5)
-        self.size = float(size)
-        self.domain_name = name
-        self.transform = None
-        self._post = transform
-
-    def generate(self) -> MeshData:
-        md = self._generate()
-        if self._post is not None:
-            md.x = np.ascontiguousarray(self._post(md.x.copy()), dtype=np.float64)
-        return md
-
-    def _generate(self) -> MeshData:
-        from .spaces import Q2_QUAD
-        N = self.N
-        base = RectangularQuadMesh(N=N, size=self.size).generate()
-        conn0, x0, lat0 = base.conn, base.x, base.lattice           # half-cell lattice
-        centres = x0[conn0[:, 4]]
-        ref = np.array([bool(self.refine(cx, cy)) for cx, cy in centres])
-        Q = 4 * N + 1                                               # quarter lattice per side
-        key = lambda qx, qy: int(qx) + Q * int(qy)
-        node_of: Dict[int, int] = {key(2 * lx, 2 * ly): k for k, (lx, ly) in enumerate(lat0)}
-        xs = [x for x in x0]
-        qlat = [(2 * lx, 2 * ly) for lx, ly in lat0]
-        conn: List[List[int]] = []
-        cell = {}                                                    # (ix, iy) -> refined?
-        for e in range(conn0.shape[0]):
-            q0 = lat0[conn0[e, 0]]
-            cell[(int(q0[0]) // 2, int(q0[1]) // 2)] = bool(ref[e])
-        for e in range(conn0.shape[0]):
-            if not ref[e]:
-                conn.append(list(conn0[e]))
-                continue
-            ix, iy = int(lat0[conn0[e, 0]][0]) // 2, int(lat0[conn0[e, 0]][1]) // 2
-            Xe = x0[conn0[e]]
-            for cy, cx in ((0, 0), (0, 1), (1, 0), (1, 1)):          # SW, SE, NW, NE
-                child = []
-                for j in range(3):
-                    for i in range(3):
-                        qx, qy = 4 * ix + 2 * cx + i, 4 * iy + 2 * cy + j
-                        k = key(qx, qy)
-                        if k not in node_of:
-                            s = np.array([(qx - 4 * ix) / 2.0 - 1.0, (qy - 4 * iy) / 2.0 - 1.0])
-                            psi, _ = Q2_QUAD.shape_c2(s)
-                            node_of[k] = len(xs)
-                            xs.append(psi @ Xe)
-                            qlat.append((qx, qy))
-                        child.append(node_of[k])
-                conn.append(child)
-        x = np.array(xs)
-        ql = np.array(qlat, dtype=np.int64)
-        n = x.shape[0]
-        # hanging nodes: quarter points of an edge between a refined and an unrefined cell
-        hang: Dict[int, List[Tuple[int, float]]] = {}
-        for (ix, iy), r in cell.items():
-            if not r:
-                continue
-            for dx, dy in ((-1, 0), (1, 0), (0, -1), (0, 1)):
-                nb = (ix + dx, iy + dy)
-                if nb not in cell or cell[nb]:
-                    continue
-                for t in (1, 3):
-                    if dx:
-                        ex = 4 * ix + (0 if dx < 0 else 4)
-                        hq, mq = (ex, 4 * iy + t), [(ex, 4 * iy), (ex, 4 * iy + 2), (ex, 4 * iy + 4)]
-                    else:
-                        ey = 4 * iy + (0 if dy < 0 else 4)
-                        hq, mq = (4 * ix + t, ey), [(4 * ix, ey), (4 * ix + 2, ey), (4 * ix + 4, ey)]
-                    hang[node_of[key(*hq)]] = [(node_of[key(*m)], w) for m, w in zip(mq, _QUARTER_WEIGHTS[t])]
-        is_vertex = np.zeros(n, dtype=bool)
-        for c in conn:
-            for s in (0, 2, 6, 8):
-                is_vertex[c[s]] = True
-        b = {"left": ql[:, 0] == 0, "right": ql[:, 0] == 4 * N, "bottom": ql[:, 1] == 0, "top": ql[:, 1] == 4 * N}
-        md = MeshData(ELEMENT_TYPES["Q2_QUAD"], x, np.array(conn, dtype=np.int32), is_vertex, b, ql)
-        md.hang = {k: hang[k] for k in sorted(hang)}
-        return md
-
-
 def complete_hanging(hang: Dict[int, List[Tuple[int, float]]], min_weight: float = 1e-8,
                      rank: Optional[Dict[int, int]] = None) -> Dict[int, List[Tuple[int, float]]]:
     """Hang infos whose masters do not hang (oomph-lib's
@@ -500,3 +404,15 @@ class AdaptiveQuadMesh(MeshTemplate):
         md = MeshData(ELEMENT_TYPES["Q2_QUAD"], x, np.array(conn, dtype=np.int32), is_vertex, b, ql)
         md.hang = hang
         return md
+
+
+class RefinedQuadMesh(AdaptiveQuadMesh):
+    """One level of quadtree refinement: the elements chosen by
+    ``refine(centre_x, centre_y)`` are split once into their four sons (an
+    AdaptiveQuadMesh with max_level 1: oomph's leaf order, node numbering
+    and hang infos)."""
+
+    def __init__(self, *, N: int = 8, refine=None, size: float = 1.0, name: str = "domain", transform=None):
+        chosen = refine or (lambda x, y: x < 0.5)
+        super().__init__(N=N, refine=lambda x, y, level: bool(chosen(x, y)), max_level=1, size=size, name=name,
+                         transform=transform)
