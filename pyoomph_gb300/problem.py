@@ -820,6 +820,67 @@ class Problem:
         self.dt_prev = dt
         return hist
 
+    def run(self, endtime: float, timestep: Optional[float] = None, *, outstep=None, numouts: Optional[int] = None,
+            out_initially: Optional[bool] = None, newton_solver_tolerance: Optional[float] = None,
+            max_newton_iterations: Optional[int] = None, starttime: Optional[float] = None,
+            temporal_error=None, spatial_adapt: int = 0, output: Optional[Callable] = None) -> float:
+        """Integrate to `endtime` with unsteady_newton_solve (pyoomph's
+        Problem.run, problem.py:4873, without temporal or spatial
+        adaptivity): steps of `timestep` (default: the output interval),
+        shortened to land on every output time and on `endtime`; `output`
+        (a callable taking the problem) at the start (out_initially) and at
+        every multiple of `outstep` (or numouts evenly spaced outputs;
+        outstep=True: after every step).  Returns the final time."""
+        if temporal_error is not None or spatial_adapt:
+            raise NotImplementedError("temporal and spatial adaptivity are not built")
+        if outstep is not None and outstep is not False and numouts is not None:
+            raise ValueError("outstep and numouts cannot both be given")
+        if starttime is not None:
+            self.set_time(float(starttime))
+        t0 = float(self.time)
+        endtime = float(endtime)
+        if numouts is not None:
+            outstep = (endtime - t0) / max(int(numouts), 1)
+        every = outstep is True
+        if outstep is None or outstep is False or every:
+            ostep = None
+        else:
+            ostep = float(outstep)
+        if timestep is None:
+            if ostep is None:
+                raise ValueError("give a timestep (or an outstep to derive it from)")
+            timestep = ostep
+        dt = float(timestep)
+        if dt <= 0.0:
+            raise ValueError("timestep must be positive")
+        if out_initially is None:
+            out_initially = outstep is not False and outstep is not None or numouts is not None
+        keep = (self.newton_solver_tolerance, self.max_newton_iterations)
+        if newton_solver_tolerance is not None:
+            self.newton_solver_tolerance = float(newton_solver_tolerance)
+        if max_newton_iterations is not None:
+            self.max_newton_iterations = int(max_newton_iterations)
+        eps = 1e-12 * max(1.0, abs(endtime))
+        try:
+            if output is not None and out_initially:
+                output(self)
+            k_out = 1
+            while self.time < endtime - eps:
+                step = min(dt, endtime - self.time)
+                if ostep is not None:
+                    t_out = t0 + k_out * ostep
+                    if t_out < self.time + step - eps:
+                        step = t_out - self.time
+                self.unsteady_newton_solve(step)
+                if output is not None and (every or (ostep is not None and
+                                                     abs(self.time - (t0 + k_out * ostep)) <= eps)):
+                    output(self)
+                if ostep is not None and self.time >= t0 + k_out * ostep - eps:
+                    k_out += 1
+        finally:
+            self.newton_solver_tolerance, self.max_newton_iterations = keep
+        return float(self.time)
+
     def set_time(self, t: float) -> None:
         """Set the current time: the parameter var("time") reads and the
         Dirichlet values given as functions with a keyword ``t``

@@ -391,3 +391,35 @@ def test_bdf_weights_are_the_references():
         t = np.array([dt + dtp, dtp, 0.0])
         f = 1.0 + 3.0 * t - 2.0 * t * t
         assert abs(np.dot(ref, f) - (3.0 - 4.0 * (dt + dtp))) <= 1e-9 * max(1.0, 1.0 / dt)
+
+
+def test_run_steps_to_the_output_times_and_the_end():
+    """Problem.run's time loop (host logic; the step itself stubbed): steps
+    of `timestep`, shortened to land on every output time and on the end
+    time; outputs at the start and at every outstep; the Newton settings of
+    the call restored afterwards."""
+    from pyoomph_gb300 import workloads as W
+    P = W.poisson_problem(N=4, transient=True)
+    steps, outs = [], []
+
+    def fake_step(dt):
+        steps.append(dt)
+        P.time += dt
+
+    P.unsteady_newton_solve = fake_step
+    t = P.run(1.0, 0.3, outstep=0.25, output=lambda p: outs.append(round(p.time, 12)),
+              newton_solver_tolerance=1e-3)
+    assert abs(t - 1.0) < 1e-12 and P.newton_solver_tolerance == 1e-8
+    assert outs == [0.0, 0.25, 0.5, 0.75, 1.0]
+    assert np.allclose(steps, [0.25, 0.25, 0.25, 0.25])        # the output interval caps the step
+    steps.clear()
+    outs.clear()
+    P.run(1.3, 0.1, outstep=True, output=lambda p: outs.append(round(p.time, 12)))
+    assert len(steps) == 3 and abs(sum(steps) - 0.3) < 1e-12 and len(outs) == 4
+    steps.clear()
+    P.run(2.0, numouts=4)                                        # step = output interval
+    assert np.allclose(steps, [0.175] * 4)
+    with pytest.raises(ValueError):
+        P.run(3.0, 0.1, outstep=0.5, numouts=3)
+    with pytest.raises(NotImplementedError):
+        P.run(3.0, 0.1, temporal_error=1e-3)
