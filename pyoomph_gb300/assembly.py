@@ -68,10 +68,23 @@ class GB300Assembler(CustomAssemblyBase):
     weak form as the host problem (same equation numbering).  If the host
     problem is not set, the engine's own dof state is assembled."""
 
-    def __init__(self, engine) -> None:
+    def __init__(self, engine, device_linear_solve: bool = False) -> None:
         super().__init__()
         self.engine = engine
+        self.device_linear_solve = bool(device_linear_solve)
         self._last_J = None
+
+    def has_custom_solve_routine(self) -> bool:
+        return self.device_linear_solve
+
+    def custom_solve_routine(self, solve_Jx_b, b):
+        """J x = b for pyoomph's Newton step (assembly.py:47-50 of pyoomph)
+        on the device: the engine's native BiCGStab on the Jacobian of the
+        last assembly, still resident.  A matrix the solver refuses
+        (saddle-point systems) raises LinearSolverError: construct the
+        assembler without device_linear_solve to keep pyoomph's own solver."""
+        return np.ascontiguousarray(self.engine.solve_linear_device(np.asarray(b, dtype=np.float64)),
+                                    dtype=np.float64)
 
     def initialize(self) -> None:
         self.engine.initialise()

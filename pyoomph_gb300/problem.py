@@ -789,6 +789,19 @@ class Problem:
             return self.linear_solver(A, R)
         return spla.splu(A.tocsc()).solve(R)
 
+    def solve_linear_device(self, b: np.ndarray) -> np.ndarray:
+        """x with J x = b, J the Jacobian of the last assembly (resident on
+        the device), by the native batched BiCGStab (linsolve.py) to
+        linear_solver_tolerance; raises LinearSolverError where the solver
+        refuses the matrix or does not converge."""
+        torch = _torch()
+        from .linsolve import BatchedBiCGStab, DeviceCSR
+        if getattr(self, "_krylov", None) is None:
+            self._krylov = BatchedBiCGStab(DeviceCSR.of_problem(self), blocks=self.replicas)
+        bd = torch.as_tensor(np.ascontiguousarray(b, dtype=np.float64), device=self.x_dev.device)
+        x, _ = self._krylov.solve(bd, tol=self.linear_solver_tolerance, atol=self.linear_solver_atol)
+        return x.view(-1)[:self.n_dof].cpu().numpy()
+
     # -- time stepping ---------------------------------------------------
     def unsteady_newton_solve(self, dt: float) -> List[float]:
         """One implicit time step of size dt (pyoomph's

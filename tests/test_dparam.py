@@ -160,3 +160,30 @@ def test_gpu_assembler_parameter_derivative_and_sync():
     R2 = asm.get_residuals_and_jacobian(False)
     # R is linear in the viscosity
     assert np.max(np.abs(R2 - R1 - 0.01 * D)) <= 1e-12 * max(1.0, np.max(np.abs(R1)))
+
+
+def test_assembler_custom_solve_routine_host_logic():
+    """pyoomph's hook for the Newton linear solve: off by default (pyoomph
+    keeps its own solver); with device_linear_solve the engine's device
+    solve answers, and its refusal propagates instead of a silent
+    fallback."""
+    from pyoomph_gb300 import GB300Assembler
+    from pyoomph_gb300.linsolve import LinearSolverError
+
+    class Engine:
+        refuse = False
+
+        def solve_linear_device(self, b):
+            if self.refuse:
+                raise LinearSolverError("zero diagonal")
+            return 2.0 * b
+
+    eng = Engine()
+    assert not GB300Assembler(eng).has_custom_solve_routine()
+    asm = GB300Assembler(eng, device_linear_solve=True)
+    assert asm.has_custom_solve_routine()
+    never = lambda b: (_ for _ in ()).throw(AssertionError("host solve called"))
+    assert np.array_equal(asm.custom_solve_routine(never, np.arange(3.0)), 2.0 * np.arange(3.0))
+    eng.refuse = True
+    with pytest.raises(LinearSolverError):
+        asm.custom_solve_routine(never, np.arange(3.0))
