@@ -592,7 +592,13 @@ class Problem:
         fills them itself."""
         if not self.is_transient:
             raise RuntimeError("a steady problem keeps no time levels")
-        v = np.ascontiguousarray(values, dtype=np.float64).reshape(self.mesh.n_nodes, len(self.fields))
+        v = np.array(values, dtype=np.float64).reshape(self.mesh.n_nodes, len(self.fields))
+        # hanging values follow their masters at every time level (the
+        # device constrains the current values only)
+        flat = v.reshape(-1)
+        for k, s_ in enumerate(self.hang_slots):
+            a, b = self.hang_ptr[k], self.hang_ptr[k + 1]
+            flat[s_] = np.dot(self.hang_weight[a:b], flat[self.hang_master[a:b]])
         N.check(N.load().fe_problem_set_history(self._h, int(level), v.ctypes.data))
 
     def get_current_dofs(self):

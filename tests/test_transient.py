@@ -423,3 +423,35 @@ def test_run_steps_to_the_output_times_and_the_end():
         P.run(3.0, 0.1, outstep=0.5, numouts=3)
     with pytest.raises(NotImplementedError):
         P.run(3.0, 0.1, temporal_error=1e-3)
+
+
+def test_history_levels_keep_hanging_values_consistent(monkeypatch):
+    """set_history_values constrains the hanging values of the level it
+    uploads (the device interpolates the current values only)."""
+    from pyoomph_gb300 import DiffusionEquation, DirichletBC, Problem
+    from pyoomph_gb300 import problem as PR
+    from pyoomph_gb300.meshes import RefinedQuadMesh
+    P = Problem()
+    P.transient = True
+    P += RefinedQuadMesh(N=4)
+    P += (DiffusionEquation() + DirichletBC(u=0.0) @ ["left", "right", "top", "bottom"]) @ "domain"
+    P.lower()
+    assert P.is_transient and len(P.hang_slots) > 0
+    got = []
+
+    class Lib:
+        def fe_problem_set_history(self, h, level, ptr):
+            got.append(np.ctypeslib.as_array((PR.ctypes.c_double * P.mesh.n_nodes).from_address(ptr)).copy())
+            return 0
+
+    monkeypatch.setattr(PR.N, "load", lambda: Lib())
+    P._h = object()
+    v = np.random.default_rng(0).normal(size=(P.mesh.n_nodes, 1))
+    P.set_history_values(0, v)
+    up = got[0]
+    for h, ms in P.mesh.hang.items():
+        assert abs(up[h] - sum(w * up[m] for m, w in ms)) < 1e-14
+    free = np.ones(P.mesh.n_nodes, dtype=bool)
+    free[list(P.mesh.hang)] = False
+    assert np.array_equal(up[free], v[free, 0])
+    P._h = None
