@@ -834,7 +834,7 @@ class Problem:
         w = bdf_weights(1 if self.steps_done == 0 else 2, dt, self.dt_prev)
         self.set_parameters(**dict(zip(BDF_PARAMS, w)))
         self.set_time(self.time + dt)            # var("time") and timed boundary values at t_{n+1}
-        hist = self.solve()
+        hist = self._newton()
         self.steps_done += 1
         self.dt_prev = dt
         return hist
@@ -1037,9 +1037,25 @@ class Problem:
         return self._last_eigen[1] if getattr(self, "_last_eigen", None) else np.zeros((0, 0), dtype=complex)
 
     def solve(self, **_ignored) -> List[float]:
-        """Stationary Newton solve; returns the residual max-norm history."""
-        torch = _torch()
+        """Stationary Newton solve; returns the residual max-norm history.
+        A transient problem is solved for its steady state (BDF weights 0
+        during the solve: pyoomph's ResidualAndJacobianSteady); its time
+        stepping state is kept."""
         self.initialise()
+        if not self.is_transient:
+            return self._newton()
+        idx = [self.param_names.index(k) for k in BDF_PARAMS]
+        keep = self.params[idx].copy()
+        self.set_parameters(**{k: 0.0 for k in BDF_PARAMS})
+        try:
+            return self._newton()
+        finally:
+            self.set_parameters(**dict(zip(BDF_PARAMS, keep)))
+
+    def _newton(self) -> List[float]:
+        """Newton on R(u) = 0 with the parameters as set (a time step when
+        the BDF weights are)."""
+        torch = _torch()
         self._pattern_cache = self.pattern()
         hist = []
         t_asm = 0.0

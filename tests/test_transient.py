@@ -455,3 +455,25 @@ def test_history_levels_keep_hanging_values_consistent(monkeypatch):
     free[list(P.mesh.hang)] = False
     assert np.array_equal(up[free], v[free, 0])
     P._h = None
+
+
+def test_steady_solve_of_a_transient_problem_zeroes_the_bdf_weights():
+    """Problem.solve is the steady solve also for a transient problem (the
+    BDF weights are 0 during its Newton loop and restored after); a time
+    step keeps them."""
+    from pyoomph_gb300 import workloads as W
+    P = W.poisson_problem(N=4, transient=True)
+    P.lower()
+    k = [P.param_names.index(n) for n in ("_bdf_w0", "_bdf_w1", "_bdf_w2")]
+    P.params[k] = (3.0, -4.0, 1.0)
+    seen = []
+    P.initialise = lambda: None
+
+    def set_parameters(replica=None, **kw):
+        for n, v in kw.items():
+            P.params[P.param_names.index(n)] = v
+
+    P.set_parameters = set_parameters
+    P._newton = lambda: seen.append(P.params[k].copy()) or [0.0]
+    P.solve()
+    assert np.array_equal(seen[0], np.zeros(3)) and np.array_equal(P.params[k], (3.0, -4.0, 1.0))
