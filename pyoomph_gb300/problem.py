@@ -16,6 +16,7 @@ reference's default serial solver, or a caller-supplied solver), x -= dx.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import time
 from dataclasses import dataclass
@@ -977,12 +978,13 @@ class Problem:
             raise KeyError(f"unknown parameter {parameter!r}; have {self.param_names}")
         st = self._arclength if getattr(self, "_arclength_param", None) == parameter else None
         self._arclength_prev = st
-        new, nds = arclength_step(
-            _ProblemContinuationOps(self, parameter), st, float(step),
-            tol=self.newton_solver_tolerance if newton_solver_tolerance is None else newton_solver_tolerance,
-            max_newton_iterations=self.max_newton_iterations if max_newton_iterations is None
-            else max_newton_iterations,
-            min_ds=1e-8 if min_ds is None else min_ds, max_ds=max_ds)
+        with self._steady():            # continuation of steady states
+            new, nds = arclength_step(
+                _ProblemContinuationOps(self, parameter), st, float(step),
+                tol=self.newton_solver_tolerance if newton_solver_tolerance is None else newton_solver_tolerance,
+                max_newton_iterations=self.max_newton_iterations if max_newton_iterations is None
+                else max_newton_iterations,
+                min_ds=1e-8 if min_ds is None else min_ds, max_ds=max_ds)
         self._arclength, self._arclength_param = new, parameter
         self.assemble_device(with_jacobian=False)      # nodal values at the new point
         return nds
@@ -998,8 +1000,9 @@ class Problem:
         prev, last = getattr(self, "_arclength_prev", None), getattr(self, "_arclength", None)
         if prev is None or last is None or np.sign(prev.dp) == np.sign(last.dp):
             raise RuntimeError("the last arclength step did not pass a fold")
-        st = locate_fold(_ProblemContinuationOps(self, self._arclength_param), prev, last.ds, rel_tol=rel_tol,
-                         tol=self.newton_solver_tolerance, max_newton_iterations=self.max_newton_iterations)
+        with self._steady():
+            st = locate_fold(_ProblemContinuationOps(self, self._arclength_param), prev, last.ds, rel_tol=rel_tol,
+                             tol=self.newton_solver_tolerance, max_newton_iterations=self.max_newton_iterations)
         self._arclength = st
         self.assemble_device(with_jacobian=False)
         return st.p0
@@ -1014,17 +1017,8 @@ class Problem:
         (eigenvalues [n], eigenvectors [n, n_dof]), also kept for
         get_last_eigenvalues / get_last_eigenvectors."""
         M = self.get_mass_matrix()
-        # the steady Jacobian: BDF weights 0 for the assembly
-        keep = None
-        if self.is_transient:
-            idx = [self.param_names.index(k) for k in BDF_PARAMS]
-            keep = self.params[idx].copy()
-            self.set_parameters(**{k: 0.0 for k in BDF_PARAMS})
-        try:
+        with self._steady():            # the steady Jacobian
             _, J = self.get_jacobian()
-        finally:
-            if keep is not None:
-                self.set_parameters(**dict(zip(BDF_PARAMS, keep)))
         ev, vec = solve_generalized_eigenproblem(J, M, n, shift=shift, sort=sort, which=which, v0=v0,
                                                  target=target)
         self._last_eigen = (ev, vec)
@@ -1042,13 +1036,21 @@ class Problem:
         during the solve: pyoomph's ResidualAndJacobianSteady); its time
         stepping state is kept."""
         self.initialise()
-        if not self.is_transient:
+        with self._steady():
             return self._newton()
+
+    @contextlib.contextmanager
+    def _steady(self):
+        """The steady form for the block (a transient problem's BDF weights
+        0, restored after)."""
+        if not self.is_transient:
+            yield
+            return
         idx = [self.param_names.index(k) for k in BDF_PARAMS]
         keep = self.params[idx].copy()
         self.set_parameters(**{k: 0.0 for k in BDF_PARAMS})
         try:
-            return self._newton()
+            yield
         finally:
             self.set_parameters(**dict(zip(BDF_PARAMS, keep)))
 
