@@ -179,6 +179,46 @@ class _ProblemContinuationOps:
         return self.P.get_parameter_derivative(self.name)
 
 
+class _ProblemAdaptiveOps:
+    """The adaptive stepper's operations on a Problem; the two previous time
+    levels are kept on the host to undo a rejected step."""
+
+    def __init__(self, P: "Problem", prev):
+        self.P, self.prev = P, list(prev)
+        self._pending = None
+
+    def step(self, dt):
+        self._before = self.P.get_values()
+        self.P.unsteady_newton_solve(dt)
+
+    def dofs(self):
+        return self.P.get_dofs()
+
+    def snapshot(self):
+        P = self.P
+        k = [P.param_names.index(n) for n in BDF_PARAMS]
+        return (P.get_values(), P.get_dofs(), list(self.prev), P.time, P.steps_done, P.dt_prev, P.params[k].copy())
+
+    def restore(self, s):
+        P = self.P
+        vals, dofs, prev, t, steps, dtp, w = s
+        P.set_values(vals)
+        P.set_dofs(dofs)
+        P.set_history_values(0, prev[0])
+        P.set_history_values(1, prev[1])
+        P.steps_done, P.dt_prev = steps, dtp
+        P.set_parameters(**dict(zip(BDF_PARAMS, w)))
+        P.set_time(t)
+        self.prev = list(prev)
+
+    def accepted(self):
+        self.prev = [self._before, self.prev[0]]
+
+    def weights(self):
+        P = self.P
+        return tuple(float(P.params[P.param_names.index(n)]) for n in BDF_PARAMS)
+
+
 class NewtonSolverError(RuntimeError):
     """Raised when Newton diverges or exceeds its iteration cap
     (oomph's NewtonSolverError, problem.cc:9298)."""
@@ -845,14 +885,15 @@ class Problem:
             max_newton_iterations: Optional[int] = None, starttime: Optional[float] = None,
             temporal_error=None, spatial_adapt: int = 0, output: Optional[Callable] = None) -> float:
         """Integrate to `endtime` with unsteady_newton_solve (pyoomph's
-        Problem.run, problem.py:4873, without temporal or spatial
-        adaptivity): steps of `timestep` (default: the output interval),
+        Problem.run, problem.py:4873, without spatial adaptivity; with
+        temporal_error, adaptive steps, adaptive_unsteady_newton_solve):
+        steps of `timestep` (default: the output interval),
         shortened to land on every output time and on `endtime`; `output`
         (a callable taking the problem) at the start (out_initially) and at
         every multiple of `outstep` (or numouts evenly spaced outputs;
         outstep=True: after every step).  Returns the final time."""
-        if temporal_error is not None or spatial_adapt:
-            raise NotImplementedError("temporal and spatial adaptivity are not built")
+        if spatial_adapt:
+            raise NotImplementedError("spatial adaptivity is not built")
         if outstep is not None and outstep is not False and numouts is not None:
             raise ValueError("outstep and numouts cannot both be given")
         if starttime is not None:
@@ -891,7 +932,10 @@ class Problem:
                     t_out = t0 + k_out * ostep
                     if t_out < self.time + step - eps:
                         step = t_out - self.time
-                self.unsteady_newton_solve(step)
+                if temporal_error is not None:
+                    dt = self.adaptive_unsteady_newton_solve(step, float(temporal_error))
+                else:
+                    self.unsteady_newton_solve(step)
                 if output is not None and (every or (ostep is not None and
                                                      abs(self.time - (t0 + k_out * ostep)) <= eps)):
                     output(self)
@@ -921,6 +965,30 @@ class Problem:
                 for r in range(1, R):
                     vals[r * n0:(r + 1) * n0][m[:n0], f] = v
             N.check(N.load().fe_problem_set_values(self._h, np.ascontiguousarray(vals).ctypes.data))
+
+    def adaptive_unsteady_newton_solve(self, dt_desired: float, epsilon: float) -> float:
+        """One accepted time step with temporal error control (oomph-lib's
+        Problem::adaptive_unsteady_newton_solve; the algorithm is in
+        timestepping.py): a step whose error exceeds epsilon is undone (the
+        time levels restored from host copies) and redone shorter.  Returns
+        the suggested next step; the step taken is self.dt_prev.  Adaptive
+        stepping starts at the first step of a problem."""
+        from .timestepping import AdaptiveState, adaptive_step
+        if not self.transient:
+            self.make_transient()
+        self.initialise()
+        ad = getattr(self, "_adaptive", None)
+        if ad is None:
+            if self.steps_done:
+                raise NotImplementedError("adaptive stepping must start at the first time step")
+            self.assemble_device(with_jacobian=False)
+            v0 = self.get_values()
+            ad = (AdaptiveState(self.get_dofs()), _ProblemAdaptiveOps(self, [v0, v0]))
+            self._adaptive = ad
+        st, ops = ad
+        _, nxt = adaptive_step(ops, st, float(dt_desired), float(epsilon), newton_error=NewtonSolverError)
+        ops.accepted()
+        return nxt
 
     def make_transient(self) -> None:
         """Keep the partial_t terms from now on.  An initialised problem is

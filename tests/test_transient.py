@@ -422,7 +422,12 @@ def test_run_steps_to_the_output_times_and_the_end():
     with pytest.raises(ValueError):
         P.run(3.0, 0.1, outstep=0.5, numouts=3)
     with pytest.raises(NotImplementedError):
-        P.run(3.0, 0.1, temporal_error=1e-3)
+        P.run(3.0, 0.1, spatial_adapt=1)
+    # temporal_error: the adaptive step answers with the next step size
+    steps.clear()
+    P.adaptive_unsteady_newton_solve = lambda dt, eps: (fake_step(dt), 2.0 * dt)[1]
+    P.run(P.time + 0.7, 0.1, temporal_error=1e-4)
+    assert np.allclose(steps, [0.1, 0.2, 0.4])          # doubling steps, the last one cut to the end time
 
 
 def test_history_levels_keep_hanging_values_consistent(monkeypatch):
