@@ -185,16 +185,22 @@ def make_problem(workload: str, size: int, precision: str, epb=None):
 
 TUNED_EPB = {("ns", 256, "df64"): 48}
 
-# DRAM bytes (read + write) per launch of the element kernel of each bench
-# workload at its default size, from one ncu capture per workload
-# (dram__bytes_read.sum + dram__bytes_write.sum, median of 21 launches;
-# profiles/dram_traffic_element_kernels.md gives the commands).
-MEASURED_TRAFFIC = {
-    ("ns", 256, "fp64"): 207.56e6,
-    ("droplet", 110, "fp64"): 96.67e6, ("droplet", 110, "fp32"): 24.00e6,
-    ("hex", 48, "fp64"): 675.25e6,
-    ("poisson", 64, "fp64"): 0.63e6, ("poisson", 64, "fp32"): 0.62e6,
-}
+# DRAM bytes (read + write) per launch of an element kernel, keyed by the
+# generated kernel's name (its source hash): dram__bytes_read.sum +
+# dram__bytes_write.sum from one ncu capture of that exact kernel, scaled
+# from the captured mesh to the bench's by element count
+# (profiles/dram_traffic_element_kernels.md gives the commands).  A kernel
+# with no capture reports null.
+MEASURED_TRAFFIC = {}
+
+
+def measured_traffic(kernel_name: str, n_elem: int):
+    t = MEASURED_TRAFFIC.get(kernel_name)
+    if t is None:
+        return None
+    bytes_per_elem, captured_elems = t
+    return {"bytes": bytes_per_elem * n_elem, "kernel": kernel_name, "captured_n_elem": captured_elems,
+            "scaled_to_n_elem": n_elem}
 
 
 def element_algorithmic_bytes(P) -> int:
@@ -358,7 +364,8 @@ def run_gb300(args):
         "roofline": {"bound": "hbm", "kernel": P.kernel.name, "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": abytes,
-                     "traffic": MEASURED_TRAFFIC.get((args.workload, args.size, "fp64"))},
+                     "traffic": (measured_traffic(P.kernel.name, n_elem) or {}).get("bytes"),
+                     "traffic_capture": measured_traffic(P.kernel.name, n_elem)},
         "compute_roofline": {"pipe": "fp64", "kernel": P.kernel.name,
                              "flops_per_element": estimate_flops(P.kernel, P.affine)["fp64"],
                              "achieved": estimate_flops(P.kernel, P.affine)["fp64"] * n_elem / (elem_ms / 1e3) / 1e12,
@@ -471,6 +478,10 @@ def run_gb300(args):
                                  "vector kernels, CUDA-graph blocks of 8 iterations)"}
             del PN, A
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # the checker and the CPU baseline, after every timed region
+        line["parity"] = parity_vs_oracle(args, results)
+        if "fp32" in line["parity"]:
+            line["fp32_jacobian"]["max_rel_jacobian_error_vs_fp64_oracle"] = line["parity"]["fp32"].get("max_rel_J")
         line["cpu_baseline"] = cpu_baseline(args, threads=1)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -495,17 +506,32 @@ def _oracle_problem(workload: str, side: int):
 
 
 def _sample_side(workload: str, size: int) -> int:
-    # bounded CPU sample: about 10^4 elements per assembly
-    return {"ns": min(size, 64), "poisson": min(size, 64), "hex": min(size, 12)}[workload]
+    """The side the CPU baseline times: the bench's own side where one
+    assembly takes a few seconds on a host core (NS 256^2: ~2.5 s), a
+    smaller cube for the hex (48^3: ~15 s per assembly)."""
+    return {"ns": size, "poisson": size, "hex": min(size, 24)}[workload]
 
 
-def _cpu_worker(args_tuple):
-    workload, side, seconds = args_tuple
+_CPU = None
+
+
+def _cpu_init(workload: str, side: int):
+    """Pool initialiser: the oracle built with pyoomph's JIT flags, the
+    problem, one warm-up assembly."""
+    global _CPU
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
+    flags = O.use_jit_flags_build()
     OP = _oracle_problem(workload, side)
+    O.assemble(OP, True, 0.0)
+    _CPU = (O, OP, flags)
+
+
+def _cpu_time(seconds: float):
+    """Whole assemblies (the reference's default zero filter, threshold 0)
+    until `seconds` have passed; at least one."""
+    O, OP, flags = _CPU
     n_elem = OP.mesh.conn.shape[0]
-    O.assemble(OP, True, 0.0)  # warm-up
     t0 = time.perf_counter()
     done = 0
     while True:
@@ -513,26 +539,75 @@ def _cpu_worker(args_tuple):
         done += 1
         if time.perf_counter() - t0 >= seconds:
             break
-    return n_elem * done, time.perf_counter() - t0, done
+    return n_elem * done, time.perf_counter() - t0, done, flags
+
+
+class CpuPool:
+    """`threads` spawned processes, each holding the oracle problem."""
+
+    def __init__(self, workload: str, side: int, threads: int):
+        import multiprocessing as mp
+        self.threads = threads
+        self.pool = mp.get_context("spawn").Pool(threads, initializer=_cpu_init, initargs=(workload, side))
+
+    def measure(self, seconds: float):
+        res = self.pool.map(_cpu_time, [seconds] * self.threads)
+        return sum(r[0] / r[1] for r in res), sum(r[2] for r in res), res[0][3]
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
+def _cpu_sample_text(workload, side, n, seconds, flags, threads):
+    return (f"{WORKLOADS[workload][0]} side {side}, {n} full assemblies in ~{seconds:.0f} s on {threads} "
+            f"core(s) (oracle/fe_oracle.c: restated element code and vectors-of-pairs assembly with the "
+            f"default zero filter, compiled {flags})")
 
 
 def cpu_baseline(args, threads: int = 1, seconds: float = 10.0):
     """The oracle's restated reference assembly (vectors-of-pairs, restated
-    element code) timed on the host cores on a bounded sample."""
+    element code, pyoomph's JIT flags) timed on the host cores on a bounded
+    sample: whole assemblies of the bench's mesh (hex: a 24^3 cube)."""
     side = _sample_side(args.workload, args.size)
-    if threads == 1:
-        elems, dt, n = _cpu_worker((args.workload, side, seconds))
-        value = elems / dt
-    else:
-        import multiprocessing as mp
-        ctx = mp.get_context("spawn")
-        with ctx.Pool(threads) as pool:
-            res = pool.map(_cpu_worker, [(args.workload, side, seconds)] * threads)
-        value = sum(r[0] / r[1] for r in res)
-        n = sum(r[2] for r in res)
-    return {"value": value, "unit": "elements/s", "cores": threads, "kind": "port",
-            "sample": f"{WORKLOADS[args.workload][0]} side {side}, {n} full assemblies in ~{seconds:.0f}s "
-                      f"per core (oracle/fe_oracle.c, vectors-of-pairs)"}
+    pool = CpuPool(args.workload, side, threads)
+    try:
+        value, n, flags = pool.measure(seconds)
+    finally:
+        pool.close()
+    return {"value": value, "unit": "elements/s", "cores": threads, "kind": "port", "mesh_side": side,
+            "sample": _cpu_sample_text(args.workload, side, n, seconds, flags, threads)}
+
+
+def parity_vs_oracle(args, results):
+    """Full-size parity of this run's assemblies: the oracle assembles the
+    bench's mesh on the same dof vector once (structural pattern, oomph's
+    threshold -1); every precision's R and CSR J are compared with it."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    P = results["fp64"]["P"]
+    OP = _oracle_problem(args.workload, args.size)
+    if not np.array_equal(P.eqn, OP.eqn):
+        return {"vs": "oracle", "size": args.size, "error": "equation numbering differs"}
+    OP.set_dofs(P.get_dofs())
+    t0 = time.perf_counter()
+    R0, rp, ci, v = O.assemble(OP, True, -1.0)
+    out = {"vs": "oracle (oracle/fe_oracle.c, vectors-of-pairs, structural pattern)", "size": args.size,
+           "oracle_assembly_s": time.perf_counter() - t0}
+    nR = max(float(np.max(np.abs(R0))), 1e-300)
+    nJ = max(float(np.max(np.abs(v))), 1e-300)
+    for prec, r in results.items():
+        Q = r["P"]
+        if not np.array_equal(Q.get_dofs(), OP.dofs()):
+            out[prec] = {"error": "dof vector differs from the oracle's"}
+            continue
+        R, J = Q.get_jacobian()
+        out[prec] = {"pattern_bit_exact": bool(np.array_equal(J.indptr, rp) and np.array_equal(J.indices, ci)),
+                     "max_rel_R": float(np.max(np.abs(R - R0)) / nR),
+                     "max_rel_J": float(np.max(np.abs(J.data.astype(np.float64) - v)) / nJ),
+                     "tolerance_J": 1e-5 if prec == "fp32" else 1e-12}
+        del R, J
+    return out
 
 
 def droplet_problem(size: int, precision: str, shape=None):
@@ -642,7 +717,8 @@ def run_droplet(args):
         "roofline": {"bound": "hbm", "kernel": P.kernel.name, "achieved": abytes / (elem_ms / 1e3) / 1e9,
                      "peak": hbm_peak, "unit": "GB/s", "frac": abytes / (elem_ms / 1e3) / 1e9 / hbm_peak,
                      "peak_kind": peak_kind, "algorithmic_bytes_per_launch": abytes,
-                     "traffic": MEASURED_TRAFFIC.get(("droplet", args.size, "fp64"))},
+                     "traffic": (measured_traffic(P.kernel.name, n_elem) or {}).get("bytes"),
+                     "traffic_capture": measured_traffic(P.kernel.name, n_elem)},
         "compute_roofline": {"pipe": "fp64", "kernel": P.kernel.name, "flops_per_launch": flops,
                              "achieved": flops / (elem_ms / 1e3) / 1e12, "peak": peak64, "unit": "TFLOP/s",
                              "frac": flops / (elem_ms / 1e3) / 1e12 / peak64,
@@ -721,32 +797,52 @@ def droplet_cpu_baseline(size: int, seconds: float = 10.0):
 
 
 def run_reference(args):
+    """The reference arm: the oracle's restated reference assembly (pyoomph's
+    JIT flags) on every host core, one spawned process per core, each step
+    at least one whole assembly of the bench's mesh per process."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    seconds = max(2.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
+    seconds = max(1.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
     vals = []
-    cb = None
+    t_run = time.perf_counter()
     if args.workload == "droplet":
-        base = lambda sec: droplet_cpu_baseline(args.size, sec)
+        for _ in range(args.warmup):
+            droplet_cpu_baseline(args.size, seconds / 4)
+        for _ in range(args.steps):
+            cb = droplet_cpu_baseline(args.size, seconds)
+            vals.append(cb["value"])
+        side = min(args.size, 24)
     else:
-        base = lambda sec: cpu_baseline(args, threads=threads, seconds=sec)
-    for _ in range(args.warmup):
-        base(seconds / 4)
-    for _ in range(args.steps):
-        cb = base(seconds)
-        vals.append(cb["value"])
+        side = _sample_side(args.workload, args.size)
+        pool = CpuPool(args.workload, side, threads)
+        try:
+            for _ in range(args.warmup):
+                pool.measure(0.0)
+            n_total = 0
+            for _ in range(args.steps):
+                v, n, flags = pool.measure(seconds)
+                vals.append(v)
+                n_total += n
+        finally:
+            pool.close()
+        cb = {"unit": "elements/s", "cores": threads, "kind": "port", "mesh_side": side,
+              "sample": _cpu_sample_text(args.workload, side, n_total, seconds * args.steps, flags, threads)}
     value = float(np.median(vals))
     cb["value"] = value
+    wall = time.perf_counter() - t_run
     line = {"impl": "reference", "metric": "element residual+Jacobian assemblies/s (full CSR assembly)",
             "value": value, "unit": "elements/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOADS[args.workload][0], "mesh_side": args.size, "jacobian": "fp64",
+            "config": {"workload": WORKLOADS[args.workload][0], "mesh_side": side, "jacobian": "fp64",
                        "residual": "fp64"},
+            "wall_s": wall,
             "cpu_baseline": cb, "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}
+    if side != args.size:
+        line["config"]["bench_mesh_side"] = args.size
     print(json.dumps(line), flush=True)
 
 

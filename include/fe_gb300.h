@@ -176,9 +176,11 @@ int fe_problem_set_values(fe_problem_t *p, const double *values_host);
 int fe_problem_get_values(const fe_problem_t *p, double *values_host);
 /* Time history (implicit time stepping, MultiTimeStepper of
  * timestepper.hpp:46-108): level 0 is the previous step's values.
- * set_history writes one level from the host; shift_history moves every
- * level one step back and stores the current values as level 0. */
+ * set_history writes one level from the host, get_history reads one back;
+ * shift_history moves every level one step back and stores the current
+ * values as level 0. */
 int fe_problem_set_history(fe_problem_t *p, int level, const double *values_host);
+int fe_problem_get_history(const fe_problem_t *p, int level, double *values_host);
 int fe_problem_shift_history(fe_problem_t *p);
 /* Overwrite the nodal positions (moving meshes keep them as dofs). */
 int fe_problem_set_positions(fe_problem_t *p, const double *x_host);

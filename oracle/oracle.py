@@ -58,6 +58,21 @@ class _CSR(ctypes.Structure):
     ]
 
 
+JIT_LIB_PATH = os.path.join(HERE, "_build", "libfe_oracle_jit.so")
+
+
+def use_jit_flags_build() -> str:
+    """Switch this process to the oracle built with pyoomph's JIT flags
+    (-O3 -march=native, the timed CPU baseline); returns the flags used."""
+    global _lib, LIB_PATH
+    if not os.path.exists(JIT_LIB_PATH):
+        build()
+    LIB_PATH, _lib = JIT_LIB_PATH, None
+    lib()
+    with open(os.path.join(HERE, "_build", "jit_flags.txt")) as f:
+        return f.read().strip()
+
+
 def lib():
     global _lib
     if _lib is None:

@@ -29,7 +29,7 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_problem_set_params", "fe_assemble", "fe_assemble_host", "fe_residual_max", "fe_dof_update",
            "fe_problem_check", "fe_problem_launch_count", "fe_problem_set_timing", "fe_problem_stage_times", "fe_pattern_host",
            "fe_residual_max_noalloc", "fe_residual_max_noalloc_limit", "fe_problem_element_buffers",
-           "fe_problem_set_history", "fe_problem_shift_history", "fe_problem_set_positions",
+           "fe_problem_set_history", "fe_problem_get_history", "fe_problem_shift_history", "fe_problem_set_positions",
            "fe_problem_graph_capture", "fe_problem_graph_launch", "fe_problem_set_dparam",
            "fe_assemble_pipelined", "fe_csr_spmv", "fe_csr_diagonal", "fe_krylov_create", "fe_krylov_solve",
            "fe_krylov_matvec", "fe_krylov_info", "fe_krylov_destroy", "fe_problem_set_direction",
@@ -147,6 +147,7 @@ def load(build_if_missing: bool = True):
         L.fe_residual_max_noalloc.argtypes = [vp, i64, vp, vp]
         L.fe_problem_element_buffers.argtypes = [vp, c_int, vp, vp]
         L.fe_problem_set_history.argtypes = [vp, c_int, vp]
+        L.fe_problem_get_history.argtypes = [vp, c_int, vp]
         L.fe_problem_shift_history.argtypes = [vp]
         L.fe_problem_set_positions.argtypes = [vp, vp]
         L.fe_problem_graph_capture.argtypes = [vp, vp, vp, vp, c_int]

@@ -1191,6 +1191,13 @@ int fe_problem_set_history(fe_problem_t *p, int level, const double *values_host
   return FE_OK;
 }
 
+int fe_problem_get_history(const fe_problem_t *p, int level, double *values_host) {
+  if (!p || !values_host || level < 0 || level >= p->n_hist) return fail(FE_ERR_ARG, "bad history level");
+  const size_t n = sizeof(double) * p->n_nodes * p->nval;
+  CUDA_TRY(cudaMemcpy(values_host, p->hist.as<const char>() + n * level, n, cudaMemcpyDeviceToHost));
+  return FE_OK;
+}
+
 int fe_problem_shift_history(fe_problem_t *p) {
   if (!p) return fail(FE_ERR_ARG, "null problem");
   if (p->n_hist == 0) return FE_OK;

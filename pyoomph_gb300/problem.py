@@ -185,10 +185,11 @@ class _ProblemAdaptiveOps:
 
     def __init__(self, P: "Problem", prev):
         self.P, self.prev = P, list(prev)
-        self._pending = None
 
     def step(self, dt):
-        self._before = self.P.get_values()
+        # the nodal values before the step: the snapshot the stepper took
+        # just before this call holds them
+        self._before = self._last_snapshot[0]
         self.P.unsteady_newton_solve(dt)
 
     def dofs(self):
@@ -197,7 +198,9 @@ class _ProblemAdaptiveOps:
     def snapshot(self):
         P = self.P
         k = [P.param_names.index(n) for n in BDF_PARAMS]
-        return (P.get_values(), P.get_dofs(), list(self.prev), P.time, P.steps_done, P.dt_prev, P.params[k].copy())
+        self._last_snapshot = (P.get_values(), P.get_dofs(), list(self.prev), P.time, P.steps_done, P.dt_prev,
+                               P.params[k].copy())
+        return self._last_snapshot
 
     def restore(self, s):
         P = self.P
@@ -281,6 +284,12 @@ class Problem:
         self.time = 0.0
         self.steps_done = 0
         self.dt_prev: Optional[float] = None
+        # bumped by every write of the state from outside a time step (dofs,
+        # values, history levels, a rebuild); the adaptive stepper's host
+        # copies of the time levels are valid only while it is unchanged
+        self._state_generation = 0
+        # temporal error scale per field name (set_temporal_error_factor)
+        self.temporal_error_factors: Dict[str, float] = {}
         self.verbose = False
         self._initialised = False
         self.newton_history: List[float] = []
@@ -552,6 +561,7 @@ class Problem:
         self.J_dev = torch.zeros(max(self.nnz, 1), dtype=self._jdtype, device=dev)
         self._krylov = None   # device linear solver state, bound to J_dev
         self.x_dev.copy_(torch.from_numpy(self._dofs_from_values(values)))
+        self._state_generation += 1           # a new device problem
         t4 = time.perf_counter()
         self.timings.update(jit_s=t3 - t2, device_setup_s=t4 - t3)
         self._initialised = True
@@ -619,6 +629,7 @@ class Problem:
     def set_dofs(self, x: np.ndarray) -> None:
         torch = _torch()
         self.x_dev.copy_(torch.as_tensor(np.asarray(x, dtype=np.float64)))
+        self._state_generation += 1
 
     def set_values(self, values: np.ndarray) -> None:
         """Set every nodal value [n_nodes, nval] (pinned ones included) and
@@ -641,6 +652,16 @@ class Problem:
             a, b = self.hang_ptr[k], self.hang_ptr[k + 1]
             flat[s_] = np.dot(self.hang_weight[a:b], flat[self.hang_master[a:b]])
         N.check(N.load().fe_problem_set_history(self._h, int(level), v.ctypes.data))
+        self._state_generation += 1
+
+    def get_history_values(self, level: int) -> np.ndarray:
+        """Nodal values [n_nodes, nval] of a previous time level (0: u_{n-1},
+        1: u_{n-2}) as the device holds them."""
+        if not self.is_transient:
+            raise RuntimeError("a steady problem keeps no time levels")
+        v = np.zeros((self.mesh.n_nodes, len(self.fields)))
+        N.check(N.load().fe_problem_get_history(self._h, int(level), v.ctypes.data))
+        return v
 
     def get_current_dofs(self):
         """pyoomph's accessor: (dof vector, pinned values)."""
@@ -921,6 +942,8 @@ class Problem:
             self.newton_solver_tolerance = float(newton_solver_tolerance)
         if max_newton_iterations is not None:
             self.max_newton_iterations = int(max_newton_iterations)
+        if temporal_error is not None and float(temporal_error) <= 0.0:
+            temporal_error = None            # pyoomph: no positive tolerance = fixed steps
         eps = 1e-12 * max(1.0, abs(endtime))
         try:
             if output is not None and out_initially:
@@ -978,17 +1001,47 @@ class Problem:
             self.make_transient()
         self.initialise()
         ad = getattr(self, "_adaptive", None)
+        key = (self.steps_done, self.time, self._state_generation)
+        if ad is not None and ad[2] != key:
+            # the state changed since the last adaptive step (a fixed step, new
+            # dofs/values/history, a rebuild): the stepper's host copies are
+            # stale, so it restarts from the current point (no error estimate
+            # for the next step, as for the first one)
+            ad = None
         if ad is None:
-            if self.steps_done:
-                raise NotImplementedError("adaptive stepping must start at the first time step")
             self.assemble_device(with_jacobian=False)
             v0 = self.get_values()
-            ad = (AdaptiveState(self.get_dofs()), _ProblemAdaptiveOps(self, [v0, v0]))
-            self._adaptive = ad
-        st, ops = ad
+            if self.steps_done:
+                prev = [self.get_history_values(0), self.get_history_values(1)]
+            else:
+                prev = [v0, v0]
+            ad = (AdaptiveState(self.get_dofs(), scales=self._temporal_error_scales()),
+                  _ProblemAdaptiveOps(self, prev), None)
+        st, ops, _ = ad
         _, nxt = adaptive_step(ops, st, float(dt_desired), float(epsilon), newton_error=NewtonSolverError)
         ops.accepted()
+        self._adaptive = (st, ops, (self.steps_done, self.time, self._state_generation))
         return nxt
+
+    def set_temporal_error_factor(self, field: str, factor: float) -> None:
+        """The scale of a field in the temporal error norm of adaptive time
+        stepping (pyoomph's Equations.set_temporal_error_factor).  pyoomph
+        counts only fields given a factor (default 0); here, while no field
+        has one, every field counts with scale 1."""
+        self.temporal_error_factors[field] = float(factor)
+
+    def _temporal_error_scales(self) -> Optional[np.ndarray]:
+        if not self.temporal_error_factors:
+            return None
+        unknown = set(self.temporal_error_factors) - set(self.fields)
+        if unknown:
+            raise KeyError(f"temporal error factors of unknown fields {sorted(unknown)}; have {self.fields}")
+        eqn = np.asarray(self.eqn).reshape(self.mesh.n_nodes, len(self.fields))
+        s = np.zeros(self.n_dof)
+        for j, f in enumerate(self.fields):
+            col = eqn[:, j]
+            s[col[col >= 0]] = self.temporal_error_factors.get(f, 0.0)
+        return s
 
     def make_transient(self) -> None:
         """Keep the partial_t terms from now on.  An initialised problem is

@@ -10,8 +10,10 @@ After a step of size dt from t_n (previous step dtp):
   u_p = (1 - r^2) u_n + r^2 u_{n-1} + (1 + r) dt u'_n,  r = dt / dtp,
   u'_n the BDF derivative at t_n (the weights of the step that reached it);
 * the error of a value is E (u_{n+1} - u_p), E = (1 + q)^2 / (1 + 3q +
-  4q^2 + 2q^3), q = dtp / dt; the norm is the root mean square over the
-  free values (every field with error scale 1);
+  4q^2 + 2q^3), q = dtp / dt; the norm is pyoomph's: sqrt(sum_k s_k e_k^2 /
+  #{k : s_k != 0}) over the free values k, s_k the temporal error scale of
+  the value's field (set_temporal_error_factor in pyoomph, whose default
+  scale is 0; ``AdaptiveState.scales`` None means scale 1 for every value);
 * the step is rescaled by f = (eps / max(error, 1e-12))^(1/3): rejected
   (and redone with f dt) when error > eps or f <= 0.8, the next step f dt
   at most 4 dt; dt stays in [1e-12, 1e12].  A Newton failure rejects the
@@ -56,6 +58,18 @@ class AdaptiveState:
     dt_n: Optional[float] = None
     steps: int = 0
     last_error: Optional[float] = None
+    # temporal error scale of every dof (None: 1 for every dof)
+    scales: Optional[np.ndarray] = None
+
+
+def error_norm(err: np.ndarray, scales: Optional[np.ndarray]) -> float:
+    """pyoomph's temporal error norm (src/mesh.cpp:1783-1843 per mesh,
+    src/problem.cpp:660-670 summed): the root of the scale-weighted mean
+    square over the values whose field has a non-zero scale."""
+    if scales is None:
+        return float(np.sqrt(np.mean(err * err))) if err.size else 0.0
+    n = int(np.count_nonzero(scales))
+    return float(np.sqrt(np.sum(scales * err * err) / n)) if n else 0.0
 
 
 def predictor(st: AdaptiveState, dt: float) -> np.ndarray:
@@ -86,7 +100,7 @@ def adaptive_step(ops: AdaptiveOps, st: AdaptiveState, dt: float, epsilon: float
         factor, reject = 1.0, False
         if st.udot_n is not None and st.u_nm1 is not None:
             err = error_weight(dt, st.dt_n) * (u - predictor(st, dt))
-            error = max(float(np.sqrt(np.mean(err * err))) if err.size else 0.0, 1e-12)
+            error = max(error_norm(err, st.scales), 1e-12)
             st.last_error = error
             factor = (epsilon / error) ** (1.0 / 3.0)
             reject = error > epsilon

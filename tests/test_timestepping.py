@@ -78,3 +78,77 @@ def test_predictor_and_error_weight_formulas():
     st = AdaptiveState(np.array([f(0.0)]), np.array([f(-dtp)]), np.array([-1.0 + 1.4 * 0.0]), dtp)
     assert abs(predictor(st, dt)[0] - f(dt)) < 1e-14
     assert error_weight(0.1, 0.1) == pytest.approx(4.0 / 10.0)
+
+
+def test_error_norm_counts_only_scaled_values():
+    """pyoomph's norm: sum of scale * err^2 over the values with a non-zero
+    scale, divided by their count (src/mesh.cpp:1783-1843)."""
+    from pyoomph_gb300.timestepping import error_norm
+    e = np.array([1.0, 2.0, 3.0, 4.0])
+    assert error_norm(e, None) == pytest.approx(np.sqrt(np.mean(e * e)))
+    s = np.array([1.0, 0.0, 2.0, 0.0])
+    assert error_norm(e, s) == pytest.approx(np.sqrt((1.0 + 2.0 * 9.0) / 2.0))
+    assert error_norm(e, np.zeros(4)) == 0.0
+
+
+@pytest.mark.gpu
+def test_gpu_adaptive_steps_match_a_fixed_step_replay():
+    """The Problem adapter of adaptive stepping on the device: a step
+    rejected for its error and a step whose Newton solve fails are undone
+    from the host copies of the time levels; a fixed step in between makes
+    the stepper restart from the current point.  Every accepted state equals
+    a replay of the same step sizes by plain unsteady_newton_solve."""
+    from pyoomph_gb300 import DiffusionEquation, DirichletBC, Problem, RectangularQuadMesh
+    from pyoomph_gb300.problem import NewtonSolverError
+
+    def make():
+        P = Problem()
+        P += RectangularQuadMesh(N=12)
+        P += (DiffusionEquation() + DirichletBC(u=0.0) @ ["left", "right", "top", "bottom"]) @ "domain"
+        P.initialise()
+        x = P.mesh.x
+        u0 = (np.sin(np.pi * x[:, 0]) * np.sin(np.pi * x[:, 1])
+              + 0.3 * np.sin(3 * np.pi * x[:, 0]) * np.sin(2 * np.pi * x[:, 1]))[:, None]
+        P.set_values(u0)
+        return P
+
+    P = make()
+    calls, failed = [0], []
+    newton = P._newton
+
+    def flaky_newton():
+        calls[0] += 1
+        if calls[0] == 3:               # the third attempt may not iterate: NewtonSolverError
+            keep = P.max_newton_iterations
+            P.max_newton_iterations = 0
+            try:
+                return newton()
+            except NewtonSolverError:
+                failed.append(calls[0])
+                raise
+            finally:
+                P.max_newton_iterations = keep
+        return newton()
+
+    P._newton = flaky_newton
+    taken, states = [], []
+    dt = 0.05                           # lambda dt ~ 1: the first estimated step is far too long
+    while P.time < 0.12 - 1e-12:
+        dt = P.adaptive_unsteady_newton_solve(min(dt, 0.12 - P.time), 1e-4)
+        taken.append(P.dt_prev)
+        states.append(P.get_dofs())
+    P.unsteady_newton_solve(0.01)       # a fixed step: the adaptive state is stale afterwards
+    taken.append(0.01)
+    states.append(P.get_dofs())
+    while P.time < 0.3 - 1e-12:
+        dt = P.adaptive_unsteady_newton_solve(min(dt, 0.3 - P.time), 1e-4)
+        taken.append(P.dt_prev)
+        states.append(P.get_dofs())
+    assert failed == [3]
+    assert calls[0] > len(taken) + 1    # at least one step was also rejected for its error
+    Q = make()
+    for k, h in enumerate(taken):
+        Q.unsteady_newton_solve(h)
+        ref = Q.get_dofs()
+        assert np.max(np.abs(states[k] - ref)) <= 1e-12 * np.max(np.abs(ref)), k
+    assert abs(Q.time - P.time) < 1e-14 and Q.steps_done == P.steps_done
