@@ -61,10 +61,21 @@ enum {
                              (dResidual{i}dParameter_{k}, codegen.cpp:4743-4760); fixed-mesh
                              and fused code */
   /* fixed-mesh code only, in a call of its own: */
-  FE_ASSEMBLE_HVP = 32     /* J_vals receives the Hessian-vector product
+  FE_ASSEMBLE_HVP = 32,    /* J_vals receives the Hessian-vector product
                               H(y)_ij = sum_k d2R_i/du_j du_k y_k for the direction of
                               fe_problem_set_direction (HessianVectorProduct{i},
                               jitbridge.h:286, codegen.cpp:3646) */
+  /* with FE_ASSEMBLE_JACOBIAN or FE_ASSEMBLE_MASS: */
+  FE_ASSEMBLE_ZERO_FILTER = 64 /* the matrix in the pattern of oomph's default sparse assembly,
+                              which drops every element entry with |J_e(i,j)| <= threshold
+                              (Problem::Numerical_zero_for_sparse_assembly, 0.0 by default,
+                              problem.cc:110; per contribution, problem.cc:5520-5560): a slot
+                              keeps the sum of its surviving contributions in element order,
+                              a row's columns come in the order of their first surviving
+                              insertion, and slots with none are dropped.  J_vals receives
+                              the values in that pattern (at most nnz of them);
+                              fe_problem_filtered_pattern gives its rowptr/colidx.  Meshes
+                              without hanging values; not with fe_assemble_pipelined */
 };
 
 /* Jacobian value precision */
@@ -195,6 +206,17 @@ int fe_problem_set_persistent(fe_problem_t *p, int enable);
 
 /* Parameter of the next FE_ASSEMBLE_DPARAM assembly (index into params). */
 int fe_problem_set_dparam(fe_problem_t *p, int index);
+
+/* Threshold of FE_ASSEMBLE_ZERO_FILTER assemblies (oomph's
+ * Problem::Numerical_zero_for_sparse_assembly, problem.cc:110; default 0.0,
+ * must be >= 0). */
+int fe_problem_set_zero_threshold(fe_problem_t *p, double threshold);
+
+/* The pattern of the last FE_ASSEMBLE_ZERO_FILTER assembly: waits for
+ * `stream`, sets *nnz, and copies rowptr (n_dof + 1) and colidx (*nnz) to
+ * rowptr/colidx (host or device pointers; either may be NULL).
+ * FE_ERR_STATE before the first filtered assembly. */
+int fe_problem_filtered_pattern(fe_problem_t *p, int64_t *nnz, int32_t *rowptr, int32_t *colidx, void *stream);
 
 /* Update the global parameters (host array, n_params values). */
 int fe_problem_set_params(fe_problem_t *p, const double *params_host);

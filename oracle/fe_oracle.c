@@ -627,6 +627,49 @@ ofe_csr *ofe_assemble(int etype, int eq, int64_t n_nodes, int dim, const double 
   return out;
 }
 
+/* The same compressed-row insertion loop over GIVEN element matrices:     */
+/* elem_eqn[e * n + k] is the global equation of local value k of element  */
+/* e (-1: none), Je[e * n * n + i * n + j] its element matrix.  Checks a   */
+/* device compaction of the filtered pattern on the device's own element   */
+/* matrices (no residual).                                                 */
+ofe_csr *ofe_pairs_from_elements(int64_t n_elem, int n, const int32_t *elem_eqn, const double *Je, int64_t n_dof,
+                                 double zero_threshold) {
+  ofe_csr *out = (ofe_csr *)calloc(1, sizeof(ofe_csr));
+  out->n_dof = n_dof;
+  out->residual = (double *)calloc(1, sizeof(double));
+  rowvec_t *rows = (rowvec_t *)calloc((size_t)(n_dof > 0 ? n_dof : 1), sizeof(rowvec_t));
+  for (int64_t e = 0; e < n_elem; e++) {
+    const int32_t *geq = elem_eqn + e * n;
+    const double *J = Je + e * (int64_t)n * n;
+    for (int i = 0; i < n; i++) {
+      const int32_t ei = geq[i];
+      if (ei < 0) continue;
+      for (int j = 0; j < n; j++) {
+        const int32_t ej = geq[j];
+        if (ej < 0) continue;
+        const double v = J[i * n + j];
+        if (fabs(v) > zero_threshold) row_add(&rows[ei], ej, v);
+      }
+    }
+  }
+  out->rowptr = (int32_t *)malloc(sizeof(int32_t) * (n_dof + 1));
+  out->rowptr[0] = 0;
+  for (int64_t i = 0; i < n_dof; i++) out->rowptr[i + 1] = out->rowptr[i] + rows[i].n;
+  out->nnz = out->rowptr[n_dof];
+  out->colidx = (int32_t *)malloc(sizeof(int32_t) * (out->nnz > 0 ? out->nnz : 1));
+  out->vals = (double *)malloc(sizeof(double) * (out->nnz > 0 ? out->nnz : 1));
+  for (int64_t i = 0; i < n_dof; i++) {
+    int32_t o = out->rowptr[i];
+    for (int k = 0; k < rows[i].n; k++) {
+      out->colidx[o + k] = rows[i].p[k].col;
+      out->vals[o + k] = rows[i].p[k].val;
+    }
+    free(rows[i].p);
+  }
+  free(rows);
+  return out;
+}
+
 void ofe_csr_free(ofe_csr *c) {
   if (!c) return;
   free(c->rowptr);

@@ -72,6 +72,11 @@ ofe_csr *ofe_assemble(int etype, int eq, int64_t n_nodes, int dim, const double 
                       int with_jac, double zero_threshold);
 void ofe_csr_free(ofe_csr *c);
 
+/* The compressed-row insertion loop (with the zero filter) over given    */
+/* element matrices: equations elem_eqn[n_elem][n], matrices Je[n_elem][n][n]. */
+ofe_csr *ofe_pairs_from_elements(int64_t n_elem, int n, const int32_t *elem_eqn, const double *Je, int64_t n_dof,
+                                 double zero_threshold);
+
 /* Element-level R_e, J_e in the element's full local order (node-major,
  * values per node; absent values skipped).  Returns the local size. */
 int ofe_element_res_jac(int etype, int eq, int dim, const double *x, const int32_t *conn_e,

@@ -87,6 +87,8 @@ def lib():
                                    ctypes.c_int, ctypes.c_int, ctypes.c_double]
         L.ofe_assemble.restype = ctypes.POINTER(_CSR)
         L.ofe_csr_free.argtypes = [ctypes.POINTER(_CSR)]
+        L.ofe_pairs_from_elements.argtypes = [ctypes.c_int64, ctypes.c_int, p, p, ctypes.c_int64, ctypes.c_double]
+        L.ofe_pairs_from_elements.restype = ctypes.POINTER(_CSR)
         L.ofe_element_res_jac.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, p, p, ctypes.c_int,
                                           p, p, p, ctypes.c_int, p, p]
         L.ofe_element_mass.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, p, p, ctypes.c_double, p]
@@ -197,6 +199,64 @@ def assemble(P: Problem, with_jac: bool = True, zero_threshold: float = 0.0):
         colidx = np.ctypeslib.as_array(cc.colidx, shape=(max(nnz, 1),))[:nnz].copy()
         v = np.ctypeslib.as_array(cc.vals, shape=(max(nnz, 1),))[:nnz].copy()
         return R, rowptr, colidx, v
+    finally:
+        L.ofe_csr_free(c)
+
+
+def vectors_of_pairs(elem_eqns, Je, n_dof: int, threshold: float = 0.0):
+    """CSR of Problem::sparse_assemble_row_or_column_compressed_with_vectors_
+    of_pairs (problem.cc:5459-5660) over GIVEN element matrices, restated in
+    pure Python for small cases: elements in order, local i then local j;
+    an entry with |J_e(i,j)| <= threshold is skipped (problem.cc:5520-5524,
+    NaN included); otherwise row eqn_i is searched for column eqn_j
+    (problem.cc:5530-5545) and the value added, or the pair appended.  A
+    negative threshold keeps every structural coupling.  elem_eqns[e][k]:
+    global equation of local value k of element e (-1: none); Je[e]: its
+    element matrix.  Returns (rowptr, colidx, values)."""
+    rows = [[] for _ in range(n_dof)]
+    where = [dict() for _ in range(n_dof)]        # the linear search's answer, found faster
+    for e in range(len(elem_eqns)):
+        eq = [int(q) for q in elem_eqns[e]]
+        Jm = Je[e]
+        for i, ei in enumerate(eq):
+            if ei < 0:
+                continue
+            for j, ej in enumerate(eq):
+                if ej < 0:
+                    continue
+                v = float(Jm[i][j])
+                if abs(v) > threshold:
+                    k = where[ei].get(ej)
+                    if k is None:
+                        where[ei][ej] = len(rows[ei])
+                        rows[ei].append([ej, v])
+                    else:
+                        rows[ei][k][1] += v
+    rowptr = np.zeros(n_dof + 1, dtype=np.int32)
+    for r in range(n_dof):
+        rowptr[r + 1] = rowptr[r] + len(rows[r])
+    colidx = np.array([c for row in rows for c, _ in row], dtype=np.int32)
+    vals = np.array([v for row in rows for _, v in row], dtype=np.float64)
+    return rowptr, colidx, vals
+
+
+def pairs_from_elements(elem_eqns: np.ndarray, Je: np.ndarray, n_dof: int, threshold: float = 0.0):
+    """vectors_of_pairs in C (ofe_pairs_from_elements), for full-size meshes:
+    (rowptr, colidx, values)."""
+    L = lib()
+    eq = np.ascontiguousarray(elem_eqns, dtype=np.int32)
+    J = np.ascontiguousarray(Je, dtype=np.float64)
+    E, n = eq.shape
+    c = L.ofe_pairs_from_elements(E, n, _ptr(eq), _ptr(J), n_dof, float(threshold))
+    if not c:
+        raise RuntimeError("ofe_pairs_from_elements failed")
+    try:
+        cc = c.contents
+        nnz = cc.nnz
+        rowptr = np.ctypeslib.as_array(cc.rowptr, shape=(n_dof + 1,)).copy()
+        colidx = np.ctypeslib.as_array(cc.colidx, shape=(max(nnz, 1),))[:nnz].copy()
+        v = np.ctypeslib.as_array(cc.vals, shape=(max(nnz, 1),))[:nnz].copy()
+        return rowptr, colidx, v
     finally:
         L.ofe_csr_free(c)
 

@@ -14,7 +14,7 @@ from . import build as _build
 (FE_OK, FE_ERR_ARG, FE_ERR_CUDA, FE_ERR_COMPILE, FE_ERR_NOMEM, FE_ERR_STATE, FE_ERR_DEVICE, FE_ERR_NOGPU,
  FE_ERR_SOLVER) = range(9)
 FE_ASSEMBLE_RESIDUAL, FE_ASSEMBLE_JACOBIAN, FE_ASSEMBLE_VALUES_FROM_DOFS = 1, 2, 4
-FE_ASSEMBLE_MASS, FE_ASSEMBLE_DPARAM, FE_ASSEMBLE_HVP = 8, 16, 32
+FE_ASSEMBLE_MASS, FE_ASSEMBLE_DPARAM, FE_ASSEMBLE_HVP, FE_ASSEMBLE_ZERO_FILTER = 8, 16, 32, 64
 FE_JAC_F64, FE_JAC_F32 = 0, 1
 
 INCLUDE_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc")
@@ -33,7 +33,7 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_problem_graph_capture", "fe_problem_graph_launch", "fe_problem_set_dparam",
            "fe_assemble_pipelined", "fe_csr_spmv", "fe_csr_diagonal", "fe_krylov_create", "fe_krylov_solve",
            "fe_krylov_matvec", "fe_krylov_info", "fe_krylov_destroy", "fe_problem_set_direction",
-           "fe_problem_set_persistent"]
+           "fe_problem_set_persistent", "fe_problem_set_zero_threshold", "fe_problem_filtered_pattern"]
 
 
 def _header_stamp() -> str:
@@ -148,6 +148,8 @@ def load(build_if_missing: bool = True):
         L.fe_problem_element_buffers.argtypes = [vp, c_int, vp, vp]
         L.fe_problem_set_history.argtypes = [vp, c_int, vp]
         L.fe_problem_get_history.argtypes = [vp, c_int, vp]
+        L.fe_problem_set_zero_threshold.argtypes = [vp, ctypes.c_double]
+        L.fe_problem_filtered_pattern.argtypes = [vp, vp, vp, vp, vp]
         L.fe_problem_shift_history.argtypes = [vp]
         L.fe_problem_set_positions.argtypes = [vp, vp]
         L.fe_problem_graph_capture.argtypes = [vp, vp, vp, vp, c_int]

@@ -129,25 +129,25 @@ __global__ void k_scatter_dofs(const double *__restrict__ dofs, const int *__res
 
 // CSR slot s = sum of its element contributions in element order
 template <typename T>
-__global__ void k_gather_slots(const long long *__restrict__ cptr, const unsigned *__restrict__ cidx,
+__global__ void k_gather_slots(const unsigned *__restrict__ cptr, const unsigned *__restrict__ cidx,
                                const T *__restrict__ jbuf, T *__restrict__ vals, long long nnz) {
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nnz;
        s += (long long)gridDim.x * blockDim.x) {
-    const long long b = cptr[s], e = cptr[s + 1];
+    const unsigned b = cptr[s], e = cptr[s + 1];
     T acc = jbuf[cidx[b]];
-    for (long long k = b + 1; k < e; k++) acc += jbuf[cidx[k]];
+    for (unsigned k = b + 1; k < e; k++) acc += jbuf[cidx[k]];
     vals[s] = acc;
   }
 }
 
 // residual entry r = sum of its element contributions in element order
-__global__ void k_gather_rows(const long long *__restrict__ rptr, const unsigned *__restrict__ ridx,
+__global__ void k_gather_rows(const unsigned *__restrict__ rptr, const unsigned *__restrict__ ridx,
                               const double *__restrict__ rbuf, double *__restrict__ R, long long n) {
   for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;
        r += (long long)gridDim.x * blockDim.x) {
-    const long long b = rptr[r], e = rptr[r + 1];
+    const unsigned b = rptr[r], e = rptr[r + 1];
     double acc = 0.0;
-    for (long long k = b; k < e; k++) acc += rbuf[ridx[k]];
+    for (unsigned k = b; k < e; k++) acc += rbuf[ridx[k]];
     R[r] = acc;
   }
 }
@@ -166,28 +166,168 @@ __global__ void k_hang_interp(const long long *__restrict__ slot, const long lon
 // weighted scatter (meshes with hanging values): the same fixed order, each
 // contribution times its weight
 template <typename T>
-__global__ void k_gather_slots_w(const long long *__restrict__ cptr, const unsigned *__restrict__ cidx,
+__global__ void k_gather_slots_w(const unsigned *__restrict__ cptr, const unsigned *__restrict__ cidx,
                                  const double *__restrict__ cw, const T *__restrict__ jbuf, T *__restrict__ out,
                                  long long nnz) {
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nnz;
        s += (long long)gridDim.x * blockDim.x) {
-    const long long b = cptr[s], e = cptr[s + 1];
+    const unsigned b = cptr[s], e = cptr[s + 1];
     T acc = (T)0;
-    for (long long k = b; k < e; k++) acc += (T)cw[k] * jbuf[cidx[k]];
+    for (unsigned k = b; k < e; k++) acc += (T)cw[k] * jbuf[cidx[k]];
     out[s] = acc;
   }
 }
 
-__global__ void k_gather_rows_w(const long long *__restrict__ rptr, const unsigned *__restrict__ ridx,
+__global__ void k_gather_rows_w(const unsigned *__restrict__ rptr, const unsigned *__restrict__ ridx,
                                 const double *__restrict__ rw, const double *__restrict__ rbuf, double *__restrict__ R,
                                 long long n) {
   for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;
        r += (long long)gridDim.x * blockDim.x) {
-    const long long b = rptr[r], e = rptr[r + 1];
+    const unsigned b = rptr[r], e = rptr[r + 1];
     double acc = 0.0;
-    for (long long k = b; k < e; k++) acc += rw[k] * rbuf[ridx[k]];
+    for (unsigned k = b; k < e; k++) acc += rw[k] * rbuf[ridx[k]];
     R[r] = acc;
   }
+}
+
+// ---------------------------------------------------------------------------
+// oomph's zero filter (Problem::Numerical_zero_for_sparse_assembly,
+// problem.cc:110, 5520-5560): an element entry with |J_e(i,j)| <= thr is not
+// inserted, so a slot holds the sum of its surviving contributions, a row's
+// columns come in the order of their first surviving insertion, and a slot
+// with none is absent.  The contributions of a slot are numbered in
+// (domain, element, local i, local j) order, the reference's insertion
+// order, so within a row the index of a slot's first surviving contribution
+// orders the slots as the reference inserts them.
+// ---------------------------------------------------------------------------
+#define FE_ZF_DEAD 0xffffffffu
+
+template <typename T>
+__global__ void k_gather_slots_zf(const unsigned *__restrict__ cptr, const unsigned *__restrict__ cidx,
+                                  const T *__restrict__ jbuf, T *__restrict__ vals, unsigned *__restrict__ key,
+                                  long long nnz, double thr) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nnz;
+       s += (long long)gridDim.x * blockDim.x) {
+    const unsigned b = cptr[s], e = cptr[s + 1];
+    T acc = (T)0;
+    unsigned k = FE_ZF_DEAD;
+    for (unsigned c = b; c < e; c++) {
+      const unsigned at = cidx[c];
+      const T v = jbuf[at];
+      if (fabs((double)v) > thr) {   // NaN fails the test: dropped, as in the reference
+        acc = (k == FE_ZF_DEAD) ? v : acc + v;
+        if (k == FE_ZF_DEAD) k = at;
+      }
+    }
+    vals[s] = acc;
+    key[s] = k;
+  }
+}
+
+// one warp per row: the rank of each surviving slot among the row's
+// surviving slots (by first insertion), -1 for a dropped slot, and the
+// row's surviving count
+__global__ void k_zf_rank(const int *__restrict__ rowptr, const unsigned *__restrict__ key, int *__restrict__ rank,
+                          int *__restrict__ rowcnt, long long n) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+    const int b = rowptr[r], e = rowptr[r + 1];
+    int live = 0;
+    for (int t = b + lane; t < e; t += 32) {
+      const unsigned kt = key[t];
+      int rk = -1;
+      if (kt != FE_ZF_DEAD) {
+        rk = 0;
+        for (int u = b; u < e; u++) rk += key[u] < kt;
+        live++;
+      }
+      rank[t] = rk;
+    }
+    for (int o = 16; o; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
+    if (lane == 0) rowcnt[r] = live;
+  }
+}
+
+// one warp per row: surviving slots to their filtered positions
+template <typename T>
+__global__ void k_zf_scatter(const int *__restrict__ rowptr, const int *__restrict__ rank,
+                             const int *__restrict__ rowptr_zf, const int *__restrict__ colidx,
+                             const T *__restrict__ vals_st, int *__restrict__ colidx_zf, T *__restrict__ vals_zf,
+                             long long n) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+    const int b = rowptr[r], e = rowptr[r + 1], o = rowptr_zf[r];
+    for (int t = b + lane; t < e; t += 32) {
+      const int rk = rank[t];
+      if (rk >= 0) {
+        colidx_zf[o + rk] = colidx[t];
+        vals_zf[o + rk] = vals_st[t];
+      }
+    }
+  }
+}
+
+// exclusive scan of cnt[0..n) into out[0..n) with out[n] = the total, in
+// three launches: block scans with block totals, a scan of the totals (one
+// block, in chunks), the block offsets added
+#define FE_SCAN_THREADS 1024
+#define FE_SCAN_ITEMS 4
+
+__device__ __forceinline__ int block_inclusive_scan(int v, int *sh) {
+  const int t = threadIdx.x;
+  sh[t] = v;
+  __syncthreads();
+  for (int off = 1; off < FE_SCAN_THREADS; off <<= 1) {
+    const int x = t >= off ? sh[t - off] : 0;
+    __syncthreads();
+    sh[t] += x;
+    __syncthreads();
+  }
+  const int r = sh[t];
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(FE_SCAN_THREADS) k_scan_blocks(const int *__restrict__ cnt, int *__restrict__ out,
+                                                                 int *__restrict__ bsum, long long n) {
+  __shared__ int sh[FE_SCAN_THREADS];
+  const long long base = ((long long)blockIdx.x * FE_SCAN_THREADS + threadIdx.x) * FE_SCAN_ITEMS;
+  int v[FE_SCAN_ITEMS], tot = 0;
+  for (int i = 0; i < FE_SCAN_ITEMS; i++) {
+    v[i] = base + i < n ? cnt[base + i] : 0;
+    tot += v[i];
+  }
+  const int incl = block_inclusive_scan(tot, sh);
+  int run = incl - tot;
+  for (int i = 0; i < FE_SCAN_ITEMS; i++) {
+    if (base + i < n) out[base + i] = run;
+    run += v[i];
+  }
+  if (threadIdx.x == FE_SCAN_THREADS - 1) bsum[blockIdx.x] = incl;
+}
+
+__global__ void __launch_bounds__(FE_SCAN_THREADS) k_scan_totals(int *__restrict__ bsum, long long nb,
+                                                                 int *__restrict__ total) {
+  __shared__ int sh[FE_SCAN_THREADS];
+  int carry = 0;
+  for (long long c0 = 0; c0 < nb; c0 += FE_SCAN_THREADS) {
+    const long long i = c0 + threadIdx.x;
+    const int v = i < nb ? bsum[i] : 0;
+    const int incl = block_inclusive_scan(v, sh);
+    if (i < nb) bsum[i] = carry + incl - v;
+    sh[threadIdx.x] = incl;
+    __syncthreads();
+    carry += sh[FE_SCAN_THREADS - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_add(int *__restrict__ out, const int *__restrict__ bsum, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] += bsum[i / (FE_SCAN_THREADS * FE_SCAN_ITEMS)];
 }
 
 // max |R| with NaN -> inf; one block per chunk, then a single finishing block
@@ -385,6 +525,11 @@ struct fe_problem {
   DevBuf hang_slot, hang_ptr, hang_master, hang_weight, cw, rw; // weighted scatter when n_hang > 0
   DevBuf rowptr, colidx, cptr, cidx, rptr, ridx;
   DevBuf partial;
+  // zero-filtered assembly (FE_ASSEMBLE_ZERO_FILTER): threshold, structural
+  // values, per-slot keys and ranks, per-row counts, the filtered pattern
+  double zf_thr = 0.0;
+  bool zf_done = false;
+  DevBuf zf_vals, zf_key, zf_rank, zf_cnt, zf_rowptr, zf_colidx, zf_bsum;
   // the domain buffers are one allocation per kind, addressed by offsets:
   DevBuf jbuf_all, rbuf_all;
   std::vector<int32_t> h_rowptr, h_colidx;
@@ -696,9 +841,16 @@ int build_pattern(fe_problem *P, const std::vector<const int32_t *> &conn_h, con
   P->h_colidx = out.colidx;
   if ((rc = P->rowptr.upload(out.rowptr.data(), sizeof(int32_t) * (n + 1)))) return rc;
   if ((rc = P->colidx.upload(out.colidx.data(), sizeof(int32_t) * nnz))) return rc;
-  if ((rc = P->cptr.upload(out.cptr.data(), sizeof(long long) * (nnz + 1)))) return rc;
+  // contribution ranges as u32 (the lists index the element buffers, whose
+  // entries are counted in u32 as well)
+  if (out.cptr[nnz] > 0xffffffffLL || out.rptr[n] > 0xffffffffLL)
+    return fail(FE_ERR_ARG, "more than 2^32 element contributions");
+  {
+    std::vector<unsigned> c32(out.cptr.begin(), out.cptr.end()), r32(out.rptr.begin(), out.rptr.end());
+    if ((rc = P->cptr.upload(c32.data(), sizeof(unsigned) * (nnz + 1)))) return rc;
+    if ((rc = P->rptr.upload(r32.data(), sizeof(unsigned) * (n + 1)))) return rc;
+  }
   if ((rc = P->cidx.upload(out.cidx.data(), sizeof(unsigned) * out.cidx.size()))) return rc;
-  if ((rc = P->rptr.upload(out.rptr.data(), sizeof(long long) * (n + 1)))) return rc;
   if ((rc = P->ridx.upload(out.ridx.data(), sizeof(unsigned) * out.ridx.size()))) return rc;
   return FE_OK;
 }
@@ -1221,11 +1373,59 @@ int fe_problem_set_params(fe_problem_t *p, const double *params_host) {
   return FE_OK;
 }
 
+} // extern "C"
+
+namespace {
+// the zero-filtered matrix (FE_ASSEMBLE_ZERO_FILTER) from the element
+// buffers: filtered gather, ranks, scan of the row counts, scatter
+template <typename T>
+int assemble_zero_filtered(fe_problem *p, T *J_vals, cudaStream_t st) {
+  const long long n = p->n_dof, nnz = p->nnz;
+  const int sms = sm_count_cached();
+  const long long nb = (n + FE_SCAN_THREADS * FE_SCAN_ITEMS - 1) / (FE_SCAN_THREADS * FE_SCAN_ITEMS);
+  int rc;
+  if (p->zf_vals.bytes != sizeof(T) * nnz) {
+    if ((rc = p->zf_vals.alloc(sizeof(T) * nnz)) || (rc = p->zf_key.alloc(sizeof(unsigned) * nnz)) ||
+        (rc = p->zf_rank.alloc(sizeof(int) * nnz)) || (rc = p->zf_cnt.alloc(sizeof(int) * std::max(1LL, n))) ||
+        (rc = p->zf_rowptr.alloc(sizeof(int) * (n + 1))) || (rc = p->zf_colidx.alloc(sizeof(int) * nnz)) ||
+        (rc = p->zf_bsum.alloc(sizeof(int) * std::max(1LL, nb))))
+      return rc;
+  }
+  k_gather_slots_zf<T><<<grid_for(nnz, 256, sms), 256, 0, st>>>(p->cptr.as<unsigned>(), p->cidx.as<unsigned>(),
+                                                               p->jbuf_all.as<T>(), p->zf_vals.as<T>(),
+                                                               p->zf_key.as<unsigned>(), nnz, p->zf_thr);
+  CUDA_TRY(cudaGetLastError());
+  const int wgrid = grid_for(n * 32, 256, sms);
+  k_zf_rank<<<wgrid, 256, 0, st>>>(p->rowptr.as<int>(), p->zf_key.as<unsigned>(), p->zf_rank.as<int>(),
+                                   p->zf_cnt.as<int>(), n);
+  CUDA_TRY(cudaGetLastError());
+  k_scan_blocks<<<(unsigned)nb, FE_SCAN_THREADS, 0, st>>>(p->zf_cnt.as<int>(), p->zf_rowptr.as<int>(),
+                                                          p->zf_bsum.as<int>(), n);
+  CUDA_TRY(cudaGetLastError());
+  k_scan_totals<<<1, FE_SCAN_THREADS, 0, st>>>(p->zf_bsum.as<int>(), nb, p->zf_rowptr.as<int>() + n);
+  CUDA_TRY(cudaGetLastError());
+  k_scan_add<<<grid_for(n, 256, sms), 256, 0, st>>>(p->zf_rowptr.as<int>(), p->zf_bsum.as<int>(), n);
+  CUDA_TRY(cudaGetLastError());
+  k_zf_scatter<T><<<wgrid, 256, 0, st>>>(p->rowptr.as<int>(), p->zf_rank.as<int>(), p->zf_rowptr.as<int>(),
+                                         p->colidx.as<int>(), p->zf_vals.as<T>(), p->zf_colidx.as<int>(), J_vals, n);
+  CUDA_TRY(cudaGetLastError());
+  p->zf_done = true;
+  return FE_OK;
+}
+} // namespace
+
+extern "C" {
+
 int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags, void *stream) {
   if (!p) return fail(FE_ERR_ARG, "null problem");
   cudaStream_t st = (cudaStream_t)stream;
   const bool want_m = flags & FE_ASSEMBLE_MASS, want_p = flags & FE_ASSEMBLE_DPARAM;
   const bool want_h = flags & FE_ASSEMBLE_HVP;
+  const bool want_zf = flags & FE_ASSEMBLE_ZERO_FILTER;
+  if (want_zf && (want_h || !(flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS))))
+    return fail(FE_ERR_ARG, "fe_assemble: the zero filter applies to a Jacobian or mass-matrix assembly");
+  if (want_zf && p->cw.p)
+    return fail(FE_ERR_ARG, "fe_assemble: the zero filter is not available on meshes with hanging values");
   const bool want_r = (flags & FE_ASSEMBLE_RESIDUAL) || want_p;
   const bool want_j = (flags & FE_ASSEMBLE_JACOBIAN) || want_m || want_h;
   if (want_h && (p->fused || !p->dir.p || (flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS | FE_ASSEMBLE_DPARAM))))
@@ -1263,12 +1463,12 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
   if (rc) return rc;
   if (p->timing) CUDA_TRY(cudaEventRecord(ev[2], st));
   if (want_r && p->rw.p) {
-    k_gather_rows_w<<<grid_for(p->n_dof, 256, sms), 256, 0, st>>>(p->rptr.as<long long>(), p->ridx.as<unsigned>(),
+    k_gather_rows_w<<<grid_for(p->n_dof, 256, sms), 256, 0, st>>>(p->rptr.as<unsigned>(), p->ridx.as<unsigned>(),
                                                                  p->rw.as<double>(), p->rbuf_all.as<double>(), R,
                                                                  p->n_dof);
     CUDA_TRY(cudaGetLastError());
   } else if (want_r) {
-    k_gather_rows<<<grid_for(p->n_dof, 256, sms), 256, 0, st>>>(p->rptr.as<long long>(), p->ridx.as<unsigned>(),
+    k_gather_rows<<<grid_for(p->n_dof, 256, sms), 256, 0, st>>>(p->rptr.as<unsigned>(), p->ridx.as<unsigned>(),
                                                                p->rbuf_all.as<double>(), R, p->n_dof);
     CUDA_TRY(cudaGetLastError());
   }
@@ -1276,20 +1476,24 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
   if (want_j && p->nnz > 0 && p->cw.p) {
     if (p->jac_prec == FE_JAC_F64)
       k_gather_slots_w<double><<<grid_for(p->nnz, 256, sms), 256, 0, st>>>(
-          p->cptr.as<long long>(), p->cidx.as<unsigned>(), p->cw.as<double>(), p->jbuf_all.as<double>(),
+          p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->cw.as<double>(), p->jbuf_all.as<double>(),
           (double *)J_vals, p->nnz);
     else
       k_gather_slots_w<float><<<grid_for(p->nnz, 256, sms), 256, 0, st>>>(
-          p->cptr.as<long long>(), p->cidx.as<unsigned>(), p->cw.as<double>(), p->jbuf_all.as<float>(),
+          p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->cw.as<double>(), p->jbuf_all.as<float>(),
           (float *)J_vals, p->nnz);
     CUDA_TRY(cudaGetLastError());
+  } else if (want_j && p->nnz > 0 && want_zf) {
+    rc = p->jac_prec == FE_JAC_F64 ? assemble_zero_filtered<double>(p, (double *)J_vals, st)
+                                   : assemble_zero_filtered<float>(p, (float *)J_vals, st);
+    if (rc) return rc;
   } else if (want_j && p->nnz > 0) {
     if (p->jac_prec == FE_JAC_F64)
       k_gather_slots<double><<<grid_for(p->nnz, 256, sms), 256, 0, st>>>(
-          p->cptr.as<long long>(), p->cidx.as<unsigned>(), p->jbuf_all.as<double>(), (double *)J_vals, p->nnz);
+          p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->jbuf_all.as<double>(), (double *)J_vals, p->nnz);
     else
       k_gather_slots<float><<<grid_for(p->nnz, 256, sms), 256, 0, st>>>(
-          p->cptr.as<long long>(), p->cidx.as<unsigned>(), p->jbuf_all.as<float>(), (float *)J_vals, p->nnz);
+          p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->jbuf_all.as<float>(), (float *)J_vals, p->nnz);
     CUDA_TRY(cudaGetLastError());
   }
   if (p->timing) {
@@ -1458,7 +1662,7 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
       const long long r0 = run.first, r1 = run.second;
       const long long s0 = h_rp[r0], s1 = h_rp[r1];
       if (want_r) {
-        k_gather_rows<<<grid_for(r1 - r0, 256, sms), 256, 0, st>>>(p->rptr.as<long long>() + r0, p->ridx.as<unsigned>(),
+        k_gather_rows<<<grid_for(r1 - r0, 256, sms), 256, 0, st>>>(p->rptr.as<unsigned>() + r0, p->ridx.as<unsigned>(),
                                                                   p->rbuf_all.as<double>(), p->pipe_R.as<double>() + r0,
                                                                   r1 - r0);
         CUDA_TRY(cudaGetLastError());
@@ -1466,11 +1670,11 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
       if (want_j && s1 > s0) {
         if (p->jac_prec == FE_JAC_F64)
           k_gather_slots<double><<<grid_for(s1 - s0, 256, sms), 256, 0, st>>>(
-              p->cptr.as<long long>() + s0, p->cidx.as<unsigned>(), p->jbuf_all.as<double>(),
+              p->cptr.as<unsigned>() + s0, p->cidx.as<unsigned>(), p->jbuf_all.as<double>(),
               p->pipe_J.as<double>() + s0, s1 - s0);
         else
           k_gather_slots<float><<<grid_for(s1 - s0, 256, sms), 256, 0, st>>>(
-              p->cptr.as<long long>() + s0, p->cidx.as<unsigned>(), p->jbuf_all.as<float>(),
+              p->cptr.as<unsigned>() + s0, p->cidx.as<unsigned>(), p->jbuf_all.as<float>(),
               p->pipe_J.as<float>() + s0, s1 - s0);
         CUDA_TRY(cudaGetLastError());
       }
@@ -1505,6 +1709,25 @@ int fe_problem_set_direction(fe_problem_t *p, const double *y, void *stream) {
   CUDA_TRY(cudaMemsetAsync(p->dir.p, 0, sizeof(double) * n, st)); // pinned values: zero direction
   k_scatter_dofs<<<grid_for(n, 256, sm_count_cached()), 256, 0, st>>>(y, p->eqn.as<int>(), p->dir.as<double>(), n);
   CUDA_TRY(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_problem_set_zero_threshold(fe_problem_t *p, double threshold) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  if (!(threshold >= 0.0)) return fail(FE_ERR_ARG, "zero threshold must be >= 0");
+  p->zf_thr = threshold;
+  return FE_OK;
+}
+
+int fe_problem_filtered_pattern(fe_problem_t *p, int64_t *nnz, int32_t *rowptr, int32_t *colidx, void *stream) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  if (!p->zf_done) return fail(FE_ERR_STATE, "no zero-filtered assembly yet");
+  CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  int32_t m = 0;
+  CUDA_TRY(cudaMemcpy(&m, p->zf_rowptr.as<int32_t>() + p->n_dof, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (nnz) *nnz = m;
+  if (rowptr) CUDA_TRY(cudaMemcpy(rowptr, p->zf_rowptr.p, sizeof(int32_t) * (p->n_dof + 1), cudaMemcpyDefault));
+  if (colidx && m > 0) CUDA_TRY(cudaMemcpy(colidx, p->zf_colidx.p, sizeof(int32_t) * m, cudaMemcpyDefault));
   return FE_OK;
 }
 
@@ -1675,7 +1898,9 @@ int fe_problem_launch_count(const fe_problem_t *p, int flags) {
       if (d.n_elem) n++;
   }
   if (flags & (FE_ASSEMBLE_RESIDUAL | FE_ASSEMBLE_DPARAM)) n++;
-  if ((flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS | FE_ASSEMBLE_HVP)) && p->nnz > 0) n++;
+  if ((flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS | FE_ASSEMBLE_HVP)) && p->nnz > 0)
+    n += (flags & FE_ASSEMBLE_ZERO_FILTER) ? 6 : 1;   // filtered gather, ranks, three scan launches, scatter
+  if (p->n_hang > 0) n++;
   return n;
 }
 

@@ -288,6 +288,11 @@ class Problem:
         # values, history levels, a rebuild); the adaptive stepper's host
         # copies of the time levels are valid only while it is unchanged
         self._state_generation = 0
+        # oomph's Problem::Numerical_zero_for_sparse_assembly for the
+        # matrices get_jacobian returns: None = the structural pattern (every
+        # coupling kept, the fast path); a threshold >= 0 = the reference's
+        # value-dependent pattern (its default is 0.0)
+        self.numerical_zero_for_sparse_assembly: Optional[float] = None
         # temporal error scale per field name (set_temporal_error_factor)
         self.temporal_error_factors: Dict[str, float] = {}
         self.verbose = False
@@ -714,12 +719,17 @@ class Problem:
         return rp, ci[:self.nnz]
 
     # -- assembly (device) ----------------------------------------------
-    def assemble_device(self, with_jacobian: bool = True, stream=None) -> None:
-        """R (and CSR J values) into self.R_dev / self.J_dev from self.x_dev."""
+    def assemble_device(self, with_jacobian: bool = True, stream=None, zero_threshold: Optional[float] = None) -> None:
+        """R (and CSR J values) into self.R_dev / self.J_dev from self.x_dev.
+        zero_threshold: J in oomph's zero-filtered pattern instead (its
+        rowptr/colidx from fe_problem_filtered_pattern)."""
         torch = _torch()
         flags = N.FE_ASSEMBLE_RESIDUAL | N.FE_ASSEMBLE_VALUES_FROM_DOFS
         if with_jacobian:
             flags |= N.FE_ASSEMBLE_JACOBIAN
+        if zero_threshold is not None and with_jacobian:
+            N.check(N.load().fe_problem_set_zero_threshold(self._h, float(zero_threshold)))
+            flags |= N.FE_ASSEMBLE_ZERO_FILTER
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
         N.check(N.load().fe_assemble(self._h, self.x_dev.data_ptr(), self.R_dev.data_ptr(),
                                      self.J_dev.data_ptr(), flags, ctypes.c_void_p(st)))
@@ -791,15 +801,45 @@ class Problem:
         return self.R_dev[:self.n_dof].cpu().numpy()
 
     def get_jacobian(self):
-        """Problem::get_jacobian (problem.cc:4038): (R, scipy CSR J)."""
+        """Problem::get_jacobian (problem.cc:4038): (R, scipy CSR J).  With
+        numerical_zero_for_sparse_assembly set (oomph's default is 0.0), J
+        has the reference's value-dependent pattern: element entries with
+        |J_e(i,j)| <= the threshold are left out (problem.cc:5520-5560);
+        otherwise (None) the structural pattern of every coupling."""
         import scipy.sparse as sp
         self.initialise()
-        self.assemble_device(with_jacobian=True)
-        self.check()
-        R = self.R_dev[:self.n_dof].cpu().numpy()
-        rp, ci = self.pattern()
-        vals = self.J_dev[:self.nnz].cpu().numpy()
+        thr = self.numerical_zero_for_sparse_assembly
+        if thr is None:
+            self.assemble_device(with_jacobian=True)
+            self.check()
+            R = self.R_dev[:self.n_dof].cpu().numpy()
+            rp, ci = self.pattern()
+            vals = self.J_dev[:self.nnz].cpu().numpy()
+            return R, sp.csr_matrix((vals, ci, rp), shape=(self.n_dof, self.n_dof))
+        R, rp, ci, vals = self.assemble_filtered(float(thr))
         return R, sp.csr_matrix((vals, ci, rp), shape=(self.n_dof, self.n_dof))
+
+    def assemble_filtered(self, threshold: float = 0.0):
+        """R and J in oomph's zero-filtered pattern (fe_assemble with
+        FE_ASSEMBLE_ZERO_FILTER): (R, rowptr, colidx, values) on the host."""
+        torch = _torch()
+        self.initialise()
+        L = N.load()
+        N.check(L.fe_problem_set_zero_threshold(self._h, float(threshold)))
+        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        flags = (N.FE_ASSEMBLE_RESIDUAL | N.FE_ASSEMBLE_JACOBIAN | N.FE_ASSEMBLE_VALUES_FROM_DOFS
+                 | N.FE_ASSEMBLE_ZERO_FILTER)
+        N.check(L.fe_assemble(self._h, self.x_dev.data_ptr(), self.R_dev.data_ptr(), self.J_dev.data_ptr(), flags,
+                              st))
+        self.check()
+        nnz = ctypes.c_int64()
+        rp = np.zeros(self.n_dof + 1, dtype=np.int32)
+        N.check(L.fe_problem_filtered_pattern(self._h, ctypes.byref(nnz), rp.ctypes.data, None, st))
+        ci = np.zeros(max(nnz.value, 1), dtype=np.int32)
+        N.check(L.fe_problem_filtered_pattern(self._h, None, None, ci.ctypes.data, st))
+        R = self.R_dev[:self.n_dof].cpu().numpy()
+        vals = self.J_dev[:nnz.value].cpu().numpy()
+        return R, rp, ci[:nnz.value], vals
 
     def get_parameter_derivative(self, name: str) -> np.ndarray:
         """dR/dp of one global parameter at the current dofs

@@ -114,3 +114,30 @@ def test_mesh_sizes_of_the_workloads():
     n, e, k = [O.ctypes.c_int64(), O.ctypes.c_int64(), O.ctypes.c_int()]
     O.lib().ofe_mesh_sizes(O.Q2_HEX, 48, 48, 48, O.ctypes.byref(n), O.ctypes.byref(e), O.ctypes.byref(k))
     assert n.value == 912673 and e.value == 110592
+
+
+@pytest.mark.parametrize("kind", ["poisson_q2", "poisson_p2", "ns_th", "nldiff_hex"])
+@pytest.mark.parametrize("threshold", [0.0, -1.0, 0.05])
+def test_vectors_of_pairs_restatement_matches_the_c_assembler(kind, threshold):
+    """oracle.vectors_of_pairs (the insertion loop over given element
+    matrices) gives the C oracle's CSR bit for bit, with and without the
+    zero filter: it can check the device's filtered compaction on the
+    product's own element matrices."""
+    import element_cases as C
+    from pyoomph_gb300 import workloads as W
+    P, ks, values, Rr, Jr = C.build(kind, "affine", "fp64")
+    m = P.mesh
+    if kind == "ns_th":
+        OP = O.navier_stokes_problem(O.mesh(O.P2_TRI, 4, 3), rho=1.0, mu=0.01)
+    else:
+        et, nx, dim = {"poisson_q2": (O.Q2_QUAD, (4, 3, 0), 2), "poisson_p2": (O.P2_TRI, (3, 4, 0), 2),
+                       "nldiff_hex": (O.Q2_HEX, (2, 2, 3), 3)}[kind]
+        eq = O.EQ_POISSON if kind.startswith("poisson") else O.EQ_NONLINEAR_DIFFUSION
+        OP = O.poisson_problem(O.mesh(et, *nx), W.draw_gaussians(3, 8, dim), eq=eq)
+    assert np.array_equal(OP.eqn, np.asarray(P.eqn).reshape(OP.eqn.shape))
+    OP.values[:] = values
+    R0, rp0, ci0, v0 = O.assemble(OP, True, threshold)
+    lay = ks.layout
+    eqns = OP.eqn[m.conn[:, lay.node], lay.val]
+    rp, ci, v = O.vectors_of_pairs(eqns, Jr, OP.n_dof, threshold)
+    assert np.array_equal(rp, rp0) and np.array_equal(ci, ci0) and np.array_equal(v, v0)
