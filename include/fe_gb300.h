@@ -207,6 +207,25 @@ int fe_problem_set_persistent(fe_problem_t *p, int enable);
 /* Parameter of the next FE_ASSEMBLE_DPARAM assembly (index into params). */
 int fe_problem_set_dparam(fe_problem_t *p, int index);
 
+/*
+ * Element Jacobians contracted on the tensor cores (tcgen05, 3xTF32 split,
+ * FP32 accumulation) for an FP32-Jacobian domain whose generated code writes
+ * the pulled-back pointwise derivatives Dhat instead of J_e.  Replaces the
+ * contraction loop of the reference's generated Jacobian
+ * (write_generic_RJM_jacobian_contribution, codegen.cpp:1883-2258):
+ *   J_e[i][j] = sum_q sum_p phi[q][pa[p]][i] Dhat_e[q][p] phi[q][pb[p]][j]
+ * phi: HOST [nq][nc][n] reference basis (value and d/ds components at the
+ * knots, local function order); pa/pb: HOST [npair] test/trial components.
+ * n <= 32, nq <= 32, npair <= 32, nc <= 4, nq x (active test components)
+ * <= 128.  fe_problem_set_tensor_contraction attaches it to a domain of a
+ * problem (its kernel must be generated for it); fe_tc_contract runs it once
+ * on caller buffers (DEVICE dhat [n_elem][nq][npair], jbuf [n_elem][n][n]).
+ */
+int fe_problem_set_tensor_contraction(fe_problem_t *p, int domain, int n, int nq, int nc, const double *phi, int npair,
+                                      const int32_t *pa, const int32_t *pb);
+int fe_tc_contract(const float *dhat, float *jbuf, int64_t n_elem, int n, int nq, int nc, const double *phi, int npair,
+                   const int32_t *pa, const int32_t *pb, void *stream);
+
 /* Threshold of FE_ASSEMBLE_ZERO_FILTER assemblies (oomph's
  * Problem::Numerical_zero_for_sparse_assembly, problem.cc:110; default 0.0,
  * must be >= 0). */

@@ -27,7 +27,7 @@ from __future__ import annotations
 
 import hashlib
 from dataclasses import dataclass, field
-from typing import Dict, List, Tuple
+from typing import Dict, List, Optional, Tuple
 
 import numpy as np
 import sympy as sp
@@ -358,12 +358,35 @@ class KernelSpec:
     jac_precision: str
     tables: np.ndarray = field(repr=False, default=None)
     sumfac_blocks: int = 0       # > 0: sum-factorised Jacobian with this many (a, b) blocks
+    # tensor-core contraction (csrc/fe_tc.cuh): the kernel writes the
+    # pulled-back derivatives Dhat (per knot, these (test, trial) reference
+    # components) and the library contracts them into J_e; None otherwise
+    tc_pairs: Optional[List[Tuple[int, int]]] = None
     gauss_sep: int = 0           # > 0: this many Gaussians of the source evaluated separably per element
     sum_fact_interp: bool = False  # interpolation and residual contraction sum-factorised (Q2 hex)
 
     @property
     def key(self) -> str:
         return hashlib.sha1(self.source.encode()).hexdigest()[:16]
+
+
+def tc_tables(ks: "KernelSpec"):
+    """(test components, trial components, phi [nq][1 + dim][n]) of a kernel
+    generated for the tensor-core contraction: the reference basis of its
+    single field (value and d/ds_b at the knots) in local order, and the
+    component pairs of its pulled-back derivatives."""
+    et, lay = ks.et, ks.layout
+    t = et.tables()
+    psi = np.asarray(t["PSI2"]).reshape(et.nq, et.nnode)
+    dps = np.asarray(t["DPS2"]).reshape(et.nq, et.nnode, et.dim)
+    node = np.asarray(lay.node)
+    phi = np.empty((et.nq, et.dim + 1, lay.n))
+    phi[:, 0, :] = psi[:, node]
+    for b in range(et.dim):
+        phi[:, 1 + b, :] = dps[:, node, b]
+    pa = np.array([a for a, _ in ks.tc_pairs], dtype=np.int32)
+    pb = np.array([b for _, b in ks.tc_pairs], dtype=np.int32)
+    return pa, pb, np.ascontiguousarray(phi)
 
 
 def _launch_shape(et: ElementType, nloc: int, per_elem_bytes: int, table_bytes: int,
@@ -393,7 +416,7 @@ def _launch_shape(et: ElementType, nloc: int, per_elem_bytes: int, table_bytes: 
 
 def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                     name: str = None, epb: int = None, affine: bool = False, jref: bool = None,
-                    gauss_sep: bool = False) -> KernelSpec:
+                    gauss_sep: bool = False, tc: bool = None) -> KernelSpec:
     """Fused element kernel for one element type and weak form.
 
     Thread phases (all in one launch, EPB elements per block):
@@ -407,6 +430,12 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
       B. one thread per (element, local row), rows ordered field-major so a
          warp shares its test field: R_i = sum_q rhat . phi_i and
          J_ij = sum_q phi_i^T D psi_j, written to the element buffers.
+
+    With ``tc`` (default: FP32 Jacobians of steady single-field forms on
+    elements of 17-32 local values, i.e. the Q2 hex) phase B builds no
+    Jacobian: the kernel writes the pulled-back derivatives Dhat of its
+    elements to ``a.dhat`` and the library contracts them on the tensor
+    cores (csrc/fe_tc.cuh, fe_problem_set_tensor_contraction).
 
     With ``jref`` (default: FP32 Jacobians, 3D elements, single-field
     forms) the Jacobian is contracted in
@@ -447,6 +476,12 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         # and for single-field forms; slower for the FP64 Taylor-Hood
         # Jacobian, whose pulled-back D is denser than D
         jref = jac_precision == "f32" or dim == 3 or nf == 1
+    tc_ok = bool(jac_precision == "f32" and jref and nf == 1 and spaces[0] == "C2" and not pw.transient
+                 and nloc <= 32 and nq <= 32)
+    use_tc = bool(tc_ok and nloc > 16) if tc is None else bool(tc)
+    if use_tc and not tc_ok:
+        raise ValueError("the tensor-core contraction needs an FP32 Jacobian in reference coordinates of a "
+                         "steady single-field (C2) form with at most 32 local values and 32 knots")
     # Dhat blocks (test field, trial field) -> rows/cols in reference components
     blocks: Dict[Tuple[int, int], List[Tuple[int, int, int]]] = {}
     for k, (tc, ic, _) in enumerate(pw.d_entries):
@@ -532,6 +567,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         raise ValueError(f"{epb} elements per block do not fit a block ({threads} threads, {smem} B shared)")
     if name is None:
         h = hashlib.sha1((et.name + jac_precision + str(affine) + str(epb) + str(jref) + str(sumfac) + str(gsep) +
+                          ("tc" if use_tc else "") +
                           str(sfi) + (str(pw.m_entries) if transient else "") +
                           str(pw.r_exprs) +
                           str(pw.d_entries)).encode()).hexdigest()[:10]
@@ -911,6 +947,16 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    }")
     w("  }")
     w("  __syncthreads();")
+    if use_tc:
+        # ---------------- phase T: Dhat out, for the tensor-core contraction ----------------
+        w("  if (flag == 1 || flag == 4) {")
+        w("    if (a.dhat == nullptr) {")
+        w("      if (threadIdx.x == 0) atomicExch(a.status, 4);   // no contraction buffer attached")
+        w("    } else {")
+        w("      float* dh = a.dhat + e0 * (FE_NQ * FE_NDNZH);")
+        w("      for (int k = threadIdx.x; k < nel * FE_NQ * FE_NDNZH; k += FE_NT) dh[k] = sD[k];")
+        w("    }")
+        w("  }")
     if sfi:
         SA, SB, SC = sfs
         # ---------------- phase R: sum-factorised residual ----------------
@@ -998,6 +1044,14 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w("    __syncthreads();")
         w("  }")
     # ---------------- phase B: field-major rows ----------------
+    if use_tc and sfi:
+        # the residual came from phase R, the Jacobian comes from the tensor cores
+        w("}")
+        source = "\n".join(src) + "\n"
+        return KernelSpec(name=name, source=source, et=et, layout=layout, pointwise=pw, epb=epb,
+                          threads=threads, smem_bytes=smem, jac_precision=jac_precision,
+                          tables=et.packed_tables(), sumfac_blocks=0, gauss_sep=gs_n if gsep else 0,
+                          sum_fact_interp=sfi, tc_pairs=[(ah, bh) for (_, _, ah, bh) in hat])
     w("  for (int p = threadIdx.x; p < nel * FE_NLOC; p += FE_NT) {")
     w("    int tf = 0, rel = p;")
     for f in range(nf - 1):
@@ -1027,7 +1081,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("      #pragma unroll")
         w("      for (int b = 0; b < FE_DIM; ++b) racc += rh[1 + b] * tdps[(q * tn + lt) * FE_DIM + b];")
         w("      Racc += racc;")
-    if sumfac:
+    if sumfac or use_tc:
         pass
     elif jref:
         w("      if (flag) {")
@@ -1127,13 +1181,13 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                         terms.append((f"a{ic}", f"dx[{ls * dim + c - 1}]"))
                 w(f"          Jr[{layout.loc_of[f][ls]}] {_jacc_update(terms, f'Jr[{layout.loc_of[f][ls]}]', jacc)};")
             w("        }")
-    if not sumfac:
+    if not (sumfac or use_tc):
         w("      }")
     w("    }")
     w("    const long long row = (e0 + el) * FE_NLOC + i;")
     if not sfi:
         w("    a.rbuf[row] = Racc;")
-    w("    if (flag) {")
+    w("    if (flag && !" + ("true" if use_tc else "false") + ") {")
     w("      jstore* jb = reinterpret_cast<jstore*>(a.jbuf) + row * FE_NLOC;")
     if sumfac:
         w("      const jacc* Jrow = sJe + el * 729 + i * 27;")
@@ -1148,7 +1202,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     return KernelSpec(name=name, source=source, et=et, layout=layout, pointwise=pw, epb=epb,
                       threads=threads, smem_bytes=smem, jac_precision=jac_precision,
                       tables=et.packed_tables(), sumfac_blocks=len(hat) if sumfac else 0,
-                      gauss_sep=gs_n if gsep else 0, sum_fact_interp=sfi)
+                      gauss_sep=gs_n if gsep else 0, sum_fact_interp=sfi,
+                      tc_pairs=[(ah, bh) for (_, _, ah, bh) in hat] if use_tc else None)
 
 
 def _jacc_update(terms, acc: str, jacc: str) -> str:
@@ -1218,6 +1273,17 @@ def estimate_flops(ks: KernelSpec, affine: bool) -> Dict[str, float]:
         # pulled-back D per knot, then per (a, b) block 3 x (81 + 243 + 729) multiply-adds
         jac_a = NQ * (ops_d + 4 * ks.sumfac_blocks)
         jac_b = ks.sumfac_blocks * 2 * 3 * (81 + 243 + 729)
+    if ks.tc_pairs:
+        # the contraction on the tensor cores: A = Dhat Phi built in FP32
+        # (2 flops per pair, knot and trial function), then the useful
+        # multiply-adds of J_e = Phi^T A (rows x rows x knots x active test
+        # components); each one runs as three TF32 products
+        nact = len({a_ for a_, _ in ks.tc_pairs})
+        jac_b = rows * NQ * len(ks.tc_pairs) * 2
+        out = {"fp64": float(fp64), "jac": float(jac_a + jac_b),
+               "tensor": float(2 * rows * rows * NQ * nact),
+               "tensor_issued": float(3 * 2 * 128 // 4 * 32 * (-(-(NQ * nact) // 8) * 8))}
+        return out
     out = {"fp64": float(fp64), "jac": float(jac_a + jac_b)}
     if ks.jac_precision == "f64":
         out["fp64"] += out["jac"]

@@ -26,6 +26,8 @@ struct FeElemArgs {
   int aux;                  // flag 3: index of the parameter of dR/dp
   long long n_nodes;        // nodes of the problem (bounds of conn entries)
   const double *dir;        // flag 4: nodal values of the direction y of the Hessian-vector product
+  float *dhat;              // [n_elem][nq][npair] pulled-back derivatives, written instead of J_e by
+                            // kernels whose Jacobian is contracted on the tensor cores (fe_tc.cuh)
 };
 
 // One launch over several domains (bulk, interface, contact line ...): block

@@ -36,6 +36,7 @@
 #include "../../include/fe_gb300.h"
 #include "fe_abi.h"
 #include "fe_df64.cuh"
+#include "fe_tc.cuh"
 
 #define FE_VERSION "fe_gb300 0.1.0 (sm_103a)"
 
@@ -511,6 +512,10 @@ struct Domain {
   long long jbase = 0; // flat offset of this domain's entries in the global contribution space
   long long rbase = 0;
   std::vector<int32_t> local_node, local_val;
+  // tensor-core contraction of the Jacobian (fe_problem_set_tensor_contraction)
+  bool tc = false;
+  FeTcArgs tca;
+  DevBuf tc_dhat, tc_phi, tc_bhi, tc_blo;
 };
 
 struct fe_problem {
@@ -933,7 +938,106 @@ FeElemArgs domain_args(fe_problem *p, Domain &d, int flag) {
   a.aux = p->dparam;
   a.n_nodes = p->n_nodes;
   a.dir = p->dir.p ? p->dir.as<double>() : p->values.as<double>();
+  a.dhat = d.tc ? d.tc_dhat.as<float>() : nullptr;
   return a;
+}
+
+// ---------------------------------------------------------------------------
+// tensor-core contraction (fe_tc.cuh): tables and launch
+// ---------------------------------------------------------------------------
+// nearest TF32 (ties away from zero) of a float: the high part of the split
+float tf32_round_host(float x) {
+  uint32_t b;
+  memcpy(&b, &x, 4);
+  b = (b + 0x1000u) & 0xFFFFE000u;
+  float r;
+  memcpy(&r, &b, 4);
+  return r;
+}
+
+// validates the description and fills the arguments: phi [nq][nc][n] (local
+// order) becomes the staged table [nq][nc][32] and the B operand pieces in
+// the shared-memory layout [kp/4][32][4]
+int tc_setup(FeTcArgs &A, DevBuf &phi_d, DevBuf &bhi_d, DevBuf &blo_d, int n, int nq, int nc, const double *phi,
+             int npair, const int32_t *pa, const int32_t *pb) {
+  if (n < 1 || n > FE_TC_N || nq < 1 || nq > FE_TC_MAXQ || nc < 1 || nc > FE_TC_MAXC || npair < 1 ||
+      npair > FE_TC_MAXP || !phi || !pa || !pb)
+    return fail(FE_ERR_ARG, "tensor contraction: sizes out of range (n %d, nq %d, nc %d, npair %d)", n, nq, nc, npair);
+  memset(&A, 0, sizeof(A));
+  for (int p_ = 0; p_ < npair; p_++)
+    if (pa[p_] < 0 || pa[p_] >= nc || pb[p_] < 0 || pb[p_] >= nc)
+      return fail(FE_ERR_ARG, "tensor contraction: pair %d has components out of range", p_);
+  // the active test components (those some pair tests with), each with its
+  // pairs (Dhat index, trial component)
+  int nact = 0;
+  std::vector<int> act;
+  for (int c = 0; c < nc; c++) {
+    int nt = 0;
+    for (int p_ = 0; p_ < npair; p_++)
+      if (pa[p_] == c) {
+        A.tp[nact][nt] = p_;
+        A.tb[nact][nt] = pb[p_];
+        nt++;
+      }
+    if (nt) {
+      A.nterm[nact++] = nt;
+      act.push_back(c);
+    }
+  }
+  const int K = nq * nact, kp = (K + 7) / 8 * 8;
+  if (kp > FE_TC_MAXK) return fail(FE_ERR_ARG, "tensor contraction: K = %d exceeds %d", K, FE_TC_MAXK);
+  A.n = n;
+  A.nq = nq;
+  A.nc = nc;
+  A.npair = npair;
+  A.nact = nact;
+  A.kp = kp;
+  std::vector<float> ph((size_t)nq * nc * FE_TC_N, 0.0f), bhi((size_t)kp * FE_TC_N, 0.0f), blo(bhi.size(), 0.0f);
+  for (int q = 0; q < nq; q++)
+    for (int c = 0; c < nc; c++)
+      for (int i = 0; i < n; i++) ph[((size_t)q * nc + c) * FE_TC_N + i] = (float)phi[((size_t)q * nc + c) * n + i];
+  for (int k = 0; k < K; k++) {
+    const int q = k / nact, c = act[k % nact];
+    for (int i = 0; i < n; i++) {
+      const double v = phi[((size_t)q * nc + c) * n + i];
+      const float hi = tf32_round_host((float)v);
+      const size_t at = (size_t)(k / 4) * (FE_TC_N * 4) + (size_t)i * 4 + (k % 4);
+      bhi[at] = hi;
+      blo[at] = (float)(v - (double)hi);
+    }
+  }
+  int rc;
+  if ((rc = phi_d.upload(ph.data(), sizeof(float) * ph.size())) || (rc = bhi_d.upload(bhi.data(), sizeof(float) * bhi.size())) ||
+      (rc = blo_d.upload(blo.data(), sizeof(float) * blo.size())))
+    return rc;
+  A.phi = phi_d.as<float>();
+  A.b_hi = bhi_d.as<float>();
+  A.b_lo = blo_d.as<float>();
+  const fe_tc::Plan pl = fe_tc::plan(kp, nq, npair, nc);
+  if (pl.total > 227 * 1024) return fail(FE_ERR_ARG, "tensor contraction: %u bytes of shared memory", pl.total);
+  CUDA_TRY(cudaFuncSetAttribute((const void *)k_tc_contract, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)pl.total));
+  return FE_OK;
+}
+
+int tc_launch(const FeTcArgs &A, cudaStream_t st) {
+  if (A.n_elem <= 0) return FE_OK;
+  const long long tiles = (A.n_elem + FE_TC_EPT - 1) / FE_TC_EPT;
+  const int grid = (int)std::min<long long>(tiles, sm_count_cached());
+  const fe_tc::Plan pl = fe_tc::plan(A.kp, A.nq, A.npair, A.nc);
+  k_tc_contract<<<grid, FE_TC_THREADS, pl.total, st>>>(A);
+  CUDA_TRY(cudaGetLastError());
+  return FE_OK;
+}
+
+// the tensor-core contraction of domain d over elements [e0, e1)
+int tc_domain(fe_problem *p, Domain &d, long long e0, long long e1, cudaStream_t st) {
+  FeTcArgs A = d.tca;
+  A.dhat = d.tc_dhat.as<float>() + e0 * (long long)A.nq * A.npair;
+  A.jbuf = p->jbuf_all.as<float>() + d.jbase + e0 * (long long)d.nlocal * d.nlocal;
+  A.status = p->status.as<int>();
+  A.n_elem = e1 - e0;
+  return tc_launch(A, st);
 }
 
 int launch_elements(fe_problem *p, int flag, cudaStream_t st) {
@@ -1461,6 +1565,9 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
   if (p->timing) CUDA_TRY(cudaEventRecord(ev[1], st));
   int rc = launch_elements(p, eflag, st);
   if (rc) return rc;
+  if (eflag == 1 || eflag == 4)
+    for (Domain &d : p->domains)
+      if (d.tc && (rc = tc_domain(p, d, 0, d.n_elem, st))) return rc;
   if (p->timing) CUDA_TRY(cudaEventRecord(ev[2], st));
   if (want_r && p->rw.p) {
     k_gather_rows_w<<<grid_for(p->n_dof, 256, sms), 256, 0, st>>>(p->rptr.as<unsigned>(), p->ridx.as<unsigned>(),
@@ -1654,9 +1761,11 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
       a.rbuf += e0 * d.nlocal;
       a.jbuf = (char *)a.jbuf + jel * (size_t)(e0 * (long long)d.nlocal * d.nlocal);
       a.n_elem = e1 - e0;
+      if (d.tc) a.dhat += e0 * (long long)d.tca.nq * d.tca.npair;
       void *kp[] = {&a};
       unsigned grid = (unsigned)((a.n_elem + d.epb - 1) / d.epb);
       CUDA_TRY(cudaLaunchKernel((const void *)d.code->func, dim3(grid), dim3(d.threads), kp, (size_t)d.smem, st));
+      if (want_j && d.tc && (rc = tc_domain(p, d, e0, e1, st))) return rc;
     }
     for (const auto &run : p->pipe_runs[k]) {
       const long long r0 = run.first, r1 = run.second;
@@ -1709,6 +1818,44 @@ int fe_problem_set_direction(fe_problem_t *p, const double *y, void *stream) {
   CUDA_TRY(cudaMemsetAsync(p->dir.p, 0, sizeof(double) * n, st)); // pinned values: zero direction
   k_scatter_dofs<<<grid_for(n, 256, sm_count_cached()), 256, 0, st>>>(y, p->eqn.as<int>(), p->dir.as<double>(), n);
   CUDA_TRY(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_problem_set_tensor_contraction(fe_problem_t *p, int domain, int n, int nq, int nc, const double *phi, int npair,
+                                      const int32_t *pa, const int32_t *pb) {
+  if (!p || domain < 0 || domain >= (int)p->domains.size()) return fail(FE_ERR_ARG, "bad problem or domain");
+  if (p->jac_prec != FE_JAC_F32) return fail(FE_ERR_ARG, "tensor contraction: FP32 Jacobians only");
+  if (p->fused) return fail(FE_ERR_ARG, "tensor contraction: fixed-mesh (unfused) code only");
+  Domain &d = p->domains[domain];
+  if (n != d.nlocal) return fail(FE_ERR_ARG, "tensor contraction: n %d != the domain's %d local values", n, d.nlocal);
+  int rc;
+  if ((rc = tc_setup(d.tca, d.tc_phi, d.tc_bhi, d.tc_blo, n, nq, nc, phi, npair, pa, pb))) return rc;
+  if ((rc = d.tc_dhat.alloc(sizeof(float) * std::max(1LL, d.n_elem * (long long)nq * npair)))) return rc;
+  CUDA_TRY(cudaMemset(d.tc_dhat.p, 0, d.tc_dhat.bytes));
+  d.tc = true;
+  return FE_OK;
+}
+
+int fe_tc_contract(const float *dhat, float *jbuf, int64_t n_elem, int n, int nq, int nc, const double *phi, int npair,
+                   const int32_t *pa, const int32_t *pb, void *stream) {
+  if ((!dhat || !jbuf) && n_elem > 0) return fail(FE_ERR_ARG, "fe_tc_contract: null buffer");
+  int rc = ensure_context();
+  if (rc) return rc;
+  FeTcArgs A;
+  DevBuf ph, bhi, blo, status;
+  if ((rc = tc_setup(A, ph, bhi, blo, n, nq, nc, phi, npair, pa, pb))) return rc;
+  if ((rc = status.alloc(sizeof(int)))) return rc;
+  CUDA_TRY(cudaMemset(status.p, 0, sizeof(int)));
+  A.dhat = dhat;
+  A.jbuf = jbuf;
+  A.status = status.as<int>();
+  A.n_elem = n_elem;
+  cudaStream_t st = (cudaStream_t)stream;
+  if ((rc = tc_launch(A, st))) return rc;
+  CUDA_TRY(cudaStreamSynchronize(st));
+  int sw = 0;
+  CUDA_TRY(cudaMemcpy(&sw, status.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (sw) return fail(FE_ERR_DEVICE, "fe_tc_contract: status word %d (a bounded wait gave up)", sw);
   return FE_OK;
 }
 
@@ -1898,6 +2045,9 @@ int fe_problem_launch_count(const fe_problem_t *p, int flags) {
       if (d.n_elem) n++;
   }
   if (flags & (FE_ASSEMBLE_RESIDUAL | FE_ASSEMBLE_DPARAM)) n++;
+  if (flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_HVP))
+    for (const Domain &d : p->domains)
+      if (d.tc && d.n_elem) n++;
   if ((flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS | FE_ASSEMBLE_HVP)) && p->nnz > 0)
     n += (flags & FE_ASSEMBLE_ZERO_FILTER) ? 6 : 1;   // filtered gather, ranks, three scan launches, scatter
   if (p->n_hang > 0) n++;

@@ -263,6 +263,9 @@ class Problem:
         # contract the Jacobian in reference coordinates (None: the generator's
         # default, on for 3D elements)
         self.jacobian_reference: Optional[bool] = None
+        # contract FP32 element Jacobians on the tensor cores (None: where the
+        # generator supports it and it pays, the Q2 hex's 27 x 27 matrices)
+        self.tensor_cores: Optional[bool] = None
         # linear_solver = "bicgstab": J dx = R solved on the device (linsolve.py)
         # to this relative tolerance; None: SuperLU on the host (the reference's default)
         self.linear_solver_tolerance = 1e-13
@@ -401,12 +404,12 @@ class Problem:
         # geometry kind only -- not on the mesh size: cache it per process
         gsep = bool(self.separable_source and self.affine and mesh_is_axis_aligned(mesh))
         key = (mesh.etype.name, tuple(fields), str(integrand), tuple(used), kprec, self.affine, gsep,
-               self.is_transient, self.elems_per_block, self.jacobian_reference)
+               self.is_transient, self.tensor_cores, self.elems_per_block, self.jacobian_reference)
         ks = _KERNEL_CACHE.get(key)
         if ks is None:
             pw = differentiate(fields, mesh.dim, integrand, used)
             ks = generate_kernel(mesh.etype, pw, kprec, epb=self.elems_per_block, affine=self.affine,
-                                 jref=self.jacobian_reference, gauss_sep=gsep)
+                                 jref=self.jacobian_reference, gauss_sep=gsep, tc=self.tensor_cores)
             _KERNEL_CACHE[key] = ks
         if self.elems_per_block is None and int(self.replicas) == 1:
             # balance the waves: with W = ceil(E / (SMs x EPB)) waves of one
@@ -426,7 +429,7 @@ class Problem:
                 if ks2 is None:
                     ks2 = generate_kernel(mesh.etype, differentiate(fields, mesh.dim, integrand, used), kprec,
                                           epb=epb, affine=self.affine, jref=self.jacobian_reference,
-                                          gauss_sep=gsep)
+                                          gauss_sep=gsep, tc=self.tensor_cores)
                     _KERNEL_CACHE[key2] = ks2
                 ks = ks2
         self.kernel: KernelSpec = ks
@@ -554,6 +557,10 @@ class Problem:
         h = ctypes.c_void_p()
         N.check(L.fe_problem_create(ctypes.byref(desc), ctypes.byref(h)))
         self._h = h
+        if self.kernel.tc_pairs:
+            pa, pb, phi = self.tensor_contraction_tables()
+            N.check(L.fe_problem_set_tensor_contraction(h, 0, self.kernel.layout.n, mesh.etype.nq, mesh.dim + 1,
+                                                        phi.ctypes.data, len(pa), pa.ctypes.data, pb.ctypes.data))
         N.check(L.fe_problem_set_values(h, values.ctypes.data))
         nd = ctypes.c_int64()
         nnz = ctypes.c_int64()
@@ -570,6 +577,11 @@ class Problem:
         t4 = time.perf_counter()
         self.timings.update(jit_s=t3 - t2, device_setup_s=t4 - t3)
         self._initialised = True
+
+    def tensor_contraction_tables(self):
+        """The tables of the tensor-core contraction (codegen.tc_tables)."""
+        from .codegen import tc_tables
+        return tc_tables(self.kernel)
 
     def _descriptors(self, with_code: bool):
         mesh = self.mesh

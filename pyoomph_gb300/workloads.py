@@ -113,6 +113,9 @@ def _main(argv=None) -> None:
     ap.add_argument("--epb", type=int, default=None, help="elements per block (default: the generator's)")
     ap.add_argument("--jref", type=int, choices=[0, 1], default=None,
                     help="1: contract the Jacobian in reference coordinates, 0: physical (default: the generator's)")
+    ap.add_argument("--tc", type=int, choices=[0, 1], default=None,
+                    help="1: FP32 Jacobian contracted on the tensor cores, 0: on the FP32 pipes "
+                         "(default: the generator's)")
     ap.add_argument("--transient", action="store_true",
                     help="the transient form (BDF2 weights of dt = 1e-3, both previous levels = the current values)")
     a = ap.parse_args(argv)
@@ -125,6 +128,8 @@ def _main(argv=None) -> None:
     P.elems_per_block = a.epb
     if a.jref is not None:
         P.jacobian_reference = bool(a.jref)
+    if a.tc is not None:
+        P.tensor_cores = bool(a.tc)
     P.initialise()
     perturb_dofs(P, seed=0, sigma=1e-3)
     if a.transient:

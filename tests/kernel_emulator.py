@@ -67,7 +67,8 @@ class _Args(ctypes.Structure):
                 ("jbuf", ctypes.c_void_p), ("n_elem", ctypes.c_longlong), ("nval", ctypes.c_int),
                 ("flag", ctypes.c_int), ("status", ctypes.c_void_p), ("replica_elems", ctypes.c_longlong),
                 ("params_stride", ctypes.c_int), ("hist", ctypes.c_void_p), ("x0", ctypes.c_void_p),
-                ("n_hist", ctypes.c_int), ("hist_stride", ctypes.c_longlong), ("aux", ctypes.c_int), ("n_nodes", ctypes.c_longlong), ("dir", ctypes.c_void_p)]
+                ("n_hist", ctypes.c_int), ("hist_stride", ctypes.c_longlong), ("aux", ctypes.c_int), ("n_nodes", ctypes.c_longlong), ("dir", ctypes.c_void_p),
+                ("dhat", ctypes.c_void_p)]
 
 
 def build(ks) -> ctypes.CDLL:
@@ -116,11 +117,21 @@ def run(ks, x, conn, values, params, flag: int = 1, direction=None, aux: int = 0
         hist = np.ascontiguousarray(hist, dtype=np.float64)
         assert hist.shape[1:] == values.shape
         nh = hist.shape[0]
+    dhat = None
+    if ks.tc_pairs:
+        # the kernel writes the pulled-back derivatives; the tensor-core
+        # contraction (csrc/fe_tc.cuh) is emulated exactly below
+        dhat = np.zeros((E, ks.et.nq, len(ks.tc_pairs)), dtype=np.float32)
     a = _Args(x.ctypes.data, conn.ctypes.data, values.ctypes.data, params.ctypes.data, tables.ctypes.data,
               rbuf.ctypes.data, jbuf.ctypes.data, E, values.shape[1], flag, status.ctypes.data, 0, 0,
               None if hist is None else hist.ctypes.data, None, nh, values.size, aux,
-              x.shape[0], values.ctypes.data if direction is None else direction.ctypes.data)
+              x.shape[0], values.ctypes.data if direction is None else direction.ctypes.data,
+              None if dhat is None else dhat.ctypes.data)
     L.fe_emu_run(ctypes.byref(a), (E + ks.epb - 1) // ks.epb)
+    if ks.tc_pairs and flag in (1, 4):
+        from pyoomph_gb300.codegen import tc_tables
+        pa, pb, phi = tc_tables(ks)
+        jbuf[:] = np.einsum("qpi,eqp,qpj->eij", phi[:, pa, :], dhat.astype(np.float64), phi[:, pb, :])
     return rbuf, jbuf, status
 
 
@@ -178,7 +189,7 @@ def run_fused(fk, conns, values, hist, x0, params, flag: int = 1, aux: int = 0, 
         fa.d[k] = _Args(x0.ctypes.data, conn.ctypes.data, values.ctypes.data, params.ctypes.data,
                         tables.ctypes.data, rbuf.ctypes.data, jbuf.ctypes.data, E, nval, flag,
                         status.ctypes.data, 0, 0, hist_arr.ctypes.data, x0.ctypes.data, len(hist),
-                        values.size, aux, values.shape[0], values.ctypes.data)
+                        values.size, aux, values.shape[0], values.ctypes.data, None)
         fa.block_start[k] = nb
         nb += (E + dc.epb - 1) // dc.epb
     fa.block_start[len(fk.domains)] = nb
