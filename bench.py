@@ -490,16 +490,172 @@ def run_gb300(args):
                 "linear_solver": "native batched Jacobi-BiCGStab (fe_krylov_solve: fe_csr_spmv + fused "
                                  "vector kernels, CUDA-graph blocks of 8 iterations)"}
             del PN, A
+    if args.workload == "ns" and world == 1:
+        # the whole Newton solve of the Navier-Stokes problem on the device
+        # (fieldsplit.py: GMRES with the block-triangular multigrid
+        # preconditioner) from the perturbed state to max |R| < 1e-10, with
+        # the FP64 and the FP32 Jacobian; a small solve first loads the kernels
+        PW = make_problem("ns", 8, "fp64")
+        PW.linear_solver = "fieldsplit"
+        PW.solve()
+        del PW
+        sols = {}
+        for prec in ("fp64", "fp32"):
+            PN = make_problem("ns", args.size, prec)
+            PN.linear_solver = "fieldsplit"
+            PN.newton_solver_tolerance = 1e-10
+            PN.max_newton_iterations = 30
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            PN.assemble_device(with_jacobian=True)
+            PN._fieldsplit_solver().setup()          # the multigrid hierarchy (host, once per mesh)
+            t_setup = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            hist = PN.solve()
+            torch.cuda.synchronize()
+            t_solve = time.perf_counter() - t0
+            sols[prec] = PN.get_dofs()
+            line.setdefault("newton_device_solve", {})[prec] = {
+                "s": t_solve, "preconditioner_setup_s": t_setup, "n_dof": PN.n_dof,
+                "newton_iterations": len(hist) - 1, "residuals": hist,
+                "krylov_iterations": PN.timings.get("krylov_iterations"),
+                "linear_solve_s": PN.timings.get("newton_linear_solve_s"),
+                "multigrid_levels": PN._fieldsplit.sizes,
+                "linear_solver": "GMRES(60), block upper-triangular preconditioner: smoothed-aggregation V-cycle "
+                                 "on the velocity block, lumped pressure mass / viscosity for the Schur complement "
+                                 "(fieldsplit.py)"}
+            del PN
+        line["newton_device_solve"]["max_rel_solution_difference_fp32_vs_fp64_jacobian"] = float(
+            np.max(np.abs(sols["fp32"] - sols["fp64"])) / np.max(np.abs(sols["fp64"])))
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        # the checker and the CPU baseline, after every timed region
+        # the checker, after every timed region
         line["parity"] = parity_vs_oracle(args, results)
         if "fp32" in line["parity"]:
             line["fp32_jacobian"]["max_rel_jacobian_error_vs_fp64_oracle"] = line["parity"]["fp32"].get("max_rel_J")
+    if rank == 0 and world == 1 and args.workload == "ns" and not args.no_extras:
+        # the other workloads of the survey, measured in this same run (after
+        # the headline's timed regions): Poisson Q2 64^2, the Q2 hex 48^3
+        # (FP32 Jacobian on the tensor cores), the moving-mesh droplet and a
+        # bounded serving stream
+        extras = {}
+        for wl in ("poisson", "hex"):
+            extras[wl] = measure_extra(wl, WORKLOADS[wl][1], args.steps, args.warmup, hbm_peak, peak64)
+        extras["droplet"] = measure_droplet_compact(WORKLOADS["droplet"][1], args.steps, args.warmup, hbm_peak,
+                                                    peak64)
+        extras["serving"] = measure_serving_bounded()
+        line["other_workloads"] = extras
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, threads=1)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def measure_extra(workload: str, size: int, steps: int, warmup: int, hbm_peak: float, peak64: float,
+                  with_parity: bool = True):
+    """A compact record of another workload in the same run: per Jacobian
+    precision the device-resident step, the element kernel (and, for the
+    tensor-core contraction, its own kernel), the end-to-end step through
+    the host-buffer API, flop rates; full-size parity against the oracle;
+    for Poisson and the hex the whole Newton solve on the device."""
+    import torch
+    from types import SimpleNamespace
+    from pyoomph_gb300.codegen import estimate_flops
+    out = {"workload": WORKLOADS[workload][0], "mesh_side": size}
+    results = {}
+    for prec in ("fp64", "fp32", "df64"):
+        P = make_problem(workload, size, prec)
+        E = P.mesh.n_elem
+        asm = lambda: P.assemble_device(with_jacobian=True)
+        ms = time_steps(torch, asm, steps, warmup)
+        P.check()
+        P.set_stage_timing(True)
+        for _ in range(5):
+            asm()
+        st, calls = P.stage_times()
+        P.set_stage_timing(False)
+        st = st / max(calls, 1)
+        xh = torch.from_numpy(P.get_dofs()).pin_memory()
+        Rh = torch.empty(P.n_dof, dtype=torch.float64).pin_memory()
+        Jh = torch.empty(P.nnz, dtype=P.J_dev.dtype).pin_memory()
+        ms_e2e = time_steps(torch, lambda: P.assemble_host(xh, Rh, Jh, True, chunks=4), steps, warmup)
+        P.check()
+        fl = estimate_flops(P.kernel, P.affine)
+        d = {"ms_per_step": ms, "value": E / (ms / 1e3), "unit": "elements/s", "kernel": P.kernel.name,
+             "element_kernel_ms": float(st[1]), "jacobian_gather_ms": float(st[3]),
+             "e2e": {"value": E / (ms_e2e / 1e3), "ms_per_step": ms_e2e, "h2d_bytes_per_step": int(P.n_dof * 8),
+                     "d2h_bytes_per_step": int(P.n_dof * 8 + P.nnz * P.J_dev.element_size()),
+                     "api": "Problem.assemble_host (fe_assemble_pipelined)"},
+             "fp64_tflops": fl["fp64"] * E / (float(st[1]) / 1e3) / 1e12,
+             "fp64_frac_of_dgemm": fl["fp64"] * E / (float(st[1]) / 1e3) / 1e12 / peak64,
+             "roofline_hbm_frac": element_algorithmic_bytes(P) / (float(st[1]) / 1e3) / 1e9 / hbm_peak}
+        if P.kernel.tc_pairs:
+            d["tensor_cores"] = {
+                "kernel": "k_tc_contract (tcgen05.mma kind::tf32, 3xTF32 split)",
+                "ms": float(st[4]), "useful_tflops": fl["tensor"] * E / (float(st[4]) / 1e3) / 1e12,
+                "issued_tflops": fl["tensor_issued"] * E / 4 / (float(st[4]) / 1e3) / 1e12,
+                "useful_flops_per_element": fl["tensor"]}
+        results[prec] = {"P": P}
+        out[prec] = d
+    n_elem = results["fp64"]["P"].mesh.n_elem
+    out.update(n_elem=n_elem, n_dof=results["fp64"]["P"].n_dof, nnz=results["fp64"]["P"].nnz)
+    if with_parity:
+        out["parity"] = parity_vs_oracle(SimpleNamespace(workload=workload, size=size), results)
+    for r in results.values():
+        del r["P"]
+    if workload in ("hex", "poisson"):
+        out["newton_device_solve"] = {}
+        for prec in ("fp64", "fp32"):
+            PN = make_problem(workload, size, prec)
+            PN.set_dofs(np.zeros(PN.n_dof))
+            PN.linear_solver = "bicgstab"
+            PN.newton_solver_tolerance = 1e-10
+            PN.max_newton_iterations = 20
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            hist = PN.solve()
+            torch.cuda.synchronize()
+            out["newton_device_solve"][prec] = {
+                "s": time.perf_counter() - t0, "newton_iterations": len(hist) - 1, "residuals": hist,
+                "krylov_iterations": PN.timings.get("krylov_iterations")}
+            del PN
+    return out
+
+
+def measure_serving_bounded(requests: int = 200, rate: float = 50.0, side_max: int = 64, seq_requests: int = 40):
+    """A bounded serving stream: Poisson-process arrivals of Poisson and
+    Navier-Stokes assemble+Newton requests (sides log-uniform in
+    [16, side_max]) through the continuous-batching FP32-Jacobian server
+    (Poisson requests solved on the device, Navier-Stokes ones by SuperLU
+    in worker processes), and the plain FP64 one-request-at-a-time path on
+    the first seq_requests of the same stream."""
+    import copy
+    from pyoomph_gb300 import serving as S
+    workers = max(1, (os.cpu_count() or 2) - 2)
+    for kind in ("poisson", "ns"):
+        for prec in ("fp32", "fp64"):
+            S._class_problem(kind, 8, prec, 1).initialise()
+    reqs = S.make_stream(requests, rate=rate, seed=0, side_range=(16, side_max), ns_side_max=side_max)
+    srv = S.Server(slots=4, jacobian_precision="fp32", workers=workers, device_solver=True)
+    t0 = time.perf_counter()
+    done = srv.run(copy.deepcopy(reqs))
+    wall = time.perf_counter() - t0
+    out = {"requests": requests, "rate_per_s": rate, "side_range": [16, side_max], "wall_s": wall,
+           "batched_fp32": S.summary(done, wall), "assemblies": srv.assemblies,
+           "gpu_launches": srv.launches + srv.solver_launches, "device_solves": srv.device_solves,
+           "linear_solver": f"Poisson: native batched BiCGStab on the device; Navier-Stokes: SuperLU, {workers} "
+                            f"worker processes"}
+    srv.close()
+    sub = copy.deepcopy(reqs[:seq_requests])
+    t0 = time.perf_counter()
+    seq = S.serve_sequential(sub, precision="fp64", device_solver=True)
+    wall2 = time.perf_counter() - t0
+    out["sequential_fp64_first_requests"] = dict(S.summary(seq, wall2), requests=seq_requests)
+    by = {r.rid: r.dofs for r in done}
+    out["max_rel_solution_difference_batched_vs_sequential"] = max(
+        float(np.max(np.abs(by[r.rid] - r.dofs)) / max(1.0, float(np.max(np.abs(r.dofs))))) for r in seq)
+    return out
 
 
 def _oracle_problem(workload: str, side: int):
@@ -785,6 +941,52 @@ def run_droplet(args):
     print(json.dumps(line), flush=True)
 
 
+def measure_droplet_compact(size: int, steps: int, warmup: int, hbm_peak: float, peak64: float):
+    """The moving-mesh droplet's fused assembly (bulk + interface + contact
+    line in one launch) per Jacobian precision, device-resident and end to
+    end; df64's Jacobian against the FP64 one on the same state."""
+    import torch
+    out = {"workload": WORKLOADS["droplet"][0], "mesh_side": size}
+    Ps = {}
+    for prec in ("fp64", "fp32", "df64"):
+        P, theta = droplet_problem(size, prec)
+        asm = lambda: P.assemble_device(with_jacobian=True)
+        ms = time_steps(torch, asm, steps, warmup)
+        P.check()
+        P.set_stage_timing(True)
+        for _ in range(5):
+            asm()
+        st, calls = P.stage_times()
+        P.set_stage_timing(False)
+        st = st / max(calls, 1)
+        xh = P.x_dev[:P.n_dof].cpu().pin_memory()
+        Rh = torch.empty(P.n_dof, dtype=torch.float64).pin_memory()
+        Jh = torch.empty(P.nnz, dtype=P.J_dev.dtype).pin_memory()
+
+        def e2e():
+            P.x_dev[:P.n_dof].copy_(xh, non_blocking=True)
+            P.assemble_device(with_jacobian=True)
+            Rh.copy_(P.R_dev[:P.n_dof], non_blocking=True)
+            Jh.copy_(P.J_dev[:P.nnz], non_blocking=True)
+
+        ms_e2e = time_steps(torch, e2e, steps, warmup)
+        flops = sum(dc.flops * c.shape[0] for dc, c in zip(P.domains, P.conns))
+        out[prec] = {"ms_per_step": ms, "value": P.n_elem / (ms / 1e3), "unit": "elements/s",
+                     "element_kernel_fused_ms": float(st[1]), "kernel": P.kernel.name,
+                     "e2e": {"value": P.n_elem / (ms_e2e / 1e3), "ms_per_step": ms_e2e,
+                             "h2d_bytes_per_step": int(P.n_dof * 8),
+                             "d2h_bytes_per_step": int(P.n_dof * 8 + P.nnz * P.J_dev.element_size())}}
+        if prec == "fp64":
+            out[prec]["fp64_frac_of_dgemm"] = flops / (float(st[1]) / 1e3) / 1e12 / peak64
+        Ps[prec] = P
+        out.update(n_elem=P.n_elem, n_dof=P.n_dof, nnz=P.nnz, contact_angle_deg=theta)
+    Ps["fp64"].assemble_device(with_jacobian=True)
+    Ps["df64"].assemble_device(with_jacobian=True)
+    Jf, Jd = Ps["fp64"].J_dev[:Ps["fp64"].nnz], Ps["df64"].J_dev[:Ps["df64"].nnz]
+    out["df64_max_rel_jacobian_difference_vs_fp64"] = float((Jd - Jf).abs().max() / Jf.abs().max())
+    return out
+
+
 def droplet_cpu_baseline(size: int, seconds: float = 10.0):
     """The ALE oracle (numpy, vectorised over elements, complex-step
     Jacobians) on one host core: element residuals and Jacobians of the
@@ -868,6 +1070,8 @@ def main():
     ap.add_argument("--workload", default="ns", choices=list(WORKLOADS))
     ap.add_argument("--size", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default NS run: skip the other workloads' compact records")
     ap.add_argument("--autotune", action="store_true", help="time the element kernels' launch shapes first")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--rates", default="10,20,50")

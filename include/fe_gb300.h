@@ -226,6 +226,21 @@ int fe_problem_set_tensor_contraction(fe_problem_t *p, int domain, int n, int nq
 int fe_tc_contract(const float *dhat, float *jbuf, int64_t n_elem, int n, int nq, int nc, const double *phi, int npair,
                    const int32_t *pa, const int32_t *pb, void *stream);
 
+/*
+ * Aggregation of the unknowns of a square CSR matrix (HOST arrays) for a
+ * smoothed-aggregation multigrid preconditioner of the velocity block of a
+ * saddle-point Jacobian (no counterpart on the reference's path, which
+ * solves with SuperLU, pyoomph/solvers/scipy.py).  i and j are strongly
+ * coupled when comp[i] == comp[j] and |a_ij| >= theta sqrt(|a_ii a_jj|).
+ * Three passes in index order (deterministic): a free unknown whose strong
+ * neighbours are all free starts an aggregate with them; a remaining
+ * unknown joins the aggregate of its first aggregated strong neighbour; the
+ * rest start aggregates with their free strong neighbours.  agg[i] in
+ * [0, *n_agg).
+ */
+int fe_sa_aggregate(int64_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
+                    const int32_t *comp, double theta, int32_t *agg, int64_t *n_agg);
+
 /* Threshold of FE_ASSEMBLE_ZERO_FILTER assemblies (oomph's
  * Problem::Numerical_zero_for_sparse_assembly, problem.cc:110; default 0.0,
  * must be >= 0). */
@@ -387,10 +402,11 @@ int fe_problem_check(fe_problem_t *p);
 
 /*
  * Stage tracing.  With timing enabled, fe_assemble records CUDA events on
- * its stream around its four stages; fe_problem_stage_times synchronises,
+ * its stream around its stages; fe_problem_stage_times synchronises,
  * returns the summed milliseconds per stage since the last query
  * (ms[0] dof scatter, ms[1] element kernels, ms[2] residual gather,
- * ms[3] Jacobian gather) and the number of calls, and resets the sums.
+ * ms[3] Jacobian gather, ms[4] tensor-core contraction of the element
+ * matrices; ms has room for 5) and the number of calls, and resets the sums.
  * The counterpart of oomph's Jacobian_setup_time (linear_solver.cc:884-894).
  */
 int fe_problem_set_timing(fe_problem_t *p, int enable);

@@ -1259,7 +1259,7 @@ class DropletProblem:
         N.check(N.load().fe_problem_set_timing(self._h, int(enable)))
 
     def stage_times(self):
-        ms = np.zeros(4)
+        ms = np.zeros(5)
         calls = ctypes.c_int64()
         N.check(N.load().fe_problem_stage_times(self._h, ms.ctypes.data, ctypes.byref(calls)))
         return ms, calls.value

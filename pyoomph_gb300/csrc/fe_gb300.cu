@@ -540,8 +540,8 @@ struct fe_problem {
   std::vector<int32_t> h_rowptr, h_colidx;
   // stage timing (tracing): events recorded around the stages of fe_assemble
   bool timing = false;
-  std::vector<std::vector<cudaEvent_t>> pending; // per call: 5 events
-  double stage_ms[4] = {0, 0, 0, 0};
+  std::vector<std::vector<cudaEvent_t>> pending; // per call: 6 events
+  double stage_ms[5] = {0, 0, 0, 0, 0};
   long long stage_calls = 0;
   // one recorded assembly (fe_problem_graph_capture), replayed by fe_problem_graph_launch
   cudaGraphExec_t graph = nullptr;
@@ -1546,7 +1546,9 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
   const int sms = sm_count_cached();
   std::vector<cudaEvent_t> ev;
   if (p->timing) {
-    ev.resize(5);
+    // 0 start, 1 after the dof scatter, 5 after the element kernels, 2 after
+    // the tensor-core contraction, 3 after the residual gather, 4 at the end
+    ev.resize(6);
     for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
     CUDA_TRY(cudaEventRecord(ev[0], st));
   }
@@ -1565,6 +1567,7 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
   if (p->timing) CUDA_TRY(cudaEventRecord(ev[1], st));
   int rc = launch_elements(p, eflag, st);
   if (rc) return rc;
+  if (p->timing) CUDA_TRY(cudaEventRecord(ev[5], st));
   if (eflag == 1 || eflag == 4)
     for (Domain &d : p->domains)
       if (d.tc && (rc = tc_domain(p, d, 0, d.n_elem, st))) return rc;
@@ -1859,6 +1862,53 @@ int fe_tc_contract(const float *dhat, float *jbuf, int64_t n_elem, int n, int nq
   return FE_OK;
 }
 
+int fe_sa_aggregate(int64_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
+                    const int32_t *comp, double theta, int32_t *agg, int64_t *n_agg) {
+  if (n < 0 || (n > 0 && (!rowptr || !colidx || !vals || !comp || !agg)) || !n_agg)
+    return fail(FE_ERR_ARG, "fe_sa_aggregate: null argument");
+  std::vector<double> diag((size_t)n, 0.0);
+  for (int64_t i = 0; i < n; i++)
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++) {
+      if (colidx[k] < 0 || colidx[k] >= n) return fail(FE_ERR_ARG, "fe_sa_aggregate: column out of range");
+      if (colidx[k] == i) diag[i] = std::fabs(vals[k]);
+    }
+  auto strong = [&](int64_t i, int32_t k) {
+    const int32_t j = colidx[k];
+    return j != i && comp[j] == comp[i] && std::fabs(vals[k]) >= theta * std::sqrt(diag[i] * diag[j]);
+  };
+  for (int64_t i = 0; i < n; i++) agg[i] = -1;
+  int32_t na = 0;
+  for (int64_t i = 0; i < n; i++) {   // roots with a free strong neighbourhood
+    if (agg[i] >= 0) continue;
+    bool free_ = true;
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1] && free_; k++)
+      if (strong(i, k) && agg[colidx[k]] >= 0) free_ = false;
+    if (!free_) continue;
+    agg[i] = na;
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++)
+      if (strong(i, k)) agg[colidx[k]] = na;
+    na++;
+  }
+  std::vector<int32_t> first(agg, agg + n);
+  for (int64_t i = 0; i < n; i++) {   // join a neighbouring aggregate (of the first pass)
+    if (agg[i] >= 0) continue;
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++)
+      if (strong(i, k) && first[colidx[k]] >= 0) {
+        agg[i] = first[colidx[k]];
+        break;
+      }
+  }
+  for (int64_t i = 0; i < n; i++) {   // leftovers: new aggregates with their free strong neighbours
+    if (agg[i] >= 0) continue;
+    agg[i] = na;
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++)
+      if (strong(i, k) && agg[colidx[k]] < 0) agg[colidx[k]] = na;
+    na++;
+  }
+  *n_agg = na;
+  return FE_OK;
+}
+
 int fe_problem_set_zero_threshold(fe_problem_t *p, double threshold) {
   if (!p) return fail(FE_ERR_ARG, "null problem");
   if (!(threshold >= 0.0)) return fail(FE_ERR_ARG, "zero threshold must be >= 0");
@@ -1900,9 +1950,10 @@ int fe_problem_stage_times(fe_problem_t *p, double *ms, int64_t *calls) {
   if (!p) return fail(FE_ERR_ARG, "null problem");
   for (auto &v : p->pending) {
     CUDA_TRY(cudaEventSynchronize(v[4]));
-    for (int k = 0; k < 4; k++) {
+    const int from[5] = {0, 1, 2, 3, 5}, to[5] = {1, 5, 3, 4, 2};
+    for (int k = 0; k < 5; k++) {
       float t = 0.f;
-      CUDA_TRY(cudaEventElapsedTime(&t, v[k], v[k + 1]));
+      CUDA_TRY(cudaEventElapsedTime(&t, v[from[k]], v[to[k]]));
       p->stage_ms[k] += t;
     }
     for (auto e : v) cudaEventDestroy(e);
@@ -1910,9 +1961,9 @@ int fe_problem_stage_times(fe_problem_t *p, double *ms, int64_t *calls) {
   }
   p->pending.clear();
   if (ms)
-    for (int k = 0; k < 4; k++) ms[k] = p->stage_ms[k];
+    for (int k = 0; k < 5; k++) ms[k] = p->stage_ms[k];
   if (calls) *calls = p->stage_calls;
-  for (int k = 0; k < 4; k++) p->stage_ms[k] = 0;
+  for (int k = 0; k < 5; k++) p->stage_ms[k] = 0;
   p->stage_calls = 0;
   return FE_OK;
 }

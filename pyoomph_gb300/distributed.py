@@ -13,9 +13,11 @@ redistribution of the assembled rows (``parallel_sparse_assemble``,
   pattern, which every rank builds identically on the host
   (``fe_pattern_host``);
 * one exchange completes the assembly: the *halo* slots -- slots of a row
-  that a rank other than the row's owner touches -- are all-gathered and
-  each owner sums them in rank order, so the result is deterministic.
-  Everything else is touched by its owner alone and is already final.
+  that a rank other than the row's owner touches -- go to their row's owner
+  only (one all-to-all: every rank sends owner k its values of k's halo),
+  and each owner sums what it receives in rank order, so the result is
+  deterministic.  Everything else is touched by its owner alone and is
+  already final.
 
 The plan (slot maps, halo lists) is built once per mesh; the exchange moves
 only halo values.  Works with any torch.distributed backend (gloo on CPU
@@ -68,6 +70,8 @@ class ShardPlan:
     local_rows: np.ndarray           # [local n_dof] touched rows (global numbers)
     halo_slots: np.ndarray           # global slots exchanged (all owners), sorted
     halo_rows: np.ndarray            # global rows whose residual is exchanged, sorted
+    halo_slot_ptr: np.ndarray = None  # [world + 1] owner k's halo slots: halo_slots[ptr[k]:ptr[k+1]]
+    halo_row_ptr: np.ndarray = None   # [world + 1] the same for the halo rows
 
 
 def make_plan(rank: int, world: int, rowptr: np.ndarray, colidx: np.ndarray,
@@ -98,16 +102,24 @@ def make_plan(rank: int, world: int, rowptr: np.ndarray, colidx: np.ndarray,
     for k, (s, r) in enumerate(allv):
         foreign_s[s[slot_owner[s] != k]] = True
         foreign_r[r[row_owner[r] != k]] = True
-    return ShardPlan(rank, world, n_dof, int(rowptr[-1]), rr[rank], l2g, touched_rows,
-                     np.nonzero(foreign_s)[0].astype(np.int64), np.nonzero(foreign_r)[0].astype(np.int64))
+    hs = np.nonzero(foreign_s)[0].astype(np.int64)
+    hr = np.nonzero(foreign_r)[0].astype(np.int64)
+    # owners' row ranges are contiguous and ascending: each owner's halo is a run
+    sp = np.searchsorted(hs, [int(rowptr[a]) for a, _ in rr] + [int(rowptr[-1])])
+    rp_ = np.searchsorted(hr, [a for a, _ in rr] + [n_dof])
+    return ShardPlan(rank, world, n_dof, int(rowptr[-1]), rr[rank], l2g, touched_rows, hs, hr,
+                     sp.astype(np.int64), rp_.astype(np.int64))
 
 
 def reduce_owned(plan: ShardPlan, local_vals, local_R_global, group=None):
-    """Complete the assembly: returns (values of the global CSR slots of the
-    owned rows, residual of the owned rows).  local_vals: this rank's values
-    on its local pattern; local_R_global: this rank's partial residual as a
-    full-length vector (zeros where untouched).  Tensors may live on CPU
-    (gloo) or GPU (NCCL); the result stays on the same device."""
+    """Complete the assembly: returns (values of the global CSR slots, with
+    the owned rows final; residual, owned rows final).  local_vals: this
+    rank's values on its local pattern; local_R_global: this rank's partial
+    residual as a full-length vector (zeros where untouched).  One
+    all-to-all: owner k receives from every rank that rank's values of k's
+    halo slots and rows (zeros where it touches none) and sums them in rank
+    order.  Tensors may live on CPU (gloo) or GPU (NCCL); the result stays
+    on the same device."""
     import torch
     import torch.distributed as dist
     dev = local_vals.device
@@ -115,16 +127,27 @@ def reduce_owned(plan: ShardPlan, local_vals, local_R_global, group=None):
     full[torch.as_tensor(plan.local_to_global, device=dev)] = local_vals
     hs = torch.as_tensor(plan.halo_slots, device=dev)
     hr = torch.as_tensor(plan.halo_rows, device=dev)
-    seg = torch.cat([full[hs], local_R_global[hr].to(local_vals.dtype)]) if hs.numel() + hr.numel() else \
-        torch.zeros(0, dtype=local_vals.dtype, device=dev)
-    parts = [torch.empty_like(seg) for _ in range(plan.world)]
-    dist.all_gather(parts, seg, group=group)
-    acc = parts[0].clone()
-    for p in parts[1:]:
-        acc += p                     # rank order: deterministic
-    full[hs] = acc[:hs.numel()]
     R = local_R_global.clone()
-    R[hr] = acc[hs.numel():].to(R.dtype)
+    sends, sizes = [], []
+    for k in range(plan.world):
+        s_k = hs[int(plan.halo_slot_ptr[k]):int(plan.halo_slot_ptr[k + 1])]
+        r_k = hr[int(plan.halo_row_ptr[k]):int(plan.halo_row_ptr[k + 1])]
+        sends.append(torch.cat([full[s_k], R[r_k].to(full.dtype)]))
+        sizes.append(int(s_k.numel() + r_k.numel()))
+    me = plan.rank
+    mine = sizes[me]
+    inp = torch.cat(sends) if sends else torch.zeros(0, dtype=full.dtype, device=dev)
+    out = torch.empty(mine * plan.world, dtype=full.dtype, device=dev)
+    dist.all_to_all_single(out, inp, output_split_sizes=[mine] * plan.world, input_split_sizes=sizes,
+                           group=group)
+    if mine:
+        parts = out.view(plan.world, mine)
+        acc = parts[0].clone()
+        for k in range(1, plan.world):
+            acc += parts[k]              # rank order: deterministic
+        ns = int(plan.halo_slot_ptr[me + 1] - plan.halo_slot_ptr[me])
+        full[hs[int(plan.halo_slot_ptr[me]):int(plan.halo_slot_ptr[me + 1])]] = acc[:ns]
+        R[hr[int(plan.halo_row_ptr[me]):int(plan.halo_row_ptr[me + 1])]] = acc[ns:].to(R.dtype)
     return full, R
 
 

@@ -199,6 +199,13 @@ class StokesEquations(Equations):
         self.define_vector_field(self.velocity_name, "C2")
         self.define_scalar_field(self.pressure_name, "C1")
 
+    def saddle_point(self):
+        """(constrained field, parameter scaling its Schur complement): the
+        pressure, whose diagonal block is zero, and the viscosity (the
+        device saddle-point solver approximates the Schur complement by the
+        pressure mass over it)."""
+        return self.pressure_name, "dynamic_viscosity"
+
     def define_residuals(self):
         u, v = var_and_test(self.velocity_name)
         p, q = var_and_test(self.pressure_name)

@@ -1,0 +1,355 @@
+"""Device solve of saddle-point Newton systems (Taylor-Hood Navier-Stokes).
+
+The reference solves every Newton system J dx = R on the host with SuperLU
+(``pyoomph/solvers/scipy.py``, ``src/pybind/solver.cpp:105-133``).  For a
+Jacobian with a zero diagonal block -- velocity u and pressure p,
+
+    J = [[A, Bt],
+         [B,  0]],
+
+Jacobi- or ILU-preconditioned Krylov methods need iteration counts that grow
+with the mesh.  This solver keeps everything on the device and converges in
+a mesh-independent number of iterations:
+
+* right-preconditioned GMRES (restarted, classical Gram-Schmidt applied
+  twice, so one host synchronisation per iteration) on the resident CSR
+  Jacobian (``fe_csr_spmv``);
+* the block upper-triangular preconditioner P = [[A, Bt], [0, S_hat]]:
+  p = S_hat^-1 r_p, u = A_hat^-1 (r_u - Bt p), which would need two GMRES
+  iterations with exact blocks;
+* S_hat = sigma M_p / mu: the lumped mass matrix of the pressure space
+  divided by the viscosity, spectrally equivalent to the Schur complement
+  -B A^-1 Bt of Stokes-dominated flow; the sign sigma is measured on the
+  matrix itself;
+* A_hat^-1 = one V-cycle of smoothed-aggregation multigrid on the velocity
+  block (aggregates of strongly coupled unknowns of the same component,
+  ``fe_sa_aggregate``; prolongators smoothed by one damped-Jacobi step;
+  Galerkin coarse operators; damped-Jacobi smoothing; a dense inverse on
+  the coarsest level), every level applied with the library's CSR kernel.
+
+The hierarchy is built on the host once, from the first Jacobian, and kept
+for the following Newton steps (only the finest velocity block is refreshed
+from each new Jacobian): the preconditioner changes slowly along a Newton
+solve, and GMRES stays exact whatever the preconditioner.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import List, Optional
+
+import numpy as np
+
+from . import _native as N
+from .linsolve import DeviceCSR, LinearSolverError
+
+
+class _DevCSR:
+    """A CSR matrix on the device in the layout of fe_csr_spmv (int32
+    indices, FP64 values); rectangular matrices too."""
+
+    def __init__(self, torch, A, dev):
+        A = A.tocsr()
+        A.sort_indices()
+        self.n, self.m = A.shape
+        self.nnz = int(A.nnz)
+        self.rp = torch.as_tensor(A.indptr.astype(np.int32), device=dev)
+        self.ci = torch.as_tensor(A.indices.astype(np.int32) if A.nnz else np.zeros(1, np.int32), device=dev)
+        self.v = torch.as_tensor(A.data.astype(np.float64) if A.nnz else np.zeros(1), device=dev)
+
+    def mv(self, x, y, stream) -> None:
+        if self.n == 0:
+            return
+        N.check(N.load().fe_csr_spmv(ctypes.c_void_p(self.rp.data_ptr()), ctypes.c_void_p(self.ci.data_ptr()),
+                                     ctypes.c_void_p(self.v.data_ptr()), N.FE_JAC_F64,
+                                     ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()), self.n,
+                                     self.nnz, ctypes.c_void_p(stream)))
+
+
+def aggregate(A, comp: np.ndarray, theta: float):
+    """Aggregates of A's unknowns (fe_sa_aggregate): (agg [n], n_agg)."""
+    A = A.tocsr()
+    n = A.shape[0]
+    agg = np.zeros(max(n, 1), dtype=np.int32)
+    na = ctypes.c_int64()
+    rp = np.ascontiguousarray(A.indptr, dtype=np.int32)
+    ci = np.ascontiguousarray(A.indices, dtype=np.int32)
+    v = np.ascontiguousarray(A.data, dtype=np.float64)
+    c = np.ascontiguousarray(comp, dtype=np.int32)
+    N.check(N.load().fe_sa_aggregate(n, rp.ctypes.data, ci.ctypes.data, v.ctypes.data, c.ctypes.data,
+                                     float(theta), agg.ctypes.data, ctypes.byref(na)))
+    return agg[:n], int(na.value)
+
+
+def spectral_radius_dinv_a(A, iters: int = 12, seed: int = 0) -> float:
+    """Estimate of rho(D^-1 A) by power iteration (host), with a margin."""
+    D = A.diagonal()
+    x = np.random.default_rng(seed).uniform(0.5, 1.5, A.shape[0])
+    lam = 1.0
+    for _ in range(iters):
+        y = (A @ x) / D
+        lam = float(np.linalg.norm(y) / max(np.linalg.norm(x), 1e-300))
+        x = y / max(np.linalg.norm(y), 1e-300)
+    return 1.1 * lam
+
+
+def lumped_field_mass(P, field: str) -> np.ndarray:
+    """Row sums of the mass matrix of one field (lumped mass), per dof of
+    that field: sum over elements and knots of w |det J| psi_k."""
+    mesh, et = P.mesh, P.mesh.etype
+    t = et.tables()
+    names = [n_ for n_, _ in P.fields]
+    f = names.index(field)
+    space = P.fields[f][1]
+    W = np.asarray(t["W"]).reshape(et.nq)
+    dps2 = np.asarray(t["DPS2"]).reshape(et.nq, et.nnode, et.dim)
+    if space == "C1":
+        psi = np.asarray(t["PSI1"]).reshape(et.nq, et.nnode_c1)
+        slots = np.asarray(et.c1_index)
+    else:
+        psi = np.asarray(t["PSI2"]).reshape(et.nq, et.nnode)
+        slots = np.arange(et.nnode)
+    X = mesh.x[mesh.conn]                              # [E, nnode, dim]
+    G = np.einsum("eld,qlb->eqdb", X, dps2)            # dx_d/ds_b per element and knot
+    det = np.abs(np.linalg.det(G))                     # [E, nq]
+    contrib = np.einsum("q,eq,qk->ek", W, det, psi)    # [E, nslots]
+    eqn = np.asarray(P.eqn).reshape(mesh.n_nodes, len(P.fields))[:, f]
+    rows = eqn[mesh.conn[:, slots]]
+    ok = rows >= 0
+    out = np.zeros(P.n_dof)
+    np.add.at(out, rows[ok], contrib[ok])
+    return out
+
+
+class SaddlePointSolver:
+    """GMRES with the block-triangular multigrid preconditioner for the
+    Jacobian of a problem with one constrained field (the pressure):
+    ``solve(R)`` returns dx with J dx = R, J the problem's current device
+    Jacobian (J_dev).  schur_scale is the viscosity (the Schur complement is
+    approximated by the pressure mass over it)."""
+
+    def __init__(self, P, schur_field: str, schur_scale: float, restart: int = 60, smooth_steps: int = 2,
+                 theta: float = 0.08, coarse_size: int = 800, max_levels: int = 12):
+        import scipy.sparse as sps
+        import torch
+        self.torch = torch
+        self.P = P
+        self.dev = P.J_dev.device
+        self.restart = int(restart)
+        self.nu = max(1, int(smooth_steps))
+        self.theta = float(theta)
+        self.coarse_size = int(coarse_size)
+        self.max_levels = int(max_levels)
+        n = P.n_dof
+        eqn = np.asarray(P.eqn).reshape(P.mesh.n_nodes, len(P.fields))
+        f = [n_ for n_, _ in P.fields].index(schur_field)
+        comp = np.full(n, -1, dtype=np.int32)
+        for k in range(len(P.fields)):
+            col = eqn[:, k]
+            comp[col[col >= 0]] = k
+        is_p = comp == f
+        self.vel = np.nonzero(~is_p)[0]
+        self.pre = np.nonzero(is_p)[0]
+        self.comp_v = comp[self.vel]
+        rp, ci = P.pattern()
+        # slot maps of the velocity block A and the coupling Bt inside the CSR
+        rows = np.repeat(np.arange(n), np.diff(rp))
+        where_v = np.full(n, -1, dtype=np.int64)
+        where_v[self.vel] = np.arange(self.vel.size)
+        where_p = np.full(n, -1, dtype=np.int64)
+        where_p[self.pre] = np.arange(self.pre.size)
+        rv, cv, cp = where_v[rows], where_v[ci], where_p[ci]
+        rpre = where_p[rows]
+        sel_a = (rv >= 0) & (cv >= 0)
+        sel_b = (rv >= 0) & (cp >= 0)
+        sel_c = (rpre >= 0) & (cv >= 0)
+        slots = np.arange(rp[-1])
+        A_pat = sps.csr_matrix((slots[sel_a] + 1.0, (rv[sel_a], cv[sel_a])), shape=(self.vel.size,) * 2)
+        A_pat.sort_indices()
+        B_pat = sps.csr_matrix((slots[sel_b] + 1.0, (rv[sel_b], cp[sel_b])), shape=(self.vel.size, self.pre.size))
+        B_pat.sort_indices()
+        C_pat = sps.csr_matrix((slots[sel_c] + 1.0, (rpre[sel_c], cv[sel_c])), shape=(self.pre.size, self.vel.size))
+        C_pat.sort_indices()
+        self.A_shape, self.B_shape, self.C_shape = A_pat, B_pat, C_pat
+        self.map_a = torch.as_tensor((A_pat.data - 1.0).astype(np.int64), device=self.dev)
+        self.map_b = torch.as_tensor((B_pat.data - 1.0).astype(np.int64), device=self.dev)
+        self.vel_t = torch.as_tensor(self.vel, device=self.dev)
+        self.pre_t = torch.as_tensor(self.pre, device=self.dev)
+        mass = lumped_field_mass(P, schur_field)[self.pre]
+        if np.any(mass <= 0):
+            raise LinearSolverError("pressure lumped mass is not positive")
+        self.mass = mass
+        self.schur_scale = float(schur_scale)
+        self.levels: Optional[List[dict]] = None
+        self.iterations = 0
+        self.J = DeviceCSR.of_problem(P)
+
+    # -- set-up ------------------------------------------------------------
+    def _host_blocks(self):
+        """(A, Bt, B) of the current Jacobian on the host."""
+        import scipy.sparse as sps
+        vals = self.P.J_dev[:self.P.nnz].to(self.torch.float64).cpu().numpy()
+
+        def take(pat):
+            return sps.csr_matrix((vals[(pat.data - 1).astype(np.int64)], pat.indices, pat.indptr), shape=pat.shape)
+        return take(self.A_shape), take(self.B_shape), take(self.C_shape)
+
+    def setup(self) -> None:
+        """The multigrid hierarchy of the current velocity block and the
+        sign of the Schur approximation (host, once)."""
+        import scipy.sparse as sps
+        torch = self.torch
+        A, Bt, B = self._host_blocks()
+        D = A.diagonal()
+        if np.any(D == 0) or not np.all(np.isfinite(A.data)):
+            raise LinearSolverError("velocity block has a zero diagonal entry or non-finite values")
+        # the Schur complement S = -B A^-1 Bt ~ sigma M_p / mu: its sign from
+        # q^T B D^-1 Bt q for a random q (the weak form fixes the signs of B, Bt)
+        q = np.random.default_rng(1).normal(size=self.pre.size)
+        s = float(q @ (B @ ((Bt @ q) / D)))
+        self.sigma = -1.0 if s > 0 else 1.0
+        self.sinv = torch.as_tensor(self.sigma * self.schur_scale / self.mass, device=self.dev)
+        levels = []
+        comp = self.comp_v
+        while A.shape[0] > self.coarse_size and len(levels) < self.max_levels:
+            agg, na = aggregate(A, comp, self.theta)
+            if na >= 0.9 * A.shape[0]:
+                break
+            n = A.shape[0]
+            P0 = sps.csr_matrix((np.ones(n), (np.arange(n), agg)), shape=(n, na))
+            Dl = A.diagonal()
+            lam = spectral_radius_dinv_a(A)
+            Pm = (P0 - (4.0 / 3.0 / lam) * (sps.diags(1.0 / Dl) @ A @ P0)).tocsr()
+            Ac = (Pm.T @ A @ Pm).tocsr()
+            cc = np.zeros(na, dtype=np.int32)
+            cc[agg] = comp
+            levels.append({"A": _DevCSR(torch, A, self.dev), "P": _DevCSR(torch, Pm, self.dev),
+                           "R": _DevCSR(torch, Pm.T.tocsr(), self.dev),
+                           "dinv": torch.as_tensor(1.0 / Dl, device=self.dev), "om": 1.0 / lam, "n": n, "nc": na,
+                           "x": torch.zeros(n, dtype=torch.float64, device=self.dev),
+                           "t": torch.zeros(n, dtype=torch.float64, device=self.dev),
+                           "bc": torch.zeros(na, dtype=torch.float64, device=self.dev)})
+            A, comp = Ac, cc
+        self.coarse_inv = torch.linalg.inv(torch.as_tensor(A.toarray(), device=self.dev))
+        self.levels = levels
+        self.Bt = _DevCSR(torch, Bt, self.dev)
+        self.sizes = [lv["n"] for lv in levels] + [A.shape[0]]
+
+    # -- application -------------------------------------------------------
+    def _vcycle(self, lvl: int, b):
+        """One V-cycle on level lvl for right-hand side b: nu damped-Jacobi
+        steps from zero, the coarse-grid correction, nu steps.  Returns the
+        level's iterate buffer (valid until the next cycle on this level)."""
+        torch = self.torch
+        st = torch.cuda.current_stream().cuda_stream
+        if lvl == len(self.levels):
+            return self.coarse_inv @ b
+        L = self.levels[lvl]
+        x, t, dinv, om = L["x"], L["t"], L["dinv"], L["om"]
+        torch.mul(b, dinv, out=x).mul_(om)
+        for _ in range(self.nu - 1):
+            L["A"].mv(x, t, st)
+            x.addcmul_(b - t, dinv, value=om)
+        L["A"].mv(x, t, st)
+        L["R"].mv(b - t, L["bc"], st)
+        L["P"].mv(self._vcycle(lvl + 1, L["bc"]), t, st)
+        x.add_(t)
+        for _ in range(self.nu):
+            L["A"].mv(x, t, st)
+            x.addcmul_(b - t, dinv, value=om)
+        return x
+
+    def precondition(self, r):
+        """z = P^-1 r: p = S_hat^-1 r_p, u = A_hat^-1 (r_u - Bt p)."""
+        torch = self.torch
+        st = torch.cuda.current_stream().cuda_stream
+        p = self.sinv * r.index_select(0, self.pre_t)
+        tv = torch.empty(self.vel.size, dtype=torch.float64, device=self.dev)
+        self.Bt.mv(p, tv, st)
+        u = self._vcycle(0, r.index_select(0, self.vel_t) - tv)
+        z = torch.empty_like(r)
+        z.index_copy_(0, self.vel_t, u)
+        z.index_copy_(0, self.pre_t, p)
+        return z
+
+    def refresh(self) -> None:
+        """Take the finest velocity block (and Bt) from the current Jacobian;
+        the coarse levels stay."""
+        vals = self.P.J_dev[:self.P.nnz].to(self.torch.float64)
+        if self.levels:
+            self.levels[0]["A"].v.copy_(vals.index_select(0, self.map_a))
+        self.Bt.v.copy_(vals.index_select(0, self.map_b))
+
+    def solve(self, b, tol: float = 1e-10, atol: float = 0.0, maxiter: int = 2000):
+        """x with J x = b (device vectors), stopping at ||b - J x||_2 <=
+        max(tol ||b||_2, atol).  Returns (x, iterations)."""
+        torch = self.torch
+        if self.levels is None:
+            self.setup()
+        else:
+            self.refresh()
+        st = torch.cuda.current_stream().cuda_stream
+        n = self.P.n_dof
+        b = b.reshape(-1)[:n].to(torch.float64)
+        if not bool(torch.isfinite(b).all()):
+            raise LinearSolverError("non-finite right-hand side")
+        bnorm = float(torch.linalg.vector_norm(b))
+        target = max(tol * bnorm, atol)
+        x = torch.zeros(n, dtype=torch.float64, device=self.dev)
+        if bnorm == 0.0:
+            return x, 0
+        m = self.restart
+        V = torch.zeros((m + 1, n), dtype=torch.float64, device=self.dev)
+        Az = torch.empty(n, dtype=torch.float64, device=self.dev)
+        its = 0
+        r = b.clone()
+        beta = bnorm
+        while its < maxiter:
+            V[0] = r / beta
+            H = np.zeros((m + 1, m))
+            g = np.zeros(m + 1)
+            g[0] = beta
+            cs, sn = np.zeros(m), np.zeros(m)
+            k = 0
+            for k in range(m):
+                z = self.precondition(V[k])
+                self.J.matvec(z, Az, st)
+                w = Az
+                h = V[:k + 1] @ w
+                w = w - V[:k + 1].T @ h
+                h2 = V[:k + 1] @ w               # second pass (classical Gram-Schmidt twice)
+                w = w - V[:k + 1].T @ h2
+                hk = (h + h2)
+                nw = torch.linalg.vector_norm(w)
+                hv = torch.cat([hk, nw.reshape(1)]).cpu().numpy()   # one synchronisation per iteration
+                H[:k + 1, k] = hv[:-1]
+                H[k + 1, k] = hv[-1]
+                if hv[-1] > 0:
+                    V[k + 1] = w / hv[-1]
+                for i in range(k):               # Givens rotations
+                    t_ = cs[i] * H[i, k] + sn[i] * H[i + 1, k]
+                    H[i + 1, k] = -sn[i] * H[i, k] + cs[i] * H[i + 1, k]
+                    H[i, k] = t_
+                den = np.hypot(H[k, k], H[k + 1, k])
+                cs[k], sn[k] = (1.0, 0.0) if den == 0 else (H[k, k] / den, H[k + 1, k] / den)
+                H[k, k] = den
+                H[k + 1, k] = 0.0
+                g[k + 1] = -sn[k] * g[k]
+                g[k] = cs[k] * g[k]
+                its += 1
+                if not np.isfinite(g[k + 1]):
+                    raise LinearSolverError("GMRES broke down (non-finite residual)")
+                if abs(g[k + 1]) <= target or its >= maxiter:
+                    break
+            kk = k + 1
+            y = np.linalg.solve(np.triu(H[:kk, :kk]), g[:kk]) if kk else np.zeros(0)
+            yt = torch.as_tensor(y, device=self.dev)
+            x += self.precondition(V[:kk].T @ yt)
+            self.J.matvec(x, Az, st)
+            r = b - Az
+            beta = float(torch.linalg.vector_norm(r))
+            if beta <= target:
+                self.iterations = its
+                return x, its
+        self.iterations = its
+        raise LinearSolverError(f"GMRES did not converge in {maxiter} iterations (residual {beta:.3e}, "
+                                f"target {target:.3e})")

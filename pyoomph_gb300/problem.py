@@ -266,7 +266,9 @@ class Problem:
         # contract FP32 element Jacobians on the tensor cores (None: where the
         # generator supports it and it pays, the Q2 hex's 27 x 27 matrices)
         self.tensor_cores: Optional[bool] = None
-        # linear_solver = "bicgstab": J dx = R solved on the device (linsolve.py)
+        # linear_solver = "bicgstab": J dx = R solved on the device (linsolve.py);
+        # "fieldsplit": saddle-point systems (Taylor-Hood) on the device
+        # (fieldsplit.py: GMRES, block-triangular multigrid preconditioner)
         # to this relative tolerance; None: SuperLU on the host (the reference's default)
         self.linear_solver_tolerance = 1e-13
         # Gaussian source terms on axis-aligned affine Q2 meshes: evaluate the
@@ -277,6 +279,11 @@ class Problem:
         # absolute floor of the device solve's residual (0: relative only);
         # e.g. 0.1 x newton_solver_tolerance for an inexact Newton step
         self.linear_solver_atol = 0.0
+        # "fieldsplit" (saddle-point GMRES, fieldsplit.py): relative
+        # tolerances below this are raised to it (the 2-norm residual of a
+        # Krylov solve of these systems stalls near cond x eps)
+        self.fieldsplit_min_tolerance = 1e-11
+        self.saddle_point = None
         # time-dependent solve: the weak form's partial_t terms are kept (BDF
         # weights of the step as parameters, two previous time levels on the
         # device); False: they vanish (the steady ResidualAndJacobianSteady
@@ -296,6 +303,11 @@ class Problem:
         # coupling kept, the fast path); a threshold >= 0 = the reference's
         # value-dependent pattern (its default is 0.0)
         self.numerical_zero_for_sparse_assembly: Optional[float] = None
+        # assemble only the elements [lo, hi) of the mesh, with the global
+        # numbering (oomph's First_el_for_assembly / Last_el_plus_one_for_
+        # assembly split, problem.cc:5354-5358): R and J hold this range's
+        # contributions; distributed.py completes the sum across ranks
+        self.element_range: Optional[Tuple[int, int]] = None
         # temporal error scale per field name (set_temporal_error_factor)
         self.temporal_error_factors: Dict[str, float] = {}
         self.verbose = False
@@ -348,6 +360,7 @@ class Problem:
         if not bulk:
             raise RuntimeError("no bulk equations")
         self._bcs = bcs
+        self.saddle_point = next((b.saddle_point() for b in bulk if hasattr(b, "saddle_point")), None)
         fields: List[Tuple[str, str]] = []
         integrand = 0
         params: Dict[str, float] = {}
@@ -420,7 +433,8 @@ class Problem:
             # replicated problems: serving classes of many sizes then share
             # one kernel instead of compiling one per size.
             sms = _sm_count()
-            n_el = mesh.n_elem
+            lo_, hi_ = self._element_slice()
+            n_el = max(1, hi_ - lo_)
             waves = -(-n_el // (sms * ks.epb))
             epb = max(1, -(-n_el // (sms * waves)))
             if epb < ks.epb:
@@ -572,6 +586,7 @@ class Problem:
         self.R_dev = torch.zeros(max(self.n_dof, 1), dtype=torch.float64, device=dev)
         self.J_dev = torch.zeros(max(self.nnz, 1), dtype=self._jdtype, device=dev)
         self._krylov = None   # device linear solver state, bound to J_dev
+        self._fieldsplit = None
         self.x_dev.copy_(torch.from_numpy(self._dofs_from_values(values)))
         self._state_generation += 1           # a new device problem
         t4 = time.perf_counter()
@@ -583,11 +598,23 @@ class Problem:
         from .codegen import tc_tables
         return tc_tables(self.kernel)
 
+    def _element_slice(self) -> Tuple[int, int]:
+        """The elements this problem assembles: all, or element_range."""
+        if self.element_range is None:
+            return 0, self.mesh.n_elem
+        lo, hi = (int(v) for v in self.element_range)
+        if not 0 <= lo <= hi <= self.mesh.n_elem:
+            raise ValueError(f"element_range {self.element_range} outside [0, {self.mesh.n_elem}]")
+        if int(self.replicas) != 1:
+            raise NotImplementedError("element ranges of replicated problems")
+        return lo, hi
+
     def _descriptors(self, with_code: bool):
         mesh = self.mesh
         lay = self.kernel.layout
+        lo, hi = self._element_slice()
         keep = dict(
-            conn=np.ascontiguousarray(mesh.conn, dtype=np.int32),
+            conn=np.ascontiguousarray(mesh.conn[lo:hi], dtype=np.int32),
             lnode=np.ascontiguousarray(lay.node, dtype=np.int32),
             lval=np.ascontiguousarray(lay.val, dtype=np.int32),
             tables=np.ascontiguousarray(self.kernel.tables, dtype=np.float64),
@@ -600,7 +627,7 @@ class Problem:
             hw=np.ascontiguousarray(self.hang_weight if self.hang_weight.size else np.zeros(1)),
         )
         k = keep
-        dd = N.DomainDesc(self.code.handle if with_code else None, mesh.etype.nnode, lay.n, mesh.n_elem,
+        dd = N.DomainDesc(self.code.handle if with_code else None, mesh.etype.nnode, lay.n, hi - lo,
                           k["conn"].ctypes.data, k["lnode"].ctypes.data, k["lval"].ctypes.data,
                           k["tables"].ctypes.data, k["tables"].size, self.kernel.epb, self.kernel.threads,
                           self.kernel.smem_bytes, getattr(self, "replica_elems", 0))
@@ -787,15 +814,17 @@ class Problem:
 
     def stage_times(self):
         """Summed ms per stage (dof scatter, element kernels, residual gather,
-        Jacobian gather) since the last call, and the number of assemblies."""
-        ms = np.zeros(4)
+        Jacobian gather, tensor-core contraction) since the last call, and
+        the number of assemblies."""
+        ms = np.zeros(5)
         calls = ctypes.c_int64()
         N.check(N.load().fe_problem_stage_times(self._h, ms.ctypes.data, ctypes.byref(calls)))
         return ms, calls.value
 
     def element_buffers(self):
         """(R_e [E, nloc], J_e [E, nloc, nloc]) of the last assembly."""
-        E, n = self.mesh.n_elem, self.kernel.layout.n
+        lo, hi = self._element_slice()
+        E, n = hi - lo, self.kernel.layout.n
         R = np.zeros((E, n))
         J = np.zeros((E, n, n), dtype=np.float64 if self._prec == "f64" else np.float32)
         N.check(N.load().fe_problem_element_buffers(self._h, 0, R.ctypes.data, J.ctypes.data))
@@ -908,6 +937,21 @@ class Problem:
         if callable(self.linear_solver):
             return self.linear_solver(A, R)
         return spla.splu(A.tocsc()).solve(R)
+
+    def _fieldsplit_solver(self):
+        """The device saddle-point solver of this problem (fieldsplit.py),
+        built at the first solve: the constrained field and the viscosity
+        scaling its Schur complement come from the equations
+        (StokesEquations.saddle_point)."""
+        if getattr(self, "_fieldsplit", None) is None:
+            from .fieldsplit import SaddlePointSolver
+            if self.saddle_point is None:
+                raise RuntimeError("linear_solver='fieldsplit' needs equations with a constrained field "
+                                   "(Stokes / Navier-Stokes)")
+            field, scale_param = self.saddle_point
+            scale = float(self.params[self.param_names.index(scale_param)])
+            self._fieldsplit = SaddlePointSolver(self, field, scale)
+        return self._fieldsplit
 
     def solve_linear_device(self, b: np.ndarray) -> np.ndarray:
         """x with J x = b, J the Jacobian of the last assembly (resident on
@@ -1085,12 +1129,13 @@ class Problem:
     def _temporal_error_scales(self) -> Optional[np.ndarray]:
         if not self.temporal_error_factors:
             return None
-        unknown = set(self.temporal_error_factors) - set(self.fields)
+        names = [n for n, _ in self.fields]
+        unknown = set(self.temporal_error_factors) - set(names)
         if unknown:
-            raise KeyError(f"temporal error factors of unknown fields {sorted(unknown)}; have {self.fields}")
+            raise KeyError(f"temporal error factors of unknown fields {sorted(unknown)}; have {names}")
         eqn = np.asarray(self.eqn).reshape(self.mesh.n_nodes, len(self.fields))
         s = np.zeros(self.n_dof)
-        for j, f in enumerate(self.fields):
+        for j, f in enumerate(names):
             col = eqn[:, j]
             s[col[col >= 0]] = self.temporal_error_factors.get(f, 0.0)
         return s
@@ -1246,14 +1291,19 @@ class Problem:
             if hist[-1] > self.max_residuals:
                 raise NewtonSolverError(f"max residuals ({self.max_residuals}) exceeded: {hist}")
             ta = time.perf_counter()
-            device_solve = self.linear_solver == "bicgstab"
+            device_solve = self.linear_solver in ("bicgstab", "fieldsplit")
             with nvtx_range("fe_assemble R+J"):
                 self.assemble_device(with_jacobian=True)
                 self.check()
                 R = None if device_solve else self.R_dev[:self.n_dof].cpu().numpy()
             tb = time.perf_counter()
             with nvtx_range("linear solve"):
-                if device_solve:
+                if self.linear_solver == "fieldsplit":
+                    dxd, its = self._fieldsplit_solver().solve(
+                        self.R_dev[:self.n_dof], tol=max(self.linear_solver_tolerance, self.fieldsplit_min_tolerance),
+                        atol=self.linear_solver_atol)
+                    self.timings["krylov_iterations"] = self.timings.get("krylov_iterations", 0) + int(its)
+                elif device_solve:
                     from .linsolve import BatchedBiCGStab, DeviceCSR
                     if getattr(self, "_krylov", None) is None:
                         # one block per replica: each replica's solve is its own

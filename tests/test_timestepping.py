@@ -152,3 +152,20 @@ def test_gpu_adaptive_steps_match_a_fixed_step_replay():
         ref = Q.get_dofs()
         assert np.max(np.abs(states[k] - ref)) <= 1e-12 * np.max(np.abs(ref)), k
     assert abs(Q.time - P.time) < 1e-14 and Q.steps_done == P.steps_done
+
+
+def test_temporal_error_scales_per_field():
+    """Problem.set_temporal_error_factor: the scale of every dof of a field;
+    fields without a factor count with scale 0 once any field has one."""
+    from pyoomph_gb300 import workloads as W
+    P = W.navier_stokes_problem(N=3)
+    P.lower()
+    assert P._temporal_error_scales() is None
+    P.set_temporal_error_factor("velocity_x", 2.0)
+    s = P._temporal_error_scales()
+    eqn = np.asarray(P.eqn).reshape(P.mesh.n_nodes, 3)
+    ux = eqn[:, 0][eqn[:, 0] >= 0]
+    assert np.all(s[ux] == 2.0) and np.count_nonzero(s) == ux.size
+    P.set_temporal_error_factor("nonexistent", 1.0)
+    with pytest.raises(KeyError):
+        P._temporal_error_scales()
