@@ -17,7 +17,21 @@ from typing import Callable, Optional, Tuple, Union
 import numpy as np
 
 
-class CustomAssemblyBase:
+def _reference_base():
+    """pyoomph's own CustomAssemblyBase (pyoomph/generic/assembly.py:36) when
+    pyoomph imports here, so that the assembler is an instance of the class
+    pyoomph's Problem.set_custom_assembler expects; None otherwise."""
+    try:
+        from pyoomph.generic.assembly import CustomAssemblyBase as base  # type: ignore
+        return base
+    except Exception:
+        return None
+
+
+class _LocalCustomAssemblyBase:
+    """The plugin contract of pyoomph's CustomAssemblyBase, for hosts where
+    pyoomph itself does not import."""
+
     def __init__(self) -> None:
         self.problem = None
 
@@ -61,18 +75,68 @@ class CustomAssemblyBase:
         return None, None
 
 
+CustomAssemblyBase = _reference_base() or _LocalCustomAssemblyBase
+
+
+def numbering_fingerprint(eqn) -> str:
+    """A hash of an equation-number table [n_nodes, nval] (int32)."""
+    import hashlib
+    return hashlib.sha1(np.ascontiguousarray(eqn, dtype=np.int32).tobytes()).hexdigest()[:16]
+
+
 class GB300Assembler(CustomAssemblyBase):
     """Residual and CSR Jacobian from the GB300 engine.
 
     ``engine`` is a ``pyoomph_gb300.Problem`` describing the same mesh and
-    weak form as the host problem (same equation numbering).  If the host
-    problem is not set, the engine's own dof state is assembled."""
+    weak form as the host problem (same equation numbering, which
+    ``check_numbering`` verifies against the host problem when it is set).
+    If the host problem is not set, the engine's own dof state is
+    assembled."""
 
-    def __init__(self, engine, device_linear_solve: bool = False) -> None:
+    def __init__(self, engine, device_linear_solve: bool = False, mesh_name: str = "domain") -> None:
         super().__init__()
         self.engine = engine
         self.device_linear_solve = bool(device_linear_solve)
+        self.mesh_name = mesh_name
         self._last_J = None
+        self._numbering_checked = False
+
+    def check_numbering(self) -> None:
+        """Refuse a host problem numbered differently from the engine: its
+        number of equations (pyoomph's Problem.ndof) and, where the host
+        exposes its mesh (Problem.get_mesh(name).nodes(), Node.nvalue,
+        Node.eqn_number), the equation of every nodal value, which fixes the
+        CSR rows and columns.  A mismatch would otherwise assemble a
+        different system without any error."""
+        P = self.problem
+        if P is None:
+            return
+        self.engine.lower()
+        nd = P.ndof() if callable(getattr(P, "ndof", None)) else None
+        if nd is not None and int(nd) != self.engine.n_dof:
+            raise RuntimeError(f"host problem has {nd} equations, the engine {self.engine.n_dof}")
+        getm = getattr(P, "get_mesh", None)
+        if not callable(getm):
+            return
+        mesh = getm(self.mesh_name)
+        if mesh is None or not hasattr(mesh, "nodes"):
+            return
+        eqn = np.asarray(self.engine.eqn).reshape(self.engine.mesh.n_nodes, len(self.engine.fields))
+        host = np.full_like(eqn, -1)
+        k = -1
+        for k, node in enumerate(mesh.nodes()):
+            if k >= eqn.shape[0]:
+                raise RuntimeError(f"host mesh {self.mesh_name!r} has more nodes than the engine's")
+            nv = min(int(node.nvalue()), eqn.shape[1])
+            for vi in range(nv):
+                host[k, vi] = int(node.eqn_number(vi))
+        if k + 1 != eqn.shape[0]:
+            raise RuntimeError(f"host mesh {self.mesh_name!r} has {k + 1} nodes, the engine {eqn.shape[0]}")
+        if numbering_fingerprint(host) != numbering_fingerprint(eqn):
+            bad = np.argwhere(host != eqn)[0]
+            raise RuntimeError(f"equation numbering differs from the host problem's (first at node {bad[0]}, "
+                               f"value {bad[1]}: host {host[tuple(bad)]}, engine {eqn[tuple(bad)]})")
+        self._numbering_checked = True
 
     def has_custom_solve_routine(self) -> bool:
         return self.device_linear_solve
@@ -87,7 +151,12 @@ class GB300Assembler(CustomAssemblyBase):
                                     dtype=np.float64)
 
     def initialize(self) -> None:
+        self.check_numbering()
         self.engine.initialise()
+
+    def actions_after_equation_numbering(self) -> None:
+        self.invalidate_cache()
+        self.check_numbering()
 
     def _sync_dofs(self) -> None:
         if self.problem is not None and hasattr(self.problem, "get_current_dofs"):

@@ -262,3 +262,55 @@ def test_launch_shapes_balance_the_waves():
     P = W.poisson_problem(N=64)
     P.elems_per_block = 32                # an explicit shape is kept
     assert P.lower().epb == 32
+
+
+def test_assembler_refuses_a_differently_numbered_host_problem():
+    """GB300Assembler.check_numbering against a host problem that exposes
+    pyoomph's ndof() and get_mesh(name).nodes() with Node.eqn_number: equal
+    numbering passes; another dof count or a swapped pair of equations is an
+    error (the CSR would otherwise belong to a different system)."""
+    from pyoomph_gb300 import GB300Assembler, workloads as W
+    eng = W.navier_stokes_problem(N=3)
+    eng.lower()
+    eqn = np.asarray(eng.eqn).reshape(eng.mesh.n_nodes, 3).copy()
+
+    class Node:
+        def __init__(self, row):
+            self.row = row
+
+        def nvalue(self):
+            return 3 if self.row[2] != -2 else 2
+
+        def eqn_number(self, vi):
+            return int(self.row[vi])
+
+    class Mesh:
+        def __init__(self, table):
+            self.table = table
+
+        def nodes(self):
+            return [Node(r) for r in self.table]
+
+    class Host:
+        def __init__(self, table, ndof):
+            self.table, self.n = table, ndof
+
+        def ndof(self):
+            return self.n
+
+        def get_mesh(self, name):
+            return Mesh(self.table)
+
+    asm = GB300Assembler(eng)
+    asm._set_problem(Host(eqn, eng.n_dof))
+    asm.check_numbering()
+    assert asm._numbering_checked
+    asm._set_problem(Host(eqn, eng.n_dof + 1))
+    with pytest.raises(RuntimeError):
+        asm.check_numbering()
+    swapped = eqn.copy()
+    a, b = np.argwhere(swapped >= 0)[:2]
+    swapped[tuple(a)], swapped[tuple(b)] = swapped[tuple(b)], swapped[tuple(a)]
+    asm._set_problem(Host(swapped, eng.n_dof))
+    with pytest.raises(RuntimeError, match="numbering differs"):
+        asm.check_numbering()
