@@ -303,7 +303,9 @@ class SaddlePointSolver:
         its = 0
         r = b.clone()
         beta = bnorm
+        stalled = 0
         while its < maxiter:
+            beta_start = beta
             V[0] = r / beta
             H = np.zeros((m + 1, m))
             g = np.zeros(m + 1)
@@ -350,6 +352,10 @@ class SaddlePointSolver:
             if beta <= target:
                 self.iterations = its
                 return x, its
+            # a restart cycle that gains less than 1% twice in a row: stagnation
+            stalled = stalled + 1 if beta > 0.99 * beta_start else 0
+            if stalled >= 2:
+                break
         self.iterations = its
-        raise LinearSolverError(f"GMRES did not converge in {maxiter} iterations (residual {beta:.3e}, "
+        raise LinearSolverError(f"GMRES did not converge in {its} iterations (residual {beta:.3e}, "
                                 f"target {target:.3e})")

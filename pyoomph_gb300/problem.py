@@ -1299,9 +1299,12 @@ class Problem:
             tb = time.perf_counter()
             with nvtx_range("linear solve"):
                 if self.linear_solver == "fieldsplit":
+                    # an inexact Newton step: no more accuracy than the Newton
+                    # criterion can see (a relative target below the attainable
+                    # accuracy of a small late-step residual would stall)
                     dxd, its = self._fieldsplit_solver().solve(
                         self.R_dev[:self.n_dof], tol=max(self.linear_solver_tolerance, self.fieldsplit_min_tolerance),
-                        atol=self.linear_solver_atol)
+                        atol=max(self.linear_solver_atol, 0.01 * self.newton_solver_tolerance))
                     self.timings["krylov_iterations"] = self.timings.get("krylov_iterations", 0) + int(its)
                 elif device_solve:
                     from .linsolve import BatchedBiCGStab, DeviceCSR
