@@ -627,8 +627,9 @@ def measure_serving_bounded(requests: int = 200, rate: float = 50.0, side_max: i
     """A bounded serving stream: Poisson-process arrivals of Poisson and
     Navier-Stokes assemble+Newton requests (sides log-uniform in
     [16, side_max]) through the continuous-batching FP32-Jacobian server
-    (Poisson requests solved on the device, Navier-Stokes ones by SuperLU
-    in worker processes), and the plain FP64 one-request-at-a-time path on
+    (every Newton system solved on the device: batched BiCGStab for the
+    Poisson requests, the saddle-point GMRES for the Navier-Stokes ones),
+    and the plain FP64 one-request-at-a-time path on
     the first seq_requests of the same stream."""
     import copy
     from pyoomph_gb300 import serving as S
@@ -644,8 +645,8 @@ def measure_serving_bounded(requests: int = 200, rate: float = 50.0, side_max: i
     out = {"requests": requests, "rate_per_s": rate, "side_range": [16, side_max], "wall_s": wall,
            "batched_fp32": S.summary(done, wall), "assemblies": srv.assemblies,
            "gpu_launches": srv.launches + srv.solver_launches, "device_solves": srv.device_solves,
-           "linear_solver": f"Poisson: native batched BiCGStab on the device; Navier-Stokes: SuperLU, {workers} "
-                            f"worker processes"}
+           "linear_solver": "Poisson: native batched BiCGStab on the device; Navier-Stokes: saddle-point GMRES "
+                            "with the block-triangular multigrid preconditioner on the device (fieldsplit.py)"}
     srv.close()
     sub = copy.deepcopy(reqs[:seq_requests])
     t0 = time.perf_counter()

@@ -120,6 +120,33 @@ def lumped_field_mass(P, field: str) -> np.ndarray:
     return out
 
 
+class BlockView:
+    """One diagonal block (replica s) of a problem stacking independent
+    replicas, seen as a problem of its own by SaddlePointSolver: replica
+    0's pattern, numbering and mesh (every replica has them), replica s's
+    Jacobian values (a view of `vals`, the stacked values or a snapshot of
+    them)."""
+
+    def __init__(self, P, s: int, vals, rp_host, ci_host, rp_dev, ci_dev):
+        from types import SimpleNamespace
+        n0, e0 = P.base_n_nodes, P.base_n_elem
+        self.n_dof = int(rp_host.shape[0] - 1)
+        self.nnz = int(ci_host.shape[0])
+        self.J_dev = vals[s * self.nnz:(s + 1) * self.nnz]
+        self.fields = P.fields
+        self.eqn = np.asarray(P.eqn).reshape(P.mesh.n_nodes, len(P.fields))[:n0]
+        self.mesh = SimpleNamespace(n_nodes=n0, n_elem=e0, x=P.mesh.x[:n0], conn=P.mesh.conn[:e0],
+                                    etype=P.mesh.etype)
+        self._rp, self._ci = rp_host, ci_host
+        self._rpd, self._cid = rp_dev, ci_dev
+
+    def pattern(self):
+        return self._rp, self._ci
+
+    def device_csr(self) -> DeviceCSR:
+        return DeviceCSR(self._rpd.data_ptr(), self._cid.data_ptr(), self.J_dev, self.n_dof, self.nnz)
+
+
 class SaddlePointSolver:
     """GMRES with the block-triangular multigrid preconditioner for the
     Jacobian of a problem with one constrained field (the pressure):
@@ -181,7 +208,8 @@ class SaddlePointSolver:
         self.schur_scale = float(schur_scale)
         self.levels: Optional[List[dict]] = None
         self.iterations = 0
-        self.J = DeviceCSR.of_problem(P)
+        self.stagnated = False
+        self.J = P.device_csr() if hasattr(P, "device_csr") else DeviceCSR.of_problem(P)
 
     # -- set-up ------------------------------------------------------------
     def _host_blocks(self):
@@ -353,9 +381,46 @@ class SaddlePointSolver:
                 self.iterations = its
                 return x, its
             # a restart cycle that gains less than 1% twice in a row: stagnation
+            # at the attainable accuracy; the Newton step is taken as it is
+            # (the Newton loop's residual check decides), unless nothing was
+            # gained at all
             stalled = stalled + 1 if beta > 0.99 * beta_start else 0
             if stalled >= 2:
                 break
         self.iterations = its
+        if np.isfinite(beta) and beta <= 1e-3 * bnorm:
+            self.stagnated = True
+            return x, its
         raise LinearSolverError(f"GMRES did not converge in {its} iterations (residual {beta:.3e}, "
                                 f"target {target:.3e})")
+
+
+def _main(argv=None) -> None:
+    """One device Newton solve of the Navier-Stokes workload with this
+    solver (a small driver for profiling): ``python -m
+    pyoomph_gb300.fieldsplit 128 fp64`` = side 128, FP64 Jacobian."""
+    import argparse
+    import time
+    import torch
+    from . import workloads as W
+    ap = argparse.ArgumentParser(prog="python -m pyoomph_gb300.fieldsplit")
+    ap.add_argument("side", type=int)
+    ap.add_argument("precision", choices=["fp64", "fp32"], nargs="?", default="fp64")
+    a = ap.parse_args(argv)
+    P = W.navier_stokes_problem(N=a.side, jacobian_precision=a.precision)
+    P.initialise()
+    W.perturb_dofs(P, seed=0, sigma=1e-3)
+    P.linear_solver = "fieldsplit"
+    P.newton_solver_tolerance = 1e-10
+    P.max_newton_iterations = 30
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = P.solve()
+    torch.cuda.synchronize()
+    print(f"ns side {a.side} {a.precision}: {P.n_dof} dofs, {len(hist) - 1} Newton steps, "
+          f"{P.timings.get('krylov_iterations')} GMRES iterations, {time.perf_counter() - t0:.3f} s, "
+          f"max |R| {hist[-1]:.2e}, levels {P._fieldsplit.sizes}")
+
+
+if __name__ == "__main__":
+    _main()

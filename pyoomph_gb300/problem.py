@@ -1304,7 +1304,7 @@ class Problem:
                     # accuracy of a small late-step residual would stall)
                     dxd, its = self._fieldsplit_solver().solve(
                         self.R_dev[:self.n_dof], tol=max(self.linear_solver_tolerance, self.fieldsplit_min_tolerance),
-                        atol=max(self.linear_solver_atol, 0.01 * self.newton_solver_tolerance))
+                        atol=max(self.linear_solver_atol, 1e-3 * self.newton_solver_tolerance))
                     self.timings["krylov_iterations"] = self.timings.get("krylov_iterations", 0) + int(its)
                 elif device_solve:
                     from .linsolve import BatchedBiCGStab, DeviceCSR

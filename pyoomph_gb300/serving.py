@@ -19,9 +19,13 @@ sequence for all its replicas (dof scatter, element kernel, residual and
 Jacobian scatter) on the class's own CUDA stream, with the per-replica
 residual max-norms reduced on the device -- so the solves of all active
 requests run in parallel on the host cores while the GPU assembles.  With
-``device_solver=True`` the Poisson requests of a class are solved on the
-device instead: one batched Jacobi-BiCGStab over the class's replicas
-(``linsolve.BatchedBiCGStab``, CUDA-graph blocks of iterations).
+``device_solver=True`` every request is solved on the device instead: the
+Poisson requests of a class by one batched Jacobi-BiCGStab over the class's
+replicas (``linsolve.BatchedBiCGStab``, CUDA-graph blocks of iterations),
+each Navier-Stokes request by its own saddle-point solver over its
+replica's diagonal block (``fieldsplit.SaddlePointSolver``: GMRES with a
+block-triangular multigrid preconditioner built from that request's own
+Jacobian).
 
 Results do not depend on the mix: every element, CSR slot and residual
 entry of a replica is computed from that replica's values only, in a fixed
@@ -163,6 +167,8 @@ class _Batch:
         self.x0 = P.get_dofs()[:self.n_dof].copy()
         self.last_used = time.perf_counter()
         self.krylov = None      # device solver of the class (device_solver=True)
+        self.fs = {}            # Navier-Stokes: the device saddle-point solver of each slot's request
+        self.pat_dev = None     # replica 0's pattern on the device (for those solvers)
         self.jsnap = None       # the J values and residual the in-flight device solve reads
         self.rsnap = None
         self.inflight = False   # a device solve of this class is running
@@ -267,7 +273,7 @@ class Server:
         P = b.P
         done = []
         dev_solve: List[int] = []
-        on_device = self.device_solver and b.key[0] == "poisson"
+        on_device = self.device_solver
         with torch.cuda.stream(b.stream):
             P.assemble_device(with_jacobian=True, stream=b.stream.cuda_stream)
             self.launches += P.launch_count(True)
@@ -286,6 +292,7 @@ class Server:
                 req.t_done = time.perf_counter() - t0
                 b.req[s] = None
                 b.state[s] = "free"
+                b.fs.pop(s, None)
                 done.append(req)
                 continue
             if on_device:
@@ -307,9 +314,10 @@ class Server:
             # class can be re-assembled meanwhile
             from .linsolve import BatchedBiCGStab, DeviceCSR
             with torch.cuda.stream(b.stream):
-                if b.krylov is None:
+                if b.jsnap is None:
                     b.jsnap = torch.empty_like(P.J_dev[:P.nnz])
                     b.rsnap = torch.empty_like(P.R_dev[:P.n_dof])
+                if b.krylov is None and b.key[0] == "poisson":
                     b.krylov = BatchedBiCGStab(DeviceCSR.of_problem(P, vals=b.jsnap), blocks=b.slots)
                 b.jsnap.copy_(P.J_dev[:P.nnz])
                 b.rsnap.copy_(P.R_dev[:P.n_dof])
@@ -323,7 +331,8 @@ class Server:
             # max(1e-13 |R_s|, 0.1 tol) -- a pure 1e-13 relative target is
             # below the attainable accuracy of large meshes (cond x eps) --
             # and the target depends on the block's own residual only
-            fut = self.tpool.submit(self._device_solve, b, mask, 0.1 * self.tol)
+            solve = self._device_solve if b.key[0] == "poisson" else self._device_solve_saddle
+            fut = self.tpool.submit(solve, b, mask, 0.1 * self.tol)
             futs[fut] = (b, tuple(dev_solve), time.perf_counter())
         b.last_used = time.perf_counter()
         return done
@@ -333,6 +342,33 @@ class Server:
         l0 = b.krylov.info()["launches"]
         dx, _ = b.krylov.solve(b.rsnap, active=mask, tol=1e-13, atol=atol, stream=b.stream.cuda_stream)
         return dx, b.krylov.info()["launches"] - l0
+
+    def _device_solve_saddle(self, b: _Batch, mask: np.ndarray, atol: float):
+        """Worker thread: the Navier-Stokes Newton steps of one class on the
+        device, one request after the other, each with its own saddle-point
+        solver (fieldsplit.py) over its replica's diagonal block of the J
+        snapshot.  A request's solver is built from its own first Jacobian
+        and kept for its later steps, so nothing it computes depends on the
+        other requests of the class."""
+        from .fieldsplit import BlockView, SaddlePointSolver
+        torch = self.torch
+        P = b.P
+        with torch.cuda.stream(b.stream):
+            if b.pat_dev is None:
+                rp, ci = P.pattern()
+                rp0, ci0 = rp[:b.n_dof + 1].copy(), ci[:b.nnz].copy()
+                b.pat_dev = (rp0, ci0, torch.as_tensor(rp0, device="cuda"), torch.as_tensor(ci0, device="cuda"))
+            rp0, ci0, rpd, cid = b.pat_dev
+            dx = torch.zeros((b.slots, b.n_dof), dtype=torch.float64, device="cuda")
+            rv = b.rsnap.view(b.slots, b.n_dof)
+            for s in np.nonzero(mask)[0]:
+                sol = b.fs.get(int(s))
+                if sol is None:
+                    view = BlockView(P, int(s), b.jsnap, rp0, ci0, rpd, cid)
+                    sol = b.fs[int(s)] = SaddlePointSolver(view, "pressure", 1.0 / b.req[s].Re)
+                x, _ = sol.solve(rv[s], tol=1e-11, atol=atol)
+                dx[s] = x
+        return dx, 0
 
     def _apply_device(self, b: _Batch, slots, result) -> None:
         dx, launches = result
@@ -366,6 +402,7 @@ class Server:
             req.t_done = time.perf_counter() - t0
             b.req[s] = None
             b.state[s] = "free"
+            b.fs.pop(s, None)
             out.append(req)
         if device:
             b.inflight = False
@@ -443,8 +480,8 @@ def serve_sequential(requests: List[Request], precision: str = "fp64", tol: floa
         key = (req.kind, req.side)
         if key not in cache:
             P = _class_problem(req.kind, req.side, precision, 1)
-            if device_solver and req.kind == "poisson":
-                P.linear_solver = "bicgstab"
+            if device_solver:
+                P.linear_solver = "bicgstab" if req.kind == "poisson" else "fieldsplit"
                 P.linear_solver_atol = 0.1 * tol     # the batched server's inexact step
             P.initialise()
             cache[key] = (P, P.get_dofs().copy())

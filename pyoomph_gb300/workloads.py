@@ -116,6 +116,8 @@ def _main(argv=None) -> None:
     ap.add_argument("--tc", type=int, choices=[0, 1], default=None,
                     help="1: FP32 Jacobian contracted on the tensor cores, 0: on the FP32 pipes "
                          "(default: the generator's)")
+    ap.add_argument("--zero-filter", action="store_true",
+                    help="assemble J in the reference's zero-filtered pattern (threshold 0.0)")
     ap.add_argument("--transient", action="store_true",
                     help="the transient form (BDF2 weights of dt = 1e-3, both previous levels = the current values)")
     a = ap.parse_args(argv)
@@ -138,12 +140,13 @@ def _main(argv=None) -> None:
         P.set_history_values(0, P.get_values())
         P.set_history_values(1, P.get_values())
         P.set_parameters(**dict(zip(("_bdf_w0", "_bdf_w1", "_bdf_w2"), bdf_weights(2, 1e-3, 1e-3))))
-    P.assemble_device(with_jacobian=True)
+    zt = 0.0 if a.zero_filter else None
+    P.assemble_device(with_jacobian=True, zero_threshold=zt)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(a.repeat):
-        P.assemble_device(with_jacobian=True)
+        P.assemble_device(with_jacobian=True, zero_threshold=zt)
     e1.record()
     torch.cuda.synchronize()
     P.check()

@@ -100,3 +100,25 @@ def test_failed_device_solve_ends_only_its_requests(monkeypatch):
         if r.error is None:
             x = _oracle_solution(r)
             assert np.max(np.abs(r.dofs - x)) <= 1e-10 * max(1.0, np.max(np.abs(x)))
+
+
+def test_navier_stokes_requests_on_the_device_alone_equal_mix():
+    """Navier-Stokes requests solved on the device (each by its own
+    saddle-point solver over its replica's block): bit-identical alone or
+    in a mix with other requests of the class, and within 1e-10 of the
+    oracle's solution."""
+    from pyoomph_gb300 import serving as S
+    srv = S.Server(slots=3, tol=1e-12, device_solver=True)
+    alone = srv.run([S.Request(0, "ns", 10, 0.0, seed=5, Re=70.0)], realtime=False)[0]
+    srv.close()
+    assert alone.error is None, alone.error
+    mix = [S.Request(1, "ns", 10, 0.0, seed=1, Re=40.0), S.Request(2, "poisson", 8, 0.0, seed=2),
+           S.Request(0, "ns", 10, 0.0, seed=5, Re=70.0), S.Request(3, "ns", 10, 0.0, seed=3, Re=100.0)]
+    srv = S.Server(slots=3, tol=1e-12, device_solver=True)
+    out = {r.rid: r for r in srv.run(mix, realtime=False)}
+    srv.close()
+    assert np.array_equal(out[0].dofs, alone.dofs)
+    for r in out.values():
+        assert r.error is None, r.error
+        x = _oracle_solution(r)
+        assert np.max(np.abs(r.dofs - x)) <= 1e-10 * max(1.0, np.max(np.abs(x)))
