@@ -11,13 +11,13 @@ import oracle as O
 pytestmark = pytest.mark.gpu
 
 
-def _oracle_solution(req):
+def _oracle_solution(req, tol: float = 1e-10):
     from pyoomph_gb300 import workloads as W
     if req.kind == "poisson":
         OP = O.poisson_problem(O.mesh(O.Q2_QUAD, req.side, req.side), W.draw_gaussians(req.seed, 8, 2))
     else:
         OP = O.navier_stokes_problem(O.mesh(O.P2_TRI, req.side, req.side), rho=1.0, mu=1.0 / req.Re)
-    O.newton(OP, tol=1e-10)
+    O.newton(OP, tol=tol)
     return OP.dofs()
 
 
@@ -120,5 +120,8 @@ def test_navier_stokes_requests_on_the_device_alone_equal_mix():
     assert np.array_equal(out[0].dofs, alone.dofs)
     for r in out.values():
         assert r.error is None, r.error
-        x = _oracle_solution(r)
+        # the device solves take inexact Newton steps, so the requests follow
+        # other iterates than the oracle's exact ones: both are compared
+        # converged well below the tolerance (the oracle to 1e-13)
+        x = _oracle_solution(r, tol=1e-13)
         assert np.max(np.abs(r.dofs - x)) <= 1e-10 * max(1.0, np.max(np.abs(x)))
