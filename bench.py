@@ -627,9 +627,10 @@ def measure_serving_bounded(requests: int = 200, rate: float = 50.0, side_max: i
     """A bounded serving stream: Poisson-process arrivals of Poisson and
     Navier-Stokes assemble+Newton requests (sides log-uniform in
     [16, side_max]) through the continuous-batching FP32-Jacobian server
-    (every Newton system solved on the device: batched BiCGStab for the
-    Poisson requests, the saddle-point GMRES for the Navier-Stokes ones),
-    and the plain FP64 one-request-at-a-time path on
+    (Poisson Newton systems solved on the device by the batched BiCGStab;
+    Navier-Stokes ones by SuperLU in worker processes below the server's
+    device_saddle_min_side, by the device saddle-point GMRES from it), and
+    the plain FP64 one-request-at-a-time path on
     the first seq_requests of the same stream."""
     import copy
     from pyoomph_gb300 import serving as S
@@ -645,17 +646,21 @@ def measure_serving_bounded(requests: int = 200, rate: float = 50.0, side_max: i
     out = {"requests": requests, "rate_per_s": rate, "side_range": [16, side_max], "wall_s": wall,
            "batched_fp32": S.summary(done, wall), "assemblies": srv.assemblies,
            "gpu_launches": srv.launches + srv.solver_launches, "device_solves": srv.device_solves,
-           "linear_solver": "Poisson: native batched BiCGStab on the device; Navier-Stokes: saddle-point GMRES "
-                            "with the block-triangular multigrid preconditioner on the device (fieldsplit.py)"}
+           "linear_solver": f"Poisson: native batched BiCGStab on the device; Navier-Stokes: SuperLU in "
+                            f"{workers} worker processes below side {srv.device_saddle_min_side}, the device "
+                            f"saddle-point GMRES (fieldsplit.py) from it"}
     srv.close()
     sub = copy.deepcopy(reqs[:seq_requests])
     t0 = time.perf_counter()
     seq = S.serve_sequential(sub, precision="fp64", device_solver=True)
     wall2 = time.perf_counter() - t0
     out["sequential_fp64_first_requests"] = dict(S.summary(seq, wall2), requests=seq_requests)
-    by = {r.rid: r.dofs for r in done}
+    by = {r.rid: r for r in done}
+    ok = [r for r in seq if r.error is None and by[r.rid].error is None]
     out["max_rel_solution_difference_batched_vs_sequential"] = max(
-        float(np.max(np.abs(by[r.rid] - r.dofs)) / max(1.0, float(np.max(np.abs(r.dofs))))) for r in seq)
+        [float(np.max(np.abs(by[r.rid].dofs - r.dofs)) / max(1.0, float(np.max(np.abs(r.dofs))))) for r in ok],
+        default=None)
+    out["requests_compared"] = len(ok)
     return out
 
 

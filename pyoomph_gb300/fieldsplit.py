@@ -209,7 +209,17 @@ class SaddlePointSolver:
         self.levels: Optional[List[dict]] = None
         self.iterations = 0
         self.stagnated = False
+        self.use_graph = True
+        self._graph = None
         self.J = P.device_csr() if hasattr(P, "device_csr") else DeviceCSR.of_problem(P)
+
+    def renew_if_changed(self, key, schur_scale: float) -> None:
+        """Forget the hierarchy (rebuilt at the next solve) when `key` (the
+        problem's parameters) differs from the one it was built for."""
+        if key != getattr(self, "_key", None):
+            self._key = key
+            self.schur_scale = float(schur_scale)
+            self.levels = None
 
     # -- set-up ------------------------------------------------------------
     def _host_blocks(self):
@@ -259,6 +269,7 @@ class SaddlePointSolver:
             A, comp = Ac, cc
         self.coarse_inv = torch.linalg.inv(torch.as_tensor(A.toarray(), device=self.dev))
         self.levels = levels
+        self._graph = None                          # recaptured for the new hierarchy
         self.Bt = _DevCSR(torch, Bt, self.dev)
         self.sizes = [lv["n"] for lv in levels] + [A.shape[0]]
 
@@ -287,6 +298,33 @@ class SaddlePointSolver:
         return x
 
     def precondition(self, r):
+        """z = P^-1 r (the captured CUDA graph where there is one)."""
+        if self._graph is None and self.use_graph:
+            self._capture()
+        if self._graph is None:
+            return self._precondition(r)
+        self._gin.copy_(r)
+        self._graph.replay()
+        return self._gout
+
+    def _capture(self) -> None:
+        """Record one preconditioner application (every level's SpMVs, the
+        smoothing and transfer updates, the coarse solve: about a hundred
+        launches) as a CUDA graph on fixed buffers; the matrices it reads are
+        refreshed in place between Newton steps."""
+        torch = self.torch
+        self._gin = torch.zeros(self.P.n_dof, dtype=torch.float64, device=self.dev)
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self._precondition(self._gin)           # warm-up: kernels loaded, buffers cached
+        torch.cuda.current_stream().wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._gout = self._precondition(self._gin)
+        self._graph = g
+
+    def _precondition(self, r):
         """z = P^-1 r: p = S_hat^-1 r_p, u = A_hat^-1 (r_u - Bt p)."""
         torch = self.torch
         st = torch.cuda.current_stream().cuda_stream

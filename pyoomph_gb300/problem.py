@@ -943,14 +943,18 @@ class Problem:
         built at the first solve: the constrained field and the viscosity
         scaling its Schur complement come from the equations
         (StokesEquations.saddle_point)."""
+        if self.saddle_point is None:
+            raise RuntimeError("linear_solver='fieldsplit' needs equations with a constrained field "
+                               "(Stokes / Navier-Stokes)")
+        field, scale_param = self.saddle_point
+        scale = float(self.params[self.param_names.index(scale_param)])
         if getattr(self, "_fieldsplit", None) is None:
             from .fieldsplit import SaddlePointSolver
-            if self.saddle_point is None:
-                raise RuntimeError("linear_solver='fieldsplit' needs equations with a constrained field "
-                                   "(Stokes / Navier-Stokes)")
-            field, scale_param = self.saddle_point
-            scale = float(self.params[self.param_names.index(scale_param)])
             self._fieldsplit = SaddlePointSolver(self, field, scale)
+        # the hierarchy belongs to the parameters it was built for: new
+        # parameters (another viscosity, another request) rebuild it at the
+        # next solve
+        self._fieldsplit.renew_if_changed(tuple(np.asarray(self.params, dtype=float)), scale)
         return self._fieldsplit
 
     def solve_linear_device(self, b: np.ndarray) -> np.ndarray:

@@ -22,10 +22,12 @@ requests run in parallel on the host cores while the GPU assembles.  With
 ``device_solver=True`` every request is solved on the device instead: the
 Poisson requests of a class by one batched Jacobi-BiCGStab over the class's
 replicas (``linsolve.BatchedBiCGStab``, CUDA-graph blocks of iterations),
-each Navier-Stokes request by its own saddle-point solver over its
-replica's diagonal block (``fieldsplit.SaddlePointSolver``: GMRES with a
-block-triangular multigrid preconditioner built from that request's own
-Jacobian).
+each Navier-Stokes request of side >= ``device_saddle_min_side`` by its
+own saddle-point solver over its replica's diagonal block
+(``fieldsplit.SaddlePointSolver``: GMRES with a block-triangular multigrid
+preconditioner built from that request's own Jacobian); smaller
+Navier-Stokes systems stay with SuperLU in the workers, which solves many
+of them in parallel faster.
 
 Results do not depend on the mix: every element, CSR slot and residual
 entry of a replica is computed from that replica's values only, in a fixed
@@ -212,6 +214,10 @@ class Server:
         # request's iterates never depend on its neighbours), instead of
         # SuperLU in the workers
         self.device_solver = device_solver
+        # Navier-Stokes requests of at least this side are solved on the
+        # device (saddle-point GMRES), smaller ones by SuperLU in the worker
+        # processes, which solve many small systems in parallel faster
+        self.device_saddle_min_side = 96
         # device solves run in threads (the native solve releases the GIL),
         # so a long solve of one class does not stall the others
         self.tpool = cf.ThreadPoolExecutor(max_workers=4) if device_solver else None
@@ -273,7 +279,7 @@ class Server:
         P = b.P
         done = []
         dev_solve: List[int] = []
-        on_device = self.device_solver
+        on_device = self.device_solver and (b.key[0] == "poisson" or b.key[1] >= self.device_saddle_min_side)
         with torch.cuda.stream(b.stream):
             P.assemble_device(with_jacobian=True, stream=b.stream.cuda_stream)
             self.launches += P.launch_count(True)
@@ -466,7 +472,8 @@ class Server:
 
 
 def serve_sequential(requests: List[Request], precision: str = "fp64", tol: float = 1e-10,
-                     realtime: bool = True, device_solver: bool = False) -> List[Request]:
+                     realtime: bool = True, device_solver: bool = False,
+                     device_saddle_min_side: int = 96) -> List[Request]:
     """The plain path: requests one at a time in arrival order, one problem
     per request (resident meshes cached per class), Newton with SuperLU
     (with device_solver: Poisson requests with the device BiCGStab, as the
@@ -480,7 +487,7 @@ def serve_sequential(requests: List[Request], precision: str = "fp64", tol: floa
         key = (req.kind, req.side)
         if key not in cache:
             P = _class_problem(req.kind, req.side, precision, 1)
-            if device_solver:
+            if device_solver and (req.kind == "poisson" or req.side >= device_saddle_min_side):
                 P.linear_solver = "bicgstab" if req.kind == "poisson" else "fieldsplit"
                 P.linear_solver_atol = 0.1 * tol     # the batched server's inexact step
             P.initialise()

@@ -109,13 +109,16 @@ def test_navier_stokes_requests_on_the_device_alone_equal_mix():
     oracle's solution."""
     from pyoomph_gb300 import serving as S
     srv = S.Server(slots=3, tol=1e-12, device_solver=True)
+    srv.device_saddle_min_side = 8
     alone = srv.run([S.Request(0, "ns", 10, 0.0, seed=5, Re=70.0)], realtime=False)[0]
     srv.close()
     assert alone.error is None, alone.error
     mix = [S.Request(1, "ns", 10, 0.0, seed=1, Re=40.0), S.Request(2, "poisson", 8, 0.0, seed=2),
            S.Request(0, "ns", 10, 0.0, seed=5, Re=70.0), S.Request(3, "ns", 10, 0.0, seed=3, Re=100.0)]
     srv = S.Server(slots=3, tol=1e-12, device_solver=True)
+    srv.device_saddle_min_side = 8
     out = {r.rid: r for r in srv.run(mix, realtime=False)}
+    assert srv.device_solves > 0
     srv.close()
     assert np.array_equal(out[0].dofs, alone.dofs)
     for r in out.values():
