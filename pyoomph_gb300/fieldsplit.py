@@ -267,7 +267,9 @@ class SaddlePointSolver:
                            "t": torch.zeros(n, dtype=torch.float64, device=self.dev),
                            "bc": torch.zeros(na, dtype=torch.float64, device=self.dev)})
             A, comp = Ac, cc
-        self.coarse_inv = torch.linalg.inv(torch.as_tensor(A.toarray(), device=self.dev))
+        # the coarsest operator's inverse on the host (<= coarse_size unknowns;
+        # numpy, so no device linear-algebra library is loaded for it)
+        self.coarse_inv = torch.as_tensor(np.linalg.inv(A.toarray()), device=self.dev)
         self.levels = levels
         self._graph = None                          # recaptured for the new hierarchy
         self.Bt = _DevCSR(torch, Bt, self.dev)
