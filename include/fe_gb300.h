@@ -311,6 +311,13 @@ int fe_assemble_host(fe_problem_t *p, const double *dofs, double *R, void *J_val
  */
 int fe_csr_spmv(const int32_t *rowptr, const int32_t *colidx, const void *vals, int val_precision, const double *x,
                 double *y, int64_t n, int64_t nnz, void *stream);
+/* y = z + sc * w o (b - A x) for an FP64 CSR matrix (square or not; DEVICE
+ * pointers), z, b, w each optional (NULL: 0, 0, 1): the damped-Jacobi,
+ * residual and prolongation updates of the saddle-point solver's multigrid
+ * cycle in one pass over the matrix (no counterpart on the reference's
+ * path, which solves with SuperLU).  y must not alias x. */
+int fe_csr_update(const int32_t *rowptr, const int32_t *colidx, const double *vals, const double *x, const double *b,
+                  const double *z, const double *w, double sc, double *y, int64_t n, int64_t nnz, void *stream);
 int fe_csr_diagonal(const int32_t *rowptr, const int32_t *colidx, const void *vals, int val_precision, double *diag,
                     int64_t n, void *stream);
 

@@ -34,7 +34,8 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_assemble_pipelined", "fe_csr_spmv", "fe_csr_diagonal", "fe_krylov_create", "fe_krylov_solve",
            "fe_krylov_matvec", "fe_krylov_info", "fe_krylov_destroy", "fe_problem_set_direction",
            "fe_problem_set_persistent", "fe_problem_set_zero_threshold", "fe_problem_filtered_pattern",
-           "fe_problem_set_tensor_contraction", "fe_tc_contract", "fe_sa_aggregate"]
+           "fe_problem_set_tensor_contraction", "fe_tc_contract", "fe_sa_aggregate",
+           "fe_csr_update"]
 
 
 def _header_stamp() -> str:
@@ -154,6 +155,7 @@ def load(build_if_missing: bool = True):
         L.fe_problem_set_tensor_contraction.argtypes = [vp, c_int, c_int, c_int, c_int, vp, c_int, vp, vp]
         L.fe_tc_contract.argtypes = [vp, vp, i64, c_int, c_int, c_int, vp, c_int, vp, vp, vp]
         L.fe_sa_aggregate.argtypes = [i64, vp, vp, vp, vp, ctypes.c_double, vp, vp]
+        L.fe_csr_update.argtypes = [vp, vp, vp, vp, vp, vp, vp, ctypes.c_double, vp, i64, i64, vp]
         L.fe_problem_shift_history.argtypes = [vp]
         L.fe_problem_set_positions.argtypes = [vp, vp]
         L.fe_problem_graph_capture.argtypes = [vp, vp, vp, vp, c_int]

@@ -56,6 +56,16 @@ class _DevCSR:
         self.ci = torch.as_tensor(A.indices.astype(np.int32) if A.nnz else np.zeros(1, np.int32), device=dev)
         self.v = torch.as_tensor(A.data.astype(np.float64) if A.nnz else np.zeros(1), device=dev)
 
+    def update(self, x, b, z, w, sc: float, y, stream) -> None:
+        """y = z + sc * w o (b - A x) (fe_csr_update; None: 0, 0, 1)."""
+        if self.n == 0:
+            return
+        ptr = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
+        N.check(N.load().fe_csr_update(ctypes.c_void_p(self.rp.data_ptr()), ctypes.c_void_p(self.ci.data_ptr()),
+                                       ctypes.c_void_p(self.v.data_ptr()), ptr(x), ptr(b), ptr(z), ptr(w),
+                                       float(sc), ctypes.c_void_p(y.data_ptr()), self.n, self.nnz,
+                                       ctypes.c_void_p(stream)))
+
     def mv(self, x, y, stream) -> None:
         if self.n == 0:
             return
@@ -211,6 +221,7 @@ class SaddlePointSolver:
         self.stagnated = False
         self.use_graph = True
         self._graph = None
+        self.check_every = 4          # Arnoldi steps between host looks at the residual estimate
         self.J = P.device_csr() if hasattr(P, "device_csr") else DeviceCSR.of_problem(P)
 
     def renew_if_changed(self, key, schur_scale: float) -> None:
@@ -263,7 +274,9 @@ class SaddlePointSolver:
             levels.append({"A": _DevCSR(torch, A, self.dev), "P": _DevCSR(torch, Pm, self.dev),
                            "R": _DevCSR(torch, Pm.T.tocsr(), self.dev),
                            "dinv": torch.as_tensor(1.0 / Dl, device=self.dev), "om": 1.0 / lam, "n": n, "nc": na,
+                           "dinv_om": torch.as_tensor((1.0 / lam) / Dl, device=self.dev),
                            "x": torch.zeros(n, dtype=torch.float64, device=self.dev),
+                           "x2": torch.zeros(n, dtype=torch.float64, device=self.dev),
                            "t": torch.zeros(n, dtype=torch.float64, device=self.dev),
                            "bc": torch.zeros(na, dtype=torch.float64, device=self.dev)})
             A, comp = Ac, cc
@@ -278,25 +291,27 @@ class SaddlePointSolver:
     # -- application -------------------------------------------------------
     def _vcycle(self, lvl: int, b):
         """One V-cycle on level lvl for right-hand side b: nu damped-Jacobi
-        steps from zero, the coarse-grid correction, nu steps.  Returns the
-        level's iterate buffer (valid until the next cycle on this level)."""
+        steps from zero, the coarse-grid correction, nu steps; every update
+        one fused pass over its matrix (fe_csr_update).  Returns one of the
+        level's iterate buffers (valid until the next cycle on this level)."""
         torch = self.torch
         st = torch.cuda.current_stream().cuda_stream
         if lvl == len(self.levels):
             return self.coarse_inv @ b
         L = self.levels[lvl]
-        x, t, dinv, om = L["x"], L["t"], L["dinv"], L["om"]
-        torch.mul(b, dinv, out=x).mul_(om)
+        A, dinv, om = L["A"], L["dinv"], L["om"]
+        x, y = L["x"], L["x2"]
+        torch.mul(b, L["dinv_om"], out=x)                     # the first step from zero
         for _ in range(self.nu - 1):
-            L["A"].mv(x, t, st)
-            x.addcmul_(b - t, dinv, value=om)
-        L["A"].mv(x, t, st)
-        L["R"].mv(b - t, L["bc"], st)
-        L["P"].mv(self._vcycle(lvl + 1, L["bc"]), t, st)
-        x.add_(t)
+            A.update(x, b, x, dinv, om, y, st)
+            x, y = y, x
+        A.update(x, b, None, None, 1.0, L["t"], st)            # residual
+        L["R"].mv(L["t"], L["bc"], st)                         # restriction
+        L["P"].update(self._vcycle(lvl + 1, L["bc"]), None, x, None, -1.0, y, st)   # x + P xc
+        x, y = y, x
         for _ in range(self.nu):
-            L["A"].mv(x, t, st)
-            x.addcmul_(b - t, dinv, value=om)
+            A.update(x, b, x, dinv, om, y, st)
+            x, y = y, x
         return x
 
     def precondition(self, r):
@@ -379,36 +394,45 @@ class SaddlePointSolver:
             g = np.zeros(m + 1)
             g[0] = beta
             cs, sn = np.zeros(m), np.zeros(m)
+            Hd = torch.zeros((m + 1, m), dtype=torch.float64, device=self.dev)
             k = 0
+            done = False
             for k in range(m):
                 z = self.precondition(V[k])
                 self.J.matvec(z, Az, st)
-                w = Az
-                h = V[:k + 1] @ w
-                w = w - V[:k + 1].T @ h
+                h = V[:k + 1] @ Az
+                w = Az - V[:k + 1].T @ h
                 h2 = V[:k + 1] @ w               # second pass (classical Gram-Schmidt twice)
-                w = w - V[:k + 1].T @ h2
-                hk = (h + h2)
+                w -= V[:k + 1].T @ h2
                 nw = torch.linalg.vector_norm(w)
-                hv = torch.cat([hk, nw.reshape(1)]).cpu().numpy()   # one synchronisation per iteration
-                H[:k + 1, k] = hv[:-1]
-                H[k + 1, k] = hv[-1]
-                if hv[-1] > 0:
-                    V[k + 1] = w / hv[-1]
-                for i in range(k):               # Givens rotations
-                    t_ = cs[i] * H[i, k] + sn[i] * H[i + 1, k]
-                    H[i + 1, k] = -sn[i] * H[i, k] + cs[i] * H[i + 1, k]
-                    H[i, k] = t_
-                den = np.hypot(H[k, k], H[k + 1, k])
-                cs[k], sn[k] = (1.0, 0.0) if den == 0 else (H[k, k] / den, H[k + 1, k] / den)
-                H[k, k] = den
-                H[k + 1, k] = 0.0
-                g[k + 1] = -sn[k] * g[k]
-                g[k] = cs[k] * g[k]
+                Hd[:k + 1, k] = h + h2
+                Hd[k + 1, k] = nw
+                V[k + 1] = w / nw.clamp_min(1e-300)
                 its += 1
-                if not np.isfinite(g[k + 1]):
-                    raise LinearSolverError("GMRES broke down (non-finite residual)")
-                if abs(g[k + 1]) <= target or its >= maxiter:
+                if (k + 1) % self.check_every and k + 1 < m and its < maxiter:
+                    continue                     # the host looks every check_every steps only
+                # Givens rotations of the columns since the last look (one synchronisation)
+                k0 = (k // self.check_every) * self.check_every if (k + 1) % self.check_every else k + 1 - self.check_every
+                k0 = max(0, min(k0, k))
+                H[:, k0:k + 1] = Hd[:, k0:k + 1].cpu().numpy()
+                for j in range(k0, k + 1):
+                    for i in range(j):
+                        t_ = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
+                        H[i + 1, j] = -sn[i] * H[i, j] + cs[i] * H[i + 1, j]
+                        H[i, j] = t_
+                    den = np.hypot(H[j, j], H[j + 1, j])
+                    cs[j], sn[j] = (1.0, 0.0) if den == 0 else (H[j, j] / den, H[j + 1, j] / den)
+                    H[j, j] = den
+                    H[j + 1, j] = 0.0
+                    g[j + 1] = -sn[j] * g[j]
+                    g[j] = cs[j] * g[j]
+                    if not np.isfinite(g[j + 1]):
+                        raise LinearSolverError("GMRES broke down (non-finite residual)")
+                    if abs(g[j + 1]) <= target or H[j, j] == 0.0:
+                        k = j                    # the least-squares problem up to column j
+                        done = True
+                        break
+                if done or its >= maxiter:
                     break
             kk = k + 1
             y = np.linalg.solve(np.triu(H[:kk, :kk]), g[:kk]) if kk else np.zeros(0)
