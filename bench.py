@@ -190,8 +190,12 @@ TUNED_EPB = {("ns", 256, "df64"): 48}
 # dram__bytes_write.sum from one ncu capture of that exact kernel, scaled
 # from the captured mesh to the bench's by element count
 # (profiles/dram_traffic_element_kernels.md gives the commands).  A kernel
-# with no capture reports null.
-MEASURED_TRAFFIC = {}
+# with no capture reports null.  Value: (bytes per element, elements of the
+# captured launch).
+MEASURED_TRAFFIC = {
+    # NS Taylor-Hood 256^2, FP64: 15,403,264 read + 195,289,088 written
+    "fe_elem_p2_tri_f64_aff_0ca0c04fab": ((15403264 + 195289088) / 131072, 131072),
+}
 
 
 def measured_traffic(kernel_name: str, n_elem: int):

@@ -281,8 +281,12 @@ class SaddlePointSolver:
                            "bc": torch.zeros(na, dtype=torch.float64, device=self.dev)})
             A, comp = Ac, cc
         # the coarsest operator's inverse on the host (<= coarse_size unknowns;
-        # numpy, so no device linear-algebra library is loaded for it)
-        self.coarse_inv = torch.as_tensor(np.linalg.inv(A.toarray()), device=self.dev)
+        # numpy), applied on the device as a dense matrix in CSR form by the
+        # library's kernel: its summation order is fixed, so a solve does not
+        # depend on the stream or the library workspace it runs with
+        inv = np.linalg.inv(A.toarray())
+        self.coarse_inv = _DevCSR(torch, sps.csr_matrix(inv), self.dev)
+        self.coarse_out = torch.zeros(inv.shape[0], dtype=torch.float64, device=self.dev)
         self.levels = levels
         self._graph = None                          # recaptured for the new hierarchy
         self.Bt = _DevCSR(torch, Bt, self.dev)
@@ -297,7 +301,8 @@ class SaddlePointSolver:
         torch = self.torch
         st = torch.cuda.current_stream().cuda_stream
         if lvl == len(self.levels):
-            return self.coarse_inv @ b
+            self.coarse_inv.mv(b, self.coarse_out, st)
+            return self.coarse_out
         L = self.levels[lvl]
         A, dinv, om = L["A"], L["dinv"], L["om"]
         x, y = L["x"], L["x2"]
@@ -372,7 +377,10 @@ class SaddlePointSolver:
             self.refresh()
         st = torch.cuda.current_stream().cuda_stream
         n = self.P.n_dof
-        b = b.reshape(-1)[:n].to(torch.float64)
+        # a private copy: b may be a slice of a stacked vector at any offset,
+        # and a reduction's vector width (so its summation order) follows
+        # the alignment of the memory it reads
+        b = b.reshape(-1)[:n].to(torch.float64).clone()
         if not bool(torch.isfinite(b).all()):
             raise LinearSolverError("non-finite right-hand side")
         bnorm = float(torch.linalg.vector_norm(b))
