@@ -241,6 +241,26 @@ int fe_tc_contract(const float *dhat, float *jbuf, int64_t n_elem, int n, int nq
 int fe_sa_aggregate(int64_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
                     const int32_t *comp, double theta, int32_t *agg, int64_t *n_agg);
 
+/* How the CSR values are summed from the element matrices (the reference's
+ * scatter loop, problem.cc:5500-5560: each slot the sum of its element
+ * contributions in element order).  FE_GATHER_SLOTS (default): a thread
+ * per slot over the contribution lists, four slots per thread in flight.
+ * FE_GATHER_TILES: a warp per tile of whole rows, the residual summed in
+ * the same launch, each element-matrix row read once and coalesced; it
+ * moves a third less DRAM traffic but is bound by latency at the occupancy
+ * its registers allow, and measures faster on small meshes only.  Both give
+ * the same bits.  The pipelined host assembly (fe_assemble_pipelined)
+ * always sums per slot. */
+enum { FE_GATHER_SLOTS = 0, FE_GATHER_TILES = 1 };
+int fe_problem_set_gather(fe_problem_t *p, int mode);
+
+/* Lanes per incidence of the tile gather in use, 0 when the per-slot gather
+ * runs (FE_GATHER_SLOTS, hanging values, an element wider than 32 local
+ * values, a row wider than 255 slots or with more element incidences than
+ * a tile holds: 32, or 16 for elements wider than 16 local values); -1 for
+ * a null problem. */
+int fe_problem_gather_lanes(const fe_problem_t *p);
+
 /* Threshold of FE_ASSEMBLE_ZERO_FILTER assemblies (oomph's
  * Problem::Numerical_zero_for_sparse_assembly, problem.cc:110; default 0.0,
  * must be >= 0). */

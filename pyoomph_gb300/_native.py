@@ -15,6 +15,7 @@ from . import build as _build
  FE_ERR_SOLVER) = range(9)
 FE_ASSEMBLE_RESIDUAL, FE_ASSEMBLE_JACOBIAN, FE_ASSEMBLE_VALUES_FROM_DOFS = 1, 2, 4
 FE_ASSEMBLE_MASS, FE_ASSEMBLE_DPARAM, FE_ASSEMBLE_HVP, FE_ASSEMBLE_ZERO_FILTER = 8, 16, 32, 64
+FE_GATHER_SLOTS, FE_GATHER_TILES = 0, 1
 FE_JAC_F64, FE_JAC_F32 = 0, 1
 
 INCLUDE_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc")
@@ -34,6 +35,7 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_assemble_pipelined", "fe_csr_spmv", "fe_csr_diagonal", "fe_krylov_create", "fe_krylov_solve",
            "fe_krylov_matvec", "fe_krylov_info", "fe_krylov_destroy", "fe_problem_set_direction",
            "fe_problem_set_persistent", "fe_problem_set_zero_threshold", "fe_problem_filtered_pattern",
+           "fe_problem_set_gather", "fe_problem_gather_lanes",
            "fe_problem_set_tensor_contraction", "fe_tc_contract", "fe_sa_aggregate",
            "fe_csr_update"]
 
@@ -151,6 +153,8 @@ def load(build_if_missing: bool = True):
         L.fe_problem_set_history.argtypes = [vp, c_int, vp]
         L.fe_problem_get_history.argtypes = [vp, c_int, vp]
         L.fe_problem_set_zero_threshold.argtypes = [vp, ctypes.c_double]
+        L.fe_problem_set_gather.argtypes = [vp, c_int]
+        L.fe_problem_gather_lanes.argtypes = [vp]
         L.fe_problem_filtered_pattern.argtypes = [vp, vp, vp, vp, vp]
         L.fe_problem_set_tensor_contraction.argtypes = [vp, c_int, c_int, c_int, c_int, vp, c_int, vp, vp]
         L.fe_tc_contract.argtypes = [vp, vp, i64, c_int, c_int, c_int, vp, c_int, vp, vp, vp]

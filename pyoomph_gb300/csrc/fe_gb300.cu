@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
@@ -128,17 +129,72 @@ __global__ void k_scatter_dofs(const double *__restrict__ dofs, const int *__res
   }
 }
 
-// CSR slot s = sum of its element contributions in element order
-template <typename T>
+// CSR slot s = sum of its element contributions in element order.  With
+// U > 1 each thread takes U slots at once (a grid stride apart, so every
+// load stays coalesced across the warp) and issues their range, index and
+// value loads together -- the first two contributions of every slot in one
+// go, the rest after -- so a warp keeps U dependent chains in flight
+// instead of one; each slot still sums its contributions in order.
+template <typename T, int U>
 __global__ void k_gather_slots(const unsigned *__restrict__ cptr, const unsigned *__restrict__ cidx,
                                const T *__restrict__ jbuf, T *__restrict__ vals, long long nnz) {
-  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nnz;
-       s += (long long)gridDim.x * blockDim.x) {
-    const unsigned b = cptr[s], e = cptr[s + 1];
-    T acc = jbuf[cidx[b]];
-    for (unsigned k = b + 1; k < e; k++) acc += jbuf[cidx[k]];
-    vals[s] = acc;
+  const long long nthr = (long long)gridDim.x * blockDim.x;
+  if constexpr (U == 1) {
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nnz; s += nthr) {
+      const unsigned b = cptr[s], e = cptr[s + 1];
+      T acc = jbuf[cidx[b]];
+      for (unsigned k = b + 1; k < e; k++) acc += jbuf[cidx[k]];
+      vals[s] = acc;
+    }
+    return;
   }
+  for (long long s0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; s0 < nnz; s0 += U * nthr) {
+    unsigned b[U], e[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const long long s = s0 + u * nthr;
+      b[u] = e[u] = 0;
+      if (s < nnz) {
+        b[u] = cptr[s];
+        e[u] = cptr[s + 1];
+      }
+    }
+    unsigned i0[U], i1[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      i0[u] = b[u] < e[u] ? cidx[b[u]] : 0u;
+      i1[u] = b[u] + 1 < e[u] ? cidx[b[u] + 1] : i0[u];
+    }
+    T acc[U], v1[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      acc[u] = b[u] < e[u] ? jbuf[i0[u]] : (T)0;
+      v1[u] = b[u] + 1 < e[u] ? jbuf[i1[u]] : (T)0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const long long s = s0 + u * nthr;
+      if (s >= nnz) continue;
+      if (b[u] + 1 < e[u]) acc[u] += v1[u];
+      for (unsigned k = b[u] + 2; k < e[u]; k++) acc[u] += jbuf[cidx[k]];
+      vals[s] = acc[u];
+    }
+  }
+}
+
+// four slots per thread where it measured faster: FP32 values (the FP64
+// variant's registers cost more occupancy than the extra loads in flight
+// gain) over patterns large enough to fill the GPU at a quarter of the
+// threads
+int grid_for(long long n, int threads, int sms);
+
+template <typename T>
+void launch_gather_slots(const unsigned *cptr, const unsigned *cidx, const T *jbuf, T *vals, long long nnz, int sms,
+                         cudaStream_t st) {
+  if (sizeof(T) == 4 && nnz >= (1LL << 22))
+    k_gather_slots<T, 4><<<grid_for((nnz + 3) / 4, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz);
+  else
+    k_gather_slots<T, 1><<<grid_for(nnz, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz);
 }
 
 // residual entry r = sum of its element contributions in element order
@@ -150,6 +206,92 @@ __global__ void k_gather_rows(const unsigned *__restrict__ rptr, const unsigned 
     double acc = 0.0;
     for (unsigned k = b; k < e; k++) acc += rbuf[ridx[k]];
     R[r] = acc;
+  }
+}
+
+// Tile gather: R (when R) and the CSR values of whole rows, each entry the
+// sum of its element contributions in element order -- the order of
+// k_gather_rows / k_gather_slots, so all give the same bits.  One warp per
+// tile: consecutive rows whose incidences (element e, local row i; ranked
+// in element order within a row) fit KT records.  The records of a tile are
+// rank-major -- every row's rank-0 incidence, then every rank-1 incidence,
+// ... -- each rank padded to whole passes of PG incidences, so a pass never
+// holds two incidences of one row.  Record (16 bytes): first entry of the
+// element-matrix row e,i in jbuf; offset of its column positions in gpos;
+// its residual entry in rbuf (bits 0-25) and local values (26-31; 0 marks
+// padding); the slot base of its row within the tile (bits 0-10), its row
+// within the tile (11-15), its rank (16-20) and the first column position
+// it introduces (21-28).  A row's columns are in order of first insertion,
+// so a contribution at position p >= that first position is the first of
+// its slot: it is stored, every later one added.  Tile (16 bytes): first
+// row, first slot, slots, rows.  Two dependent loads per tile: the records,
+// then every value, position and residual entry of the tile at once (lanes
+// j of G-lane groups, PG incidences per pass).  The sums build in shared
+// memory pass after pass (positions within one incidence are distinct, the
+// incidences of a pass belong to different rows), so every slot receives
+// its contributions in element order.
+template <typename T, int G>
+__global__ void __launch_bounds__(256, 3) k_gather_tiles(const uint4 *__restrict__ tmeta,
+                                                         const uint4 *__restrict__ tinfo,
+                                                         const unsigned char *__restrict__ gpos,
+                                                         const double *__restrict__ rbuf, const T *__restrict__ jbuf,
+                                                         double *__restrict__ R, T *__restrict__ vals, long long t0,
+                                                         long long t1, int acc_stride) {
+  constexpr int KT = G == 32 ? 16 : 32; // records per tile
+  constexpr int PG = 32 / G;            // incidences per pass
+  constexpr int NP = KT / PG;           // passes
+  extern __shared__ __align__(16) unsigned char g_smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G, j = lane % G;
+  double *racc = reinterpret_cast<double *>(g_smem) + warp * 32;
+  T *acc = reinterpret_cast<T *>(g_smem + (blockDim.x >> 5) * 32 * sizeof(double)) + (size_t)warp * acc_stride;
+  const long long step = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long t = t0 + (long long)blockIdx.x * (blockDim.x >> 5) + warp; t < t1; t += step) {
+    uint4 m = make_uint4(0u, 0u, 0u, 0u);
+    if (lane < KT) m = tmeta[(size_t)t * KT + lane];
+    const uint4 ti = tinfo[t];
+    const bool live = (m.z >> 26) != 0;
+    double rv = 0.0;
+    if (R && live) rv = rbuf[m.z & 0x3FFFFFFu];
+    T v[NP];
+    unsigned sq[NP]; // accumulator slot | first << 16, or ~0u: nothing to add
+#pragma unroll
+    for (int q = 0; q < NP; q++) {
+      const int i = q * PG + sub;
+      const unsigned jr = __shfl_sync(0xffffffffu, m.x, i), go = __shfl_sync(0xffffffffu, m.y, i);
+      const unsigned nl = __shfl_sync(0xffffffffu, m.z, i) >> 26, w = __shfl_sync(0xffffffffu, m.w, i);
+      v[q] = (T)0;
+      sq[q] = ~0u;
+      if ((unsigned)j < nl) {
+        const unsigned pos = gpos[go + j];
+        v[q] = jbuf[(size_t)jr + j];
+        if (pos != 0xFFu) sq[q] = ((w & 0x7FFu) + pos) | ((pos >= ((w >> 21) & 0xFFu)) ? (1u << 16) : 0u);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NP; q++) {
+      if (sq[q] != ~0u) {
+        const unsigned s = sq[q] & 0xFFFFu;
+        acc[s] = (sq[q] >> 16) ? v[q] : acc[s] + v[q];
+      }
+      __syncwarp();
+    }
+    if (R) {
+      // each row's residual entries in rank order, from 0.0
+      racc[lane] = 0.0;
+      unsigned rk = live ? (m.w >> 16) & 31u : 0u;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) rk = max(rk, __shfl_xor_sync(0xffffffffu, rk, o));
+      __syncwarp();
+      for (unsigned r = 0; r <= rk; r++) {
+        if (live && ((m.w >> 16) & 31u) == r) racc[(m.w >> 11) & 31u] += rv;
+        __syncwarp();
+      }
+      if (lane < (int)ti.w) R[ti.x + lane] = racc[lane];
+    }
+    const int ns = (int)ti.z;
+    for (int s = lane; s < ns; s += 32) vals[ti.y + s] = acc[s];
+    __syncwarp();
   }
 }
 
@@ -564,6 +706,12 @@ struct fe_problem {
   long long n_hang = 0;
   DevBuf hang_slot, hang_ptr, hang_master, hang_weight, cw, rw; // weighted scatter when n_hang > 0
   DevBuf rowptr, colidx, cptr, cidx, rptr, ridx;
+  // tile gather (k_gather_tiles): positions, records, tiles; lanes per
+  // incidence, accumulator stride; gather_mode FE_GATHER_TILES selects it
+  DevBuf gpos, tmeta, tinfo;
+  bool g_ok = false;
+  int g_G = 0, g_acc = 0, gather_mode = 0;
+  long long g_ntiles = 0;
   DevBuf partial;
   // zero-filtered assembly (FE_ASSEMBLE_ZERO_FILTER): threshold, structural
   // values, per-slot keys and ranks, per-row counts, the filtered pattern
@@ -634,6 +782,14 @@ struct PatternOut {
   std::vector<long long> rptr; // [n_dof+1] per-row residual contributions
   std::vector<unsigned> ridx;
   std::vector<double> cw, rw;  // contribution weights (hanging nodes), empty if all 1
+  // tile gather (k_gather_tiles): column positions of every (incidence,
+  // local value) (0xFF: pinned), the tiles' records and descriptors (4 u32
+  // each), lanes per incidence, records per tile, the most slots of a tile
+  std::vector<unsigned char> gpos;
+  std::vector<uint32_t> tmeta, tinfo;
+  int gG = 0, gKT = 0;
+  long long gacc = 0;
+  bool gok = false;
 };
 
 // Hanging values (oomph's HangInfo, nodes.h; constrained values have no
@@ -668,6 +824,13 @@ struct PatternBuilder {
   const HangMap *hang = nullptr;
   std::vector<long long> inc_ptr;
   std::vector<Incident> inc;
+
+  // the element-residual entry of incidence k
+  long long ridx_of(long long k) const {
+    const Incident &I = inc[k];
+    const PatDomain &d = (*doms)[I.dom];
+    return d.rbase + I.e * d.nlocal + I.i;
+  }
 
   // the equations (and weights) a local value of an element stands for: its
   // own equation, or the equations of its masters if it hangs
@@ -782,6 +945,133 @@ struct PatternBuilder {
   }
 };
 
+// The tile gather's tables (k_gather_tiles) from the finished pattern.
+// out.gok stays false, and the per-slot gather is used, where an element
+// has more than 32 local values, a row more than 255 slots or more
+// incidences than a tile holds, the tables more than 2^32 entries, or one
+// incidence meets a column twice.
+void build_tile_gather(const PatternBuilder &B, PatternOut &out, unsigned nthreads) {
+  const long long n = B.n_dof, ninc = (long long)B.inc.size();
+  out.gok = false;
+  int maxnl = 1;
+  for (const PatDomain &d : *B.doms) maxnl = std::max(maxnl, d.nlocal);
+  long long maxrow = 0;
+  for (long long r = 0; r < n; r++) maxrow = std::max(maxrow, (long long)(out.rowptr[r + 1] - out.rowptr[r]));
+  if (maxnl > 32 || maxrow > 255) return;
+  int G = 4;
+  while (G < maxnl) G *= 2;
+  const int KT = G == 32 ? 16 : 32;
+  // accumulators of one warp: 8 warps x (32 residual + (704 | 1) FP64
+  // slots) fit the 48 KB of dynamic shared memory a launch gets without
+  // opting in
+  const long long max_slots = 704;
+  std::vector<long long> goff(ninc + 1, 0);
+  for (long long k = 0; k < ninc; k++) goff[k + 1] = goff[k] + (*B.doms)[B.inc[k].dom].nlocal;
+  if (goff[ninc] > 0xffffffffLL) return;
+  std::vector<uint32_t> jrow(ninc);
+  std::vector<unsigned char> cfirst(ninc);
+  out.gpos.assign(goff[ninc], (unsigned char)0xFF);
+  std::atomic<bool> bad{false};
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < nthreads; t++) {
+    th.emplace_back([&, t]() {
+      std::vector<int32_t> marker(n > 0 ? n : 1, -1);
+      std::vector<long long> stamp(256, -1);
+      const long long lo = n * t / nthreads, hi = n * (t + 1) / nthreads;
+      for (long long r = lo; r < hi; r++) {
+        const int32_t s0 = out.rowptr[r], len = out.rowptr[r + 1] - s0;
+        for (int32_t s = 0; s < len; s++) marker[out.colidx[s0 + s]] = s;
+        int32_t seen = 0; // columns introduced by the row's incidences so far
+        for (long long k = B.inc_ptr[r]; k < B.inc_ptr[r + 1]; k++) {
+          const Incident &I = B.inc[k];
+          const PatDomain &d = (*B.doms)[I.dom];
+          const long long jr = d.jbase + (I.e * d.nlocal + I.i) * (long long)d.nlocal;
+          if (jr + d.nlocal > 0xffffffffLL || B.ridx_of(k) >= (1LL << 26)) bad = true;
+          jrow[k] = (uint32_t)jr;
+          for (int j = 0; j < d.nlocal; j++) {
+            int cnt = 0;
+            int32_t pos = -1;
+            B.expand(d, I.e, j, [&](int32_t c, double) {
+              cnt++;
+              pos = marker[c];
+            });
+            if (cnt == 0) continue; // pinned
+            if (cnt > 1 || pos < 0 || stamp[pos] == k) {
+              bad = true;
+              continue;
+            }
+            stamp[pos] = k;
+            out.gpos[goff[k] + j] = (unsigned char)pos;
+          }
+          // the columns this incidence introduces follow those of the
+          // incidences before it (first-insertion order): cfirst, cfirst+1, ...
+          int32_t nnew = 0, top = seen;
+          for (int j = 0; j < d.nlocal; j++) {
+            const unsigned char p = out.gpos[goff[k] + j];
+            if (p == 0xFF || p < seen) continue;
+            nnew++;
+            top = std::max(top, (int32_t)p + 1);
+          }
+          if (top - seen != nnew) bad = true;
+          cfirst[k] = (unsigned char)seen;
+          seen = top;
+        }
+        for (int32_t s = 0; s < len; s++) marker[out.colidx[s0 + s]] = -1;
+      }
+    });
+  }
+  for (auto &x : th) x.join();
+  if (bad) return;
+  // tiles: consecutive rows while their records, rank-major with each rank
+  // padded to whole passes, fit KT, their slots the accumulator and their
+  // count a warp
+  const int PG = 32 / G;
+  out.tmeta.clear();
+  out.tinfo.clear();
+  long long gacc = 0;
+  std::vector<long long> cnt(KT + 1), sbase;
+  for (long long r = 0; r < n;) {
+    const long long r0 = r;
+    long long nsl = 0;
+    std::fill(cnt.begin(), cnt.end(), 0);
+    sbase.clear();
+    while (r < n && r - r0 < 32) {
+      const long long ki = B.inc_ptr[r + 1] - B.inc_ptr[r], si = out.rowptr[r + 1] - out.rowptr[r];
+      if (ki * PG > KT || si > max_slots) return;
+      long long padded = 0;
+      for (int t = 0; t < KT; t++) padded += (cnt[t] + (t < ki) + PG - 1) / PG * PG;
+      if (padded > KT || nsl + si > max_slots) break;
+      for (long long t = 0; t < ki; t++) cnt[t]++;
+      sbase.push_back(nsl);
+      nsl += si;
+      r++;
+    }
+    const size_t first = out.tmeta.size();
+    for (int t = 0; t < KT && cnt[t]; t++) {
+      long long emitted = 0;
+      for (long long q = r0; q < r; q++) {
+        if (B.inc_ptr[q + 1] - B.inc_ptr[q] <= t) continue;
+        const long long k = B.inc_ptr[q] + t;
+        const uint32_t nl = (uint32_t)(*B.doms)[B.inc[k].dom].nlocal;
+        const uint32_t w = (uint32_t)sbase[q - r0] | ((uint32_t)(q - r0) << 11) | ((uint32_t)t << 16) |
+                           ((uint32_t)cfirst[k] << 21);
+        const uint32_t one[4] = {jrow[k], (uint32_t)goff[k], (uint32_t)B.ridx_of(k) | (nl << 26), w};
+        out.tmeta.insert(out.tmeta.end(), one, one + 4);
+        emitted++;
+      }
+      out.tmeta.resize(out.tmeta.size() + 4 * ((PG - emitted % PG) % PG), 0u);
+    }
+    out.tmeta.resize(first + 4 * (size_t)KT, 0u);
+    const uint32_t info[4] = {(uint32_t)r0, (uint32_t)out.rowptr[r0], (uint32_t)nsl, (uint32_t)(r - r0)};
+    out.tinfo.insert(out.tinfo.end(), info, info + 4);
+    gacc = std::max(gacc, nsl);
+  }
+  out.gG = G;
+  out.gKT = KT;
+  out.gacc = gacc;
+  out.gok = true;
+}
+
 int build_pattern_host(long long n_dof, int nval, const int32_t *eqn, const std::vector<PatDomain> &doms,
                        bool with_contributions, PatternOut &out, const HangMap *hang = nullptr) {
   PatternBuilder B;
@@ -855,6 +1145,7 @@ int build_pattern_host(long long n_dof, int nval, const int32_t *eqn, const std:
       out.rw.resize(B.inc.size());
       for (size_t k = 0; k < B.inc.size(); k++) out.rw[k] = B.inc[k].w;
     }
+    if (!weighted) build_tile_gather(B, out, nthreads);
   }
   return FE_OK;
 }
@@ -892,6 +1183,16 @@ int build_pattern(fe_problem *P, const std::vector<const int32_t *> &conn_h, con
   }
   if ((rc = P->cidx.upload(out.cidx.data(), sizeof(unsigned) * out.cidx.size()))) return rc;
   if ((rc = P->ridx.upload(out.ridx.data(), sizeof(unsigned) * out.ridx.size()))) return rc;
+  P->g_ok = false;
+  if (out.gok && !out.tinfo.empty() && !out.gpos.empty()) {
+    P->g_G = out.gG;
+    P->g_acc = (int)(out.gacc | 1);
+    P->g_ntiles = (long long)out.tinfo.size() / 4;
+    if ((rc = P->gpos.upload(out.gpos.data(), out.gpos.size()))) return rc;
+    if ((rc = P->tmeta.upload(out.tmeta.data(), sizeof(uint32_t) * out.tmeta.size()))) return rc;
+    if ((rc = P->tinfo.upload(out.tinfo.data(), sizeof(uint32_t) * out.tinfo.size()))) return rc;
+    P->g_ok = true;
+  }
   return FE_OK;
 }
 
@@ -1073,6 +1374,33 @@ int tc_domain(fe_problem *p, Domain &d, long long e0, long long e1, cudaStream_t
   A.status = p->status.as<int>();
   A.n_elem = e1 - e0;
   return tc_launch(A, st);
+}
+
+// the tile gather is used for the Jacobian (and the residual with it) where
+// it is asked for and its tables exist
+bool tile_gather(const fe_problem *p) { return p->g_ok && p->gather_mode == FE_GATHER_TILES && !p->cw.p; }
+
+// every tile: R when given, the CSR values
+template <typename T>
+int launch_tile_gather(const fe_problem *p, double *R, T *vals, cudaStream_t st) {
+  if (p->g_ntiles <= 0) return FE_OK;
+  const int warps = 8;
+  const size_t smem = (size_t)warps * (32 * sizeof(double) + p->g_acc * sizeof(T));
+  const long long need = (p->g_ntiles + warps - 1) / warps;
+  const unsigned grid = (unsigned)std::max(1LL, std::min(need, 8LL * sm_count_cached()));
+  const uint4 *tm = p->tmeta.as<uint4>(), *ti = p->tinfo.as<uint4>();
+  const unsigned char *gp = p->gpos.as<unsigned char>();
+  const double *rb = p->rbuf_all.as<double>();
+  const T *jb = p->jbuf_all.as<T>();
+  switch (p->g_G) {
+  case 4: k_gather_tiles<T, 4><<<grid, 32 * warps, smem, st>>>(tm, ti, gp, rb, jb, R, vals, 0, p->g_ntiles, p->g_acc); break;
+  case 8: k_gather_tiles<T, 8><<<grid, 32 * warps, smem, st>>>(tm, ti, gp, rb, jb, R, vals, 0, p->g_ntiles, p->g_acc); break;
+  case 16: k_gather_tiles<T, 16><<<grid, 32 * warps, smem, st>>>(tm, ti, gp, rb, jb, R, vals, 0, p->g_ntiles, p->g_acc); break;
+  case 32: k_gather_tiles<T, 32><<<grid, 32 * warps, smem, st>>>(tm, ti, gp, rb, jb, R, vals, 0, p->g_ntiles, p->g_acc); break;
+  default: return fail(FE_ERR_STATE, "tile gather: no kernel for %d lanes", p->g_G);
+  }
+  CUDA_TRY(cudaGetLastError());
+  return FE_OK;
 }
 
 int launch_elements(fe_problem *p, int flag, cudaStream_t st) {
@@ -1607,7 +1935,10 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
     for (Domain &d : p->domains)
       if (d.tc && (rc = tc_domain(p, d, 0, d.n_elem, st))) return rc;
   if (p->timing) CUDA_TRY(cudaEventRecord(ev[2], st));
-  if (want_r && p->rw.p) {
+  // the tile gather sums the residual in the Jacobian's launch
+  const bool rowg = want_j && p->nnz > 0 && !want_zf && tile_gather(p);
+  if (rowg) {
+  } else if (want_r && p->rw.p) {
     k_gather_rows_w<<<grid_for(p->n_dof, 256, sms), 256, 0, st>>>(p->rptr.as<unsigned>(), p->ridx.as<unsigned>(),
                                                                  p->rw.as<double>(), p->rbuf_all.as<double>(), R,
                                                                  p->n_dof);
@@ -1632,13 +1963,17 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
     rc = p->jac_prec == FE_JAC_F64 ? assemble_zero_filtered<double>(p, (double *)J_vals, st)
                                    : assemble_zero_filtered<float>(p, (float *)J_vals, st);
     if (rc) return rc;
+  } else if (rowg) {
+    rc = p->jac_prec == FE_JAC_F64 ? launch_tile_gather<double>(p, want_r ? R : nullptr, (double *)J_vals, st)
+                                   : launch_tile_gather<float>(p, want_r ? R : nullptr, (float *)J_vals, st);
+    if (rc) return rc;
   } else if (want_j && p->nnz > 0) {
     if (p->jac_prec == FE_JAC_F64)
-      k_gather_slots<double><<<grid_for(p->nnz, 256, sms), 256, 0, st>>>(
-          p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->jbuf_all.as<double>(), (double *)J_vals, p->nnz);
+      launch_gather_slots<double>(p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->jbuf_all.as<double>(),
+                                  (double *)J_vals, p->nnz, sms, st);
     else
-      k_gather_slots<float><<<grid_for(p->nnz, 256, sms), 256, 0, st>>>(
-          p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->jbuf_all.as<float>(), (float *)J_vals, p->nnz);
+      launch_gather_slots<float>(p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->jbuf_all.as<float>(),
+                                 (float *)J_vals, p->nnz, sms, st);
     CUDA_TRY(cudaGetLastError());
   }
   if (p->timing) {
@@ -1816,13 +2151,11 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
       }
       if (want_j && s1 > s0) {
         if (p->jac_prec == FE_JAC_F64)
-          k_gather_slots<double><<<grid_for(s1 - s0, 256, sms), 256, 0, st>>>(
-              p->cptr.as<unsigned>() + s0, p->cidx.as<unsigned>(), p->jbuf_all.as<double>(),
-              p->pipe_J.as<double>() + s0, s1 - s0);
+          launch_gather_slots<double>(p->cptr.as<unsigned>() + s0, p->cidx.as<unsigned>(), p->jbuf_all.as<double>(),
+                                      p->pipe_J.as<double>() + s0, s1 - s0, sms, st);
         else
-          k_gather_slots<float><<<grid_for(s1 - s0, 256, sms), 256, 0, st>>>(
-              p->cptr.as<unsigned>() + s0, p->cidx.as<unsigned>(), p->jbuf_all.as<float>(),
-              p->pipe_J.as<float>() + s0, s1 - s0);
+          launch_gather_slots<float>(p->cptr.as<unsigned>() + s0, p->cidx.as<unsigned>(), p->jbuf_all.as<float>(),
+                                     p->pipe_J.as<float>() + s0, s1 - s0, sms, st);
         CUDA_TRY(cudaGetLastError());
       }
     }
@@ -1949,6 +2282,18 @@ int fe_problem_set_zero_threshold(fe_problem_t *p, double threshold) {
   if (!(threshold >= 0.0)) return fail(FE_ERR_ARG, "zero threshold must be >= 0");
   p->zf_thr = threshold;
   return FE_OK;
+}
+
+int fe_problem_set_gather(fe_problem_t *p, int mode) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  if (mode != FE_GATHER_SLOTS && mode != FE_GATHER_TILES) return fail(FE_ERR_ARG, "unknown gather mode %d", mode);
+  p->gather_mode = mode;
+  return FE_OK;
+}
+
+int fe_problem_gather_lanes(const fe_problem_t *p) {
+  if (!p) return -1;
+  return tile_gather(p) ? p->g_G : 0;
 }
 
 int fe_problem_filtered_pattern(fe_problem_t *p, int64_t *nnz, int32_t *rowptr, int32_t *colidx, void *stream) {
@@ -2146,12 +2491,14 @@ int fe_problem_launch_count(const fe_problem_t *p, int flags) {
     for (const Domain &d : p->domains)
       if (d.n_elem) n++;
   }
-  if (flags & (FE_ASSEMBLE_RESIDUAL | FE_ASSEMBLE_DPARAM)) n++;
+  const bool want_j = (flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS | FE_ASSEMBLE_HVP)) && p->nnz > 0;
+  const bool zf = flags & FE_ASSEMBLE_ZERO_FILTER;
+  // the tile gather sums the residual in the Jacobian's launch
+  if ((flags & (FE_ASSEMBLE_RESIDUAL | FE_ASSEMBLE_DPARAM)) && !(want_j && !zf && tile_gather(p))) n++;
   if (flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_HVP))
     for (const Domain &d : p->domains)
       if (d.tc && d.n_elem) n++;
-  if ((flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS | FE_ASSEMBLE_HVP)) && p->nnz > 0)
-    n += (flags & FE_ASSEMBLE_ZERO_FILTER) ? 6 : 1;   // filtered gather, ranks, three scan launches, scatter
+  if (want_j) n += zf ? 6 : 1;   // filtered gather, ranks, three scan launches, scatter
   if (p->n_hang > 0) n++;
   return n;
 }

@@ -12,8 +12,10 @@ with the mesh.  This solver keeps everything on the device and converges in
 a mesh-independent number of iterations:
 
 * right-preconditioned GMRES (restarted, classical Gram-Schmidt applied
-  twice, so one host synchronisation per iteration) on the resident CSR
-  Jacobian (``fe_csr_spmv``);
+  twice; the Hessenberg matrix stays on the device and the host reads it
+  every few iterations for the Givens rotations) on the resident CSR
+  Jacobian (``fe_csr_spmv``), to the relative tolerance of an inexact
+  Newton step (``newton_forcing``);
 * the block upper-triangular preconditioner P = [[A, Bt], [0, S_hat]]:
   p = S_hat^-1 r_p, u = A_hat^-1 (r_u - Bt p), which would need two GMRES
   iterations with exact blocks;
@@ -155,6 +157,20 @@ class BlockView:
 
     def device_csr(self) -> DeviceCSR:
         return DeviceCSR(self._rpd.data_ptr(), self._cid.data_ptr(), self.J_dev, self.n_dof, self.nnz)
+
+
+def newton_forcing(eta: float = 1e-5, eta_min: float = 1e-11) -> float:
+    """Relative tolerance of the linear solve of a Newton step: the forcing
+    term eta, not below eta_min (the 2-norm residual of a Krylov solve of
+    these systems stalls near cond x eps).  The step's linear error enters
+    the next residual as about eta |R| (inexact Newton: Dembo, Eisenstat and
+    Steihaug, SIAM J. Numer. Anal. 19, 1982), far below the quadratic term of
+    the steps a Newton solve takes from a perturbed state, so the residual
+    history is that of exact steps.  Restarted GMRES with the block
+    preconditioner reaches 1e-5 within its first restart cycle on these
+    systems and then gains about 1.5x per cycle, so a tighter target would
+    spend most iterations on accuracy the next residual cannot show."""
+    return max(float(eta_min), float(eta))
 
 
 class SaddlePointSolver:
@@ -395,6 +411,8 @@ class SaddlePointSolver:
         r = b.clone()
         beta = bnorm
         stalled = 0
+        self.stagnated = False
+        self.restart_residuals = [bnorm]     # ||b - J x||_2 at every restart
         while its < maxiter:
             beta_start = beta
             V[0] = r / beta
@@ -449,6 +467,7 @@ class SaddlePointSolver:
             self.J.matvec(x, Az, st)
             r = b - Az
             beta = float(torch.linalg.vector_norm(r))
+            self.restart_residuals.append(beta)
             if beta <= target:
                 self.iterations = its
                 return x, its

@@ -266,10 +266,11 @@ class Problem:
         # contract FP32 element Jacobians on the tensor cores (None: where the
         # generator supports it and it pays, the Q2 hex's 27 x 27 matrices)
         self.tensor_cores: Optional[bool] = None
-        # linear_solver = "bicgstab": J dx = R solved on the device (linsolve.py);
-        # "fieldsplit": saddle-point systems (Taylor-Hood) on the device
-        # (fieldsplit.py: GMRES, block-triangular multigrid preconditioner)
-        # to this relative tolerance; None: SuperLU on the host (the reference's default)
+        # linear_solver = "bicgstab": J dx = R solved on the device (linsolve.py)
+        # to this relative tolerance; "fieldsplit": saddle-point systems
+        # (Taylor-Hood) on the device (fieldsplit.py: GMRES, block-triangular
+        # multigrid preconditioner) to fieldsplit_forcing; None: SuperLU on the
+        # host (the reference's default)
         self.linear_solver_tolerance = 1e-13
         # Gaussian source terms on axis-aligned affine Q2 meshes: evaluate the
         # per-axis factors once per element (3 dim exponentials per Gaussian
@@ -279,9 +280,13 @@ class Problem:
         # absolute floor of the device solve's residual (0: relative only);
         # e.g. 0.1 x newton_solver_tolerance for an inexact Newton step
         self.linear_solver_atol = 0.0
-        # "fieldsplit" (saddle-point GMRES, fieldsplit.py): relative
-        # tolerances below this are raised to it (the 2-norm residual of a
-        # Krylov solve of these systems stalls near cond x eps)
+        # "fieldsplit" (saddle-point GMRES, fieldsplit.py): each Newton step
+        # solves to the relative tolerance fieldsplit_forcing, an inexact
+        # Newton step whose linear error stays below the quadratic term
+        # (fieldsplit.newton_forcing), never below fieldsplit_min_tolerance
+        # (the 2-norm residual of a Krylov solve of these systems stalls near
+        # cond x eps)
+        self.fieldsplit_forcing = 1e-5
         self.fieldsplit_min_tolerance = 1e-11
         self.saddle_point = None
         # time-dependent solve: the weak form's partial_t terms are kept (BDF
@@ -1303,11 +1308,14 @@ class Problem:
             tb = time.perf_counter()
             with nvtx_range("linear solve"):
                 if self.linear_solver == "fieldsplit":
-                    # an inexact Newton step: no more accuracy than the Newton
-                    # criterion can see (a relative target below the attainable
-                    # accuracy of a small late-step residual would stall)
+                    # an inexact Newton step (the forcing term), and no more
+                    # accuracy than the Newton criterion can see (a target
+                    # below the attainable accuracy of a small late-step
+                    # residual would stall)
+                    from .fieldsplit import newton_forcing
                     dxd, its = self._fieldsplit_solver().solve(
-                        self.R_dev[:self.n_dof], tol=max(self.linear_solver_tolerance, self.fieldsplit_min_tolerance),
+                        self.R_dev[:self.n_dof],
+                        tol=newton_forcing(self.fieldsplit_forcing, self.fieldsplit_min_tolerance),
                         atol=max(self.linear_solver_atol, 1e-3 * self.newton_solver_tolerance))
                     self.timings["krylov_iterations"] = self.timings.get("krylov_iterations", 0) + int(its)
                 elif device_solve:

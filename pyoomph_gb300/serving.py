@@ -356,7 +356,7 @@ class Server:
         snapshot.  A request's solver is built from its own first Jacobian
         and kept for its later steps, so nothing it computes depends on the
         other requests of the class."""
-        from .fieldsplit import BlockView, SaddlePointSolver
+        from .fieldsplit import BlockView, SaddlePointSolver, newton_forcing
         torch = self.torch
         P = b.P
         with torch.cuda.stream(b.stream):
@@ -372,7 +372,7 @@ class Server:
                 if sol is None:
                     view = BlockView(P, int(s), b.jsnap, rp0, ci0, rpd, cid)
                     sol = b.fs[int(s)] = SaddlePointSolver(view, "pressure", 1.0 / b.req[s].Re)
-                x, _ = sol.solve(rv[s], tol=1e-11, atol=atol)
+                x, _ = sol.solve(rv[s], tol=newton_forcing(), atol=atol)
                 dx[s] = x
         return dx, 0
 

@@ -120,6 +120,8 @@ def _main(argv=None) -> None:
                     help="assemble J in the reference's zero-filtered pattern (threshold 0.0)")
     ap.add_argument("--transient", action="store_true",
                     help="the transient form (BDF2 weights of dt = 1e-3, both previous levels = the current values)")
+    ap.add_argument("--tile-gather", action="store_true",
+                    help="sum the CSR values with a warp per tile of rows instead of a thread per slot")
     a = ap.parse_args(argv)
     if a.workload == "ns":
         P = navier_stokes_problem(N=a.side, jacobian_precision=a.precision, transient=a.transient)
@@ -133,6 +135,9 @@ def _main(argv=None) -> None:
     if a.tc is not None:
         P.tensor_cores = bool(a.tc)
     P.initialise()
+    if a.tile_gather:
+        from . import _native as N
+        N.check(N.load().fe_problem_set_gather(P._h, N.FE_GATHER_TILES))
     perturb_dofs(P, seed=0, sigma=1e-3)
     if a.transient:
         from .ale import bdf_weights
@@ -150,8 +155,18 @@ def _main(argv=None) -> None:
     e1.record()
     torch.cuda.synchronize()
     P.check()
+    # the same assemblies once more with events around the stages
+    P.set_stage_timing(True)
+    P.stage_times()
+    for _ in range(a.repeat):
+        P.assemble_device(with_jacobian=True, zero_threshold=zt)
+    torch.cuda.synchronize()
+    ms, calls = P.stage_times()
+    P.set_stage_timing(False)
+    stages = ", ".join(f"{k} {v / max(calls, 1):.4f}" for k, v in
+                       zip(("dof scatter", "element kernels", "residual gather", "jacobian gather", "tensor cores"), ms))
     print(f"{a.workload} side {a.side} {a.precision}: {P.mesh.n_elem} elements, kernel {P.kernel.name}, "
-          f"{e0.elapsed_time(e1) / a.repeat:.4f} ms per assembly")
+          f"{e0.elapsed_time(e1) / a.repeat:.4f} ms per assembly ({stages} ms)")
 
 
 if __name__ == "__main__":
