@@ -261,6 +261,38 @@ int fe_problem_set_gather(fe_problem_t *p, int mode);
  * a null problem. */
 int fe_problem_gather_lanes(const fe_problem_t *p);
 
+/* One level of the smoothed-aggregation hierarchy (host, threads), from the
+ * n x n CSR matrix A (int32 indices) and its aggregates agg[n] in [0, n_agg)
+ * (fe_sa_aggregate):
+ *   lam = 1.1 x the largest eigenvalue of D^-1 A (12 power iterations from
+ *         a fixed start; D = diag(A), nonzero),
+ *   P   = P0 - (4/3)/lam D^-1 A P0   (n x n_agg; P0 the aggregation),
+ *   Ac  = P^T A P                    (n_agg x n_agg).
+ * Rows are computed independently and sum in a fixed order, columns
+ * ascending: the level does not depend on the number of threads.  The
+ * handle holds P and Ac until fe_sa_level_copy (rowptr n + 1 / n_agg + 1,
+ * colidx and values of the sizes fe_sa_level_info reports); free it with
+ * fe_sa_level_destroy.  Replaces the setup of the Newton systems' direct
+ * solve (SuperLU, pyoomph/solvers/scipy.py) for Taylor-Hood Jacobians. */
+typedef struct fe_sa_level fe_sa_level_t;
+int fe_sa_level_build(int64_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
+                      const int32_t *agg, int64_t n_agg, fe_sa_level_t **out);
+int fe_sa_level_info(const fe_sa_level_t *level, int64_t *nnz_p, int64_t *nnz_ac, double *lam);
+int fe_sa_level_copy(const fe_sa_level_t *level, int32_t *p_rowptr, int32_t *p_colidx, double *p_vals,
+                     int32_t *ac_rowptr, int32_t *ac_colidx, double *ac_vals);
+void fe_sa_level_destroy(fe_sa_level_t *level);
+
+/* One block of an n x n CSR matrix split by a label (0 or 1) per row and
+ * column index: the rows labelled rl, in order, with their entries in
+ * columns labelled cl; rows and columns renumbered within their label,
+ * columns ascending within a row, b_slot[k] the entry's position in the
+ * input (the saddle-point solver's A, Bt and B blocks of a Taylor-Hood
+ * Jacobian).  *nnz is set first; with the three outputs NULL nothing else
+ * is written, otherwise b_rowptr (rows labelled rl + 1), b_colidx and
+ * b_slot (*nnz) are filled. */
+int fe_csr_block(int64_t n, const int32_t *rowptr, const int32_t *colidx, const int8_t *label, int rl, int cl,
+                 int64_t *nnz, int32_t *b_rowptr, int32_t *b_colidx, int64_t *b_slot);
+
 /* Threshold of FE_ASSEMBLE_ZERO_FILTER assemblies (oomph's
  * Problem::Numerical_zero_for_sparse_assembly, problem.cc:110; default 0.0,
  * must be >= 0). */

@@ -37,7 +37,8 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_problem_set_persistent", "fe_problem_set_zero_threshold", "fe_problem_filtered_pattern",
            "fe_problem_set_gather", "fe_problem_gather_lanes",
            "fe_problem_set_tensor_contraction", "fe_tc_contract", "fe_sa_aggregate",
-           "fe_csr_update"]
+           "fe_csr_update", "fe_sa_level_build", "fe_sa_level_info", "fe_sa_level_copy", "fe_sa_level_destroy",
+           "fe_csr_block"]
 
 
 def _header_stamp() -> str:
@@ -154,6 +155,12 @@ def load(build_if_missing: bool = True):
         L.fe_problem_get_history.argtypes = [vp, c_int, vp]
         L.fe_problem_set_zero_threshold.argtypes = [vp, ctypes.c_double]
         L.fe_problem_set_gather.argtypes = [vp, c_int]
+        L.fe_sa_level_build.argtypes = [ctypes.c_int64, vp, vp, vp, vp, ctypes.c_int64, ctypes.POINTER(vp)]
+        L.fe_sa_level_info.argtypes = [vp, vp, vp, vp]
+        L.fe_sa_level_copy.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        L.fe_sa_level_destroy.argtypes = [vp]
+        L.fe_sa_level_destroy.restype = None
+        L.fe_csr_block.argtypes = [ctypes.c_int64, vp, vp, vp, c_int, c_int, vp, vp, vp, vp]
         L.fe_problem_gather_lanes.argtypes = [vp]
         L.fe_problem_filtered_pattern.argtypes = [vp, vp, vp, vp, vp]
         L.fe_problem_set_tensor_contraction.argtypes = [vp, c_int, c_int, c_int, c_int, vp, c_int, vp, vp]

@@ -2506,3 +2506,4 @@ int fe_problem_launch_count(const fe_problem_t *p, int flags) {
 } // extern "C"
 
 #include "fe_krylov.cuh"
+#include "fe_sa_level.cuh"

@@ -92,16 +92,63 @@ def aggregate(A, comp: np.ndarray, theta: float):
     return agg[:n], int(na.value)
 
 
-def spectral_radius_dinv_a(A, iters: int = 12, seed: int = 0) -> float:
-    """Estimate of rho(D^-1 A) by power iteration (host), with a margin."""
-    D = A.diagonal()
-    x = np.random.default_rng(seed).uniform(0.5, 1.5, A.shape[0])
-    lam = 1.0
-    for _ in range(iters):
-        y = (A @ x) / D
-        lam = float(np.linalg.norm(y) / max(np.linalg.norm(x), 1e-300))
-        x = y / max(np.linalg.norm(y), 1e-300)
-    return 1.1 * lam
+class _Block:
+    """The pattern of one block of a CSR matrix (fe_csr_block): indptr,
+    indices (columns ascending), shape, and each entry's slot in the
+    matrix."""
+
+    def __init__(self, indptr, indices, slots, shape):
+        self.indptr, self.indices, self.slots, self.shape = indptr, indices, slots, shape
+
+
+def csr_block(rp, ci, label: np.ndarray, rl: int, cl: int) -> _Block:
+    """Rows labelled rl and columns labelled cl of the CSR pattern (rp, ci),
+    renumbered within their label."""
+    rp = np.ascontiguousarray(rp, dtype=np.int32)
+    ci = np.ascontiguousarray(ci, dtype=np.int32)
+    n = rp.size - 1
+    L = N.load()
+    nnz = ctypes.c_int64()
+    N.check(L.fe_csr_block(n, rp.ctypes.data, ci.ctypes.data, label.ctypes.data, rl, cl, ctypes.byref(nnz),
+                           None, None, None))
+    nr, nc = int(np.count_nonzero(label == rl)), int(np.count_nonzero(label == cl))
+    indptr = np.zeros(nr + 1, np.int32)
+    indices = np.zeros(max(nnz.value, 1), np.int32)
+    slots = np.zeros(max(nnz.value, 1), np.int64)
+    N.check(L.fe_csr_block(n, rp.ctypes.data, ci.ctypes.data, label.ctypes.data, rl, cl, ctypes.byref(nnz),
+                           indptr.ctypes.data, indices.ctypes.data, slots.ctypes.data))
+    return _Block(indptr, indices[:nnz.value], slots[:nnz.value], (nr, nc))
+
+
+def sa_level(A, agg: np.ndarray, n_agg: int):
+    """One smoothed-aggregation level of A from its aggregates
+    (fe_sa_level_build, host threads): (P, Ac, lam) with lam = 1.1 x the
+    largest eigenvalue of D^-1 A, P = P0 - (4/3)/lam D^-1 A P0 (P0 the
+    aggregation) and Ac = P^T A P, as scipy CSR matrices."""
+    import scipy.sparse as sps
+    A = A.tocsr()
+    n = A.shape[0]
+    rp = np.ascontiguousarray(A.indptr, dtype=np.int32)
+    ci = np.ascontiguousarray(A.indices, dtype=np.int32)
+    v = np.ascontiguousarray(A.data, dtype=np.float64)
+    a = np.ascontiguousarray(agg, dtype=np.int32)
+    L = N.load()
+    h = ctypes.c_void_p()
+    N.check(L.fe_sa_level_build(n, rp.ctypes.data, ci.ctypes.data, v.ctypes.data, a.ctypes.data, int(n_agg),
+                                ctypes.byref(h)))
+    try:
+        nnz_p, nnz_a, lam = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
+        N.check(L.fe_sa_level_info(h, ctypes.byref(nnz_p), ctypes.byref(nnz_a), ctypes.byref(lam)))
+        prp, arp = np.empty(n + 1, np.int32), np.empty(n_agg + 1, np.int32)
+        pci, pv = np.empty(max(nnz_p.value, 1), np.int32), np.empty(max(nnz_p.value, 1))
+        aci, av = np.empty(max(nnz_a.value, 1), np.int32), np.empty(max(nnz_a.value, 1))
+        N.check(L.fe_sa_level_copy(h, prp.ctypes.data, pci.ctypes.data, pv.ctypes.data, arp.ctypes.data,
+                                   aci.ctypes.data, av.ctypes.data))
+    finally:
+        L.fe_sa_level_destroy(h)
+    P = sps.csr_matrix((pv[:nnz_p.value], pci[:nnz_p.value], prp), shape=(n, n_agg))
+    Ac = sps.csr_matrix((av[:nnz_a.value], aci[:nnz_a.value], arp), shape=(n_agg, n_agg))
+    return P, Ac, float(lam.value)
 
 
 def lumped_field_mass(P, field: str) -> np.ndarray:
@@ -121,9 +168,16 @@ def lumped_field_mass(P, field: str) -> np.ndarray:
         psi = np.asarray(t["PSI2"]).reshape(et.nq, et.nnode)
         slots = np.arange(et.nnode)
     X = mesh.x[mesh.conn]                              # [E, nnode, dim]
-    G = np.einsum("eld,qlb->eqdb", X, dps2)            # dx_d/ds_b per element and knot
-    det = np.abs(np.linalg.det(G))                     # [E, nq]
-    contrib = np.einsum("q,eq,qk->ek", W, det, psi)    # [E, nslots]
+    G = np.tensordot(X, dps2, axes=([1], [1]))         # dx_d/ds_b: [E, dim, nq, dim]
+    if et.dim == 2:
+        det = G[:, 0, :, 0] * G[:, 1, :, 1] - G[:, 0, :, 1] * G[:, 1, :, 0]
+    elif et.dim == 3:
+        det = (G[:, 0, :, 0] * (G[:, 1, :, 1] * G[:, 2, :, 2] - G[:, 1, :, 2] * G[:, 2, :, 1])
+               - G[:, 0, :, 1] * (G[:, 1, :, 0] * G[:, 2, :, 2] - G[:, 1, :, 2] * G[:, 2, :, 0])
+               + G[:, 0, :, 2] * (G[:, 1, :, 0] * G[:, 2, :, 1] - G[:, 1, :, 1] * G[:, 2, :, 0]))
+    else:
+        det = G[:, 0, :, 0]
+    contrib = (np.abs(det) * W) @ psi                  # [E, nslots]
     eqn = np.asarray(P.eqn).reshape(mesh.n_nodes, len(P.fields))[:, f]
     rows = eqn[mesh.conn[:, slots]]
     ok = rows >= 0
@@ -204,27 +258,16 @@ class SaddlePointSolver:
         self.pre = np.nonzero(is_p)[0]
         self.comp_v = comp[self.vel]
         rp, ci = P.pattern()
-        # slot maps of the velocity block A and the coupling Bt inside the CSR
-        rows = np.repeat(np.arange(n), np.diff(rp))
-        where_v = np.full(n, -1, dtype=np.int64)
-        where_v[self.vel] = np.arange(self.vel.size)
-        where_p = np.full(n, -1, dtype=np.int64)
-        where_p[self.pre] = np.arange(self.pre.size)
-        rv, cv, cp = where_v[rows], where_v[ci], where_p[ci]
-        rpre = where_p[rows]
-        sel_a = (rv >= 0) & (cv >= 0)
-        sel_b = (rv >= 0) & (cp >= 0)
-        sel_c = (rpre >= 0) & (cv >= 0)
-        slots = np.arange(rp[-1])
-        A_pat = sps.csr_matrix((slots[sel_a] + 1.0, (rv[sel_a], cv[sel_a])), shape=(self.vel.size,) * 2)
-        A_pat.sort_indices()
-        B_pat = sps.csr_matrix((slots[sel_b] + 1.0, (rv[sel_b], cp[sel_b])), shape=(self.vel.size, self.pre.size))
-        B_pat.sort_indices()
-        C_pat = sps.csr_matrix((slots[sel_c] + 1.0, (rpre[sel_c], cv[sel_c])), shape=(self.pre.size, self.vel.size))
-        C_pat.sort_indices()
+        # patterns and slot maps of the velocity block A, the coupling Bt and
+        # the constraint block B inside the CSR (native split)
+        label = np.ascontiguousarray(is_p, dtype=np.int8)
+        A_pat = csr_block(rp, ci, label, 0, 0)
+        B_pat = csr_block(rp, ci, label, 0, 1)
+        C_pat = csr_block(rp, ci, label, 1, 0)
         self.A_shape, self.B_shape, self.C_shape = A_pat, B_pat, C_pat
-        self.map_a = torch.as_tensor((A_pat.data - 1.0).astype(np.int64), device=self.dev)
-        self.map_b = torch.as_tensor((B_pat.data - 1.0).astype(np.int64), device=self.dev)
+        self.map_a = torch.as_tensor(A_pat.slots, device=self.dev)
+        self.map_b = torch.as_tensor(B_pat.slots, device=self.dev)
+        self.map_c = torch.as_tensor(C_pat.slots, device=self.dev)
         self.vel_t = torch.as_tensor(self.vel, device=self.dev)
         self.pre_t = torch.as_tensor(self.pre, device=self.dev)
         mass = lumped_field_mass(P, schur_field)[self.pre]
@@ -250,13 +293,15 @@ class SaddlePointSolver:
 
     # -- set-up ------------------------------------------------------------
     def _host_blocks(self):
-        """(A, Bt, B) of the current Jacobian on the host."""
+        """(A, Bt, B) of the current Jacobian on the host (gathered on the
+        device)."""
         import scipy.sparse as sps
-        vals = self.P.J_dev[:self.P.nnz].to(self.torch.float64).cpu().numpy()
+        vals = self.P.J_dev[:self.P.nnz].to(self.torch.float64)
 
-        def take(pat):
-            return sps.csr_matrix((vals[(pat.data - 1).astype(np.int64)], pat.indices, pat.indptr), shape=pat.shape)
-        return take(self.A_shape), take(self.B_shape), take(self.C_shape)
+        def take(pat, m):
+            return sps.csr_matrix((vals.index_select(0, m).cpu().numpy(), pat.indices, pat.indptr), shape=pat.shape)
+        return (take(self.A_shape, self.map_a), take(self.B_shape, self.map_b),
+                take(self.C_shape, self.map_c))
 
     def setup(self) -> None:
         """The multigrid hierarchy of the current velocity block and the
@@ -280,11 +325,8 @@ class SaddlePointSolver:
             if na >= 0.9 * A.shape[0]:
                 break
             n = A.shape[0]
-            P0 = sps.csr_matrix((np.ones(n), (np.arange(n), agg)), shape=(n, na))
             Dl = A.diagonal()
-            lam = spectral_radius_dinv_a(A)
-            Pm = (P0 - (4.0 / 3.0 / lam) * (sps.diags(1.0 / Dl) @ A @ P0)).tocsr()
-            Ac = (Pm.T @ A @ Pm).tocsr()
+            Pm, Ac, lam = sa_level(A, agg, na)
             cc = np.zeros(na, dtype=np.int32)
             cc[agg] = comp
             levels.append({"A": _DevCSR(torch, A, self.dev), "P": _DevCSR(torch, Pm, self.dev),

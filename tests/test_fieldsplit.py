@@ -43,6 +43,46 @@ def test_pressure_lumped_mass_and_aggregates():
         assert np.unique(comp[agg == a]).size == 1
 
 
+def test_native_block_split_and_multigrid_level_match_scipy():
+    """Host parts of the set-up: fe_csr_block cuts the same blocks as scipy
+    slicing, its slot map points at the right entries; fe_sa_level_build's
+    prolongator and Galerkin operator equal the scipy products with the
+    same spectral radius estimate (to rounding); a second build gives the
+    same bits."""
+    import scipy.sparse as sps
+    from pyoomph_gb300 import fieldsplit as F
+    rng = np.random.default_rng(3)
+    n = 3000
+    A = sps.random(n, n, density=0.004, random_state=2, format="csr")
+    A = (A + A.T + sps.eye(n) * 6.0).tocsr()
+    A.data += rng.normal(0.0, 1e-3, A.data.size)
+    label = (rng.random(n) < 0.25).astype(np.int8)
+    for rl in (0, 1):
+        for cl in (0, 1):
+            blk = F.csr_block(A.indptr, A.indices, label, rl, cl)
+            rows, cols = np.flatnonzero(label == rl), np.flatnonzero(label == cl)
+            ref = A[rows][:, cols].tocsr()
+            ref.sort_indices()
+            got = sps.csr_matrix((A.data[blk.slots], blk.indices, blk.indptr), shape=blk.shape)
+            assert got.shape == ref.shape
+            assert np.array_equal(got.indptr, ref.indptr) and np.array_equal(got.indices, ref.indices)
+            assert np.array_equal(got.data, ref.data)
+    comp = np.zeros(n, np.int32)
+    agg, na = F.aggregate(A, comp, 0.05)
+    Pn, Acn, lam = F.sa_level(A, agg, na)
+    D = A.diagonal()
+    ev = abs(sps.linalg.eigs(sps.diags(1.0 / D) @ A, k=1, which="LM", return_eigenvectors=False)[0])
+    assert 1.0 * ev <= lam <= 1.15 * ev
+    P0 = sps.csr_matrix((np.ones(n), (np.arange(n), agg)), shape=(n, na))
+    Pr = (P0 - (4.0 / 3.0 / lam) * (sps.diags(1.0 / D) @ A @ P0)).tocsr()
+    Acr = (Pr.T @ A @ Pr).tocsr()
+    for got, ref in ((Pn, Pr), (Acn, Acr)):
+        d = (got - ref).tocsr()
+        assert abs(d).max() <= 1e-13 * abs(ref).max()
+    P2, Ac2, lam2 = F.sa_level(A, agg, na)
+    assert lam2 == lam and np.array_equal(P2.data, Pn.data) and np.array_equal(Ac2.data, Acn.data)
+
+
 @pytest.mark.gpu
 def test_linear_solve_matches_superlu():
     import scipy.sparse.linalg as spla
