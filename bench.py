@@ -61,6 +61,8 @@ def run_serving(args):
         reqs = S.make_stream(args.requests, rate=rate, seed=0, side_range=(16, args.size),
                              ns_side_max=args.ns_side_max)
         srv = S.Server(slots=4, jacobian_precision="fp32", workers=workers, device_solver=args.device_solver)
+        if args.ns_device_min_side is not None:
+            srv.device_saddle_min_side = args.ns_device_min_side
         t0 = time.perf_counter()
         done = srv.run(copy.deepcopy(reqs))
         wall = time.perf_counter() - t0
@@ -75,7 +77,9 @@ def run_serving(args):
     reqs = S.make_stream(args.requests, rate=rates[0], seed=0, side_range=(16, args.size),
                          ns_side_max=args.ns_side_max)
     t0 = time.perf_counter()
-    seq = S.serve_sequential(copy.deepcopy(reqs), precision="fp64", device_solver=args.device_solver)
+    seq = S.serve_sequential(copy.deepcopy(reqs), precision="fp64", device_solver=args.device_solver,
+                             **({} if args.ns_device_min_side is None else
+                                {"device_saddle_min_side": args.ns_device_min_side}))
     wall = time.perf_counter() - t0
     s_ = S.summary(seq, wall)
     s_["wall_s"] = wall
@@ -90,7 +94,10 @@ def run_serving(args):
                        "ns_side_max": args.ns_side_max,
                        "slots_per_class": 4,
                        "linear_solver": (f"Poisson: native batched BiCGStab on the device; Navier-Stokes: SuperLU "
-                                         f"(scipy), {workers} worker processes") if args.device_solver else
+                                         f"(scipy) in {workers} worker processes below side "
+                                         f"{args.ns_device_min_side or S.Server.default_saddle_min_side()}, "
+                                         f"the device saddle-point GMRES (fieldsplit.py) from it")
+                                        if args.device_solver else
                                         f"SuperLU (scipy), {workers} worker processes"},
             "batched_fp32_by_rate": per_rate, "sequential_fp64_at_first_rate": s_,
             "max_rel_solution_difference_batched_vs_sequential": err,
@@ -1088,7 +1095,10 @@ def main():
     ap.add_argument("--ns-side-max", type=int, default=None,
                     help="serving: cap the Navier-Stokes requests' sides (their solves stay on the host)")
     ap.add_argument("--device-solver", action="store_true",
-                    help="serving: solve the Poisson requests' Newton systems on the device")
+                    help="serving: solve the Newton systems on the device (Poisson: batched BiCGStab; "
+                         "Navier-Stokes from --ns-device-min-side: the saddle-point GMRES)")
+    ap.add_argument("--ns-device-min-side", type=int, default=None,
+                    help="serving: smallest Navier-Stokes side solved on the device (default: the server's)")
     args = ap.parse_args()
     if args.size is None:
         args.size = WORKLOADS[args.workload][1]

@@ -76,7 +76,7 @@ def _complete(hang: Dict[int, List[Tuple[int, float]]], min_weight: float = 1e-8
     return hang
 
 
-def refine_levels(m: O.Mesh, chosen, max_level: int):
+def refine_levels(m: O.Mesh, chosen, max_level: int, with_c1: bool = False):
     """(x, conn, hang, on_boundary) of a quadtree refinement to several
     levels: an element (a map X(s) of the reference square) is split into
     its sons SW, SE, NW, NE -- son maps composed with the parent's -- while
@@ -145,7 +145,29 @@ def refine_levels(m: O.Mesh, chosen, max_level: int):
     lo, hi = x.min(axis=0), x.max(axis=0)
     on_b = (np.abs(x[:, 0] - lo[0]) < 1e-12) | (np.abs(x[:, 0] - hi[0]) < 1e-12) | \
            (np.abs(x[:, 1] - lo[1]) < 1e-12) | (np.abs(x[:, 1] - hi[1]) < 1e-12)
-    return x, conn, hang, on_b
+    if not with_c1:
+        return x, conn, hang, on_b
+    # C1 values live on the leaves' vertices and interpolate bilinearly: a
+    # vertex strictly inside a leaf edge -- its middle node included --
+    # takes the value interpolated linearly between the edge's two end
+    # vertices (setup_hang_for_value with the vertices as the interpolating
+    # nodes, pyoomph's BulkElementQuad2dC2::interpolating_node_pt,
+    # elements.cpp:9162-9250), completed through hanging masters
+    vertices = sorted(set(int(c[s_]) for c in conn for s_ in (0, 2, 6, 8)))
+    hang_c1: Dict[int, List[Tuple[int, float]]] = {}
+    for k in vertices:
+        for a, mid, b in edges:
+            if k in (a, b):
+                continue
+            pa, pb = x[a], x[b]
+            t = pb - pa
+            u = np.dot(x[k] - pa, t) / np.dot(t, t)
+            if 0.0 < u < 1.0 and np.linalg.norm(pa + u * t - x[k]) < 1e-12:
+                u = np.round(u * 2.0 ** 20) / 2.0 ** 20              # dyadic, as the tree's coordinates
+                hang_c1[k] = [(a, 1.0 - u), (b, u)]
+                break
+    hang_c1 = _complete(hang_c1, rank=rank)
+    return x, conn, hang, hang_c1, on_b
 
 
 def refinement_plan(m: O.Mesh, chosen, max_level: int):
@@ -301,6 +323,134 @@ class HangProblem:
                         for (cc, wc) in exp[j]:
                             Jl[pos[r], pos[cc]] += wr * wc * J[i, j]
             # the vectors-of-pairs insertion: (local equation i, local equation j)
+            for a, r in enumerate(dofs):
+                R[r] += Rl[a]
+                row = rows[r]
+                for b, cc in enumerate(dofs):
+                    row[cc] = row.get(cc, 0.0) + Jl[a, b]
+        rp = np.zeros(self.n_dof + 1, dtype=np.int64)
+        for i, row in enumerate(rows):
+            rp[i + 1] = rp[i] + len(row)
+        ci = np.fromiter((k for row in rows for k in row), dtype=np.int64, count=int(rp[-1]))
+        v = np.fromiter((val for row in rows for val in row.values()), dtype=np.float64, count=int(rp[-1]))
+        return R, rp, ci, v
+
+    def newton(self, tol: float = 1e-11, max_iter: int = 20) -> np.ndarray:
+        import scipy.sparse as sps
+        import scipy.sparse.linalg as spla
+        for _ in range(max_iter):
+            R, rp, ci, v = self.assemble()
+            if np.max(np.abs(R)) < tol:
+                return self.dofs()
+            A = sps.csr_matrix((v, ci, rp), shape=(self.n_dof, self.n_dof))
+            self.set_dofs(self.dofs() - spla.splu(A.tocsc()).solve(R))
+        raise RuntimeError("oracle Newton did not converge")
+
+
+class HangNSProblem:
+    """Taylor-Hood Navier-Stokes (Q2 velocity, Q1 pressure) on a refined
+    mesh: the lid-driven cavity of ``O.navier_stokes_problem`` (velocity
+    pinned on the boundary, u_x = 16x^2(1-x)^2 on top; the pressure pinned
+    at the first node of the first element).  Velocity values hang by the C2
+    hang infos, pressure values (vertices only) by the C1 ones.  oomph's
+    local equations of an element: its own free values in local order (node
+    by node, velocity then pressure: fe_oracle.c's layout), then the
+    (master node, value) pairs of its hanging values that are not values of
+    its own, by first appearance (RefineableElement::
+    assign_hanging_local_eqn_numbers); equations numbered node by node,
+    value by value (Node::assign_eqn_numbers)."""
+
+    def __init__(self, N: int, chosen, max_level: int, rho: float = 1.0, mu: float = 0.01):
+        self.x, self.conn, hang, hang_c1, on_b = refine_levels(O.mesh(O.Q2_QUAD, N, N), chosen, max_level,
+                                                                with_c1=True)
+        self.hang, self.hang_c1 = hang, hang_c1
+        n = self.x.shape[0]
+        self.isv = np.zeros(n, dtype=np.uint8)
+        self.isv[np.unique(self.conn[:, [0, 2, 6, 8]])] = 1
+        present = np.ones((n, 3), dtype=bool)
+        present[:, 2] = self.isv != 0
+        pinned = np.zeros((n, 3), dtype=bool)
+        pinned[on_b, 0] = pinned[on_b, 1] = True
+        pinned[int(self.conn[0, 0]), 2] = True
+        self.values = np.zeros((n, 3))
+        top = np.abs(self.x[:, 1] - self.x[:, 1].max()) < 1e-12
+        self.values[top, 0] = O.lid_velocity(self.x[top, 0])
+        # hang infos per (node, value)
+        self.hv: Dict[Tuple[int, int], List[Tuple[int, float]]] = {}
+        for h, ms in hang.items():
+            for f in (0, 1):
+                self.hv[(h, f)] = ms
+        for h, ms in hang_c1.items():
+            if present[h, 2]:
+                self.hv[(h, 2)] = ms
+        self.present = present
+        self.eqn = np.full((n, 3), -1, dtype=np.int64)
+        k = 0
+        for i in range(n):
+            for f in range(3):
+                if present[i, f] and not pinned[i, f] and (i, f) not in self.hv:
+                    self.eqn[i, f] = k
+                    k += 1
+        self.n_dof = k
+        self.params = np.array([rho, mu])
+        self._interpolate_hanging()
+
+    def _interpolate_hanging(self) -> None:
+        for (h, f), ms in self.hv.items():
+            self.values[h, f] = sum(w * self.values[m, f] for m, w in ms)
+
+    def dofs(self) -> np.ndarray:
+        m = self.eqn >= 0
+        out = np.zeros(self.n_dof)
+        out[self.eqn[m]] = self.values[m]
+        return out
+
+    def set_dofs(self, d: np.ndarray) -> None:
+        m = self.eqn >= 0
+        self.values[m] = d[self.eqn[m]]
+        self._interpolate_hanging()
+
+    def expand(self, node: int, f: int) -> List[Tuple[int, float]]:
+        if (node, f) in self.hv:
+            return [(int(self.eqn[mm, f]), w) for mm, w in self.hv[(node, f)] if self.eqn[mm, f] >= 0]
+        return [(int(self.eqn[node, f]), 1.0)] if self.eqn[node, f] >= 0 else []
+
+    def assemble(self):
+        L = O.lib()
+        R = np.zeros(self.n_dof)
+        rows: List[Dict[int, float]] = [dict() for _ in range(self.n_dof)]
+        vals = np.ascontiguousarray(self.values)
+        xx = np.ascontiguousarray(self.x)
+        isv = np.ascontiguousarray(self.isv)
+        layout = [(l, f) for l in range(9) for f in range(3) if f < 2 or l in (0, 2, 6, 8)]
+        nl = len(layout)
+        Re = np.zeros(nl)
+        Je = np.zeros(nl * nl)
+        for e in range(self.conn.shape[0]):
+            c = np.ascontiguousarray(self.conn[e])
+            rc = L.ofe_element_res_jac(O.Q2_QUAD, O.EQ_NAVIER_STOKES_TH, 2, O._ptr(xx), O._ptr(c), 3, O._ptr(vals),
+                                       O._ptr(isv), O._ptr(self.params), len(self.params), O._ptr(Re), O._ptr(Je))
+            if rc != nl:                      # the local size on success
+                raise RuntimeError("oracle element failed")
+            J = Je.reshape(nl, nl)
+            slots = [(int(c[l]), f) for l, f in layout]
+            exp = [self.expand(nd, f) for nd, f in slots]
+            dofs = [int(self.eqn[nd, f]) for nd, f in slots if (nd, f) not in self.hv and self.eqn[nd, f] >= 0]
+            own = set(slots)
+            for nd, f in slots:
+                for mm, _ in self.hv.get((nd, f), []):
+                    q = int(self.eqn[mm, f])
+                    if (mm, f) not in own and q >= 0 and q not in dofs:
+                        dofs.append(q)
+            pos = {q: a for a, q in enumerate(dofs)}
+            Jl = np.zeros((len(dofs), len(dofs)))
+            Rl = np.zeros(len(dofs))
+            for i in range(nl):
+                for (r, wr) in exp[i]:
+                    Rl[pos[r]] += wr * Re[i]
+                    for j in range(nl):
+                        for (cc, wc) in exp[j]:
+                            Jl[pos[r], pos[cc]] += wr * wc * J[i, j]
             for a, r in enumerate(dofs):
                 R[r] += Rl[a]
                 row = rows[r]

@@ -400,7 +400,10 @@ class SaddlePointSolver:
             self._precondition(self._gin)           # warm-up: kernels loaded, buffers cached
         torch.cuda.current_stream().wait_stream(side)
         g = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(g):
+        # thread-local: other threads' work (another request's assembly, a
+        # synchronous copy) must not abort this capture, nor be refused
+        # while it runs
+        with torch.cuda.graph(g, capture_error_mode="thread_local"):
             self._gout = self._precondition(self._gin)
         self._graph = g
 

@@ -42,6 +42,7 @@ class MeshData:
     boundaries: Dict[str, np.ndarray] = field(default_factory=dict)  # name -> bool mask over nodes
     lattice: Optional[np.ndarray] = None  # [n_nodes, dim] int64 half-cell coordinates
     hang: Optional[Dict[int, list]] = None  # hanging node -> [(master node, weight)] (refined meshes)
+    hang_c1: Optional[Dict[int, list]] = None  # the same for C1 (vertex) values
 
     @property
     def n_nodes(self) -> int:
@@ -399,10 +400,34 @@ class AdaptiveQuadMesh(MeshTemplate):
         for c in conn:
             for s_ in (0, 2, 6, 8):
                 is_vertex[c[s_]] = True
+        # C1 values (element vertices, bilinear): a vertex strictly inside an
+        # edge of a coarser leaf -- the edge's midpoint too, which the C2
+        # values share with that leaf -- hangs on the edge's two end
+        # vertices with the 1D linear weights at its position (the vertices
+        # are the C1 space's interpolating nodes in setup_hang_for_value:
+        # BulkElementQuad2dC2::interpolating_node_pt, elements.cpp:9162-9250)
+        hang_c1: Dict[int, List[Tuple[int, float]]] = {}
+        for k in np.flatnonzero(is_vertex):
+            qx, qy = int(ql[k, 0]), int(ql[k, 1])
+            found = None
+            for a, b in hor.get(qy, ()):
+                if a < qx < b:
+                    found = ((a, qy), (b, qy), (qx - a) / (b - a))
+                    break
+            if found is None:
+                for a, b in ver.get(qx, ()):
+                    if a < qy < b:
+                        found = ((qx, a), (qx, b), (qy - a) / (b - a))
+                        break
+            if found is not None:
+                pa, pb, t = found
+                hang_c1[int(k)] = [(node_of[key(*pa)], 1.0 - t), (node_of[key(*pb)], t)]
+        hang_c1 = complete_hanging(hang_c1, rank=rank)
         top = N * S
         b = {"left": ql[:, 0] == 0, "right": ql[:, 0] == top, "bottom": ql[:, 1] == 0, "top": ql[:, 1] == top}
         md = MeshData(ELEMENT_TYPES["Q2_QUAD"], x, np.array(conn, dtype=np.int32), is_vertex, b, ql)
         md.hang = hang
+        md.hang_c1 = hang_c1
         return md
 
 

@@ -516,11 +516,17 @@ class Problem:
         if getattr(mesh, "hang", None):
             if R > 1:
                 raise NotImplementedError("replicas of meshes with hanging nodes")
-            if any(sp_ != "C2" for _, sp_ in fields):
-                raise NotImplementedError("hanging nodes with C1 fields")
+            if any(sp_ not in ("C2", "C1") for _, sp_ in fields):
+                raise NotImplementedError("hanging nodes with fields other than C2 and C1")
+            if any(sp_ == "C1" for _, sp_ in fields) and getattr(mesh, "hang_c1", None) is None:
+                raise NotImplementedError("this mesh has no hang infos of its C1 values")
+            # each field hangs by the interpolation of its space: C2 values on
+            # the coarse edge's three nodes, C1 values on its two vertices
             slots, ptr, mas, wts = [], [0], [], []
-            for h, ms in mesh.hang.items():
-                for f in range(nval):
+            for f, (_, sp_) in enumerate(fields):
+                for h, ms in (mesh.hang if sp_ == "C2" else mesh.hang_c1).items():
+                    if not present[h, f]:
+                        continue
                     slots.append(h * nval + f)
                     for m, w in ms:
                         mas.append(m * nval + f)

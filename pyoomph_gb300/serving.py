@@ -197,6 +197,10 @@ class Server:
     solve in a worker -> update -> assemble ...); a class's pending
     assemblies are served by one launch sequence for all its replicas."""
 
+    @staticmethod
+    def default_saddle_min_side() -> int:
+        return 96
+
     def __init__(self, slots: int = 4, jacobian_precision: str = "fp32", tol: float = 1e-10,
                  max_newton: int = 20, workers: int = 8, hbm_reserve: float = 0.1, device_solver: bool = False):
         import torch
@@ -209,15 +213,20 @@ class Server:
         # linear solves in worker processes (spawned: safe after CUDA init)
         self.pool = cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn"))
         self.hbm_reserve = hbm_reserve
-        # device_solver: Poisson requests solve J dx = R on the device, one
-        # batched BiCGStab per class and round (a block per replica, so a
-        # request's iterates never depend on its neighbours), instead of
-        # SuperLU in the workers
+        # device_solver: Newton systems solved on the device instead of by
+        # SuperLU in the workers -- Poisson requests by one batched BiCGStab
+        # per class and round (a block per replica, so a request's iterates
+        # never depend on its neighbours), Navier-Stokes requests by their
+        # own saddle-point solvers
         self.device_solver = device_solver
         # Navier-Stokes requests of at least this side are solved on the
         # device (saddle-point GMRES), smaller ones by SuperLU in the worker
-        # processes, which solve many small systems in parallel faster
-        self.device_saddle_min_side = 96
+        # processes.  Alone, a request's Newton solve is faster on the device
+        # from side 32 (0.16 s against SuperLU's 0.30 s); in a stream of
+        # sides 16..64 the workers' 14 parallel SuperLU solves still serve
+        # more requests per second below side 96 (16.4/s against 11.0/s
+        # with the threshold at 32)
+        self.device_saddle_min_side = self.default_saddle_min_side()
         # device solves run in threads (the native solve releases the GIL),
         # so a long solve of one class does not stall the others
         self.tpool = cf.ThreadPoolExecutor(max_workers=4) if device_solver else None
@@ -473,7 +482,7 @@ class Server:
 
 def serve_sequential(requests: List[Request], precision: str = "fp64", tol: float = 1e-10,
                      realtime: bool = True, device_solver: bool = False,
-                     device_saddle_min_side: int = 96) -> List[Request]:
+                     device_saddle_min_side: int = 32) -> List[Request]:
     """The plain path: requests one at a time in arrival order, one problem
     per request (resident meshes cached per class), Newton with SuperLU
     (with device_solver: Poisson requests with the device BiCGStab, as the

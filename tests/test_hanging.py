@@ -265,3 +265,72 @@ def test_gpu_newton_on_a_multilevel_mesh_matches_the_oracle():
     v = P.get_values()[:, 0]
     for h, ms in P.mesh.hang.items():
         assert abs(v[h] - sum(w * v[m] for m, w in ms)) < 1e-14
+
+
+# Taylor-Hood (Q2 velocity, Q1 pressure) on refined meshes: the pressure of
+# a vertex strictly inside a coarser leaf's edge -- the edge's middle node
+# too -- hangs linearly on the edge's two end vertices
+NS_LEVELS = {"half_L1": (4, lambda x, y, l: x < 0.5, 1), "point_L3": (4, lambda x, y, l: _around(0.26, 0.26, 4)(x, y, l), 3)}
+
+
+def _ns_problem_levels(case, prec="fp64"):
+    from pyoomph_gb300.equations import NavierStokesEquations, PressureFixation
+    from pyoomph_gb300.workloads import lid_velocity
+    n, refine, L = NS_LEVELS[case]
+    P = Problem()
+    P.jacobian_precision = prec
+    P += AdaptiveQuadMesh(N=n, refine=refine, max_level=L)
+    eqs = NavierStokesEquations(mass_density=1.0, dynamic_viscosity=0.01)
+    eqs += DirichletBC(velocity_x=lid_velocity, velocity_y=0.0) @ "top"
+    eqs += DirichletBC(velocity_x=0.0, velocity_y=0.0) @ ["left", "right", "bottom"]
+    eqs += PressureFixation("pressure", 0.0)
+    P += eqs @ "domain"
+    return P, H.HangNSProblem(n, refine, L, rho=1.0, mu=0.01)
+
+
+@pytest.mark.parametrize("case", list(NS_LEVELS))
+def test_taylor_hood_hanging_pressure_numbering_and_pattern_match_the_oracle(case):
+    P, HP = _ns_problem_levels(case)
+    P.lower()
+    assert np.array_equal(P.mesh.conn, HP.conn)
+    assert P.mesh.hang == HP.hang and P.mesh.hang_c1 == HP.hang_c1 and len(HP.hang_c1) > 0
+    # the middle node of a coarse edge: velocity free, pressure hanging
+    mids = [h for h in HP.hang_c1 if h not in HP.hang]
+    assert mids
+    for h, ms in P.mesh.hang_c1.items():        # linear fields are reproduced
+        assert abs(sum(w for _, w in ms) - 1.0) < 1e-14
+        assert np.allclose(sum(w * P.mesh.x[m] for m, w in ms), P.mesh.x[h], atol=1e-14, rtol=0)
+        assert all(HP.isv[m] for m, _ in ms)
+    assert np.array_equal(P.eqn, HP.eqn)
+    rp, ci = P.host_pattern()
+    _, orp, oci, _ = HP.assemble()
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", list(NS_LEVELS))
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_taylor_hood_hanging_assembly_and_newton_match_the_oracle(case, prec):
+    P, HP = _ns_problem_levels(case, prec)
+    P.initialise()
+    rng = np.random.default_rng(3)
+    d = rng.normal(0.0, 0.05, P.n_dof)
+    P.set_dofs(d)
+    HP.set_dofs(d)
+    R, J = P.get_jacobian()
+    Ro, orp, oci, ov = HP.assemble()
+    assert np.array_equal(J.indptr, orp) and np.array_equal(J.indices, oci)
+    assert np.max(np.abs(R - Ro)) <= 1e-12 * np.max(np.abs(Ro))
+    jtol = 1e-12 if prec == "fp64" else 1e-5
+    assert np.max(np.abs(J.data - ov)) <= jtol * np.max(np.abs(ov))
+    # Newton from rest to max |R| < 1e-10; the hanging values follow their masters
+    P.set_dofs(np.zeros(P.n_dof))
+    HP.set_dofs(np.zeros(HP.n_dof))
+    P.newton_solver_tolerance = 1e-10
+    hist = P.solve()
+    assert hist[-1] < 1e-10
+    x0 = HP.newton(tol=1e-10)
+    assert np.max(np.abs(P.get_dofs() - x0)) <= 1e-9 * max(1.0, np.max(np.abs(x0)))
+    v = P.get_values()
+    for h, ms in P.mesh.hang_c1.items():
+        assert abs(v[h, 2] - sum(w * v[m, 2] for m, w in ms)) <= 1e-13 * max(1.0, np.max(np.abs(v[:, 2])))
