@@ -190,7 +190,7 @@ def make_problem(workload: str, size: int, precision: str, epb=None):
     return P
 
 
-TUNED_EPB = {("ns", 256, "df64"): 48}
+TUNED_EPB = {("ns", 256, "df64"): 32}
 
 # DRAM bytes (read + write) per launch of an element kernel, keyed by the
 # generated kernel's name (its source hash): dram__bytes_read.sum +
@@ -200,8 +200,9 @@ TUNED_EPB = {("ns", 256, "df64"): 48}
 # with no capture reports null.  Value: (bytes per element, elements of the
 # captured launch).
 MEASURED_TRAFFIC = {
-    # NS Taylor-Hood 256^2, FP64: 15,403,264 read + 195,289,088 written
-    "fe_elem_p2_tri_f64_aff_0ca0c04fab": ((15403264 + 195289088) / 131072, 131072),
+    # NS Taylor-Hood 256^2, FP64 (registers bounded for two blocks per SM):
+    # 16,041,728 read + 217,390,848 written
+    "fe_elem_p2_tri_f64_aff_ca1e687b31": ((16041728 + 217390848) / 131072, 131072),
 }
 
 
@@ -408,7 +409,8 @@ def run_gb300(args):
         "zero_filter": dict(main["zf"], what="the reference's default sparse assembly: oomph's zero filter at "
                             "0.0, value-dependent CSR pattern compacted on the device (FE_ASSEMBLE_ZERO_FILTER)"),
         "launch_shape": {"elems_per_block": P.kernel.epb, "threads": P.kernel.threads,
-                         "smem_bytes": P.kernel.smem_bytes, "autotuned": tuned or None},
+                         "smem_bytes": P.kernel.smem_bytes, "min_blocks_per_sm": P.kernel.min_blocks or None,
+                         "autotuned": tuned or None},
     }
     r32 = results["fp32"]
     f32 = estimate_flops(r32["P"].kernel, r32["P"].affine)

@@ -364,6 +364,7 @@ class KernelSpec:
     tc_pairs: Optional[List[Tuple[int, int]]] = None
     gauss_sep: int = 0           # > 0: this many Gaussians of the source evaluated separably per element
     sum_fact_interp: bool = False  # interpolation and residual contraction sum-factorised (Q2 hex)
+    min_blocks: int = 0          # > 0: registers bounded for this many resident blocks per SM
 
     @property
     def key(self) -> str:
@@ -416,7 +417,7 @@ def _launch_shape(et: ElementType, nloc: int, per_elem_bytes: int, table_bytes: 
 
 def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                     name: str = None, epb: int = None, affine: bool = False, jref: bool = None,
-                    gauss_sep: bool = False, tc: bool = None) -> KernelSpec:
+                    gauss_sep: bool = False, tc: bool = None, min_blocks: int = None) -> KernelSpec:
     """Fused element kernel for one element type and weak form.
 
     Thread phases (all in one launch, EPB elements per block):
@@ -565,9 +566,20 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     smem = (smem + 15) // 16 * 16
     if threads > 1024 or smem > 227 * 1024:
         raise ValueError(f"{epb} elements per block do not fit a block ({threads} threads, {smem} B shared)")
+    if min_blocks is None:
+        # FP64 / double-float Jacobians of 2D elements: bound the registers
+        # for two resident blocks where their shared memory allows it.
+        # Unbounded, the Taylor-Hood kernel takes 78 (FP64) / 101 (df64)
+        # registers, so one 480-thread block per SM; bounded to 64 it spills
+        # 88 / 324 bytes and runs 6% / 10% faster on GB300 (the FP64 pipe
+        # gets a second block's work across the first's barriers)
+        if jac_precision in ("f64", "df64") and et.dim == 2 and threads <= 512 and 2 * smem <= 227 * 1024:
+            min_blocks = 2
+    elif min_blocks <= 0:
+        min_blocks = None
     if name is None:
         h = hashlib.sha1((et.name + jac_precision + str(affine) + str(epb) + str(jref) + str(sumfac) + str(gsep) +
-                          ("tc" if use_tc else "") +
+                          ("tc" if use_tc else "") + (f"mb{int(min_blocks)}" if min_blocks else "") +
                           str(sfi) + (str(pw.m_entries) if transient else "") +
                           str(pw.r_exprs) +
                           str(pw.d_entries)).encode()).hexdigest()[:10]
@@ -605,7 +617,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w(f"__constant__ double c_M[18] = {{{', '.join(Mv)}}};")
     w(pointwise_source(pw, jreal))
     w(dparam_source(pw))
-    w(f'extern "C" __global__ void __launch_bounds__(FE_NT) {name}(const FeElemArgs a) {{')
+    lb = f"FE_NT, {int(min_blocks)}" if min_blocks else "FE_NT"
+    w(f'extern "C" __global__ void __launch_bounds__({lb}) {name}(const FeElemArgs a) {{')
     w("  extern __shared__ __align__(16) unsigned char fe_smem[];")
     w("  double* sW = reinterpret_cast<double*>(fe_smem);")
     w("  double* sPsi2 = sW + FE_NQ;")
@@ -1051,7 +1064,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         return KernelSpec(name=name, source=source, et=et, layout=layout, pointwise=pw, epb=epb,
                           threads=threads, smem_bytes=smem, jac_precision=jac_precision,
                           tables=et.packed_tables(), sumfac_blocks=0, gauss_sep=gs_n if gsep else 0,
-                          sum_fact_interp=sfi, tc_pairs=[(ah, bh) for (_, _, ah, bh) in hat])
+                          sum_fact_interp=sfi, tc_pairs=[(ah, bh) for (_, _, ah, bh) in hat],
+                          min_blocks=int(min_blocks or 0))
     w("  for (int p = threadIdx.x; p < nel * FE_NLOC; p += FE_NT) {")
     w("    int tf = 0, rel = p;")
     for f in range(nf - 1):
@@ -1203,7 +1217,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                       threads=threads, smem_bytes=smem, jac_precision=jac_precision,
                       tables=et.packed_tables(), sumfac_blocks=len(hat) if sumfac else 0,
                       gauss_sep=gs_n if gsep else 0, sum_fact_interp=sfi,
-                      tc_pairs=[(ah, bh) for (_, _, ah, bh) in hat] if use_tc else None)
+                      tc_pairs=[(ah, bh) for (_, _, ah, bh) in hat] if use_tc else None,
+                      min_blocks=int(min_blocks or 0))
 
 
 def _jacc_update(terms, acc: str, jacc: str) -> str:

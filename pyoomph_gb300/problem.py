@@ -266,6 +266,10 @@ class Problem:
         # contract FP32 element Jacobians on the tensor cores (None: where the
         # generator supports it and it pays, the Q2 hex's 27 x 27 matrices)
         self.tensor_cores: Optional[bool] = None
+        # resident blocks per SM the element kernel's registers are bounded
+        # for (__launch_bounds__ minimum; None: the generator's choice, 0:
+        # no bound)
+        self.min_blocks_per_sm: Optional[int] = None
         # linear_solver = "bicgstab": J dx = R solved on the device (linsolve.py)
         # to this relative tolerance; "fieldsplit": saddle-point systems
         # (Taylor-Hood) on the device (fieldsplit.py: GMRES, block-triangular
@@ -422,12 +426,14 @@ class Problem:
         # geometry kind only -- not on the mesh size: cache it per process
         gsep = bool(self.separable_source and self.affine and mesh_is_axis_aligned(mesh))
         key = (mesh.etype.name, tuple(fields), str(integrand), tuple(used), kprec, self.affine, gsep,
-               self.is_transient, self.tensor_cores, self.elems_per_block, self.jacobian_reference)
+               self.is_transient, self.tensor_cores, self.min_blocks_per_sm, self.elems_per_block,
+               self.jacobian_reference)
         ks = _KERNEL_CACHE.get(key)
         if ks is None:
             pw = differentiate(fields, mesh.dim, integrand, used)
             ks = generate_kernel(mesh.etype, pw, kprec, epb=self.elems_per_block, affine=self.affine,
-                                 jref=self.jacobian_reference, gauss_sep=gsep, tc=self.tensor_cores)
+                                 jref=self.jacobian_reference, gauss_sep=gsep, tc=self.tensor_cores,
+                                 min_blocks=self.min_blocks_per_sm)
             _KERNEL_CACHE[key] = ks
         if self.elems_per_block is None and int(self.replicas) == 1:
             # balance the waves: with W = ceil(E / (SMs x EPB)) waves of one
@@ -448,7 +454,7 @@ class Problem:
                 if ks2 is None:
                     ks2 = generate_kernel(mesh.etype, differentiate(fields, mesh.dim, integrand, used), kprec,
                                           epb=epb, affine=self.affine, jref=self.jacobian_reference,
-                                          gauss_sep=gsep, tc=self.tensor_cores)
+                                          gauss_sep=gsep, tc=self.tensor_cores, min_blocks=self.min_blocks_per_sm)
                     _KERNEL_CACHE[key2] = ks2
                 ks = ks2
         self.kernel: KernelSpec = ks

@@ -120,6 +120,8 @@ def _main(argv=None) -> None:
                     help="assemble J in the reference's zero-filtered pattern (threshold 0.0)")
     ap.add_argument("--transient", action="store_true",
                     help="the transient form (BDF2 weights of dt = 1e-3, both previous levels = the current values)")
+    ap.add_argument("--min-blocks", type=int, default=None,
+                    help="resident blocks per SM to bound the element kernel's registers for")
     ap.add_argument("--tile-gather", action="store_true",
                     help="sum the CSR values with a warp per tile of rows instead of a thread per slot")
     a = ap.parse_args(argv)
@@ -130,6 +132,7 @@ def _main(argv=None) -> None:
     else:
         P = nonlinear_diffusion_problem(N=a.side, seed=0, jacobian_precision=a.precision, transient=a.transient)
     P.elems_per_block = a.epb
+    P.min_blocks_per_sm = a.min_blocks
     if a.jref is not None:
         P.jacobian_reference = bool(a.jref)
     if a.tc is not None:

@@ -33,7 +33,7 @@ static fe_emu_dim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, gridDim = {1, 1,
 #define __constant__ static
 #define __forceinline__ inline
 #define __noinline__
-#define __launch_bounds__(x)
+#define __launch_bounds__(...)
 #define __restrict__ __restrict
 #define __align__(n) alignas(n)
 #define __syncthreads() do {} while (0)
