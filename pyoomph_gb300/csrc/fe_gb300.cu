@@ -135,12 +135,16 @@ __global__ void k_scatter_dofs(const double *__restrict__ dofs, const int *__res
 // value loads together -- the first two contributions of every slot in one
 // go, the rest after -- so a warp keeps U dependent chains in flight
 // instead of one; each slot still sums its contributions in order.
+// With `list`, slot list[i] for i < nnz instead of slot i (the rows one
+// chunk of the pipelined assembly completes).
 template <typename T, int U>
 __global__ void k_gather_slots(const unsigned *__restrict__ cptr, const unsigned *__restrict__ cidx,
-                               const T *__restrict__ jbuf, T *__restrict__ vals, long long nnz) {
+                               const T *__restrict__ jbuf, T *__restrict__ vals, long long nnz,
+                               const int *__restrict__ list) {
   const long long nthr = (long long)gridDim.x * blockDim.x;
   if constexpr (U == 1) {
-    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nnz; s += nthr) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nnz; i += nthr) {
+      const long long s = list ? (long long)list[i] : i;
       const unsigned b = cptr[s], e = cptr[s + 1];
       T acc = jbuf[cidx[b]];
       for (unsigned k = b + 1; k < e; k++) acc += jbuf[cidx[k]];
@@ -150,13 +154,16 @@ __global__ void k_gather_slots(const unsigned *__restrict__ cptr, const unsigned
   }
   for (long long s0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; s0 < nnz; s0 += U * nthr) {
     unsigned b[U], e[U];
+    long long sl[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      const long long s = s0 + u * nthr;
+      const long long i = s0 + u * nthr;
       b[u] = e[u] = 0;
-      if (s < nnz) {
-        b[u] = cptr[s];
-        e[u] = cptr[s + 1];
+      sl[u] = -1;
+      if (i < nnz) {
+        sl[u] = list ? (long long)list[i] : i;
+        b[u] = cptr[sl[u]];
+        e[u] = cptr[sl[u] + 1];
       }
     }
     unsigned i0[U], i1[U];
@@ -173,11 +180,10 @@ __global__ void k_gather_slots(const unsigned *__restrict__ cptr, const unsigned
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      const long long s = s0 + u * nthr;
-      if (s >= nnz) continue;
+      if (sl[u] < 0) continue;
       if (b[u] + 1 < e[u]) acc[u] += v1[u];
       for (unsigned k = b[u] + 2; k < e[u]; k++) acc[u] += jbuf[cidx[k]];
-      vals[s] = acc[u];
+      vals[sl[u]] = acc[u];
     }
   }
 }
@@ -190,18 +196,21 @@ int grid_for(long long n, int threads, int sms);
 
 template <typename T>
 void launch_gather_slots(const unsigned *cptr, const unsigned *cidx, const T *jbuf, T *vals, long long nnz, int sms,
-                         cudaStream_t st) {
+                         cudaStream_t st, const int *list = nullptr) {
   if (sizeof(T) == 4 && nnz >= (1LL << 22))
-    k_gather_slots<T, 4><<<grid_for((nnz + 3) / 4, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz);
+    k_gather_slots<T, 4><<<grid_for((nnz + 3) / 4, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list);
   else
-    k_gather_slots<T, 1><<<grid_for(nnz, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz);
+    k_gather_slots<T, 1><<<grid_for(nnz, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list);
 }
 
 // residual entry r = sum of its element contributions in element order
+// (with `list`, row list[i] for i < n)
 __global__ void k_gather_rows(const unsigned *__restrict__ rptr, const unsigned *__restrict__ ridx,
-                              const double *__restrict__ rbuf, double *__restrict__ R, long long n) {
-  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;
-       r += (long long)gridDim.x * blockDim.x) {
+                              const double *__restrict__ rbuf, double *__restrict__ R, long long n,
+                              const int *__restrict__ list = nullptr) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long r = list ? (long long)list[i] : i;
     const unsigned b = rptr[r], e = rptr[r + 1];
     double acc = 0.0;
     for (unsigned k = b; k < e; k++) acc += rbuf[ridx[k]];
@@ -735,6 +744,10 @@ struct fe_problem {
   int pipe_chunks = 0, pipe_requested = 0;
   std::vector<long long> pipe_elem;
   std::vector<std::vector<std::pair<long long, long long>>> pipe_runs; // per chunk: row ranges it completes
+  // per chunk, the rows and the CSR slots it completes as index lists (one
+  // gather launch each), at pipe_row_off[k] / pipe_slot_off[k]
+  DevBuf pipe_rowlist, pipe_slotlist;
+  std::vector<long long> pipe_row_off, pipe_slot_off;
   DevBuf pipe_dofs, pipe_R, pipe_J;
   cudaStream_t pipe_copy = nullptr;
   std::vector<cudaEvent_t> pipe_ev;
@@ -2032,14 +2045,40 @@ int plan_pipeline(fe_problem *p, int nchunks) {
   const long long blocks = (d.n_elem + d.epb - 1) / d.epb;
   const long long waves = (blocks + wave - 1) / wave;
   nchunks = (int)std::max(1LL, std::min<long long>(nchunks, waves));
-  const long long wave_per_chunk = (waves + nchunks - 1) / nchunks;
-  nchunks = (int)((waves + wave_per_chunk - 1) / wave_per_chunk);
+  // decreasing chunks (waves in proportion to n, n-1, ..., 1): the copy of
+  // each chunk's rows overlaps the next chunk's elements, and the last
+  // chunk's copy, left exposed at the end, is the smallest
+  std::vector<long long> wv(nchunks, 1);
+  {
+    const long long wsum = (long long)nchunks * (nchunks + 1) / 2;
+    long long given = 0;
+    for (int k = 0; k < nchunks; k++) {
+      wv[k] = std::max(1LL, (waves * (nchunks - k) + wsum / 2) / wsum);
+      given += wv[k];
+    }
+    // whole waves: the difference goes to (or comes from) the first chunks
+    // (nchunks <= waves, so a chunk above one wave exists while given > waves)
+    for (int k = 0; waves > 0 && given != waves; k = (k + 1) % nchunks) {
+      if (given < waves) {
+        wv[k]++;
+        given++;
+      } else if (wv[k] > 1) {
+        wv[k]--;
+        given--;
+      }
+    }
+  }
   const long long units = blocks;
   if (p->pipe_copy) CUDA_TRY(cudaStreamSynchronize(p->pipe_copy)); // copies of the old plan
   p->pipe_release();
   p->pipe_elem.assign(nchunks + 1, 0);
-  for (int k = 0; k <= nchunks; k++)
-    p->pipe_elem[k] = std::min(d.n_elem, std::min(units, k * wave_per_chunk * wave) * d.epb);
+  {
+    long long w_at = 0;
+    for (int k = 0; k <= nchunks; k++) {
+      p->pipe_elem[k] = std::min(d.n_elem, std::min(units, w_at * wave) * d.epb);
+      if (k < nchunks) w_at += wv[k];
+    }
+  }
   p->pipe_elem[nchunks] = d.n_elem;
   // a row is complete after the chunk holding its last contributing element;
   // maximal runs of consecutive rows completed by the same chunk become one
@@ -2086,6 +2125,27 @@ int plan_pipeline(fe_problem *p, int nchunks) {
   }
   p->pipe_runs.assign(nchunks, {});
   for (auto &q : runs) p->pipe_runs[q[0]].push_back({q[1], q[2]});
+  {
+    // the chunks' rows and slots as index lists, chunk by chunk
+    const int32_t *rp = p->h_rowptr.data();
+    std::vector<int32_t> rl, sl;
+    rl.reserve((size_t)p->n_dof);
+    sl.reserve((size_t)p->nnz);
+    p->pipe_row_off.assign(nchunks + 1, 0);
+    p->pipe_slot_off.assign(nchunks + 1, 0);
+    for (int k = 0; k < nchunks; k++) {
+      for (const auto &run : p->pipe_runs[k])
+        for (long long r = run.first; r < run.second; r++) {
+          rl.push_back((int32_t)r);
+          for (int32_t q = rp[r]; q < rp[r + 1]; q++) sl.push_back(q);
+        }
+      p->pipe_row_off[k + 1] = (long long)rl.size();
+      p->pipe_slot_off[k + 1] = (long long)sl.size();
+    }
+    int rc;
+    if (!rl.empty() && (rc = p->pipe_rowlist.upload(rl.data(), sizeof(int32_t) * rl.size()))) return rc;
+    if (!sl.empty() && (rc = p->pipe_slotlist.upload(sl.data(), sizeof(int32_t) * sl.size()))) return rc;
+  }
   CUDA_TRY(cudaStreamCreateWithFlags(&p->pipe_copy, cudaStreamNonBlocking));
   p->pipe_ev.resize(nchunks + 1);
   for (auto &e : p->pipe_ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -2140,22 +2200,23 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
       CUDA_TRY(cudaLaunchKernel((const void *)d.code->func, dim3(grid), dim3(d.threads), kp, (size_t)d.smem, st));
       if (want_j && d.tc && (rc = tc_domain(p, d, e0, e1, st))) return rc;
     }
-    for (const auto &run : p->pipe_runs[k]) {
-      const long long r0 = run.first, r1 = run.second;
-      const long long s0 = h_rp[r0], s1 = h_rp[r1];
-      if (want_r) {
-        k_gather_rows<<<grid_for(r1 - r0, 256, sms), 256, 0, st>>>(p->rptr.as<unsigned>() + r0, p->ridx.as<unsigned>(),
-                                                                  p->rbuf_all.as<double>(), p->pipe_R.as<double>() + r0,
-                                                                  r1 - r0);
+    // the rows and slots this chunk completes: one gather launch each
+    {
+      const long long q0 = p->pipe_row_off[k], q1 = p->pipe_row_off[k + 1];
+      const long long z0 = p->pipe_slot_off[k], z1 = p->pipe_slot_off[k + 1];
+      if (want_r && q1 > q0) {
+        k_gather_rows<<<grid_for(q1 - q0, 256, sms), 256, 0, st>>>(
+            p->rptr.as<unsigned>(), p->ridx.as<unsigned>(), p->rbuf_all.as<double>(), p->pipe_R.as<double>(),
+            q1 - q0, p->pipe_rowlist.as<int>() + q0);
         CUDA_TRY(cudaGetLastError());
       }
-      if (want_j && s1 > s0) {
+      if (want_j && z1 > z0) {
         if (p->jac_prec == FE_JAC_F64)
-          launch_gather_slots<double>(p->cptr.as<unsigned>() + s0, p->cidx.as<unsigned>(), p->jbuf_all.as<double>(),
-                                      p->pipe_J.as<double>() + s0, s1 - s0, sms, st);
+          launch_gather_slots<double>(p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->jbuf_all.as<double>(),
+                                      p->pipe_J.as<double>(), z1 - z0, sms, st, p->pipe_slotlist.as<int>() + z0);
         else
-          launch_gather_slots<float>(p->cptr.as<unsigned>() + s0, p->cidx.as<unsigned>(), p->jbuf_all.as<float>(),
-                                     p->pipe_J.as<float>() + s0, s1 - s0, sms, st);
+          launch_gather_slots<float>(p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->jbuf_all.as<float>(),
+                                     p->pipe_J.as<float>(), z1 - z0, sms, st, p->pipe_slotlist.as<int>() + z0);
         CUDA_TRY(cudaGetLastError());
       }
     }
