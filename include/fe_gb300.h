@@ -370,6 +370,10 @@ int fe_csr_spmv(const int32_t *rowptr, const int32_t *colidx, const void *vals, 
  * path, which solves with SuperLU).  y must not alias x. */
 int fe_csr_update(const int32_t *rowptr, const int32_t *colidx, const double *vals, const double *x, const double *b,
                   const double *z, const double *w, double sc, double *y, int64_t n, int64_t nnz, void *stream);
+/* The same in FP32 (values and vectors): the saddle-point solver's FP32
+ * multigrid cycle.  With b, z, w NULL and sc = -1 it is y = A x. */
+int fe_csr_update_f32(const int32_t *rowptr, const int32_t *colidx, const float *vals, const float *x, const float *b,
+                      const float *z, const float *w, float sc, float *y, int64_t n, int64_t nnz, void *stream);
 int fe_csr_diagonal(const int32_t *rowptr, const int32_t *colidx, const void *vals, int val_precision, double *diag,
                     int64_t n, void *stream);
 

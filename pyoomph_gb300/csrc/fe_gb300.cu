@@ -563,19 +563,20 @@ __global__ void __launch_bounds__(256) k_csr_spmv(const int *__restrict__ rowptr
 // Jacobi step (z = x, w = 1/diag, sc = omega), a residual (z = w = null,
 // sc = 1), a prolongation-and-add (b = w = null, z = the iterate, sc = -1,
 // A = P).  The same 4-lane row groups and summation order as k_csr_spmv.
-template <int L>
+// T = float: the FP32 copy of the multigrid cycle (a preconditioner needs no
+// FP64 accuracy; on GB300 the FP64 pipe bounds the FP64 variant).
+template <int L, typename T>
 __global__ void __launch_bounds__(256) k_csr_update(const int *__restrict__ rowptr, const int *__restrict__ colidx,
-                                                    const double *__restrict__ vals, const double *__restrict__ x,
-                                                    const double *__restrict__ b, const double *__restrict__ z,
-                                                    const double *__restrict__ w, double sc, double *__restrict__ y,
-                                                    long long n) {
+                                                    const T *__restrict__ vals, const T *__restrict__ x,
+                                                    const T *__restrict__ b, const T *__restrict__ z,
+                                                    const T *__restrict__ w, T sc, T *__restrict__ y, long long n) {
   const int sub = threadIdx.x & (L - 1);
   const unsigned gmask = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << ((threadIdx.x & 31) & ~(L - 1)));
   const long long ng = ((long long)gridDim.x * blockDim.x) / L;
   for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / L; r < n; r += ng) {
     const int e = rowptr[r + 1];
     int k = rowptr[r] + sub;
-    double a0 = 0.0, a1 = 0.0;
+    T a0 = (T)0, a1 = (T)0;
     for (; k + 3 * L < e; k += 4 * L) {
       a0 = fma(__ldcs(vals + k), x[__ldcs(colidx + k)], a0);
       a1 = fma(__ldcs(vals + k + L), x[__ldcs(colidx + k + L)], a1);
@@ -583,11 +584,11 @@ __global__ void __launch_bounds__(256) k_csr_update(const int *__restrict__ rowp
       a1 = fma(__ldcs(vals + k + 3 * L), x[__ldcs(colidx + k + 3 * L)], a1);
     }
     for (; k < e; k += L) a0 = fma(__ldcs(vals + k), x[__ldcs(colidx + k)], a0);
-    double acc = a0 + a1;
+    T acc = a0 + a1;
 #pragma unroll
     for (int o = L / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o);
     if (sub == 0) {
-      const double br = b ? b[r] : 0.0, wr = w ? w[r] : 1.0, zr = z ? z[r] : 0.0;
+      const T br = b ? b[r] : (T)0, wr = w ? w[r] : (T)1, zr = z ? z[r] : (T)0;
       y[r] = fma(sc * wr, br - acc, zr);
     }
   }
@@ -2490,9 +2491,25 @@ int fe_csr_update(const int32_t *rowptr, const int32_t *colidx, const double *va
   const int g = grid_for(n * L, 256, sm_count_cached());
   cudaStream_t st = (cudaStream_t)stream;
   if (L == 4)
-    k_csr_update<4><<<g, 256, 0, st>>>(rowptr, colidx, vals, x, b, z, w, sc, y, n);
+    k_csr_update<4, double><<<g, 256, 0, st>>>(rowptr, colidx, vals, x, b, z, w, sc, y, n);
   else
-    k_csr_update<32><<<g, 256, 0, st>>>(rowptr, colidx, vals, x, b, z, w, sc, y, n);
+    k_csr_update<32, double><<<g, 256, 0, st>>>(rowptr, colidx, vals, x, b, z, w, sc, y, n);
+  CUDA_TRY(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_csr_update_f32(const int32_t *rowptr, const int32_t *colidx, const float *vals, const float *x, const float *b,
+                      const float *z, const float *w, float sc, float *y, int64_t n, int64_t nnz, void *stream) {
+  if (n < 0 || nnz < 0 || (n > 0 && (!rowptr || !y || (nnz > 0 && (!colidx || !vals || !x)))))
+    return fail(FE_ERR_ARG, "fe_csr_update_f32: bad arguments");
+  if (n == 0) return FE_OK;
+  const int L = (double)nnz > 128.0 * (double)n ? 32 : 4;
+  const int g = grid_for(n * L, 256, sm_count_cached());
+  cudaStream_t st = (cudaStream_t)stream;
+  if (L == 4)
+    k_csr_update<4, float><<<g, 256, 0, st>>>(rowptr, colidx, vals, x, b, z, w, sc, y, n);
+  else
+    k_csr_update<32, float><<<g, 256, 0, st>>>(rowptr, colidx, vals, x, b, z, w, sc, y, n);
   CUDA_TRY(cudaGetLastError());
   return FE_OK;
 }

@@ -11,11 +11,12 @@ Jacobi- or ILU-preconditioned Krylov methods need iteration counts that grow
 with the mesh.  This solver keeps everything on the device and converges in
 a mesh-independent number of iterations:
 
-* right-preconditioned GMRES (restarted, classical Gram-Schmidt applied
-  twice; the Hessenberg matrix stays on the device and the host reads it
-  every few iterations for the Givens rotations) on the resident CSR
-  Jacobian (``fe_csr_spmv``), to the relative tolerance of an inexact
-  Newton step (``newton_forcing``);
+* flexible right-preconditioned GMRES (restarted, classical Gram-Schmidt
+  applied twice; the preconditioned vectors kept for the update; the
+  Hessenberg matrix stays on the device and the host reads it every few
+  iterations for the Givens rotations) on the resident CSR Jacobian
+  (``fe_csr_spmv``), to the relative tolerance of an inexact Newton step
+  (``newton_forcing``);
 * the block upper-triangular preconditioner P = [[A, Bt], [0, S_hat]]:
   p = S_hat^-1 r_p, u = A_hat^-1 (r_u - Bt p), which would need two GMRES
   iterations with exact blocks;
@@ -27,7 +28,10 @@ a mesh-independent number of iterations:
   block (aggregates of strongly coupled unknowns of the same component,
   ``fe_sa_aggregate``; prolongators smoothed by one damped-Jacobi step;
   Galerkin coarse operators; damped-Jacobi smoothing; a dense inverse on
-  the coarsest level), every level applied with the library's CSR kernel.
+  the coarsest level), every level applied with the library's CSR kernel;
+* the preconditioner in FP32 by default (``fe_csr_update_f32``): on GB300
+  the FP64 pipe bounds an FP64 SpMV, and flexible GMRES takes an inexact
+  preconditioner at no cost in accuracy.
 
 The hierarchy is built on the host once, from the first Jacobian, and kept
 for the following Newton steps (only the finest velocity block is refreshed
@@ -47,29 +51,36 @@ from .linsolve import DeviceCSR, LinearSolverError
 
 class _DevCSR:
     """A CSR matrix on the device in the layout of fe_csr_spmv (int32
-    indices, FP64 values); rectangular matrices too."""
+    indices, FP64 or FP32 values -- with vectors of the same type);
+    rectangular matrices too."""
 
-    def __init__(self, torch, A, dev):
+    def __init__(self, torch, A, dev, dtype=None):
         A = A.tocsr()
         A.sort_indices()
         self.n, self.m = A.shape
         self.nnz = int(A.nnz)
+        self.f32 = dtype is not None and dtype == torch.float32
+        npd = np.float32 if self.f32 else np.float64
         self.rp = torch.as_tensor(A.indptr.astype(np.int32), device=dev)
         self.ci = torch.as_tensor(A.indices.astype(np.int32) if A.nnz else np.zeros(1, np.int32), device=dev)
-        self.v = torch.as_tensor(A.data.astype(np.float64) if A.nnz else np.zeros(1), device=dev)
+        self.v = torch.as_tensor(A.data.astype(npd) if A.nnz else np.zeros(1, npd), device=dev)
 
     def update(self, x, b, z, w, sc: float, y, stream) -> None:
-        """y = z + sc * w o (b - A x) (fe_csr_update; None: 0, 0, 1)."""
+        """y = z + sc * w o (b - A x) (fe_csr_update / _f32; None: 0, 0, 1)."""
         if self.n == 0:
             return
         ptr = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
-        N.check(N.load().fe_csr_update(ctypes.c_void_p(self.rp.data_ptr()), ctypes.c_void_p(self.ci.data_ptr()),
-                                       ctypes.c_void_p(self.v.data_ptr()), ptr(x), ptr(b), ptr(z), ptr(w),
-                                       float(sc), ctypes.c_void_p(y.data_ptr()), self.n, self.nnz,
-                                       ctypes.c_void_p(stream)))
+        f = N.load().fe_csr_update_f32 if self.f32 else N.load().fe_csr_update
+        N.check(f(ctypes.c_void_p(self.rp.data_ptr()), ctypes.c_void_p(self.ci.data_ptr()),
+                  ctypes.c_void_p(self.v.data_ptr()), ptr(x), ptr(b), ptr(z), ptr(w),
+                  float(sc), ctypes.c_void_p(y.data_ptr()), self.n, self.nnz, ctypes.c_void_p(stream)))
 
     def mv(self, x, y, stream) -> None:
+        """y = A x."""
         if self.n == 0:
+            return
+        if self.f32:
+            self.update(x, None, None, None, -1.0, y, stream)
             return
         N.check(N.load().fe_csr_spmv(ctypes.c_void_p(self.rp.data_ptr()), ctypes.c_void_p(self.ci.data_ptr()),
                                      ctypes.c_void_p(self.v.data_ptr()), N.FE_JAC_F64,
@@ -235,10 +246,16 @@ class SaddlePointSolver:
     approximated by the pressure mass over it)."""
 
     def __init__(self, P, schur_field: str, schur_scale: float, restart: int = 60, smooth_steps: int = 2,
-                 theta: float = 0.08, coarse_size: int = 800, max_levels: int = 12):
+                 theta: float = 0.08, coarse_size: int = 800, max_levels: int = 12, precond_precision: str = "fp32"):
         import scipy.sparse as sps
         import torch
         self.torch = torch
+        if precond_precision not in ("fp32", "fp64"):
+            raise ValueError("precond_precision: 'fp32' or 'fp64'")
+        # the preconditioner's arithmetic: the multigrid cycle, Bt and the
+        # Schur scaling in FP32 (flexible GMRES keeps every preconditioned
+        # vector, so its rounding does not enter the solution's accuracy)
+        self.pdt = torch.float32 if precond_precision == "fp32" else torch.float64
         self.P = P
         self.dev = P.J_dev.device
         self.restart = int(restart)
@@ -317,7 +334,8 @@ class SaddlePointSolver:
         q = np.random.default_rng(1).normal(size=self.pre.size)
         s = float(q @ (B @ ((Bt @ q) / D)))
         self.sigma = -1.0 if s > 0 else 1.0
-        self.sinv = torch.as_tensor(self.sigma * self.schur_scale / self.mass, device=self.dev)
+        pdt = self.pdt
+        self.sinv = torch.as_tensor(self.sigma * self.schur_scale / self.mass, device=self.dev).to(pdt)
         levels = []
         comp = self.comp_v
         while A.shape[0] > self.coarse_size and len(levels) < self.max_levels:
@@ -329,25 +347,25 @@ class SaddlePointSolver:
             Pm, Ac, lam = sa_level(A, agg, na)
             cc = np.zeros(na, dtype=np.int32)
             cc[agg] = comp
-            levels.append({"A": _DevCSR(torch, A, self.dev), "P": _DevCSR(torch, Pm, self.dev),
-                           "R": _DevCSR(torch, Pm.T.tocsr(), self.dev),
-                           "dinv": torch.as_tensor(1.0 / Dl, device=self.dev), "om": 1.0 / lam, "n": n, "nc": na,
-                           "dinv_om": torch.as_tensor((1.0 / lam) / Dl, device=self.dev),
-                           "x": torch.zeros(n, dtype=torch.float64, device=self.dev),
-                           "x2": torch.zeros(n, dtype=torch.float64, device=self.dev),
-                           "t": torch.zeros(n, dtype=torch.float64, device=self.dev),
-                           "bc": torch.zeros(na, dtype=torch.float64, device=self.dev)})
+            levels.append({"A": _DevCSR(torch, A, self.dev, pdt), "P": _DevCSR(torch, Pm, self.dev, pdt),
+                           "R": _DevCSR(torch, Pm.T.tocsr(), self.dev, pdt),
+                           "dinv": torch.as_tensor(1.0 / Dl, device=self.dev).to(pdt), "om": 1.0 / lam, "n": n,
+                           "nc": na, "dinv_om": torch.as_tensor((1.0 / lam) / Dl, device=self.dev).to(pdt),
+                           "x": torch.zeros(n, dtype=pdt, device=self.dev),
+                           "x2": torch.zeros(n, dtype=pdt, device=self.dev),
+                           "t": torch.zeros(n, dtype=pdt, device=self.dev),
+                           "bc": torch.zeros(na, dtype=pdt, device=self.dev)})
             A, comp = Ac, cc
         # the coarsest operator's inverse on the host (<= coarse_size unknowns;
         # numpy), applied on the device as a dense matrix in CSR form by the
         # library's kernel: its summation order is fixed, so a solve does not
         # depend on the stream or the library workspace it runs with
         inv = np.linalg.inv(A.toarray())
-        self.coarse_inv = _DevCSR(torch, sps.csr_matrix(inv), self.dev)
-        self.coarse_out = torch.zeros(inv.shape[0], dtype=torch.float64, device=self.dev)
+        self.coarse_inv = _DevCSR(torch, sps.csr_matrix(inv), self.dev, pdt)
+        self.coarse_out = torch.zeros(inv.shape[0], dtype=pdt, device=self.dev)
         self.levels = levels
         self._graph = None                          # recaptured for the new hierarchy
-        self.Bt = _DevCSR(torch, Bt, self.dev)
+        self.Bt = _DevCSR(torch, Bt, self.dev, pdt)
         self.sizes = [lv["n"] for lv in levels] + [A.shape[0]]
 
     # -- application -------------------------------------------------------
@@ -408,16 +426,19 @@ class SaddlePointSolver:
         self._graph = g
 
     def _precondition(self, r):
-        """z = P^-1 r: p = S_hat^-1 r_p, u = A_hat^-1 (r_u - Bt p)."""
+        """z = P^-1 r: p = S_hat^-1 r_p, u = A_hat^-1 (r_u - Bt p), in the
+        preconditioner's precision; z in FP64."""
         torch = self.torch
         st = torch.cuda.current_stream().cuda_stream
-        p = self.sinv * r.index_select(0, self.pre_t)
-        tv = torch.empty(self.vel.size, dtype=torch.float64, device=self.dev)
+        rp_ = r.to(self.pdt)
+        p = self.sinv * rp_.index_select(0, self.pre_t)
+        tv = torch.empty(self.vel.size, dtype=self.pdt, device=self.dev)
         self.Bt.mv(p, tv, st)
-        u = self._vcycle(0, r.index_select(0, self.vel_t) - tv)
-        z = torch.empty_like(r)
+        u = self._vcycle(0, rp_.index_select(0, self.vel_t) - tv)
+        z = torch.empty(r.shape, dtype=self.pdt, device=self.dev)
         z.index_copy_(0, self.vel_t, u)
         z.index_copy_(0, self.pre_t, p)
+        z = z.to(torch.float64)
         return z
 
     def refresh(self) -> None:
@@ -451,6 +472,10 @@ class SaddlePointSolver:
             return x, 0
         m = self.restart
         V = torch.zeros((m + 1, n), dtype=torch.float64, device=self.dev)
+        # flexible GMRES: the preconditioned vectors are kept, and the
+        # update is built from them (x += Z y), so a preconditioner that is
+        # not exactly linear (FP32 rounding) costs no accuracy
+        Z = torch.zeros((m, n), dtype=torch.float64, device=self.dev)
         Az = torch.empty(n, dtype=torch.float64, device=self.dev)
         its = 0
         r = b.clone()
@@ -469,8 +494,8 @@ class SaddlePointSolver:
             k = 0
             done = False
             for k in range(m):
-                z = self.precondition(V[k])
-                self.J.matvec(z, Az, st)
+                Z[k].copy_(self.precondition(V[k]))
+                self.J.matvec(Z[k], Az, st)
                 h = V[:k + 1] @ Az
                 w = Az - V[:k + 1].T @ h
                 h2 = V[:k + 1] @ w               # second pass (classical Gram-Schmidt twice)
@@ -508,7 +533,7 @@ class SaddlePointSolver:
             kk = k + 1
             y = np.linalg.solve(np.triu(H[:kk, :kk]), g[:kk]) if kk else np.zeros(0)
             yt = torch.as_tensor(y, device=self.dev)
-            x += self.precondition(V[:kk].T @ yt)
+            x += Z[:kk].T @ yt
             self.J.matvec(x, Az, st)
             r = b - Az
             beta = float(torch.linalg.vector_norm(r))
