@@ -293,6 +293,18 @@ void fe_sa_level_destroy(fe_sa_level_t *level);
 int fe_csr_block(int64_t n, const int32_t *rowptr, const int32_t *colidx, const int8_t *label, int rl, int cl,
                  int64_t *nnz, int32_t *b_rowptr, int32_t *b_colidx, int64_t *b_slot);
 
+/* One Arnoldi step of GMRES with classical Gram-Schmidt applied twice, on
+ * DEVICE vectors: for the basis rows V[0..k] (n doubles each, row stride
+ * ldv >= n; row k+1 receives the new vector) and w = A z (overwritten):
+ * h = V w, w -= V^T h, h2 = V w, w -= V^T h2; hcol[j] = h[j] + h2[j] for
+ * j <= k, hcol[k+1] = |w|, V[k+1] = w / |w|.  Reductions over fixed
+ * chunks of rows in a fixed order (deterministic).  work: device scratch of
+ * fe_gmres_cgs2_scratch(n, kmax) doubles, kmax >= k, k + 2 <= 128.
+ * Ordered on `stream`.  The saddle-point solver's Arnoldi process (no
+ * counterpart on the reference's path, which solves with SuperLU). */
+int64_t fe_gmres_cgs2_scratch(int64_t n, int kmax);
+int fe_gmres_cgs2(double *V, int64_t ldv, int64_t n, int k, double *w, double *hcol, double *work, void *stream);
+
 /* Threshold of FE_ASSEMBLE_ZERO_FILTER assemblies (oomph's
  * Problem::Numerical_zero_for_sparse_assembly, problem.cc:110; default 0.0,
  * must be >= 0). */

@@ -2585,3 +2585,4 @@ int fe_problem_launch_count(const fe_problem_t *p, int flags) {
 
 #include "fe_krylov.cuh"
 #include "fe_sa_level.cuh"
+#include "fe_gmres.cuh"

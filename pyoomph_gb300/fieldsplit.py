@@ -477,6 +477,9 @@ class SaddlePointSolver:
         # not exactly linear (FP32 rounding) costs no accuracy
         Z = torch.zeros((m, n), dtype=torch.float64, device=self.dev)
         Az = torch.empty(n, dtype=torch.float64, device=self.dev)
+        L = N.load()
+        work = torch.empty(int(L.fe_gmres_cgs2_scratch(n, m)), dtype=torch.float64, device=self.dev)
+        vp = ctypes.c_void_p
         its = 0
         r = b.clone()
         beta = bnorm
@@ -490,27 +493,22 @@ class SaddlePointSolver:
             g = np.zeros(m + 1)
             g[0] = beta
             cs, sn = np.zeros(m), np.zeros(m)
-            Hd = torch.zeros((m + 1, m), dtype=torch.float64, device=self.dev)
+            HdT = torch.zeros((m, m + 1), dtype=torch.float64, device=self.dev)   # row k: column k of H
             k = 0
             done = False
             for k in range(m):
                 Z[k].copy_(self.precondition(V[k]))
                 self.J.matvec(Z[k], Az, st)
-                h = V[:k + 1] @ Az
-                w = Az - V[:k + 1].T @ h
-                h2 = V[:k + 1] @ w               # second pass (classical Gram-Schmidt twice)
-                w -= V[:k + 1].T @ h2
-                nw = torch.linalg.vector_norm(w)
-                Hd[:k + 1, k] = h + h2
-                Hd[k + 1, k] = nw
-                V[k + 1] = w / nw.clamp_min(1e-300)
+                # classical Gram-Schmidt twice, Az overwritten (fe_gmres_cgs2)
+                N.check(L.fe_gmres_cgs2(vp(V.data_ptr()), n, n, k, vp(Az.data_ptr()), vp(HdT[k].data_ptr()),
+                                        vp(work.data_ptr()), vp(st)))
                 its += 1
                 if (k + 1) % self.check_every and k + 1 < m and its < maxiter:
                     continue                     # the host looks every check_every steps only
                 # Givens rotations of the columns since the last look (one synchronisation)
                 k0 = (k // self.check_every) * self.check_every if (k + 1) % self.check_every else k + 1 - self.check_every
                 k0 = max(0, min(k0, k))
-                H[:, k0:k + 1] = Hd[:, k0:k + 1].cpu().numpy()
+                H[:, k0:k + 1] = HdT[k0:k + 1].cpu().numpy().T
                 for j in range(k0, k + 1):
                     for i in range(j):
                         t_ = cs[i] * H[i, j] + sn[i] * H[i + 1, j]

@@ -137,3 +137,40 @@ def test_problems_without_a_constrained_field_are_refused():
     P.linear_solver = "fieldsplit"
     with pytest.raises(RuntimeError):
         P.solve()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,k", [(1000, 0), (5000, 7), (300001, 40)])
+def test_native_gram_schmidt_step_matches_torch_and_repeats(n, k):
+    """fe_gmres_cgs2 against classical Gram-Schmidt twice written in torch
+    (to rounding), and bit-identical when repeated."""
+    import ctypes
+    import torch
+    from pyoomph_gb300 import _native as N
+    L = N.load()
+    g = torch.Generator(device="cuda").manual_seed(k + 1)
+    m = 60
+    V = torch.zeros((m + 1, n), dtype=torch.float64, device="cuda")
+    Q, _ = torch.linalg.qr(torch.randn((n, k + 1), dtype=torch.float64, device="cuda", generator=g))
+    V[:k + 1] = Q.T
+    a = torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
+    h = V[:k + 1] @ a
+    w = a - V[:k + 1].T @ h
+    h2 = V[:k + 1] @ w
+    w -= V[:k + 1].T @ h2
+    nw = torch.linalg.vector_norm(w)
+    ref_h, ref_v = torch.cat([h + h2, nw.view(1)]), w / nw
+    work = torch.empty(int(L.fe_gmres_cgs2_scratch(n, m)), dtype=torch.float64, device="cuda")
+    outs = []
+    for _ in range(2):
+        Vc, wc = V.clone(), a.clone()
+        hc = torch.zeros(m + 1, dtype=torch.float64, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream
+        N.check(L.fe_gmres_cgs2(ctypes.c_void_p(Vc.data_ptr()), n, n, k, ctypes.c_void_p(wc.data_ptr()),
+                                ctypes.c_void_p(hc.data_ptr()), ctypes.c_void_p(work.data_ptr()), ctypes.c_void_p(st)))
+        torch.cuda.synchronize()
+        outs.append((hc[:k + 2].clone(), Vc[k + 1].clone()))
+    assert torch.max(torch.abs(outs[0][0] - ref_h)) <= 1e-12 * torch.max(torch.abs(ref_h))
+    assert torch.max(torch.abs(outs[0][1] - ref_v)) <= 1e-12
+    assert torch.equal(outs[0][0].view(torch.int64), outs[1][0].view(torch.int64))
+    assert torch.equal(outs[0][1].view(torch.int64), outs[1][1].view(torch.int64))
