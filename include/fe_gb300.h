@@ -305,6 +305,18 @@ int fe_csr_block(int64_t n, const int32_t *rowptr, const int32_t *colidx, const 
 int64_t fe_gmres_cgs2_scratch(int64_t n, int kmax);
 int fe_gmres_cgs2(double *V, int64_t ldv, int64_t n, int k, double *w, double *hcol, double *work, void *stream);
 
+/* Vector steps of the saddle-point solver's FP32 preconditioner (DEVICE
+ * pointers, ordered on `stream`):
+ *   fe_gather_cast_f32:  dst[i] = (float) src[idx[i]] (times scale[i] when
+ *                        scale is not NULL), i < n;
+ *   fe_sub_mul_f32:      t = a[i] - b[i] (b NULL: a[i]); c[i] = t (c not
+ *                        NULL); x[i] = d[i] t;
+ *   fe_scatter_cast_f64: dst[idx[i]] = (double) src[i]. */
+int fe_gather_cast_f32(const double *src, const int64_t *idx, int64_t n, const float *scale, float *dst,
+                       void *stream);
+int fe_sub_mul_f32(const float *a, const float *b, const float *d, float *c, float *x, int64_t n, void *stream);
+int fe_scatter_cast_f64(const float *src, const int64_t *idx, int64_t n, double *dst, void *stream);
+
 /* Threshold of FE_ASSEMBLE_ZERO_FILTER assemblies (oomph's
  * Problem::Numerical_zero_for_sparse_assembly, problem.cc:110; default 0.0,
  * must be >= 0). */

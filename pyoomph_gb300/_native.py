@@ -38,7 +38,8 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_problem_set_gather", "fe_problem_gather_lanes",
            "fe_problem_set_tensor_contraction", "fe_tc_contract", "fe_sa_aggregate",
            "fe_csr_update", "fe_sa_level_build", "fe_sa_level_info", "fe_sa_level_copy", "fe_sa_level_destroy",
-           "fe_csr_block", "fe_csr_update_f32", "fe_gmres_cgs2_scratch", "fe_gmres_cgs2"]
+           "fe_csr_block", "fe_csr_update_f32", "fe_gmres_cgs2_scratch", "fe_gmres_cgs2",
+           "fe_gather_cast_f32", "fe_sub_mul_f32", "fe_scatter_cast_f64"]
 
 
 def _header_stamp() -> str:
@@ -166,6 +167,9 @@ def load(build_if_missing: bool = True):
         L.fe_gmres_cgs2_scratch.argtypes = [ctypes.c_int64, c_int]
         L.fe_gmres_cgs2_scratch.restype = ctypes.c_int64
         L.fe_gmres_cgs2.argtypes = [vp, ctypes.c_int64, ctypes.c_int64, c_int, vp, vp, vp, vp]
+        L.fe_gather_cast_f32.argtypes = [vp, vp, ctypes.c_int64, vp, vp, vp]
+        L.fe_sub_mul_f32.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int64, vp]
+        L.fe_scatter_cast_f64.argtypes = [vp, vp, ctypes.c_int64, vp, vp]
         L.fe_problem_gather_lanes.argtypes = [vp]
         L.fe_problem_filtered_pattern.argtypes = [vp, vp, vp, vp, vp]
         L.fe_problem_set_tensor_contraction.argtypes = [vp, c_int, c_int, c_int, c_int, vp, c_int, vp, vp]

@@ -137,14 +137,14 @@ __global__ void k_scatter_dofs(const double *__restrict__ dofs, const int *__res
 // instead of one; each slot still sums its contributions in order.
 // With `list`, slot list[i] for i < nnz instead of slot i (the rows one
 // chunk of the pipelined assembly completes).
-template <typename T, int U>
+template <typename T, int U, bool LIST>
 __global__ void k_gather_slots(const unsigned *__restrict__ cptr, const unsigned *__restrict__ cidx,
                                const T *__restrict__ jbuf, T *__restrict__ vals, long long nnz,
                                const int *__restrict__ list) {
   const long long nthr = (long long)gridDim.x * blockDim.x;
   if constexpr (U == 1) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nnz; i += nthr) {
-      const long long s = list ? (long long)list[i] : i;
+      const long long s = LIST ? (long long)list[i] : i;
       const unsigned b = cptr[s], e = cptr[s + 1];
       T acc = jbuf[cidx[b]];
       for (unsigned k = b + 1; k < e; k++) acc += jbuf[cidx[k]];
@@ -161,7 +161,7 @@ __global__ void k_gather_slots(const unsigned *__restrict__ cptr, const unsigned
       b[u] = e[u] = 0;
       sl[u] = -1;
       if (i < nnz) {
-        sl[u] = list ? (long long)list[i] : i;
+        sl[u] = LIST ? (long long)list[i] : i;
         b[u] = cptr[sl[u]];
         e[u] = cptr[sl[u] + 1];
       }
@@ -197,10 +197,15 @@ int grid_for(long long n, int threads, int sms);
 template <typename T>
 void launch_gather_slots(const unsigned *cptr, const unsigned *cidx, const T *jbuf, T *vals, long long nnz, int sms,
                          cudaStream_t st, const int *list = nullptr) {
-  if (sizeof(T) == 4 && nnz >= (1LL << 22))
-    k_gather_slots<T, 4><<<grid_for((nnz + 3) / 4, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list);
+  const bool big = sizeof(T) == 4 && nnz >= (1LL << 22);
+  if (big && list)
+    k_gather_slots<T, 4, true><<<grid_for((nnz + 3) / 4, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list);
+  else if (big)
+    k_gather_slots<T, 4, false><<<grid_for((nnz + 3) / 4, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list);
+  else if (list)
+    k_gather_slots<T, 1, true><<<grid_for(nnz, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list);
   else
-    k_gather_slots<T, 1><<<grid_for(nnz, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list);
+    k_gather_slots<T, 1, false><<<grid_for(nnz, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list);
 }
 
 // residual entry r = sum of its element contributions in element order

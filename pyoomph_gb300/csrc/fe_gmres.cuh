@@ -140,9 +140,61 @@ __global__ void k_cgs_scale(const double *__restrict__ w, const double *__restri
     vnext[i] = w[i] * inv;
 }
 
+// the FP32 preconditioner's vector steps (the library's own kernels: torch's
+// FP32 kernels cost seconds at their first use in a process on this machine)
+__global__ void k_gather_cast_f32(const double *__restrict__ src, const int64_t *__restrict__ idx, long long n,
+                                  const float *__restrict__ scale, float *__restrict__ dst) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float v = (float)src[idx[i]];
+    dst[i] = scale ? scale[i] * v : v;
+  }
+}
+
+__global__ void k_sub_mul_f32(const float *__restrict__ a, const float *__restrict__ b,
+                              const float *__restrict__ d, float *__restrict__ c, float *__restrict__ x,
+                              long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float t = b ? a[i] - b[i] : a[i];
+    if (c) c[i] = t;
+    x[i] = d[i] * t;
+  }
+}
+
+__global__ void k_scatter_cast_f64(const float *__restrict__ src, const int64_t *__restrict__ idx, long long n,
+                                   double *__restrict__ dst) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[idx[i]] = (double)src[i];
+}
+
 } // namespace fe_gm
 
 extern "C" {
+
+int fe_gather_cast_f32(const double *src, const int64_t *idx, int64_t n, const float *scale, float *dst,
+                       void *stream) {
+  if (n < 0 || (n > 0 && (!src || !idx || !dst))) return fail(FE_ERR_ARG, "fe_gather_cast_f32: bad arguments");
+  if (n == 0) return FE_OK;
+  fe_gm::k_gather_cast_f32<<<grid_for(n, 256, sm_count_cached()), 256, 0, (cudaStream_t)stream>>>(src, idx, n, scale,
+                                                                                                  dst);
+  CUDA_TRY(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_sub_mul_f32(const float *a, const float *b, const float *d, float *c, float *x, int64_t n, void *stream) {
+  if (n < 0 || (n > 0 && (!a || !d || !x))) return fail(FE_ERR_ARG, "fe_sub_mul_f32: bad arguments");
+  if (n == 0) return FE_OK;
+  fe_gm::k_sub_mul_f32<<<grid_for(n, 256, sm_count_cached()), 256, 0, (cudaStream_t)stream>>>(a, b, d, c, x, n);
+  CUDA_TRY(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_scatter_cast_f64(const float *src, const int64_t *idx, int64_t n, double *dst, void *stream) {
+  if (n < 0 || (n > 0 && (!src || !idx || !dst))) return fail(FE_ERR_ARG, "fe_scatter_cast_f64: bad arguments");
+  if (n == 0) return FE_OK;
+  fe_gm::k_scatter_cast_f64<<<grid_for(n, 256, sm_count_cached()), 256, 0, (cudaStream_t)stream>>>(src, idx, n, dst);
+  CUDA_TRY(cudaGetLastError());
+  return FE_OK;
+}
 
 int64_t fe_gmres_cgs2_scratch(int64_t n, int kmax) {
   const int64_t nb = (n + fe_gm::CHUNK - 1) / fe_gm::CHUNK;

@@ -335,7 +335,12 @@ class SaddlePointSolver:
         s = float(q @ (B @ ((Bt @ q) / D)))
         self.sigma = -1.0 if s > 0 else 1.0
         pdt = self.pdt
-        self.sinv = torch.as_tensor(self.sigma * self.schur_scale / self.mass, device=self.dev).to(pdt)
+        npdt = np.float32 if pdt == torch.float32 else np.float64
+        # host-side casts and uninitialised buffers: no torch FP32 kernel runs
+        # (their first use in a process costs seconds on this machine)
+        dv = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=npdt), device=self.dev)
+        buf = lambda m: torch.empty(m, dtype=pdt, device=self.dev)
+        self.sinv = dv(self.sigma * self.schur_scale / self.mass)
         levels = []
         comp = self.comp_v
         while A.shape[0] > self.coarse_size and len(levels) < self.max_levels:
@@ -349,12 +354,9 @@ class SaddlePointSolver:
             cc[agg] = comp
             levels.append({"A": _DevCSR(torch, A, self.dev, pdt), "P": _DevCSR(torch, Pm, self.dev, pdt),
                            "R": _DevCSR(torch, Pm.T.tocsr(), self.dev, pdt),
-                           "dinv": torch.as_tensor(1.0 / Dl, device=self.dev).to(pdt), "om": 1.0 / lam, "n": n,
-                           "nc": na, "dinv_om": torch.as_tensor((1.0 / lam) / Dl, device=self.dev).to(pdt),
-                           "x": torch.zeros(n, dtype=pdt, device=self.dev),
-                           "x2": torch.zeros(n, dtype=pdt, device=self.dev),
-                           "t": torch.zeros(n, dtype=pdt, device=self.dev),
-                           "bc": torch.zeros(na, dtype=pdt, device=self.dev)})
+                           "dinv": dv(1.0 / Dl), "om": 1.0 / lam, "n": n, "nc": na,
+                           "dinv_om": dv((1.0 / lam) / Dl),
+                           "x": buf(n), "x2": buf(n), "t": buf(n), "bc": buf(na)})
             A, comp = Ac, cc
         # the coarsest operator's inverse on the host (<= coarse_size unknowns;
         # numpy), applied on the device as a dense matrix in CSR form by the
@@ -362,18 +364,25 @@ class SaddlePointSolver:
         # depend on the stream or the library workspace it runs with
         inv = np.linalg.inv(A.toarray())
         self.coarse_inv = _DevCSR(torch, sps.csr_matrix(inv), self.dev, pdt)
-        self.coarse_out = torch.zeros(inv.shape[0], dtype=pdt, device=self.dev)
+        self.coarse_out = buf(inv.shape[0])
         self.levels = levels
         self._graph = None                          # recaptured for the new hierarchy
         self.Bt = _DevCSR(torch, Bt, self.dev, pdt)
+        # the FP32 preconditioner's vectors
+        nv, npre = self.vel.size, self.pre.size
+        self._rv, self._p, self._tv, self._b0 = buf(nv), buf(npre), buf(nv), buf(nv)
+        self._x0 = buf(nv)
+        self._ones = dv(np.ones(nv))
+        self._z = torch.zeros(self.P.n_dof, dtype=torch.float64, device=self.dev)
         self.sizes = [lv["n"] for lv in levels] + [A.shape[0]]
 
     # -- application -------------------------------------------------------
-    def _vcycle(self, lvl: int, b):
+    def _vcycle(self, lvl: int, b, first_done: bool = False):
         """One V-cycle on level lvl for right-hand side b: nu damped-Jacobi
         steps from zero, the coarse-grid correction, nu steps; every update
         one fused pass over its matrix (fe_csr_update).  Returns one of the
-        level's iterate buffers (valid until the next cycle on this level)."""
+        level's iterate buffers (valid until the next cycle on this level).
+        first_done: the first step from zero is already in the level's x."""
         torch = self.torch
         st = torch.cuda.current_stream().cuda_stream
         if lvl == len(self.levels):
@@ -382,7 +391,14 @@ class SaddlePointSolver:
         L = self.levels[lvl]
         A, dinv, om = L["A"], L["dinv"], L["om"]
         x, y = L["x"], L["x2"]
-        torch.mul(b, L["dinv_om"], out=x)                     # the first step from zero
+        if first_done:
+            pass
+        elif self.pdt == torch.float32:                       # the first step from zero
+            vp = ctypes.c_void_p
+            N.check(N.load().fe_sub_mul_f32(vp(b.data_ptr()), None, vp(L["dinv_om"].data_ptr()), None,
+                                            vp(x.data_ptr()), L["n"], vp(st)))
+        else:
+            torch.mul(b, L["dinv_om"], out=x)
         for _ in range(self.nu - 1):
             A.update(x, b, x, dinv, om, y, st)
             x, y = y, x
@@ -430,6 +446,33 @@ class SaddlePointSolver:
         preconditioner's precision; z in FP64."""
         torch = self.torch
         st = torch.cuda.current_stream().cuda_stream
+        if self.pdt == torch.float32:
+            # the library's kernels only (gather-cast, subtract-scale,
+            # scatter-cast): fixed buffers, no torch FP32 kernel
+            L, vp = N.load(), ctypes.c_void_p
+            nv, npre = self.vel.size, self.pre.size
+            r = r.contiguous()
+            N.check(L.fe_gather_cast_f32(vp(r.data_ptr()), vp(self.vel_t.data_ptr()), nv, None,
+                                         vp(self._rv.data_ptr()), vp(st)))
+            N.check(L.fe_gather_cast_f32(vp(r.data_ptr()), vp(self.pre_t.data_ptr()), npre,
+                                         vp(self.sinv.data_ptr()), vp(self._p.data_ptr()), vp(st)))
+            self.Bt.mv(self._p, self._tv, st)
+            if self.levels:
+                L0 = self.levels[0]
+                N.check(L.fe_sub_mul_f32(vp(self._rv.data_ptr()), vp(self._tv.data_ptr()),
+                                         vp(L0["dinv_om"].data_ptr()), vp(self._b0.data_ptr()),
+                                         vp(L0["x"].data_ptr()), nv, vp(st)))
+                u = self._vcycle(0, self._b0, first_done=True)
+            else:
+                N.check(L.fe_sub_mul_f32(vp(self._rv.data_ptr()), vp(self._tv.data_ptr()),
+                                         vp(self._ones.data_ptr()), vp(self._b0.data_ptr()),
+                                         vp(self._x0.data_ptr()), nv, vp(st)))
+                u = self._vcycle(0, self._b0)
+            N.check(L.fe_scatter_cast_f64(vp(u.data_ptr()), vp(self.vel_t.data_ptr()), nv,
+                                          vp(self._z.data_ptr()), vp(st)))
+            N.check(L.fe_scatter_cast_f64(vp(self._p.data_ptr()), vp(self.pre_t.data_ptr()), npre,
+                                          vp(self._z.data_ptr()), vp(st)))
+            return self._z
         rp_ = r.to(self.pdt)
         p = self.sinv * rp_.index_select(0, self.pre_t)
         tv = torch.empty(self.vel.size, dtype=self.pdt, device=self.dev)
@@ -444,7 +487,17 @@ class SaddlePointSolver:
     def refresh(self) -> None:
         """Take the finest velocity block (and Bt) from the current Jacobian;
         the coarse levels stay."""
-        vals = self.P.J_dev[:self.P.nnz].to(self.torch.float64)
+        torch = self.torch
+        vals = self.P.J_dev[:self.P.nnz].to(torch.float64)
+        if self.pdt == torch.float32:
+            L, vp = N.load(), ctypes.c_void_p
+            st = torch.cuda.current_stream().cuda_stream
+            vals = vals.contiguous()
+            pairs = ([(self.levels[0]["A"], self.map_a)] if self.levels else []) + [(self.Bt, self.map_b)]
+            for M, m in pairs:
+                N.check(L.fe_gather_cast_f32(vp(vals.data_ptr()), vp(m.data_ptr()), int(m.numel()), None,
+                                             vp(M.v.data_ptr()), vp(st)))
+            return
         if self.levels:
             self.levels[0]["A"].v.copy_(vals.index_select(0, self.map_a))
         self.Bt.v.copy_(vals.index_select(0, self.map_b))
