@@ -159,11 +159,19 @@ __global__ void k_gather_slots(const unsigned *__restrict__ cptr, const unsigned
     for (int u = 0; u < U; u++) {
       const long long i = s0 + u * nthr;
       b[u] = e[u] = 0;
-      sl[u] = -1;
-      if (i < nnz) {
-        sl[u] = LIST ? (long long)list[i] : i;
-        b[u] = cptr[sl[u]];
-        e[u] = cptr[sl[u] + 1];
+      if constexpr (LIST) {
+        sl[u] = -1;
+        if (i < nnz) {
+          sl[u] = (long long)list[i];
+          b[u] = cptr[sl[u]];
+          e[u] = cptr[sl[u] + 1];
+        }
+      } else {
+        sl[u] = i;
+        if (i < nnz) {
+          b[u] = cptr[i];
+          e[u] = cptr[i + 1];
+        }
       }
     }
     unsigned i0[U], i1[U];
@@ -180,10 +188,13 @@ __global__ void k_gather_slots(const unsigned *__restrict__ cptr, const unsigned
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      if (sl[u] < 0) continue;
+      if (LIST ? sl[u] < 0 : s0 + u * nthr >= nnz) continue;
       if (b[u] + 1 < e[u]) acc[u] += v1[u];
       for (unsigned k = b[u] + 2; k < e[u]; k++) acc[u] += jbuf[cidx[k]];
-      vals[sl[u]] = acc[u];
+      if constexpr (LIST)
+        vals[sl[u]] = acc[u];
+      else
+        vals[s0 + u * nthr] = acc[u];
     }
   }
 }
