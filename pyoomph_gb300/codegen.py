@@ -104,6 +104,51 @@ class _Printer(C99CodePrinter):
         return self._lit(3.141592653589793)
 
 
+class _DF64Printer(_Printer):
+    """C printer for double-float (``fe_df64``) arithmetic: every literal is
+    split into its binary32 pair at generation time (the binary64 value of
+    the FP64 code, to 48 bits), operations are + - * / and small integer
+    powers.  Anything else (libm calls, Gaussian sums) is refused: see
+    ``df64_residual_supported``."""
+
+    def _lit(self, v: float) -> str:
+        hi = float(np.float32(v))
+        lo = float(np.float32(v - hi))
+        return f"fe_df64({hi!r}f, {lo!r}f)"
+
+    def _print_Rational(self, e):
+        return self._lit(float(e.p) / float(e.q))
+
+    def _print_Pow(self, e):
+        x = e.args[1]
+        if x.is_Integer and int(x) in (2, 3, 4, -1, -2):
+            return super()._print_Pow(e)
+        raise NotImplementedError(f"no double-float form of {e}")
+
+    def _print_exp(self, e):
+        raise NotImplementedError("no double-float exp")
+
+    def _print_GaussianSum(self, e):
+        raise NotImplementedError("no double-float Gaussian sum")
+
+    def _print_Function(self, e):
+        raise NotImplementedError(f"no double-float {e.func}")
+
+
+def df64_residual_supported(pw: "Pointwise") -> bool:
+    """Whether the pointwise residual and derivatives are rational in the
+    fields, coordinates and parameters (+ - * / and integer powers between
+    -2 and 4): the forms a double-float residual can be generated for."""
+    ok = (sp.Add, sp.Mul, sp.Symbol, sp.Number, sp.Pow)
+    for e in list(pw.r_exprs) + [d for (_, _, d) in pw.d_entries]:
+        for s in sp.preorder_traversal(sp.sympify(e)):
+            if not isinstance(s, ok):
+                return False
+            if isinstance(s, sp.Pow) and not (s.args[1].is_Integer and int(s.args[1]) in (2, 3, 4, -1, -2)):
+                return False
+    return True
+
+
 # the BDF weights of the current step (time derivative at a node:
 # du/dt = w0 u + w1 u_{n-1} + w2 u_{n-2}), appended to the parameter array
 # of a transient problem (the timestepper weights of pyoomph's shape buffer,
@@ -195,9 +240,9 @@ def _symbol_names(pw: Pointwise, prefix: str = "") -> Dict[sp.Symbol, str]:
     return names
 
 
-def _emit(exprs, names, fp32: bool, outs, indent="  "):
-    real = "float" if fp32 else "double"
-    pr = _Printer(dict(names), fp32=fp32)
+def _emit(exprs, names, fp32: bool, outs, indent="  ", df64: bool = False):
+    real = "fe_df64" if df64 else "float" if fp32 else "double"
+    pr = _DF64Printer(dict(names)) if df64 else _Printer(dict(names), fp32=fp32)
     repl, reduced = sp.cse(exprs, symbols=sp.numbered_symbols("t_"), optimizations="basic")
     lines = []
     for s_, e in repl:
@@ -259,26 +304,44 @@ def dparam_source(pw: Pointwise) -> str:
     return "\n".join(lines)
 
 
-def pointwise_source(pw: Pointwise, jreal: str = "double") -> str:
+def pointwise_source(pw: Pointwise, jreal: str = "double", rdf: bool = False) -> str:
     """The generated device functions.
 
     ``fe_pointwise(U, Xq, P, r, D, flag)`` computes the residual coefficients
     r in FP64 and, when jreal is double, the derivatives D too (sharing the
     common subexpressions).  With jreal float, D comes from the separate
     single-precision ``fe_pointwise_jac(U, Xq, P, D)``: the Jacobian then
-    costs no FP64 instructions."""
+    costs no FP64 instructions.  With ``rdf`` (double-float residual) U and
+    r are ``fe_df64`` and the arithmetic runs on the FP32 pipes; D too when
+    jreal is double (the double-float Jacobian)."""
     names = _symbol_names(pw)
     nr = len(pw.r_exprs)
     nd = len(pw.d_entries)
-    hdr = ("__device__ __forceinline__ void fe_pointwise(const double* __restrict__ U, "
-           "const double* __restrict__ Xq, const double* __restrict__ P, double* __restrict__ r, "
-           "jreal* __restrict__ D, int flag, const double* __restrict__ gsT, const int* __restrict__ gsI) {")
-    lines = [hdr, "  (void)gsT; (void)gsI;"]
+    if rdf:
+        # parameters and coordinates converted once per call
+        names = {k_: v_.replace("P[", "Pd[").replace("Xq[", "Xd[") for k_, v_ in names.items()}
+        dt = "fe_df64" if jreal == "double" else "jreal"
+        hdr = ("__device__ __forceinline__ void fe_pointwise(const fe_df64* __restrict__ U, "
+               "const double* __restrict__ Xq, const double* __restrict__ P, fe_df64* __restrict__ r, "
+               f"{dt}* __restrict__ D, int flag, const double* __restrict__ gsT, const int* __restrict__ gsI) {{")
+        lines = [hdr, "  (void)gsT; (void)gsI; (void)Xq; (void)P; (void)D; (void)flag;",
+                 f"  fe_df64 Pd[{max(1, len(pw.params))}];",
+                 "  #pragma unroll",
+                 f"  for (int k = 0; k < {len(pw.params)}; ++k) Pd[k] = fe_df64(P[k]);",
+                 "  fe_df64 Xd[3];",
+                 "  #pragma unroll",
+                 "  for (int k = 0; k < 3; ++k) Xd[k] = fe_df64(Xq[k]);",
+                 "  (void)Pd; (void)Xd;"]
+    else:
+        hdr = ("__device__ __forceinline__ void fe_pointwise(const double* __restrict__ U, "
+               "const double* __restrict__ Xq, const double* __restrict__ P, double* __restrict__ r, "
+               "jreal* __restrict__ D, int flag, const double* __restrict__ gsT, const int* __restrict__ gsI) {")
+        lines = [hdr, "  (void)gsT; (void)gsI;"]
     mass = _mass_lines(pw, names, False) if pw.transient else []
     if jreal == "double" and nd:
         exprs = list(pw.r_exprs) + [d for (_, _, d) in pw.d_entries]
         outs = [f"r[{k}]" for k in range(nr)] + [f"D[{k}]" for k in range(nd)]
-        body = _emit(exprs, names, False, outs, "  ")
+        body = _emit(exprs, names, False, outs, "  ", df64=rdf)
         # D assignments only when flag: move them under the branch
         rl = [l for l in body if not l.strip().startswith("D[")]
         dl = [l for l in body if l.strip().startswith("D[")]
@@ -288,8 +351,9 @@ def pointwise_source(pw: Pointwise, jreal: str = "double") -> str:
         else:
             lines += ["  if (flag) {"] + ["  " + l for l in dl] + ["  }"]
     else:
-        lines += _emit(list(pw.r_exprs), names, False, [f"r[{k}]" for k in range(nr)], "  ")
+        lines += _emit(list(pw.r_exprs), names, False, [f"r[{k}]" for k in range(nr)], "  ", df64=rdf)
     lines.append("}")
+    names = _symbol_names(pw)
     # Hessian-vector product: D'(U; V) = sum_c dD/dU_c V_c, V the interpolated direction
     nc = 1 + pw.dim
     usyms, vsyms = [], []
@@ -316,13 +380,15 @@ def pointwise_source(pw: Pointwise, jreal: str = "double") -> str:
     lines.append("}")
     if jreal != "double":
         fl = _symbol_names(pw, prefix="f")
-        lines.append("__device__ __forceinline__ void fe_pointwise_jac(const double* __restrict__ U, "
+        ut = "fe_df64" if rdf else "double"
+        lines.append(f"__device__ __forceinline__ void fe_pointwise_jac(const {ut}* __restrict__ U, "
                      "const double* __restrict__ Xq, const double* __restrict__ P, float* __restrict__ D, int flag) {")
         lines.append("  (void)flag;")
         nc = 1 + pw.dim
         nu = len(pw.fields) * nc + (len(pw.fields) if pw.transient else 0)
         lines.append(f"  float fU[{max(1, nu)}]; float fXq[3]; float fP[{max(1, len(pw.params))}];")
-        lines.append(f"  #pragma unroll\n  for (int k = 0; k < {nu}; ++k) fU[k] = (float)U[k];")
+        # (a double-float value's high word is its nearest binary32)
+        lines.append(f"  #pragma unroll\n  for (int k = 0; k < {nu}; ++k) fU[k] = {'U[k].hi' if rdf else '(float)U[k]'};")
         lines.append("  fXq[0] = (float)Xq[0]; fXq[1] = (float)Xq[1]; fXq[2] = (float)Xq[2];")
         if pw.params:
             lines.append(f"  #pragma unroll\n  for (int k = 0; k < {len(pw.params)}; ++k) fP[k] = (float)P[k];")
@@ -417,7 +483,8 @@ def _launch_shape(et: ElementType, nloc: int, per_elem_bytes: int, table_bytes: 
 
 def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                     name: str = None, epb: int = None, affine: bool = False, jref: bool = None,
-                    gauss_sep: bool = False, tc: bool = None, min_blocks: int = None) -> KernelSpec:
+                    gauss_sep: bool = False, tc: bool = None, min_blocks: int = None,
+                    residual_precision: str = "f64") -> KernelSpec:
     """Fused element kernel for one element type and weak form.
 
     Thread phases (all in one launch, EPB elements per block):
@@ -446,6 +513,16 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     elements.  Nothing of size (knots x nodes x dim) is kept per element, so
     a block holds several times more elements (the Q2 hex element needs 27 x
     27 x 3 physical gradients otherwise).
+
+    With ``residual_precision="df64"`` (FP32 or double-float Jacobians of
+    steady forms whose pointwise terms are rational) the residual path runs
+    in double-float on the FP32 pipes: interpolation, pointwise residual,
+    pull-back and the contraction with the test functions; the geometry
+    stays FP64.  Nodal values are staged as differences from the element's
+    node 0, formed in FP64 (u = u_0 + sum_l (u_l - u_0) psi_l, grad u =
+    sum_l (u_l - u_0) grad psi_l by the partition of unity), so that the
+    48-bit significand rounds only the small differences: the cancellation
+    in the reference gradients does not amplify it.
     """
     dim, nn, nn1, nq = et.dim, et.nnode, et.nnode_c1, et.nq
     fields = pw.fields
@@ -461,6 +538,22 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     if jac_precision not in ("f64", "f32", "df64"):
         raise ValueError(f"unknown Jacobian precision {jac_precision!r}")
     df64 = jac_precision == "df64"
+    if residual_precision not in ("f64", "df64"):
+        raise ValueError(f"unknown residual precision {residual_precision!r}")
+    rdf = residual_precision == "df64"
+    if rdf:
+        if jac_precision == "f64":
+            raise ValueError("a double-float residual goes with an FP32 or double-float Jacobian")
+        if pw.transient:
+            raise ValueError("the double-float residual is generated for steady forms")
+        if not df64_residual_supported(pw):
+            raise ValueError("the double-float residual needs pointwise terms rational in the fields "
+                             "(+ - * / and integer powers)")
+        if not et.c1_index or et.c1_index[0] != 0:
+            raise ValueError("the double-float residual stages values relative to node 0, a C1 node")
+        if jref is False:
+            raise ValueError("the double-float residual goes with the reference-coordinate Jacobian (jref)")
+        jref = True
     # jreal: phase A (pointwise D and its pull-back); jacc: phase B (the
     # contraction that builds J) -- for df64 D is formed in FP64 and the
     # contraction runs in double-float on the FP32 pipes (fe_df64.cuh)
@@ -503,6 +596,10 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     tabt = jacc if tab_copy else "double"
     tabf = (nq * nn * (1 + dim) + nq * nn1 * (1 + dim)) if tab_copy else 0
     table_bytes += ((tabf * (8 if df64 else 4) + 15) // 16) * 16
+    # double-float residual with an FP32 Jacobian: double-float tables too
+    rtab = rdf and not df64
+    if rtab:
+        table_bytes += tabf * 8
     geo_doubles = (dim * dim + 1) if affine else 0
     # separable Gaussian source (axis-aligned affine Q2 elements, the caller
     # checks the alignment): the element's per-axis factors in shared memory
@@ -532,7 +629,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     # at the 27 knots) and of the residual's test-function contraction of the
     # Q2 hex: one axis at a time, 729 multiply-adds each instead of 27 x 27 x 4
     sfi = bool(jref and et.name == "Q2_HEX" and nf == 1 and spaces[0] == "C2"
-               and list(layout.loc_of[0]) == list(range(nn)))
+               and list(layout.loc_of[0]) == list(range(nn)) and not rdf)
     # transient forms: nodal du/dt = w0 u + w1 u_{n-1} + w2 u_{n-2} staged per
     # element beside the values, interpolated as one more input per field
     transient = pw.transient
@@ -580,10 +677,11 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     if name is None:
         h = hashlib.sha1((et.name + jac_precision + str(affine) + str(epb) + str(jref) + str(sumfac) + str(gsep) +
                           ("tc" if use_tc else "") + (f"mb{int(min_blocks)}" if min_blocks else "") +
+                          ("rdf" if rdf else "") +
                           str(sfi) + (str(pw.m_entries) if transient else "") +
                           str(pw.r_exprs) +
                           str(pw.d_entries)).encode()).hexdigest()[:10]
-        name = f"fe_elem_{et.name.lower()}_{jac_precision}{'_aff' if affine else ''}_{h}"
+        name = f"fe_elem_{et.name.lower()}_{jac_precision}{'_rdf' if rdf else ''}{'_aff' if affine else ''}_{h}"
 
     nsub = [nn if s_ == "C2" else nn1 for s_ in spaces]
     loc_of_flat = [layout.loc_of[f][k] for f in range(nf) for k in range(nsub[f])]
@@ -615,7 +713,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         from .spaces import _G3_1D, _lag3
         Mv = [repr(float(_lag3(g)[c][i])) for c in range(2) for g in _G3_1D for i in range(3)]
         w(f"__constant__ double c_M[18] = {{{', '.join(Mv)}}};")
-    w(pointwise_source(pw, jreal))
+    w(pointwise_source(pw, jreal, rdf=rdf))
     w(dparam_source(pw))
     lb = f"FE_NT, {int(min_blocks)}" if min_blocks else "FE_NT"
     w(f'extern "C" __global__ void __launch_bounds__({lb}) {name}(const FeElemArgs a) {{')
@@ -637,6 +735,11 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w(f"  double* sGe = sG + FE_EPB * {geo_doubles};  // separable Gaussian factors, {gsd} per element")
     w(f"  jacc* sD = reinterpret_cast<jacc*>(sGe + FE_EPB * {gsd});")
     w("  (void)sGe;")
+    if rdf:
+        # double-float residual: values staged as differences from node 0
+        # (node 0: its value), residual coefficients per knot in double-float
+        w("  fe_df64* sUr = reinterpret_cast<fe_df64*>(sU);")
+        w("  fe_df64* sRhr = reinterpret_cast<fe_df64*>(sRh);")
     if jref:
         w("  jacc* sEnd = sD + FE_EPB * FE_NQ * FE_NDNZH;")
         if tab_copy:
@@ -645,6 +748,14 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w("  jacc* sDps2j = sPsi2j + FE_NQ * FE_NN;")
             w("  jacc* sPsi1j = sDps2j + FE_NQ * FE_NN * FE_DIM;")
             w("  jacc* sDps1j = sPsi1j + FE_NQ * FE_NN1;")
+            if rtab:
+                off = ((tabf * 4 + 15) // 16 * 16) // 4
+                w(f"  fe_df64* sPsi2r = reinterpret_cast<fe_df64*>(sPsi2j + {off});  // double-float tables (residual)")
+                w("  fe_df64* sDps2r = sPsi2r + FE_NQ * FE_NN;")
+                w("  fe_df64* sPsi1r = sDps2r + FE_NQ * FE_NN * FE_DIM;")
+                w("  fe_df64* sDps1r = sPsi1r + FE_NQ * FE_NN1;")
+            elif rdf:
+                w("  fe_df64* sPsi2r = sPsi2j; fe_df64* sDps2r = sDps2j; fe_df64* sPsi1r = sPsi1j; fe_df64* sDps1r = sDps1j;")
         else:
             w("  (void)sEnd;")
             w("  const double* sPsi2j = sPsi2; const double* sDps2j = sDps2;")
@@ -684,6 +795,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w(f"  for (int k = threadIdx.x; k < {table_doubles}; k += FE_NT) sW[k] = a.tables[k];")
     if tab_copy:
         w(f"  for (int k = threadIdx.x; k < {tabf}; k += FE_NT) sPsi2j[k] = (jacc)a.tables[FE_NQ + k];")
+    if rtab:
+        w(f"  for (int k = threadIdx.x; k < {tabf}; k += FE_NT) sPsi2r[k] = fe_df64(a.tables[FE_NQ + k]);")
     if sfi:
         # 1D Lagrange values M0[q][i] and derivatives M1[q][i] at the 1D Gauss points
         w("  __shared__ double sM[18];")
@@ -705,8 +818,16 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     w("    FE_CHECK_NODE(node, e0 + el, a);")
     w("    #pragma unroll")
     w("    for (int d = 0; d < FE_DIM; ++d) sX[k * FE_DIM + d] = a.x[(long long)node * FE_DIM + d];")
-    w("    #pragma unroll")
-    w("    for (int v = 0; v < FE_NVAL; ++v) sU[k * FE_NVAL + v] = a.values[(long long)node * a.nval + v];")
+    if rdf:
+        w("    { int node0 = a.conn[(e0 + el) * FE_NN];")
+        w("      FE_CHECK_NODE(node0, e0 + el, a);")
+        w("      #pragma unroll")
+        w("      for (int v = 0; v < FE_NVAL; ++v) {")
+        w("        const double u = a.values[(long long)node * a.nval + v];")
+        w("        sUr[k * FE_NVAL + v] = fe_df64(l == 0 ? u : u - a.values[(long long)node0 * a.nval + v]); } }")
+    else:
+        w("    #pragma unroll")
+        w("    for (int v = 0; v < FE_NVAL; ++v) sU[k * FE_NVAL + v] = a.values[(long long)node * a.nval + v];")
     w("    if (flag == 4)")
     w("      for (int v = 0; v < FE_NVAL; ++v) sY[k * FE_NVAL + v] = a.dir[(long long)node * a.nval + v];")
     if transient:
@@ -865,7 +986,61 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w(f"{ind}    {dst}[{base} + 1 + i] = s; }}")
             w(f"{ind}}}")
 
-    if sfi:
+    def interp_r():
+        # u = u_0 + sum_{l>0} d_l psi_l, grad u = sum_{l>0} d_l grad psi_l
+        # (d_l = u_l - u_0 as staged), renormalised every 4 nodes
+        w("    fe_df64 gr[FE_DIM][FE_DIM];")
+        w("    #pragma unroll")
+        w("    for (int b = 0; b < FE_DIM; ++b)")
+        w("      #pragma unroll")
+        w("      for (int i = 0; i < FE_DIM; ++i) gr[b][i] = fe_df64(g[b][i]);")
+        w("    fe_df64 U[FE_NTC];")
+        for f, (fname, fsp) in enumerate(fields):
+            base = f * nc
+            w(f"    {{ fe_df64 v = sUr[(el * FE_NN) * FE_NVAL + {f}];")
+            w("      fe_df64 gs[FE_DIM];")
+            w("      #pragma unroll")
+            w("      for (int b = 0; b < FE_DIM; ++b) gs[b] = fe_df64(0.0f, 0.0f);")
+            if fsp == "C2":
+                w("      #pragma unroll")
+                w("      for (int l = 1; l < FE_NN; ++l) {")
+                w(f"        const fe_df64 u = sUr[(el * FE_NN + l) * FE_NVAL + {f}];")
+                w("        fe_mac(v, u, sPsi2r[q * FE_NN + l]);")
+                w("        #pragma unroll")
+                w("        for (int b = 0; b < FE_DIM; ++b) fe_mac(gs[b], u, sDps2r[(q * FE_NN + l) * FE_DIM + b]);")
+                w("        if ((l & 3) == 0) {")
+                w("          v = fe_norm(v);")
+                w("          #pragma unroll")
+                w("          for (int b = 0; b < FE_DIM; ++b) gs[b] = fe_norm(gs[b]); }")
+                w("      }")
+            else:
+                w("      const fe_df64* ps1 = sPsi1r + q * FE_NN1;")
+                w("      const fe_df64* dp1 = sDps1r + q * FE_NN1 * FE_DIM;")
+                for l, node in enumerate(et.c1_index):
+                    if l == 0:
+                        continue
+                    w(f"      {{ const fe_df64 u = sUr[(el * FE_NN + {node}) * FE_NVAL + {f}];")
+                    w(f"        fe_mac(v, u, ps1[{l}]);")
+                    for b in range(dim):
+                        w(f"        fe_mac(gs[{b}], u, dp1[{l * dim + b}]);")
+                    if l % 4 == 0:
+                        w("        v = fe_norm(v);")
+                        for b in range(dim):
+                            w(f"        gs[{b}] = fe_norm(gs[{b}]);")
+                    w("      }")
+            w(f"      U[{base}] = fe_norm(v);")
+            w("      #pragma unroll")
+            w("      for (int b = 0; b < FE_DIM; ++b) gs[b] = fe_norm(gs[b]);")
+            w("      #pragma unroll")
+            w("      for (int i = 0; i < FE_DIM; ++i) { fe_df64 s_ = fe_df64(0.0f, 0.0f);")
+            w("        #pragma unroll")
+            w("        for (int b = 0; b < FE_DIM; ++b) fe_mac(s_, gr[b][i], gs[b]);")
+            w(f"        U[{base} + 1 + i] = fe_norm(s_); }}")
+            w("    }")
+
+    if rdf:
+        interp_r()
+    elif sfi:
         w(f"    double U[{nu if transient else 'FE_NTC'}];")
         w(f"    {{ const double* C = sIc + el * {SC} + q;")
         w("      const double gs[3] = {C[27], C[54], C[81]};")
@@ -885,8 +1060,32 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     else:
         interp("U", "sU", "    ", with_dt=True)
     w("    const double* Pe = a.params + (a.replica_elems > 0 ? ((e0 + el) / a.replica_elems) * a.params_stride : 0);")
-    w("    double r[FE_NTC]; jreal D[FE_NDNZ];")
-    if gsep:
+    if rdf:
+        w(f"    fe_df64 r[FE_NTC]; {'fe_df64' if df64 else 'jreal'} D[FE_NDNZ];")
+        w("    if (dpar) {")
+        w("      double Ud[FE_NTC], rt[FE_NTC];")
+        w("      #pragma unroll")
+        w("      for (int k = 0; k < FE_NTC; ++k) Ud[k] = fe_widen(U[k]);")
+        w("      fe_pointwise_dparam(Ud, Xq, Pe, rt, a.aux);")
+        w("      #pragma unroll")
+        w("      for (int k = 0; k < FE_NTC; ++k) r[k] = fe_df64(rt[k]);")
+        w("    } else fe_pointwise(U, Xq, Pe, r, D, flag, nullptr, nullptr);")
+        w("    fe_df64* rh = sRhr + (el * FE_NQ + q) * FE_NTC;")
+        w("    const fe_df64 wqr = fe_df64(wq);")
+        w("    #pragma unroll")
+        w("    for (int f = 0; f < FE_NF; ++f) {")
+        w("      rh[f * (1 + FE_DIM)] = wqr * r[f * (1 + FE_DIM)];")
+        w("      #pragma unroll")
+        w("      for (int b = 0; b < FE_DIM; ++b) { fe_df64 s_ = fe_df64(0.0f, 0.0f);")
+        w("        #pragma unroll")
+        w("        for (int i = 0; i < FE_DIM; ++i) fe_mac(s_, gr[b][i], r[f * (1 + FE_DIM) + 1 + i]);")
+        w("        rh[f * (1 + FE_DIM) + 1 + b] = wqr * fe_norm(s_); }")
+        w("    }")
+    else:
+        w("    double r[FE_NTC]; jreal D[FE_NDNZ];")
+    if rdf:
+        pass
+    elif gsep:
         w("    int qI[FE_DIM];")
         w("    { int qq = q;")
         w("      #pragma unroll")
@@ -896,22 +1095,35 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     else:
         w("    if (dpar) fe_pointwise_dparam(U, Xq, Pe, r, a.aux);")
         w("    else fe_pointwise(U, Xq, Pe, r, D, flag, nullptr, nullptr);")
-    w("    double* rh = sRh + (el * FE_NQ + q) * FE_NTC;")
-    w("    #pragma unroll")
-    w("    for (int f = 0; f < FE_NF; ++f) {")
-    w("      rh[f * (1 + FE_DIM)] = wq * r[f * (1 + FE_DIM)];")
-    w("      #pragma unroll")
-    w("      for (int b = 0; b < FE_DIM; ++b) { double s = 0.0;")
-    w("        #pragma unroll")
-    w("        for (int i = 0; i < FE_DIM; ++i) s += g[b][i] * r[f * (1 + FE_DIM) + 1 + i];")
-    w("        rh[f * (1 + FE_DIM) + 1 + b] = wq * s; }")
-    w("    }")
+    if not rdf:
+        w("    double* rh = sRh + (el * FE_NQ + q) * FE_NTC;")
+        w("    #pragma unroll")
+        w("    for (int f = 0; f < FE_NF; ++f) {")
+        w("      rh[f * (1 + FE_DIM)] = wq * r[f * (1 + FE_DIM)];")
+        w("      #pragma unroll")
+        w("      for (int b = 0; b < FE_DIM; ++b) { double s = 0.0;")
+        w("        #pragma unroll")
+        w("        for (int i = 0; i < FE_DIM; ++i) s += g[b][i] * r[f * (1 + FE_DIM) + 1 + i];")
+        w("        rh[f * (1 + FE_DIM) + 1 + b] = wq * s; }")
+        w("    }")
     w("    if (flag) {")
     if jreal == "float":
         w("      if (flag != 4) fe_pointwise_jac(U, Xq, Pe, D, flag);")
     w("      if (flag == 4) {")
     interp("V", "sY", "        ")
-    w("        fe_pointwise_hvp(U, V, Xq, Pe, D);")
+    if rdf:
+        w("        double Ud[FE_NTC];")
+        w("        #pragma unroll")
+        w("        for (int k = 0; k < FE_NTC; ++k) Ud[k] = fe_widen(U[k]);")
+        if df64:
+            w("        double Dh[FE_NDNZ];")
+            w("        fe_pointwise_hvp(Ud, V, Xq, Pe, Dh);")
+            w("        #pragma unroll")
+            w("        for (int k = 0; k < FE_NDNZ; ++k) D[k] = fe_df64(Dh[k]);")
+        else:
+            w("        fe_pointwise_hvp(Ud, V, Xq, Pe, D);")
+    else:
+        w("        fe_pointwise_hvp(U, V, Xq, Pe, D);")
     w("      }")
     w("      const jreal wj = (jreal)wq;")
     if jref:
@@ -1080,7 +1292,13 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("    (void)t1;")
     w("    const double* tpsi = t1 ? sPsi1 : sPsi2;")
     w("    const double* tdps = t1 ? sDps1 : sDps2;")
-    w("    double Racc = 0.0;")
+    if rdf:
+        w("    const fe_df64* tpsir = t1 ? sPsi1r : sPsi2r;")
+        w("    const fe_df64* tdpsr = t1 ? sDps1r : sDps2r;")
+        w("    (void)tpsi; (void)tdps;")
+        w("    fe_df64 Racc = fe_df64(0.0f, 0.0f);")
+    else:
+        w("    double Racc = 0.0;")
     w("    jacc Jr[FE_NLOC];")
     w("    #pragma unroll")
     w("    for (int k = 0; k < FE_NLOC; ++k) Jr[k] = (jacc)0;")
@@ -1088,7 +1306,13 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("    (void)Racc; (void)tpsi; (void)tdps;")
     # (sum-factorised Jacobian and residual: nothing is left per knot here)
     w(f"    for (int q = 0; q < {'0' if (sfi and sumfac) else 'FE_NQ'}; ++q) {{")
-    if not sfi:
+    if rdf:
+        w("      const fe_df64* rh = sRhr + (el * FE_NQ + q) * FE_NTC + tf * (1 + FE_DIM);")
+        w("      fe_mac(Racc, rh[0], tpsir[q * tn + lt]);")
+        w("      #pragma unroll")
+        w("      for (int b = 0; b < FE_DIM; ++b) fe_mac(Racc, rh[1 + b], tdpsr[(q * tn + lt) * FE_DIM + b]);")
+        w("      Racc = fe_norm(Racc);")
+    elif not sfi:
         w("      const double* rh = sRh + (el * FE_NQ + q) * FE_NTC + tf * (1 + FE_DIM);")
         w("      const double pv = tpsi[q * tn + lt];")
         w("      double racc = rh[0] * pv;")
@@ -1199,7 +1423,9 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("      }")
     w("    }")
     w("    const long long row = (e0 + el) * FE_NLOC + i;")
-    if not sfi:
+    if rdf:
+        w("    a.rbuf[row] = fe_widen(Racc);")
+    elif not sfi:
         w("    a.rbuf[row] = Racc;")
     w("    if (flag && !" + ("true" if use_tc else "false") + ") {")
     w("      jstore* jb = reinterpret_cast<jstore*>(a.jbuf) + row * FE_NLOC;")

@@ -94,6 +94,20 @@ __device__ __forceinline__ fe_df64 &operator+=(fe_df64 &a, fe_df64 b) {
   return a;
 }
 
+__device__ __forceinline__ fe_df64 operator-(fe_df64 a) { return fe_df64(-a.hi, -a.lo); }
+__device__ __forceinline__ fe_df64 operator-(fe_df64 a, fe_df64 b) { return a + (-b); }
+
+// a / b: the binary32 quotient of the high parts, corrected once by the
+// remainder a - q1 b formed in df64 (Dekker 1971, the one-correction
+// double-double division of Hida, Li & Bailey 2001); ~2^-44 relative
+__device__ __forceinline__ fe_df64 operator/(fe_df64 a, fe_df64 b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const fe_df64 r = a - fe_df64(q1, 0.0f) * b;
+  const float q2 = __fdiv_rn(r.hi, b.hi);
+  const float h = __fadd_rn(q1, q2);
+  return fe_df64(h, __fsub_rn(q2, __fsub_rn(h, q1)));
+}
+
 // acc += b * c as a compensated dot-product step (Ogita, Rump & Oishi 2005,
 // "Accurate sum and dot product", algorithm Dot2, with df64 operands): the
 // exact two-product of the high parts and the cross terms form the product's

@@ -252,6 +252,10 @@ class Problem:
         # "fp64"; "fp32": FP32 Jacobian, FP64 residual; "df64": FP64 Jacobian
         # values contracted in double-float (~2^-48) on the FP32 pipes
         self.jacobian_precision = "fp64"
+        # "fp64"; "df64": the residual path (interpolation, pointwise
+        # residual, test-function contraction) in double-float on the FP32
+        # pipes, for FP32 and df64 Jacobians of steady rational forms
+        self.residual_precision = "fp64"
         self.elems_per_block: Optional[int] = None
         # "auto": detect affine elements (constant geometry per element) on the host
         self.geometry = "auto"
@@ -415,6 +419,10 @@ class Problem:
             kprec = "df64"   # FP64 storage; contraction in double-float on the FP32 pipes
         else:
             raise ValueError(f"jacobian_precision must be fp64, fp32 or df64, not {jp!r}")
+        rp = self.residual_precision
+        if rp not in ("fp64", "f64", "double", "df64"):
+            raise ValueError(f"residual_precision must be fp64 or df64, not {rp!r}")
+        rprec = "df64" if rp == "df64" else "f64"
         prec = "f32" if kprec == "f32" else "f64"   # storage of the Jacobian values
         self._prec = prec
         self._kprec = kprec
@@ -426,14 +434,14 @@ class Problem:
         # geometry kind only -- not on the mesh size: cache it per process
         gsep = bool(self.separable_source and self.affine and mesh_is_axis_aligned(mesh))
         key = (mesh.etype.name, tuple(fields), str(integrand), tuple(used), kprec, self.affine, gsep,
-               self.is_transient, self.tensor_cores, self.min_blocks_per_sm, self.elems_per_block,
+               self.is_transient, self.tensor_cores, self.min_blocks_per_sm, rprec, self.elems_per_block,
                self.jacobian_reference)
         ks = _KERNEL_CACHE.get(key)
         if ks is None:
             pw = differentiate(fields, mesh.dim, integrand, used)
             ks = generate_kernel(mesh.etype, pw, kprec, epb=self.elems_per_block, affine=self.affine,
                                  jref=self.jacobian_reference, gauss_sep=gsep, tc=self.tensor_cores,
-                                 min_blocks=self.min_blocks_per_sm)
+                                 min_blocks=self.min_blocks_per_sm, residual_precision=rprec)
             _KERNEL_CACHE[key] = ks
         if self.elems_per_block is None and int(self.replicas) == 1:
             # balance the waves: with W = ceil(E / (SMs x EPB)) waves of one
@@ -454,7 +462,8 @@ class Problem:
                 if ks2 is None:
                     ks2 = generate_kernel(mesh.etype, differentiate(fields, mesh.dim, integrand, used), kprec,
                                           epb=epb, affine=self.affine, jref=self.jacobian_reference,
-                                          gauss_sep=gsep, tc=self.tensor_cores, min_blocks=self.min_blocks_per_sm)
+                                          gauss_sep=gsep, tc=self.tensor_cores, min_blocks=self.min_blocks_per_sm,
+                                          residual_precision=rprec)
                     _KERNEL_CACHE[key2] = ks2
                 ks = ks2
         self.kernel: KernelSpec = ks

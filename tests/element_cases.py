@@ -8,7 +8,8 @@ import oracle as O
 KINDS = ["poisson_q2", "poisson_p2", "ns_th", "nldiff_hex", "nldiff_q2"]
 
 
-def build(kind: str, geometry: str, prec: str, seed: int = 3, jref=None, transient: bool = False):
+def build(kind: str, geometry: str, prec: str, seed: int = 3, jref=None, transient: bool = False,
+          residual: str = "fp64"):
     from pyoomph_gb300 import workloads as W
     rng = np.random.default_rng(seed)
     T = W.wavy(0.03) if geometry == "general" else None
@@ -32,6 +33,7 @@ def build(kind: str, geometry: str, prec: str, seed: int = 3, jref=None, transie
         params = O.gaussian_params(gauss)
     P.geometry = geometry if geometry == "general" else "auto"
     P.jacobian_reference = jref
+    P.residual_precision = residual
     ks = P.lower()
     m = P.mesh
     values = P._values0.copy()

@@ -46,6 +46,7 @@ static inline double __longlong_as_double(long long u) { double d; std::memcpy(&
 static inline float __fadd_rn(float a, float b) { return a + b; }
 static inline float __fsub_rn(float a, float b) { return a - b; }
 static inline float __fmul_rn(float a, float b) { return a * b; }
+static inline float __fdiv_rn(float a, float b) { return a / b; }
 static inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }
 alignas(16) unsigned char fe_smem[232448];
 """

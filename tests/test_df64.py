@@ -5,8 +5,9 @@ the CPU emulator's intrinsic shims, against exact rational arithmetic:
   integer operations agree with the hardware conversions (numpy) on every
   class of value (normal, subnormal, zero, infinity, NaN, range edges);
 * splitting a double into hi + lo is exact in the binary32 normal range;
-* addition and multiplication keep relative errors near 2^-48 (bounded
-  here by 2^-45); the compensated multiply-add, renormalised every few
+* addition, subtraction and multiplication keep relative errors near
+  2^-48 (bounded here by 2^-45), division near 2^-44 (bounded by 2^-42);
+  the compensated multiply-add, renormalised every few
   terms as the generated contractions do, keeps the error of an n-term
   accumulation within (n m + 2) u^2 sum|terms| -- far below the 1e-12
   contract.
@@ -32,6 +33,10 @@ void t_add(float ah, float al, float bh, float bl, float *h, float *l) {
   fe_df64 r = fe_df64(ah, al) + fe_df64(bh, bl); *h = r.hi; *l = r.lo; }
 void t_mul(float ah, float al, float bh, float bl, float *h, float *l) {
   fe_df64 r = fe_df64(ah, al) * fe_df64(bh, bl); *h = r.hi; *l = r.lo; }
+void t_sub(float ah, float al, float bh, float bl, float *h, float *l) {
+  fe_df64 r = fe_df64(ah, al) - fe_df64(bh, bl); *h = r.hi; *l = r.lo; }
+void t_div(float ah, float al, float bh, float bl, float *h, float *l) {
+  fe_df64 r = fe_df64(ah, al) / fe_df64(bh, bl); *h = r.hi; *l = r.lo; }
 void t_dot(const float *ah, const float *al, const float *bh, const float *bl, int n, int m, float *h, float *l) {
   fe_df64 acc = (fe_df64)0;
   for (int i = 0; i < n; ++i) {
@@ -63,6 +68,8 @@ def lib():
     L.t_split.argtypes = [d, pf, pf]
     L.t_add.argtypes = [f, f, f, f, pf, pf]
     L.t_mul.argtypes = [f, f, f, f, pf, pf]
+    L.t_sub.argtypes = [f, f, f, f, pf, pf]
+    L.t_div.argtypes = [f, f, f, f, pf, pf]
     L.t_dot.argtypes = [pf, pf, pf, pf, ctypes.c_int, ctypes.c_int, pf, pf]
     return L
 
@@ -147,3 +154,16 @@ def test_add_mul_and_compensated_dot_error_bounds(lib):
         worst = max(worst, err)
         assert err <= bound
     assert worst <= 2.0 ** -44      # in practice an order below the bound
+
+
+def test_sub_and_div_error_bounds(lib):
+    rng = np.random.default_rng(5)
+    for _ in range(3000):
+        a, b = rng.standard_normal(2) * 10.0 ** rng.integers(-8, 8, 2)
+        ah, al = _split(lib, a)
+        bh, bl = _split(lib, b)
+        A, B = _val(ah, al), _val(bh, bl)
+        d = _val(*_pair(lib, lib.t_sub, ah, al, bh, bl))
+        q = _val(*_pair(lib, lib.t_div, ah, al, bh, bl))
+        assert abs(d - (A - B)) <= 2.0 ** -45 * (abs(A) + abs(B))
+        assert abs(q - A / B) <= 2.0 ** -42 * abs(A / B)

@@ -150,10 +150,15 @@ def test_newton_poisson_matches_oracle_solution():
     assert _relmax(P.get_dofs(), OP.dofs()) <= STOL
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32", "df64"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "df64", "fp32:df64", "df64:df64"])
 def test_newton_navier_stokes_matches_oracle_solution(prec):
+    """Newton on NS 8x8 to max|R| < 1e-10 with every Jacobian precision and,
+    after the colon, the double-float residual path: the same solution as
+    the oracle's FP64 Newton."""
     from pyoomph_gb300 import workloads as W
-    P = W.navier_stokes_problem(N=[8, 8], jacobian_precision=prec)
+    jp, _, rp = prec.partition(":")
+    P = W.navier_stokes_problem(N=[8, 8], jacobian_precision=jp)
+    P.residual_precision = rp or "fp64"
     P.newton_solver_tolerance = 1e-10
     P.max_newton_iterations = 20
     hist = P.solve()
@@ -286,3 +291,21 @@ def test_df64_element_level_parity(kind, geometry):
     Re, Je = P.element_buffers()
     assert C.relmax(Re, Rr) <= RTOL
     assert C.relmax(Je, Jr) <= RTOL
+
+
+@pytest.mark.parametrize("jac", ["fp32", "df64"])
+@pytest.mark.parametrize("geometry", ["affine", "general"])
+def test_df64_residual_element_level_parity(geometry, jac):
+    """The double-float residual path (interpolation, pointwise residual and
+    test-function contraction on the FP32 pipes) from the GPU element
+    buffers against the oracle's element residuals, within the FP64
+    contract; the Jacobian keeps its own precision's contract."""
+    import element_cases as C
+    P, ks, values, Rr, Jr = C.build("ns_th", geometry, jac, residual="df64")
+    assert "_rdf" in ks.name
+    P.initialise()
+    P.set_values(values)
+    P.get_jacobian()
+    Re, Je = P.element_buffers()
+    assert C.relmax(Re, Rr) <= RTOL
+    assert C.relmax(Je, Jr) <= (RTOL if jac == "df64" else 1e-5)
