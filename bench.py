@@ -170,11 +170,12 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_problem(workload: str, size: int, precision: str, epb=None):
+def make_problem(workload: str, size: int, precision: str, epb=None, residual: str = "fp64"):
     from pyoomph_gb300 import workloads as W
     if workload == "ns":
         P = W.navier_stokes_problem(N=size, jacobian_precision=precision)
         P.elems_per_block = epb
+        P.residual_precision = residual
         P.initialise()
         W.perturb_dofs(P, seed=0, sigma=1e-3)
     elif workload == "poisson":
@@ -190,7 +191,7 @@ def make_problem(workload: str, size: int, precision: str, epb=None):
     return P
 
 
-TUNED_EPB = {("ns", 256, "df64"): 32}
+TUNED_EPB = {("ns", 256, "df64"): 32, ("ns", 256, "df64:df64"): 32}
 
 # DRAM bytes (read + write) per launch of an element kernel, keyed by the
 # generated kernel's name (its source hash): dram__bytes_read.sum +
@@ -346,7 +347,7 @@ def run_gb300(args):
             P.check()
             nnz_zf = P.assemble_filtered(0.0)[2].size
             zf = {"ms_per_step": ms_zf, "nnz": int(nnz_zf), "structural_nnz": int(P.nnz),
-                  "launches_per_step": P.launch_count(True) + 5}
+                  "launches_per_step": P.launch_count(True, zero_filter=True)}
         # the same assembly replayed as one CUDA graph
         P.capture_assembly(with_jacobian=True)
         ms_graph = time_steps(torch, P.assemble_graph, args.steps, args.warmup)
@@ -354,6 +355,37 @@ def run_gb300(args):
         results[prec] = dict(P=P, ms=ms, stage_ms=stage_ms, ms_e2e=ms_e2e, clocks=cs.summary(), ms_graph=ms_graph, zf=zf,
                              ms_e2e_plain=ms_e2e_plain, e2e_chunks=chunks, e2e_by_chunks=e2e_by_chunks,
                              h2d=int(P.n_dof * 8), d2h=int(P.n_dof * 8 + P.nnz * P.J_dev.element_size()))
+    if args.workload == "ns":
+        # the FP32 and df64 Jacobians with the residual path in double-float
+        # (residual_precision="df64"): device steps, stages, graph replay and
+        # the host-buffer API at the chunk count chosen above for the same
+        # Jacobian precision
+        for prec in ("fp32:df64", "df64:df64"):
+            jp, _, rp = prec.partition(":")
+            P = make_problem(args.workload, args.size, jp, TUNED_EPB.get((args.workload, args.size, prec)), rp)
+            asm = lambda: P.assemble_device(with_jacobian=True)
+            ms = time_steps(torch, asm, args.steps, args.warmup)
+            if dist is not None:
+                t = torch.tensor([ms], device="cuda")
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                ms = float(t.item())
+            P.set_stage_timing(True)
+            for _ in range(max(3, min(args.steps, 10))):
+                asm()
+            stage_ms, calls = P.stage_times()
+            P.set_stage_timing(False)
+            xh = torch.from_numpy(P.get_dofs()).pin_memory()
+            Rh = torch.empty(P.n_dof, dtype=torch.float64).pin_memory()
+            Jh = torch.empty(P.nnz, dtype=P.J_dev.dtype).pin_memory()
+            chunks = results[jp]["e2e_chunks"]
+            ms_e2e = time_steps(torch, lambda: P.assemble_host(xh, Rh, Jh, True, chunks=chunks),
+                                max(3, args.steps), args.warmup)
+            P.capture_assembly(with_jacobian=True)
+            ms_graph = time_steps(torch, P.assemble_graph, args.steps, args.warmup)
+            P.check()
+            results[prec] = dict(P=P, ms=ms, stage_ms=stage_ms / max(calls, 1), ms_e2e=ms_e2e, ms_graph=ms_graph,
+                                 e2e_chunks=chunks, h2d=int(P.n_dof * 8),
+                                 d2h=int(P.n_dof * 8 + P.nnz * P.J_dev.element_size()))
     from pyoomph_gb300.codegen import estimate_flops
     peak64 = fp64_peak_tflops(torch)
     main = results["fp64"]
@@ -444,6 +476,26 @@ def run_gb300(args):
                 "h2d_bytes_per_step": rdf["h2d"], "d2h_bytes_per_step": rdf["d2h"], "ms_per_step": rdf["ms_e2e"]},
         "cuda_graph_ms_per_step": rdf["ms_graph"], "elems_per_block": Pdf.kernel.epb,
         "threads": Pdf.kernel.threads, "smem_bytes": Pdf.kernel.smem_bytes}
+    for jp, key in (("fp32", "fp32_jacobian"), ("df64", "df64_jacobian")):
+        r = results.get(f"{jp}:df64")
+        if r is None:
+            continue
+        kms = float(r["stage_ms"][1])
+        fr = estimate_flops(r["P"].kernel, r["P"].affine)
+        line[key]["df64_residual"] = {
+            "what": "the same Jacobian with the residual path (interpolation from FP64 differences to node 0, "
+                    "pointwise residual, pull-back, test-function contraction) in double-float on the FP32 "
+                    "pipes: Problem.residual_precision = 'df64'",
+            "value": n_elem * world / (r["ms"] / 1e3), "unit": "elements/s", "ms_per_step": r["ms"],
+            "element_kernel_ms": kms, "kernel": r["P"].kernel.name,
+            "stage_ms": {"dof_scatter": float(r["stage_ms"][0]), "element_kernel": kms,
+                         "residual_gather": float(r["stage_ms"][2]), "jacobian_gather": float(r["stage_ms"][3])},
+            "fp64_flops_per_element": fr["fp64"], "df64_residual_flops_per_element": fr["df64_residual"],
+            "e2e": {"value": n_elem * world / (r["ms_e2e"] / 1e3), "unit": "elements/s",
+                    "ms_per_step": r["ms_e2e"], "chunks_requested": r["e2e_chunks"],
+                    "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
+            "cuda_graph_ms_per_step": r["ms_graph"], "elems_per_block": r["P"].kernel.epb,
+            "threads": r["P"].kernel.threads, "smem_bytes": r["P"].kernel.smem_bytes}
     if args.workload in ("hex", "poisson") and world == 1:
         # a whole Newton solve on the device (assembly + BiCGStab on the resident
         # Jacobian), from the zero initial guess to max |R| < 1e-10; a small
@@ -545,6 +597,11 @@ def run_gb300(args):
         line["parity"] = parity_vs_oracle(args, results)
         if "fp32" in line["parity"]:
             line["fp32_jacobian"]["max_rel_jacobian_error_vs_fp64_oracle"] = line["parity"]["fp32"].get("max_rel_J")
+        for jp, key in (("fp32", "fp32_jacobian"), ("df64", "df64_jacobian")):
+            par = line["parity"].get(f"{jp}:df64")
+            if par and "df64_residual" in line[key]:
+                line[key]["df64_residual"]["max_rel_residual_error_vs_oracle"] = par.get("max_rel_R")
+                line[key]["df64_residual"]["max_rel_jacobian_error_vs_oracle"] = par.get("max_rel_J")
     if rank == 0 and world == 1 and args.workload == "ns" and not args.no_extras:
         # the other workloads of the survey, measured in this same run (after
         # the headline's timed regions): Poisson Q2 64^2, the Q2 hex 48^3
@@ -793,7 +850,7 @@ def parity_vs_oracle(args, results):
         out[prec] = {"pattern_bit_exact": bool(np.array_equal(J.indptr, rp) and np.array_equal(J.indices, ci)),
                      "max_rel_R": float(np.max(np.abs(R - R0)) / nR),
                      "max_rel_J": float(np.max(np.abs(J.data.astype(np.float64) - v)) / nJ),
-                     "tolerance_J": 1e-5 if prec == "fp32" else 1e-12}
+                     "tolerance_J": 1e-5 if prec.startswith("fp32") else 1e-12}
         del R, J
     return out
 

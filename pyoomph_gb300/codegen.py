@@ -431,6 +431,7 @@ class KernelSpec:
     gauss_sep: int = 0           # > 0: this many Gaussians of the source evaluated separably per element
     sum_fact_interp: bool = False  # interpolation and residual contraction sum-factorised (Q2 hex)
     min_blocks: int = 0          # > 0: registers bounded for this many resident blocks per SM
+    residual_precision: str = "f64"  # "df64": the residual path in double-float on the FP32 pipes
 
     @property
     def key(self) -> str:
@@ -1277,7 +1278,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                           threads=threads, smem_bytes=smem, jac_precision=jac_precision,
                           tables=et.packed_tables(), sumfac_blocks=0, gauss_sep=gs_n if gsep else 0,
                           sum_fact_interp=sfi, tc_pairs=[(ah, bh) for (_, _, ah, bh) in hat],
-                          min_blocks=int(min_blocks or 0))
+                          min_blocks=int(min_blocks or 0), residual_precision=residual_precision)
     w("  for (int p = threadIdx.x; p < nel * FE_NLOC; p += FE_NT) {")
     w("    int tf = 0, rel = p;")
     for f in range(nf - 1):
@@ -1444,7 +1445,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                       tables=et.packed_tables(), sumfac_blocks=len(hat) if sumfac else 0,
                       gauss_sep=gs_n if gsep else 0, sum_fact_interp=sfi,
                       tc_pairs=[(ah, bh) for (_, _, ah, bh) in hat] if use_tc else None,
-                      min_blocks=int(min_blocks or 0))
+                      min_blocks=int(min_blocks or 0), residual_precision=residual_precision)
 
 
 def _jacc_update(terms, acc: str, jacc: str) -> str:
@@ -1468,7 +1469,9 @@ def estimate_flops(ks: KernelSpec, affine: bool) -> Dict[str, float]:
     interpolation, pointwise residual, residual contraction; plus the
     Jacobian when it is FP64, its D and pull-back when it is df64), ``jac``
     (the Jacobian-only work) and, for df64, ``df64`` (the contraction done in
-    double-float)."""
+    double-float).  With the double-float residual, ``df64_residual`` holds
+    the residual path's flops (done in double-float, counted as the FP64
+    flops they replace) and ``fp64`` the geometry only."""
     et, pw, lay = ks.et, ks.pointwise, ks.layout
     D, NN, N1, NQ = et.dim, et.nnode, et.nnode_c1, et.nq
     nc = 1 + D
@@ -1526,6 +1529,13 @@ def estimate_flops(ks: KernelSpec, affine: bool) -> Dict[str, float]:
                "tensor_issued": float(3 * 2 * 128 // 4 * 32 * (-(-(NQ * nact) // 8) * 8))}
         return out
     out = {"fp64": float(fp64), "jac": float(jac_a + jac_b)}
+    if ks.residual_precision == "df64":
+        geo_only = float(geo if affine else NQ * geo)
+        out["df64_residual"] = float(fp64) - geo_only
+        out["fp64"] = geo_only
+        if ks.jac_precision == "df64":
+            out["df64"] = float(jac_a + jac_b)
+        return out
     if ks.jac_precision == "f64":
         out["fp64"] += out["jac"]
     elif ks.jac_precision == "df64":

@@ -136,12 +136,32 @@ __global__ void k_scatter_dofs(const double *__restrict__ dofs, const int *__res
 // go, the rest after -- so a warp keeps U dependent chains in flight
 // instead of one; each slot still sums its contributions in order.
 // With `list`, slot list[i] for i < nnz instead of slot i (the rows one
-// chunk of the pipelined assembly completes).
-template <typename T, int U, bool LIST>
+// chunk of the pipelined assembly completes).  With ROWS, each thread first
+// sums its residual rows (grid-stride, row rows.list[i] when given) in the
+// order of k_gather_rows: R and J in one launch, the rows' dependent loads
+// overlapping the slots' instead of a launch of their own.
+struct GatherRows {
+  const unsigned *rptr, *ridx;
+  const double *rbuf;
+  double *R;
+  long long n;
+  const int *list;
+};
+
+template <typename T, int U, bool LIST, bool ROWS = false>
 __global__ void k_gather_slots(const unsigned *__restrict__ cptr, const unsigned *__restrict__ cidx,
                                const T *__restrict__ jbuf, T *__restrict__ vals, long long nnz,
-                               const int *__restrict__ list) {
+                               const int *__restrict__ list, GatherRows rows = GatherRows{}) {
   const long long nthr = (long long)gridDim.x * blockDim.x;
+  if constexpr (ROWS) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < rows.n; i += nthr) {
+      const long long r = rows.list ? (long long)rows.list[i] : i;
+      const unsigned b = rows.rptr[r], e = rows.rptr[r + 1];
+      double acc = 0.0;
+      for (unsigned k = b; k < e; k++) acc += rows.rbuf[rows.ridx[k]];
+      rows.R[r] = acc;
+    }
+  }
   if constexpr (U == 1) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nnz; i += nthr) {
       const long long s = LIST ? (long long)list[i] : i;
@@ -150,8 +170,7 @@ __global__ void k_gather_slots(const unsigned *__restrict__ cptr, const unsigned
       for (unsigned k = b + 1; k < e; k++) acc += jbuf[cidx[k]];
       vals[s] = acc;
     }
-    return;
-  }
+  } else
   for (long long s0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; s0 < nnz; s0 += U * nthr) {
     unsigned b[U], e[U];
     long long sl[U];
@@ -205,18 +224,34 @@ __global__ void k_gather_slots(const unsigned *__restrict__ cptr, const unsigned
 // threads
 int grid_for(long long n, int threads, int sms);
 
+template <typename T, bool ROWS>
+void launch_gather_slots_(const unsigned *cptr, const unsigned *cidx, const T *jbuf, T *vals, long long nnz, int sms,
+                          cudaStream_t st, const int *list, const GatherRows &rows) {
+  const bool big = sizeof(T) == 4 && nnz >= (1LL << 22);
+  long long work = big ? (nnz + 3) / 4 : nnz;
+  if (ROWS && rows.n > work) work = rows.n;
+  const int g = grid_for(work, 256, sms);
+  if (big && list)
+    k_gather_slots<T, 4, true, ROWS><<<g, 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list, rows);
+  else if (big)
+    k_gather_slots<T, 4, false, ROWS><<<g, 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list, rows);
+  else if (list)
+    k_gather_slots<T, 1, true, ROWS><<<g, 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list, rows);
+  else
+    k_gather_slots<T, 1, false, ROWS><<<g, 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list, rows);
+}
+
 template <typename T>
 void launch_gather_slots(const unsigned *cptr, const unsigned *cidx, const T *jbuf, T *vals, long long nnz, int sms,
                          cudaStream_t st, const int *list = nullptr) {
-  const bool big = sizeof(T) == 4 && nnz >= (1LL << 22);
-  if (big && list)
-    k_gather_slots<T, 4, true><<<grid_for((nnz + 3) / 4, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list);
-  else if (big)
-    k_gather_slots<T, 4, false><<<grid_for((nnz + 3) / 4, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list);
-  else if (list)
-    k_gather_slots<T, 1, true><<<grid_for(nnz, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list);
-  else
-    k_gather_slots<T, 1, false><<<grid_for(nnz, 256, sms), 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list);
+  launch_gather_slots_<T, false>(cptr, cidx, jbuf, vals, nnz, sms, st, list, GatherRows{});
+}
+
+// R rows and CSR slots in one launch (ROWS prologue of k_gather_slots)
+template <typename T>
+void launch_gather_rows_slots(const GatherRows &rows, const unsigned *cptr, const unsigned *cidx, const T *jbuf,
+                              T *vals, long long nnz, int sms, cudaStream_t st, const int *list = nullptr) {
+  launch_gather_slots_<T, true>(cptr, cidx, jbuf, vals, nnz, sms, st, list, rows);
 }
 
 // residual entry r = sum of its element contributions in element order
@@ -1965,9 +2000,11 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
     for (Domain &d : p->domains)
       if (d.tc && (rc = tc_domain(p, d, 0, d.n_elem, st))) return rc;
   if (p->timing) CUDA_TRY(cudaEventRecord(ev[2], st));
-  // the tile gather sums the residual in the Jacobian's launch
+  // the tile gather sums the residual in the Jacobian's launch, and so does
+  // the per-slot gather (a row prologue) where neither carries hang weights
   const bool rowg = want_j && p->nnz > 0 && !want_zf && tile_gather(p);
-  if (rowg) {
+  const bool fused_r = want_r && want_j && p->nnz > 0 && !want_zf && !rowg && !p->rw.p && !p->cw.p;
+  if (rowg || fused_r) {
   } else if (want_r && p->rw.p) {
     k_gather_rows_w<<<grid_for(p->n_dof, 256, sms), 256, 0, st>>>(p->rptr.as<unsigned>(), p->ridx.as<unsigned>(),
                                                                  p->rw.as<double>(), p->rbuf_all.as<double>(), R,
@@ -1997,6 +2034,16 @@ int fe_assemble(fe_problem_t *p, const double *dofs, double *R, void *J_vals, in
     rc = p->jac_prec == FE_JAC_F64 ? launch_tile_gather<double>(p, want_r ? R : nullptr, (double *)J_vals, st)
                                    : launch_tile_gather<float>(p, want_r ? R : nullptr, (float *)J_vals, st);
     if (rc) return rc;
+  } else if (fused_r) {
+    const GatherRows rows{p->rptr.as<unsigned>(), p->ridx.as<unsigned>(), p->rbuf_all.as<double>(), R, p->n_dof,
+                          nullptr};
+    if (p->jac_prec == FE_JAC_F64)
+      launch_gather_rows_slots<double>(rows, p->cptr.as<unsigned>(), p->cidx.as<unsigned>(),
+                                       p->jbuf_all.as<double>(), (double *)J_vals, p->nnz, sms, st);
+    else
+      launch_gather_rows_slots<float>(rows, p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->jbuf_all.as<float>(),
+                                      (float *)J_vals, p->nnz, sms, st);
+    CUDA_TRY(cudaGetLastError());
   } else if (want_j && p->nnz > 0) {
     if (p->jac_prec == FE_JAC_F64)
       launch_gather_slots<double>(p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->jbuf_all.as<double>(),
@@ -2221,13 +2268,26 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
     {
       const long long q0 = p->pipe_row_off[k], q1 = p->pipe_row_off[k + 1];
       const long long z0 = p->pipe_slot_off[k], z1 = p->pipe_slot_off[k + 1];
-      if (want_r && q1 > q0) {
+      const GatherRows rows{p->rptr.as<unsigned>(), p->ridx.as<unsigned>(), p->rbuf_all.as<double>(),
+                            p->pipe_R.as<double>(), q1 - q0, p->pipe_rowlist.as<int>() + q0};
+      if (want_r && want_j && q1 > q0 && z1 > z0) {
+        // R rows and J slots of the chunk in one launch
+        if (p->jac_prec == FE_JAC_F64)
+          launch_gather_rows_slots<double>(rows, p->cptr.as<unsigned>(), p->cidx.as<unsigned>(),
+                                           p->jbuf_all.as<double>(), p->pipe_J.as<double>(), z1 - z0, sms, st,
+                                           p->pipe_slotlist.as<int>() + z0);
+        else
+          launch_gather_rows_slots<float>(rows, p->cptr.as<unsigned>(), p->cidx.as<unsigned>(),
+                                          p->jbuf_all.as<float>(), p->pipe_J.as<float>(), z1 - z0, sms, st,
+                                          p->pipe_slotlist.as<int>() + z0);
+        CUDA_TRY(cudaGetLastError());
+      } else if (want_r && q1 > q0) {
         k_gather_rows<<<grid_for(q1 - q0, 256, sms), 256, 0, st>>>(
             p->rptr.as<unsigned>(), p->ridx.as<unsigned>(), p->rbuf_all.as<double>(), p->pipe_R.as<double>(),
             q1 - q0, p->pipe_rowlist.as<int>() + q0);
         CUDA_TRY(cudaGetLastError());
       }
-      if (want_j && z1 > z0) {
+      if (want_j && z1 > z0 && !(want_r && q1 > q0)) {
         if (p->jac_prec == FE_JAC_F64)
           launch_gather_slots<double>(p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->jbuf_all.as<double>(),
                                       p->pipe_J.as<double>(), z1 - z0, sms, st, p->pipe_slotlist.as<int>() + z0);
@@ -2587,8 +2647,10 @@ int fe_problem_launch_count(const fe_problem_t *p, int flags) {
   }
   const bool want_j = (flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_MASS | FE_ASSEMBLE_HVP)) && p->nnz > 0;
   const bool zf = flags & FE_ASSEMBLE_ZERO_FILTER;
-  // the tile gather sums the residual in the Jacobian's launch
-  if ((flags & (FE_ASSEMBLE_RESIDUAL | FE_ASSEMBLE_DPARAM)) && !(want_j && !zf && tile_gather(p))) n++;
+  // the tile gather and the per-slot gather without hang weights sum the
+  // residual in the Jacobian's launch
+  const bool r_in_j = want_j && !zf && (tile_gather(p) || (!p->rw.p && !p->cw.p));
+  if ((flags & (FE_ASSEMBLE_RESIDUAL | FE_ASSEMBLE_DPARAM)) && !r_in_j) n++;
   if (flags & (FE_ASSEMBLE_JACOBIAN | FE_ASSEMBLE_HVP))
     for (const Domain &d : p->domains)
       if (d.tc && d.n_elem) n++;

@@ -829,10 +829,14 @@ class Problem:
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
         N.check(N.load().fe_problem_graph_launch(self._h, ctypes.c_void_p(st)))
 
-    def launch_count(self, with_jacobian: bool = True) -> int:
+    def launch_count(self, with_jacobian: bool = True, zero_filter: bool = False) -> int:
+        """Kernel launches of one assembly from the dof vector (R, and J when
+        asked; ``zero_filter``: J in the reference's value-dependent pattern)."""
         flags = N.FE_ASSEMBLE_RESIDUAL | N.FE_ASSEMBLE_VALUES_FROM_DOFS
         if with_jacobian:
             flags |= N.FE_ASSEMBLE_JACOBIAN
+        if zero_filter:
+            flags |= N.FE_ASSEMBLE_ZERO_FILTER
         return N.load().fe_problem_launch_count(self._h, flags)
 
     def set_stage_timing(self, enable: bool) -> None:

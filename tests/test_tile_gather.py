@@ -96,8 +96,8 @@ def test_tile_gather_gives_the_bits_of_the_slot_gather(case, prec):
     (R0, J0), (R1, J1) = _assemble_both(P)
     assert _same_bits(R0, R1) and _same_bits(J0, J1)
     assert bool(np.isfinite(J0.double().cpu().numpy()).all())
-    # the residual rides in the Jacobian's launch
-    assert n_tiles == n_slots - (1 if LANES[case] else 0)
+    # the residual rides in the Jacobian's launch either way
+    assert n_tiles == n_slots
     # a residual-only assembly keeps its own gather and the same bits
     P.R_dev.fill_(float("nan"))
     P.assemble_device(False)
