@@ -499,6 +499,15 @@ int fe_problem_check(fe_problem_t *p);
 int fe_problem_set_timing(fe_problem_t *p, int enable);
 int fe_problem_stage_times(fe_problem_t *p, double *ms, int64_t *calls);
 
+/*
+ * Timeline of the last fe_assemble_pipelined call made with timing enabled:
+ * per chunk k, milliseconds from the call's start to the end of its element
+ * kernel (ms[3k]), of its gathers (ms[3k+1]) and of the copies of the rows
+ * it completes (ms[3k+2]).  Synchronises on those events; returns the
+ * number of chunks (0: no timed call), FE_ERR_ARG when cap < 3 x chunks.
+ */
+int fe_problem_pipeline_times(fe_problem_t *p, float *ms, int cap);
+
 /* Number of element and scatter kernels one fe_assemble launches. */
 int fe_problem_launch_count(const fe_problem_t *p, int flags);
 

@@ -802,10 +802,25 @@ struct fe_problem {
   std::vector<long long> pipe_row_off, pipe_slot_off;
   DevBuf pipe_dofs, pipe_R, pipe_J;
   cudaStream_t pipe_copy = nullptr;
-  std::vector<cudaEvent_t> pipe_ev;
+  // the gathers run on a stream of their own: chunk k's gather overlaps
+  // chunk k+1's element kernel (memory-bound beside compute-bound work)
+  cudaStream_t pipe_gather = nullptr;
+  std::vector<cudaEvent_t> pipe_ev;  // per chunk: its gathers done (+1: all copies done)
+  std::vector<cudaEvent_t> pipe_eev; // per chunk: its element kernel done (+1: all gathers done)
+  // with stage timing: the last pipelined call's timeline (start; per chunk
+  // the end of its element kernel, of its gathers and of its copies)
+  std::vector<cudaEvent_t> pipe_tev;
+  int pipe_timed = 0; // chunks of the recorded timeline (0: none)
   void pipe_release() {
     for (auto e : pipe_ev) cudaEventDestroy(e);
     pipe_ev.clear();
+    for (auto e : pipe_eev) cudaEventDestroy(e);
+    pipe_eev.clear();
+    if (pipe_gather) cudaStreamDestroy(pipe_gather);
+    pipe_gather = nullptr;
+    for (auto e : pipe_tev) cudaEventDestroy(e);
+    pipe_tev.clear();
+    pipe_timed = 0;
     if (pipe_copy) cudaStreamDestroy(pipe_copy);
     pipe_copy = nullptr;
     pipe_chunks = 0;
@@ -2134,6 +2149,7 @@ int plan_pipeline(fe_problem *p, int nchunks) {
   }
   const long long units = blocks;
   if (p->pipe_copy) CUDA_TRY(cudaStreamSynchronize(p->pipe_copy)); // copies of the old plan
+  if (p->pipe_gather) CUDA_TRY(cudaStreamSynchronize(p->pipe_gather));
   p->pipe_release();
   p->pipe_elem.assign(nchunks + 1, 0);
   {
@@ -2211,8 +2227,11 @@ int plan_pipeline(fe_problem *p, int nchunks) {
     if (!sl.empty() && (rc = p->pipe_slotlist.upload(sl.data(), sizeof(int32_t) * sl.size()))) return rc;
   }
   CUDA_TRY(cudaStreamCreateWithFlags(&p->pipe_copy, cudaStreamNonBlocking));
+  CUDA_TRY(cudaStreamCreateWithFlags(&p->pipe_gather, cudaStreamNonBlocking));
   p->pipe_ev.resize(nchunks + 1);
   for (auto &e : p->pipe_ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  p->pipe_eev.resize(nchunks + 1);
+  for (auto &e : p->pipe_eev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   p->pipe_chunks = nchunks;
   p->pipe_requested = requested;
   return FE_OK;
@@ -2241,6 +2260,17 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
   const int sms = sm_count_cached();
   // the previous call's copies read the staging buffers: finish them first
   CUDA_TRY(cudaStreamWaitEvent(st, p->pipe_ev[p->pipe_chunks], 0));
+  cudaEvent_t *tev = nullptr;
+  if (p->timing) {
+    if (p->pipe_tev.size() != (size_t)(1 + 3 * p->pipe_chunks)) {
+      for (auto e : p->pipe_tev) cudaEventDestroy(e);
+      p->pipe_tev.assign(1 + 3 * p->pipe_chunks, nullptr);
+      for (auto &e : p->pipe_tev) CUDA_TRY(cudaEventCreate(&e));
+    }
+    tev = p->pipe_tev.data();
+    CUDA_TRY(cudaEventRecord(tev[0], st));
+    p->pipe_timed = p->pipe_chunks;
+  }
   if (flags & FE_ASSEMBLE_VALUES_FROM_DOFS) {
     CUDA_TRY(cudaMemcpyAsync(p->pipe_dofs.p, dofs, sizeof(double) * p->n_dof, cudaMemcpyHostToDevice, st));
     long long n = p->n_nodes * p->nval;
@@ -2250,6 +2280,7 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
   }
   Domain &d = p->domains[0];
   const int32_t *h_rp = p->h_rowptr.data();
+  cudaStream_t gs = p->pipe_gather;
   for (int k = 0; k < p->pipe_chunks; k++) {
     const long long e0 = p->pipe_elem[k], e1 = p->pipe_elem[k + 1];
     if (e1 > e0) {
@@ -2264,7 +2295,12 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
       CUDA_TRY(cudaLaunchKernel((const void *)d.code->func, dim3(grid), dim3(d.threads), kp, (size_t)d.smem, st));
       if (want_j && d.tc && (rc = tc_domain(p, d, e0, e1, st))) return rc;
     }
-    // the rows and slots this chunk completes: one gather launch each
+    if (tev) CUDA_TRY(cudaEventRecord(tev[1 + 3 * k], st));
+    // the rows and slots this chunk completes, on the gather stream once the
+    // chunk's elements are done (the next chunk's elements, writing other
+    // element buffers, run meanwhile): one gather launch
+    CUDA_TRY(cudaEventRecord(p->pipe_eev[k], st));
+    CUDA_TRY(cudaStreamWaitEvent(gs, p->pipe_eev[k], 0));
     {
       const long long q0 = p->pipe_row_off[k], q1 = p->pipe_row_off[k + 1];
       const long long z0 = p->pipe_slot_off[k], z1 = p->pipe_slot_off[k + 1];
@@ -2274,15 +2310,15 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
         // R rows and J slots of the chunk in one launch
         if (p->jac_prec == FE_JAC_F64)
           launch_gather_rows_slots<double>(rows, p->cptr.as<unsigned>(), p->cidx.as<unsigned>(),
-                                           p->jbuf_all.as<double>(), p->pipe_J.as<double>(), z1 - z0, sms, st,
+                                           p->jbuf_all.as<double>(), p->pipe_J.as<double>(), z1 - z0, sms, gs,
                                            p->pipe_slotlist.as<int>() + z0);
         else
           launch_gather_rows_slots<float>(rows, p->cptr.as<unsigned>(), p->cidx.as<unsigned>(),
-                                          p->jbuf_all.as<float>(), p->pipe_J.as<float>(), z1 - z0, sms, st,
+                                          p->jbuf_all.as<float>(), p->pipe_J.as<float>(), z1 - z0, sms, gs,
                                           p->pipe_slotlist.as<int>() + z0);
         CUDA_TRY(cudaGetLastError());
       } else if (want_r && q1 > q0) {
-        k_gather_rows<<<grid_for(q1 - q0, 256, sms), 256, 0, st>>>(
+        k_gather_rows<<<grid_for(q1 - q0, 256, sms), 256, 0, gs>>>(
             p->rptr.as<unsigned>(), p->ridx.as<unsigned>(), p->rbuf_all.as<double>(), p->pipe_R.as<double>(),
             q1 - q0, p->pipe_rowlist.as<int>() + q0);
         CUDA_TRY(cudaGetLastError());
@@ -2290,16 +2326,20 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
       if (want_j && z1 > z0 && !(want_r && q1 > q0)) {
         if (p->jac_prec == FE_JAC_F64)
           launch_gather_slots<double>(p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->jbuf_all.as<double>(),
-                                      p->pipe_J.as<double>(), z1 - z0, sms, st, p->pipe_slotlist.as<int>() + z0);
+                                      p->pipe_J.as<double>(), z1 - z0, sms, gs, p->pipe_slotlist.as<int>() + z0);
         else
           launch_gather_slots<float>(p->cptr.as<unsigned>(), p->cidx.as<unsigned>(), p->jbuf_all.as<float>(),
-                                     p->pipe_J.as<float>(), z1 - z0, sms, st, p->pipe_slotlist.as<int>() + z0);
+                                     p->pipe_J.as<float>(), z1 - z0, sms, gs, p->pipe_slotlist.as<int>() + z0);
         CUDA_TRY(cudaGetLastError());
       }
     }
-    if (p->pipe_runs[k].empty()) continue;
+    if (tev) CUDA_TRY(cudaEventRecord(tev[2 + 3 * k], gs));
+    if (p->pipe_runs[k].empty()) {
+      if (tev) CUDA_TRY(cudaEventRecord(tev[3 + 3 * k], gs));
+      continue;
+    }
     // copy the finished rows to the host while the next chunk computes
-    CUDA_TRY(cudaEventRecord(p->pipe_ev[k], st));
+    CUDA_TRY(cudaEventRecord(p->pipe_ev[k], gs));
     CUDA_TRY(cudaStreamWaitEvent(p->pipe_copy, p->pipe_ev[k], 0));
     for (const auto &run : p->pipe_runs[k]) {
       const long long r0 = run.first, r1 = run.second;
@@ -2311,8 +2351,11 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
         CUDA_TRY(cudaMemcpyAsync((char *)J_vals + jel * s0, (const char *)p->pipe_J.p + jel * s0, jel * (s1 - s0),
                                  cudaMemcpyDeviceToHost, p->pipe_copy));
     }
+    if (tev) CUDA_TRY(cudaEventRecord(tev[3 + 3 * k], p->pipe_copy));
   }
-  // the caller's stream completes only after the copies
+  // the caller's stream completes only after the gathers and the copies
+  CUDA_TRY(cudaEventRecord(p->pipe_eev[p->pipe_chunks], gs));
+  CUDA_TRY(cudaStreamWaitEvent(p->pipe_copy, p->pipe_eev[p->pipe_chunks], 0));
   CUDA_TRY(cudaEventRecord(p->pipe_ev[p->pipe_chunks], p->pipe_copy));
   CUDA_TRY(cudaStreamWaitEvent(st, p->pipe_ev[p->pipe_chunks], 0));
   return FE_OK;
@@ -2484,6 +2527,18 @@ int fe_problem_stage_times(fe_problem_t *p, double *ms, int64_t *calls) {
   for (int k = 0; k < 5; k++) p->stage_ms[k] = 0;
   p->stage_calls = 0;
   return FE_OK;
+}
+
+int fe_problem_pipeline_times(fe_problem_t *p, float *ms, int cap) {
+  if (!p) return fail(FE_ERR_ARG, "null problem");
+  const int n = p->pipe_timed;
+  if (n <= 0) return 0;
+  if (!ms || cap < 3 * n) return fail(FE_ERR_ARG, "fe_problem_pipeline_times: buffer shorter than 3 x chunks");
+  for (int i = 1; i <= 3 * n; i++) {
+    CUDA_TRY(cudaEventSynchronize(p->pipe_tev[i]));
+    CUDA_TRY(cudaEventElapsedTime(ms + (i - 1), p->pipe_tev[0], p->pipe_tev[i]));
+  }
+  return n;
 }
 
 int fe_assemble_host(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags) {

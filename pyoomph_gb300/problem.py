@@ -842,6 +842,16 @@ class Problem:
     def set_stage_timing(self, enable: bool) -> None:
         N.check(N.load().fe_problem_set_timing(self._h, int(enable)))
 
+    def pipeline_times(self) -> np.ndarray:
+        """Timeline of the last ``assemble_host`` call made with stage timing
+        on: per chunk, ms from its start to the end of the chunk's element
+        kernel, of its gathers and of the copies of the rows it completes
+        (array [chunks, 3]; empty when no timed call was made)."""
+        buf = np.zeros(3 * 1024, dtype=np.float32)
+        n = N.load().fe_problem_pipeline_times(self._h, buf.ctypes.data, buf.size)
+        N.check(min(n, 0))
+        return buf[:3 * n].reshape(n, 3).astype(np.float64)
+
     def stage_times(self):
         """Summed ms per stage (dof scatter, element kernels, residual gather,
         Jacobian gather, tensor-core contraction) since the last call, and

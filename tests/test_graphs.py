@@ -108,3 +108,15 @@ def test_pipelined_host_assembly_equals_device_assembly(kind, prec, chunks):
         torch.cuda.current_stream().synchronize()
         P.check()
         assert torch.equal(Rh, R0) and torch.equal(Jh, J0)
+    # with stage timing: the call's timeline, per chunk element kernel <=
+    # gathers <= copies, and the same bits
+    assert P.pipeline_times().size == 0
+    P.set_stage_timing(True)
+    P.assemble_host(xh, Rh, Jh, chunks=chunks)
+    T = P.pipeline_times()
+    P.set_stage_timing(False)
+    P.stage_times()
+    assert T.shape[1] == 3 and 1 <= T.shape[0] <= chunks
+    assert (T[:, 0] <= T[:, 1]).all() and (T[:, 1] <= T[:, 2] + 1e-3).all() and (np.diff(T[:, 0]) >= 0).all()
+    torch.cuda.current_stream().synchronize()
+    assert torch.equal(Rh, R0) and torch.equal(Jh, J0)
