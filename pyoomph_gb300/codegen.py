@@ -482,10 +482,23 @@ def _launch_shape(et: ElementType, nloc: int, per_elem_bytes: int, table_bytes: 
     return best[1], best[2]
 
 
+def _threads_for(epb: int, nq: int, nloc: int) -> int:
+    """Threads per block for EPB elements: max(knots, ceil(rows / 2)) per
+    element, in whole warps.  Phase A (one thread per element and knot)
+    then fills the block, and phase B (one thread per element and row)
+    takes two rounds where an element has more rows than knots.  With one
+    thread per row the Taylor-Hood P2/P1 element (15 rows, 7 knots) leaves
+    8 of 15 warps waiting at phase A's barrier; measured on GB300 (NS
+    256^2, 32 elements per block): 480 -> 256 threads, FP64 element kernel
+    1.461 -> 1.413 ms, FP32 0.341 -> 0.297 ms, df64 with the double-float
+    residual 0.669 -> 0.642 ms."""
+    return ((epb * max(nq, -(-nloc // 2)) + 31) // 32) * 32
+
+
 def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                     name: str = None, epb: int = None, affine: bool = False, jref: bool = None,
                     gauss_sep: bool = False, tc: bool = None, min_blocks: int = None,
-                    residual_precision: str = "f64") -> KernelSpec:
+                    residual_precision: str = "f64", threads: int = None) -> KernelSpec:
     """Fused element kernel for one element type and weak form.
 
     Thread phases (all in one launch, EPB elements per block):
@@ -539,6 +552,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     if jac_precision not in ("f64", "f32", "df64"):
         raise ValueError(f"unknown Jacobian precision {jac_precision!r}")
     df64 = jac_precision == "df64"
+    nt_req = threads     # an explicit thread count (else the launch shape's)
     if residual_precision not in ("f64", "df64"):
         raise ValueError(f"unknown residual precision {residual_precision!r}")
     rdf = residual_precision == "df64"
@@ -655,22 +669,28 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         # 48, 720 threads)
         # (the sum-factorised Q2 hex kernels are fastest at the largest block
         # that fits too: the steady FP64 one at 13 elements)
-        epb, threads = _launch_shape(et, nloc, per_elem, table_bytes,
-                                     smem_cap=224 * 1024 if df64 else 216 * 1024,
-                                     max_threads=720 if df64 else 512, largest=df64 or sumfac)
-    else:
-        threads = ((max(epb * nq, epb * nloc) + 31) // 32) * 32
+        epb, auto_threads = _launch_shape(et, nloc, per_elem, table_bytes,
+                                          smem_cap=224 * 1024 if df64 else 216 * 1024,
+                                          max_threads=720 if df64 else 512, largest=df64 or sumfac)
+        threads = _threads_for(epb, nq, nloc) if nt_req is None else nt_req
+    elif threads is None:
+        threads = _threads_for(epb, nq, nloc)
+    # (every phase is a block-strided loop: fewer threads than rows or knots
+    # take several rounds)
+    threads = (int(threads) + 31) // 32 * 32
+    row_threads = ((max(epb * nq, epb * nloc) + 31) // 32) * 32   # one thread per row
     smem = table_bytes + epb * per_elem
     smem = (smem + 15) // 16 * 16
     if threads > 1024 or smem > 227 * 1024:
         raise ValueError(f"{epb} elements per block do not fit a block ({threads} threads, {smem} B shared)")
     if min_blocks is None:
         # FP64 / double-float Jacobians of 2D elements: bound the registers
-        # for two resident blocks where their shared memory allows it.
-        # Unbounded, the Taylor-Hood kernel takes 78 (FP64) / 101 (df64)
-        # registers, so one 480-thread block per SM; bounded to 64 it spills
-        # 88 / 324 bytes and runs 6% / 10% faster on GB300 (the FP64 pipe
-        # gets a second block's work across the first's barriers)
+        # for two resident blocks where their shared memory allows it.  With
+        # one thread per row (480 threads) the Taylor-Hood kernel took 78
+        # (FP64) / 101 (df64) registers, so one block per SM; bounded to 64
+        # it spilled 88 / 324 bytes and ran 6% / 10% faster on GB300.  At the
+        # default 256 threads the bound (128 registers) no longer binds, and
+        # two blocks fit as they are
         if jac_precision in ("f64", "df64") and et.dim == 2 and threads <= 512 and 2 * smem <= 227 * 1024:
             min_blocks = 2
     elif min_blocks <= 0:
@@ -678,7 +698,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     if name is None:
         h = hashlib.sha1((et.name + jac_precision + str(affine) + str(epb) + str(jref) + str(sumfac) + str(gsep) +
                           ("tc" if use_tc else "") + (f"mb{int(min_blocks)}" if min_blocks else "") +
-                          ("rdf" if rdf else "") +
+                          ("rdf" if rdf else "") + (f"nt{threads}" if threads != row_threads else "") +
                           str(sfi) + (str(pw.m_entries) if transient else "") +
                           str(pw.r_exprs) +
                           str(pw.d_entries)).encode()).hexdigest()[:10]

@@ -257,6 +257,9 @@ class Problem:
         # pipes, for FP32 and df64 Jacobians of steady rational forms
         self.residual_precision = "fp64"
         self.elems_per_block: Optional[int] = None
+        # threads per block of the element kernel (None: one per local row
+        # of the block's elements; fewer run the rows in rounds)
+        self.threads_per_block: Optional[int] = None
         # "auto": detect affine elements (constant geometry per element) on the host
         self.geometry = "auto"
         # > 1: a stack of independent copies of the problem assembled together
@@ -434,14 +437,15 @@ class Problem:
         # geometry kind only -- not on the mesh size: cache it per process
         gsep = bool(self.separable_source and self.affine and mesh_is_axis_aligned(mesh))
         key = (mesh.etype.name, tuple(fields), str(integrand), tuple(used), kprec, self.affine, gsep,
-               self.is_transient, self.tensor_cores, self.min_blocks_per_sm, rprec, self.elems_per_block,
-               self.jacobian_reference)
+               self.is_transient, self.tensor_cores, self.min_blocks_per_sm, rprec, self.threads_per_block,
+               self.elems_per_block, self.jacobian_reference)
         ks = _KERNEL_CACHE.get(key)
         if ks is None:
             pw = differentiate(fields, mesh.dim, integrand, used)
             ks = generate_kernel(mesh.etype, pw, kprec, epb=self.elems_per_block, affine=self.affine,
                                  jref=self.jacobian_reference, gauss_sep=gsep, tc=self.tensor_cores,
-                                 min_blocks=self.min_blocks_per_sm, residual_precision=rprec)
+                                 min_blocks=self.min_blocks_per_sm, residual_precision=rprec,
+                                 threads=self.threads_per_block)
             _KERNEL_CACHE[key] = ks
         if self.elems_per_block is None and int(self.replicas) == 1:
             # balance the waves: with W = ceil(E / (SMs x EPB)) waves of one
@@ -463,7 +467,7 @@ class Problem:
                     ks2 = generate_kernel(mesh.etype, differentiate(fields, mesh.dim, integrand, used), kprec,
                                           epb=epb, affine=self.affine, jref=self.jacobian_reference,
                                           gauss_sep=gsep, tc=self.tensor_cores, min_blocks=self.min_blocks_per_sm,
-                                          residual_precision=rprec)
+                                          residual_precision=rprec, threads=self.threads_per_block)
                     _KERNEL_CACHE[key2] = ks2
                 ks = ks2
         self.kernel: KernelSpec = ks

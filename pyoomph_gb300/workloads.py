@@ -122,6 +122,8 @@ def _main(argv=None) -> None:
                     help="the transient form (BDF2 weights of dt = 1e-3, both previous levels = the current values)")
     ap.add_argument("--min-blocks", type=int, default=None,
                     help="resident blocks per SM to bound the element kernel's registers for")
+    ap.add_argument("--threads", type=int, default=None,
+                    help="threads per block of the element kernel (default: one per local row)")
     ap.add_argument("--residual", choices=["fp64", "df64"], default="fp64",
                     help="df64: the residual path in double-float on the FP32 pipes (fp32/df64 Jacobians)")
     ap.add_argument("--tile-gather", action="store_true",
@@ -136,6 +138,7 @@ def _main(argv=None) -> None:
     P.elems_per_block = a.epb
     P.min_blocks_per_sm = a.min_blocks
     P.residual_precision = a.residual
+    P.threads_per_block = a.threads
     if a.jref is not None:
         P.jacobian_reference = bool(a.jref)
     if a.tc is not None:
