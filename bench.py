@@ -203,9 +203,9 @@ TUNED_EPB = {("ns", 256, "df64"): 32, ("ns", 256, "df64:df64"): 32, ("ns", 256, 
 # with no capture reports null.  Value: (bytes per element, elements of the
 # captured launch).
 MEASURED_TRAFFIC = {
-    # NS Taylor-Hood 256^2, FP64 (registers bounded for two blocks per SM):
-    # 16,041,728 read + 217,390,848 written
-    "fe_elem_p2_tri_f64_aff_ca1e687b31": ((16041728 + 217390848) / 131072, 131072),
+    # NS Taylor-Hood 256^2, FP64 (32 elements and 256 threads per block):
+    # 16,544,512 read + 196,024,832 written
+    "fe_elem_p2_tri_f64_aff_7785240288": ((16544512 + 196024832) / 131072, 131072),
 }
 
 
