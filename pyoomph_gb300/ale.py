@@ -312,7 +312,8 @@ def _sub_nodes(dc: DomainCode, f: int) -> List[int]:
 
 
 def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: int, nh: int,
-                   smem_budget: int, nthreads_cap: int, f32: bool = False, df64: bool = False) -> str:
+                   smem_budget: int, nthreads_cap: int, f32: bool = False, df64: bool = False,
+                   rows_per_thread: int = 1) -> str:
     """Device namespace dom{k} with ``run(a, blk, smem)`` evaluating one block
     of elements of this domain: stage tables and nodal data (phase 0), one
     thread per (element, knot) for geometry, interpolation and the pointwise
@@ -494,14 +495,18 @@ def _domain_source(k: int, dc: DomainCode, dim: int, params: List[str], nval: in
     if f32:
         FQB += FQB % 2
     per_el = nn * nval * (1 + nh) + nn * d + nq * QB + nq * FQB // per8
+    # threads per element: one per knot or per `rows_per_thread` rows, the
+    # larger (the row phase then takes several rounds; every phase is a
+    # block-strided loop)
+    per_thr = max(nq, -(-nloc // max(1, int(rows_per_thread))))
     epb = 1
     for e_ in range(1, 65):
-        if max(e_ * nq, e_ * nloc) > nthreads_cap or (tabd + tabfd + e_ * per_el) * 8 > smem_budget:
+        if e_ * per_thr > nthreads_cap or (tabd + tabfd + e_ * per_el) * 8 > smem_budget:
             break
         epb = e_
     dc.epb = epb
     dc.smem = ((tabd + tabfd + epb * per_el) * 8 + 15) // 16 * 16
-    dc.rows_needed = max(epb * nq, epb * nloc)
+    dc.rows_needed = epb * per_thr
     # ---- source
     L: List[str] = []
     w = L.append
@@ -890,7 +895,7 @@ class FusedKernel:
 
 def generate_fused(domains: List[DomainCode], dim: int, params: List[str], nval: int, nh: int,
                    jac_precision: str = "f64", smem_budget: int = 100 * 1024,
-                   nthreads_cap: int = 256) -> FusedKernel:
+                   nthreads_cap: int = 256, rows_per_thread: int = 1) -> FusedKernel:
     """One kernel for all domains: block b runs the domain whose block range
     [block_start[k], block_start[k+1]) of the runtime's FeFusedArgs holds b."""
     if len(domains) > 4:
@@ -900,7 +905,7 @@ def generate_fused(domains: List[DomainCode], dim: int, params: List[str], nval:
     jreal = {"f64": "double", "f32": "float", "df64": "fe_df64"}[jac_precision]
     jstore = "float" if jac_precision == "f32" else "double"
     bodies = [_domain_source(k, dc, dim, params, nval, nh, smem_budget, nthreads_cap, jac_precision == "f32",
-                             jac_precision == "df64")
+                             jac_precision == "df64", rows_per_thread)
               for k, dc in enumerate(domains)]
     threads = max(32, max(((dc.rows_needed + 31) // 32) * 32 for dc in domains))
     smem = max(dc.smem for dc in domains)
@@ -1022,12 +1027,18 @@ class DropletProblem:
         self.timings: Dict[str, float] = {}
         self.newton_history: List[float] = []
         # launch shape of the fused kernel: thread cap and shared-memory budget
-        # per block (both decide elements per block).  Defaults: the fastest
-        # shapes autotune.tune measured on GB300 for the droplet (FP64 J: 512
-        # threads / 200 KB, FP32 J: 128 threads / 64 KB)
+        # per block (both decide elements per block) and local rows per
+        # thread of the row phase (threads per element: max(knots, rows /
+        # rows_per_thread); the bulk P2 element has 27 rows and 7 knots, so
+        # one thread per row leaves three quarters of the block idle in the
+        # knot phase).  Defaults: the fastest shapes measured on GB300 for
+        # the droplet, side 110 (FP64 J: 4 rows per thread, 512 threads /
+        # 200 KB, 0.861 -> 0.732 ms; FP32 J: 2 rows per thread, 128 threads /
+        # 64 KB, 0.345 -> 0.307 ms; both give the bits of one thread per row)
         f64 = jacobian_precision in ("fp64", "f64", "df64")
         self.nthreads_cap = 512 if f64 else 128
         self.smem_budget = (200 if f64 else 64) * 1024
+        self.rows_per_thread = 4 if f64 else 2
         # compile the element code with device-side bounds checks (status word 2)
         self.bounds_check = False
 
@@ -1075,7 +1086,8 @@ class DropletProblem:
         prec = "f32" if kprec == "f32" else "f64"   # storage of the Jacobian values
         self._prec = prec
         self.kernel = generate_fused(self.domains, 2, self.param_names, nval, 2, kprec,
-                                     smem_budget=self.smem_budget, nthreads_cap=self.nthreads_cap)
+                                     smem_budget=self.smem_budget, nthreads_cap=self.nthreads_cap,
+                                     rows_per_thread=self.rows_per_thread)
         self.conns = [m.conn, m.interface, m.contact_line]
         n = m.x.shape[0]
         present = np.ones((n, nval), dtype=bool)
