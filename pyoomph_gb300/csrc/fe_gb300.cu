@@ -218,23 +218,25 @@ __global__ void k_gather_slots(const unsigned *__restrict__ cptr, const unsigned
   }
 }
 
-// four slots per thread where it measured faster: FP32 values (the FP64
-// variant's registers cost more occupancy than the extra loads in flight
-// gain) over patterns large enough to fill the GPU at a quarter of the
-// threads
+// several slots per thread over patterns large enough to fill the GPU with
+// fewer threads: four for FP32 values, two for FP64 (measured on GB300, NS
+// 256^2: FP64 0.138 -> 0.129 ms with two, four cost more occupancy than the
+// extra loads in flight gain; FP32 0.107 -> 0.084 ms with four, eight were
+// slower again at 0.112)
 int grid_for(long long n, int threads, int sms);
 
 template <typename T, bool ROWS>
 void launch_gather_slots_(const unsigned *cptr, const unsigned *cidx, const T *jbuf, T *vals, long long nnz, int sms,
                           cudaStream_t st, const int *list, const GatherRows &rows) {
-  const bool big = sizeof(T) == 4 && nnz >= (1LL << 22);
-  long long work = big ? (nnz + 3) / 4 : nnz;
+  const bool big = nnz >= (1LL << 22);
+  constexpr int UU = sizeof(T) == 4 ? 4 : 2;
+  long long work = big ? (nnz + UU - 1) / UU : nnz;
   if (ROWS && rows.n > work) work = rows.n;
   const int g = grid_for(work, 256, sms);
   if (big && list)
-    k_gather_slots<T, 4, true, ROWS><<<g, 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list, rows);
+    k_gather_slots<T, UU, true, ROWS><<<g, 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list, rows);
   else if (big)
-    k_gather_slots<T, 4, false, ROWS><<<g, 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list, rows);
+    k_gather_slots<T, UU, false, ROWS><<<g, 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list, rows);
   else if (list)
     k_gather_slots<T, 1, true, ROWS><<<g, 256, 0, st>>>(cptr, cidx, jbuf, vals, nnz, list, rows);
   else
