@@ -309,3 +309,26 @@ def test_df64_residual_element_level_parity(geometry, jac):
     Re, Je = P.element_buffers()
     assert C.relmax(Re, Rr) <= RTOL
     assert C.relmax(Je, Jr) <= (RTOL if jac == "df64" else 1e-5)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_thread_count_changes_rounding_only(prec):
+    """Every phase of the element kernel is a block-strided loop, so any
+    thread count gives the same element values up to the compiler's choice
+    of fused multiply-adds: one thread per row, the default max(knots,
+    ceil(rows/2)) per element, and fewer threads than knots."""
+    from pyoomph_gb300 import workloads as W
+    out = {}
+    for thr in (None, 480, 96):
+        P = W.navier_stokes_problem(N=[12, 10], jacobian_precision=prec)
+        P.elems_per_block = 32
+        P.threads_per_block = thr
+        P.initialise()
+        W.perturb_dofs(P, seed=5, sigma=1e-2)
+        assert P.kernel.threads == (256 if thr is None else thr)
+        R, J = P.get_jacobian()
+        out[thr] = (R, J.data.astype(np.float64))
+    R0, J0 = out[None]
+    for thr in (480, 96):
+        R, J = out[thr]
+        assert _relmax(R, R0) <= 1e-14 and _relmax(J, J0) <= (1e-14 if prec == "fp64" else 1e-6)
