@@ -605,7 +605,7 @@ def run_gb300(args):
                 line[key]["df64_residual"]["max_rel_residual_error_vs_oracle"] = par.get("max_rel_R")
                 line[key]["df64_residual"]["max_rel_jacobian_error_vs_oracle"] = par.get("max_rel_J")
     if rank == 0 and world == 1 and args.workload == "ns" and not args.no_extras:
-        # the other workloads of the survey, measured in this same run (after
+        # the other benchmark workloads, measured in this same run (after
         # the headline's timed regions): Poisson Q2 64^2, the Q2 hex 48^3
         # (FP32 Jacobian on the tensor cores), the moving-mesh droplet and a
         # bounded serving stream
