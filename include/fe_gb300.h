@@ -508,6 +508,15 @@ int fe_problem_stage_times(fe_problem_t *p, double *ms, int64_t *calls);
  */
 int fe_problem_pipeline_times(fe_problem_t *p, float *ms, int cap);
 
+/*
+ * Element streams of fe_assemble_pipelined: 1 (chunks in order on one
+ * stream), 2 (consecutive chunks on alternating streams, which may run
+ * concurrently) or 0 (automatic: one).  The values are the same bits
+ * either way; two streams measured faster only for FP64 Jacobians, and
+ * not reliably.
+ */
+int fe_problem_set_pipeline_streams(fe_problem_t *p, int n);
+
 /* Number of element and scatter kernels one fe_assemble launches. */
 int fe_problem_launch_count(const fe_problem_t *p, int flags);
 

@@ -29,7 +29,7 @@ EXPORTS = ["fe_last_error", "fe_version", "fe_device_info", "fe_code_compile", "
            "fe_problem_pattern_device", "fe_problem_set_values", "fe_problem_get_values",
            "fe_problem_set_params", "fe_assemble", "fe_assemble_host", "fe_residual_max", "fe_dof_update",
            "fe_problem_check", "fe_problem_launch_count", "fe_problem_set_timing", "fe_problem_stage_times",
-           "fe_problem_pipeline_times", "fe_pattern_host",
+           "fe_problem_pipeline_times", "fe_problem_set_pipeline_streams", "fe_pattern_host",
            "fe_residual_max_noalloc", "fe_residual_max_noalloc_limit", "fe_problem_element_buffers",
            "fe_problem_set_history", "fe_problem_get_history", "fe_problem_shift_history", "fe_problem_set_positions",
            "fe_problem_graph_capture", "fe_problem_graph_launch", "fe_problem_set_dparam",
@@ -151,6 +151,7 @@ def load(build_if_missing: bool = True):
         L.fe_problem_set_timing.argtypes = [vp, c_int]
         L.fe_problem_stage_times.argtypes = [vp, vp, vp]
         L.fe_problem_pipeline_times.argtypes = [vp, vp, c_int]
+        L.fe_problem_set_pipeline_streams.argtypes = [vp, c_int]
         L.fe_pattern_host.argtypes = [ctypes.POINTER(ProblemDesc), vp, vp, vp]
         L.fe_residual_max_noalloc.argtypes = [vp, i64, vp, vp]
         L.fe_problem_element_buffers.argtypes = [vp, c_int, vp, vp]

@@ -807,6 +807,11 @@ struct fe_problem {
   // the gathers run on a stream of their own: chunk k's gather overlaps
   // chunk k+1's element kernel (memory-bound beside compute-bound work)
   cudaStream_t pipe_gather = nullptr;
+  // the element chunks alternate between pipe_nes streams (1 or 2; 0:
+  // automatic): chunk k+1 may start while chunk k's last blocks drain (they
+  // write disjoint element buffers)
+  cudaStream_t pipe_es[2] = {nullptr, nullptr};
+  int pipe_nes = 0;
   std::vector<cudaEvent_t> pipe_ev;  // per chunk: its gathers done (+1: all copies done)
   std::vector<cudaEvent_t> pipe_eev; // per chunk: its element kernel done (+1: all gathers done)
   // with stage timing: the last pipelined call's timeline (start; per chunk
@@ -820,6 +825,10 @@ struct fe_problem {
     pipe_eev.clear();
     if (pipe_gather) cudaStreamDestroy(pipe_gather);
     pipe_gather = nullptr;
+    for (auto &e : pipe_es) {
+      if (e) cudaStreamDestroy(e);
+      e = nullptr;
+    }
     for (auto e : pipe_tev) cudaEventDestroy(e);
     pipe_tev.clear();
     pipe_timed = 0;
@@ -2152,6 +2161,8 @@ int plan_pipeline(fe_problem *p, int nchunks) {
   const long long units = blocks;
   if (p->pipe_copy) CUDA_TRY(cudaStreamSynchronize(p->pipe_copy)); // copies of the old plan
   if (p->pipe_gather) CUDA_TRY(cudaStreamSynchronize(p->pipe_gather));
+  for (auto e : p->pipe_es)
+    if (e) CUDA_TRY(cudaStreamSynchronize(e));
   p->pipe_release();
   p->pipe_elem.assign(nchunks + 1, 0);
   {
@@ -2230,15 +2241,31 @@ int plan_pipeline(fe_problem *p, int nchunks) {
   }
   CUDA_TRY(cudaStreamCreateWithFlags(&p->pipe_copy, cudaStreamNonBlocking));
   CUDA_TRY(cudaStreamCreateWithFlags(&p->pipe_gather, cudaStreamNonBlocking));
+  for (auto &e : p->pipe_es) CUDA_TRY(cudaStreamCreateWithFlags(&e, cudaStreamNonBlocking));
   p->pipe_ev.resize(nchunks + 1);
   for (auto &e : p->pipe_ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  p->pipe_eev.resize(nchunks + 1);
+  p->pipe_eev.resize(nchunks + 2); // + the fork of the element streams
   for (auto &e : p->pipe_eev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   p->pipe_chunks = nchunks;
   p->pipe_requested = requested;
   return FE_OK;
 }
 } // namespace
+
+// element streams of the pipelined assembly; automatic: one.  Measured on
+// GB300, NS 256^2 (ms per call, best chunk count): two streams run
+// consecutive chunks concurrently rather than only across their tails;
+// FP64 J 1.72 -> 1.63-1.87 depending on the chunk count and the run, df64
+// J 1.15 -> 1.39, FP32 J 0.60 -> 0.67 (its copies start later)
+static int pipe_streams(const fe_problem *p) {
+  return p->pipe_nes == 2 ? 2 : 1;
+}
+
+int fe_problem_set_pipeline_streams(fe_problem_t *p, int n) {
+  if (!p || n < 0 || n > 2) return fail(FE_ERR_ARG, "fe_problem_set_pipeline_streams: n must be 0, 1 or 2");
+  p->pipe_nes = n;
+  return FE_OK;
+}
 
 int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *J_vals, int flags, int nchunks,
                           void *stream) {
@@ -2283,8 +2310,13 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
   Domain &d = p->domains[0];
   const int32_t *h_rp = p->h_rowptr.data();
   cudaStream_t gs = p->pipe_gather;
+  const int nes = pipe_streams(p);
+  // fork: both element streams start after the caller's work so far
+  CUDA_TRY(cudaEventRecord(p->pipe_eev[p->pipe_chunks + 1], st));
+  for (auto e : p->pipe_es) CUDA_TRY(cudaStreamWaitEvent(e, p->pipe_eev[p->pipe_chunks + 1], 0));
   for (int k = 0; k < p->pipe_chunks; k++) {
     const long long e0 = p->pipe_elem[k], e1 = p->pipe_elem[k + 1];
+    cudaStream_t es = p->pipe_es[nes == 2 ? (k & 1) : 0];
     if (e1 > e0) {
       FeElemArgs a = domain_args(p, d, want_j ? 1 : 0);
       a.conn += e0 * d.nnode;
@@ -2294,14 +2326,14 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
       if (d.tc) a.dhat += e0 * (long long)d.tca.nq * d.tca.npair;
       void *kp[] = {&a};
       unsigned grid = (unsigned)((a.n_elem + d.epb - 1) / d.epb);
-      CUDA_TRY(cudaLaunchKernel((const void *)d.code->func, dim3(grid), dim3(d.threads), kp, (size_t)d.smem, st));
-      if (want_j && d.tc && (rc = tc_domain(p, d, e0, e1, st))) return rc;
+      CUDA_TRY(cudaLaunchKernel((const void *)d.code->func, dim3(grid), dim3(d.threads), kp, (size_t)d.smem, es));
+      if (want_j && d.tc && (rc = tc_domain(p, d, e0, e1, es))) return rc;
     }
-    if (tev) CUDA_TRY(cudaEventRecord(tev[1 + 3 * k], st));
+    if (tev) CUDA_TRY(cudaEventRecord(tev[1 + 3 * k], es));
     // the rows and slots this chunk completes, on the gather stream once the
     // chunk's elements are done (the next chunk's elements, writing other
     // element buffers, run meanwhile): one gather launch
-    CUDA_TRY(cudaEventRecord(p->pipe_eev[k], st));
+    CUDA_TRY(cudaEventRecord(p->pipe_eev[k], es));
     CUDA_TRY(cudaStreamWaitEvent(gs, p->pipe_eev[k], 0));
     {
       const long long q0 = p->pipe_row_off[k], q1 = p->pipe_row_off[k + 1];

@@ -846,6 +846,12 @@ class Problem:
     def set_stage_timing(self, enable: bool) -> None:
         N.check(N.load().fe_problem_set_timing(self._h, int(enable)))
 
+    def set_pipeline_streams(self, n: int) -> None:
+        """Element streams of ``assemble_host``: 1, 2 (consecutive chunks on
+        alternating streams, which may run concurrently) or 0 (automatic:
+        one).  Same bits either way."""
+        N.check(N.load().fe_problem_set_pipeline_streams(self._h, int(n)))
+
     def pipeline_times(self) -> np.ndarray:
         """Timeline of the last ``assemble_host`` call made with stage timing
         on: per chunk, ms from its start to the end of the chunk's element

@@ -120,3 +120,13 @@ def test_pipelined_host_assembly_equals_device_assembly(kind, prec, chunks):
     assert (T[:, 0] <= T[:, 1]).all() and (T[:, 1] <= T[:, 2] + 1e-3).all() and (np.diff(T[:, 0]) >= 0).all()
     torch.cuda.current_stream().synchronize()
     assert torch.equal(Rh, R0) and torch.equal(Jh, J0)
+    # element chunks on two alternating streams: the same bits
+    P.set_pipeline_streams(2)
+    Rh.fill_(float("nan"))
+    Jh.fill_(float("nan"))
+    for _ in range(2):
+        P.assemble_host(xh, Rh, Jh, chunks=chunks)
+        torch.cuda.current_stream().synchronize()
+        P.check()
+        assert torch.equal(Rh, R0) and torch.equal(Jh, J0)
+    P.set_pipeline_streams(0)
