@@ -2311,12 +2311,14 @@ int fe_assemble_pipelined(fe_problem_t *p, const double *dofs, double *R, void *
   const int32_t *h_rp = p->h_rowptr.data();
   cudaStream_t gs = p->pipe_gather;
   const int nes = pipe_streams(p);
-  // fork: both element streams start after the caller's work so far
-  CUDA_TRY(cudaEventRecord(p->pipe_eev[p->pipe_chunks + 1], st));
-  for (auto e : p->pipe_es) CUDA_TRY(cudaStreamWaitEvent(e, p->pipe_eev[p->pipe_chunks + 1], 0));
+  if (nes == 2) {
+    // fork: both element streams start after the caller's work so far
+    CUDA_TRY(cudaEventRecord(p->pipe_eev[p->pipe_chunks + 1], st));
+    for (auto e : p->pipe_es) CUDA_TRY(cudaStreamWaitEvent(e, p->pipe_eev[p->pipe_chunks + 1], 0));
+  }
   for (int k = 0; k < p->pipe_chunks; k++) {
     const long long e0 = p->pipe_elem[k], e1 = p->pipe_elem[k + 1];
-    cudaStream_t es = p->pipe_es[nes == 2 ? (k & 1) : 0];
+    cudaStream_t es = nes == 2 ? p->pipe_es[k & 1] : st; // one stream: the caller's
     if (e1 > e0) {
       FeElemArgs a = domain_args(p, d, want_j ? 1 : 0);
       a.conn += e0 * d.nnode;
