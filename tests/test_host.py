@@ -51,6 +51,8 @@ def test_null_arguments_are_rejected():
     assert L.fe_problem_create(None, None) == N.FE_ERR_ARG
     assert L.fe_problem_sizes(None, None, None) == N.FE_ERR_ARG
     assert L.fe_assemble(None, None, None, None, 3, None) == N.FE_ERR_ARG
+    assert L.fe_problem_set_pipeline_streams(None, 1) == N.FE_ERR_ARG
+    assert L.fe_problem_pipeline_times(None, None, 0) == N.FE_ERR_ARG
 
 
 def test_krylov_solver_arguments_are_checked_before_any_device_call():
@@ -351,3 +353,63 @@ def test_assembler_refuses_a_differently_numbered_host_problem():
     asm._set_problem(Host(swapped, eng.n_dof))
     with pytest.raises(RuntimeError, match="numbering differs"):
         asm.check_numbering()
+
+
+def test_thread_layout_rule():
+    """Threads per block: max(knots, ceil(rows/2)) per element in whole
+    warps.  The Taylor-Hood element (15 rows, 7 knots) runs 8 per element;
+    elements with no more rows than knots keep one thread per row; an
+    explicit count overrides, and only a changed count renames a kernel."""
+    from pyoomph_gb300 import workloads as W
+    from pyoomph_gb300.codegen import _threads_for
+    assert _threads_for(32, 7, 15) == 256 and _threads_for(24, 7, 15) == 192
+    assert _threads_for(27, 9, 9) == 256 and _threads_for(13, 27, 27) == 352
+    P = W.navier_stokes_problem(N=256)
+    ks = P.lower()
+    assert (ks.epb, ks.threads) == (32, 256)
+    P = W.poisson_problem(N=64)
+    ks = P.lower()
+    assert ks.threads == ((ks.epb * 9 + 31) // 32) * 32
+    P = W.navier_stokes_problem(N=256, jacobian_precision="fp32")
+    P.threads_per_block = 480
+    ks480 = P.lower()
+    assert ks480.threads == 480 and "#define FE_NT 480" in ks480.source
+    P2 = W.navier_stokes_problem(N=256, jacobian_precision="fp32")
+    assert P2.lower().name != ks480.name
+
+
+def test_fused_rows_per_thread_shapes():
+    """The fused moving-mesh kernel: threads per element max(knots, rows /
+    rows_per_thread); the bulk P2 element (27 rows, 7 knots) at 4 rows per
+    thread runs 7 threads per element; one row per thread keeps 27."""
+    from pyoomph_gb300.ale import DropletProblem
+    D = DropletProblem(N=20, jacobian_precision="fp64")
+    assert D.rows_per_thread == 4
+    bulk = D.lower().domains[0]
+    assert bulk.rows_needed == bulk.epb * 7
+    D1 = DropletProblem(N=20, jacobian_precision="fp64")
+    D1.rows_per_thread = 1
+    bulk1 = D1.lower().domains[0]
+    assert bulk1.rows_needed == bulk1.epb * 27
+    assert DropletProblem(N=20, jacobian_precision="fp32").rows_per_thread == 2
+
+
+def test_df64_printer_splits_literals_exactly_and_refuses_libm():
+    """Double-float literals are the binary64 value split into its binary32
+    pair at generation time (hi + lo recovers the double to 48 bits);
+    exp, non-integer powers and Gaussian sums are refused."""
+    import re
+    import numpy as np
+    import sympy as sp
+    from pyoomph_gb300.codegen import _DF64Printer
+    pr = _DF64Printer({})
+    for v in (2.0, 0.1, 1.0 / 3.0, -1.0e-5, 123456.789):
+        m = re.fullmatch(r"fe_df64\((\S+)f, (\S+)f\)", pr._lit(v))
+        hi, lo = float(m.group(1)), float(m.group(2))
+        assert np.float32(hi) == hi and np.float32(lo) == lo
+        assert abs((hi + lo) - v) <= abs(v) * 2.0 ** -47
+    x = sp.Symbol("x")
+    assert "fe_df64(1.0f, 0.0f)" in pr.doprint(1 / x)
+    for bad in (sp.exp(x), x ** sp.Rational(1, 3)):
+        with pytest.raises(NotImplementedError):
+            pr.doprint(bad)
