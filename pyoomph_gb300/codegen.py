@@ -108,8 +108,14 @@ class _DF64Printer(_Printer):
     """C printer for double-float (``fe_df64``) arithmetic: every literal is
     split into its binary32 pair at generation time (the binary64 value of
     the FP64 code, to 48 bits), operations are + - * / and small integer
-    powers.  Anything else (libm calls, Gaussian sums) is refused: see
-    ``df64_residual_supported``."""
+    powers.  A Gaussian source term is evaluated in FP64 (the device helper
+    of the FP64 code, under the FP64 names of the coordinates and
+    parameters) and converted once.  Anything else (libm calls) is refused:
+    see ``df64_residual_supported``."""
+
+    def __init__(self, names: Dict[sp.Symbol, str], fp64_names: Optional[Dict[sp.Symbol, str]] = None):
+        super().__init__(names)
+        self._fp64_names = fp64_names
 
     def _lit(self, v: float) -> str:
         hi = float(np.float32(v))
@@ -129,7 +135,9 @@ class _DF64Printer(_Printer):
         raise NotImplementedError("no double-float exp")
 
     def _print_GaussianSum(self, e):
-        raise NotImplementedError("no double-float Gaussian sum")
+        if self._fp64_names is None:
+            raise NotImplementedError("a double-float Gaussian sum needs the FP64 names")
+        return f"fe_df64({_Printer(self._fp64_names)._print_GaussianSum(e)})"
 
     def _print_Function(self, e):
         raise NotImplementedError(f"no double-float {e.func}")
@@ -138,10 +146,15 @@ class _DF64Printer(_Printer):
 def df64_residual_supported(pw: "Pointwise") -> bool:
     """Whether the pointwise residual and derivatives are rational in the
     fields, coordinates and parameters (+ - * / and integer powers between
-    -2 and 4): the forms a double-float residual can be generated for."""
+    -2 and 4), Gaussian source terms aside (evaluated in FP64): the forms a
+    double-float residual can be generated for."""
     ok = (sp.Add, sp.Mul, sp.Symbol, sp.Number, sp.Pow)
     for e in list(pw.r_exprs) + [d for (_, _, d) in pw.d_entries]:
-        for s in sp.preorder_traversal(sp.sympify(e)):
+        it = sp.preorder_traversal(sp.sympify(e))
+        for s in it:
+            if isinstance(s, E.GaussianSum):
+                it.skip()          # evaluated in FP64, converted once
+                continue
             if not isinstance(s, ok):
                 return False
             if isinstance(s, sp.Pow) and not (s.args[1].is_Integer and int(s.args[1]) in (2, 3, 4, -1, -2)):
@@ -240,9 +253,9 @@ def _symbol_names(pw: Pointwise, prefix: str = "") -> Dict[sp.Symbol, str]:
     return names
 
 
-def _emit(exprs, names, fp32: bool, outs, indent="  ", df64: bool = False):
+def _emit(exprs, names, fp32: bool, outs, indent="  ", df64: bool = False, fp64_names=None):
     real = "fe_df64" if df64 else "float" if fp32 else "double"
-    pr = _DF64Printer(dict(names)) if df64 else _Printer(dict(names), fp32=fp32)
+    pr = _DF64Printer(dict(names), fp64_names) if df64 else _Printer(dict(names), fp32=fp32)
     repl, reduced = sp.cse(exprs, symbols=sp.numbered_symbols("t_"), optimizations="basic")
     lines = []
     for s_, e in repl:
@@ -315,6 +328,7 @@ def pointwise_source(pw: Pointwise, jreal: str = "double", rdf: bool = False) ->
     r are ``fe_df64`` and the arithmetic runs on the FP32 pipes; D too when
     jreal is double (the double-float Jacobian)."""
     names = _symbol_names(pw)
+    fp64_names = dict(names)
     nr = len(pw.r_exprs)
     nd = len(pw.d_entries)
     if rdf:
@@ -341,7 +355,7 @@ def pointwise_source(pw: Pointwise, jreal: str = "double", rdf: bool = False) ->
     if jreal == "double" and nd:
         exprs = list(pw.r_exprs) + [d for (_, _, d) in pw.d_entries]
         outs = [f"r[{k}]" for k in range(nr)] + [f"D[{k}]" for k in range(nd)]
-        body = _emit(exprs, names, False, outs, "  ", df64=rdf)
+        body = _emit(exprs, names, False, outs, "  ", df64=rdf, fp64_names=fp64_names)
         # D assignments only when flag: move them under the branch
         rl = [l for l in body if not l.strip().startswith("D[")]
         dl = [l for l in body if l.strip().startswith("D[")]
@@ -351,7 +365,8 @@ def pointwise_source(pw: Pointwise, jreal: str = "double", rdf: bool = False) ->
         else:
             lines += ["  if (flag) {"] + ["  " + l for l in dl] + ["  }"]
     else:
-        lines += _emit(list(pw.r_exprs), names, False, [f"r[{k}]" for k in range(nr)], "  ", df64=rdf)
+        lines += _emit(list(pw.r_exprs), names, False, [f"r[{k}]" for k in range(nr)], "  ", df64=rdf,
+                       fp64_names=fp64_names)
     lines.append("}")
     names = _symbol_names(pw)
     # Hessian-vector product: D'(U; V) = sum_c dD/dU_c V_c, V the interpolated direction
@@ -529,10 +544,11 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     27 x 3 physical gradients otherwise).
 
     With ``residual_precision="df64"`` (FP32 or double-float Jacobians of
-    steady forms whose pointwise terms are rational) the residual path runs
-    in double-float on the FP32 pipes: interpolation, pointwise residual,
+    steady forms whose pointwise terms are rational, Gaussian sources
+    aside) the residual path runs in double-float on the FP32 pipes:
+    interpolation (sum-factorised for the Q2 hex), pointwise residual,
     pull-back and the contraction with the test functions; the geometry
-    stays FP64.  Nodal values are staged as differences from the element's
+    and the Gaussian source factors stay FP64.  Nodal values are staged as differences from the element's
     node 0, formed in FP64 (u = u_0 + sum_l (u_l - u_0) psi_l, grad u =
     sum_l (u_l - u_0) grad psi_l by the partition of unity), so that the
     48-bit significand rounds only the small differences: the cancellation
@@ -563,7 +579,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             raise ValueError("the double-float residual is generated for steady forms")
         if not df64_residual_supported(pw):
             raise ValueError("the double-float residual needs pointwise terms rational in the fields "
-                             "(+ - * / and integer powers)")
+                             "(+ - * / and integer powers; Gaussian sources are allowed)")
         if not et.c1_index or et.c1_index[0] != 0:
             raise ValueError("the double-float residual stages values relative to node 0, a C1 node")
         if jref is False:
@@ -612,9 +628,8 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     tabf = (nq * nn * (1 + dim) + nq * nn1 * (1 + dim)) if tab_copy else 0
     table_bytes += ((tabf * (8 if df64 else 4) + 15) // 16) * 16
     # double-float residual with an FP32 Jacobian: double-float tables too
+    # (the sum-factorised Q2 hex path uses 1D tables instead: decided below)
     rtab = rdf and not df64
-    if rtab:
-        table_bytes += tabf * 8
     geo_doubles = (dim * dim + 1) if affine else 0
     # separable Gaussian source (axis-aligned affine Q2 elements, the caller
     # checks the alignment): the element's per-axis factors in shared memory
@@ -644,7 +659,10 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
     # at the 27 knots) and of the residual's test-function contraction of the
     # Q2 hex: one axis at a time, 729 multiply-adds each instead of 27 x 27 x 4
     sfi = bool(jref and et.name == "Q2_HEX" and nf == 1 and spaces[0] == "C2"
-               and list(layout.loc_of[0]) == list(range(nn)) and not rdf)
+               and list(layout.loc_of[0]) == list(range(nn)))
+    rtab = rtab and not sfi
+    if rtab:
+        table_bytes += tabf * 8
     # transient forms: nodal du/dt = w0 u + w1 u_{n-1} + w2 u_{n-2} staged per
     # element beside the values, interpolated as one more input per field
     transient = pw.transient
@@ -775,8 +793,9 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
                 w("  fe_df64* sDps2r = sPsi2r + FE_NQ * FE_NN;")
                 w("  fe_df64* sPsi1r = sDps2r + FE_NQ * FE_NN * FE_DIM;")
                 w("  fe_df64* sDps1r = sPsi1r + FE_NQ * FE_NN1;")
-            elif rdf:
+            elif rdf and df64:
                 w("  fe_df64* sPsi2r = sPsi2j; fe_df64* sDps2r = sDps2j; fe_df64* sPsi1r = sPsi1j; fe_df64* sDps1r = sDps1j;")
+                w("  (void)sPsi2r; (void)sDps2r; (void)sPsi1r; (void)sDps1r;")
         else:
             w("  (void)sEnd;")
             w("  const double* sPsi2j = sPsi2; const double* sDps2j = sDps2;")
@@ -822,6 +841,9 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         # 1D Lagrange values M0[q][i] and derivatives M1[q][i] at the 1D Gauss points
         w("  __shared__ double sM[18];")
         w("  for (int k = threadIdx.x; k < 18; k += FE_NT) sM[k] = c_M[k];")
+        if rdf:
+            w("  __shared__ fe_df64 sMr[18];")
+            w("  for (int k = threadIdx.x; k < 18; k += FE_NT) sMr[k] = fe_df64(c_M[k]);")
     if sumfac:
         from .spaces import _G3_1D, _lag3
         M = [np.array([_lag3(g)[0] for g in _G3_1D]), np.array([_lag3(g)[1] for g in _G3_1D])]
@@ -896,7 +918,50 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("    sGe[el * " + str(gsd) + " + o] = exp(-(dd * dd) / (2.0 * w * w));")
         w("  }")
         w("  __syncthreads();")
-    if sfi:
+    if sfi and rdf:
+        SA, SB, SC = sfs
+        # ---------------- phase I (double-float): sum-factorised interpolation ----------------
+        # of the staged differences d_l = u_l - u_0 (d_0 = 0; node 0 holds u_0,
+        # added to the value in phase A), one axis at a time, renormalised
+        # after each stage's three multiply-adds
+        w("  { fe_df64* Ia = reinterpret_cast<fe_df64*>(sIa); fe_df64* Ib = reinterpret_cast<fe_df64*>(sIb);")
+        w("    fe_df64* Ic = reinterpret_cast<fe_df64*>(sIc);")
+        w("  for (int p = threadIdx.x; p < nel * 27; p += FE_NT) {  // axis 0: A, B [i1][i2][q0]")
+        w("    const int el = p / 27, o = p - el * 27, i1 = o / 9, i2 = (o / 3) % 3, q0 = o % 3;")
+        w("    const fe_df64* u = sUr + el * FE_NN * FE_NVAL + (3 * i1 + 9 * i2) * FE_NVAL;")
+        w("    fe_df64 a_ = fe_df64(0.0f, 0.0f), b_ = fe_df64(0.0f, 0.0f);")
+        w("    #pragma unroll")
+        w("    for (int i0 = 0; i0 < 3; ++i0) {")
+        w("      const fe_df64 uu = (i0 == 0 && i1 == 0 && i2 == 0) ? fe_df64(0.0f, 0.0f) : u[i0 * FE_NVAL];")
+        w("      fe_mac(a_, uu, sMr[q0 * 3 + i0]); fe_mac(b_, uu, sMr[9 + q0 * 3 + i0]); }")
+        w(f"    Ia[el * {SA} + o] = fe_norm(a_); Ia[el * {SA} + 27 + o] = fe_norm(b_);")
+        w("  }")
+        w("  __syncthreads();")
+        w("  for (int p = threadIdx.x; p < nel * 27; p += FE_NT) {  // axis 1: AA, AB, BA [i2][q0][q1]")
+        w("    const int el = p / 27, o = p - el * 27, i2 = o / 9, q0 = (o / 3) % 3, q1 = o % 3;")
+        w(f"    const fe_df64* A = Ia + el * {SA} + i2 * 3 + q0;")
+        w("    fe_df64 aa = fe_df64(0.0f, 0.0f), ab = fe_df64(0.0f, 0.0f), ba = fe_df64(0.0f, 0.0f);")
+        w("    #pragma unroll")
+        w("    for (int i1 = 0; i1 < 3; ++i1) {")
+        w("      const fe_df64 av = A[i1 * 9], bv = A[27 + i1 * 9];")
+        w("      fe_mac(aa, av, sMr[q1 * 3 + i1]); fe_mac(ab, av, sMr[9 + q1 * 3 + i1]); fe_mac(ba, bv, sMr[q1 * 3 + i1]); }")
+        w(f"    Ib[el * {SB} + o] = fe_norm(aa); Ib[el * {SB} + 27 + o] = fe_norm(ab); Ib[el * {SB} + 54 + o] = fe_norm(ba);")
+        w("  }")
+        w("  __syncthreads();")
+        w("  for (int p = threadIdx.x; p < nel * 27; p += FE_NT) {  // axis 2: value, d0, d1, d2 at knot q")
+        w("    const int el = p / 27, q = p - el * 27, q0 = q / 9, q1 = (q / 3) % 3, q2 = q % 3;")
+        w(f"    const fe_df64* B = Ib + el * {SB} + q0 * 3 + q1;")
+        w("    fe_df64 v = fe_df64(0.0f, 0.0f), d0 = v, d1 = v, d2 = v;")
+        w("    #pragma unroll")
+        w("    for (int i2 = 0; i2 < 3; ++i2) {")
+        w("      const fe_df64 aa = B[i2 * 9], ab = B[27 + i2 * 9], ba = B[54 + i2 * 9];")
+        w("      const fe_df64 m0 = sMr[q2 * 3 + i2], m1 = sMr[9 + q2 * 3 + i2];")
+        w("      fe_mac(v, aa, m0); fe_mac(d2, aa, m1); fe_mac(d1, ab, m0); fe_mac(d0, ba, m0); }")
+        w(f"    fe_df64* C = Ic + el * {SC} + q;")
+        w("    C[0] = fe_norm(v); C[27] = fe_norm(d0); C[54] = fe_norm(d1); C[81] = fe_norm(d2);")
+        w("  }")
+        w("  __syncthreads(); }")
+    elif sfi:
         SA, SB, SC = sfs
         # ---------------- phase I: sum-factorised interpolation ----------------
         # u at node l = i0 + 3 i1 + 9 i2; knot q = 9 q0 + 3 q1 + q2; shapes
@@ -1059,7 +1124,24 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
             w(f"        U[{base} + 1 + i] = fe_norm(s_); }}")
             w("    }")
 
-    if rdf:
+    if rdf and sfi:
+        # value = u_0 + the interpolated differences; gradients from phase I
+        w("    fe_df64 gr[FE_DIM][FE_DIM];")
+        w("    #pragma unroll")
+        w("    for (int b = 0; b < FE_DIM; ++b)")
+        w("      #pragma unroll")
+        w("      for (int i = 0; i < FE_DIM; ++i) gr[b][i] = fe_df64(g[b][i]);")
+        w("    fe_df64 U[FE_NTC];")
+        w(f"    {{ const fe_df64* C = reinterpret_cast<const fe_df64*>(sIc) + el * {SC} + q;")
+        w("      U[0] = C[0] + sUr[(el * FE_NN) * FE_NVAL];")
+        w("      const fe_df64 gs[3] = {C[27], C[54], C[81]};")
+        w("      #pragma unroll")
+        w("      for (int i = 0; i < FE_DIM; ++i) { fe_df64 s_ = fe_df64(0.0f, 0.0f);")
+        w("        #pragma unroll")
+        w("        for (int b = 0; b < FE_DIM; ++b) fe_mac(s_, gr[b][i], gs[b]);")
+        w("        U[1 + i] = fe_norm(s_); }")
+        w("    }")
+    elif rdf:
         interp_r()
     elif sfi:
         w(f"    double U[{nu if transient else 'FE_NTC'}];")
@@ -1090,7 +1172,16 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("      fe_pointwise_dparam(Ud, Xq, Pe, rt, a.aux);")
         w("      #pragma unroll")
         w("      for (int k = 0; k < FE_NTC; ++k) r[k] = fe_df64(rt[k]);")
-        w("    } else fe_pointwise(U, Xq, Pe, r, D, flag, nullptr, nullptr);")
+        if gsep:
+            w("    } else {")
+            w("      int qI[FE_DIM];")
+            w("      { int qq = q;")
+            w("        #pragma unroll")
+            w("        for (int d = FE_DIM - 1; d >= 0; --d) { qI[d] = qq % 3; qq /= 3; } }")
+            w(f"      fe_pointwise(U, Xq, Pe, r, D, flag, sGe + el * {gsd}, qI);")
+            w("    }")
+        else:
+            w("    } else fe_pointwise(U, Xq, Pe, r, D, flag, nullptr, nullptr);")
         w("    fe_df64* rh = sRhr + (el * FE_NQ + q) * FE_NTC;")
         w("    const fe_df64 wqr = fe_df64(wq);")
         w("    #pragma unroll")
@@ -1203,7 +1294,43 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("      for (int k = threadIdx.x; k < nel * FE_NQ * FE_NDNZH; k += FE_NT) dh[k] = sD[k];")
         w("    }")
         w("  }")
-    if sfi:
+    if sfi and rdf:
+        SA, SB, SC = sfs
+        # ---------------- phase R (double-float): sum-factorised residual ----------------
+        w("  { fe_df64* Ia = reinterpret_cast<fe_df64*>(sIa); fe_df64* Ib = reinterpret_cast<fe_df64*>(sIb);")
+        w("  for (int p = threadIdx.x; p < nel * 27; p += FE_NT) {  // knot axis 2 -> node i2: T0, T1, T2 [q0][q1][i2]")
+        w("    const int el = p / 27, o = p - el * 27, q0 = o / 9, q1 = (o / 3) % 3, i2 = o % 3;")
+        w("    const fe_df64* rh = sRhr + (el * FE_NQ + q0 * 9 + q1 * 3) * FE_NTC;")
+        w("    fe_df64 t0 = fe_df64(0.0f, 0.0f), t1 = t0, t2 = t0;")
+        w("    #pragma unroll")
+        w("    for (int q2 = 0; q2 < 3; ++q2) {")
+        w("      const fe_df64* r = rh + q2 * FE_NTC;")
+        w("      const fe_df64 m0 = sMr[q2 * 3 + i2], m1 = sMr[9 + q2 * 3 + i2];")
+        w("      fe_mac(t0, r[3], m1); fe_mac(t0, r[0], m0); fe_mac(t1, r[1], m0); fe_mac(t2, r[2], m0); }")
+        w(f"    Ib[el * {SB} + o] = fe_norm(t0); Ib[el * {SB} + 27 + o] = fe_norm(t1); Ib[el * {SB} + 54 + o] = fe_norm(t2);")
+        w("  }")
+        w("  __syncthreads();")
+        w("  for (int p = threadIdx.x; p < nel * 27; p += FE_NT) {  // knot axis 1 -> node i1: S0, S1 [q0][i1][i2]")
+        w("    const int el = p / 27, o = p - el * 27, q0 = o / 9, i1 = (o / 3) % 3, i2 = o % 3;")
+        w(f"    const fe_df64* T = Ib + el * {SB} + q0 * 9 + i2;")
+        w("    fe_df64 s0 = fe_df64(0.0f, 0.0f), s1 = s0;")
+        w("    #pragma unroll")
+        w("    for (int q1 = 0; q1 < 3; ++q1) {")
+        w("      const fe_df64 m0 = sMr[q1 * 3 + i1], m1 = sMr[9 + q1 * 3 + i1];")
+        w("      fe_mac(s0, T[54 + q1 * 3], m1); fe_mac(s0, T[q1 * 3], m0); fe_mac(s1, T[27 + q1 * 3], m0); }")
+        w(f"    Ia[el * {SA} + o] = fe_norm(s0); Ia[el * {SA} + 27 + o] = fe_norm(s1);")
+        w("  }")
+        w("  __syncthreads();")
+        w("  for (int p = threadIdx.x; p < nel * 27; p += FE_NT) {  // knot axis 0 -> node i0: R at node l")
+        w("    const int el = p / 27, l = p - el * 27, i0 = l % 3, i1 = (l / 3) % 3, i2 = l / 9;")
+        w(f"    const fe_df64* S = Ia + el * {SA} + i1 * 3 + i2;")
+        w("    fe_df64 r = fe_df64(0.0f, 0.0f);")
+        w("    #pragma unroll")
+        w("    for (int q0 = 0; q0 < 3; ++q0) { fe_mac(r, S[27 + q0 * 9], sMr[9 + q0 * 3 + i0]); fe_mac(r, S[q0 * 9], sMr[q0 * 3 + i0]); }")
+        w("    a.rbuf[(e0 + el) * FE_NLOC + l] = fe_widen(fe_norm(r));")
+        w("  }")
+        w("  __syncthreads(); }")
+    elif sfi:
         SA, SB, SC = sfs
         # ---------------- phase R: sum-factorised residual ----------------
         # R_l = sum_q [rh0 psi_l + rh1 d0psi_l + rh2 d1psi_l + rh3 d2psi_l], one axis at a time
@@ -1313,7 +1440,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("    (void)t1;")
     w("    const double* tpsi = t1 ? sPsi1 : sPsi2;")
     w("    const double* tdps = t1 ? sDps1 : sDps2;")
-    if rdf:
+    if rdf and not sfi:
         w("    const fe_df64* tpsir = t1 ? sPsi1r : sPsi2r;")
         w("    const fe_df64* tdpsr = t1 ? sDps1r : sDps2r;")
         w("    (void)tpsi; (void)tdps;")
@@ -1327,7 +1454,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("    (void)Racc; (void)tpsi; (void)tdps;")
     # (sum-factorised Jacobian and residual: nothing is left per knot here)
     w(f"    for (int q = 0; q < {'0' if (sfi and sumfac) else 'FE_NQ'}; ++q) {{")
-    if rdf:
+    if rdf and not sfi:
         w("      const fe_df64* rh = sRhr + (el * FE_NQ + q) * FE_NTC + tf * (1 + FE_DIM);")
         w("      fe_mac(Racc, rh[0], tpsir[q * tn + lt]);")
         w("      #pragma unroll")
@@ -1444,7 +1571,7 @@ def generate_kernel(et: ElementType, pw: Pointwise, jac_precision: str = "f64",
         w("      }")
     w("    }")
     w("    const long long row = (e0 + el) * FE_NLOC + i;")
-    if rdf:
+    if rdf and not sfi:
         w("    a.rbuf[row] = fe_widen(Racc);")
     elif not sfi:
         w("    a.rbuf[row] = Racc;")

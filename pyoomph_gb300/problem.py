@@ -254,7 +254,8 @@ class Problem:
         self.jacobian_precision = "fp64"
         # "fp64"; "df64": the residual path (interpolation, pointwise
         # residual, test-function contraction) in double-float on the FP32
-        # pipes, for FP32 and df64 Jacobians of steady rational forms
+        # pipes, for FP32 and df64 Jacobians of steady forms whose pointwise
+        # terms are rational (Gaussian sources evaluated in FP64)
         self.residual_precision = "fp64"
         self.elems_per_block: Optional[int] = None
         # threads per block of the element kernel (None: one per local row

@@ -50,7 +50,9 @@ def _problems(workload, side):
         OP = O.poisson_problem(O.mesh(O.Q2_QUAD, side, side), W.draw_gaussians(0, 8, 2))
 
         def make(prec):
-            P = W.poisson_problem(N=side, seed=0, jacobian_precision=prec)
+            jp, _, rp = prec.partition(":")
+            P = W.poisson_problem(N=side, seed=0, jacobian_precision=jp)
+            P.residual_precision = rp or "fp64"
             P.initialise()
             P.set_dofs(np.random.default_rng(1).normal(0.0, 0.3, P.n_dof))
             return P
@@ -59,7 +61,9 @@ def _problems(workload, side):
                                eq=O.EQ_NONLINEAR_DIFFUSION)
 
         def make(prec):
-            P = W.nonlinear_diffusion_problem(N=side, seed=0, jacobian_precision=prec)
+            jp, _, rp = prec.partition(":")
+            P = W.nonlinear_diffusion_problem(N=side, seed=0, jacobian_precision=jp)
+            P.residual_precision = rp or "fp64"
             P.initialise()
             P.set_dofs(np.random.default_rng(0).normal(0.0, 0.1, P.n_dof))
             return P
@@ -67,9 +71,9 @@ def _problems(workload, side):
 
 
 CASES = [("ns", 256, ("fp64", "df64", "fp32", "fp32:df64", "df64:df64")),
-         ("poisson", 64, ("fp64", "df64", "fp32")),
-         ("hex", 24, ("fp64", "df64", "fp32")),
-         ("hex", 48, ("fp64", "fp32"))]
+         ("poisson", 64, ("fp64", "df64", "fp32", "fp32:df64")),
+         ("hex", 24, ("fp64", "df64", "fp32", "df64:df64")),
+         ("hex", 48, ("fp64", "fp32", "fp32:df64"))]
 
 
 @pytest.mark.parametrize("workload,side,precs", CASES, ids=[f"{w}{s}" for w, s, _ in CASES])

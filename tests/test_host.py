@@ -78,7 +78,8 @@ def test_krylov_solver_arguments_are_checked_before_any_device_call():
 
 
 @pytest.mark.parametrize("kind", ["poisson", "poisson_p2", "ns", "ns32", "nsdf", "hex", "hex32", "hexdf",
-                                  "ns_t", "ns32_t", "hexdf_t", "ns32_rdf", "nsdf_rdf"])
+                                  "ns_t", "ns32_t", "hexdf_t", "ns32_rdf", "nsdf_rdf", "hex32_rdf", "hexdf_rdf",
+                                  "poisson32_rdf"])
 def test_generated_kernels_compile_for_sm103a(kind, tmp_path):
     from pyoomph_gb300 import _native as N
     from pyoomph_gb300 import workloads as W
@@ -92,7 +93,10 @@ def test_generated_kernels_compile_for_sm103a(kind, tmp_path):
          "ns32_t": lambda: W.navier_stokes_problem(N=4, jacobian_precision="fp32", transient=True),
          "hexdf_t": lambda: W.nonlinear_diffusion_problem(N=2, jacobian_precision="df64", transient=True),
          "ns32_rdf": lambda: W.navier_stokes_problem(N=4, jacobian_precision="fp32"),
-         "nsdf_rdf": lambda: W.navier_stokes_problem(N=4, jacobian_precision="df64")}[kind]()
+         "nsdf_rdf": lambda: W.navier_stokes_problem(N=4, jacobian_precision="df64"),
+         "hex32_rdf": lambda: W.nonlinear_diffusion_problem(N=2, jacobian_precision="fp32"),
+         "hexdf_rdf": lambda: W.nonlinear_diffusion_problem(N=2, jacobian_precision="df64"),
+         "poisson32_rdf": lambda: W.poisson_problem(N=4, jacobian_precision="fp32")}[kind]()
     if kind.endswith("_rdf"):
         P.residual_precision = "df64"
     ks = P.lower()
@@ -250,37 +254,45 @@ def test_df64_jacobian_emulated_on_cpu_matches_oracle_elements(kind, geometry):
     assert err <= 1e-12
 
 
+@pytest.mark.parametrize("kind", ["ns_th", "poisson_q2", "poisson_p2", "nldiff_hex", "nldiff_q2"])
 @pytest.mark.parametrize("jac", ["fp32", "df64"])
 @pytest.mark.parametrize("geometry", ["affine", "general"])
-def test_df64_residual_emulated_on_cpu_matches_oracle_elements(geometry, jac):
+def test_df64_residual_emulated_on_cpu_matches_oracle_elements(geometry, jac, kind):
     """The double-float residual path (values staged as differences from
-    node 0 in FP64, interpolation, pointwise residual, pull-back and
-    test-function contraction in pairs of FP32) reproduces the oracle's
+    node 0 in FP64, interpolation -- sum-factorised for the Q2 hex --,
+    pointwise residual with the Gaussian source evaluated in FP64, pull-back
+    and test-function contraction in pairs of FP32) reproduces the oracle's
     element residuals within the FP64 contract."""
     import element_cases as C
     import kernel_emulator as KE
-    P, ks, values, Rr, Jr = C.build("ns_th", geometry, jac, residual="df64")
+    P, ks, values, Rr, Jr = C.build(kind, geometry, jac, residual="df64")
     assert "_rdf" in ks.name and "fe_df64 U[FE_NTC]" in ks.source
     rb, jb, st = KE.run(ks, P.mesh.x, P.mesh.conn, values, P.params)
     assert st[0] == 0
     err = C.relmax(rb, Rr)
-    print(geometry, jac, "df64 residual rel err", err)
+    print(kind, geometry, jac, "df64 residual rel err", err)
     assert err <= 1e-13
     assert C.relmax(jb, Jr) <= (1e-12 if jac == "df64" else 1e-5)
 
 
 def test_df64_residual_is_refused_where_it_does_not_apply():
-    """Forms with libm terms (the Gaussian source's exp), FP64 Jacobians and
-    transient forms keep the FP64 residual: asking for double-float is an
-    error, not a silent fallback."""
+    """FP64 Jacobians, transient forms and pointwise terms with libm calls
+    other than the Gaussian source keep the FP64 residual: asking for
+    double-float is an error, not a silent fallback."""
+    import types
+    import sympy as sp
     from pyoomph_gb300 import workloads as W
-    for make in (lambda: W.poisson_problem(N=4, jacobian_precision="fp32"),
-                 lambda: W.navier_stokes_problem(N=4),
+    from pyoomph_gb300.codegen import df64_residual_supported
+    for make in (lambda: W.navier_stokes_problem(N=4),
                  lambda: W.navier_stokes_problem(N=4, jacobian_precision="fp32", transient=True)):
         P = make()
         P.residual_precision = "df64"
         with pytest.raises(ValueError):
             P.lower()
+    x = sp.Symbol("x")
+    assert not df64_residual_supported(types.SimpleNamespace(r_exprs=[sp.exp(x)], d_entries=[]))
+    assert not df64_residual_supported(types.SimpleNamespace(r_exprs=[sp.sqrt(x)], d_entries=[]))
+    assert df64_residual_supported(types.SimpleNamespace(r_exprs=[x ** 2 / (1 + x)], d_entries=[(0, 0, 2 * x)]))
 
 
 def test_launch_shapes_balance_the_waves():
