@@ -44,26 +44,32 @@ template <class F> void parallel_ranges(int64_t n, unsigned nt, F &&f) {
   for (auto &x : th) x.join();
 }
 
-// dense accumulator over the columns of one output row
+// dense accumulator over the columns of one output row: value and row
+// stamp side by side, so that a term touches one cache line
 struct Row {
-  std::vector<double> acc;
-  std::vector<int64_t> mark;
+  struct Slot {
+    double acc;
+    int32_t mark;
+  };
+  std::vector<Slot> s;
   std::vector<int32_t> cols;
-  int64_t stamp = 0;
-  explicit Row(int64_t ncols) : acc((size_t)std::max<int64_t>(ncols, 1), 0.0), mark(acc.size(), -1) {}
+  int32_t stamp = 0;
+  explicit Row(int64_t ncols) : s((size_t)std::max<int64_t>(ncols, 1), Slot{0.0, -1}) {}
   void start() {
     stamp++;
     cols.clear();
   }
   void add(int32_t c, double v) {
-    if (mark[c] != stamp) {
-      mark[c] = stamp;
-      acc[c] = v;
+    Slot &x = s[c];
+    if (x.mark != stamp) {
+      x.mark = stamp;
+      x.acc = v;
       cols.push_back(c);
     } else {
-      acc[c] += v;
+      x.acc += v;
     }
   }
+  double get(int32_t c) const { return s[c].acc; }
 };
 
 // CSR of nrows rows over ncols columns, row i filled by fill(i, row)
@@ -86,7 +92,7 @@ void build_rows(int64_t nrows, int64_t ncols, Fill &&fill, std::vector<int32_t> 
       std::sort(row.cols.begin(), row.cols.end());
       for (int32_t c : row.cols) {
         c_loc.push_back(c);
-        v_loc.push_back(row.acc[c]);
+        v_loc.push_back(row.get(c));
       }
       len[i] = (int64_t)row.cols.size();
     }
@@ -163,18 +169,36 @@ int fe_sa_level_build(int64_t n, const int32_t *rowptr, const int32_t *colidx, c
     x[i] = 0.5 + (f - std::floor(f));
   }
   double lam = 1.0;
+  // y = D^-1 A x over fixed chunks of rows, each chunk also summing x_i^2
+  // and y_i^2 in row order (the sums of norm2, fused into the same pass)
+  const int64_t chunk = 4096, nch = (n + chunk - 1) / chunk;
+  std::vector<double> px((size_t)nch), py((size_t)nch);
   for (int it = 0; it < 12; it++) {
-    fe_sa::parallel_ranges(n, nt, [&](int64_t lo, int64_t hi, unsigned) {
-      for (int64_t i = lo; i < hi; i++) {
-        double s = 0.0;
-        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++) s += vals[k] * x[colidx[k]];
-        y[i] = s / d[i];
+    fe_sa::parallel_ranges(nch, nt, [&](int64_t clo, int64_t chi, unsigned) {
+      for (int64_t c = clo; c < chi; c++) {
+        double sx = 0.0, sy = 0.0;
+        for (int64_t i = c * chunk; i < std::min(n, (c + 1) * chunk); i++) {
+          double s = 0.0;
+          for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++) s += vals[k] * x[colidx[k]];
+          y[i] = s / d[i];
+          sx += x[i] * x[i];
+          sy += y[i] * y[i];
+        }
+        px[c] = sx;
+        py[c] = sy;
       }
     });
-    const double nx = fe_sa::norm2(x, nt), ny = fe_sa::norm2(y, nt);
+    double sx = 0.0, sy = 0.0;
+    for (int64_t c = 0; c < nch; c++) {
+      sx += px[c];
+      sy += py[c];
+    }
+    const double nx = std::sqrt(sx), ny = std::sqrt(sy);
     lam = ny / std::max(nx, 1e-300);
     const double sc = 1.0 / std::max(ny, 1e-300);
-    for (int64_t i = 0; i < n; i++) x[i] = y[i] * sc;
+    fe_sa::parallel_ranges(n, nt, [&](int64_t lo, int64_t hi, unsigned) {
+      for (int64_t i = lo; i < hi; i++) x[i] = y[i] * sc;
+    });
   }
   lam *= 1.1;
   if (!std::isfinite(lam) || lam <= 0.0) return fail(FE_ERR_ARG, "fe_sa_level_build: no spectral radius estimate");
@@ -201,19 +225,35 @@ int fe_sa_level_build(int64_t n, const int32_t *rowptr, const int32_t *colidx, c
                       }
                     },
                     aprp, apci, apv);
-  // P^T: rows of P in ascending order within each column
+  // P^T: rows of P in ascending order within each column.  Each thread
+  // counts its rows' entries per column, then writes them from its own
+  // offset in each column (threads own ascending row ranges)
   std::vector<int32_t> trp((size_t)n_agg + 1, 0), tci(L->pci.size());
   std::vector<double> tv(L->pci.size());
-  for (int32_t c : L->pci) trp[c + 1]++;
-  for (int64_t c = 0; c < n_agg; c++) trp[c + 1] += trp[c];
   {
-    std::vector<int32_t> pos(trp.begin(), trp.end() - 1);
-    for (int64_t i = 0; i < n; i++)
-      for (int32_t q = L->prp[i]; q < L->prp[i + 1]; q++) {
-        const int32_t at = pos[L->pci[q]]++;
-        tci[at] = (int32_t)i;
-        tv[at] = L->pv[q];
+    std::vector<std::vector<int32_t>> pos(nt, std::vector<int32_t>((size_t)n_agg, 0));
+    fe_sa::parallel_ranges(n, nt, [&](int64_t lo, int64_t hi, unsigned t) {
+      std::vector<int32_t> &cnt = pos[t];
+      for (int32_t q = L->prp[lo]; q < L->prp[hi]; q++) cnt[L->pci[q]]++;
+    });
+    for (int64_t c = 0; c < n_agg; c++) {
+      int32_t at = trp[c];
+      for (unsigned t = 0; t < nt; t++) {
+        const int32_t k = pos[t][c];
+        pos[t][c] = at;
+        at += k;
       }
+      trp[c + 1] = at;
+    }
+    fe_sa::parallel_ranges(n, nt, [&](int64_t lo, int64_t hi, unsigned t) {
+      std::vector<int32_t> &at = pos[t];
+      for (int64_t i = lo; i < hi; i++)
+        for (int32_t q = L->prp[i]; q < L->prp[i + 1]; q++) {
+          const int32_t w = at[L->pci[q]]++;
+          tci[w] = (int32_t)i;
+          tv[w] = L->pv[q];
+        }
+    });
   }
   // Ac = P^T (A P)
   fe_sa::build_rows(n_agg, n_agg,
