@@ -2447,53 +2447,6 @@ int fe_tc_contract(const float *dhat, float *jbuf, int64_t n_elem, int n, int nq
   return FE_OK;
 }
 
-int fe_sa_aggregate(int64_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
-                    const int32_t *comp, double theta, int32_t *agg, int64_t *n_agg) {
-  if (n < 0 || (n > 0 && (!rowptr || !colidx || !vals || !comp || !agg)) || !n_agg)
-    return fail(FE_ERR_ARG, "fe_sa_aggregate: null argument");
-  std::vector<double> diag((size_t)n, 0.0);
-  for (int64_t i = 0; i < n; i++)
-    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++) {
-      if (colidx[k] < 0 || colidx[k] >= n) return fail(FE_ERR_ARG, "fe_sa_aggregate: column out of range");
-      if (colidx[k] == i) diag[i] = std::fabs(vals[k]);
-    }
-  auto strong = [&](int64_t i, int32_t k) {
-    const int32_t j = colidx[k];
-    return j != i && comp[j] == comp[i] && std::fabs(vals[k]) >= theta * std::sqrt(diag[i] * diag[j]);
-  };
-  for (int64_t i = 0; i < n; i++) agg[i] = -1;
-  int32_t na = 0;
-  for (int64_t i = 0; i < n; i++) {   // roots with a free strong neighbourhood
-    if (agg[i] >= 0) continue;
-    bool free_ = true;
-    for (int32_t k = rowptr[i]; k < rowptr[i + 1] && free_; k++)
-      if (strong(i, k) && agg[colidx[k]] >= 0) free_ = false;
-    if (!free_) continue;
-    agg[i] = na;
-    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++)
-      if (strong(i, k)) agg[colidx[k]] = na;
-    na++;
-  }
-  std::vector<int32_t> first(agg, agg + n);
-  for (int64_t i = 0; i < n; i++) {   // join a neighbouring aggregate (of the first pass)
-    if (agg[i] >= 0) continue;
-    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++)
-      if (strong(i, k) && first[colidx[k]] >= 0) {
-        agg[i] = first[colidx[k]];
-        break;
-      }
-  }
-  for (int64_t i = 0; i < n; i++) {   // leftovers: new aggregates with their free strong neighbours
-    if (agg[i] >= 0) continue;
-    agg[i] = na;
-    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++)
-      if (strong(i, k) && agg[colidx[k]] < 0) agg[colidx[k]] = na;
-    na++;
-  }
-  *n_agg = na;
-  return FE_OK;
-}
-
 int fe_problem_set_zero_threshold(fe_problem_t *p, double threshold) {
   if (!p) return fail(FE_ERR_ARG, "null problem");
   if (!(threshold >= 0.0)) return fail(FE_ERR_ARG, "zero threshold must be >= 0");

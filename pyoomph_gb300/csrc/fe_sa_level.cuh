@@ -135,6 +135,70 @@ inline double norm2(const std::vector<double> &x, unsigned nt) {
 
 extern "C" {
 
+// Aggregates for the smoothed-aggregation hierarchy: greedy over the rows in
+// order (roots with a free strong neighbourhood, then joins to a first-pass
+// neighbour, then the leftovers), with the strength of connection
+// |a_ij| >= theta sqrt(|a_ii| |a_jj|) between unknowns of the same
+// component.  The strength flags are computed once per entry, in parallel;
+// the greedy passes stay serial, so the aggregates do not depend on the
+// number of threads.
+int fe_sa_aggregate(int64_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals,
+                    const int32_t *comp, double theta, int32_t *agg, int64_t *n_agg) {
+  if (n < 0 || (n > 0 && (!rowptr || !colidx || !vals || !comp || !agg)) || !n_agg)
+    return fail(FE_ERR_ARG, "fe_sa_aggregate: null argument");
+  const unsigned nt = fe_sa::threads_for(n);
+  std::vector<double> diag((size_t)n, 0.0);
+  std::vector<int> bad(nt, 0);
+  fe_sa::parallel_ranges(n, nt, [&](int64_t lo, int64_t hi, unsigned t) {
+    for (int64_t i = lo; i < hi; i++)
+      for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++) {
+        if (colidx[k] < 0 || colidx[k] >= n) bad[t] = 1;
+        else if (colidx[k] == i) diag[i] = std::fabs(vals[k]);
+      }
+  });
+  for (int b : bad)
+    if (b) return fail(FE_ERR_ARG, "fe_sa_aggregate: column out of range");
+  std::vector<uint8_t> strong(n > 0 ? (size_t)rowptr[n] : 0);
+  fe_sa::parallel_ranges(n, nt, [&](int64_t lo, int64_t hi, unsigned) {
+    for (int64_t i = lo; i < hi; i++)
+      for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++) {
+        const int32_t j = colidx[k];
+        strong[k] = j != i && comp[j] == comp[i] && std::fabs(vals[k]) >= theta * std::sqrt(diag[i] * diag[j]);
+      }
+  });
+  for (int64_t i = 0; i < n; i++) agg[i] = -1;
+  int32_t na = 0;
+  for (int64_t i = 0; i < n; i++) {   // roots with a free strong neighbourhood
+    if (agg[i] >= 0) continue;
+    bool free_ = true;
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1] && free_; k++)
+      if (strong[k] && agg[colidx[k]] >= 0) free_ = false;
+    if (!free_) continue;
+    agg[i] = na;
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++)
+      if (strong[k]) agg[colidx[k]] = na;
+    na++;
+  }
+  std::vector<int32_t> first(agg, agg + n);
+  for (int64_t i = 0; i < n; i++) {   // join a neighbouring aggregate (of the first pass)
+    if (agg[i] >= 0) continue;
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++)
+      if (strong[k] && first[colidx[k]] >= 0) {
+        agg[i] = first[colidx[k]];
+        break;
+      }
+  }
+  for (int64_t i = 0; i < n; i++) {   // leftovers: new aggregates with their free strong neighbours
+    if (agg[i] >= 0) continue;
+    agg[i] = na;
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; k++)
+      if (strong[k] && agg[colidx[k]] < 0) agg[colidx[k]] = na;
+    na++;
+  }
+  *n_agg = na;
+  return FE_OK;
+}
+
 int fe_sa_level_build(int64_t n, const int32_t *rowptr, const int32_t *colidx, const double *vals, const int32_t *agg,
                       int64_t n_agg, fe_sa_level_t **out) {
   if (!out) return fail(FE_ERR_ARG, "fe_sa_level_build: null output");
